@@ -1,0 +1,150 @@
+/*
+ * pimd_gb300.h -- C ABI of the GB300 force engine and ring-polymer propagator.
+ *
+ * Drop-in boundary for PIMD-F90's hot path. Every entry point takes plain pointers and
+ * sizes, returns an int status (PIMD_OK on success) and never aborts the process; the
+ * reference's Fortran `stop`s (math.f90:199,229,244,282) become error codes.
+ *
+ * Array layouts are the reference's Fortran column-major layouts, passed as double*:
+ *   RR(3,Natoms), RRt(3,Natoms,Nbeads), dRR(3,Natoms), virt(3,3), dip_momI(3,Nwaters),
+ * with atoms ordered O H H O H H ... Units: Angstrom, kcal/mol, amu, ps. dRR is the
+ * gradient dE/dx (not the force), as in the reference.
+ *
+ * A context replaces the reference's module state (system_mod.f90:22-44, pot_mod.f90:47-83):
+ * it owns all device memory, the Ewald tables and one induced-dipole predictor history per
+ * bead. Calls on one context must not overlap; different contexts are independent.
+ */
+#ifndef PIMD_GB300_H
+#define PIMD_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    PIMD_OK = 0,
+    PIMD_ERR_ARG = 1,               /* invalid argument / unsupported combination         */
+    PIMD_ERR_CUDA = 2,              /* CUDA runtime error (see pimd_last_error)           */
+    PIMD_ERR_NEIGHBOR_OVERFLOW = 3, /* more O-O pairs than the neighbour-list capacity     */
+    PIMD_ERR_GAMMQ = 4,             /* Thole Q(2/3,x) iteration did not converge          */
+    PIMD_ERR_NOMEM = 5,             /* device allocation failed                            */
+    PIMD_ERR_STATE = 6              /* call order violated (e.g. no normal modes set up)   */
+};
+
+enum { PIMD_FP64 = 0, PIMD_MIXED = 1 };
+
+/* Potential parameters: the input-file keys of input_file_reader.f90 that reach the
+ * force call, plus two explicit Ewald settings. With alpha > 0 the Ewald splitting
+ * parameter and the integer k shell |n|^2 <= nmax^2 are used as given; with alpha <= 0 the
+ * reference rule of ewald.f90:312-319 is applied to eps_ewald. */
+typedef struct {
+    int pot_model;      /* 2 TTM2.1-F, 3 TTM3-F, 4 q-SPC/Fw, 5 SPC/F                       */
+    int natoms;         /* 3 * Nwaters                                                     */
+    int nbeads;         /* beads evaluated per batched call (>= 1)                         */
+    double box[3];      /* orthorhombic box (A)                                            */
+    double rc;          /* real-space cutoff (A), <= min(box)/2                            */
+    double rc1;         /* start of the TTM3-F vdW force switch (A)                        */
+    double eps_ewald;   /* ewald.f90 accuracy parameter (used when alpha <= 0)             */
+    double alpha;       /* explicit Ewald alpha (1/A), or <= 0                             */
+    int nmax;           /* explicit k shell, used when alpha > 0                           */
+    int polar_maxiter;  /* induced-dipole iteration cap                                    */
+    double polar_sor;   /* SOR mixing factor                                               */
+    double polar_eps;   /* convergence threshold on DEBYE/CHARGECON/sqrt(Natoms)*|dmu|     */
+    int guess_initdip;  /* 4-step dipole predictor from the previous MD steps              */
+    int contraction;    /* skip the monomer PES (ring-polymer contraction runs)            */
+    int precision;      /* PIMD_FP64 or PIMD_MIXED                                         */
+    int device;         /* CUDA device ordinal                                             */
+} pimd_params;
+
+typedef struct pimd_ctx pimd_ctx;
+
+/* init_pot (pot_ttm/potential.f90:129-285) + ewald_set(.true.) (pot_ttm/ewald.f90:293). */
+int pimd_create(pimd_ctx **ctx, const pimd_params *p);
+int pimd_destroy(pimd_ctx *ctx);
+/* Run all work of the context on this cudaStream_t (NULL = the context's own stream). */
+int pimd_set_stream(pimd_ctx *ctx, void *cuda_stream);
+/* Text of the last error on this context. */
+const char *pimd_last_error(pimd_ctx *ctx);
+/* Ewald set-up results: alpha, number of half-space k-vectors, (hmax, kmax, lmax). */
+int pimd_ewald_info(pimd_ctx *ctx, double *alpha, int *nk, int *hkl_max);
+
+/* pot_ttm (pot_ttm/pot_ttm.f90:3): one bead, host arrays, same argument order. Uses the
+ * predictor-history slot of bead 0. Blocks until the results are in host memory. */
+int pimd_pot_ttm(pimd_ctx *ctx, const double *RR, const double *RRc, double *En, double *dRR,
+                 double *virt, double *virialc, double *dip_momI, double *Edip_mom, double *chg,
+                 int t);
+
+/* pot_spc (pot_ttm/pot_spc.f90:1): one bead, host arrays. */
+int pimd_pot_spc(pimd_ctx *ctx, const double *RR, double *En, double *dRR, double *virt,
+                 double *dip_momI, double *chg);
+
+/* The body of full_bead_forces (force_calc.f90:26-106) for all nbeads beads in one call,
+ * host arrays: RRt(3,Natoms,P), RRc(3,Natoms) in; Upott(P), dRRt(3,Natoms,P), virialt(P),
+ * virialct(P), dip_momIt(3,Nw,P), dip_momEt(3,Nw,P) and chg(Natoms) (bead P) out. Any
+ * output pointer may be NULL. virialt(k) = trace of bead k's virial tensor. */
+int pimd_full_bead_forces(pimd_ctx *ctx, const double *RRt, const double *RRc, double *Upott,
+                          double *dRRt, double *virialt, double *virialct, double *dip_momIt,
+                          double *dip_momEt, double *chg, int t);
+
+/* Same with device pointers, stream-ordered on the context's stream (no host copies). */
+int pimd_full_bead_forces_device(pimd_ctx *ctx, const double *RRt, const double *RRc,
+                                 double *Upott, double *dRRt, double *virialt, double *virialct,
+                                 double *dip_momIt, double *dip_momEt, double *chg, int t);
+
+/* Energy components of bead `bead` after the last force call (the reference's globals
+ * Umon, Uvdw, Uelec, Uind of system_mod.f90:30), the per-bead 3x3 virial tensor and the
+ * induced-dipole iteration count / final stath*|dmu|. */
+int pimd_get_energies(pimd_ctx *ctx, int bead, double U[4]);
+int pimd_get_virial(pimd_ctx *ctx, int bead, double virt[9]);
+int pimd_get_dipole_info(pimd_ctx *ctx, int bead, int *niter, double *deltadip);
+
+/* The half neighbour list of bead `bead` from the last force call: O-O pairs (i, j), 0-based,
+ * i < j, in find_neigh's order (find_neigh.f90:232-274). Writes min(npairs, cap) pairs to
+ * ij[2*cap] and the total to *npairs. */
+int pimd_get_neighbors(pimd_ctx *ctx, int bead, int *ij, int cap, int *npairs);
+
+/* Induced-dipole iteration control for batched calls: check convergence on the host every
+ * `every` iterations (0 = run exactly polar_maxiter iterations with converged beads
+ * skipped on the device, which needs no host synchronisation). Default 1. */
+int pimd_set_dipole_check(pimd_ctx *ctx, int every);
+
+/* ---------------------------------------------------------------------------------------
+ * Ring-polymer normal modes (NormalModes.f90) and PILE thermostat (Langevin.f90).
+ */
+/* InitNormalModes (NormalModes.f90:68-218) for P beads; optional outputs (NULL to skip):
+ * A11..A22, omegalist, MassScaleFactor (length P) and C(P,P) column-major. */
+int pimd_nm_init(pimd_ctx *ctx, int nbeads, double omegan, double delta, double setNMfreq,
+                 double *A11, double *A12, double *A21, double *A22, double *omegalist,
+                 double *msf, double *C);
+/* EvolveRing (NormalModes.f90:34-63) for one atom, host arrays RR(3,P), PP(3,P) inout. */
+int pimd_evolve_ring(pimd_ctx *ctx, double *RR, double *PP, int nbeads, double mass);
+/* EvolveRing for every atom of RRt(3,Natoms,P)/PPt (MD.f90:53-58); device pointers. */
+int pimd_evolve_all_device(pimd_ctx *ctx, double *RRt, double *PPt, double massO, double massH);
+/* Init_Langevin_NM (Langevin.f90:68-98) after pimd_nm_init; temp_P = P * T. */
+int pimd_langevin_init(pimd_ctx *ctx, double delt2, int centroid_thermostat, double tau_centroid,
+                       double temp_P);
+/* Langevin_NM (Langevin.f90:30-64) on device PPt(3,Natoms,P). xi(3,P,Natoms) holds the
+ * standard normal draws (device pointer); NULL draws them on the device from (seed, counter)
+ * with a counter-based generator. */
+int pimd_langevin_nm_device(pimd_ctx *ctx, double *PPt, const double *xi, double massO,
+                            double massH, unsigned long long seed, unsigned long long counter);
+
+/* One velocity-Verlet PIMD step (MD.f90:35-110, PIMD_VV without Nose-Hoover/barostat) on
+ * device state RRt, PPt, dRRt (3,Natoms,P) and RRc (3,Natoms): Langevin, half kick,
+ * EvolveRing, centroid, PBCs (main_stuff.f90:107-125), full_bead_forces, half kick,
+ * Langevin. Writes the bead-summed Upot, virial, virialc/P and the kinetic energy uk
+ * (main_stuff.f90:349-388) to device out4[4]. xi1/xi2 as in pimd_langevin_nm_device. */
+typedef struct {
+    double delt;                 /* ps */
+    double massO, massH;         /* amu */
+    int langevin;                /* PILE bead thermostat on/off */
+    unsigned long long seed;     /* Langevin stream seed when xi == NULL */
+} pimd_md_params;
+int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt,
+                        double *dRRt, double *RRc, const double *xi1, const double *xi2, int t,
+                        double *out4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PIMD_GB300_H */

@@ -1,0 +1,533 @@
+// capi.cu -- context set-up (init_pot / ewald_set) and the force-call C ABI.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "../../include/pimd_gb300.h"
+#include "engine.h"
+
+namespace pimd {
+
+// pot_mod.f90:7-44 parameter sets
+struct ModelSet {
+    double vdwA, vdwB, vdwC, vdwD, vdwE, aDD, aCCaCD, polfacO, polfacH, polfacM, polarO, polarH, polarM,
+        gammaM, dms1, dms2, dms3;
+};
+static const ModelSet TTM21F = {-1.329565985e+6, 3.632560798e+5, -2.147141323e+3, 1.e13, 13.2, 0.3, 0.2,
+                                0.837, 0.496, 0.837, 0.837, 0.496, 0.837, 0.426706882, 0.0, 0.0, 0.0};
+static const ModelSet TTM3F = {0.0, 0.0, -0.72298855e+03, 0.10211829e+06, 0.37170376e+01, 0.175, 0.175,
+                               0.837, 0.496, 0.837, 0.0, 0.0, 1.444, 0.46, 0.5, 0.9578, 0.012};
+
+static int fail(Engine &E, int code, const char *msg) {
+    E.last_error = msg;
+    return code;
+}
+
+static int cuda_check(Engine &E, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return PIMD_OK;
+    char buf[512];
+    snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+    E.last_error = buf;
+    return e == cudaErrorMemoryAllocation ? PIMD_ERR_NOMEM : PIMD_ERR_CUDA;
+}
+
+template <typename T>
+static int dalloc(Engine &E, T **p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) return cuda_check(E, e, "cudaMalloc");
+    E.allocs.push_back((void *)*p);
+    return PIMD_OK;
+}
+
+// ewald.f90:293-378 (half-space k list in the reference's loop order) and the run/chunk
+// structure used by the kernels.
+static int setup_kspace(Engine &E, const pimd_params *p) {
+    KP &kp = E.kp;
+    const bool explicit_k = p->alpha > 0;
+    double kcutsq = 0;
+    if (!explicit_k) {
+        const double PP = -std::log(p->eps_ewald);
+        kp.ew.aewald = std::sqrt(PP) / p->rc;
+        const double kcut = 2.0 * kp.ew.aewald * std::sqrt(PP);
+        kcutsq = kcut * kcut;
+        kp.hmax = (int)std::floor(kcut / TWOPI * p->box[0]);
+        kp.kmax = (int)std::floor(kcut / TWOPI * p->box[1]);
+        kp.lmax = (int)std::floor(kcut / TWOPI * p->box[2]);
+    } else {
+        kp.ew.aewald = p->alpha;
+        kp.hmax = kp.kmax = kp.lmax = p->nmax;
+    }
+    if (kp.lmax > 127 || kp.kmax > 127 || kp.hmax > 127) return fail(E, PIMD_ERR_ARG, "k shell too large (max 127)");
+    const double a = kp.ew.aewald;
+    const double fac_ew2 = -0.25 / (a * a);
+    E.h_khkl.clear();
+    E.h_kvec.clear();
+    E.h_Ak.clear();
+    for (int kx = 0; kx <= kp.hmax; kx++) {
+        const double k0 = TWOPI * kp.boxi[0] * (double)kx;
+        for (int ky = (kx == 0 ? 0 : -kp.kmax); ky <= kp.kmax; ky++) {
+            const double k1 = TWOPI * kp.boxi[1] * (double)ky;
+            const double kvxy = k0 * k0 + k1 * k1;
+            for (int kz = (kx == 0 && ky == 0) ? 1 : -kp.lmax; kz <= kp.lmax; kz++) {
+                const double k2 = TWOPI * kp.boxi[2] * (double)kz;
+                const double kvsq = kvxy + k2 * k2;
+                const bool keep = explicit_k ? (kx * kx + ky * ky + kz * kz <= p->nmax * p->nmax && kvsq > 1.e-16)
+                                             : (kvsq < kcutsq && kvsq > 1.e-16);
+                if (!keep) continue;
+                E.h_khkl.insert(E.h_khkl.end(), {kx, ky, kz});
+                E.h_kvec.insert(E.h_kvec.end(), {k0, k1, k2});
+                E.h_Ak.push_back(2.0 * std::exp(fac_ew2 * kvsq) / kvsq);
+            }
+        }
+    }
+    kp.nk = (int)E.h_Ak.size();
+    if (kp.nk == 0) return fail(E, PIMD_ERR_ARG, "empty k-vector set");
+    // runs of equal (kx, ky) with consecutive kz
+    E.h_runs.clear();
+    std::vector<int2> kidx(kp.nk);
+    for (int k = 0; k < kp.nk; k++) {
+        const int kx = E.h_khkl[3 * k], ky = E.h_khkl[3 * k + 1], kz = E.h_khkl[3 * k + 2];
+        if (E.h_runs.empty() || E.h_runs.back().kx != kx || E.h_runs.back().ky != ky) {
+            KRun r{};
+            r.kx = kx;
+            r.ky = ky;
+            r.kzlo = kz;
+            r.nkz = 0;
+            r.kbeg = k;
+            E.h_runs.push_back(r);
+        }
+        KRun &r = E.h_runs.back();
+        if (kz != r.kzlo + r.nkz) return fail(E, PIMD_ERR_ARG, "non-contiguous kz run");
+        r.nkz++;
+        kidx[k] = make_int2((int)E.h_runs.size() - 1, kz);
+    }
+    kp.nrun = (int)E.h_runs.size();
+    // chunks of <= 256 k-vectors and <= 64 runs
+    E.h_chunks.clear();
+    E.max_runs_chunk = 0;
+    KChunk c{0, 0, 0, 0};
+    for (int r = 0; r < kp.nrun; r++) {
+        const KRun &run = E.h_runs[r];
+        if (c.r1 > c.r0 && (run.kbeg + run.nkz - c.k0 > 256 || c.r1 - c.r0 >= 64)) {
+            E.h_chunks.push_back(c);
+            E.max_runs_chunk = std::max(E.max_runs_chunk, c.r1 - c.r0);
+            c = KChunk{run.kbeg, run.kbeg, r, r};
+        }
+        c.k1 = run.kbeg + run.nkz;
+        c.r1 = r + 1;
+    }
+    E.h_chunks.push_back(c);
+    E.max_runs_chunk = std::max(E.max_runs_chunk, c.r1 - c.r0);
+    E.nchunk = (int)E.h_chunks.size();
+    kp.nchunk = E.nchunk;
+    kp.ntab = kp.hmax + 1 + kp.kmax + 1 + kp.lmax + 1;
+    // device copies
+    int rc;
+    KRun *d_runs;
+    KChunk *d_chunks;
+    double4_32a *d_kinfo;
+    double *d_Ak;
+    int2 *d_kidx;
+    if ((rc = dalloc(E, &d_runs, kp.nrun)) || (rc = dalloc(E, &d_chunks, E.nchunk)) || (rc = dalloc(E, &d_kinfo, kp.nk)) ||
+        (rc = dalloc(E, &d_Ak, kp.nk)) || (rc = dalloc(E, &d_kidx, kp.nk)))
+        return rc;
+    std::vector<double4_32a> kinfo(kp.nk);
+    for (int k = 0; k < kp.nk; k++)
+        kinfo[k] = make_double4_32a(E.h_kvec[3 * k], E.h_kvec[3 * k + 1], E.h_kvec[3 * k + 2], FOURPI * E.h_Ak[k] / kp.volume);
+    cudaMemcpy(d_runs, E.h_runs.data(), sizeof(KRun) * kp.nrun, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_chunks, E.h_chunks.data(), sizeof(KChunk) * E.nchunk, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_kinfo, kinfo.data(), sizeof(double4_32a) * kp.nk, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_Ak, E.h_Ak.data(), sizeof(double) * kp.nk, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_kidx, kidx.data(), sizeof(int2) * kp.nk, cudaMemcpyHostToDevice);
+    kp.runs = d_runs;
+    kp.chunks = d_chunks;
+    kp.kinfo = d_kinfo;
+    kp.kAk = d_Ak;
+    kp.kidx = d_kidx;
+    return cuda_check(E, cudaGetLastError(), "k-space upload");
+}
+
+static int create(Engine &E, const pimd_params *p) {
+    if (!p || p->natoms <= 0 || p->natoms % 3 || p->nbeads < 1) return fail(E, PIMD_ERR_ARG, "natoms/nbeads");
+    if (p->pot_model != 2 && p->pot_model != 3) return fail(E, PIMD_ERR_ARG, "pot_model must be 2 or 3");
+    if (!(p->box[0] > 0 && p->box[1] > 0 && p->box[2] > 0)) return fail(E, PIMD_ERR_ARG, "box");
+    const double lmin = std::min(p->box[0], std::min(p->box[1], p->box[2]));
+    // InputOutput.f90:277-281: the cutoff may not exceed half the box
+    if (!(p->rc > 0) || p->rc > 0.5 * lmin) return fail(E, PIMD_ERR_ARG, "rc must be in (0, min(box)/2]");
+    if (p->alpha <= 0 && !(p->eps_ewald > 0 && p->eps_ewald < 1)) return fail(E, PIMD_ERR_ARG, "eps_ewald");
+    if (p->alpha > 0 && p->nmax < 1) return fail(E, PIMD_ERR_ARG, "nmax");
+    if (p->polar_maxiter < 1) return fail(E, PIMD_ERR_ARG, "polar_maxiter must be >= 1");
+    if (p->precision != PIMD_FP64) return fail(E, PIMD_ERR_ARG, "only PIMD_FP64 is available");
+    int rc = cuda_check(E, cudaSetDevice(p->device), "cudaSetDevice");
+    if (rc) return rc;
+    E.device = p->device;
+    E.precision = p->precision;
+    rc = cuda_check(E, cudaStreamCreateWithFlags(&E.stream, cudaStreamNonBlocking), "stream");
+    if (rc) return rc;
+    E.own_stream = true;
+    KP &kp = E.kp;
+    std::memset(&kp, 0, sizeof(kp));
+    kp.model = p->pot_model;
+    kp.natoms = p->natoms;
+    kp.N = p->natoms / 3;
+    kp.S = 4 * kp.N;
+    kp.P = p->nbeads;
+    for (int c = 0; c < 3; c++) {
+        kp.box[c] = p->box[c];
+        kp.boxi[c] = 1.0 / p->box[c];
+    }
+    kp.volume = p->box[0] * p->box[1] * p->box[2];
+    kp.rc2 = p->rc * p->rc;
+    kp.rc1 = p->rc1;
+    kp.contraction = p->contraction;
+    kp.guess = p->guess_initdip;
+    kp.polar_maxiter = p->polar_maxiter;
+    kp.polar_sor = p->polar_sor;
+    kp.polar_eps = p->polar_eps;
+    const ModelSet &m = (p->pot_model == 2) ? TTM21F : TTM3F;
+    kp.vdwA = m.vdwA;
+    kp.vdwB = m.vdwB;
+    kp.vdwC = m.vdwC;
+    kp.vdwD = m.vdwD;
+    kp.vdwE = m.vdwE;
+    kp.gammaM = m.gammaM;
+    kp.dms1 = m.dms1;
+    kp.dms2 = m.dms2;
+    kp.dms3 = m.dms3;
+    kp.polar[1] = m.polarO;
+    kp.polar[2] = m.polarH;
+    kp.polar[3] = m.polarH;
+    kp.polar[4] = m.polarM;
+    kp.same_acd = std::fabs(m.aCCaCD - m.aDD) < 1.e-12 ? 1 : 0;
+    if (p->pot_model == 3 && p->rc != p->rc1) {
+        // potential.f90:197-198 GROMACS-style vdW force switch
+        const double Rc = p->rc, r1 = p->rc1;
+        const double rc8 = Rc * Rc * Rc * Rc * Rc * Rc * Rc * Rc;
+        kp.shiftA = -(10 * Rc - 7 * r1) / (rc8 * ((Rc - r1) * (Rc - r1)));
+        kp.shiftB = (9 * Rc - 7 * r1) / (rc8 * ((Rc - r1) * (Rc - r1) * (Rc - r1)));
+    }
+    if (p->pot_model == 2) {
+        kp.fd = 0;
+        kp.ld = 3 * kp.N;
+        kp.ndd = 9;
+    } else {
+        kp.fd = 3 * kp.N;
+        kp.ld = 4 * kp.N;
+        kp.ndd = 1;
+    }
+    {  // potential.f90:238-239 long-range vdW correction
+        const double Rc = p->rc, r3 = Rc * Rc * Rc, r7 = r3 * r3 * Rc, r9 = r7 * Rc * Rc;
+        kp.Uvdw_lrc = TWOPI * (double)(kp.N * kp.N) / kp.volume * (m.vdwA / (9.0 * r9) + m.vdwB / (7.0 * r7) + m.vdwC / (3.0 * r3));
+    }
+    // potential.f90:244-245 polfac = polfac^(-1/2) by way of the sixth root
+    double pf[5];
+    const double base[5] = {0, m.polfacO, m.polfacH, m.polfacH, m.polfacM};
+    for (int i = 1; i <= 4; i++) {
+        const double r = std::pow(base[i], 1.0 / 6.0);
+        pf[i] = 1.0 / (r * r * r);
+    }
+    for (int i = 1; i <= 4; i++)
+        for (int j = 1; j <= 4; j++) {
+            kp.pt.apol_qq[i][j] = (m.aCCaCD * pf[i]) * pf[j];
+            kp.pt.ra_qq[i][j] = std::pow(kp.pt.apol_qq[i][j], 1.0 / 3.0);
+            kp.pt.apol_dd[i][j] = (m.aDD * pf[i]) * pf[j];
+            kp.pt.apol_cd[i][j] = (m.aCCaCD * pf[i]) * pf[j];
+        }
+    if ((rc = setup_kspace(E, p))) return rc;
+    const double a = kp.ew.aewald;
+    kp.ew.a2 = a * a;
+    kp.ew.cts1 = 2.0 * a / SQPI;
+    kp.ew.cts2 = 4.0 * a * a * a / (3.0 * SQPI);
+    kp.ew.cts3 = 8.0 * (a * a * a * a * a) / (15.0 * SQPI);
+    kp.stath = DEBYE / CHARGECON / std::sqrt((double)kp.natoms);
+    kp.factor = 4.0 * (a * a * a) / (3.0 * std::sqrt(PI));
+    // neighbour-list capacity: 3x the expected O-O pairs, at most all pairs
+    const double shell = 4.0 / 3.0 * PI * p->rc * p->rc * p->rc / kp.volume;
+    const double est = 0.5 * kp.N * (double)kp.N * shell;
+    const double all = 0.5 * kp.N * (double)(kp.N - 1);
+    E.cap = (size_t)std::max(1.0, std::min(all, std::max(1024.0, 3.0 * est)));
+    kp.cap = (int)E.cap;
+    const size_t P = kp.P, S = kp.S, N = kp.N;
+    const int nsq = kp.S - kp.N, nsd = kp.ld - kp.fd;
+    const size_t maxgroups = (size_t)std::max((nsq + 63) / 64, (nsd + 63) / 64);
+    if ((rc = dalloc(E, (double **)&kp.RRt, P * kp.natoms * 3)) || (rc = dalloc(E, (double **)&kp.RRc, kp.natoms * 3)) ||
+        (rc = dalloc(E, &kp.dRRt, P * kp.natoms * 3)) || (rc = dalloc(E, &kp.dipI, P * N * 3)) ||
+        (rc = dalloc(E, &kp.dipE, P * N * 3)) || (rc = dalloc(E, &kp.chg, P * kp.natoms)) ||
+        (rc = dalloc(E, &kp.pos, P * S)) || (rc = dalloc(E, &kp.posc, S)) || (rc = dalloc(E, &kp.F, P * S)) ||
+        (rc = dalloc(E, &kp.dR, P * S * 3)) || (rc = dalloc(E, &kp.dip, P * S * 3)) || (rc = dalloc(E, &kp.Efdr, P * S * 3)) ||
+        (rc = dalloc(E, &kp.txdip, P * 4 * S * 3)) || (rc = dalloc(E, &kp.grdq, P * N * 27)) ||
+        (rc = dalloc(E, &kp.Tdd, P * E.cap * kp.ndd * 6)) || (rc = dalloc(E, &kp.Tself, P * N * 18)) ||
+        (rc = dalloc(E, &kp.pairs, P * E.cap)) || (rc = dalloc(E, &kp.npair, P)) ||
+        (rc = dalloc(E, &kp.tab, P * kp.ntab * S)) || (rc = dalloc(E, &kp.Spart, P * maxgroups * kp.nk * 3)) ||
+        (rc = dalloc(E, &kp.Sq, P * kp.nk)) || (rc = dalloc(E, &kp.Sm, P * kp.nk)) || (rc = dalloc(E, &kp.Sdip, P * kp.nk * 3)) ||
+        (rc = dalloc(E, &kp.acc, P * NACC)) || (rc = dalloc(E, &kp.err, 1)) || (rc = dalloc(E, &kp.allconv, 1)) ||
+        (rc = dalloc(E, &kp.nbrtmp, P * N)) || (rc = dalloc(E, &E.d_out, 3 * P + 16)))
+        return rc;
+    cudaMemset(kp.txdip, 0, sizeof(double) * P * 4 * S * 3);
+    cudaMemset(kp.Sm, 0, sizeof(double2) * P * kp.nk);
+    cudaMemset(kp.err, 0, sizeof(unsigned));
+    if ((rc = cuda_check(E, cudaMallocHost((void **)&E.h_allconv, sizeof(int)), "cudaMallocHost"))) return rc;
+    pot_init_constants(E);
+    return cuda_check(E, cudaDeviceSynchronize(), "init");
+}
+
+// One force call for all beads of the context (pot_ttm.f90:3-630 per bead).
+int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt, double *virialct, double *virt9) {
+    KP &kp = E.kp;
+    kp.t = t;
+    cudaMemsetAsync(kp.acc, 0, sizeof(double) * kp.P * NACC, E.stream);
+    cudaMemsetAsync(kp.err, 0, sizeof(unsigned), E.stream);
+    launch_sites(E);
+    launch_neighbors(E);
+    launch_pair_qq(E);
+    launch_ewald_tables(E);
+    launch_ewald_sq(E);
+    launch_ewald_fq(E);
+    launch_after_qq(E);
+    int iter = 1;
+    for (; iter <= kp.polar_maxiter; iter++) {
+        launch_dd_real(E);
+        launch_ewald_smu(E);
+        launch_dd_update(E, iter);
+        launch_dd_check(E, iter);
+        if (check_every > 0 && (iter % check_every) == 0 && iter < kp.polar_maxiter) {
+            cudaMemcpyAsync(E.h_allconv, kp.allconv, sizeof(int), cudaMemcpyDeviceToHost, E.stream);
+            cudaError_t e = cudaStreamSynchronize(E.stream);
+            if (e != cudaSuccess) return cuda_check(E, e, "dipole iteration");
+            if (*E.h_allconv) break;
+        }
+    }
+    E.last_niter_max = std::min(iter, kp.polar_maxiter);
+    launch_pair_force(E);
+    launch_ewald_qd(E);
+    launch_finish(E);
+    launch_totals(E, Upott, virialt, virialct, virt9);
+    return cuda_check(E, cudaGetLastError(), "force kernels");
+}
+
+static int read_err(Engine &E) {
+    unsigned err = 0;
+    cudaError_t e = cudaMemcpyAsync(&err, E.kp.err, sizeof(unsigned), cudaMemcpyDeviceToHost, E.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(E.stream);
+    if (e != cudaSuccess) return cuda_check(E, e, "force call");
+    if (err & 1u) return fail(E, PIMD_ERR_NEIGHBOR_OVERFLOW, "neighbour list capacity exceeded");
+    if (err & 4u) return fail(E, PIMD_ERR_GAMMQ, "gammq2_3 did not converge");
+    return PIMD_OK;
+}
+
+}  // namespace pimd
+
+using namespace pimd;
+
+extern "C" {
+
+int pimd_create(pimd_ctx **ctx, const pimd_params *p) {
+    if (!ctx) return PIMD_ERR_ARG;
+    *ctx = nullptr;
+    pimd_ctx *c = new pimd_ctx();
+    int rc = create(c->E, p);
+    if (rc) {
+        fprintf(stderr, "pimd_create: %s\n", c->E.last_error.c_str());
+        pimd_destroy(c);
+        return rc;
+    }
+    *ctx = c;
+    return PIMD_OK;
+}
+
+int pimd_destroy(pimd_ctx *ctx) {
+    if (!ctx) return PIMD_OK;
+    Engine &E = ctx->E;
+    cudaSetDevice(E.device);
+    if (E.stream) cudaStreamSynchronize(E.stream);
+    for (void *p : E.allocs) cudaFree(p);
+    if (E.h_allconv) cudaFreeHost(E.h_allconv);
+    if (E.h_pin) cudaFreeHost(E.h_pin);
+    if (E.own_stream && E.stream) cudaStreamDestroy(E.stream);
+    delete ctx;
+    return PIMD_OK;
+}
+
+int pimd_set_stream(pimd_ctx *ctx, void *s) {
+    if (!ctx) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    if (s) {
+        if (E.own_stream && E.stream) cudaStreamDestroy(E.stream);
+        E.stream = (cudaStream_t)s;
+        E.own_stream = false;
+    }
+    return PIMD_OK;
+}
+
+const char *pimd_last_error(pimd_ctx *ctx) { return ctx ? ctx->E.last_error.c_str() : "null context"; }
+
+int pimd_ewald_info(pimd_ctx *ctx, double *alpha, int *nk, int *hkl_max) {
+    if (!ctx) return PIMD_ERR_ARG;
+    const KP &kp = ctx->E.kp;
+    if (alpha) *alpha = kp.ew.aewald;
+    if (nk) *nk = kp.nk;
+    if (hkl_max) {
+        hkl_max[0] = kp.hmax;
+        hkl_max[1] = kp.kmax;
+        hkl_max[2] = kp.lmax;
+    }
+    return PIMD_OK;
+}
+
+int pimd_set_dipole_check(pimd_ctx *ctx, int every) {
+    if (!ctx || every < 0) return PIMD_ERR_ARG;
+    ctx->check_every = every;
+    return PIMD_OK;
+}
+
+int pimd_full_bead_forces_device(pimd_ctx *ctx, const double *RRt, const double *RRc, double *Upott, double *dRRt,
+                                 double *virialt, double *virialct, double *dip_momIt, double *dip_momEt, double *chg,
+                                 int t) {
+    if (!ctx || !RRt || !RRc) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    cudaSetDevice(E.device);
+    KP saved = E.kp;
+    E.kp.RRt = RRt;
+    E.kp.RRc = RRc;
+    if (dRRt) E.kp.dRRt = dRRt;
+    if (dip_momIt) E.kp.dipI = dip_momIt;
+    if (dip_momEt) E.kp.dipE = dip_momEt;
+    int rc = run_forces(E, t, ctx->check_every, Upott, virialt, virialct, nullptr);
+    if (!rc && chg)
+        rc = cuda_check(E, cudaMemcpyAsync(chg, E.kp.chg + (size_t)(E.kp.P - 1) * E.kp.natoms, sizeof(double) * E.kp.natoms,
+                                           cudaMemcpyDeviceToDevice, E.stream), "chg");
+    const double *keepRRt = saved.RRt, *keepRRc = saved.RRc;
+    double *kd = saved.dRRt, *ki = saved.dipI, *ke = saved.dipE;
+    E.kp.RRt = keepRRt;
+    E.kp.RRc = keepRRc;
+    E.kp.dRRt = kd;
+    E.kp.dipI = ki;
+    E.kp.dipE = ke;
+    return rc;
+}
+
+int pimd_full_bead_forces(pimd_ctx *ctx, const double *RRt, const double *RRc, double *Upott, double *dRRt,
+                          double *virialt, double *virialct, double *dip_momIt, double *dip_momEt, double *chg, int t) {
+    if (!ctx || !RRt || !RRc) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    cudaSetDevice(E.device);
+    KP &kp = E.kp;
+    const size_t P = kp.P, na = kp.natoms, nw = kp.N;
+    cudaMemcpyAsync((void *)kp.RRt, RRt, sizeof(double) * P * na * 3, cudaMemcpyHostToDevice, E.stream);
+    cudaMemcpyAsync((void *)kp.RRc, RRc, sizeof(double) * na * 3, cudaMemcpyHostToDevice, E.stream);
+    double *d_out = E.d_out;  // Upott, virialt, virialct staged on the device
+    int rc = run_forces(E, t, ctx->check_every, d_out, d_out + P, d_out + 2 * P, nullptr);
+    if (!rc) {
+        std::vector<double> h(3 * P);
+        cudaMemcpyAsync(h.data(), d_out, sizeof(double) * 3 * P, cudaMemcpyDeviceToHost, E.stream);
+        if (dRRt) cudaMemcpyAsync(dRRt, kp.dRRt, sizeof(double) * P * na * 3, cudaMemcpyDeviceToHost, E.stream);
+        if (dip_momIt) cudaMemcpyAsync(dip_momIt, kp.dipI, sizeof(double) * P * nw * 3, cudaMemcpyDeviceToHost, E.stream);
+        if (dip_momEt) cudaMemcpyAsync(dip_momEt, kp.dipE, sizeof(double) * P * nw * 3, cudaMemcpyDeviceToHost, E.stream);
+        if (chg) cudaMemcpyAsync(chg, kp.chg + (P - 1) * na, sizeof(double) * na, cudaMemcpyDeviceToHost, E.stream);
+        rc = read_err(E);
+        if (!rc) {
+            if (Upott) std::copy(h.begin(), h.begin() + P, Upott);
+            if (virialt) std::copy(h.begin() + P, h.begin() + 2 * P, virialt);
+            if (virialct) std::copy(h.begin() + 2 * P, h.end(), virialct);
+        }
+    }
+    cudaStreamSynchronize(E.stream);
+    return rc;
+}
+
+int pimd_pot_ttm(pimd_ctx *ctx, const double *RR, const double *RRc, double *En, double *dRR, double *virt,
+                 double *virialc, double *dip_momI, double *Edip_mom, double *chg, int t) {
+    if (!ctx || !RR || !RRc) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    cudaSetDevice(E.device);
+    KP saved = E.kp;
+    E.kp.P = 1;  // bead-0 view of the context
+    const size_t na = E.kp.natoms, nw = E.kp.N;
+    cudaMemcpyAsync((void *)E.kp.RRt, RR, sizeof(double) * na * 3, cudaMemcpyHostToDevice, E.stream);
+    cudaMemcpyAsync((void *)E.kp.RRc, RRc, sizeof(double) * na * 3, cudaMemcpyHostToDevice, E.stream);
+    double *d_out = E.d_out;  // En, virialc, virt(9)
+    int rc = run_forces(E, t, ctx->check_every, d_out, nullptr, d_out + 1, d_out + 2);
+    if (!rc) {
+        double h[12];
+        cudaMemcpyAsync(h, d_out, sizeof(h) - sizeof(double), cudaMemcpyDeviceToHost, E.stream);
+        if (dRR) cudaMemcpyAsync(dRR, E.kp.dRRt, sizeof(double) * na * 3, cudaMemcpyDeviceToHost, E.stream);
+        if (dip_momI) cudaMemcpyAsync(dip_momI, E.kp.dipI, sizeof(double) * nw * 3, cudaMemcpyDeviceToHost, E.stream);
+        if (Edip_mom) cudaMemcpyAsync(Edip_mom, E.kp.dipE, sizeof(double) * nw * 3, cudaMemcpyDeviceToHost, E.stream);
+        if (chg) cudaMemcpyAsync(chg, E.kp.chg, sizeof(double) * na, cudaMemcpyDeviceToHost, E.stream);
+        rc = read_err(E);
+        if (!rc) {
+            if (En) *En = h[0];
+            if (virialc) *virialc = h[1];
+            if (virt) std::copy(h + 2, h + 11, virt);
+        }
+    }
+    cudaStreamSynchronize(E.stream);
+    E.kp = saved;
+    return rc;
+}
+
+int pimd_pot_spc(pimd_ctx *ctx, const double *, double *, double *, double *, double *, double *) {
+    if (!ctx) return PIMD_ERR_ARG;
+    return fail(ctx->E, PIMD_ERR_ARG, "context was not created for pot_model 4/5");
+}
+
+int pimd_get_energies(pimd_ctx *ctx, int bead, double U[4]) {
+    if (!ctx || bead < 0 || bead >= ctx->E.kp.P || !U) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    double a[NACC];
+    cudaMemcpyAsync(a, E.kp.acc + (size_t)bead * NACC, sizeof(a), cudaMemcpyDeviceToHost, E.stream);
+    int rc = cuda_check(E, cudaStreamSynchronize(E.stream), "get_energies");
+    if (rc) return rc;
+    U[0] = a[ACC_UMON];
+    U[1] = a[ACC_UVDW];
+    U[2] = 0.5 * a[ACC_UELEC2];
+    U[3] = a[ACC_UIND];
+    return PIMD_OK;
+}
+
+int pimd_get_virial(pimd_ctx *ctx, int bead, double virt[9]) {
+    if (!ctx || bead < 0 || bead >= ctx->E.kp.P || !virt) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    double a[NACC];
+    cudaMemcpyAsync(a, E.kp.acc + (size_t)bead * NACC, sizeof(a), cudaMemcpyDeviceToHost, E.stream);
+    int rc = cuda_check(E, cudaStreamSynchronize(E.stream), "get_virial");
+    if (rc) return rc;
+    for (int i = 0; i < 9; i++) virt[i] = a[ACC_VIRT + i];
+    virt[0] -= E.kp.Uvdw_lrc;
+    virt[4] -= E.kp.Uvdw_lrc;
+    virt[8] -= E.kp.Uvdw_lrc;
+    return PIMD_OK;
+}
+
+int pimd_get_neighbors(pimd_ctx *ctx, int bead, int *ij, int cap, int *npairs) {
+    if (!ctx || bead < 0 || bead >= ctx->E.kp.P || cap < 0) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    int n = 0;
+    cudaMemcpyAsync(&n, E.kp.npair + bead, sizeof(int), cudaMemcpyDeviceToHost, E.stream);
+    int rc = cuda_check(E, cudaStreamSynchronize(E.stream), "get_neighbors");
+    if (rc) return rc;
+    if (npairs) *npairs = n;
+    const int m = std::min(n, cap);
+    if (ij && m > 0) {
+        cudaMemcpyAsync(ij, E.kp.pairs + (size_t)bead * E.kp.cap, sizeof(int2) * m, cudaMemcpyDeviceToHost, E.stream);
+        rc = cuda_check(E, cudaStreamSynchronize(E.stream), "get_neighbors");
+    }
+    return rc;
+}
+
+int pimd_get_dipole_info(pimd_ctx *ctx, int bead, int *niter, double *deltadip) {
+    if (!ctx || bead < 0 || bead >= ctx->E.kp.P) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    double a[NACC];
+    cudaMemcpyAsync(a, E.kp.acc + (size_t)bead * NACC, sizeof(a), cudaMemcpyDeviceToHost, E.stream);
+    int rc = cuda_check(E, cudaStreamSynchronize(E.stream), "get_dipole_info");
+    if (rc) return rc;
+    if (niter) *niter = (int)a[ACC_NITER];
+    if (deltadip) *deltadip = a[ACC_DELTADIP];
+    return PIMD_OK;
+}
+
+}  // extern "C"

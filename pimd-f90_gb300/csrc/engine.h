@@ -1,0 +1,137 @@
+// engine.h -- internal state of one force-engine context and the kernel launchers.
+//
+// One context holds the module state the reference keeps in pot_mod/system_mod
+// (pot_ttm/pot_mod.f90:47-83, system_mod.f90:22-44): model parameters, Ewald k-vector
+// tables, scratch arrays and the per-bead induced-dipole predictor history. All P beads of
+// a ring polymer are evaluated together: every kernel has the bead as a grid axis.
+//
+// HBM layout (per context, P beads, N waters, S sites per bead = 4N for TTM / 3N for SPC,
+// sites in the reference's block order O(0..N-1) H1(N..2N-1) H2(2N..3N-1) M(3N..4N-1)):
+//   pos   [P][S]      double4_32a (x, y, z, q)   site positions and charges
+//   posc  [S]         double4_32a                centroid sites (for the centroid virial)
+//   F     [P][S]      double4_32a (Ex,Ey,Ez,phi) charge field Efq and potential phi
+//   dR    [P][S][3]   gradient accumulator
+//   dip   [P][S][3]   induced dipoles (non-zero on the dipole sites only)
+//   Efdr  [P][S][3]   real-space dipole field of the current iteration
+//   pairs [P][cap]    int2 half neighbour list of O-O pairs (i < j), ordered as find_neigh
+//   Tdd   [P][cap][ND][6]  cached dipole-dipole tensors for the iterations
+//   tab   [P][nx+ny+nz][S]  double2 e^{i 2pi n x/L} recurrence tables (ssincos)
+//   Spart [P][tiles][nk]    double2 per-site-tile structure-factor partials
+//   Sq, Sm [P][nk]          double2 charge / dipole structure factors
+//   Sdip  [P][nk][3]        double2 sum mu_c e^{ik.r} for the reciprocal virial
+//   acc   [P][NACC]         per-bead energy / virial accumulators
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace pimd {
+
+enum { ACC_UMON = 0, ACC_UVDW, ACC_UELEC2, ACC_UIND, ACC_VIRT, ACC_VIRIALC = ACC_VIRT + 9, ACC_DSQ,
+       ACC_MUEFQ, ACC_DELTADIP, ACC_NITER, ACC_CONV, NACC = 24 };
+
+// site-kind parameter tables, index [isp][jsp] with isp, jsp = 1..4 (O, H1, H2, M)
+struct PairTables {
+    double apol_qq[5][5];  // aCCaCD * polfac(i) * polfac(j) for the charge phase
+    double ra_qq[5][5];    // apol_qq^(1/3)
+    double apol_dd[5][5];  // aDD * polfac(i) * polfac(j)
+    double apol_cd[5][5];  // aCCaCD * polfac(i) * polfac(j)
+};
+
+// k-space run: a maximal block of consecutive k-vectors with equal (kx, ky); kz runs over
+// [kzlo, kzlo + nkz). kbeg is the index of the first k-vector of the run.
+struct KRun {
+    int kx, ky, kzlo, nkz, kbeg, pad0, pad1, pad2;
+};
+// structure-factor chunk: k in [k0, k1), runs [r0, r1)
+struct KChunk {
+    int k0, k1, r0, r1;
+};
+
+// Everything a kernel needs, passed by value.
+struct KP {
+    int model, N, S, P, natoms, cap, nk, nrun, nchunk, ntab, hmax, kmax, lmax;
+    int fd, ld;          // dipole sites [fd, ld)
+    int ndd;             // dipole site pairs per molecule pair (TTM3 1, TTM2 9)
+    int contraction, guess, t, polar_maxiter, same_acd;
+    double polar_eps;
+    double box[3], boxi[3], volume, rc2, rc1;
+    double vdwA, vdwB, vdwC, vdwD, vdwE, shiftA, shiftB;
+    double gammaM, polar[5], dms1, dms2, dms3, polar_sor, stath, factor, Uvdw_lrc;
+    double qO, qH, roh0, th0, harmkb, harmka;
+    EwC ew;
+    PairTables pt;
+    // buffers
+    const double *RRt, *RRc;
+    double *dRRt, *dipI, *dipE, *chg;
+    double4_32a *pos, *posc, *F;
+    double *dR, *dip, *Efdr, *txdip, *grdq, *Tdd, *Tself;
+    int2 *pairs;
+    int *npair;
+    double2 *tab, *Spart, *Sq, *Sm, *Sdip;
+    const KRun *runs;
+    const KChunk *chunks;
+    const double4_32a *kinfo;  // (kx, ky, kz) vector, 4pi Ak / V
+    const double *kAk;     // Ak = 2 exp(-k^2/4a^2)/k^2
+    const int2 *kidx;      // (run index, kz) of each k-vector
+    int *nbrtmp;           // [P][N] neighbour counts / offsets
+    double *acc;
+    unsigned *err;
+    int *allconv;
+};
+
+struct Engine {
+    KP kp;
+    int precision = 0;
+    int device = 0;
+    cudaStream_t stream = 0;
+    bool own_stream = false;
+    int nchunk = 0, ntile_q = 0, ntile_d = 0, max_runs_chunk = 0;
+    size_t cap = 0;
+    std::vector<KRun> h_runs;
+    std::vector<KChunk> h_chunks;
+    std::vector<int> h_khkl;
+    std::vector<double> h_kvec, h_Ak;
+    // host pinned staging
+    double *h_pin = nullptr;
+    size_t h_pin_bytes = 0;
+    int *h_allconv = nullptr;
+    double *d_out = nullptr;  // small device staging for per-bead scalar outputs
+    std::vector<void *> allocs;
+    std::string last_error;
+    int last_niter_max = 0;
+    // normal modes (filled by pimd_nm_init)
+    int nm_P = 0;
+    double *d_nmC = nullptr, *d_nmA = nullptr;  // C(P,P), [A11,A12,A21,A22,msf,c1,c2] x P
+    std::vector<double> h_nm;                     // host copy: A11..A22, omegalist, msf, C
+};
+
+// launchers (pot.cu)
+void pot_init_constants(Engine &E);
+void launch_sites(Engine &E);
+void launch_neighbors(Engine &E);
+void launch_pair_qq(Engine &E);
+void launch_after_qq(Engine &E);
+void launch_dd_real(Engine &E);
+void launch_dd_update(Engine &E, int iter);
+void launch_dd_check(Engine &E, int iter);
+void launch_pair_force(Engine &E);
+void launch_finish(Engine &E);
+void launch_totals(Engine &E, double *Upott, double *virialt, double *virialct, double *virt9);
+// launchers (ewald.cu)
+void launch_ewald_tables(Engine &E);
+void launch_ewald_sq(Engine &E);
+void launch_ewald_fq(Engine &E);
+void launch_ewald_smu(Engine &E);
+void launch_ewald_qd(Engine &E);
+
+}  // namespace pimd
+
+// The opaque handle of the C ABI (include/pimd_gb300.h).
+struct pimd_ctx {
+    pimd::Engine E;
+    int check_every = 1;  // host convergence check period of the dipole iterations
+};

@@ -1,0 +1,472 @@
+// nm.cu -- ring-polymer normal modes, PILE Langevin thermostat and the velocity-Verlet PIMD
+// step on the device. Restates NormalModes.f90 (EvolveRing 34-63, InitNormalModes 68-218,
+// real2NM/NM2real 308-341), Langevin.f90 (Langevin_NM 30-64, Init_Langevin_NM 68-98),
+// MD.f90:35-110 (PIMD_VV) and main_stuff.f90 (PBCs 107-125, calc_uk 349-388).
+//
+// One group of 3P threads owns one atom (thread = (bead j, component c)); the P x P mode
+// matrix C sits in shared memory. The transforms are summed in the reference's order with
+// every product and sum rounded separately, so they are bit-identical to the FP64 oracle.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/pimd_gb300.h"
+#include "engine.h"
+
+namespace pimd {
+
+int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt, double *virialct, double *virt9);
+
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, SC'11).
+PIMD_D uint4 philox4x32(uint4 ctr, uint2 key) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const unsigned hi0 = __umulhi(0xD2511F53u, ctr.x), lo0 = 0xD2511F53u * ctr.x;
+        const unsigned hi1 = __umulhi(0xCD9E8D57u, ctr.z), lo1 = 0xCD9E8D57u * ctr.z;
+        ctr = make_uint4(hi1 ^ ctr.y ^ key.x, lo1, hi0 ^ ctr.w ^ key.y, lo0);
+        key.x += 0x9E3779B9u;
+        key.y += 0xBB67AE85u;
+    }
+    return ctr;
+}
+// standard normal from two uniform 32-bit words (Box-Muller, radius branch)
+PIMD_D double gauss_from(unsigned a, unsigned b) {
+    const double u1 = ((double)a + 1.0) * 2.3283064365386963e-10;  // (0, 1]
+    const double u2 = (double)b * 2.3283064365386963e-10;          // [0, 1)
+    return sqrt(-2.0 * log(u1)) * cos(TWOPI * u2);
+}
+
+struct NMArgs {
+    int P, natoms;
+    const double *C;    // C(P,P) column-major: C[j + P*k] = C(j+1, k+1)
+    const double *A;    // [A11, A12, A21, A22, msf, c1, c2] x P
+    double massO, massH;
+    double delt, delt2, box0, boxi0;
+    int langevin, evolve;
+    const double *xi;   // (3, P, Natoms) standard normals, or null
+    unsigned long long seed, counter;
+};
+
+PIMD_D double noise(const NMArgs &a, int atom, int j, int c) {
+    if (a.xi) return a.xi[c + 3 * j + (size_t)3 * a.P * atom];
+    const unsigned long long idx = ((unsigned long long)atom * a.P + j) * 3 + c;
+    const uint4 r = philox4x32(make_uint4((unsigned)idx, (unsigned)(idx >> 32), (unsigned)a.counter,
+                                          (unsigned)(a.counter >> 32)),
+                               make_uint2((unsigned)a.seed, (unsigned)(a.seed >> 32)));
+    return gauss_from(r.x, r.y);
+}
+
+// x~_j = sum_k C(j,k) x_k  (real2NM) or x_j = sum_k C(k,j) x~_k (NM2real), rounded per op
+PIMD_D double nm_row(const double *Cs, const double *v, int P, int j, int c, bool fwd) {
+    double s = 0.0;
+    for (int k = 0; k < P; k++) {
+        const double ck = fwd ? Cs[j + P * k] : Cs[k + P * j];
+        s = __dadd_rn(s, __dmul_rn(ck, v[3 * k + c]));
+    }
+    return s;
+}
+
+// Langevin_NM on one atom's momenta held in shared memory p[3P] (group-local).
+PIMD_D void langevin_atom(const NMArgs &a, const double *Cs, double *p, double *tr, int atom, int j, int c,
+                          bool active) {
+    if (active) tr[3 * j + c] = nm_row(Cs, p, a.P, j, c, true);
+    __syncthreads();
+    if (active) {
+        const double m = (atom % 3 == 0) ? a.massO : a.massH;
+        const double sqrtmass = sqrt(m * a.A[4 * a.P + j]);
+        const double c1 = a.A[5 * a.P + j], c2 = a.A[6 * a.P + j];
+        tr[3 * j + c] = __dadd_rn(__dmul_rn(c1, tr[3 * j + c]), __dmul_rn(c2, __dmul_rn(sqrtmass, noise(a, atom, j, c))));
+    }
+    __syncthreads();
+    if (active) p[3 * j + c] = nm_row(Cs, tr, a.P, j, c, false);
+    __syncthreads();
+}
+
+// MD.f90:40-73 up to the force call: Langevin, half kick, EvolveRing (or free flight for
+// P = 1), centroid and the centroid-following PBC shift (main_stuff.f90:107-125).
+__global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt, double *RRc) {
+    extern __shared__ double sh[];
+    const int P = a.P, G = blockDim.x / (3 * P);
+    const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
+    const int atom = blockIdx.x * G + g;
+    double *Cs = sh;
+    double *x = Cs + P * P + g * 9 * P, *p = x + 3 * P, *tr = p + 3 * P;
+    for (int i = threadIdx.x; i < P * P; i += blockDim.x) Cs[i] = a.C[i];
+    const bool active = g < G && atom < a.natoms;
+    const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
+    if (active) {
+        x[3 * j + c] = RRt[gi];
+        p[3 * j + c] = PPt[gi];
+    }
+    __syncthreads();
+    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active);
+    if (active) p[3 * j + c] = __dsub_rn(p[3 * j + c], __dmul_rn(__dmul_rn(MASSCON, dRRt[gi]), a.delt2));
+    __syncthreads();
+    const double m = (atom % 3 == 0) ? a.massO : a.massH;
+    if (a.evolve) {
+        double xt = 0, pt = 0;
+        if (active) {
+            xt = nm_row(Cs, x, P, j, c, true);
+            pt = nm_row(Cs, p, P, j, c, true);
+        }
+        __syncthreads();
+        if (active) {
+            const double A11 = a.A[j], A12 = a.A[P + j], A21 = a.A[2 * P + j], A22 = a.A[3 * P + j], msf = a.A[4 * P + j];
+            const double xn = __dadd_rn(__dmul_rn(A11, xt), __ddiv_rn(__dmul_rn(A12, pt), __dmul_rn(m, msf)));
+            const double pn = __dadd_rn(__dmul_rn(__dmul_rn(__dmul_rn(A21, m), msf), xt), __dmul_rn(A22, pt));
+            tr[3 * j + c] = xn;
+            x[3 * j + c] = pn;  // reuse x as the momentum-mode buffer
+        }
+        __syncthreads();
+        double xr = 0, pr = 0;
+        if (active) {
+            xr = nm_row(Cs, tr, P, j, c, false);
+            pr = nm_row(Cs, x, P, j, c, false);
+        }
+        __syncthreads();
+        if (active) {
+            x[3 * j + c] = xr;
+            p[3 * j + c] = pr;
+        }
+        __syncthreads();
+    } else if (active) {
+        x[3 * j + c] = __dadd_rn(x[3 * j + c], __dmul_rn(__dmul_rn(1.0 / m, p[3 * j + c]), a.delt));
+    }
+    __syncthreads();
+    if (active && j == 0) {
+        double s = 0.0;
+        for (int k = 0; k < P; k++) s = __dadd_rn(s, x[3 * k + c]);
+        double rc = __ddiv_rn(s, (double)P);
+        const double shift = __dmul_rn(a.box0, round(__dmul_rn(rc, a.boxi0)));
+        RRc[3 * atom + c] = __dsub_rn(rc, shift);
+        tr[c] = shift;
+    }
+    __syncthreads();
+    if (active) {
+        RRt[gi] = __dsub_rn(x[3 * j + c], tr[c]);
+        PPt[gi] = p[3 * j + c];
+    }
+}
+
+// MD.f90:94-101: half kick with the new gradient, Langevin, kinetic energy (calc_uk)
+__global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk) {
+    extern __shared__ double sh[];
+    const int P = a.P, G = blockDim.x / (3 * P);
+    const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
+    const int atom = blockIdx.x * G + g;
+    double *Cs = sh;
+    double *p = Cs + P * P + g * 9 * P, *tr = p + 3 * P;
+    for (int i = threadIdx.x; i < P * P; i += blockDim.x) Cs[i] = a.C[i];
+    const bool active = g < G && atom < a.natoms;
+    const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
+    if (active) p[3 * j + c] = __dsub_rn(PPt[gi], __dmul_rn(__dmul_rn(MASSCON, dRRt[gi]), a.delt2));
+    __syncthreads();
+    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active);
+    double ke = 0.0;
+    if (active) {
+        PPt[gi] = p[3 * j + c];
+        const double m = (atom % 3 == 0) ? a.massO : a.massH;
+        ke = (1.0 / m) * p[3 * j + c] * p[3 * j + c];
+    }
+    for (int o = 16; o > 0; o >>= 1) ke += __shfl_xor_sync(0xffffffffu, ke, o);
+    if ((threadIdx.x & 31) == 0 && uk) atomicAdd(uk, 0.5 * ke);
+}
+
+// EvolveRing alone for every atom (no kick, no thermostat)
+__global__ void k_evolve(NMArgs a, double *RRt, double *PPt) {
+    extern __shared__ double sh[];
+    const int P = a.P, G = blockDim.x / (3 * P);
+    const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
+    const int atom = blockIdx.x * G + g;
+    double *Cs = sh;
+    double *x = Cs + P * P + g * 9 * P, *p = x + 3 * P, *tr = p + 3 * P;
+    for (int i = threadIdx.x; i < P * P; i += blockDim.x) Cs[i] = a.C[i];
+    const bool active = g < G && atom < a.natoms;
+    const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
+    if (active) {
+        x[3 * j + c] = RRt[gi];
+        p[3 * j + c] = PPt[gi];
+    }
+    __syncthreads();
+    const double m = (atom % 3 == 0) ? a.massO : a.massH;
+    double xt = 0, pt = 0;
+    if (active) {
+        xt = nm_row(Cs, x, P, j, c, true);
+        pt = nm_row(Cs, p, P, j, c, true);
+    }
+    __syncthreads();
+    if (active) {
+        const double A11 = a.A[j], A12 = a.A[P + j], A21 = a.A[2 * P + j], A22 = a.A[3 * P + j], msf = a.A[4 * P + j];
+        tr[3 * j + c] = __dadd_rn(__dmul_rn(A11, xt), __ddiv_rn(__dmul_rn(A12, pt), __dmul_rn(m, msf)));
+        x[3 * j + c] = __dadd_rn(__dmul_rn(__dmul_rn(__dmul_rn(A21, m), msf), xt), __dmul_rn(A22, pt));
+    }
+    __syncthreads();
+    if (active) {
+        RRt[gi] = nm_row(Cs, tr, P, j, c, false);
+        PPt[gi] = nm_row(Cs, x, P, j, c, false);
+    }
+}
+
+__global__ void k_langevin(NMArgs a, double *PPt) {
+    extern __shared__ double sh[];
+    const int P = a.P, G = blockDim.x / (3 * P);
+    const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
+    const int atom = blockIdx.x * G + g;
+    double *Cs = sh;
+    double *p = Cs + P * P + g * 9 * P, *tr = p + 3 * P;
+    for (int i = threadIdx.x; i < P * P; i += blockDim.x) Cs[i] = a.C[i];
+    const bool active = g < G && atom < a.natoms;
+    const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
+    if (active) p[3 * j + c] = PPt[gi];
+    __syncthreads();
+    langevin_atom(a, Cs, p, tr, atom, j, c, active);
+    if (active) PPt[gi] = p[3 * j + c];
+}
+
+__global__ void k_md_sum(int P, const double *Upott, const double *virialt, const double *virialct, const double *uk,
+                         double *out4) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double u = 0, v = 0, vc = 0;
+    for (int k = 0; k < P; k++) {
+        u += Upott[k];
+        v += virialt[k];
+        vc += virialct[k];
+    }
+    out4[0] = u;
+    out4[1] = v;
+    out4[2] = vc / P;
+    out4[3] = *uk;
+}
+
+// ---------------------------------------------------------------------------------------
+static void nm_launch_shape(int P, int natoms, int *threads, int *blocks, size_t *smem) {
+    int G = 256 / (3 * P);
+    if (G < 1) G = 1;
+    *threads = G * 3 * P;
+    *blocks = (natoms + G - 1) / G;
+    *smem = sizeof(double) * ((size_t)P * P + (size_t)G * 9 * P);
+}
+
+static NMArgs nm_args(Engine &E, double massO, double massH) {
+    NMArgs a{};
+    a.P = E.nm_P;
+    a.natoms = E.kp.natoms;
+    a.C = E.d_nmC;
+    a.A = E.d_nmA;
+    a.massO = massO;
+    a.massH = massH;
+    a.box0 = E.kp.box[0];
+    a.boxi0 = E.kp.boxi[0];
+    return a;
+}
+
+// NormalModes.f90:68-218
+static void nm_init_host(int P, double omegan, double delta, double setNMfreq, std::vector<double> &A11,
+                         std::vector<double> &A12, std::vector<double> &A21, std::vector<double> &A22,
+                         std::vector<double> &om, std::vector<double> &msf, std::vector<double> &C) {
+    A11.assign(P, 0);
+    A12.assign(P, 0);
+    A21.assign(P, 0);
+    A22.assign(P, 0);
+    om.assign(P, 0);
+    msf.assign(P, 1.0);
+    C.assign((size_t)P * P, 0);
+    const int l = (P % 2 == 0) ? (P - 2) / 2 : (P - 1) / 2;
+    for (int i = 1; i <= P; i++) {
+        C[0 + P * (i - 1)] = std::sqrt(1.0 / P);
+        for (int k = 1; k <= l; k++) {
+            C[k + P * (i - 1)] = std::sqrt(2.0 / P) * std::cos((double)(k * i) * 2.0 * PI / P);
+            C[k + l + P * (i - 1)] = std::sqrt(2.0 / P) * std::sin((double)(k * i) * 2.0 * PI / P);
+        }
+        if (P % 2 == 0) C[2 * l + 1 + P * (i - 1)] = std::sqrt(1.0 / P) * ((i % 2 == 0) ? 1.0 : -1.0);
+    }
+    A11[0] = 1.0;
+    A12[0] = delta;
+    A21[0] = 0.0;
+    A22[0] = 1.0;
+    auto set_mode = [&](int idx, int k) {
+        // NormalModes.f90:126: abs(k)/real(Nbeads) is a single-precision quotient
+        const float ratio = (float)std::abs(k) / (float)P;
+        const double omega = 2 * omegan * std::sin(PI * (double)ratio);
+        om[idx] = omega;
+        A11[idx] = std::cos(omega * delta);
+        A12[idx] = (1.0 / omega) * std::sin(omega * delta);
+        A21[idx] = -omega * std::sin(omega * delta);
+        A22[idx] = std::cos(omega * delta);
+    };
+    for (int k = 1; k <= l; k++) set_mode(k, k);
+    for (int k = 1; k <= l; k++) set_mode(k + l, k);
+    if (P % 2 == 0) set_mode(2 * l + 1, l + 1);
+    if (setNMfreq != 0) {
+        const double omega = (2 * PI) * setNMfreq / 33.33333;
+        for (int i = 0; i < P; i++) msf[i] = (om[i] == 0) ? 1.0 : (om[i] / omega) * (om[i] / omega);
+        const int hi = (P % 2 == 0) ? 2 * l + 1 : 2 * l;
+        for (int i = 1; i <= hi; i++) {
+            om[i] = omega;
+            A11[i] = std::cos(omega * delta);
+            A12[i] = (1.0 / omega) * std::sin(omega * delta);
+            A21[i] = -omega * std::sin(omega * delta);
+            A22[i] = std::cos(omega * delta);
+        }
+    }
+}
+
+}  // namespace pimd
+
+using namespace pimd;
+
+static int nm_err(Engine &E, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return PIMD_OK;
+    E.last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return PIMD_ERR_CUDA;
+}
+
+extern "C" {
+
+int pimd_nm_init(pimd_ctx *ctx, int P, double omegan, double delta, double setNMfreq, double *A11, double *A12,
+                 double *A21, double *A22, double *omegalist, double *msf, double *C) {
+    if (!ctx || P < 1 || P > 64) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    cudaSetDevice(E.device);
+    std::vector<double> a11, a12, a21, a22, om, ms, CC;
+    nm_init_host(P, omegan, delta, setNMfreq, a11, a12, a21, a22, om, ms, CC);
+    if (E.nm_P != P) {
+        if (E.d_nmC) cudaFree(E.d_nmC);
+        if (E.d_nmA) cudaFree(E.d_nmA);
+        if (cudaMalloc((void **)&E.d_nmC, sizeof(double) * P * P) != cudaSuccess ||
+            cudaMalloc((void **)&E.d_nmA, sizeof(double) * 7 * P) != cudaSuccess)
+            return PIMD_ERR_NOMEM;
+        E.nm_P = P;
+    }
+    std::vector<double> A(7 * P, 0.0);
+    for (int j = 0; j < P; j++) {
+        A[j] = a11[j];
+        A[P + j] = a12[j];
+        A[2 * P + j] = a21[j];
+        A[3 * P + j] = a22[j];
+        A[4 * P + j] = ms[j];
+        A[5 * P + j] = 1.0;  // c1, c2 until pimd_langevin_init
+        A[6 * P + j] = 0.0;
+    }
+    E.h_nm = A;
+    E.h_nm.insert(E.h_nm.end(), om.begin(), om.end());
+    cudaMemcpy(E.d_nmC, CC.data(), sizeof(double) * P * P, cudaMemcpyHostToDevice);
+    cudaMemcpy(E.d_nmA, A.data(), sizeof(double) * 7 * P, cudaMemcpyHostToDevice);
+    auto out = [&](double *dst, const std::vector<double> &v) {
+        if (dst) std::memcpy(dst, v.data(), sizeof(double) * v.size());
+    };
+    out(A11, a11);
+    out(A12, a12);
+    out(A21, a21);
+    out(A22, a22);
+    out(omegalist, om);
+    out(msf, ms);
+    out(C, CC);
+    return nm_err(E, cudaGetLastError(), "nm_init");
+}
+
+int pimd_langevin_init(pimd_ctx *ctx, double delt2, int centroid_thermostat, double tau_centroid, double temp_P) {
+    if (!ctx) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    if (!E.nm_P) return PIMD_ERR_STATE;
+    const int P = E.nm_P;
+    std::vector<double> &A = E.h_nm;
+    const double *om = A.data() + 7 * P;
+    for (int i = 0; i < P; i++) {
+        double gammak = (i == 0) ? (centroid_thermostat ? 1.0 / tau_centroid : 0.0) : 2 * om[i];
+        const double c1 = std::exp(-delt2 * gammak);
+        double c2 = std::sqrt(1 - c1 * c1);
+        c2 = std::sqrt(KB_AMU * temp_P) * c2;
+        A[5 * P + i] = c1;
+        A[6 * P + i] = c2;
+    }
+    cudaSetDevice(E.device);
+    return nm_err(E, cudaMemcpy(E.d_nmA, A.data(), sizeof(double) * 7 * P, cudaMemcpyHostToDevice), "langevin_init");
+}
+
+int pimd_evolve_ring(pimd_ctx *ctx, double *RR, double *PP, int P, double mass) {
+    if (!ctx || !RR || !PP || P != ctx->E.nm_P) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    cudaSetDevice(E.device);
+    double *d;
+    if (cudaMalloc((void **)&d, sizeof(double) * 6 * P) != cudaSuccess) return PIMD_ERR_NOMEM;
+    cudaMemcpy(d, RR, sizeof(double) * 3 * P, cudaMemcpyHostToDevice);
+    cudaMemcpy(d + 3 * P, PP, sizeof(double) * 3 * P, cudaMemcpyHostToDevice);
+    NMArgs a = nm_args(E, mass, mass);
+    a.natoms = 1;
+    int threads, blocks;
+    size_t smem;
+    nm_launch_shape(P, 1, &threads, &blocks, &smem);
+    k_evolve<<<blocks, threads, smem, E.stream>>>(a, d, d + 3 * P);
+    cudaMemcpyAsync(RR, d, sizeof(double) * 3 * P, cudaMemcpyDeviceToHost, E.stream);
+    cudaMemcpyAsync(PP, d + 3 * P, sizeof(double) * 3 * P, cudaMemcpyDeviceToHost, E.stream);
+    cudaError_t e = cudaStreamSynchronize(E.stream);
+    cudaFree(d);
+    return nm_err(E, e, "evolve_ring");
+}
+
+int pimd_evolve_all_device(pimd_ctx *ctx, double *RRt, double *PPt, double massO, double massH) {
+    if (!ctx || !RRt || !PPt || !ctx->E.nm_P) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    NMArgs a = nm_args(E, massO, massH);
+    int threads, blocks;
+    size_t smem;
+    nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
+    k_evolve<<<blocks, threads, smem, E.stream>>>(a, RRt, PPt);
+    return nm_err(E, cudaGetLastError(), "evolve_all");
+}
+
+int pimd_langevin_nm_device(pimd_ctx *ctx, double *PPt, const double *xi, double massO, double massH,
+                            unsigned long long seed, unsigned long long counter) {
+    if (!ctx || !PPt || !ctx->E.nm_P) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    NMArgs a = nm_args(E, massO, massH);
+    a.xi = xi;
+    a.seed = seed;
+    a.counter = counter;
+    a.langevin = 1;
+    int threads, blocks;
+    size_t smem;
+    nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
+    k_langevin<<<blocks, threads, smem, E.stream>>>(a, PPt);
+    return nm_err(E, cudaGetLastError(), "langevin_nm");
+}
+
+int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,
+                        const double *xi1, const double *xi2, int t, double *out4) {
+    if (!ctx || !mp || !RRt || !PPt || !dRRt || !RRc) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    if (E.nm_P != E.kp.P) return PIMD_ERR_STATE;
+    cudaSetDevice(E.device);
+    NMArgs a = nm_args(E, mp->massO, mp->massH);
+    a.delt = mp->delt;
+    a.delt2 = mp->delt / 2.0;
+    a.langevin = mp->langevin;
+    a.evolve = E.kp.P > 1;
+    a.seed = mp->seed;
+    a.counter = 2ull * (unsigned long long)t;
+    a.xi = xi1;
+    int threads, blocks;
+    size_t smem;
+    nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
+    k_md_pre<<<blocks, threads, smem, E.stream>>>(a, RRt, PPt, dRRt, RRc);
+    KP saved = E.kp;
+    E.kp.RRt = RRt;
+    E.kp.RRc = RRc;
+    E.kp.dRRt = dRRt;
+    double *d = E.d_out;  // Upott, virialt, virialct (3P) then uk
+    int rc = run_forces(E, t, ctx->check_every, d, d + E.kp.P, d + 2 * E.kp.P, nullptr);
+    E.kp.RRt = saved.RRt;
+    E.kp.RRc = saved.RRc;
+    E.kp.dRRt = saved.dRRt;
+    if (rc) return rc;
+    double *uk = d + 3 * E.kp.P;
+    cudaMemsetAsync(uk, 0, sizeof(double), E.stream);
+    a.xi = xi2;
+    a.counter = 2ull * (unsigned long long)t + 1ull;
+    k_md_post<<<blocks, threads, smem, E.stream>>>(a, PPt, dRRt, uk);
+    if (out4) k_md_sum<<<1, 32, 0, E.stream>>>(E.kp.P, d, d + E.kp.P, d + 2 * E.kp.P, uk, out4);
+    return nm_err(E, cudaGetLastError(), "md_step");
+}
+
+}  // extern "C"

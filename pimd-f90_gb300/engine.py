@@ -1,0 +1,228 @@
+"""Python host mirror of PIMD-F90's hot-path interfaces over the C ABI (libpimd_gb300.so).
+
+Names, argument order and meaning follow the reference:
+  ForceEngine.pot_ttm(RR, RRc, t)            pot_ttm/pot_ttm.f90:3
+  ForceEngine.full_bead_forces(RRt, RRc, t)  force_calc.f90:26-106 (all beads in one call)
+  ForceEngine.nm_init / evolve_ring          NormalModes.f90:68, :34
+Arrays are numpy float64 in the reference's layouts stored C-order: RR (Natoms, 3) is the
+Fortran RR(3, Natoms); RRt (P, Natoms, 3) is RRt(3, Natoms, P).
+
+The engine runs only on the GPU: if the shared library or a CUDA device is missing every
+call raises; there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libpimd_gb300.so")
+
+PIMD_FP64, PIMD_MIXED = 0, 1
+ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "neighbour list overflow", 4: "gammq did not converge",
+          5: "out of device memory", 6: "call-order violation"}
+
+
+class PimdError(RuntimeError):
+    pass
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("pot_model", ctypes.c_int), ("natoms", ctypes.c_int), ("nbeads", ctypes.c_int),
+                ("box", ctypes.c_double * 3), ("rc", ctypes.c_double), ("rc1", ctypes.c_double),
+                ("eps_ewald", ctypes.c_double), ("alpha", ctypes.c_double), ("nmax", ctypes.c_int),
+                ("polar_maxiter", ctypes.c_int), ("polar_sor", ctypes.c_double), ("polar_eps", ctypes.c_double),
+                ("guess_initdip", ctypes.c_int), ("contraction", ctypes.c_int), ("precision", ctypes.c_int),
+                ("device", ctypes.c_int)]
+
+
+class MDParams(ctypes.Structure):
+    _fields_ = [("delt", ctypes.c_double), ("massO", ctypes.c_double), ("massH", ctypes.c_double),
+                ("langevin", ctypes.c_int), ("seed", ctypes.c_ulonglong)]
+
+
+# every entry point of include/pimd_gb300.h with its ctypes signature
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+_V = ctypes.c_void_p
+SIGNATURES = {
+    "pimd_create": [ctypes.POINTER(_V), ctypes.POINTER(Params)],
+    "pimd_destroy": [_V],
+    "pimd_set_stream": [_V, _V],
+    "pimd_last_error": [_V],
+    "pimd_ewald_info": [_V, _D, _I, _I],
+    "pimd_pot_ttm": [_V, _D, _D, _D, _D, _D, _D, _D, _D, _D, ctypes.c_int],
+    "pimd_pot_spc": [_V, _D, _D, _D, _D, _D, _D],
+    "pimd_full_bead_forces": [_V, _D, _D, _D, _D, _D, _D, _D, _D, _D, ctypes.c_int],
+    "pimd_full_bead_forces_device": [_V, _V, _V, _V, _V, _V, _V, _V, _V, _V, ctypes.c_int],
+    "pimd_get_energies": [_V, ctypes.c_int, _D],
+    "pimd_get_virial": [_V, ctypes.c_int, _D],
+    "pimd_get_dipole_info": [_V, ctypes.c_int, _I, _D],
+    "pimd_set_dipole_check": [_V, ctypes.c_int],
+    "pimd_get_neighbors": [_V, ctypes.c_int, _I, ctypes.c_int, _I],
+    "pimd_nm_init": [_V, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, _D, _D, _D, _D, _D, _D,
+                     _D],
+    "pimd_evolve_ring": [_V, _D, _D, ctypes.c_int, ctypes.c_double],
+    "pimd_evolve_all_device": [_V, _V, _V, ctypes.c_double, ctypes.c_double],
+    "pimd_langevin_init": [_V, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double],
+    "pimd_langevin_nm_device": [_V, _V, _V, ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong,
+                                ctypes.c_ulonglong],
+    "pimd_md_step_device": [_V, ctypes.POINTER(MDParams), _V, _V, _V, _V, _V, _V, ctypes.c_int, _V],
+}
+
+_lib = None
+
+
+def load(path=LIB):
+    """Load the engine library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise PimdError("libpimd_gb300.so not built: run __graft_entry__.build()")
+        L = ctypes.CDLL(path)
+        for name, args in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = ctypes.c_char_p if name == "pimd_last_error" else ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(_D) if a is not None else None
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def make_params(d, precision=PIMD_FP64, device=0):
+    p = Params()
+    p.pot_model = int(d["pot_model"])
+    p.natoms = int(d["natoms"])
+    p.nbeads = int(d.get("nbeads", 1))
+    for i in range(3):
+        p.box[i] = float(d["box"][i])
+    p.rc = float(d["rc"])
+    p.rc1 = float(d.get("rc1", 0.8 * d["rc"]))
+    p.eps_ewald = float(d.get("eps_ewald", 1e-6))
+    a = d.get("alpha")
+    p.alpha = float(a) if a else 0.0
+    p.nmax = int(d.get("nmax", 0) or 0)
+    p.polar_maxiter = int(d.get("polar_maxiter", 15))
+    p.polar_sor = float(d.get("polar_sor", 0.7))
+    p.polar_eps = float(d.get("polar_eps", 1e-5))
+    p.guess_initdip = int(d.get("guess_initdip", 0))
+    p.contraction = int(d.get("contraction", 0))
+    p.precision = int(d.get("precision", precision))
+    p.device = int(d.get("device", device))
+    return p
+
+
+class ForceEngine:
+    """One engine context: the reference's init_pot module state for P beads."""
+
+    def __init__(self, params, precision=PIMD_FP64, device=0):
+        L = load()
+        self.params = dict(params)
+        self._p = make_params(params, precision, device)
+        h = _V()
+        rc = L.pimd_create(ctypes.byref(h), ctypes.byref(self._p))
+        if rc:
+            raise PimdError("pimd_create failed (%d: %s)" % (rc, ERRORS.get(rc, "?")))
+        self.h = h
+        self.natoms = self._p.natoms
+        self.nw = self.natoms // 3
+        self.P = self._p.nbeads
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().pimd_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def _check(self, rc, what):
+        if rc:
+            msg = load().pimd_last_error(self.h)
+            raise PimdError("%s failed (%d: %s): %s" % (what, rc, ERRORS.get(rc, "?"), msg.decode() if msg else ""))
+
+    def ewald_info(self):
+        a = ctypes.c_double()
+        nk = ctypes.c_int()
+        hkl = (ctypes.c_int * 3)()
+        self._check(load().pimd_ewald_info(self.h, ctypes.byref(a), ctypes.byref(nk), hkl), "ewald_info")
+        return a.value, nk.value, tuple(hkl)
+
+    def set_dipole_check(self, every):
+        self._check(load().pimd_set_dipole_check(self.h, int(every)), "set_dipole_check")
+
+    def energies(self, bead=0):
+        U = np.zeros(4)
+        self._check(load().pimd_get_energies(self.h, bead, _p(U)), "get_energies")
+        n = ctypes.c_int()
+        dd = ctypes.c_double()
+        self._check(load().pimd_get_dipole_info(self.h, bead, ctypes.byref(n), ctypes.byref(dd)), "dipole_info")
+        return dict(Umon=U[0], Uvdw=U[1], Uelec=U[2], Uind=U[3], niter=n.value, deltadip=dd.value)
+
+    def neighbors(self, bead=0):
+        """The O-O half neighbour list (npairs, 2) of the last force call."""
+        n = ctypes.c_int()
+        self._check(load().pimd_get_neighbors(self.h, bead, None, 0, ctypes.byref(n)), "get_neighbors")
+        ij = np.zeros((max(1, n.value), 2), np.int32)
+        self._check(load().pimd_get_neighbors(self.h, bead, ij.ctypes.data_as(_I), n.value, ctypes.byref(n)),
+                    "get_neighbors")
+        return ij[:n.value].copy()
+
+    def virial(self, bead=0):
+        v = np.zeros(9)
+        self._check(load().pimd_get_virial(self.h, bead, _p(v)), "get_virial")
+        return v.reshape(3, 3, order="F")
+
+    def pot_ttm(self, RR, RRc, t=1):
+        """pot_ttm(RR, RRc, En, dRR, virt, virialc, dip_momI, Edip_mom, chg, t)"""
+        RR, RRc = _f64(RR), _f64(RRc)
+        En, vc = ctypes.c_double(), ctypes.c_double()
+        dRR = np.zeros_like(RR)
+        virt = np.zeros(9)
+        dI = np.zeros((self.nw, 3))
+        dE = np.zeros((self.nw, 3))
+        chg = np.zeros(self.natoms)
+        rc = load().pimd_pot_ttm(self.h, _p(RR), _p(RRc), ctypes.byref(En), _p(dRR), _p(virt), ctypes.byref(vc),
+                                 _p(dI), _p(dE), _p(chg), int(t))
+        self._check(rc, "pot_ttm")
+        out = dict(En=En.value, dRR=dRR, virt=virt.reshape(3, 3, order="F"), virialc=vc.value, dip_momI=dI,
+                   Edip_mom=dE, chg=chg)
+        out.update(self.energies(0))
+        return out
+
+    def full_bead_forces(self, RRt, RRc, t=1):
+        RRt, RRc = _f64(RRt), _f64(RRc)
+        P = self.P
+        Upott, virialt, virialct = np.zeros(P), np.zeros(P), np.zeros(P)
+        dRRt = np.zeros_like(RRt)
+        dI = np.zeros((P, self.nw, 3))
+        dE = np.zeros((P, self.nw, 3))
+        chg = np.zeros(self.natoms)
+        rc = load().pimd_full_bead_forces(self.h, _p(RRt), _p(RRc), _p(Upott), _p(dRRt), _p(virialt), _p(virialct),
+                                          _p(dI), _p(dE), _p(chg), int(t))
+        self._check(rc, "full_bead_forces")
+        return dict(Upott=Upott, dRRt=dRRt, virialt=virialt, virialct=virialct, dip_momIt=dI, dip_momEt=dE, chg=chg,
+                    Upot=Upott.sum(), virial=virialt.sum(), virialc=virialct.sum() / P)
+
+    # ---- NormalModes.f90 / Langevin.f90 ------------------------------------------------
+    def nm_init(self, P, omegan, delta, setNMfreq=0.0):
+        A = [np.zeros(P) for _ in range(6)]
+        C = np.zeros(P * P)
+        rc = load().pimd_nm_init(self.h, P, omegan, delta, setNMfreq, *[_p(a) for a in A], _p(C))
+        self._check(rc, "nm_init")
+        return dict(A11=A[0], A12=A[1], A21=A[2], A22=A[3], omegalist=A[4], msf=A[5], C=C.reshape(P, P, order="F"))
+
+    def evolve_ring(self, RR, PP, mass):
+        RR, PP = _f64(RR).copy(), _f64(PP).copy()
+        self._check(load().pimd_evolve_ring(self.h, _p(RR), _p(PP), RR.shape[0], float(mass)), "evolve_ring")
+        return RR, PP
+
+    def langevin_init(self, delt2, centroid_thermostat, tau, temp_P):
+        rc = load().pimd_langevin_init(self.h, float(delt2), int(centroid_thermostat), float(tau), float(temp_P))
+        self._check(rc, "langevin_init")

@@ -1,0 +1,131 @@
+"""GPU parity: the CUDA engine, called through the C ABI, against the CPU FP64 oracle on the
+same seeded inputs. Tolerance for FP64 mode: 1e-10 relative (normwise: max |diff| over the
+array divided by max |oracle value|); neighbour lists bit-exact."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def small_case(pkg, model=3, nw=32, P=3, seed=None, **kw):
+    W = pkg.waterbox
+    name = "ttm3f_512x32" if model == 3 else "ttm21f_128x32"
+    c = W.make_config(name, nw=nw, P=P, seed=seed)
+    L = c["params"]["box"][0]
+    rc = min(9.0, L / 2 - 0.01)
+    p = dict(c["params"], rc=rc, rc1=0.8 * rc, alpha=3.5 / rc, nmax=8, polar_maxiter=30, polar_eps=0.0)
+    p.update(kw)
+    return c, p
+
+
+def compare_beads(got, ref, tol=RTOL):
+    assert rel(got["dRRt"], ref["dRRt"]) < tol
+    assert rel(got["Upott"], ref["Upott"]) < tol
+    assert rel(got["dip_momIt"], ref["dip_momIt"]) < tol
+    assert rel(got["dip_momEt"], ref["dip_momEt"]) < tol
+    assert rel(got["virialct"], ref["virialct"]) < 1e3 * tol
+    assert rel(got["virialt"], ref["virialt"]) < 1e3 * tol
+    assert rel(got["chg"], ref["chg"]) < tol
+
+
+@pytest.mark.parametrize("model", [3, 2])
+def test_full_bead_forces_small(pkg, orc, engine_lib, model):
+    c, p = small_case(pkg, model)
+    eng = pkg.ForceEngine(p)
+    got = eng.full_bead_forces(c["RRt"], c["RRc"], t=1)
+    ref = orc.full_bead_forces(p, c["RRt"], c["RRc"], t=1)
+    compare_beads(got, ref)
+    o = orc.Oracle(p)
+    for k in range(p["nbeads"]):
+        r = o.pot_ttm(c["RRt"][k], c["RRc"], bead=k)
+        e = eng.energies(k)
+        for key in ("Umon", "Uvdw", "Uelec", "Uind"):
+            assert abs(e[key] - r[key]) < RTOL * (abs(r["Umon"]) + abs(r["Uvdw"]) + abs(r["Uelec"]) + abs(r["Uind"]))
+        assert rel(eng.virial(k), r["virt"]) < 1e-8
+        assert e["niter"] == p["polar_maxiter"]
+
+
+def test_neighbour_list_bit_exact(pkg, orc, engine_lib):
+    c, p = small_case(pkg, 3, nw=128, P=2)
+    eng = pkg.ForceEngine(p)
+    eng.full_bead_forces(c["RRt"], c["RRc"])
+    o = orc.Oracle(p)
+    for k in range(2):
+        assert np.array_equal(eng.neighbors(k), o.neighbors(c["RRt"][k]))
+
+
+def test_dipole_convergence_same_iterations(pkg, orc, engine_lib):
+    """With a convergence threshold the engine stops at the same iteration as the oracle."""
+    c, p = small_case(pkg, 3, nw=64, P=2, polar_eps=1e-8, polar_maxiter=100)
+    eng = pkg.ForceEngine(p)
+    got = eng.full_bead_forces(c["RRt"], c["RRc"])
+    o = orc.Oracle(p)
+    for k in range(2):
+        r = o.pot_ttm(c["RRt"][k], c["RRc"], bead=k)
+        assert eng.energies(k)["niter"] == r["niter"]
+        assert rel(got["dRRt"][k], r["dRR"]) < RTOL
+
+
+def test_pot_ttm_dropin(pkg, orc, engine_lib):
+    """The per-bead drop-in with the reference's pot_ttm argument list."""
+    c, p = small_case(pkg, 3, nw=32, P=1)
+    eng = pkg.ForceEngine(p)
+    got = eng.pot_ttm(c["RRt"][0], c["RRc"], t=1)
+    ref = orc.Oracle(p).pot_ttm(c["RRt"][0], c["RRc"])
+    assert abs(got["En"] - ref["En"]) < RTOL * (abs(ref["Umon"]) + abs(ref["Uvdw"]) + abs(ref["Uelec"]) + abs(ref["Uind"]))
+    assert rel(got["dRR"], ref["dRR"]) < RTOL
+    assert rel(got["virt"], ref["virt"]) < 1e-8
+    assert abs(got["virialc"] - ref["virialc"]) < 1e-8 * np.abs(ref["virt"]).max()
+    assert rel(got["dip_momI"], ref["dip_momI"]) < RTOL
+    assert rel(got["chg"], ref["chg"]) < RTOL
+
+
+def test_predictor_history_per_bead(pkg, orc, engine_lib):
+    """guess_initdip: the 4-step predictor from each bead's own history (steps 1..6)."""
+    c, p = small_case(pkg, 3, nw=32, P=2, guess_initdip=1, polar_maxiter=6)
+    eng = pkg.ForceEngine(p)
+    o = orc.Oracle(p)
+    rng = np.random.default_rng(3)
+    for t in range(1, 7):
+        RRt = c["RRt"] + rng.normal(scale=0.002, size=c["RRt"].shape)
+        got = eng.full_bead_forces(RRt, c["RRc"], t=t)
+        for k in range(2):
+            r = o.pot_ttm(RRt[k], c["RRc"], t=t, bead=k)
+            assert rel(got["dRRt"][k], r["dRR"]) < RTOL
+
+
+def test_headline_size_two_beads(pkg, orc, engine_lib):
+    """TTM3-F 512 H2O, L = 24.86 A, Rc = 9 A, |n| <= 12: beads 0 and 31 of 32."""
+    c = pkg.waterbox.make_config("ttm3f_512x32")
+    p = dict(c["params"], polar_maxiter=12, polar_eps=0.0)
+    eng = pkg.ForceEngine(p)
+    assert eng.ewald_info()[1] == orc.Oracle(p).ewald_info()[1]
+    got = eng.full_bead_forces(c["RRt"], c["RRc"])
+    o = orc.Oracle(p)
+    for k in (0, 31):
+        r = o.pot_ttm(c["RRt"][k], c["RRc"], bead=k)
+        assert rel(got["dRRt"][k], r["dRR"]) < RTOL
+        assert abs(got["Upott"][k] - r["En"]) < RTOL * (abs(r["Umon"]) + abs(r["Uvdw"]) + abs(r["Uelec"]) + abs(r["Uind"]))
+
+
+def test_normal_modes_bit_exact(pkg, orc, engine_lib):
+    """InitNormalModes arrays and EvolveRing are bit-identical to the oracle."""
+    c, p = small_case(pkg, 3, nw=8, P=8)
+    eng = pkg.ForceEngine(p)
+    for P in (8, 5):
+        a = eng.nm_init(P, 1500.0, 2.5e-4)
+        b = orc.nm_init(P, 1500.0, 2.5e-4)
+        for key in ("A11", "A12", "A21", "A22", "omegalist", "msf", "C"):
+            assert np.array_equal(a[key], b[key]), key
+        rng = np.random.default_rng(P)
+        RR, PP = rng.normal(size=(P, 3)), rng.normal(size=(P, 3))
+        g = eng.evolve_ring(RR, PP, 1.008)
+        r = orc.evolve_ring(b, RR, PP, 1.008)
+        assert np.array_equal(g[0], r[0]) and np.array_equal(g[1], r[1])
