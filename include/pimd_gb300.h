@@ -103,6 +103,13 @@ int pimd_get_dipole_info(pimd_ctx *ctx, int bead, int *niter, double *deltadip);
  * ij[2*cap] and the total to *npairs. */
 int pimd_get_neighbors(pimd_ctx *ctx, int bead, int *ij, int cap, int *npairs);
 
+/* Named phase timers (the reference's dans_timer.f90 start_timer/stop_timer/
+ * print_timing_report), kept as CUDA events on the context's stream. reset clears the
+ * totals and switches recording on (enable != 0) or off. get returns the number of timers
+ * and, for 0 <= i < that number, timer i's name, total milliseconds and call count. */
+int pimd_timers_reset(pimd_ctx *ctx, int enable);
+int pimd_timers_get(pimd_ctx *ctx, int i, char *name, int namelen, double *ms, long long *count);
+
 /* Induced-dipole iteration control for batched calls: check convergence on the host every
  * `every` iterations (0 = run exactly polar_maxiter iterations with converged beads
  * skipped on the device, which needs no host synchronisation). Default 1. */
@@ -143,6 +150,16 @@ typedef struct {
 int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt,
                         double *dRRt, double *RRc, const double *xi1, const double *xi2, int t,
                         double *out4);
+/* The same step on host arrays (copied in and out every call): RRt, PPt, dRRt inout
+ * (3,Natoms,P), RRc out (3,Natoms), out4 host [Upot, virial, virialc, uk]; xi1/xi2 host
+ * standard normals (3,P,Natoms) or NULL for the device generator. */
+int pimd_md_step(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
+                 double *RRc, const double *xi1, const double *xi2, int t, double *out4);
+
+/* Measured CUDA-core FMA throughput of `device` in TFLOP/s (fp64 != 0: double, else float):
+ * the roofline denominator for kernels bound by the FP64 / FP32 pipes. No counterpart in the
+ * reference (which has no GPU path). */
+int pimd_peak_flops(int device, int fp64, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -97,6 +97,12 @@ def lib():
                                   ctypes.c_double, D, D]
         L.orc_pimd_vv_step.argtypes = [ctypes.c_void_p, ctypes.POINTER(MDParams), ctypes.c_int, D, D, D, D, D, D,
                                        ctypes.c_int, D, D, D, D]
+        L.orc_pool_create.restype = ctypes.c_void_p
+        L.orc_pool_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int]
+        L.orc_pool_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_pool_forces.argtypes = [ctypes.c_void_p, D, D, D, D, D, D, ctypes.c_int]
+        L.orc_pimd_vv_step_pool.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(MDParams),
+                                            ctypes.c_int, D, D, D, D, D, D, ctypes.c_int, D, D, D, D]
         _lib = L
     return _lib
 
@@ -246,8 +252,31 @@ def calc_uk(nm, massO, massH, PPt, setNMfreq=0.0):
     return lib().orc_calc_uk(P, na, massO, massH, _p(_f64(PPt)), setNMfreq, _p(C), _p(nm["msf"]))
 
 
-def pimd_vv_step(orc, md, RRt, PPt, dRRt, xi1=None, xi2=None, t=1):
-    """MD.f90:35-110 one velocity-Verlet PIMD step; arrays (P, Natoms, 3) updated in place."""
+class Pool:
+    """Host-core bead pool: bead k always on worker k % nthreads (an MPI rank per thread)."""
+
+    def __init__(self, params, nthreads=None):
+        self._p = make_params(params)
+        self.nthreads = int(nthreads or os.cpu_count() or 1)
+        self.h = lib().orc_pool_create(ctypes.byref(self._p), self.nthreads)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_pool_destroy(self.h)
+            self.h = None
+
+    def forces(self, RRt, RRc, t=1):
+        P = self._p.nbeads
+        RRt, RRc = _f64(RRt), _f64(RRc)
+        U, v, vc = np.zeros(P), np.zeros(P), np.zeros(P)
+        dRRt = np.zeros_like(RRt)
+        lib().orc_pool_forces(self.h, _p(RRt), _p(RRc), _p(U), _p(dRRt), _p(v), _p(vc), int(t))
+        return dict(Upott=U, dRRt=dRRt, virialt=v, virialct=vc)
+
+
+def pimd_vv_step(orc, md, RRt, PPt, dRRt, xi1=None, xi2=None, t=1, pool=None):
+    """MD.f90:35-110 one velocity-Verlet PIMD step; arrays (P, Natoms, 3) updated in place.
+    With a Pool the force call is spread over its worker threads."""
     mp = MDParams()
     mp.delt = md["delt"]
     mp.massO = md["massO"]
@@ -262,6 +291,7 @@ def pimd_vv_step(orc, md, RRt, PPt, dRRt, xi1=None, xi2=None, t=1):
     U, v, vc, uk = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
     x1 = _p(_f64(xi1)) if xi1 is not None else None
     x2 = _p(_f64(xi2)) if xi2 is not None else None
-    lib().orc_pimd_vv_step(orc.h, ctypes.byref(mp), P, _p(RRt), _p(PPt), _p(dRRt), _p(RRc), x1, x2, int(t),
-                           ctypes.byref(U), ctypes.byref(v), ctypes.byref(vc), ctypes.byref(uk))
+    lib().orc_pimd_vv_step_pool(orc.h, pool.h if pool is not None else None, ctypes.byref(mp), P, _p(RRt), _p(PPt),
+                                _p(dRRt), _p(RRc), x1, x2, int(t), ctypes.byref(U), ctypes.byref(v),
+                                ctypes.byref(vc), ctypes.byref(uk))
     return dict(Upot=U.value, virial=v.value, virialc=vc.value, uk=uk.value, RRc=RRc)

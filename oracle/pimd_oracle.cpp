@@ -1760,6 +1760,53 @@ void orc_full_bead_forces(const orc_params *p, int nthreads, const double *RRt, 
     for (auto &x : th) x.join();
 }
 
+// A persistent pool of oracle states, one per worker thread, bead k always on thread
+// k % nthreads, so each bead's predictor history lives across calls like an MPI rank's.
+struct OrcPool {
+    orc_params p;
+    int nthreads;
+    std::vector<Orc *> w;
+};
+
+void *orc_pool_create(const orc_params *p, int nthreads) {
+    OrcPool *pool = new OrcPool();
+    pool->p = *p;
+    pool->nthreads = std::max(1, std::min(nthreads, p->nbeads));
+    for (int i = 0; i < pool->nthreads; i++) pool->w.push_back(new Orc(p));
+    return pool;
+}
+
+void orc_pool_destroy(void *h) {
+    OrcPool *pool = static_cast<OrcPool *>(h);
+    for (Orc *o : pool->w) delete o;
+    delete pool;
+}
+
+void orc_pool_forces(void *h, const double *RRt, const double *RRc, double *Upott, double *dRRt, double *virialt,
+                     double *virialct, int t) {
+    OrcPool *pool = static_cast<OrcPool *>(h);
+    const int P = pool->p.nbeads, na = pool->p.natoms, nw = na / 3;
+    std::vector<std::thread> th;
+    for (int w = 0; w < pool->nthreads; w++) {
+        th.emplace_back([=]() {
+            Orc &o = *pool->w[w];
+            std::vector<double> dI(3 * nw), dE(3 * nw), chg(na);
+            for (int k = w; k < P; k += pool->nthreads) {
+                double virt[9];
+                if (o.polar)
+                    o.pot_ttm(k, RRt + (size_t)3 * na * k, RRc, &Upott[k], dRRt + (size_t)3 * na * k, virt, &virialct[k],
+                              dI.data(), dE.data(), chg.data(), t);
+                else {
+                    o.pot_spc(RRt + (size_t)3 * na * k, &Upott[k], dRRt + (size_t)3 * na * k, virt, dI.data(), chg.data());
+                    virialct[k] = 0.0;
+                }
+                virialt[k] = virt[0] + virt[4] + virt[8];
+            }
+        });
+    }
+    for (auto &x : th) x.join();
+}
+
 // NormalModes.f90:68-218
 void orc_nm_init(int P, double omegan, double delta, double setNMfreq, double *A11, double *A12,
                  double *A21, double *A22, double *omegalist, double *msf, double *C) {
@@ -1909,6 +1956,13 @@ double orc_calc_uk(int P, int natoms, double massO, double massH, const double *
 void orc_pimd_vv_step(void *h, const orc_md_params *mp, int P, double *RRt, double *PPt, double *dRRt,
                       double *RRc, const double *xi1, const double *xi2, int t, double *Upot,
                       double *virial, double *virialc, double *uk) {
+    orc_pimd_vv_step_pool(h, nullptr, mp, P, RRt, PPt, dRRt, RRc, xi1, xi2, t, Upot, virial, virialc, uk);
+}
+
+// As orc_pimd_vv_step with the force call spread over a thread pool (orc_pool_create).
+void orc_pimd_vv_step_pool(void *h, void *pool, const orc_md_params *mp, int P, double *RRt, double *PPt,
+                           double *dRRt, double *RRc, const double *xi1, const double *xi2, int t, double *Upot,
+                           double *virial, double *virialc, double *uk) {
     Orc *o = static_cast<Orc *>(h);
     int na = o->Natoms, nw = na / 3;
     double delt2 = mp->delt / 2.0;
@@ -1957,19 +2011,29 @@ void orc_pimd_vv_step(void *h, const orc_md_params *mp, int P, double *RRt, doub
         for (int j = 0; j < P; j++) RRt[i + (size_t)3 * na * j] = RRt[i + (size_t)3 * na * j] - shift;
     }
     double U = 0, vir = 0, virc = 0;
-    std::vector<double> dipI(3 * nw), dipE(3 * nw), chg(na);
-    for (int k = 0; k < P; k++) {
-        double En, virt[9], vc;
-        if (o->polar)
-            o->pot_ttm(k, RRt + (size_t)3 * na * k, RRc, &En, dRRt + (size_t)3 * na * k, virt, &vc, dipI.data(),
-                       dipE.data(), chg.data(), t);
-        else {
-            o->pot_spc(RRt + (size_t)3 * na * k, &En, dRRt + (size_t)3 * na * k, virt, dipI.data(), chg.data());
-            vc = 0.0;
+    if (pool) {
+        std::vector<double> Upott(P), virialt(P), virialct(P);
+        orc_pool_forces(pool, RRt, RRc, Upott.data(), dRRt, virialt.data(), virialct.data(), t);
+        for (int k = 0; k < P; k++) {
+            U += Upott[k];
+            vir += virialt[k];
+            virc += virialct[k];
         }
-        U += En;
-        vir += virt[0] + virt[4] + virt[8];
-        virc += vc;
+    } else {
+        std::vector<double> dipI(3 * nw), dipE(3 * nw), chg(na);
+        for (int k = 0; k < P; k++) {
+            double En, virt[9], vc;
+            if (o->polar)
+                o->pot_ttm(k, RRt + (size_t)3 * na * k, RRc, &En, dRRt + (size_t)3 * na * k, virt, &vc, dipI.data(),
+                           dipE.data(), chg.data(), t);
+            else {
+                o->pot_spc(RRt + (size_t)3 * na * k, &En, dRRt + (size_t)3 * na * k, virt, dipI.data(), chg.data());
+                vc = 0.0;
+            }
+            U += En;
+            vir += virt[0] + virt[4] + virt[8];
+            virc += vc;
+        }
     }
     *Upot = U;
     *virial = vir;

@@ -99,6 +99,18 @@ void orc_pimd_vv_step(void *h, const orc_md_params *mp, int P, double *RRt, doub
                       double *dRRt, double *RRc, const double *xi1, const double *xi2, int t,
                       double *Upot, double *virial, double *virialc, double *uk);
 
+/* A pool of nthreads oracle states; bead k is always evaluated by thread k % nthreads, so
+ * the per-bead predictor history persists across calls (the MPI-over-beads analogue of
+ * force_calc.f90:26-106 on the host cores). */
+void *orc_pool_create(const orc_params *p, int nthreads);
+void orc_pool_destroy(void *pool);
+void orc_pool_forces(void *pool, const double *RRt, const double *RRc, double *Upott, double *dRRt,
+                     double *virialt, double *virialct, int t);
+void orc_pimd_vv_step_pool(void *h, void *pool, const orc_md_params *mp, int P, double *RRt,
+                           double *PPt, double *dRRt, double *RRc, const double *xi1,
+                           const double *xi2, int t, double *Upot, double *virial,
+                           double *virialc, double *uk);
+
 #ifdef __cplusplus
 }
 #endif

@@ -274,25 +274,87 @@ static int create(Engine &E, const pimd_params *p) {
     return cuda_check(E, cudaDeviceSynchronize(), "init");
 }
 
+// ---------------------------------------------------------------------------------------
+// Phase timers: a pair of events around each named phase on the engine stream.
+static int timer_slot(PhaseTimers &T, const char *name) {
+    for (size_t i = 0; i < T.names.size(); i++)
+        if (T.names[i] == name) return (int)i;
+    T.names.push_back(name);
+    T.ms.push_back(0.0);
+    T.count.push_back(0);
+    return (int)T.names.size() - 1;
+}
+
+static cudaEvent_t timer_event(PhaseTimers &T) {
+    if (!T.pool.empty()) {
+        cudaEvent_t e = T.pool.back();
+        T.pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+static void timer_resolve(Engine &E) {
+    PhaseTimers &T = E.timers;
+    if (T.pending.empty()) return;
+    cudaEventSynchronize(T.pending.back().second.second);
+    for (auto &p : T.pending) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+        T.ms[p.first] += ms;
+        T.count[p.first] += 1;
+        T.pool.push_back(p.second.first);
+        T.pool.push_back(p.second.second);
+    }
+    T.pending.clear();
+}
+
+void timer_begin(Engine &E, const char *name) {
+    PhaseTimers &T = E.timers;
+    if (!T.on) return;
+    if (T.pending.size() > 8192) timer_resolve(E);
+    T.cur = timer_slot(T, name);
+    T.cur0 = timer_event(T);
+    cudaEventRecord(T.cur0, E.stream);
+}
+
+void timer_end(Engine &E) {
+    PhaseTimers &T = E.timers;
+    if (!T.on || T.cur < 0) return;
+    cudaEvent_t e1 = timer_event(T);
+    cudaEventRecord(e1, E.stream);
+    T.pending.push_back({T.cur, {T.cur0, e1}});
+    T.cur = -1;
+}
+
+#define PHASE(name, call) \
+    do {                  \
+        timer_begin(E, name); \
+        call;             \
+        timer_end(E);     \
+    } while (0)
+
 // One force call for all beads of the context (pot_ttm.f90:3-630 per bead).
 int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt, double *virialct, double *virt9) {
     KP &kp = E.kp;
     kp.t = t;
     cudaMemsetAsync(kp.acc, 0, sizeof(double) * kp.P * NACC, E.stream);
     cudaMemsetAsync(kp.err, 0, sizeof(unsigned), E.stream);
-    launch_sites(E);
-    launch_neighbors(E);
-    launch_pair_qq(E);
-    launch_ewald_tables(E);
-    launch_ewald_sq(E);
-    launch_ewald_fq(E);
-    launch_after_qq(E);
+    PHASE("sites", launch_sites(E));
+    PHASE("neighbors", launch_neighbors(E));
+    PHASE("pair_qq", launch_pair_qq(E));
+    PHASE("ewald_tables", launch_ewald_tables(E));
+    PHASE("ewald_sq", launch_ewald_sq(E));
+    PHASE("ewald_fq", launch_ewald_fq(E));
+    PHASE("after_qq", launch_after_qq(E));
     int iter = 1;
     for (; iter <= kp.polar_maxiter; iter++) {
-        launch_dd_real(E);
-        launch_ewald_smu(E);
-        launch_dd_update(E, iter);
-        launch_dd_check(E, iter);
+        PHASE("dd_real", launch_dd_real(E));
+        PHASE("dd_smu", launch_ewald_smu(E));
+        PHASE("dd_update", launch_dd_update(E, iter));
+        PHASE("dd_check", launch_dd_check(E, iter));
         if (check_every > 0 && (iter % check_every) == 0 && iter < kp.polar_maxiter) {
             cudaMemcpyAsync(E.h_allconv, kp.allconv, sizeof(int), cudaMemcpyDeviceToHost, E.stream);
             cudaError_t e = cudaStreamSynchronize(E.stream);
@@ -301,10 +363,10 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
         }
     }
     E.last_niter_max = std::min(iter, kp.polar_maxiter);
-    launch_pair_force(E);
-    launch_ewald_qd(E);
-    launch_finish(E);
-    launch_totals(E, Upott, virialt, virialct, virt9);
+    PHASE("pair_force", launch_pair_force(E));
+    PHASE("ewald_qd", launch_ewald_qd(E));
+    PHASE("finish", launch_finish(E));
+    PHASE("totals", launch_totals(E, Upott, virialt, virialct, virt9));
     return cuda_check(E, cudaGetLastError(), "force kernels");
 }
 
@@ -344,6 +406,13 @@ int pimd_destroy(pimd_ctx *ctx) {
     cudaSetDevice(E.device);
     if (E.stream) cudaStreamSynchronize(E.stream);
     for (void *p : E.allocs) cudaFree(p);
+    if (E.d_nmC) cudaFree(E.d_nmC);
+    if (E.d_nmA) cudaFree(E.d_nmA);
+    for (cudaEvent_t e : E.timers.pool) cudaEventDestroy(e);
+    for (auto &pe : E.timers.pending) {
+        cudaEventDestroy(pe.second.first);
+        cudaEventDestroy(pe.second.second);
+    }
     if (E.h_allconv) cudaFreeHost(E.h_allconv);
     if (E.h_pin) cudaFreeHost(E.h_pin);
     if (E.own_stream && E.stream) cudaStreamDestroy(E.stream);
@@ -500,6 +569,34 @@ int pimd_get_virial(pimd_ctx *ctx, int bead, double virt[9]) {
     virt[4] -= E.kp.Uvdw_lrc;
     virt[8] -= E.kp.Uvdw_lrc;
     return PIMD_OK;
+}
+
+int pimd_timers_reset(pimd_ctx *ctx, int enable) {
+    if (!ctx) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    timer_resolve(E);
+    PhaseTimers &T = E.timers;
+    for (size_t i = 0; i < T.ms.size(); i++) {
+        T.ms[i] = 0.0;
+        T.count[i] = 0;
+    }
+    T.on = enable != 0;
+    return PIMD_OK;
+}
+
+int pimd_timers_get(pimd_ctx *ctx, int i, char *name, int namelen, double *ms, long long *count) {
+    if (!ctx) return -1;
+    Engine &E = ctx->E;
+    timer_resolve(E);
+    PhaseTimers &T = E.timers;
+    if (i < 0 || i >= (int)T.names.size()) return (int)T.names.size();
+    if (name && namelen > 0) {
+        std::strncpy(name, T.names[i].c_str(), namelen - 1);
+        name[namelen - 1] = 0;
+    }
+    if (ms) *ms = T.ms[i];
+    if (count) *count = T.count[i];
+    return (int)T.names.size();
 }
 
 int pimd_get_neighbors(pimd_ctx *ctx, int bead, int *ij, int cap, int *npairs) {

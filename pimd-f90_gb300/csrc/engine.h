@@ -83,8 +83,22 @@ struct KP {
     int *allconv;
 };
 
+// Named phase timers (the reference's dans_timer.f90 start_timer/stop_timer), recorded as
+// CUDA events on the engine stream and resolved lazily.
+struct PhaseTimers {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    std::vector<std::string> names;
+    std::vector<double> ms;
+    std::vector<long> count;
+    cudaEvent_t cur0 = nullptr;
+    int cur = -1;
+};
+
 struct Engine {
     KP kp;
+    PhaseTimers timers;
     int precision = 0;
     int device = 0;
     cudaStream_t stream = 0;
@@ -100,6 +114,7 @@ struct Engine {
     size_t h_pin_bytes = 0;
     int *h_allconv = nullptr;
     double *d_out = nullptr;  // small device staging for per-bead scalar outputs
+    double *d_md = nullptr;   // device MD state for the host-array step (pimd_md_step)
     std::vector<void *> allocs;
     std::string last_error;
     int last_niter_max = 0;
@@ -108,6 +123,11 @@ struct Engine {
     double *d_nmC = nullptr, *d_nmA = nullptr;  // C(P,P), [A11,A12,A21,A22,msf,c1,c2] x P
     std::vector<double> h_nm;                     // host copy: A11..A22, omegalist, msf, C
 };
+
+// phase timers (capi.cu)
+void timer_begin(Engine &E, const char *name);
+void timer_end(Engine &E);
+int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt, double *virialct, double *virt9);
 
 // launchers (pot.cu)
 void pot_init_constants(Engine &E);

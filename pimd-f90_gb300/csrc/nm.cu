@@ -242,7 +242,7 @@ __global__ void k_md_sum(int P, const double *Upott, const double *virialt, cons
 static void nm_launch_shape(int P, int natoms, int *threads, int *blocks, size_t *smem) {
     int G = 256 / (3 * P);
     if (G < 1) G = 1;
-    *threads = G * 3 * P;
+    *threads = ((G * 3 * P + 31) / 32) * 32;  // whole warps (the KE reduction shuffles)
     *blocks = (natoms + G - 1) / G;
     *smem = sizeof(double) * ((size_t)P * P + (size_t)G * 9 * P);
 }
@@ -449,7 +449,9 @@ int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, do
     int threads, blocks;
     size_t smem;
     nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
+    timer_begin(E, "md_pre");
     k_md_pre<<<blocks, threads, smem, E.stream>>>(a, RRt, PPt, dRRt, RRc);
+    timer_end(E);
     KP saved = E.kp;
     E.kp.RRt = RRt;
     E.kp.RRc = RRc;
@@ -464,9 +466,38 @@ int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, do
     cudaMemsetAsync(uk, 0, sizeof(double), E.stream);
     a.xi = xi2;
     a.counter = 2ull * (unsigned long long)t + 1ull;
+    timer_begin(E, "md_post");
     k_md_post<<<blocks, threads, smem, E.stream>>>(a, PPt, dRRt, uk);
     if (out4) k_md_sum<<<1, 32, 0, E.stream>>>(E.kp.P, d, d + E.kp.P, d + 2 * E.kp.P, uk, out4);
+    timer_end(E);
     return nm_err(E, cudaGetLastError(), "md_step");
+}
+
+int pimd_md_step(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,
+                 const double *xi1, const double *xi2, int t, double *out4) {
+    if (!ctx || !mp || !RRt || !PPt || !dRRt) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    cudaSetDevice(E.device);
+    const size_t n = (size_t)E.kp.P * E.kp.natoms * 3, nc = (size_t)E.kp.natoms * 3;
+    if (!E.d_md) {
+        // device copies of the MD state: RRt, PPt, dRRt, RRc, xi1, xi2, out4
+        if (cudaMalloc((void **)&E.d_md, sizeof(double) * (5 * n + nc + 8)) != cudaSuccess) return PIMD_ERR_NOMEM;
+        E.allocs.push_back(E.d_md);
+    }
+    double *dR = E.d_md, *dP = dR + n, *dG = dP + n, *dx1 = dG + n, *dx2 = dx1 + n, *dC = dx2 + n, *dO = dC + nc;
+    cudaMemcpyAsync(dR, RRt, sizeof(double) * n, cudaMemcpyHostToDevice, E.stream);
+    cudaMemcpyAsync(dP, PPt, sizeof(double) * n, cudaMemcpyHostToDevice, E.stream);
+    cudaMemcpyAsync(dG, dRRt, sizeof(double) * n, cudaMemcpyHostToDevice, E.stream);
+    if (xi1) cudaMemcpyAsync(dx1, xi1, sizeof(double) * n, cudaMemcpyHostToDevice, E.stream);
+    if (xi2) cudaMemcpyAsync(dx2, xi2, sizeof(double) * n, cudaMemcpyHostToDevice, E.stream);
+    int rc = pimd_md_step_device(ctx, mp, dR, dP, dG, dC, xi1 ? dx1 : nullptr, xi2 ? dx2 : nullptr, t, dO);
+    if (rc) return rc;
+    cudaMemcpyAsync(RRt, dR, sizeof(double) * n, cudaMemcpyDeviceToHost, E.stream);
+    cudaMemcpyAsync(PPt, dP, sizeof(double) * n, cudaMemcpyDeviceToHost, E.stream);
+    cudaMemcpyAsync(dRRt, dG, sizeof(double) * n, cudaMemcpyDeviceToHost, E.stream);
+    if (RRc) cudaMemcpyAsync(RRc, dC, sizeof(double) * nc, cudaMemcpyDeviceToHost, E.stream);
+    if (out4) cudaMemcpyAsync(out4, dO, sizeof(double) * 4, cudaMemcpyDeviceToHost, E.stream);
+    return nm_err(E, cudaStreamSynchronize(E.stream), "md_step");
 }
 
 }  // extern "C"

@@ -68,6 +68,10 @@ SIGNATURES = {
     "pimd_langevin_nm_device": [_V, _V, _V, ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong,
                                 ctypes.c_ulonglong],
     "pimd_md_step_device": [_V, ctypes.POINTER(MDParams), _V, _V, _V, _V, _V, _V, ctypes.c_int, _V],
+    "pimd_md_step": [_V, ctypes.POINTER(MDParams), _D, _D, _D, _D, _D, _D, ctypes.c_int, _D],
+    "pimd_peak_flops": [ctypes.c_int, ctypes.c_int, _D],
+    "pimd_timers_reset": [_V, ctypes.c_int],
+    "pimd_timers_get": [_V, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, _D, ctypes.POINTER(ctypes.c_longlong)],
 }
 
 _lib = None
@@ -226,3 +230,52 @@ class ForceEngine:
     def langevin_init(self, delt2, centroid_thermostat, tau, temp_P):
         rc = load().pimd_langevin_init(self.h, float(delt2), int(centroid_thermostat), float(tau), float(temp_P))
         self._check(rc, "langevin_init")
+
+    # ---- MD.f90 PIMD_VV --------------------------------------------------------------
+    @staticmethod
+    def md_params(delt, massO, massH, langevin=1, seed=12345):
+        mp = MDParams()
+        mp.delt = float(delt)
+        mp.massO = float(massO)
+        mp.massH = float(massH)
+        mp.langevin = int(langevin)
+        mp.seed = int(seed)
+        return mp
+
+    def md_step(self, mp, RRt, PPt, dRRt, t, xi1=None, xi2=None):
+        """One PIMD_VV step on host arrays (updated in place); returns (Upot, virial, virialc, uk), RRc."""
+        for a in (RRt, PPt, dRRt):
+            assert a.dtype == np.float64 and a.flags.c_contiguous
+        RRc = np.zeros((self.natoms, 3))
+        out = np.zeros(4)
+        x1 = _f64(xi1) if xi1 is not None else None
+        x2 = _f64(xi2) if xi2 is not None else None
+        rc = load().pimd_md_step(self.h, ctypes.byref(mp), _p(RRt), _p(PPt), _p(dRRt), _p(RRc), _p(x1), _p(x2),
+                                 int(t), _p(out))
+        self._check(rc, "md_step")
+        return out, RRc
+
+    def md_step_device(self, mp, RRt, PPt, dRRt, RRc, t, out4, xi1=0, xi2=0):
+        """PIMD_VV on device buffers given as raw pointers (ints), stream-ordered."""
+        rc = load().pimd_md_step_device(self.h, ctypes.byref(mp), RRt, PPt, dRRt, RRc, xi1 or None, xi2 or None,
+                                        int(t), out4)
+        self._check(rc, "md_step_device")
+
+    def set_stream(self, stream_ptr):
+        self._check(load().pimd_set_stream(self.h, stream_ptr), "set_stream")
+
+    # ---- dans_timer-style phase timers ----------------------------------------------------
+    def timers_reset(self, enable=True):
+        self._check(load().pimd_timers_reset(self.h, int(enable)), "timers_reset")
+
+    def timers(self):
+        L = load()
+        n = L.pimd_timers_get(self.h, -1, None, 0, None, None)
+        out = {}
+        buf = ctypes.create_string_buffer(64)
+        for i in range(n):
+            ms = ctypes.c_double()
+            cnt = ctypes.c_longlong()
+            L.pimd_timers_get(self.h, i, buf, 64, ctypes.byref(ms), ctypes.byref(cnt))
+            out[buf.value.decode()] = (ms.value, cnt.value)
+        return out
