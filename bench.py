@@ -1,0 +1,295 @@
+#!/usr/bin/env python3
+"""Benchmark: full PIMD velocity-Verlet MD steps per second for TTM3-F water, 512 H2O x 32
+beads (L = 24.86 A, Rc = 9 A, Ewald |n| <= 12, T = 300 K, dt = 0.25 fs, PILE thermostat),
+on synthetic jittered-lattice boxes (seeded; the reference ships no benchmark dataset).
+
+One step = Langevin_NM, half kick, EvolveRing for every atom, centroid + PBCs, the force
+call for all 32 beads (monomer PES, real-space charge/dipole sums, Ewald reciprocal sums,
+induced-dipole solve to 1e-8 with the 4-step predictor), half kick, Langevin_NM
+(MD.f90:35-110).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm times the CUDA engine through its C ABI with the MD state resident in HBM (value)
+and again through the host-array entry point with host<->device copies every step (e2e).
+The reference arm times the reference algorithm (CPU FP64 restatement, threads over beads
+like the reference's MPI ranks) on this machine's host cores. Multi-GPU runs are
+independent replicas, one per rank (the path has no cross-replica exchange).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as ge  # noqa: E402
+
+METRIC = "TTM3-F 512 H2O×32 beads: MD steps/s mixed vs FP64 GPU at ≤1e-4 rel force err"
+CONFIG = "ttm3f_512x32"
+DT_FS = 0.25
+TEMP = 300.0
+POLAR = dict(polar_eps=1e-8, polar_maxiter=100, guess_initdip=1, polar_sor=0.7)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default=CONFIG)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(pkg, name):
+    c = pkg.waterbox.make_config(name)
+    p = dict(c["params"])
+    p.update(POLAR)
+    return c, p
+
+
+def flops_ewald_dd(nk, ndip, P):
+    """Algorithmic flops of one ewald_std_dd call for P beads (ewald.f90:56-119): 22 per
+    (k-vector, dipole site), the per-unit count of the reference's loop body."""
+    return 22.0 * nk * ndip * P
+
+
+# ---------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for ln in fh:
+                parts = [x.strip() for x in ln.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------------------
+def run_gpu_arm(args, pkg, rank, world, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    c, p = workload(pkg, args.config)
+    P, na, nw = p["nbeads"], p["natoms"], p["natoms"] // 3
+    stream = torch.cuda.current_stream(dev)
+    eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_FP64, device=local)
+    eng.set_stream(stream.cuda_stream)
+    alpha, nk, _ = eng.ewald_info()
+    delt = DT_FS / 1000.0
+    omegan = pkg.waterbox.KB_AMU * TEMP * P / pkg.waterbox.HBAR
+    eng.nm_init(P, omegan, delt)
+    eng.langevin_init(delt / 2, 0, 0.1, P * TEMP)
+    mp = eng.md_params(delt, c["massO"], c["massH"], langevin=1, seed=20261203 + rank)
+    # device-resident MD state
+    RRt = torch.from_numpy(c["RRt"]).to(dev)
+    PPt = torch.from_numpy(c["PPt"]).to(dev)
+    dRRt = torch.zeros_like(RRt)
+    RRc = torch.zeros((na, 3), dtype=torch.float64, device=dev)
+    out4 = torch.zeros(4, dtype=torch.float64, device=dev)
+    RRc.copy_(RRt.mean(0))
+    pkg.engine.load().pimd_full_bead_forces_device(eng.h, RRt.data_ptr(), RRc.data_ptr(), None, dRRt.data_ptr(),
+                                                   None, None, None, None, None, 1)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    t = 1
+    for _ in range(args.warmup):
+        eng.md_step_device(mp, RRt.data_ptr(), PPt.data_ptr(), dRRt.data_ptr(), RRc.data_ptr(), t, out4.data_ptr())
+        t += 1
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    eng.timers_reset(True)
+    L = pkg.engine.load()
+    launches0 = L.pimd_launch_count(eng.h)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    niters = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize(dev)
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            ev[k][0].record(stream)
+            eng.md_step_device(mp, RRt.data_ptr(), PPt.data_ptr(), dRRt.data_ptr(), RRc.data_ptr(), t, out4.data_ptr())
+            ev[k][1].record(stream)
+            niters.append(eng.energies(0)["niter"])
+            t += 1
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - wall0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    launches = L.pimd_launch_count(eng.h) - launches0
+    timers = eng.timers()
+    eng.timers_reset(False)
+    dev_ms = sum(step_ms)
+    if world > 1:
+        tt = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        dev_ms = float(tt.item())
+    out = out4.cpu().numpy()
+    # e2e: the host-array C-ABI step, copies in and out every step
+    hR, hP, hG = RRt.cpu().numpy().copy(), PPt.cpu().numpy().copy(), dRRt.cpu().numpy().copy()
+    e2e_steps = max(3, args.steps // 2)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        eng.md_step(mp, hR, hP, hG, t)
+        t += 1
+    e2e_s = time.perf_counter() - t0
+    res = dict(dev_ms=dev_ms, step_ms=step_ms, wall=wall, timers=timers, niters=niters, clocks=clk.summary(),
+               launches=launches,
+               out=out.tolist(), nk=nk, alpha=alpha, P=P, nw=nw, e2e_s=e2e_s, e2e_steps=e2e_steps,
+               h2d=3 * hR.nbytes, d2h=3 * hR.nbytes + 4 * 8 + hR.shape[1] * 24)
+    eng.close()
+    return res
+
+
+def cpu_baseline(pkg, orc, steps):
+    """Reference algorithm (CPU FP64 restatement) on all host cores: bead pool threads."""
+    c, p = workload(pkg, CONFIG)
+    ncores = os.cpu_count() or 1
+    pool = orc.Pool(p, nthreads=ncores)
+    o = orc.Oracle(p)
+    md = dict(delt=DT_FS / 1000.0, massO=c["massO"], massH=c["massH"], temp=TEMP, langevin=1)
+    RRt, PPt = c["RRt"].copy(), c["PPt"].copy()
+    dRRt = np.zeros_like(RRt)
+    rng = np.random.default_rng(1)
+    P, na = RRt.shape[0], RRt.shape[1]
+    ts = []
+    for k in range(steps):
+        xi1, xi2 = rng.standard_normal((na, P, 3)), rng.standard_normal((na, P, 3))
+        t0 = time.perf_counter()
+        orc.pimd_vv_step(o, md, RRt, PPt, dRRt, xi1, xi2, t=k + 1, pool=pool)
+        ts.append(time.perf_counter() - t0)
+    # the first step has no predictor history and a zero gradient for the first kick
+    timed = ts[1:] if len(ts) > 1 else ts
+    return dict(value=len(timed) / sum(timed), cores=ncores, step_s=ts)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pkg = ge.load_package()
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        orc = ge.load_oracle()
+        orc.build()
+        steps = max(1, args.steps) + 1
+        r = cpu_baseline(pkg, orc, steps)
+        line = dict(metric=METRIC, value=r["value"], unit="steps/s", n_gpus=args.gpus, steps=steps - 1,
+                    warmup=1, ms_per_step=1000.0 / r["value"], higher_is_better=True, scaling="weak",
+                    vs_baseline=None, dtype="f64", data="synthetic", impl="reference",
+                    config=dict(workload=CONFIG + " (TTM3-F, 512 H2O x 32 beads, L=24.86 A, Rc=9 A, |n|<=12)",
+                                polar_eps=POLAR["polar_eps"], dt_fs=DT_FS),
+                    cpu_baseline=dict(value=r["value"], unit="steps/s", cores=r["cores"], kind="port",
+                                      sample="%d MD steps of 512 H2O x 32 beads (first excluded)" % (steps - 1)),
+                    e2e=dict(value=r["value"], unit="steps/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+        print(json.dumps(line))
+        return 0
+
+    pkg.build_lib.build()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", rank=rank, world_size=world)
+    res = run_gpu_arm(args, pkg, rank, world, local)
+    if rank != 0:
+        return 0
+    steps_total = args.steps * world
+    value = steps_total / (res["dev_ms"] / 1000.0)
+    ms_per_step = res["dev_ms"] / args.steps
+    timers = res["timers"]
+    # dominant phase and the ewald_std_dd roofline (dd_smu + dd_update implement ewald_std_dd)
+    phases = sorted(timers.items(), key=lambda kv: -kv[1][0])
+    dd_ms = timers.get("dd_smu", (0, 0))[0] + timers.get("dd_update", (0, 0))[0]
+    dd_calls = timers.get("dd_update", (0, 1))[1]
+    L = pkg.engine.load()
+    import ctypes
+
+    pk = ctypes.c_double()
+    L.pimd_peak_flops(0, 1, ctypes.byref(pk))
+    peak64 = pk.value
+    ach = flops_ewald_dd(res["nk"], res["nw"], res["P"]) * dd_calls / (dd_ms / 1000.0) / 1e12 if dd_ms else None
+    cpu = None
+    if not args.no_cpu_baseline:
+        orc = ge.load_oracle()
+        orc.build()
+        r = cpu_baseline(pkg, orc, args.cpu_steps + 1)
+        cpu = dict(value=r["value"], unit="steps/s", cores=r["cores"], kind="port",
+                   sample="%d MD steps of 512 H2O x 32 beads on the host cores (first step excluded)" % args.cpu_steps)
+    line = dict(
+        metric=METRIC, value=value, unit="steps/s", n_gpus=world, steps=args.steps, warmup=args.warmup,
+        ms_per_step=ms_per_step, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64",
+        data="synthetic (seeded jittered-lattice water boxes with free ring-polymer beads)",
+        config=dict(workload=CONFIG + " (TTM3-F, 512 H2O x 32 beads, L=24.86 A, Rc=9 A, |n|<=12, %d k-vectors)" % res["nk"],
+                    precision="fp64", polar_eps=POLAR["polar_eps"], predictor=True, dt_fs=DT_FS,
+                    l2="256 MB buffer written between timed steps", parallelism="replicas" if world > 1 else "1 GPU",
+                    dipole_iterations_mean=float(np.mean(res["niters"]))),
+        e2e=dict(value=res["e2e_steps"] / res["e2e_s"], unit="steps/s", h2d_bytes_per_step=res["h2d"],
+                 d2h_bytes_per_step=res["d2h"]),
+        roofline=dict(kernel="ewald_std_dd (k_spass<MU> + k_sreduce + k_field<D>)", bound="fp64-pipe",
+                      achieved=ach, peak=peak64, unit="TFLOP/s", frac=(ach / peak64) if ach else None, traffic=None,
+                      peak_source="measured in-run: FP64 FMA-throughput kernel (MEASURED_PEAKS.json has no FP64 figure)"),
+        cpu_baseline=cpu,
+        clocks=res["clocks"],
+        gpu_launches=res["launches"],
+        phases_ms={k: round(v[0] / args.steps, 4) for k, v in phases},
+        phase_calls={k: v[1] for k, v in phases},
+        dominant_phase=phases[0][0] if phases else None,
+        energy=dict(Upot=res["out"][0], virial=res["out"][1], virialc=res["out"][2], uk=res["out"][3]),
+    )
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

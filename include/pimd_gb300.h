@@ -108,6 +108,8 @@ int pimd_get_neighbors(pimd_ctx *ctx, int bead, int *ij, int cap, int *npairs);
  * totals and switches recording on (enable != 0) or off. get returns the number of timers
  * and, for 0 <= i < that number, timer i's name, total milliseconds and call count. */
 int pimd_timers_reset(pimd_ctx *ctx, int enable);
+/* Number of CUDA kernels this context has launched so far. */
+long long pimd_launch_count(pimd_ctx *ctx);
 int pimd_timers_get(pimd_ctx *ctx, int i, char *name, int namelen, double *ms, long long *count);
 
 /* Induced-dipole iteration control for batched calls: check convergence on the host every

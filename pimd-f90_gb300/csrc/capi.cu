@@ -571,6 +571,8 @@ int pimd_get_virial(pimd_ctx *ctx, int bead, double virt[9]) {
     return PIMD_OK;
 }
 
+long long pimd_launch_count(pimd_ctx *ctx) { return ctx ? ctx->E.nlaunch : -1; }
+
 int pimd_timers_reset(pimd_ctx *ctx, int enable) {
     if (!ctx) return PIMD_ERR_ARG;
     Engine &E = ctx->E;

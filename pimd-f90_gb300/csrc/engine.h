@@ -118,6 +118,7 @@ struct Engine {
     std::vector<void *> allocs;
     std::string last_error;
     int last_niter_max = 0;
+    long long nlaunch = 0;  // kernels launched by this context
     // normal modes (filled by pimd_nm_init)
     int nm_P = 0;
     double *d_nmC = nullptr, *d_nmA = nullptr;  // C(P,P), [A11,A12,A21,A22,msf,c1,c2] x P

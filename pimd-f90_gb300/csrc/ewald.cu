@@ -409,9 +409,9 @@ static void run_spass(Engine &E, int s0, int nsites, int skipconv) {
         attr_set[OP] = true;
     }
     dim3 g(E.nchunk, ngr, E.kp.P);
-    k_spass<OP><<<g, SP_NT, smem, E.stream>>>(E.kp, s0, nsites, tsg, ngr, skipconv);
+    k_spass<OP><<<g, SP_NT, smem, E.stream>>>(E.kp, s0, nsites, tsg, ngr, skipconv); ++E.nlaunch;
     dim3 g2((E.kp.nk + 255) / 256, E.kp.P);
-    k_sreduce<OP><<<g2, 256, 0, E.stream>>>(E.kp, ngr, skipconv);
+    k_sreduce<OP><<<g2, 256, 0, E.stream>>>(E.kp, ngr, skipconv); ++E.nlaunch;
 }
 
 template <int MODE>
@@ -427,7 +427,7 @@ static void run_field(Engine &E, int s0, int s1, int iter) {
             set = true;
         }
         dim3 g((s1 - s0 + NT - 1) / NT, E.kp.P);
-        k_field<MODE, NT><<<g, NT, smem, E.stream>>>(E.kp, s0, s1, iter);
+        k_field<MODE, NT><<<g, NT, smem, E.stream>>>(E.kp, s0, s1, iter); ++E.nlaunch;
     } else {
         constexpr int NT = 64;
         const size_t smem = (size_t)LZ * NT * 16 + base;
@@ -437,13 +437,13 @@ static void run_field(Engine &E, int s0, int s1, int iter) {
             set = true;
         }
         dim3 g((s1 - s0 + NT - 1) / NT, E.kp.P);
-        k_field<MODE, NT><<<g, NT, smem, E.stream>>>(E.kp, s0, s1, iter);
+        k_field<MODE, NT><<<g, NT, smem, E.stream>>>(E.kp, s0, s1, iter); ++E.nlaunch;
     }
 }
 
 void launch_ewald_tables(Engine &E) {
     dim3 g((E.kp.S + 127) / 128, E.kp.P);
-    k_ewald_tables<<<g, 128, 0, E.stream>>>(E.kp);
+    k_ewald_tables<<<g, 128, 0, E.stream>>>(E.kp); ++E.nlaunch;
 }
 
 // ewald_std_qq: S(k) over the charged sites, then the field at the sites that need it
@@ -464,7 +464,7 @@ void launch_dd_update(Engine &E, int iter) { run_field<F_D>(E, E.kp.fd, E.kp.ld,
 void launch_ewald_qd(Engine &E) {
     run_spass<OP_DIP>(E, E.kp.fd, E.kp.ld - E.kp.fd, 0);
     dim3 g((E.kp.nk + 127) / 128, E.kp.P);
-    k_qd_virial<<<g, 128, 0, E.stream>>>(E.kp);
+    k_qd_virial<<<g, 128, 0, E.stream>>>(E.kp); ++E.nlaunch;
     const int s0 = (E.kp.model == 2) ? 0 : E.kp.N;
     run_field<F_QD>(E, s0, E.kp.S, 0);
 }

@@ -397,7 +397,7 @@ int pimd_evolve_ring(pimd_ctx *ctx, double *RR, double *PP, int P, double mass) 
     int threads, blocks;
     size_t smem;
     nm_launch_shape(P, 1, &threads, &blocks, &smem);
-    k_evolve<<<blocks, threads, smem, E.stream>>>(a, d, d + 3 * P);
+    k_evolve<<<blocks, threads, smem, E.stream>>>(a, d, d + 3 * P); ++E.nlaunch;
     cudaMemcpyAsync(RR, d, sizeof(double) * 3 * P, cudaMemcpyDeviceToHost, E.stream);
     cudaMemcpyAsync(PP, d + 3 * P, sizeof(double) * 3 * P, cudaMemcpyDeviceToHost, E.stream);
     cudaError_t e = cudaStreamSynchronize(E.stream);
@@ -412,7 +412,7 @@ int pimd_evolve_all_device(pimd_ctx *ctx, double *RRt, double *PPt, double massO
     int threads, blocks;
     size_t smem;
     nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
-    k_evolve<<<blocks, threads, smem, E.stream>>>(a, RRt, PPt);
+    k_evolve<<<blocks, threads, smem, E.stream>>>(a, RRt, PPt); ++E.nlaunch;
     return nm_err(E, cudaGetLastError(), "evolve_all");
 }
 
@@ -428,7 +428,7 @@ int pimd_langevin_nm_device(pimd_ctx *ctx, double *PPt, const double *xi, double
     int threads, blocks;
     size_t smem;
     nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
-    k_langevin<<<blocks, threads, smem, E.stream>>>(a, PPt);
+    k_langevin<<<blocks, threads, smem, E.stream>>>(a, PPt); ++E.nlaunch;
     return nm_err(E, cudaGetLastError(), "langevin_nm");
 }
 
@@ -450,7 +450,7 @@ int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, do
     size_t smem;
     nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
     timer_begin(E, "md_pre");
-    k_md_pre<<<blocks, threads, smem, E.stream>>>(a, RRt, PPt, dRRt, RRc);
+    k_md_pre<<<blocks, threads, smem, E.stream>>>(a, RRt, PPt, dRRt, RRc); ++E.nlaunch;
     timer_end(E);
     KP saved = E.kp;
     E.kp.RRt = RRt;
@@ -467,8 +467,11 @@ int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, do
     a.xi = xi2;
     a.counter = 2ull * (unsigned long long)t + 1ull;
     timer_begin(E, "md_post");
-    k_md_post<<<blocks, threads, smem, E.stream>>>(a, PPt, dRRt, uk);
-    if (out4) k_md_sum<<<1, 32, 0, E.stream>>>(E.kp.P, d, d + E.kp.P, d + 2 * E.kp.P, uk, out4);
+    k_md_post<<<blocks, threads, smem, E.stream>>>(a, PPt, dRRt, uk); ++E.nlaunch;
+    if (out4) {
+        k_md_sum<<<1, 32, 0, E.stream>>>(E.kp.P, d, d + E.kp.P, d + 2 * E.kp.P, uk, out4);
+        ++E.nlaunch;
+    }
     timer_end(E);
     return nm_err(E, cudaGetLastError(), "md_step");
 }

@@ -852,6 +852,7 @@ __global__ void k_totals(KP kp, double *Upott, double *virialt, double *virialct
             KERN<2><<<GRID, BLOCK, 0, (E).stream>>>((E).kp, ##__VA_ARGS__);                  \
         else                                                                                 \
             KERN<3><<<GRID, BLOCK, 0, (E).stream>>>((E).kp, ##__VA_ARGS__);                  \
+        ++(E).nlaunch;                                                                       \
     } while (0)
 
 static int pair_blocks(const Engine &E) {
@@ -871,9 +872,9 @@ void launch_sites(Engine &E) {
 void launch_neighbors(Engine &E) {
     int *tmp = E.kp.nbrtmp;
     dim3 g((E.kp.N + 127) / 128, E.kp.P);
-    k_nbr_count<<<g, 128, 0, E.stream>>>(E.kp, tmp);
-    k_nbr_scan<<<E.kp.P, 1024, 0, E.stream>>>(E.kp, tmp);
-    k_nbr_fill<<<g, 128, 0, E.stream>>>(E.kp, tmp);
+    k_nbr_count<<<g, 128, 0, E.stream>>>(E.kp, tmp); ++E.nlaunch;
+    k_nbr_scan<<<E.kp.P, 1024, 0, E.stream>>>(E.kp, tmp); ++E.nlaunch;
+    k_nbr_fill<<<g, 128, 0, E.stream>>>(E.kp, tmp); ++E.nlaunch;
 }
 
 void launch_pair_qq(Engine &E) {
@@ -903,7 +904,7 @@ void launch_dd_real(Engine &E) {
 }
 
 void launch_dd_check(Engine &E, int iter) {
-    k_dd_check<<<1, 256, 0, E.stream>>>(E.kp, iter, E.kp.polar_eps);
+    k_dd_check<<<1, 256, 0, E.stream>>>(E.kp, iter, E.kp.polar_eps); ++E.nlaunch;
 }
 
 void launch_pair_force(Engine &E) {
@@ -917,7 +918,7 @@ void launch_finish(Engine &E) {
 }
 
 void launch_totals(Engine &E, double *Upott, double *virialt, double *virialct, double *virt9) {
-    k_totals<<<(E.kp.P + 63) / 64, 64, 0, E.stream>>>(E.kp, Upott, virialt, virialct, virt9);
+    k_totals<<<(E.kp.P + 63) / 64, 64, 0, E.stream>>>(E.kp, Upott, virialt, virialct, virt9); ++E.nlaunch;
 }
 
 }  // namespace pimd

@@ -71,6 +71,7 @@ SIGNATURES = {
     "pimd_md_step": [_V, ctypes.POINTER(MDParams), _D, _D, _D, _D, _D, _D, ctypes.c_int, _D],
     "pimd_peak_flops": [ctypes.c_int, ctypes.c_int, _D],
     "pimd_timers_reset": [_V, ctypes.c_int],
+    "pimd_launch_count": [_V],
     "pimd_timers_get": [_V, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, _D, ctypes.POINTER(ctypes.c_longlong)],
 }
 
@@ -87,7 +88,7 @@ def load(path=LIB):
         for name, args in SIGNATURES.items():
             f = getattr(L, name)
             f.argtypes = args
-            f.restype = ctypes.c_char_p if name == "pimd_last_error" else ctypes.c_int
+            f.restype = {"pimd_last_error": ctypes.c_char_p, "pimd_launch_count": ctypes.c_longlong}.get(name, ctypes.c_int)
         _lib = L
     return _lib
 
