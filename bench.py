@@ -113,7 +113,22 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------------------
-def run_gpu_arm(args, pkg, rank, world, local):
+def force_error(pkg, local):
+    """Mixed vs FP64 engine on the initial frame: RMS and max relative gradient error."""
+    c, p = workload(pkg, CONFIG)
+    out = {}
+    for prec in (pkg.engine.PIMD_FP64, pkg.engine.PIMD_MIXED):
+        eng = pkg.ForceEngine(p, precision=prec, device=local)
+        out[prec] = eng.full_bead_forces(c["RRt"], c["RRc"], t=1)
+        eng.close()
+    a, b = out[pkg.engine.PIMD_MIXED]["dRRt"], out[pkg.engine.PIMD_FP64]["dRRt"]
+    rms = float(np.sqrt(((a - b) ** 2).mean() / (b ** 2).mean()))
+    mx = float(np.abs(a - b).max() / np.abs(b).max())
+    ue = out[pkg.engine.PIMD_MIXED]["Upott"] - out[pkg.engine.PIMD_FP64]["Upott"]
+    return dict(force_rel_rms=rms, force_rel_max=mx, energy_abs_max=float(np.abs(ue).max()))
+
+
+def run_gpu_arm(args, pkg, rank, world, local, precision):
     import torch
 
     torch.cuda.set_device(local)
@@ -121,7 +136,7 @@ def run_gpu_arm(args, pkg, rank, world, local):
     c, p = workload(pkg, args.config)
     P, na, nw = p["nbeads"], p["natoms"], p["natoms"] // 3
     stream = torch.cuda.current_stream(dev)
-    eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_FP64, device=local)
+    eng = pkg.ForceEngine(p, precision=precision, device=local)
     eng.set_stream(stream.cuda_stream)
     alpha, nk, _ = eng.ewald_info()
     delt = DT_FS / 1000.0
@@ -241,9 +256,11 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl", rank=rank, world_size=world)
-    res = run_gpu_arm(args, pkg, rank, world, local)
+    res64 = run_gpu_arm(args, pkg, rank, world, local, pkg.engine.PIMD_FP64)
+    res = run_gpu_arm(args, pkg, rank, world, local, pkg.engine.PIMD_MIXED)
     if rank != 0:
         return 0
+    ferr = force_error(pkg, local)
     steps_total = args.steps * world
     value = steps_total / (res["dev_ms"] / 1000.0)
     ms_per_step = res["dev_ms"] / args.steps
@@ -256,9 +273,15 @@ def main():
     import ctypes
 
     pk = ctypes.c_double()
-    L.pimd_peak_flops(0, 1, ctypes.byref(pk))
+    L.pimd_peak_flops(local, 0, ctypes.byref(pk))
+    peak32 = pk.value
+    L.pimd_peak_flops(local, 1, ctypes.byref(pk))
     peak64 = pk.value
     ach = flops_ewald_dd(res["nk"], res["nw"], res["P"]) * dd_calls / (dd_ms / 1000.0) / 1e12 if dd_ms else None
+    t64 = res64["timers"]
+    dd64_ms = t64.get("dd_smu", (0, 0))[0] + t64.get("dd_update", (0, 0))[0]
+    ach64 = flops_ewald_dd(res64["nk"], res64["nw"], res64["P"]) * t64.get("dd_update", (0, 1))[1] / (dd64_ms / 1e3) / 1e12
+    fp64_value = steps_total / (res64["dev_ms"] / 1000.0)
     cpu = None
     if not args.no_cpu_baseline:
         orc = ge.load_oracle()
@@ -268,17 +291,25 @@ def main():
                    sample="%d MD steps of 512 H2O x 32 beads on the host cores (first step excluded)" % args.cpu_steps)
     line = dict(
         metric=METRIC, value=value, unit="steps/s", n_gpus=world, steps=args.steps, warmup=args.warmup,
-        ms_per_step=ms_per_step, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64",
+        ms_per_step=ms_per_step, higher_is_better=True, scaling="weak", vs_baseline=None,
+        dtype="f32 pair/phase arithmetic, f64 accumulation, f64 integrator",
         data="synthetic (seeded jittered-lattice water boxes with free ring-polymer beads)",
         config=dict(workload=CONFIG + " (TTM3-F, 512 H2O x 32 beads, L=24.86 A, Rc=9 A, |n|<=12, %d k-vectors)" % res["nk"],
-                    precision="fp64", polar_eps=POLAR["polar_eps"], predictor=True, dt_fs=DT_FS,
+                    precision="mixed", polar_eps=POLAR["polar_eps"], predictor=True, dt_fs=DT_FS,
                     l2="256 MB buffer written between timed steps", parallelism="replicas" if world > 1 else "1 GPU",
-                    dipole_iterations_mean=float(np.mean(res["niters"]))),
+                    dipole_iterations_mean=float(np.mean(res["niters"])),
+                    fp64_dipole_iterations_mean=float(np.mean(res64["niters"]))),
+        fp64=dict(value=fp64_value, ms_per_step=res64["dev_ms"] / args.steps,
+                  phases_ms={k: round(v[0] / args.steps, 4) for k, v in sorted(t64.items(), key=lambda kv: -kv[1][0])},
+                  roofline=dict(kernel="ewald_std_dd", bound="fp64-pipe", achieved=ach64, peak=peak64,
+                                unit="TFLOP/s", frac=ach64 / peak64)),
+        mixed_over_fp64=value / fp64_value,
+        accuracy=ferr,
         e2e=dict(value=res["e2e_steps"] / res["e2e_s"], unit="steps/s", h2d_bytes_per_step=res["h2d"],
                  d2h_bytes_per_step=res["d2h"]),
-        roofline=dict(kernel="ewald_std_dd (k_spass<MU> + k_sreduce + k_field<D>)", bound="fp64-pipe",
-                      achieved=ach, peak=peak64, unit="TFLOP/s", frac=(ach / peak64) if ach else None, traffic=None,
-                      peak_source="measured in-run: FP64 FMA-throughput kernel (MEASURED_PEAKS.json has no FP64 figure)"),
+        roofline=dict(kernel="ewald_std_dd (k_spass<MU,f32> + k_sreduce + k_field<D,f32>)", bound="fp32-pipe",
+                      achieved=ach, peak=peak32, unit="TFLOP/s", frac=(ach / peak32) if ach else None, traffic=None,
+                      peak_source="measured in-run: FP32 FMA-throughput kernel (MEASURED_PEAKS.json has no FP32 figure)"),
         cpu_baseline=cpu,
         clocks=res["clocks"],
         gpu_launches=res["launches"],

@@ -160,7 +160,7 @@ static int create(Engine &E, const pimd_params *p) {
     if (p->alpha <= 0 && !(p->eps_ewald > 0 && p->eps_ewald < 1)) return fail(E, PIMD_ERR_ARG, "eps_ewald");
     if (p->alpha > 0 && p->nmax < 1) return fail(E, PIMD_ERR_ARG, "nmax");
     if (p->polar_maxiter < 1) return fail(E, PIMD_ERR_ARG, "polar_maxiter must be >= 1");
-    if (p->precision != PIMD_FP64) return fail(E, PIMD_ERR_ARG, "only PIMD_FP64 is available");
+    if (p->precision != PIMD_FP64 && p->precision != PIMD_MIXED) return fail(E, PIMD_ERR_ARG, "precision");
     int rc = cuda_check(E, cudaSetDevice(p->device), "cudaSetDevice");
     if (rc) return rc;
     E.device = p->device;
@@ -242,6 +242,7 @@ static int create(Engine &E, const pimd_params *p) {
     kp.ew.cts1 = 2.0 * a / SQPI;
     kp.ew.cts2 = 4.0 * a * a * a / (3.0 * SQPI);
     kp.ew.cts3 = 8.0 * (a * a * a * a * a) / (15.0 * SQPI);
+    kp.ewf = EwCf{(float)kp.ew.aewald, (float)kp.ew.a2, (float)kp.ew.cts1, (float)kp.ew.cts2, (float)kp.ew.cts3};
     kp.stath = DEBYE / CHARGECON / std::sqrt((double)kp.natoms);
     kp.factor = 4.0 * (a * a * a) / (3.0 * std::sqrt(PI));
     // neighbour-list capacity: 3x the expected O-O pairs, at most all pairs
@@ -266,6 +267,14 @@ static int create(Engine &E, const pimd_params *p) {
         (rc = dalloc(E, &kp.acc, P * NACC)) || (rc = dalloc(E, &kp.err, 1)) || (rc = dalloc(E, &kp.allconv, 1)) ||
         (rc = dalloc(E, &kp.nbrtmp, P * N)) || (rc = dalloc(E, &E.d_out, 3 * P + 16)))
         return rc;
+    if (E.precision == PIMD_MIXED) {
+        kp.fcap = (int)std::min(2.0 * E.cap, (double)kp.N * (kp.N - 1));
+        if ((rc = dalloc(E, &kp.tabf, P * kp.ntab * S)) || (rc = dalloc(E, &kp.posf, P * S)) ||
+            (rc = dalloc(E, &kp.rhof, P * S)) || (rc = dalloc(E, &kp.fcnt, P * N)) || (rc = dalloc(E, &kp.foff, P * N)) ||
+            (rc = dalloc(E, &kp.fnbr, P * (size_t)kp.fcap * 2)) || (rc = dalloc(E, &kp.fntot, P)) ||
+            (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd * 6)))
+            return rc;
+    }
     cudaMemset(kp.txdip, 0, sizeof(double) * P * 4 * S * 3);
     cudaMemset(kp.Sm, 0, sizeof(double2) * P * kp.nk);
     cudaMemset(kp.err, 0, sizeof(unsigned));
@@ -342,16 +351,26 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
     kp.t = t;
     cudaMemsetAsync(kp.acc, 0, sizeof(double) * kp.P * NACC, E.stream);
     cudaMemsetAsync(kp.err, 0, sizeof(unsigned), E.stream);
+    const bool mixed = E.precision == PIMD_MIXED;
     PHASE("sites", launch_sites(E));
-    PHASE("neighbors", launch_neighbors(E));
-    PHASE("pair_qq", launch_pair_qq(E));
+    if (mixed) {
+        PHASE("site_offsets", launch_site_offsets(E));
+        PHASE("neighbors", launch_neighbors_m(E));
+        PHASE("pair_qq", launch_pair_qq_m(E));
+    } else {
+        PHASE("neighbors", launch_neighbors(E));
+        PHASE("pair_qq", launch_pair_qq(E));
+    }
     PHASE("ewald_tables", launch_ewald_tables(E));
     PHASE("ewald_sq", launch_ewald_sq(E));
     PHASE("ewald_fq", launch_ewald_fq(E));
     PHASE("after_qq", launch_after_qq(E));
     int iter = 1;
     for (; iter <= kp.polar_maxiter; iter++) {
-        PHASE("dd_real", launch_dd_real(E));
+        if (mixed)
+            PHASE("dd_real", launch_dd_real_m(E));
+        else
+            PHASE("dd_real", launch_dd_real(E));
         PHASE("dd_smu", launch_ewald_smu(E));
         PHASE("dd_update", launch_dd_update(E, iter));
         PHASE("dd_check", launch_dd_check(E, iter));
@@ -363,7 +382,10 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
         }
     }
     E.last_niter_max = std::min(iter, kp.polar_maxiter);
-    PHASE("pair_force", launch_pair_force(E));
+    if (mixed)
+        PHASE("pair_force", launch_pair_force_m(E));
+    else
+        PHASE("pair_force", launch_pair_force(E));
     PHASE("ewald_qd", launch_ewald_qd(E));
     PHASE("finish", launch_finish(E));
     PHASE("totals", launch_totals(E, Upott, virialt, virialct, virt9));

@@ -91,11 +91,14 @@ PIMD_D R gammq2_3(R x, unsigned *err) {
 struct EwC {
     double aewald, a2, cts1, cts2, cts3;
 };
+struct EwCf {
+    float aewald, a2, cts1, cts2, cts3;
+};
 
 // smear.f90:2-34 PBCsmear01: screened + Thole-smeared charge-charge tensors ts0, ts1.
 // ra = a_pol12^(1/3) is passed precomputed (a function of the site kinds only).
-template <typename R>
-PIMD_D void smear01(R drsq, R a_pol12, R ra, const EwC &e, R *ts0, R *ts1, unsigned *err) {
+template <typename R, typename EC>
+PIMD_D void smear01(R drsq, R a_pol12, R ra, const EC &e, R *ts0, R *ts1, unsigned *err) {
     const R g23 = R(1.3541179394264);
     R dd = sqrt(drsq);
     R dri = R(1) / dd;
@@ -117,8 +120,8 @@ PIMD_D void smear01(R drsq, R a_pol12, R ra, const EwC &e, R *ts0, R *ts1, unsig
 }
 
 // smear.f90:36-69 PBCsmear2
-template <typename R>
-PIMD_D void smear2(R drsq, R a_pol12, const EwC &e, R *ts1, R *ts2) {
+template <typename R, typename EC>
+PIMD_D void smear2(R drsq, R a_pol12, const EC &e, R *ts1, R *ts2) {
     R dd = sqrt(drsq);
     R dri = R(1) / dd;
     R drsqi = dri * dri;
@@ -141,8 +144,8 @@ PIMD_D void smear2(R drsq, R a_pol12, const EwC &e, R *ts1, R *ts2) {
 }
 
 // smear.f90:71-107 PBCsmear3
-template <typename R>
-PIMD_D void smear3(R drsq, R a_pol12, const EwC &e, R *ts1, R *ts2, R *ts3) {
+template <typename R, typename EC>
+PIMD_D void smear3(R drsq, R a_pol12, const EC &e, R *ts1, R *ts2, R *ts3) {
     R dd = sqrt(drsq);
     R dri = R(1) / dd;
     R drsqi = dri * dri;

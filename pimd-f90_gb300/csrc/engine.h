@@ -30,6 +30,8 @@
 
 namespace pimd {
 
+enum { PIMD_PREC_FP64 = 0, PIMD_PREC_MIXED = 1 };
+
 enum { ACC_UMON = 0, ACC_UVDW, ACC_UELEC2, ACC_UIND, ACC_VIRT, ACC_VIRIALC = ACC_VIRT + 9, ACC_DSQ,
        ACC_MUEFQ, ACC_DELTADIP, ACC_NITER, ACC_CONV, NACC = 24 };
 
@@ -63,6 +65,7 @@ struct KP {
     double gammaM, polar[5], dms1, dms2, dms3, polar_sor, stath, factor, Uvdw_lrc;
     double qO, qH, roh0, th0, harmkb, harmka;
     EwC ew;
+    EwCf ewf;  // FP32 copy for the mixed engine
     PairTables pt;
     // buffers
     const double *RRt, *RRc;
@@ -78,6 +81,15 @@ struct KP {
     const double *kAk;     // Ak = 2 exp(-k^2/4a^2)/k^2
     const int2 *kidx;      // (run index, kz) of each k-vector
     int *nbrtmp;           // [P][N] neighbour counts / offsets
+    // mixed-precision engine
+    float2 *tabf;          // [P][ntab][S] FP32 copies of the FP64 recurrence tables
+    float4 *posf;          // [P][S] (site - own O (min image), q)
+    float4 *rhof;          // [P][S] centroid site - own bead O (raw difference)
+    int *fcnt, *foff;      // [P][N] full neighbour list counts / offsets
+    int *fnbr;             // [P][fcap] full neighbour list (j ascending per i)
+    int *fntot;            // [P] full-list length
+    float *Tf;             // [P][fcap][ndd][6] FP32 dipole tensors of the full list
+    int fcap;
     double *acc;
     unsigned *err;
     int *allconv;
@@ -142,6 +154,12 @@ void launch_dd_check(Engine &E, int iter);
 void launch_pair_force(Engine &E);
 void launch_finish(Engine &E);
 void launch_totals(Engine &E, double *Upott, double *virialt, double *virialct, double *virt9);
+// launchers (mixed.cu): FP32 pair arithmetic, FP64 accumulation
+void launch_site_offsets(Engine &E);
+void launch_neighbors_m(Engine &E);
+void launch_pair_qq_m(Engine &E);
+void launch_dd_real_m(Engine &E);
+void launch_pair_force_m(Engine &E);
 // launchers (ewald.cu)
 void launch_ewald_tables(Engine &E);
 void launch_ewald_sq(Engine &E);

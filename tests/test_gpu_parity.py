@@ -129,3 +129,46 @@ def test_normal_modes_bit_exact(pkg, orc, engine_lib):
         g = eng.evolve_ring(RR, PP, 1.008)
         r = orc.evolve_ring(b, RR, PP, 1.008)
         assert np.array_equal(g[0], r[0]) and np.array_equal(g[1], r[1])
+
+
+# ---------------------------------------------------------------------------------------
+# Mixed precision (FP32 pair/phase arithmetic, FP64 accumulation): error budget against the
+# FP64 oracle. Force RMS error must stay below 1e-4 relative (the stated target); energy,
+# dipoles and virial are held to the tolerances written below.
+def rms_rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return np.sqrt(((a - b) ** 2).mean()) / np.sqrt((b ** 2).mean())
+
+
+@pytest.mark.parametrize("model", [3, 2])
+def test_mixed_error_budget_small(pkg, orc, engine_lib, model):
+    c, p = small_case(pkg, model, nw=64, P=3, polar_maxiter=40)
+    eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_MIXED)
+    got = eng.full_bead_forces(c["RRt"], c["RRc"], t=1)
+    ref = orc.full_bead_forces(p, c["RRt"], c["RRc"], t=1)
+    assert rms_rel(got["dRRt"], ref["dRRt"]) < 1e-5
+    assert rel(got["dRRt"], ref["dRRt"]) < 1e-4
+    o = orc.Oracle(p)
+    for k in range(p["nbeads"]):
+        r = o.pot_ttm(c["RRt"][k], c["RRc"], bead=k)
+        scale = abs(r["Umon"]) + abs(r["Uvdw"]) + abs(r["Uelec"]) + abs(r["Uind"])
+        assert abs(got["Upott"][k] - r["En"]) < 1e-6 * scale
+    assert rms_rel(got["dip_momEt"], ref["dip_momEt"]) < 1e-5
+    assert np.abs(got["virialt"] - ref["virialt"]).max() < 1e-5 * np.abs(ref["virialt"]).max() + 1e-3
+    assert np.array_equal(eng.neighbors(0), o.neighbors(c["RRt"][0]))
+
+
+def test_mixed_headline_and_convergence(pkg, orc, engine_lib):
+    """TTM3-F 512 H2O x 32 beads: force RMS error <= 1e-4 relative, and the induced dipoles
+    converge to the 1e-8 threshold (deterministic FP32 field, FP64 residual)."""
+    c = pkg.waterbox.make_config("ttm3f_512x32")
+    p = dict(c["params"], polar_maxiter=100, polar_eps=1e-8)
+    eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_MIXED)
+    got = eng.full_bead_forces(c["RRt"], c["RRc"])
+    o = orc.Oracle(p)
+    for k in (0, 17):
+        r = o.pot_ttm(c["RRt"][k], c["RRc"], bead=k)
+        assert rms_rel(got["dRRt"][k], r["dRR"]) < 1e-4
+        e = eng.energies(k)
+        assert e["niter"] < p["polar_maxiter"] and e["deltadip"] < p["polar_eps"]
+        assert abs(e["niter"] - r["niter"]) <= 2
