@@ -158,6 +158,23 @@ int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, do
 int pimd_md_step(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
                  double *RRc, const double *xi1, const double *xi2, int t, double *out4);
 
+/* O-O half neighbour list of one bead without any device allocation. No counterpart in the
+ * reference; it serves callers that must not let a library allocate device memory (drivers
+ * that own all GPU memory through their own pool, applications with a fixed per-GPU budget,
+ * code recording CUDA graphs, where cudaMalloc is not a stream operation).
+ * In (device): RR(3,Natoms) of one bead, atoms O H H ...; box[3] and rc on the host.
+ * Out (device): ij[2*cap] int pairs (i, j), 0-based, i < j, in find_neigh's order, bit-identical
+ * to pimd_get_neighbors; *npairs (device int) = total pairs found, which may exceed cap (then
+ * only the first cap pairs are written). Stream-ordered on cuda_stream (NULL = default stream);
+ * allocates nothing and does not synchronise.
+ * Limit: Natoms/3 <= 16384 molecules; larger inputs return PIMD_ERR_ARG with a message.
+ * Its per-molecule counts and offsets live in one fixed 128 KB device array per GPU that is
+ * shared by every call and fully rewritten by each call; calls that overlap on the GPU (two
+ * streams, or two host threads) race on it. The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) and should come before any stream capture. */
+int pimd_neighbors_noalloc(const double *RR, int natoms, const double *box, double rc, int *ij,
+                           int cap, int *npairs, void *cuda_stream);
+
 /* Measured CUDA-core FMA throughput of `device` in TFLOP/s (fp64 != 0: double, else float):
  * the roofline denominator for kernels bound by the FP64 / FP32 pipes. No counterpart in the
  * reference (which has no GPU path). */

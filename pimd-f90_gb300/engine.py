@@ -70,6 +70,7 @@ SIGNATURES = {
     "pimd_md_step_device": [_V, ctypes.POINTER(MDParams), _V, _V, _V, _V, _V, _V, ctypes.c_int, _V],
     "pimd_md_step": [_V, ctypes.POINTER(MDParams), _D, _D, _D, _D, _D, _D, ctypes.c_int, _D],
     "pimd_peak_flops": [ctypes.c_int, ctypes.c_int, _D],
+    "pimd_neighbors_noalloc": [_V, ctypes.c_int, _D, ctypes.c_double, _V, ctypes.c_int, _V, _V],
     "pimd_timers_reset": [_V, ctypes.c_int],
     "pimd_launch_count": [_V],
     "pimd_timers_get": [_V, ctypes.c_int, ctypes.c_char_p, ctypes.c_int, _D, ctypes.POINTER(ctypes.c_longlong)],
