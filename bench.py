@@ -47,7 +47,19 @@ def parse():
     ap.add_argument("--config", default=CONFIG)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-force", choices=["fp64", "mixed"],
+                    help="run two force calls of the workload and exit (the case profiled with ncu)")
     return ap.parse_args()
+
+
+def profile_force(pkg, which):
+    c, p = workload(pkg, CONFIG)
+    prec = pkg.engine.PIMD_MIXED if which == "mixed" else pkg.engine.PIMD_FP64
+    eng = pkg.ForceEngine(p, precision=prec)
+    for t in (1, 2):
+        r = eng.full_bead_forces(c["RRt"], c["RRc"], t=t)
+    print(json.dumps(dict(profile_force=which, Upot=float(r["Upot"]), niter=eng.energies(0)["niter"])))
+    eng.close()
 
 
 def workload(pkg, name):
@@ -233,6 +245,10 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     pkg = ge.load_package()
+    if args.profile_force:
+        pkg.build_lib.build()
+        profile_force(pkg, args.profile_force)
+        return 0
     if args.impl == "reference":
         if rank != 0:
             return 0

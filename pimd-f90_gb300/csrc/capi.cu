@@ -265,7 +265,8 @@ static int create(Engine &E, const pimd_params *p) {
         (rc = dalloc(E, &kp.tab, P * kp.ntab * S)) || (rc = dalloc(E, &kp.Spart, P * maxgroups * kp.nk * 3)) ||
         (rc = dalloc(E, &kp.Sq, P * kp.nk)) || (rc = dalloc(E, &kp.Sm, P * kp.nk)) || (rc = dalloc(E, &kp.Sdip, P * kp.nk * 3)) ||
         (rc = dalloc(E, &kp.acc, P * NACC)) || (rc = dalloc(E, &kp.err, 1)) || (rc = dalloc(E, &kp.allconv, 1)) ||
-        (rc = dalloc(E, &kp.nbrtmp, P * N)) || (rc = dalloc(E, &E.d_out, 3 * P + 16)))
+        (rc = dalloc(E, &kp.nbrtmp, P * N)) || (rc = dalloc(E, &E.d_out, 3 * P + 16)) ||
+        (rc = dalloc(E, &kp.Fpart, (size_t)E.max_slices * P * S)))
         return rc;
     if (E.precision == PIMD_MIXED) {
         kp.fcap = (int)std::min(2.0 * E.cap, (double)kp.N * (kp.N - 1));
@@ -355,7 +356,7 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
     PHASE("sites", launch_sites(E));
     if (mixed) {
         PHASE("site_offsets", launch_site_offsets(E));
-        PHASE("neighbors", launch_neighbors_m(E));
+        PHASE("neighbors", launch_neighbors(E));
         PHASE("pair_qq", launch_pair_qq_m(E));
     } else {
         PHASE("neighbors", launch_neighbors(E));

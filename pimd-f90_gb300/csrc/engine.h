@@ -90,6 +90,7 @@ struct KP {
     int *fntot;            // [P] full-list length
     float *Tf;             // [P][fcap][ndd][6] FP32 dipole tensors of the full list
     int fcap;
+    double4_32a *Fpart;    // [slices][P][S] per-k-slice partial fields of the Ewald field passes
     double *acc;
     unsigned *err;
     int *allconv;
@@ -116,6 +117,7 @@ struct Engine {
     cudaStream_t stream = 0;
     bool own_stream = false;
     int nchunk = 0, ntile_q = 0, ntile_d = 0, max_runs_chunk = 0;
+    int max_slices = 16;  // k-slices of the Ewald field passes (Fpart capacity)
     size_t cap = 0;
     std::vector<KRun> h_runs;
     std::vector<KChunk> h_chunks;
@@ -142,10 +144,11 @@ void timer_begin(Engine &E, const char *name);
 void timer_end(Engine &E);
 int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt, double *virialct, double *virt9);
 
+// launchers (neighbors.cu)
+void launch_neighbors(Engine &E);
 // launchers (pot.cu)
 void pot_init_constants(Engine &E);
 void launch_sites(Engine &E);
-void launch_neighbors(Engine &E);
 void launch_pair_qq(Engine &E);
 void launch_after_qq(Engine &E);
 void launch_dd_real(Engine &E);
@@ -156,7 +159,6 @@ void launch_finish(Engine &E);
 void launch_totals(Engine &E, double *Upott, double *virialt, double *virialct, double *virt9);
 // launchers (mixed.cu): FP32 pair arithmetic, FP64 accumulation
 void launch_site_offsets(Engine &E);
-void launch_neighbors_m(Engine &E);
 void launch_pair_qq_m(Engine &E);
 void launch_dd_real_m(Engine &E);
 void launch_pair_force_m(Engine &E);

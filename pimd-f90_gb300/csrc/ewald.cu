@@ -16,6 +16,8 @@
 // sums (double in the FP64 engine, float in the mixed engine). The e^{i n 2pi x/L} tables
 // always come from the FP64 recurrence (k.r reduced in FP64) and are stored as R; tile
 // partials and chunk partials are added in FP64.
+#include <algorithm>
+
 #include "engine.h"
 
 namespace pimd {
@@ -241,10 +243,13 @@ __global__ void __launch_bounds__(256) k_sreduce(KP kp, int ngroups, int skipcon
 enum { F_Q = 0, F_D = 1, F_QD = 2 };
 constexpr int KCH = 256;  // k-vectors staged per chunk (== SP_NT)
 
+// The k-list is split over gridDim.z slices (whole chunks each); every block writes its
+// slice's FP64 partial (E or G, phi) per site to Fpart[slice][bead][site], and
+// k_field_finish adds the slices in a fixed order and applies the epilogue.
 template <int MODE, int NT, typename R>
-__global__ void __launch_bounds__(NT) k_field(KP kp, int s0, int s1, int iter) {
+__global__ void __launch_bounds__(NT) k_field(KP kp, int s0, int s1) {
     using V = typename C2<R>::T;
-    const int b = blockIdx.y;
+    const int b = blockIdx.y, slice = blockIdx.z, nslice = gridDim.z;
     if (MODE == F_D && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
     const int s = s0 + blockIdx.x * NT + threadIdx.x;
     const bool valid = s < s1;
@@ -274,7 +279,8 @@ __global__ void __launch_bounds__(NT) k_field(KP kp, int s0, int s1, int iter) {
     const R qr = R(q), mur[3] = {R(mu[0]), R(mu[1]), R(mu[2])};
     double E[3] = {0, 0, 0}, phi = 0.0, G[3] = {0, 0, 0};
     const double2 *S1 = (MODE == F_Q) ? kp.Sq : kp.Sm;
-    for (int chn = 0; chn < kp.nchunk; chn++) {
+    const int c0 = (int)((long)slice * kp.nchunk / nslice), c1 = (int)((long)(slice + 1) * kp.nchunk / nslice);
+    for (int chn = c0; chn < c1; chn++) {
         const KChunk ch = kp.chunks[chn];
         __syncthreads();
         for (int i = threadIdx.x; i < ch.k1 - ch.k0; i += NT) {
@@ -348,6 +354,33 @@ __global__ void __launch_bounds__(NT) k_field(KP kp, int s0, int s1, int iter) {
             G[c] += (double)cG[c];
         }
     }
+    if (valid) {
+        double4_32a *o = kp.Fpart + ((size_t)slice * kp.P + b) * (s1 - s0) + (s - s0);
+        if (MODE == F_QD)
+            *o = make_double4_32a(G[0], G[1], G[2], phi);
+        else
+            *o = make_double4_32a(E[0], E[1], E[2], phi);
+    }
+}
+
+// Sum the slices of k_field in order and apply the pass's epilogue, one thread per site.
+template <int MODE, int NT>
+__global__ void __launch_bounds__(NT) k_field_finish(KP kp, int s0, int s1, int nslice, int iter) {
+    const int b = blockIdx.y;
+    if (MODE == F_D && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
+    const int s = s0 + blockIdx.x * NT + threadIdx.x;
+    const bool valid = s < s1;
+    const size_t gs = (size_t)b * kp.S + (valid ? s : s0);
+    double E[3] = {0, 0, 0}, phi = 0.0;
+    if (valid) {
+        for (int z = 0; z < nslice; z++) {
+            const double4_32a p = kp.Fpart[((size_t)z * kp.P + b) * (s1 - s0) + (s - s0)];
+            E[0] += p.x;
+            E[1] += p.y;
+            E[2] += p.z;
+            phi += p.w;
+        }
+    }
     if (MODE == F_Q) {
         if (valid) {
             double4_32a f = kp.F[gs];
@@ -360,14 +393,18 @@ __global__ void __launch_bounds__(NT) k_field(KP kp, int s0, int s1, int iter) {
     } else if (MODE == F_QD) {
         if (valid) {
             if (s >= kp.N) kp.F[gs].w += phi;
-            kp.dR[3 * gs + 0] += G[0];
-            kp.dR[3 * gs + 1] += G[1];
-            kp.dR[3 * gs + 2] += G[2];
+            kp.dR[3 * gs + 0] += E[0];
+            kp.dR[3 * gs + 1] += E[1];
+            kp.dR[3 * gs + 2] += E[2];
         }
     } else {
         // pot_ttm.f90:371-381 Efd = Efd_real + Efd_rec + Efq + factor mu; SOR update (FP64)
         double av[2] = {0.0, 0.0};
+        double mu[3] = {0, 0, 0};
         if (valid) {
+            mu[0] = kp.dip[3 * gs];
+            mu[1] = kp.dip[3 * gs + 1];
+            mu[2] = kp.dip[3 * gs + 2];
             const double4_32a f = kp.F[gs];
             const double efq[3] = {f.x, f.y, f.z};
             const int kind = s / kp.N + 1;
@@ -487,9 +524,16 @@ static void launch_field_nt(Engine &E, int s0, int s1, int iter) {
         cudaFuncSetAttribute(k_field<MODE, NT, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         set = true;
     }
-    dim3 g((s1 - s0 + NT - 1) / NT, E.kp.P);
-    k_field<MODE, NT, R><<<g, NT, smem, E.stream>>>(E.kp, s0, s1, iter);
-    ++E.nlaunch;
+    // k-slices: enough blocks for ~8 (FP32) / ~4 (FP64) resident blocks per SM
+    const int sblocks = (s1 - s0 + NT - 1) / NT;
+    const long want = (sizeof(R) == 4 ? 8L : 4L) * 152;
+    int ns = (int)((want + (long)sblocks * E.kp.P - 1) / ((long)sblocks * E.kp.P));
+    ns = std::max(1, std::min(ns, std::min(E.nchunk, E.max_slices)));
+    dim3 g(sblocks, E.kp.P, ns);
+    k_field<MODE, NT, R><<<g, NT, smem, E.stream>>>(E.kp, s0, s1);
+    dim3 g2((s1 - s0 + 127) / 128, E.kp.P);
+    k_field_finish<MODE, 128><<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns, iter);
+    E.nlaunch += 2;
 }
 
 template <int MODE>

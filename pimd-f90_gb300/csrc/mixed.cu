@@ -33,20 +33,6 @@ struct TM {
 
 PIMD_D float wrapf(float v, float L, float Li) { return v - L * rintf(v * Li); }
 
-// exact (bit-identical) O-O test, FP32 prefilter with an FP64 decision near the cutoff
-PIMD_D bool oo_within_pre(const double4_32a &a, const double4_32a &b, const KP &kp, float rc2f) {
-    float d2 = 0.f;
-    const float dx = wrapf((float)(a.x - b.x), (float)kp.box[0], (float)kp.boxi[0]);
-    const float dy = wrapf((float)(a.y - b.y), (float)kp.box[1], (float)kp.boxi[1]);
-    const float dz = wrapf((float)(a.z - b.z), (float)kp.box[2], (float)kp.boxi[2]);
-    d2 = dx * dx + dy * dy + dz * dz;
-    if (fabsf(d2 - rc2f) > 1e-4f * rc2f + 1e-3f) return d2 < rc2f;
-    const double x = min_image_rn(__dsub_rn(a.x, b.x), kp.box[0], kp.boxi[0]);
-    const double y = min_image_rn(__dsub_rn(a.y, b.y), kp.box[1], kp.boxi[1]);
-    const double z = min_image_rn(__dsub_rn(a.z, b.z), kp.box[2], kp.boxi[2]);
-    return dot3_rn(x, y, z) < kp.rc2;
-}
-
 // ---------------------------------------------------------------------------------------
 // per-site offsets: delta = site - own O (min image), rho = centroid site - own bead O (raw)
 __global__ void __launch_bounds__(128) k_site_offsets(KP kp) {
@@ -65,66 +51,6 @@ __global__ void __launch_bounds__(128) k_site_offsets(KP kp) {
     }
     kp.posf[gs] = d;
     kp.rhof[gs] = make_float4((float)(C.x - O.x), (float)(C.y - O.y), (float)(C.z - O.z), 0.f);
-}
-
-// half (j > i) and full (j != i) neighbour lists with the prefiltered exact test
-template <bool FULL>
-__global__ void __launch_bounds__(128) k_nbr_count_m(KP kp, int *cnt) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
-    if (i >= kp.N) return;
-    const double4_32a *O = kp.pos + (size_t)b * kp.S;
-    const double4_32a oi = O[i];
-    const float rc2f = (float)kp.rc2;
-    int n = 0;
-    for (int j = FULL ? 0 : i + 1; j < kp.N; j++)
-        if (j != i) n += oo_within_pre(oi, O[j], kp, rc2f) ? 1 : 0;
-    cnt[(size_t)b * kp.N + i] = n;
-}
-
-template <bool FULL>
-__global__ void __launch_bounds__(128) k_nbr_fill_m(KP kp, const int *off) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
-    if (i >= kp.N) return;
-    const double4_32a *O = kp.pos + (size_t)b * kp.S;
-    const double4_32a oi = O[i];
-    const float rc2f = (float)kp.rc2;
-    int o = off[(size_t)b * kp.N + i];
-    const int cap = FULL ? kp.fcap : kp.cap;
-    int2 *out = (FULL ? reinterpret_cast<int2 *>(kp.fnbr) : kp.pairs) + (size_t)b * cap;
-    for (int j = FULL ? 0 : i + 1; j < kp.N; j++)
-        if (j != i && oo_within_pre(oi, O[j], kp, rc2f)) {
-            if (o < cap) out[o] = make_int2(i, j);
-            o++;
-        }
-}
-
-// exclusive scan of per-molecule counts, one block per bead; total -> tot[b]
-__global__ void __launch_bounds__(1024) k_scan_counts(const int *cnt, int *off, int *tot, int N, int cap, unsigned *err) {
-    __shared__ int part[1024];
-    const int b = blockIdx.x, nt = blockDim.x;
-    const int per = (N + nt - 1) / nt, i0 = threadIdx.x * per, i1 = min(N, i0 + per);
-    const int *c = cnt + (size_t)b * N;
-    int *o = off + (size_t)b * N;
-    int s = 0;
-    for (int i = i0; i < i1; i++) s += c[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int d = 1; d < nt; d <<= 1) {
-        int v = (threadIdx.x >= d) ? part[threadIdx.x - d] : 0;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    int base = part[threadIdx.x] - s;
-    for (int i = i0; i < i1; i++) {
-        const int v = c[i];  // off may alias cnt
-        o[i] = base;
-        base += v;
-    }
-    if (threadIdx.x == nt - 1) {
-        tot[b] = min(part[nt - 1], cap);
-        if (part[nt - 1] > cap) atomicOr(err, 1u);
-    }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -293,21 +219,24 @@ __global__ void __launch_bounds__(128) k_dd_tensors_m(KP kp) {
     }
 }
 
-// real-space dipole field of one iteration: gather over the full list, one molecule per
-// thread, deterministic order; writes Efdr (pot_ttm.f90:311-365)
+// real-space dipole field of one iteration: gather over the full list, one warp per
+// molecule, lanes striding over its entries, butterfly reduction in a fixed order
+// (deterministic); writes Efdr (pot_ttm.f90:311-365)
 template <int MODEL>
 __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
     using T = TM<MODEL>;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y, N = kp.N;
+    const int lane = threadIdx.x & 31;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, b = blockIdx.y, N = kp.N;
     if (i >= N) return;
     if (kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
     const double *dip = kp.dip + (size_t)b * kp.S * 3;
     const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
-    const int e0 = kp.foff[(size_t)b * N + i], e1 = e0 + kp.fcnt[(size_t)b * N + i];
+    const int e0 = kp.foff[(size_t)b * N + i];
+    const int e1 = (i + 1 < N) ? kp.foff[(size_t)b * N + i + 1] : kp.fntot[b];
     float ei[5][3];
 #pragma unroll
     for (int k = 0; k < 5; k++) ei[k][0] = ei[k][1] = ei[k][2] = 0.f;
-    for (int e = e0; e < e1; e++) {
+    for (int e = e0 + lane; e < e1; e += 32) {
         const int j = fl[e].y;
         const float *Te = kp.Tf + ((size_t)b * kp.fcap + e) * kp.ndd * 6;
         int t = 0;
@@ -323,6 +252,16 @@ __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
                 ei[isp][2] += Tt[4] * mx + Tt[5] * my + Tt[2] * mz;
             }
     }
+#pragma unroll
+    for (int k = T::FDI; k <= T::LDI; k++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            float v = ei[k][c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            ei[k][c] = v;
+        }
+    if (lane != 0) return;
     if (MODEL == 2) {  // intramolecular O-H1, O-H2, H1-H2 from the FP64 per-molecule cache
         const double *Tw = kp.Tself + ((size_t)b * N + i) * 18;
         int t = 0;
@@ -564,18 +503,6 @@ void launch_site_offsets(Engine &E) {
     ++E.nlaunch;
 }
 
-void launch_neighbors_m(Engine &E) {
-    KP &kp = E.kp;
-    dim3 g((kp.N + 127) / 128, kp.P);
-    k_nbr_count_m<false><<<g, 128, 0, E.stream>>>(kp, kp.nbrtmp);
-    k_scan_counts<<<kp.P, 1024, 0, E.stream>>>(kp.nbrtmp, kp.nbrtmp, kp.npair, kp.N, kp.cap, kp.err);
-    k_nbr_fill_m<false><<<g, 128, 0, E.stream>>>(kp, kp.nbrtmp);
-    k_nbr_count_m<true><<<g, 128, 0, E.stream>>>(kp, kp.fcnt);
-    k_scan_counts<<<kp.P, 1024, 0, E.stream>>>(kp.fcnt, kp.foff, kp.fntot, kp.N, kp.fcap, kp.err);
-    k_nbr_fill_m<true><<<g, 128, 0, E.stream>>>(kp, kp.foff);
-    E.nlaunch += 6;
-}
-
 void launch_pair_qq_m(Engine &E) {
     dim3 g(pair_blocks_m(E, 64), E.kp.P);
     DISPATCH_M(E, k_pair_qq_m, g, 128);
@@ -584,7 +511,7 @@ void launch_pair_qq_m(Engine &E) {
 }
 
 void launch_dd_real_m(Engine &E) {
-    dim3 g((E.kp.N + 127) / 128, E.kp.P);
+    dim3 g((E.kp.N * 32 + 127) / 128, E.kp.P);
     DISPATCH_M(E, k_dd_real_m, g, 128);
 }
 

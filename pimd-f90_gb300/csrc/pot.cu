@@ -209,69 +209,6 @@ __global__ void __launch_bounds__(128) k_sites(KP kp) {
 }
 
 // ---------------------------------------------------------------------------------------
-// find_neigh.f90:171-277: for molecule i all j > i with |R_Oi - R_Oj|^2 < Rc^2 under the
-// anint minimum image, ascending j; computed once per force call (the reference repeats the
-// identical search 2 + n_iter times). Bit-exact: every operation rounded as the reference.
-PIMD_D bool oo_within(const double4_32a &a, const double4_32a &b, const KP &kp) {
-    const double x = min_image_rn(__dsub_rn(a.x, b.x), kp.box[0], kp.boxi[0]);
-    const double y = min_image_rn(__dsub_rn(a.y, b.y), kp.box[1], kp.boxi[1]);
-    const double z = min_image_rn(__dsub_rn(a.z, b.z), kp.box[2], kp.boxi[2]);
-    return dot3_rn(x, y, z) < kp.rc2;
-}
-
-__global__ void __launch_bounds__(128) k_nbr_count(KP kp, int *cnt) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
-    if (i >= kp.N) return;
-    const double4_32a *O = kp.pos + (size_t)b * kp.S;
-    const double4_32a oi = O[i];
-    int n = 0;
-    for (int j = i + 1; j < kp.N; j++) n += oo_within(oi, O[j], kp) ? 1 : 0;
-    cnt[(size_t)b * kp.N + i] = n;
-}
-
-// exclusive scan of the per-molecule counts of one bead (one block per bead)
-__global__ void __launch_bounds__(1024) k_nbr_scan(KP kp, int *cnt) {
-    __shared__ int part[1024];
-    const int b = blockIdx.x, N = kp.N, nt = blockDim.x;
-    const int per = (N + nt - 1) / nt, i0 = threadIdx.x * per, i1 = min(N, i0 + per);
-    int *c = cnt + (size_t)b * N;
-    int s = 0;
-    for (int i = i0; i < i1; i++) s += c[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int off = 1; off < nt; off <<= 1) {
-        int v = (threadIdx.x >= off) ? part[threadIdx.x - off] : 0;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
-    }
-    int base = part[threadIdx.x] - s;
-    for (int i = i0; i < i1; i++) {
-        int v = c[i];
-        c[i] = base;
-        base += v;
-    }
-    if (threadIdx.x == nt - 1) {
-        const int tot = part[nt - 1];
-        kp.npair[b] = min(tot, kp.cap);
-        if (tot > kp.cap) atomicOr(kp.err, 1u);
-    }
-}
-
-__global__ void __launch_bounds__(128) k_nbr_fill(KP kp, const int *off) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
-    if (i >= kp.N) return;
-    const double4_32a *O = kp.pos + (size_t)b * kp.S;
-    const double4_32a oi = O[i];
-    int o = off[(size_t)b * kp.N + i];
-    int2 *out = kp.pairs + (size_t)b * kp.cap;
-    for (int j = i + 1; j < kp.N; j++)
-        if (oo_within(oi, O[j], kp)) {
-            if (o < kp.cap) out[o] = make_int2(i, j);
-            o++;
-        }
-}
-
 // ---------------------------------------------------------------------------------------
 // pot_ttm.f90:159-228: O-O van der Waals and the charge-charge real-space sum (screened
 // Coulomb with Thole smearing below 5 A) over all site pairs of each neighbour pair. Also
@@ -867,14 +804,6 @@ static int pair_blocks(const Engine &E) {
 void launch_sites(Engine &E) {
     dim3 g((E.kp.N + 127) / 128, E.kp.P);
     DISPATCH_TTM(E, k_sites, g, 128);
-}
-
-void launch_neighbors(Engine &E) {
-    int *tmp = E.kp.nbrtmp;
-    dim3 g((E.kp.N + 127) / 128, E.kp.P);
-    k_nbr_count<<<g, 128, 0, E.stream>>>(E.kp, tmp); ++E.nlaunch;
-    k_nbr_scan<<<E.kp.P, 1024, 0, E.stream>>>(E.kp, tmp); ++E.nlaunch;
-    k_nbr_fill<<<g, 128, 0, E.stream>>>(E.kp, tmp); ++E.nlaunch;
 }
 
 void launch_pair_qq(Engine &E) {
