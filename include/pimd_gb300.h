@@ -158,6 +158,19 @@ int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, do
 int pimd_md_step(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
                  double *RRc, const double *xi1, const double *xi2, int t, double *out4);
 
+/* CUDA-graph execution of pimd_md_step_device / pimd_md_step (enable != 0). The whole step --
+ * Langevin, kicks, EvolveRing, PBCs and the force call -- is captured on its first call and
+ * replayed on later calls with the same buffers and parameters (a change of any pointer or
+ * md parameter re-captures). The induced-dipole iterations run inside the graph as a
+ * conditional while node: the device tests convergence after each iteration and stops at the
+ * same iteration as the host loop, without returning to the host. The MD step index t is
+ * written to the device before each launch, so the predictor and the Langevin stream follow t
+ * exactly as in the eager path. Phase timers then report the step as one phase ("md_graph").
+ * No counterpart in the reference (MD.f90:35-110 is a host loop). */
+int pimd_set_graph(pimd_ctx *ctx, int enable);
+/* Number of graph captures and graph launches made by this context so far. */
+int pimd_graph_info(pimd_ctx *ctx, long long *captures, long long *launches);
+
 /* O-O half neighbour list of one bead without any device allocation. No counterpart in the
  * reference; it serves callers that must not let a library allocate device memory (drivers
  * that own all GPU memory through their own pool, applications with a fixed per-GPU budget,

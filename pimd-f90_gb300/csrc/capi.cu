@@ -18,6 +18,11 @@ static const ModelSet TTM21F = {-1.329565985e+6, 3.632560798e+5, -2.147141323e+3
                                 0.837, 0.496, 0.837, 0.837, 0.496, 0.837, 0.426706882, 0.0, 0.0, 0.0};
 static const ModelSet TTM3F = {0.0, 0.0, -0.72298855e+03, 0.10211829e+06, 0.37170376e+01, 0.175, 0.175,
                                0.837, 0.496, 0.837, 0.0, 0.0, 1.444, 0.46, 0.5, 0.9578, 0.012};
+// q-SPC/Fw and SPC/F (pot_mod.f90:29-44): only the Lennard-Jones A/r^12 + C/r^6 terms are used
+static const ModelSet QSPCFW = {629326.57249877361701443513, 0.0, -625.50206521141523463400, 0, 0, 0, 0,
+                                0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+static const ModelSet SPCF = {628213.72817108343399678768, 0.0, -624.97858519194071637260, 0, 0, 0, 0,
+                              0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 
 static int fail(Engine &E, int code, const char *msg) {
     E.last_error = msg;
@@ -142,6 +147,19 @@ static int setup_kspace(Engine &E, const pimd_params *p) {
     cudaMemcpy(d_kinfo, kinfo.data(), sizeof(double4_32a) * kp.nk, cudaMemcpyHostToDevice);
     cudaMemcpy(d_Ak, E.h_Ak.data(), sizeof(double) * kp.nk, cudaMemcpyHostToDevice);
     cudaMemcpy(d_kidx, kidx.data(), sizeof(int2) * kp.nk, cudaMemcpyHostToDevice);
+    // FP32 copies of the k-vector components for the mixed engine's phase arithmetic
+    std::vector<float2> runkf(kp.nrun);
+    std::vector<float> kzf(kp.nk);
+    for (int r = 0; r < kp.nrun; r++)
+        runkf[r] = make_float2((float)E.h_kvec[3 * E.h_runs[r].kbeg], (float)E.h_kvec[3 * E.h_runs[r].kbeg + 1]);
+    for (int k = 0; k < kp.nk; k++) kzf[k] = (float)E.h_kvec[3 * k + 2];
+    float2 *d_runkf;
+    float *d_kzf;
+    if ((rc = dalloc(E, &d_runkf, kp.nrun)) || (rc = dalloc(E, &d_kzf, kp.nk))) return rc;
+    cudaMemcpy(d_runkf, runkf.data(), sizeof(float2) * kp.nrun, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_kzf, kzf.data(), sizeof(float) * kp.nk, cudaMemcpyHostToDevice);
+    kp.runkf = d_runkf;
+    kp.kzf = d_kzf;
     kp.runs = d_runs;
     kp.chunks = d_chunks;
     kp.kinfo = d_kinfo;
@@ -152,7 +170,9 @@ static int setup_kspace(Engine &E, const pimd_params *p) {
 
 static int create(Engine &E, const pimd_params *p) {
     if (!p || p->natoms <= 0 || p->natoms % 3 || p->nbeads < 1) return fail(E, PIMD_ERR_ARG, "natoms/nbeads");
-    if (p->pot_model != 2 && p->pot_model != 3) return fail(E, PIMD_ERR_ARG, "pot_model must be 2 or 3");
+    if (p->pot_model < 2 || p->pot_model > 5) return fail(E, PIMD_ERR_ARG, "pot_model must be 2, 3, 4 or 5");
+    const bool spc = p->pot_model >= 4;
+    if (spc && p->precision != PIMD_FP64) return fail(E, PIMD_ERR_ARG, "the SPC models run in FP64 only");
     if (!(p->box[0] > 0 && p->box[1] > 0 && p->box[2] > 0)) return fail(E, PIMD_ERR_ARG, "box");
     const double lmin = std::min(p->box[0], std::min(p->box[1], p->box[2]));
     // InputOutput.f90:277-281: the cutoff may not exceed half the box
@@ -173,7 +193,8 @@ static int create(Engine &E, const pimd_params *p) {
     kp.model = p->pot_model;
     kp.natoms = p->natoms;
     kp.N = p->natoms / 3;
-    kp.S = 4 * kp.N;
+    kp.S = (spc ? 3 : 4) * kp.N;  // potential.f90:53-80: no M site in the SPC models
+    kp.fq = spc ? 0 : kp.N;
     kp.P = p->nbeads;
     for (int c = 0; c < 3; c++) {
         kp.box[c] = p->box[c];
@@ -187,7 +208,7 @@ static int create(Engine &E, const pimd_params *p) {
     kp.polar_maxiter = p->polar_maxiter;
     kp.polar_sor = p->polar_sor;
     kp.polar_eps = p->polar_eps;
-    const ModelSet &m = (p->pot_model == 2) ? TTM21F : TTM3F;
+    const ModelSet &m = (p->pot_model == 2) ? TTM21F : (p->pot_model == 3) ? TTM3F : (p->pot_model == 4) ? QSPCFW : SPCF;
     kp.vdwA = m.vdwA;
     kp.vdwB = m.vdwB;
     kp.vdwC = m.vdwC;
@@ -209,7 +230,17 @@ static int create(Engine &E, const pimd_params *p) {
         kp.shiftA = -(10 * Rc - 7 * r1) / (rc8 * ((Rc - r1) * (Rc - r1)));
         kp.shiftB = (9 * Rc - 7 * r1) / (rc8 * ((Rc - r1) * (Rc - r1) * (Rc - r1)));
     }
-    if (p->pot_model == 2) {
+    if (spc) {  // pot_mod.f90:29-44
+        const bool q = p->pot_model == 4;
+        kp.qO = q ? -0.84 : -0.82;
+        kp.qH = q ? 0.42 : 0.41;
+        kp.roh0 = q ? 1.012 : 1.0;
+        kp.th0 = q ? 1.95476876223364912614 : 1.91061193215819258784;
+        kp.harmkb = q ? 529.581 : 0.0;
+        kp.harmka = q ? 37.95 : 0.0;
+        kp.fd = kp.ld = 0;
+        kp.ndd = 0;
+    } else if (p->pot_model == 2) {
         kp.fd = 0;
         kp.ld = 3 * kp.N;
         kp.ndd = 9;
@@ -227,7 +258,7 @@ static int create(Engine &E, const pimd_params *p) {
     const double base[5] = {0, m.polfacO, m.polfacH, m.polfacH, m.polfacM};
     for (int i = 1; i <= 4; i++) {
         const double r = std::pow(base[i], 1.0 / 6.0);
-        pf[i] = 1.0 / (r * r * r);
+        pf[i] = spc ? 0.0 : 1.0 / (r * r * r);
     }
     for (int i = 1; i <= 4; i++)
         for (int j = 1; j <= 4; j++) {
@@ -252,8 +283,8 @@ static int create(Engine &E, const pimd_params *p) {
     E.cap = (size_t)std::max(1.0, std::min(all, std::max(1024.0, 3.0 * est)));
     kp.cap = (int)E.cap;
     const size_t P = kp.P, S = kp.S, N = kp.N;
-    const int nsq = kp.S - kp.N, nsd = kp.ld - kp.fd;
-    const size_t maxgroups = (size_t)std::max((nsq + 63) / 64, (nsd + 63) / 64);
+    const int nsq = kp.S - kp.fq, nsd = kp.ld - kp.fd;
+    const size_t maxgroups = (size_t)std::max((nsq + 31) / 32, (nsd + 31) / 32);  // 32-site tiles at most
     if ((rc = dalloc(E, (double **)&kp.RRt, P * kp.natoms * 3)) || (rc = dalloc(E, (double **)&kp.RRc, kp.natoms * 3)) ||
         (rc = dalloc(E, &kp.dRRt, P * kp.natoms * 3)) || (rc = dalloc(E, &kp.dipI, P * N * 3)) ||
         (rc = dalloc(E, &kp.dipE, P * N * 3)) || (rc = dalloc(E, &kp.chg, P * kp.natoms)) ||
@@ -265,6 +296,7 @@ static int create(Engine &E, const pimd_params *p) {
         (rc = dalloc(E, &kp.tab, P * kp.ntab * S)) || (rc = dalloc(E, &kp.Spart, P * maxgroups * kp.nk * 3)) ||
         (rc = dalloc(E, &kp.Sq, P * kp.nk)) || (rc = dalloc(E, &kp.Sm, P * kp.nk)) || (rc = dalloc(E, &kp.Sdip, P * kp.nk * 3)) ||
         (rc = dalloc(E, &kp.acc, P * NACC)) || (rc = dalloc(E, &kp.err, 1)) || (rc = dalloc(E, &kp.allconv, 1)) ||
+        (rc = dalloc(E, &kp.dstep, 2)) ||
         (rc = dalloc(E, &kp.nbrtmp, P * N)) || (rc = dalloc(E, &E.d_out, 3 * P + 16)) ||
         (rc = dalloc(E, &kp.Fpart, (size_t)E.max_slices * P * S)))
         return rc;
@@ -273,14 +305,17 @@ static int create(Engine &E, const pimd_params *p) {
         if ((rc = dalloc(E, &kp.tabf, P * kp.ntab * S)) || (rc = dalloc(E, &kp.posf, P * S)) ||
             (rc = dalloc(E, &kp.rhof, P * S)) || (rc = dalloc(E, &kp.fcnt, P * N)) || (rc = dalloc(E, &kp.foff, P * N)) ||
             (rc = dalloc(E, &kp.fnbr, P * (size_t)kp.fcap * 2)) || (rc = dalloc(E, &kp.fntot, P)) ||
-            (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd * 6)))
+            (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd * 6)) || (rc = dalloc(E, &kp.Wf, P * 2 * (size_t)kp.nk)))
             return rc;
     }
     cudaMemset(kp.txdip, 0, sizeof(double) * P * 4 * S * 3);
     cudaMemset(kp.Sm, 0, sizeof(double2) * P * kp.nk);
+    if (kp.Wf) cudaMemset(kp.Wf, 0, sizeof(float2) * P * 2 * kp.nk);
     cudaMemset(kp.err, 0, sizeof(unsigned));
     if ((rc = cuda_check(E, cudaMallocHost((void **)&E.h_allconv, sizeof(int)), "cudaMallocHost"))) return rc;
+    cudaMemset(kp.dstep, 0, sizeof(int) * 2);
     pot_init_constants(E);
+    ewald_init(E);
     return cuda_check(E, cudaDeviceSynchronize(), "init");
 }
 
@@ -346,13 +381,77 @@ void timer_end(Engine &E) {
         timer_end(E);     \
     } while (0)
 
+// One induced-dipole iteration (pot_ttm.f90:298-390): real-space dipole field, ewald_std_dd
+// structure factor, field + SOR update, convergence test.
+static void dipole_iteration(Engine &E, bool mixed) {
+    if (mixed)
+        PHASE("dd_real", launch_dd_real_m(E));
+    else
+        PHASE("dd_real", launch_dd_real(E));
+    PHASE("dd_smu", launch_ewald_smu(E));
+    PHASE("dd_update", launch_dd_update(E));
+    PHASE("dd_check", launch_dd_check(E));
+}
+
+// While capturing a CUDA graph: the dipole iterations become a conditional while node whose
+// body is one iteration; k_dd_check sets the condition on the device, so the loop runs with
+// no host round trip and stops at convergence (or polar_maxiter) exactly like the host loop.
+static int capture_dipole_loop(Engine &E, bool mixed) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(E.stream, &st, nullptr, &g, &deps, nullptr, &ndeps);
+    if (e != cudaSuccess) return cuda_check(E, e, "cudaStreamGetCaptureInfo");
+    if (st != cudaStreamCaptureStatusActive) return fail(E, PIMD_ERR_STATE, "dipole loop capture outside a capture");
+    cudaGraphConditionalHandle h;
+    e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return cuda_check(E, e, "cudaGraphConditionalHandleCreate");
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};  // aggregate init zeroes the rest
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp);
+    if (e != cudaSuccess) return cuda_check(E, e, "conditional node");
+    e = cudaStreamUpdateCaptureDependencies(E.stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return cuda_check(E, e, "cudaStreamUpdateCaptureDependencies");
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(E.body_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_check(E, e, "body capture");
+    cudaStream_t keep = E.stream;
+    E.stream = E.body_stream;
+    E.kp.cond = h;
+    dipole_iteration(E, mixed);
+    E.kp.cond = 0;
+    E.stream = keep;
+    cudaGraph_t out = nullptr;
+    e = cudaStreamEndCapture(E.body_stream, &out);
+    return cuda_check(E, e, "body capture end");
+}
+
 // One force call for all beads of the context (pot_ttm.f90:3-630 per bead).
 int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt, double *virialct, double *virt9) {
     KP &kp = E.kp;
     kp.t = t;
     cudaMemsetAsync(kp.acc, 0, sizeof(double) * kp.P * NACC, E.stream);
     cudaMemsetAsync(kp.err, 0, sizeof(unsigned), E.stream);
+    if (E.capturing)
+        cudaMemsetAsync(kp.dstep + 1, 0, sizeof(int), E.stream);  // t is set before each graph launch
+    else
+        launch_set_step(E, t);
     const bool mixed = E.precision == PIMD_MIXED;
+    if (kp.model >= 4) {  // pot_spc.f90: no induced dipoles
+        PHASE("sites", launch_sites_spc(E));
+        PHASE("neighbors", launch_neighbors(E));
+        PHASE("pair_qq", launch_pair_spc(E));
+        PHASE("ewald_tables", launch_ewald_tables(E));
+        PHASE("ewald_pw", launch_ewald_pw(E));
+        PHASE("finish", launch_finish_spc(E));
+        E.last_niter_max = 0;
+        PHASE("totals", launch_totals(E, Upott, virialt, virialct, virt9));
+        return cuda_check(E, cudaGetLastError(), "force kernels");
+    }
     PHASE("sites", launch_sites(E));
     if (mixed) {
         PHASE("site_offsets", launch_site_offsets(E));
@@ -366,23 +465,23 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
     PHASE("ewald_sq", launch_ewald_sq(E));
     PHASE("ewald_fq", launch_ewald_fq(E));
     PHASE("after_qq", launch_after_qq(E));
-    int iter = 1;
-    for (; iter <= kp.polar_maxiter; iter++) {
-        if (mixed)
-            PHASE("dd_real", launch_dd_real_m(E));
-        else
-            PHASE("dd_real", launch_dd_real(E));
-        PHASE("dd_smu", launch_ewald_smu(E));
-        PHASE("dd_update", launch_dd_update(E, iter));
-        PHASE("dd_check", launch_dd_check(E, iter));
-        if (check_every > 0 && (iter % check_every) == 0 && iter < kp.polar_maxiter) {
-            cudaMemcpyAsync(E.h_allconv, kp.allconv, sizeof(int), cudaMemcpyDeviceToHost, E.stream);
-            cudaError_t e = cudaStreamSynchronize(E.stream);
-            if (e != cudaSuccess) return cuda_check(E, e, "dipole iteration");
-            if (*E.h_allconv) break;
+    if (E.capturing) {
+        int rc = capture_dipole_loop(E, mixed);
+        if (rc) return rc;
+        E.last_niter_max = -1;  // known on the device only
+    } else {
+        int iter = 1;
+        for (; iter <= kp.polar_maxiter; iter++) {
+            dipole_iteration(E, mixed);
+            if (check_every > 0 && (iter % check_every) == 0 && iter < kp.polar_maxiter) {
+                cudaMemcpyAsync(E.h_allconv, kp.allconv, sizeof(int), cudaMemcpyDeviceToHost, E.stream);
+                cudaError_t e = cudaStreamSynchronize(E.stream);
+                if (e != cudaSuccess) return cuda_check(E, e, "dipole iteration");
+                if (*E.h_allconv) break;
+            }
         }
+        E.last_niter_max = std::min(iter, kp.polar_maxiter);
     }
-    E.last_niter_max = std::min(iter, kp.polar_maxiter);
     if (mixed)
         PHASE("pair_force", launch_pair_force_m(E));
     else
@@ -438,6 +537,8 @@ int pimd_destroy(pimd_ctx *ctx) {
     }
     if (E.h_allconv) cudaFreeHost(E.h_allconv);
     if (E.h_pin) cudaFreeHost(E.h_pin);
+    if (E.gexec) cudaGraphExecDestroy(E.gexec);
+    if (E.body_stream) cudaStreamDestroy(E.body_stream);
     if (E.own_stream && E.stream) cudaStreamDestroy(E.stream);
     delete ctx;
     return PIMD_OK;
@@ -446,7 +547,7 @@ int pimd_destroy(pimd_ctx *ctx) {
 int pimd_set_stream(pimd_ctx *ctx, void *s) {
     if (!ctx) return PIMD_ERR_ARG;
     Engine &E = ctx->E;
-    if (s) {
+    if (s && (cudaStream_t)s != E.stream) {
         if (E.own_stream && E.stream) cudaStreamDestroy(E.stream);
         E.stream = (cudaStream_t)s;
         E.own_stream = false;
@@ -561,9 +662,33 @@ int pimd_pot_ttm(pimd_ctx *ctx, const double *RR, const double *RRc, double *En,
     return rc;
 }
 
-int pimd_pot_spc(pimd_ctx *ctx, const double *, double *, double *, double *, double *, double *) {
-    if (!ctx) return PIMD_ERR_ARG;
-    return fail(ctx->E, PIMD_ERR_ARG, "context was not created for pot_model 4/5");
+int pimd_pot_spc(pimd_ctx *ctx, const double *RR, double *En, double *dRR, double *virt, double *dip_momI,
+                 double *chg) {
+    if (!ctx || !RR) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    if (E.kp.model < 4) return fail(E, PIMD_ERR_ARG, "context was not created for pot_model 4/5");
+    cudaSetDevice(E.device);
+    KP saved = E.kp;
+    E.kp.P = 1;  // bead-0 view of the context
+    const size_t na = E.kp.natoms, nw = E.kp.N;
+    cudaMemcpyAsync((void *)E.kp.RRt, RR, sizeof(double) * na * 3, cudaMemcpyHostToDevice, E.stream);
+    double *d_out = E.d_out;  // En, (unused), virt(9)
+    int rc = run_forces(E, 0, ctx->check_every, d_out, nullptr, nullptr, d_out + 2);
+    if (!rc) {
+        double h[11];
+        cudaMemcpyAsync(h, d_out, sizeof(h), cudaMemcpyDeviceToHost, E.stream);
+        if (dRR) cudaMemcpyAsync(dRR, E.kp.dRRt, sizeof(double) * na * 3, cudaMemcpyDeviceToHost, E.stream);
+        if (dip_momI) cudaMemcpyAsync(dip_momI, E.kp.dipI, sizeof(double) * nw * 3, cudaMemcpyDeviceToHost, E.stream);
+        if (chg) cudaMemcpyAsync(chg, E.kp.chg, sizeof(double) * na, cudaMemcpyDeviceToHost, E.stream);
+        rc = read_err(E);
+        if (!rc) {
+            if (En) *En = h[0];
+            if (virt) std::copy(h + 2, h + 11, virt);
+        }
+    }
+    cudaStreamSynchronize(E.stream);
+    E.kp = saved;
+    return rc;
 }
 
 int pimd_get_energies(pimd_ctx *ctx, int bead, double U[4]) {

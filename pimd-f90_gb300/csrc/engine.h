@@ -57,6 +57,7 @@ struct KChunk {
 struct KP {
     int model, N, S, P, natoms, cap, nk, nrun, nchunk, ntab, hmax, kmax, lmax;
     int fd, ld;          // dipole sites [fd, ld)
+    int fq;              // first site of the Ewald charge sums (TTM: N, O is uncharged; SPC: 0)
     int ndd;             // dipole site pairs per molecule pair (TTM3 1, TTM2 9)
     int contraction, guess, t, polar_maxiter, same_acd;
     double polar_eps;
@@ -80,6 +81,9 @@ struct KP {
     const double4_32a *kinfo;  // (kx, ky, kz) vector, 4pi Ak / V
     const double *kAk;     // Ak = 2 exp(-k^2/4a^2)/k^2
     const int2 *kidx;      // (run index, kz) of each k-vector
+    const float2 *runkf;   // FP32 (kx, ky) components of each run's k-vectors (mixed engine)
+    const float *kzf;      // FP32 kz component of each k-vector (mixed engine)
+    float2 *Wf;            // [P][2][nk] FP32 field weights 4pi Ak/V conj(S): slot 0 charge, 1 dipole
     int *nbrtmp;           // [P][N] neighbour counts / offsets
     // mixed-precision engine
     float2 *tabf;          // [P][ntab][S] FP32 copies of the FP64 recurrence tables
@@ -94,6 +98,8 @@ struct KP {
     double *acc;
     unsigned *err;
     int *allconv;
+    int *dstep;                   // [0] MD step t of the force call, [1] dipole iterations done
+    unsigned long long cond;      // CUDA-graph conditional handle of the dipole loop (0: host loop)
 };
 
 // Named phase timers (the reference's dans_timer.f90 start_timer/stop_timer), recorded as
@@ -118,6 +124,8 @@ struct Engine {
     bool own_stream = false;
     int nchunk = 0, ntile_q = 0, ntile_d = 0, max_runs_chunk = 0;
     int max_slices = 16;  // k-slices of the Ewald field passes (Fpart capacity)
+    bool sf_tiled = true;  // mixed engine: register-tiled structure factors (k_sfac_f)
+    int sf_groups = 0;     // site groups of k_sfac_f (0: sized from the SM count)
     size_t cap = 0;
     std::vector<KRun> h_runs;
     std::vector<KChunk> h_chunks;
@@ -133,6 +141,14 @@ struct Engine {
     std::string last_error;
     int last_niter_max = 0;
     long long nlaunch = 0;  // kernels launched by this context
+    // CUDA-graph execution of the MD step (pimd_set_graph): captured once per set of device
+    // pointers and replayed; the dipole iterations run in a conditional while node
+    bool graph_mode = false;
+    bool capturing = false;
+    cudaStream_t body_stream = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<const void *> gkey;
+    long long graph_launches = 0, graph_captures = 0;
     // normal modes (filled by pimd_nm_init)
     int nm_P = 0;
     double *d_nmC = nullptr, *d_nmA = nullptr;  // C(P,P), [A11,A12,A21,A22,msf,c1,c2] x P
@@ -152,8 +168,9 @@ void launch_sites(Engine &E);
 void launch_pair_qq(Engine &E);
 void launch_after_qq(Engine &E);
 void launch_dd_real(Engine &E);
-void launch_dd_update(Engine &E, int iter);
-void launch_dd_check(Engine &E, int iter);
+void launch_dd_update(Engine &E);
+void launch_dd_check(Engine &E);
+void launch_set_step(Engine &E, int t);
 void launch_pair_force(Engine &E);
 void launch_finish(Engine &E);
 void launch_totals(Engine &E, double *Upott, double *virialt, double *virialct, double *virt9);
@@ -163,11 +180,17 @@ void launch_pair_qq_m(Engine &E);
 void launch_dd_real_m(Engine &E);
 void launch_pair_force_m(Engine &E);
 // launchers (ewald.cu)
+void ewald_init(Engine &E);
 void launch_ewald_tables(Engine &E);
 void launch_ewald_sq(Engine &E);
 void launch_ewald_fq(Engine &E);
 void launch_ewald_smu(Engine &E);
 void launch_ewald_qd(Engine &E);
+void launch_ewald_pw(Engine &E);
+// launchers (spc.cu): q-SPC/Fw and SPC/F
+void launch_sites_spc(Engine &E);
+void launch_pair_spc(Engine &E);
+void launch_finish_spc(Engine &E);
 
 }  // namespace pimd
 

@@ -90,6 +90,29 @@ __global__ void __launch_bounds__(128) k_ewald_tables(KP kp) {
     }
 }
 
+// k-vector components in the arithmetic type of the phase sums: FP64 from kinfo, FP32 from
+// the precomputed FP32 tables (no double-to-float conversion inside the mixed kernels)
+template <typename R>
+struct KV;
+template <>
+struct KV<double> {
+    PIMD_D static void run_xy(const KP &kp, int r, double &x, double &y) {
+        const double4_32a v = kp.kinfo[kp.runs[r].kbeg];
+        x = v.x;
+        y = v.y;
+    }
+    PIMD_D static double z(const KP &kp, int k) { return kp.kinfo[k].z; }
+};
+template <>
+struct KV<float> {
+    PIMD_D static void run_xy(const KP &kp, int r, float &x, float &y) {
+        const float2 v = kp.runkf[r];
+        x = v.x;
+        y = v.y;
+    }
+    PIMD_D static float z(const KP &kp, int k) { return kp.kzf[k]; }
+};
+
 enum { OP_Q = 0, OP_MU = 1, OP_DIP = 2 };
 constexpr int SP_NT = 256;  // threads (k-vectors) per structure-factor block
 constexpr int SP_TS = 64;   // sites per shared-memory tile
@@ -135,7 +158,7 @@ __global__ void __launch_bounds__(SP_NT) k_spass(KP kp, int s0, int nsites, int 
         const int2 ki = kp.kidx[k];
         rk = ki.x - ch.r0;
         kz = ki.y;
-        kzv = R(kp.kinfo[k].z);
+        kzv = KV<R>::z(kp, k);
     }
     V acc[NC];
 #pragma unroll
@@ -169,8 +192,9 @@ __global__ void __launch_bounds__(SP_NT) k_spass(KP kp, int s0, int nsites, int 
             // ewald.f90:30-31: coskxky = cx cy - sx sy, sinkxky = sx cy + cx sy
             exy[site * nr + r] = C2<R>::make(ex.x * ey.x - ex.y * ey.y, ex.y * ey.x + ex.x * ey.y);
             if (OP == OP_MU) {
-                const double4_32a kv = kp.kinfo[run.kbeg];
-                aa[site * nr + r] = R(kv.x) * wt[4 * site] + R(kv.y) * wt[4 * site + 1];
+                R kx, ky;
+                KV<R>::run_xy(kp, ch.r0 + r, kx, ky);
+                aa[site * nr + r] = kx * wt[4 * site] + ky * wt[4 * site + 1];
             }
         }
         __syncthreads();
@@ -205,6 +229,157 @@ __global__ void __launch_bounds__(SP_NT) k_spass(KP kp, int s0, int nsites, int 
     }
 }
 
+// Register-tiled FP32 structure factors of the mixed engine. With e^{ik.r} = exy(kx,ky) ez(kz)
+// every structure factor is a set of M small complex GEMMs over the sites of a group,
+//   G_m[run][kz] = sum_s A_m[s][run] ez[s][kz],   A_m = w_m exy(run)
+// (OP_Q: w = q; OP_MU: w = kx mu_x + ky mu_y and mu_z, S = G_0 + k_z G_1; OP_DIP: w = mu_c).
+// A block owns SF_RT runs of one bead and one site group; a thread owns SF_TR runs x SF_TK kz
+// slots (all M products) in registers, so each site costs 2-3 128-bit shared loads of A and a
+// broadcast of ez for SF_TR * SF_TK * M complex multiply-adds. kz slots outside a run's sphere
+// are computed and dropped. Partials per site group go to Spart like k_spass's.
+constexpr int SF_NRP = 32;               // run groups per block (one warp across)
+constexpr int SF_TR = 2;                 // runs per thread
+constexpr int SF_RT = SF_NRP * SF_TR;    // runs per block
+constexpr int SF_TK = 5;                 // kz slots per thread
+constexpr int SF_TS = 32;                // sites per shared-memory tile
+constexpr int SF_MAXT = 320;             // threads per block for 2 lmax + 1 <= 50
+
+template <int OP>
+__global__ void __launch_bounds__(SF_MAXT) k_sfac_f(KP kp, int s0, int nsites, int tsg, int ngroups, int skipconv) {
+    constexpr int M = (OP == OP_Q) ? 1 : (OP == OP_MU) ? 2 : 3;
+    constexpr int NC = (OP == OP_DIP) ? 3 : 1;
+    const int b = blockIdx.z;
+    if (skipconv && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
+    const int grp = blockIdx.y;
+    const int r0 = blockIdx.x * SF_RT;
+    const int nr = min(SF_RT, kp.nrun - r0);
+    const int L = kp.lmax, LZ = 2 * L + 1;
+    const int nkg = (LZ + SF_TK - 1) / SF_TK, KZP = nkg * SF_TK;
+    const int tid = threadIdx.x, rp = tid % SF_NRP, kg = tid / SF_NRP;
+    extern __shared__ float4 smf[];
+    float2 *A = reinterpret_cast<float2 *>(smf);  // [TS][RT][M]
+    float2 *ez = A + SF_TS * SF_RT * M;            // [TS][KZP]
+    float4 *wt = reinterpret_cast<float4 *>(ez + SF_TS * KZP);  // [TS]
+    __shared__ int2 rxy[SF_RT];
+    __shared__ float2 rkv[SF_RT];
+    if (tid < SF_RT) {
+        if (tid < nr) {
+            const KRun run = kp.runs[r0 + tid];
+            rxy[tid] = make_int2(run.kx, run.ky);
+            rkv[tid] = kp.runkf[r0 + tid];
+        } else {
+            rxy[tid] = make_int2(0, 0);
+            rkv[tid] = make_float2(0.f, 0.f);
+        }
+    }
+    float2 acc[SF_TR][SF_TK][M];
+#pragma unroll
+    for (int i = 0; i < SF_TR; i++)
+#pragma unroll
+        for (int j = 0; j < SF_TK; j++)
+#pragma unroll
+            for (int m = 0; m < M; m++) acc[i][j][m] = make_float2(0.f, 0.f);
+    const int gbeg = s0 + grp * tsg, gend = min(s0 + nsites, gbeg + tsg);
+    for (int sb = gbeg; sb < gend; sb += SF_TS) {
+        const int nloc = min(SF_TS, gend - sb);
+        __syncthreads();
+        if (tid < SF_TS) {
+            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (tid < nloc) {
+                const size_t gs = (size_t)b * kp.S + sb + tid;
+                if (OP == OP_Q)
+                    w.x = (float)kp.pos[gs].w;
+                else
+                    w = make_float4((float)kp.dip[3 * gs], (float)kp.dip[3 * gs + 1], (float)kp.dip[3 * gs + 2], 0.f);
+            }
+            wt[tid] = w;
+        }
+        for (int idx = tid; idx < SF_TS * KZP; idx += blockDim.x) {
+            const int site = idx / KZP, j = idx - site * KZP, kz = j - L;
+            float2 v = make_float2(0.f, 0.f);
+            if (site < nloc && j < LZ) {
+                v = tab_z<float>(kp, b, kz < 0 ? -kz : kz, sb + site);
+                if (kz < 0) v = cconj(v);
+            }
+            ez[idx] = v;
+        }
+        __syncthreads();
+        for (int idx = tid; idx < SF_TS * SF_RT; idx += blockDim.x) {
+            const int site = idx % SF_TS, r = idx / SF_TS;
+            float2 a[M];
+#pragma unroll
+            for (int m = 0; m < M; m++) a[m] = make_float2(0.f, 0.f);
+            if (site < nloc && r < nr) {
+                const int2 xy = rxy[r];
+                const float2 ex = tab_x<float>(kp, b, xy.x, sb + site);
+                const float2 ey = tab_y<float>(kp, b, xy.y, sb + site);
+                // ewald.f90:30-31: coskxky = cx cy - sx sy, sinkxky = sx cy + cx sy
+                const float2 exy = make_float2(ex.x * ey.x - ex.y * ey.y, ex.y * ey.x + ex.x * ey.y);
+                const float4 w = wt[site];
+                if (OP == OP_Q) {
+                    a[0] = make_float2(w.x * exy.x, w.x * exy.y);
+                } else if (OP == OP_MU) {
+                    const float2 kv = rkv[r];
+                    const float t = kv.x * w.x + kv.y * w.y;
+                    a[0] = make_float2(t * exy.x, t * exy.y);
+                    a[M - 1] = make_float2(w.z * exy.x, w.z * exy.y);
+                } else {
+                    a[0] = make_float2(w.x * exy.x, w.x * exy.y);
+                    a[1] = make_float2(w.y * exy.x, w.y * exy.y);
+                    a[M - 1] = make_float2(w.z * exy.x, w.z * exy.y);
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < M; m++) A[(site * SF_RT + r) * M + m] = a[m];
+        }
+        __syncthreads();
+        if (kg < nkg) {
+            for (int site = 0; site < nloc; site++) {
+                float2 a[SF_TR][M], e[SF_TK];
+                const float2 *ap = A + (site * SF_RT + rp * SF_TR) * M;
+#pragma unroll
+                for (int i = 0; i < SF_TR; i++)
+#pragma unroll
+                    for (int m = 0; m < M; m++) a[i][m] = ap[i * M + m];
+                const float2 *ep = ez + site * KZP + kg * SF_TK;
+#pragma unroll
+                for (int j = 0; j < SF_TK; j++) e[j] = ep[j];
+#pragma unroll
+                for (int i = 0; i < SF_TR; i++)
+#pragma unroll
+                    for (int j = 0; j < SF_TK; j++)
+#pragma unroll
+                        for (int m = 0; m < M; m++) {
+                            // ewald.f90:37-39: coskr = cxy cz - sxy sz, sinkr = sxy cz + cxy sz
+                            acc[i][j][m].x += a[i][m].x * e[j].x - a[i][m].y * e[j].y;
+                            acc[i][j][m].y += a[i][m].y * e[j].x + a[i][m].x * e[j].y;
+                        }
+            }
+        }
+    }
+    if (kg >= nkg) return;
+#pragma unroll
+    for (int i = 0; i < SF_TR; i++) {
+        const int r = rp * SF_TR + i;
+        if (r >= nr) continue;
+        const KRun run = kp.runs[r0 + r];
+#pragma unroll
+        for (int j = 0; j < SF_TK; j++) {
+            const int kz = kg * SF_TK + j - L;
+            if (kz < run.kzlo || kz >= run.kzlo + run.nkz) continue;
+            const int k = run.kbeg + kz - run.kzlo;
+            float2 *out = reinterpret_cast<float2 *>(kp.Spart) + (((size_t)b * ngroups + grp) * kp.nk + k) * NC;
+            if (OP == OP_MU) {
+                const float kzv = kp.kzf[k];
+                out[0] = make_float2(acc[i][j][0].x + kzv * acc[i][j][M - 1].x, acc[i][j][0].y + kzv * acc[i][j][M - 1].y);
+            } else {
+#pragma unroll
+                for (int c = 0; c < NC; c++) out[c] = acc[i][j][c];
+            }
+        }
+    }
+}
+
 // Sum the tile partials in FP64 in a fixed order. OP_MU stores (rQm, iQm) = (-Im, Re) of
 // sum (k.mu) e (ewald.f90:106-107).
 template <int OP, typename R>
@@ -228,6 +403,12 @@ __global__ void __launch_bounds__(256) k_sreduce(KP kp, int ngroups, int skipcon
     }
     if (OP == OP_Q) kp.Sq[(size_t)b * kp.nk + k] = s[0];
     if (OP == OP_MU) kp.Sm[(size_t)b * kp.nk + k] = make_double2(-s[0].y, s[0].x);
+    if (sizeof(R) == 4 && OP != OP_DIP) {
+        // FP32 field weights 4 pi Ak / V conj(S) of the mixed engine's field passes
+        const double w = kp.kinfo[k].w;
+        const double2 a = (OP == OP_Q) ? s[0] : make_double2(-s[0].y, s[0].x);
+        kp.Wf[((size_t)b * 2 + (OP == OP_Q ? 0 : 1)) * kp.nk + k] = make_float2((float)(w * a.x), (float)(-w * a.y));
+    }
     if (OP == OP_DIP)
 #pragma unroll
         for (int c = 0; c < 3; c++) kp.Sdip[((size_t)b * kp.nk + k) * 3 + c] = s[c];
@@ -285,14 +466,21 @@ __global__ void __launch_bounds__(NT) k_field(KP kp, int s0, int s1) {
         __syncthreads();
         for (int i = threadIdx.x; i < ch.k1 - ch.k0; i += NT) {
             const int k = ch.k0 + i;
-            const double4_32a ki = kp.kinfo[k];
-            const double2 a = S1[(size_t)b * kp.nk + k];
-            W1[i] = C2<R>::make(R(ki.w * a.x), R(-ki.w * a.y));  // 4 pi Ak / V conj(S)
-            if (MODE == F_QD) {
-                const double2 c = kp.Sq[(size_t)b * kp.nk + k];
-                W2[i] = C2<R>::make(R(ki.w * (c.x + a.x)), R(-ki.w * (c.y + a.y)));
+            if constexpr (sizeof(R) == 4) {
+                const float2 wq = kp.Wf[((size_t)b * 2) * kp.nk + k], wm = kp.Wf[((size_t)b * 2 + 1) * kp.nk + k];
+                W1[i] = (MODE == F_Q) ? wq : wm;
+                if (MODE == F_QD) W2[i] = make_float2(wq.x + wm.x, wq.y + wm.y);
+                kzs[i] = kp.kzf[k];
+            } else {
+                const double4_32a ki = kp.kinfo[k];
+                const double2 a = S1[(size_t)b * kp.nk + k];
+                W1[i] = C2<R>::make(R(ki.w * a.x), R(-ki.w * a.y));  // 4 pi Ak / V conj(S)
+                if (MODE == F_QD) {
+                    const double2 c = kp.Sq[(size_t)b * kp.nk + k];
+                    W2[i] = C2<R>::make(R(ki.w * (c.x + a.x)), R(-ki.w * (c.y + a.y)));
+                }
+                kzs[i] = R(ki.z);
             }
-            kzs[i] = R(ki.z);
         }
         __syncthreads();
         if (!valid) continue;
@@ -300,8 +488,8 @@ __global__ void __launch_bounds__(NT) k_field(KP kp, int s0, int s1) {
         R cE[3] = {R(0), R(0), R(0)}, cphi = R(0), cG[3] = {R(0), R(0), R(0)};
         for (int r = ch.r0; r < ch.r1; r++) {
             const KRun run = kp.runs[r];
-            const double4_32a kvd = kp.kinfo[run.kbeg];
-            const R kvx = R(kvd.x), kvy = R(kvd.y);
+            R kvx, kvy;
+            KV<R>::run_xy(kp, r, kvx, kvy);
             const V ex = tab_x<R>(kp, b, run.kx, s);
             const V ey = tab_y<R>(kp, b, run.ky, s);
             const V exy = C2<R>::make(ex.x * ey.x - ex.y * ey.y, ex.y * ey.x + ex.x * ey.y);
@@ -365,8 +553,9 @@ __global__ void __launch_bounds__(NT) k_field(KP kp, int s0, int s1) {
 
 // Sum the slices of k_field in order and apply the pass's epilogue, one thread per site.
 template <int MODE, int NT>
-__global__ void __launch_bounds__(NT) k_field_finish(KP kp, int s0, int s1, int nslice, int iter) {
+__global__ void __launch_bounds__(NT) k_field_finish(KP kp, int s0, int s1, int nslice) {
     const int b = blockIdx.y;
+    const int iter = kp.dstep[1] + 1;  // dipole iteration of this update (F_D)
     if (MODE == F_D && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
     const int s = s0 + blockIdx.x * NT + threadIdx.x;
     const bool valid = s < s1;
@@ -387,12 +576,12 @@ __global__ void __launch_bounds__(NT) k_field_finish(KP kp, int s0, int s1, int 
             f.x += E[0];
             f.y += E[1];
             f.z += E[2];
-            if (s >= kp.N) f.w += phi;
+            if (s >= kp.fq) f.w += phi;
             kp.F[gs] = f;
         }
     } else if (MODE == F_QD) {
         if (valid) {
-            if (s >= kp.N) kp.F[gs].w += phi;
+            if (s >= kp.fq) kp.F[gs].w += phi;
             kp.dR[3 * gs + 0] += E[0];
             kp.dR[3 * gs + 1] += E[1];
             kp.dR[3 * gs + 2] += E[2];
@@ -440,7 +629,10 @@ __global__ void __launch_bounds__(NT) k_field_finish(KP kp, int s0, int s1, int 
     }
 }
 
-// ewald.f90:194-224: reciprocal-space virial, one thread per (k, bead), FP64
+// Reciprocal-space virial, one thread per (k, bead), FP64. DIP: ewald.f90:194-224 (charges
+// and induced dipoles, also the centroid-virial trace); !DIP: ewald.f90:276-289
+// (ewald_pw_std_qq, charges only).
+template <bool DIP>
 __global__ void __launch_bounds__(128) k_qd_virial(KP kp) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     double av[14];
@@ -450,17 +642,20 @@ __global__ void __launch_bounds__(128) k_qd_virial(KP kp) {
         const double4_32a ki = kp.kinfo[k];
         const double kv[3] = {ki.x, ki.y, ki.z};
         const double Akk = kp.kAk[k];
-        const double2 sq = kp.Sq[(size_t)b * kp.nk + k], sm = kp.Sm[(size_t)b * kp.nk + k];
+        const double2 sq = kp.Sq[(size_t)b * kp.nk + k];
+        const double2 sm = DIP ? kp.Sm[(size_t)b * kp.nk + k] : make_double2(0.0, 0.0);
         const double rQqm = sq.x + sm.x, iQqm = sq.y + sm.y;
         const double ksq = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
         const double coeff2 = 2.0 / ksq + 0.5 / (kp.ew.aewald * kp.ew.aewald);
         const double Ureck = Akk * (rQqm * rQqm + iQqm * iQqm);
         double rdip[3] = {0, 0, 0}, idip[3] = {0, 0, 0};
+        if (DIP) {
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const double2 d = kp.Sdip[((size_t)b * kp.nk + k) * 3 + c];
-            rdip[c] = -d.y;
-            idip[c] = d.x;
+            for (int c = 0; c < 3; c++) {
+                const double2 d = kp.Sdip[((size_t)b * kp.nk + k) * 3 + c];
+                rdip[c] = -d.y;
+                idip[c] = d.x;
+            }
         }
         const double sc = -0.5 * FOURPI / kp.volume;
 #pragma unroll
@@ -471,7 +666,7 @@ __global__ void __launch_bounds__(128) k_qd_virial(KP kp) {
                 const double v1 = 2.0 * Akk * kv[a] * (rQqm * rdip[bb] + iQqm * idip[bb]);
                 av[ACC_VIRT + a + 3 * bb] = sc * (v + v1);
             }
-        av[ACC_VIRIALC] = av[ACC_VIRT + 0] + av[ACC_VIRT + 4] + av[ACC_VIRT + 8];
+        if (DIP) av[ACC_VIRIALC] = av[ACC_VIRT + 0] + av[ACC_VIRT + 4] + av[ACC_VIRT + 8];
     }
     block_reduce_add<14, 128>(av, kp.acc + (size_t)b * NACC);
 }
@@ -494,11 +689,6 @@ static void run_spass_t(Engine &E, int s0, int nsites, int skipconv) {
     const int ngr = (nsites + tsg - 1) / tsg;
     const int LZ = 2 * E.kp.lmax + 1;
     const size_t smem = ((size_t)SP_TS * LZ * 2 + (size_t)SP_TS * E.max_runs_chunk * 3 + (size_t)SP_TS * 4) * sizeof(R);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_spass<OP, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
-    }
     dim3 g(E.nchunk, ngr, E.kp.P);
     k_spass<OP, R><<<g, SP_NT, smem, E.stream>>>(E.kp, s0, nsites, tsg, ngr, skipconv);
     ++E.nlaunch;
@@ -507,23 +697,45 @@ static void run_spass_t(Engine &E, int s0, int nsites, int skipconv) {
     ++E.nlaunch;
 }
 
+// the mixed engine's register-tiled structure factor; site groups of whole 32-site tiles sized
+// for about 8 blocks of 160-320 threads per SM
+template <int OP>
+static void run_sfac_f(Engine &E, int s0, int nsites, int skipconv) {
+    const KP &kp = E.kp;
+    constexpr int M = (OP == OP_Q) ? 1 : (OP == OP_MU) ? 2 : 3;
+    const int LZ = 2 * kp.lmax + 1, nkg = (LZ + SF_TK - 1) / SF_TK, KZP = nkg * SF_TK;
+    const int rtiles = (kp.nrun + SF_RT - 1) / SF_RT;
+    const int ntile = (nsites + SF_TS - 1) / SF_TS;
+    const long per = (long)rtiles * kp.P;
+    int ng = E.sf_groups > 0 ? E.sf_groups : (int)((152L * 8 + per - 1) / per);
+    ng = std::max(1, std::min(ng, ntile));
+    const int tsg = ((ntile + ng - 1) / ng) * SF_TS;
+    const int ngr = (nsites + tsg - 1) / tsg;
+    const size_t smem = sizeof(float2) * ((size_t)SF_TS * SF_RT * M + (size_t)SF_TS * KZP) + sizeof(float4) * SF_TS;
+    dim3 g(rtiles, ngr, kp.P);
+    k_sfac_f<OP><<<g, SF_NRP * nkg, smem, E.stream>>>(E.kp, s0, nsites, tsg, ngr, skipconv);
+    ++E.nlaunch;
+    dim3 g2((kp.nk + 255) / 256, kp.P);
+    k_sreduce<OP, float><<<g2, 256, 0, E.stream>>>(E.kp, ngr, skipconv);
+    ++E.nlaunch;
+}
+
 template <int OP>
 static void run_spass(Engine &E, int s0, int nsites, int skipconv) {
-    if (E.precision == PIMD_PREC_MIXED)
-        run_spass_t<OP, float>(E, s0, nsites, skipconv);
-    else
+    if (E.precision == PIMD_PREC_MIXED) {
+        if (E.sf_tiled && 2 * E.kp.lmax + 1 <= SF_TK * (SF_MAXT / SF_NRP))
+            run_sfac_f<OP>(E, s0, nsites, skipconv);
+        else
+            run_spass_t<OP, float>(E, s0, nsites, skipconv);
+    } else {
         run_spass_t<OP, double>(E, s0, nsites, skipconv);
+    }
 }
 
 template <int MODE, int NT, typename R>
-static void launch_field_nt(Engine &E, int s0, int s1, int iter) {
+static void launch_field_nt(Engine &E, int s0, int s1) {
     const int LZ = 2 * E.kp.lmax + 1;
     const size_t smem = ((size_t)LZ * NT * 2 + (size_t)KCH * 5) * sizeof(R);
-    static bool set = false;
-    if (!set) {
-        cudaFuncSetAttribute(k_field<MODE, NT, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        set = true;
-    }
     // k-slices: enough blocks for ~8 (FP32) / ~4 (FP64) resident blocks per SM
     const int sblocks = (s1 - s0 + NT - 1) / NT;
     const long want = (sizeof(R) == 4 ? 8L : 4L) * 152;
@@ -532,24 +744,47 @@ static void launch_field_nt(Engine &E, int s0, int s1, int iter) {
     dim3 g(sblocks, E.kp.P, ns);
     k_field<MODE, NT, R><<<g, NT, smem, E.stream>>>(E.kp, s0, s1);
     dim3 g2((s1 - s0 + 127) / 128, E.kp.P);
-    k_field_finish<MODE, 128><<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns, iter);
+    k_field_finish<MODE, 128><<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns);
     E.nlaunch += 2;
 }
 
 template <int MODE>
-static void run_field(Engine &E, int s0, int s1, int iter) {
+static void run_field(Engine &E, int s0, int s1) {
     const int LZ = 2 * E.kp.lmax + 1;
     if (E.precision == PIMD_PREC_MIXED) {
         if ((size_t)LZ * 128 * 8 <= 64 * 1024)
-            launch_field_nt<MODE, 128, float>(E, s0, s1, iter);
+            launch_field_nt<MODE, 128, float>(E, s0, s1);
         else
-            launch_field_nt<MODE, 64, float>(E, s0, s1, iter);
+            launch_field_nt<MODE, 64, float>(E, s0, s1);
     } else {
         if ((size_t)LZ * 128 * 16 <= 64 * 1024)
-            launch_field_nt<MODE, 128, double>(E, s0, s1, iter);
+            launch_field_nt<MODE, 128, double>(E, s0, s1);
         else
-            launch_field_nt<MODE, 64, double>(E, s0, s1, iter);
+            launch_field_nt<MODE, 64, double>(E, s0, s1);
     }
+}
+
+// dynamic shared-memory limits of the Ewald kernels, set once per context on its device
+template <typename R>
+static void ewald_attrs() {
+    const int lim = 200 * 1024;
+    cudaFuncSetAttribute(k_spass<OP_Q, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_spass<OP_MU, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_spass<OP_DIP, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_field<F_Q, 128, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_field<F_D, 128, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_field<F_QD, 128, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_field<F_Q, 64, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_field<F_D, 64, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_field<F_QD, 64, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+}
+void ewald_init(Engine &E) {
+    (void)E;
+    ewald_attrs<double>();
+    ewald_attrs<float>();
+    cudaFuncSetAttribute(k_sfac_f<OP_Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    cudaFuncSetAttribute(k_sfac_f<OP_MU>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    cudaFuncSetAttribute(k_sfac_f<OP_DIP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
 }
 
 void launch_ewald_tables(Engine &E) {
@@ -561,28 +796,32 @@ void launch_ewald_tables(Engine &E) {
     ++E.nlaunch;
 }
 
+// first site whose charge field is read: TTM3-F never reads the O-site field (no charge, no
+// dipole); TTM2.1-F polarises O; the SPC models charge O
+static int field_s0(const Engine &E) { return (E.kp.model == 3) ? E.kp.N : 0; }
+
 // ewald_std_qq: S(k) over the charged sites, then the field at the sites that need it
-void launch_ewald_sq(Engine &E) {
-    const int N = E.kp.N;
-    run_spass<OP_Q>(E, N, E.kp.S - N, 0);
-}
-void launch_ewald_fq(Engine &E) {
-    const int N = E.kp.N;
-    // TTM3-F never reads the O-site field (no charge, no dipole); TTM2.1-F polarises O
-    const int s0 = (E.kp.model == 2) ? 0 : N;
-    run_field<F_Q>(E, s0, E.kp.S, 0);
-}
+void launch_ewald_sq(Engine &E) { run_spass<OP_Q>(E, E.kp.fq, E.kp.S - E.kp.fq, 0); }
+void launch_ewald_fq(Engine &E) { run_field<F_Q>(E, field_s0(E), E.kp.S); }
 // one induced-dipole iteration's reciprocal part (ewald_std_dd) fused with the update
 void launch_ewald_smu(Engine &E) { run_spass<OP_MU>(E, E.kp.fd, E.kp.ld - E.kp.fd, 1); }
-void launch_dd_update(Engine &E, int iter) { run_field<F_D>(E, E.kp.fd, E.kp.ld, iter); }
+void launch_dd_update(Engine &E) { run_field<F_D>(E, E.kp.fd, E.kp.ld); }
 // ewald_std_qd
 void launch_ewald_qd(Engine &E) {
     run_spass<OP_DIP>(E, E.kp.fd, E.kp.ld - E.kp.fd, 0);
     dim3 g((E.kp.nk + 127) / 128, E.kp.P);
-    k_qd_virial<<<g, 128, 0, E.stream>>>(E.kp);
+    k_qd_virial<true><<<g, 128, 0, E.stream>>>(E.kp);
     ++E.nlaunch;
-    const int s0 = (E.kp.model == 2) ? 0 : E.kp.N;
-    run_field<F_QD>(E, s0, E.kp.S, 0);
+    run_field<F_QD>(E, field_s0(E), E.kp.S);
+}
+// ewald_pw_std_qq (ewald.f90:230-291): charge structure factor over all sites, field and
+// potential at all sites, reciprocal virial
+void launch_ewald_pw(Engine &E) {
+    launch_ewald_sq(E);
+    launch_ewald_fq(E);
+    dim3 g((E.kp.nk + 127) / 128, E.kp.P);
+    k_qd_virial<false><<<g, 128, 0, E.stream>>>(E.kp);
+    ++E.nlaunch;
 }
 
 }  // namespace pimd

@@ -45,13 +45,16 @@ struct NMArgs {
     int langevin, evolve;
     const double *xi;   // (3, P, Natoms) standard normals, or null
     unsigned long long seed, counter;
+    const int *tstep;   // device step word: when set, counter = 2 t + phase
+    int phase;
 };
 
 PIMD_D double noise(const NMArgs &a, int atom, int j, int c) {
     if (a.xi) return a.xi[c + 3 * j + (size_t)3 * a.P * atom];
     const unsigned long long idx = ((unsigned long long)atom * a.P + j) * 3 + c;
-    const uint4 r = philox4x32(make_uint4((unsigned)idx, (unsigned)(idx >> 32), (unsigned)a.counter,
-                                          (unsigned)(a.counter >> 32)),
+    const unsigned long long ctr = a.tstep ? 2ull * (unsigned long long)(long long)a.tstep[0] + (unsigned long long)a.phase
+                                           : a.counter;
+    const uint4 r = philox4x32(make_uint4((unsigned)idx, (unsigned)(idx >> 32), (unsigned)ctr, (unsigned)(ctr >> 32)),
                                make_uint2((unsigned)a.seed, (unsigned)(a.seed >> 32)));
     return gauss_from(r.x, r.y);
 }
@@ -432,23 +435,24 @@ int pimd_langevin_nm_device(pimd_ctx *ctx, double *PPt, const double *xi, double
     return nm_err(E, cudaGetLastError(), "langevin_nm");
 }
 
-int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,
-                        const double *xi1, const double *xi2, int t, double *out4) {
-    if (!ctx || !mp || !RRt || !PPt || !dRRt || !RRc) return PIMD_ERR_ARG;
+// Enqueue one PIMD_VV step on the context's stream (everything but the step word, which the
+// force call or the graph launcher sets).
+static int md_step_enqueue(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
+                           double *RRc, const double *xi1, const double *xi2, int t, double *out4) {
     Engine &E = ctx->E;
-    if (E.nm_P != E.kp.P) return PIMD_ERR_STATE;
-    cudaSetDevice(E.device);
     NMArgs a = nm_args(E, mp->massO, mp->massH);
     a.delt = mp->delt;
     a.delt2 = mp->delt / 2.0;
     a.langevin = mp->langevin;
     a.evolve = E.kp.P > 1;
     a.seed = mp->seed;
-    a.counter = 2ull * (unsigned long long)t;
+    a.tstep = E.kp.dstep;
+    a.phase = 0;
     a.xi = xi1;
     int threads, blocks;
     size_t smem;
     nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
+    if (!E.capturing) launch_set_step(E, t);  // the Langevin counter of k_md_pre reads t
     timer_begin(E, "md_pre");
     k_md_pre<<<blocks, threads, smem, E.stream>>>(a, RRt, PPt, dRRt, RRc); ++E.nlaunch;
     timer_end(E);
@@ -465,7 +469,7 @@ int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, do
     double *uk = d + 3 * E.kp.P;
     cudaMemsetAsync(uk, 0, sizeof(double), E.stream);
     a.xi = xi2;
-    a.counter = 2ull * (unsigned long long)t + 1ull;
+    a.phase = 1;
     timer_begin(E, "md_post");
     k_md_post<<<blocks, threads, smem, E.stream>>>(a, PPt, dRRt, uk); ++E.nlaunch;
     if (out4) {
@@ -474,6 +478,86 @@ int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, do
     }
     timer_end(E);
     return nm_err(E, cudaGetLastError(), "md_step");
+}
+
+// Graph mode: the step is captured once per set of buffers and parameters (the dipole loop as a
+// conditional while node) and replayed; only the step word is written before each launch.
+static int md_step_graph(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
+                         double *RRc, const double *xi1, const double *xi2, int t, double *out4) {
+    Engine &E = ctx->E;
+    double mpv[3] = {mp->delt, mp->massO, mp->massH};
+    std::vector<const void *> key = {RRt, PPt, dRRt, RRc, xi1, xi2, out4, (const void *)(size_t)mp->langevin,
+                                     (const void *)(size_t)mp->seed};
+    for (double v : mpv) {
+        unsigned long long u;
+        std::memcpy(&u, &v, sizeof u);
+        key.push_back((const void *)(size_t)u);
+    }
+    if (!E.gexec || key != E.gkey) {
+        if (E.gexec) {
+            cudaGraphExecDestroy(E.gexec);
+            E.gexec = nullptr;
+        }
+        if (!E.body_stream && cudaStreamCreateWithFlags(&E.body_stream, cudaStreamNonBlocking) != cudaSuccess)
+            return nm_err(E, cudaGetLastError(), "body stream");
+        cudaError_t e = cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return nm_err(E, e, "graph capture");
+        const bool timers_on = E.timers.on;
+        E.timers.on = false;  // event records cannot sit inside a conditional body
+        E.capturing = true;
+        int rc = md_step_enqueue(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, out4);
+        E.capturing = false;
+        E.timers.on = timers_on;
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(E.stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return nm_err(E, e, "graph capture end");
+        e = cudaGraphInstantiate(&E.gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return nm_err(E, e, "graph instantiate");
+        E.gkey = key;
+        E.graph_captures++;
+    }
+    launch_set_step(E, t);
+    timer_begin(E, "md_graph");
+    cudaError_t e = cudaGraphLaunch(E.gexec, E.stream);
+    timer_end(E);
+    E.graph_launches++;
+    return nm_err(E, e, "graph launch");
+}
+
+int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,
+                        const double *xi1, const double *xi2, int t, double *out4) {
+    if (!ctx || !mp || !RRt || !PPt || !dRRt || !RRc) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    if (E.nm_P != E.kp.P) return PIMD_ERR_STATE;
+    cudaSetDevice(E.device);
+    if (E.graph_mode) return md_step_graph(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, out4);
+    return md_step_enqueue(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, out4);
+}
+
+int pimd_set_graph(pimd_ctx *ctx, int enable) {
+    if (!ctx) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    E.graph_mode = enable != 0;
+    if (!E.graph_mode && E.gexec) {
+        cudaSetDevice(E.device);
+        cudaStreamSynchronize(E.stream);
+        cudaGraphExecDestroy(E.gexec);
+        E.gexec = nullptr;
+        E.gkey.clear();
+    }
+    return PIMD_OK;
+}
+
+int pimd_graph_info(pimd_ctx *ctx, long long *captures, long long *launches) {
+    if (!ctx) return PIMD_ERR_ARG;
+    if (captures) *captures = ctx->E.graph_captures;
+    if (launches) *launches = ctx->E.graph_launches;
+    return PIMD_OK;
 }
 
 int pimd_md_step(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,

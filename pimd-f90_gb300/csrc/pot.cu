@@ -355,9 +355,23 @@ __global__ void __launch_bounds__(128) k_pair_qq(KP kp) {
 // ---------------------------------------------------------------------------------------
 // pot_ttm.f90:273-297: charge forces -q Efq, Uelec, and the initial induced dipoles
 // (polarisability times the charge field, or the 4-step predictor from the history).
+// pot_ttm.f90:649-675 calc_dpcf: the 4-step predictor coefficients for MD step t, from the
+// history slots mod(t,4) (oldest first in the reference's rotation)
+PIMD_D double4_32a predictor_coefficients(int t) {
+    switch (t % 4) {
+        case 0: return make_double4_32a(-1, 4, -6, 4);
+        case 1: return make_double4_32a(4, -1, 4, -6);
+        case 2: return make_double4_32a(-6, 4, -1, 4);
+        default: return make_double4_32a(4, -6, 4, -1);
+    }
+}
+
 template <int MODEL>
-__global__ void __launch_bounds__(128) k_after_qq(KP kp, double4_32a dpcf, int use_pred) {
+__global__ void __launch_bounds__(128) k_after_qq(KP kp) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    const int t = kp.dstep[0];
+    const bool use_pred = (t > 4) && kp.guess;
+    const double4_32a dpcf = predictor_coefficients(t);
     double av[3] = {0.0, 0.0, 0.0};
     if (s < kp.S) {
         const size_t gs = (size_t)b * kp.S + s;
@@ -462,9 +476,12 @@ __global__ void __launch_bounds__(128) k_dd_real(KP kp) {
     }
 }
 
-// pot_ttm.f90:379-385: convergence test per bead after an update
-__global__ void k_dd_check(KP kp, int iter, double eps) {
+// pot_ttm.f90:379-385: convergence test per bead after an update. The iteration number comes
+// from the device step word; the kernel advances it, and inside a CUDA graph it sets the
+// conditional of the dipole loop (continue while some bead is not converged).
+__global__ void k_dd_check(KP kp, double eps) {
     __shared__ int nconv;
+    const int iter = kp.dstep[1] + 1;
     if (threadIdx.x == 0) nconv = 0;
     __syncthreads();
     for (int b = threadIdx.x; b < kp.P; b += blockDim.x) {
@@ -481,7 +498,18 @@ __global__ void k_dd_check(KP kp, int iter, double eps) {
         if (a[ACC_CONV] != 0.0) atomicAdd(&nconv, 1);
     }
     __syncthreads();
-    if (threadIdx.x == 0) *kp.allconv = (nconv == kp.P) ? 1 : 0;
+    if (threadIdx.x == 0) {
+        *kp.allconv = (nconv == kp.P) ? 1 : 0;
+        kp.dstep[1] = iter;
+        if (kp.cond) cudaGraphSetConditional(kp.cond, nconv == kp.P ? 0u : 1u);
+    }
+}
+
+__global__ void k_set_step(int *dstep, int t) {
+    if (threadIdx.x == 0) {
+        dstep[0] = t;
+        dstep[1] = 0;
+    }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -740,7 +768,7 @@ __global__ void __launch_bounds__(128) k_finish(KP kp) {
             dI[c] = H1.w * a + H2.w * bb;
         }
         const double *dip = kp.dip + 3 * base;
-        const int slot = kp.t % 4;
+        const int slot = kp.dstep[0] % 4;
         double *hist = kp.txdip + ((size_t)b * 4 + slot) * kp.S * 3;
 #pragma unroll
         for (int k = T::FDI; k <= T::LDI; k++) {
@@ -777,7 +805,8 @@ __global__ void k_totals(KP kp, double *Upott, double *virialt, double *virialct
     v[8] -= kp.Uvdw_lrc;
     if (Upott) Upott[b] = En;
     if (virialt) virialt[b] = v[0] + v[4] + v[8];
-    if (virialct) virialct[b] = a[ACC_VIRIALC] - 3 * kp.Uvdw_lrc;
+    // pot_spc never sets virialc (its value in the reference is whatever the caller held); 0 here
+    if (virialct) virialct[b] = (kp.model >= 4) ? 0.0 : a[ACC_VIRIALC] - 3 * kp.Uvdw_lrc;
     if (virt9)
         for (int i = 0; i < 9; i++) virt9[9 * b + i] = v[i];
 }
@@ -812,19 +841,13 @@ void launch_pair_qq(Engine &E) {
 }
 
 void launch_after_qq(Engine &E) {
-    const int t = E.kp.t;
-    const bool pred = (t > 4) && E.kp.guess;
-    double4_32a d = make_double4_32a(0, 0, 0, 0);
-    if (pred) {
-        switch (t % 4) {
-            case 0: d = make_double4_32a(-1, 4, -6, 4); break;
-            case 1: d = make_double4_32a(4, -1, 4, -6); break;
-            case 2: d = make_double4_32a(-6, 4, -1, 4); break;
-            default: d = make_double4_32a(4, -6, 4, -1); break;
-        }
-    }
     dim3 g((E.kp.S + 127) / 128, E.kp.P);
-    DISPATCH_TTM(E, k_after_qq, g, 128, d, pred ? 1 : 0);
+    DISPATCH_TTM(E, k_after_qq, g, 128);
+}
+
+void launch_set_step(Engine &E, int t) {
+    k_set_step<<<1, 32, 0, E.stream>>>(E.kp.dstep, t);
+    ++E.nlaunch;
 }
 
 void launch_dd_real(Engine &E) {
@@ -832,8 +855,8 @@ void launch_dd_real(Engine &E) {
     DISPATCH_TTM(E, k_dd_real, g, 128);
 }
 
-void launch_dd_check(Engine &E, int iter) {
-    k_dd_check<<<1, 256, 0, E.stream>>>(E.kp, iter, E.kp.polar_eps); ++E.nlaunch;
+void launch_dd_check(Engine &E) {
+    k_dd_check<<<1, 256, 0, E.stream>>>(E.kp, E.kp.polar_eps); ++E.nlaunch;
 }
 
 void launch_pair_force(Engine &E) {

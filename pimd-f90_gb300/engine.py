@@ -70,6 +70,8 @@ SIGNATURES = {
     "pimd_md_step_device": [_V, ctypes.POINTER(MDParams), _V, _V, _V, _V, _V, _V, ctypes.c_int, _V],
     "pimd_md_step": [_V, ctypes.POINTER(MDParams), _D, _D, _D, _D, _D, _D, ctypes.c_int, _D],
     "pimd_peak_flops": [ctypes.c_int, ctypes.c_int, _D],
+    "pimd_set_graph": [_V, ctypes.c_int],
+    "pimd_graph_info": [_V, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
     "pimd_neighbors_noalloc": [_V, ctypes.c_int, _D, ctypes.c_double, _V, ctypes.c_int, _V, _V],
     "pimd_timers_reset": [_V, ctypes.c_int],
     "pimd_launch_count": [_V],
@@ -202,6 +204,26 @@ class ForceEngine:
         out.update(self.energies(0))
         return out
 
+    def pot_spc(self, RR):
+        """pot_spc(RR, En, dRR, virt, dip_momI, chg) (pot_ttm/pot_spc.f90:1)"""
+        RR = _f64(RR)
+        En = ctypes.c_double()
+        dRR = np.zeros_like(RR)
+        virt = np.zeros(9)
+        dI = np.zeros((self.nw, 3))
+        chg = np.zeros(self.natoms)
+        rc = load().pimd_pot_spc(self.h, _p(RR), ctypes.byref(En), _p(dRR), _p(virt), _p(dI), _p(chg))
+        self._check(rc, "pot_spc")
+        out = dict(En=En.value, dRR=dRR, virt=virt.reshape(3, 3, order="F"), dip_momI=dI, chg=chg)
+        out.update(self.energies(0))
+        return out
+
+    def potential(self, RR, RRc, t=1):
+        """force_calc.f90:112-170 dispatch on pot_model (one bead)."""
+        if self._p.pot_model in (2, 3):
+            return self.pot_ttm(RR, RRc, t)
+        return self.pot_spc(RR)
+
     def full_bead_forces(self, RRt, RRc, t=1):
         RRt, RRc = _f64(RRt), _f64(RRc)
         P = self.P
@@ -262,6 +284,15 @@ class ForceEngine:
         rc = load().pimd_md_step_device(self.h, ctypes.byref(mp), RRt, PPt, dRRt, RRc, xi1 or None, xi2 or None,
                                         int(t), out4)
         self._check(rc, "md_step_device")
+
+    def set_graph(self, enable=True):
+        """Run md_step/md_step_device as a captured CUDA graph (dipole loop on the device)."""
+        self._check(load().pimd_set_graph(self.h, int(enable)), "set_graph")
+
+    def graph_info(self):
+        c, n = ctypes.c_longlong(), ctypes.c_longlong()
+        self._check(load().pimd_graph_info(self.h, ctypes.byref(c), ctypes.byref(n)), "graph_info")
+        return c.value, n.value
 
     def set_stream(self, stream_ptr):
         self._check(load().pimd_set_stream(self.h, stream_ptr), "set_stream")
