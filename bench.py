@@ -47,6 +47,11 @@ def parse():
     ap.add_argument("--config", default=CONFIG)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch", action="store_true",
+                    help="the batching form instead of the headline: 64 TTM3-F replicas of uneven sizes in one graph")
+    ap.add_argument("--batch-replicas", type=int, default=64)
+    ap.add_argument("--config-large", action="store_true",
+                    help="TTM3-F 4096 H2O x 32 beads (|n| <= 24) steps/s for FP64, mixed and mixed+graph")
     ap.add_argument("--profile-force", choices=["fp64", "mixed"],
                     help="run two force calls of the workload and exit (the case profiled with ncu)")
     return ap.parse_args()
@@ -60,6 +65,77 @@ def profile_force(pkg, which):
         r = eng.full_bead_forces(c["RRt"], c["RRc"], t=t)
     print(json.dumps(dict(profile_force=which, Upot=float(r["Upot"]), niter=eng.energies(0)["niter"])))
     eng.close()
+
+
+def batch_workload(pkg, nrep, seed=20261203 + 4):
+    """64 replicas: N from {32, 64, 128, 256}, P from {8, 16, 32}, T uniform in [250, 350] K, each at
+    0.997 g/cm^3 (L = (N 29.96 A^3)^(1/3)) with cutoff min(9 A, L/2), seeded."""
+    rng = np.random.default_rng(seed)
+    reps, states = [], []
+    for i in range(nrep):
+        nw = int(rng.choice([32, 64, 128, 256]))
+        P = int(rng.choice([8, 16, 32]))
+        T = float(rng.uniform(250.0, 350.0))
+        c = pkg.waterbox.make_config("ttm3f_512x32", nw=nw, P=P, T=T, seed=seed + 1000 + i)
+        L = c["params"]["box"][0]
+        reps.append(dict(natoms=3 * nw, nbeads=P, box=(L, L, L), temp=T))
+        states.append(c)
+    return reps, states
+
+
+def run_batch(args, pkg):
+    import torch
+
+    reps, states = batch_workload(pkg, args.batch_replicas)
+    common = dict(pot_model=3, rc=9.0, rc1=7.2, alpha=0.0, eps_ewald=1e-6, **POLAR)
+    out = {}
+    for name, prec, steps in (("mixed", pkg.engine.PIMD_MIXED, args.steps), ("fp64", pkg.engine.PIMD_FP64,
+                                                                          max(3, min(args.steps, 20)))):
+        bt = pkg.engine.ReplicaBatch(common, reps, DT_FS / 1000.0, 15.9994, 1.008, langevin=1, seed=20261203,
+                                     precision=prec)
+        for i, c in enumerate(states):
+            bt.set_state(i, c["RRt"], c["PPt"])
+        t0 = time.perf_counter()
+        bt.autotune()
+        tune_s = time.perf_counter() - t0
+        bt.forces()
+        bt.step(args.warmup)
+        bt.sync()
+        with ClockSampler(0) as clk:
+            t0 = time.perf_counter()
+            bt.step(steps)
+            bt.sync()
+            dt = time.perf_counter() - t0
+        ng, gof = bt.groups()
+        energies = [bt.get_state(i)[3][0] for i in range(len(reps))]
+        out[name] = dict(batch_steps_per_s=steps / dt, steps=steps, ms_per_step=1000 * dt / steps, groups=ng,
+                         autotune_s=round(tune_s, 2), clocks=clk.summary(),
+                         finite=bool(np.all(np.isfinite(energies))))
+        bt.close()
+    beads = sum(r["nbeads"] for r in reps)
+    mol_beads = sum(r["nbeads"] * r["natoms"] // 3 for r in reps)
+    line = dict(metric="batch of %d uneven TTM3-F replicas: batch MD steps/s (all replicas advance one step)" % len(reps),
+                value=out["mixed"]["batch_steps_per_s"], unit="batch steps/s", n_gpus=1, higher_is_better=True,
+                dtype="f32 pair/phase arithmetic, f64 accumulation", data="synthetic (seeded replicas)",
+                config=dict(workload="64 replicas, N in {32,64,128,256}, P in {8,16,32}, T in [250,350] K, "
+                                     "rc = min(9, L/2), Ewald eps 1e-6", replicas=len(reps), total_beads=beads,
+                            molecule_beads=mol_beads, timing="host wall clock around stream-ordered graph launches"),
+                mixed=out["mixed"], fp64=out["fp64"], mixed_over_fp64=out["mixed"]["batch_steps_per_s"] /
+                out["fp64"]["batch_steps_per_s"])
+    print(json.dumps(line))
+
+
+def run_large(args, pkg):
+    """TTM3-F 4096 H2O x 32 beads, L = 49.72 A, Rc = 9 A, |n| <= 24: steps/s per precision form."""
+    res = {}
+    for name, prec, graph, steps in (("mixed_graph", pkg.engine.PIMD_MIXED, True, args.steps),
+                                     ("mixed", pkg.engine.PIMD_MIXED, False, args.steps),
+                                     ("fp64", pkg.engine.PIMD_FP64, False, max(2, min(args.steps, 5)))):
+        r = run_gpu_arm(args, pkg, 0, 1, 0, prec, steps, graph=graph)
+        res[name] = dict(steps_per_s=steps / (r["dev_ms"] / 1000.0), ms_per_step=r["dev_ms"] / steps, steps=steps,
+                         dipole_iterations_mean=float(np.mean(r["niters"])), clocks=r["clocks"])
+    print(json.dumps(dict(metric="TTM3-F 4096 H2O x 32 beads: MD steps/s", unit="steps/s",
+                          value=res["mixed_graph"]["steps_per_s"], config=dict(workload="ttm3f_4096x32"), **res)))
 
 
 def workload(pkg, name):
@@ -276,6 +352,13 @@ def main():
         return 0
 
     pkg.build_lib.build()
+    if args.batch:
+        run_batch(args, pkg)
+        return 0
+    if args.config_large:
+        args.config = "ttm3f_4096x32"
+        run_large(args, pkg)
+        return 0
     if world > 1:
         import torch.distributed as dist
 

@@ -171,6 +171,53 @@ int pimd_set_graph(pimd_ctx *ctx, int enable);
 /* Number of graph captures and graph launches made by this context so far. */
 int pimd_graph_info(pimd_ctx *ctx, long long *captures, long long *launches);
 
+/* ---------------------------------------------------------------------------------------
+ * Tile-shape autotuner. Times force calls of this context on its current positions (device
+ * RRt(3,Natoms,P) and RRc(3,Natoms) if given, else the last ones it was called with) for
+ * candidate launch shapes -- site groups of the structure-factor kernels, k-slices of the field
+ * passes, register-tiled vs. generic Ewald kernels, one-launch vs. three-launch neighbour lists
+ * -- by coordinate descent, and keeps the fastest. Results change only by FP32 summation order.
+ * Call before MD starts (it overwrites the dipole predictor history) and before graph capture.
+ * No counterpart in the reference. */
+int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc);
+/* The chosen shapes: [tiled structure factors, site groups (0 = sized from the SM count),
+ * register-row field kernels, max k-slices, one-launch neighbour lists]; n >= 5. */
+int pimd_get_tuning(pimd_ctx *ctx, int *knobs, int n);
+
+/* ---------------------------------------------------------------------------------------
+ * Batches of independent ring polymers (replicas) of uneven sizes: each replica has its own
+ * molecule count, bead count, box and temperature (the reference runs one per job). Replicas
+ * sharing a box are stacked on the bead axis of one engine, so each force kernel covers all of
+ * them in one launch; the whole PIMD_VV step of the batch (MD.f90:35-110, PILE thermostat with
+ * the device generator, seed = md.seed + replica index) is one CUDA graph with one branch per
+ * box. Cutoff per replica: min(common.rc, half its smallest box edge); rc1 scales with it;
+ * Ewald by common.eps_ewald (common.alpha <= 0) or the explicit alpha/nmax. No counterpart in
+ * the reference. */
+typedef struct {
+    int natoms;      /* 3 * Nwaters */
+    int nbeads;      /* 1..64 */
+    double box[3];   /* A */
+    double temp;     /* K: normal-mode frequencies and thermostat */
+} pimd_replica;
+typedef struct pimd_batch pimd_batch;
+int pimd_batch_create(pimd_batch **bt, const pimd_params *common, const pimd_replica *reps, int nrep,
+                      const pimd_md_params *md);
+int pimd_batch_destroy(pimd_batch *bt);
+const char *pimd_batch_last_error(pimd_batch *bt);
+/* number of box groups and the group of each replica (group_of_replica[nrep], may be NULL) */
+int pimd_batch_info(pimd_batch *bt, int *ngroups, int *group_of_replica);
+/* host arrays RRt, PPt (3,Natoms,P) of replica r; the centroid is computed from RRt */
+int pimd_batch_set_state(pimd_batch *bt, int r, const double *RRt, const double *PPt);
+/* host copies of replica r's state; out4 = [Upot, virial, virialc, uk] of its last step */
+int pimd_batch_get_state(pimd_batch *bt, int r, double *RRt, double *PPt, double *dRRt, double *out4);
+/* gradients of the current positions of every replica (call once before the first step) */
+int pimd_batch_forces(pimd_batch *bt);
+/* pimd_autotune for every box group (before the first pimd_batch_step) */
+int pimd_batch_autotune(pimd_batch *bt);
+/* nsteps steps of every replica; stream-ordered, returns without waiting */
+int pimd_batch_step(pimd_batch *bt, int nsteps);
+int pimd_batch_sync(pimd_batch *bt);
+
 /* O-O half neighbour list of one bead without any device allocation. No counterpart in the
  * reference; it serves callers that must not let a library allocate device memory (drivers
  * that own all GPU memory through their own pool, applications with a fixed per-GPU budget,

@@ -168,7 +168,7 @@ static int setup_kspace(Engine &E, const pimd_params *p) {
     return cuda_check(E, cudaGetLastError(), "k-space upload");
 }
 
-static int create(Engine &E, const pimd_params *p) {
+static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
     if (!p || p->natoms <= 0 || p->natoms % 3 || p->nbeads < 1) return fail(E, PIMD_ERR_ARG, "natoms/nbeads");
     if (p->pot_model < 2 || p->pot_model > 5) return fail(E, PIMD_ERR_ARG, "pot_model must be 2, 3, 4 or 5");
     const bool spc = p->pot_model >= 4;
@@ -196,6 +196,7 @@ static int create(Engine &E, const pimd_params *p) {
     kp.S = (spc ? 3 : 4) * kp.N;  // potential.f90:53-80: no M site in the SPC models
     kp.fq = spc ? 0 : kp.N;
     kp.P = p->nbeads;
+    kp.nrep = nrep;
     for (int c = 0; c < 3; c++) {
         kp.box[c] = p->box[c];
         kp.boxi[c] = 1.0 / p->box[c];
@@ -284,11 +285,16 @@ static int create(Engine &E, const pimd_params *p) {
     kp.cap = (int)E.cap;
     const size_t P = kp.P, S = kp.S, N = kp.N;
     const int nsq = kp.S - kp.fq, nsd = kp.ld - kp.fd;
-    const size_t maxgroups = (size_t)std::max((nsq + 31) / 32, (nsd + 31) / 32);  // 32-site tiles at most
-    if ((rc = dalloc(E, (double **)&kp.RRt, P * kp.natoms * 3)) || (rc = dalloc(E, (double **)&kp.RRc, kp.natoms * 3)) ||
+    // structure-factor partials: at most one site group per 32-site tile, at most 32 groups, and
+    // at most ~256 MB for all beads (large boxes have enough k-vectors to fill the GPU anyway)
+    const size_t tiles = (size_t)std::max((nsq + 31) / 32, (nsd + 31) / 32);
+    const size_t memcap = std::max<size_t>(1, (256ull << 20) / (P * (size_t)kp.nk * 3 * sizeof(double2)));
+    const size_t maxgroups = std::max<size_t>(1, std::min<size_t>(std::min<size_t>(tiles, 32), memcap));
+    E.sp_cap = (int)maxgroups;
+    if ((rc = dalloc(E, (double **)&kp.RRt, P * kp.natoms * 3)) || (rc = dalloc(E, (double **)&kp.RRc, (size_t)kp.nrep * kp.natoms * 3)) ||
         (rc = dalloc(E, &kp.dRRt, P * kp.natoms * 3)) || (rc = dalloc(E, &kp.dipI, P * N * 3)) ||
         (rc = dalloc(E, &kp.dipE, P * N * 3)) || (rc = dalloc(E, &kp.chg, P * kp.natoms)) ||
-        (rc = dalloc(E, &kp.pos, P * S)) || (rc = dalloc(E, &kp.posc, S)) || (rc = dalloc(E, &kp.F, P * S)) ||
+        (rc = dalloc(E, &kp.pos, P * S)) || (rc = dalloc(E, &kp.posc, (size_t)kp.nrep * S)) || (rc = dalloc(E, &kp.F, P * S)) ||
         (rc = dalloc(E, &kp.dR, P * S * 3)) || (rc = dalloc(E, &kp.dip, P * S * 3)) || (rc = dalloc(E, &kp.Efdr, P * S * 3)) ||
         (rc = dalloc(E, &kp.txdip, P * 4 * S * 3)) || (rc = dalloc(E, &kp.grdq, P * N * 27)) ||
         (rc = dalloc(E, &kp.Tdd, P * E.cap * kp.ndd * 6)) || (rc = dalloc(E, &kp.Tself, P * N * 18)) ||
@@ -305,7 +311,7 @@ static int create(Engine &E, const pimd_params *p) {
         if ((rc = dalloc(E, &kp.tabf, P * kp.ntab * S)) || (rc = dalloc(E, &kp.posf, P * S)) ||
             (rc = dalloc(E, &kp.rhof, P * S)) || (rc = dalloc(E, &kp.fcnt, P * N)) || (rc = dalloc(E, &kp.foff, P * N)) ||
             (rc = dalloc(E, &kp.fnbr, P * (size_t)kp.fcap * 2)) || (rc = dalloc(E, &kp.fntot, P)) ||
-            (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd * 6)) || (rc = dalloc(E, &kp.Wf, P * 2 * (size_t)kp.nk)))
+            (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd * 6)) || (rc = dalloc(E, &kp.Wf, P * 2 * (size_t)kp.nk)) || (rc = dalloc(E, &kp.dipf, P * S)))
             return rc;
     }
     cudaMemset(kp.txdip, 0, sizeof(double) * P * 4 * S * 3);
@@ -314,9 +320,21 @@ static int create(Engine &E, const pimd_params *p) {
     cudaMemset(kp.err, 0, sizeof(unsigned));
     if ((rc = cuda_check(E, cudaMallocHost((void **)&E.h_allconv, sizeof(int)), "cudaMallocHost"))) return rc;
     cudaMemset(kp.dstep, 0, sizeof(int) * 2);
+    if (nrep > 1) {
+        int *d_brep;
+        if ((rc = dalloc(E, &d_brep, P))) return rc;
+        cudaMemcpy(d_brep, brep, sizeof(int) * P, cudaMemcpyHostToDevice);
+        kp.brep = d_brep;
+    }
     pot_init_constants(E);
     ewald_init(E);
+    neighbors_init(E);
     return cuda_check(E, cudaDeviceSynchronize(), "init");
+}
+
+int create_context(Engine &E, const pimd_params *p, int nrep, const int *brep) {
+    if (nrep < 1 || (nrep > 1 && !brep)) return fail(E, PIMD_ERR_ARG, "replicas");
+    return create(E, p, nrep, brep);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -512,7 +530,7 @@ int pimd_create(pimd_ctx **ctx, const pimd_params *p) {
     if (!ctx) return PIMD_ERR_ARG;
     *ctx = nullptr;
     pimd_ctx *c = new pimd_ctx();
-    int rc = create(c->E, p);
+    int rc = create(c->E, p, 1, nullptr);
     if (rc) {
         fprintf(stderr, "pimd_create: %s\n", c->E.last_error.c_str());
         pimd_destroy(c);
@@ -774,6 +792,101 @@ int pimd_get_dipole_info(pimd_ctx *ctx, int bead, int *niter, double *deltadip) 
     if (rc) return rc;
     if (niter) *niter = (int)a[ACC_NITER];
     if (deltadip) *deltadip = a[ACC_DELTADIP];
+    return PIMD_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Autotuner: coordinate descent over the launch-shape knobs, each candidate timed as the best of
+// two force calls (after one warm-up) with CUDA events on the context's stream.
+static int tune_time(pimd_ctx *ctx, float *ms) {
+    Engine &E = ctx->E;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    double *d = E.d_out;
+    float best = 1e30f;
+    int rc = PIMD_OK;
+    for (int rep = 0; rep < 3 && !rc; rep++) {
+        cudaEventRecord(a, E.stream);
+        rc = run_forces(E, 0, ctx->check_every, d, d + E.kp.P, d + 2 * E.kp.P, nullptr);
+        cudaEventRecord(b, E.stream);
+        cudaError_t e = cudaEventSynchronize(b);
+        if (!rc && e != cudaSuccess) rc = cuda_check(E, e, "autotune");
+        float t = 0.f;
+        cudaEventElapsedTime(&t, a, b);
+        if (rep > 0) best = std::min(best, t);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = best;
+    return rc;
+}
+
+int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
+    if (!ctx) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    cudaSetDevice(E.device);
+    KP saved = E.kp;
+    if (RRt) E.kp.RRt = RRt;
+    if (RRc) E.kp.RRc = RRc;
+    const bool timers_on = E.timers.on;
+    E.timers.on = false;
+    struct Knob {
+        int *v;
+        std::vector<int> cand;
+    };
+    int sf_tiled = E.sf_tiled, ff_regs = E.ff_regs, nbr_block = E.nbr_block;
+    std::vector<Knob> knobs;
+    const bool mixed = E.precision == PIMD_MIXED && E.kp.model < 4;
+    if (mixed) {
+        knobs.push_back({&sf_tiled, {1, 0}});
+        knobs.push_back({&E.sf_groups, {0, 4, 8, 16, 32}});
+        knobs.push_back({&ff_regs, {1, 0}});
+    }
+    knobs.push_back({&E.max_slices, {16, 8, 4, 2}});
+    knobs.push_back({&nbr_block, {1, 0}});
+    auto apply = [&]() {
+        E.sf_tiled = sf_tiled != 0;
+        E.ff_regs = ff_regs != 0;
+        E.nbr_block = nbr_block != 0;
+    };
+    int rc = PIMD_OK;
+    float best;
+    apply();
+    rc = tune_time(ctx, &best);
+    for (size_t k = 0; k < knobs.size() && !rc; k++) {
+        int keep = *knobs[k].v;
+        for (int c : knobs[k].cand) {
+            if (c == keep) continue;
+            *knobs[k].v = c;
+            apply();
+            float t;
+            if ((rc = tune_time(ctx, &t))) break;
+            if (t < best) {
+                best = t;
+                keep = c;
+            }
+        }
+        *knobs[k].v = keep;
+        apply();
+    }
+    // the Fpart buffer holds max_slices slices: never exceed the allocated 16
+    E.max_slices = std::min(E.max_slices, 16);
+    E.timers.on = timers_on;
+    const double *kr = saved.RRt, *kc = saved.RRc;
+    E.kp.RRt = kr;
+    E.kp.RRc = kc;
+    return rc;
+}
+
+int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
+    if (!ctx || !k || n < 5) return PIMD_ERR_ARG;
+    const Engine &E = ctx->E;
+    k[0] = E.sf_tiled;
+    k[1] = E.sf_groups;
+    k[2] = E.ff_regs;
+    k[3] = E.max_slices;
+    k[4] = E.nbr_block;
     return PIMD_OK;
 }
 

@@ -26,6 +26,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/pimd_gb300.h"
 #include "common.cuh"
 
 namespace pimd {
@@ -84,11 +85,14 @@ struct KP {
     const float2 *runkf;   // FP32 (kx, ky) components of each run's k-vectors (mixed engine)
     const float *kzf;      // FP32 kz component of each k-vector (mixed engine)
     float2 *Wf;            // [P][2][nk] FP32 field weights 4pi Ak/V conj(S): slot 0 charge, 1 dipole
+    const int *sfrun;      // runs in the order of the structure-factor tiles (sorted by nkz)
+    const int4 *sftile;    // per tile: first ez slot, kz groups, runs, offset into sfrun
     int *nbrtmp;           // [P][N] neighbour counts / offsets
     // mixed-precision engine
     float2 *tabf;          // [P][ntab][S] FP32 copies of the FP64 recurrence tables
     float4 *posf;          // [P][S] (site - own O (min image), q)
     float4 *rhof;          // [P][S] centroid site - own bead O (raw difference)
+    float4 *dipf;          // [P][S] FP32 copy of the induced dipoles (written with every update)
     int *fcnt, *foff;      // [P][N] full neighbour list counts / offsets
     int *fnbr;             // [P][fcap] full neighbour list (j ascending per i)
     int *fntot;            // [P] full-list length
@@ -98,9 +102,16 @@ struct KP {
     double *acc;
     unsigned *err;
     int *allconv;
+    const int *brep;              // replica of each bead when one context holds several ring
+                                  // polymers (null: one replica); RRc and posc are per replica
+    int nrep;                     // replicas in this context (>= 1)
     int *dstep;                   // [0] MD step t of the force call, [1] dipole iterations done
     unsigned long long cond;      // CUDA-graph conditional handle of the dipole loop (0: host loop)
 };
+
+// replica of bead b and its centroid sites (posc[replica][S])
+PIMD_HD int rep_of(const KP &kp, int b) { return kp.brep ? kp.brep[b] : 0; }
+PIMD_HD const double4_32a *posc_of(const KP &kp, int b) { return kp.posc + (size_t)rep_of(kp, b) * kp.S; }
 
 // Named phase timers (the reference's dans_timer.f90 start_timer/stop_timer), recorded as
 // CUDA events on the engine stream and resolved lazily.
@@ -126,6 +137,10 @@ struct Engine {
     int max_slices = 16;  // k-slices of the Ewald field passes (Fpart capacity)
     bool sf_tiled = true;  // mixed engine: register-tiled structure factors (k_sfac_f)
     int sf_groups = 0;     // site groups of k_sfac_f (0: sized from the SM count)
+    int sf_ntiles = 0, sf_nkg_max = 0;  // run tiles of k_sfac_f and the largest kz-group count
+    int sp_cap = 1;        // site groups the structure-factor partial buffer (Spart) holds
+    bool ff_regs = true;   // mixed engine: field passes with the kz row in registers (k_field_f)
+    bool nbr_block = true; // one-launch neighbour lists per bead for N <= 1024 (k_nbr_block)
     size_t cap = 0;
     std::vector<KRun> h_runs;
     std::vector<KChunk> h_chunks;
@@ -155,12 +170,38 @@ struct Engine {
     std::vector<double> h_nm;                     // host copy: A11..A22, omegalist, msf, C
 };
 
+// Arguments of the normal-mode / thermostat / integrator kernels for one ring polymer
+// (nm.cu); a context with several replicas launches them once per replica.
+struct NMArgs {
+    int P, natoms;
+    const double *C;    // C(P,P) column-major: C[j + P*k] = C(j+1, k+1)
+    const double *A;    // [A11, A12, A21, A22, msf, c1, c2] x P
+    double massO, massH;
+    double delt, delt2, box0, boxi0;
+    int langevin, evolve;
+    const double *xi;   // (3, P, Natoms) standard normals, or null
+    unsigned long long seed, counter;
+    const int *tstep;   // device step word: when set, counter = 2 t + phase
+    int phase;
+};
+__global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt, double *RRc);
+__global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk);
+__global__ void k_md_sum(int P, const double *Upott, const double *virialt, const double *virialct, const double *uk,
+                         double *out4);
+void nm_launch_shape(int P, int natoms, int *threads, int *blocks, size_t *smem);
+void nm_init_host(int P, double omegan, double delta, double setNMfreq, std::vector<double> &A11,
+                  std::vector<double> &A12, std::vector<double> &A21, std::vector<double> &A22,
+                  std::vector<double> &om, std::vector<double> &msf, std::vector<double> &C);
+// context creation with nrep ring polymers sharing one box (brep: replica of each bead, host)
+int create_context(Engine &E, const pimd_params *p, int nrep, const int *brep);
+
 // phase timers (capi.cu)
 void timer_begin(Engine &E, const char *name);
 void timer_end(Engine &E);
 int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt, double *virialct, double *virt9);
 
 // launchers (neighbors.cu)
+void neighbors_init(Engine &E);
 void launch_neighbors(Engine &E);
 // launchers (pot.cu)
 void pot_init_constants(Engine &E);

@@ -233,16 +233,24 @@ __global__ void __launch_bounds__(SP_NT) k_spass(KP kp, int s0, int nsites, int 
 // every structure factor is a set of M small complex GEMMs over the sites of a group,
 //   G_m[run][kz] = sum_s A_m[s][run] ez[s][kz],   A_m = w_m exy(run)
 // (OP_Q: w = q; OP_MU: w = kx mu_x + ky mu_y and mu_z, S = G_0 + k_z G_1; OP_DIP: w = mu_c).
-// A block owns SF_RT runs of one bead and one site group; a thread owns SF_TR runs x SF_TK kz
-// slots (all M products) in registers, so each site costs 2-3 128-bit shared loads of A and a
-// broadcast of ez for SF_TR * SF_TK * M complex multiply-adds. kz slots outside a run's sphere
-// are computed and dropped. Partials per site group go to Spart like k_spass's.
-constexpr int SF_NRP = 32;               // run groups per block (one warp across)
-constexpr int SF_TR = 2;                 // runs per thread
-constexpr int SF_RT = SF_NRP * SF_TR;    // runs per block
-constexpr int SF_TK = 5;                 // kz slots per thread
+// Runs are processed in tiles of SF_RT runs of similar kz extent (sorted by nkz on the host,
+// kp.sfrun / kp.sftile), so a tile only spans the kz window its runs need. A block owns one
+// tile of one bead and one site group; lane = run, warp = group of SF_TK kz slots, so per site
+// a thread reads its A values with one conflict-free shared load and its ez slots with
+// broadcast 128-bit loads, then issues SF_TK * M * 4 FFMAs in registers. Slots outside a run's
+// own kz range are computed and dropped. Partials per site group go to Spart like k_spass's.
+constexpr int SF_RT = 32;                // runs per tile (one per lane)
+constexpr int SF_TK = 4;                 // kz slots per thread
 constexpr int SF_TS = 32;                // sites per shared-memory tile
-constexpr int SF_MAXT = 320;             // threads per block for 2 lmax + 1 <= 50
+constexpr int SF_MAXT = 416;             // threads per block: kz window <= 52 slots
+
+// acc += a * e (complex), as four FFMAs
+PIMD_D void cmac(float2 &acc, float2 a, float2 e) {
+    acc.x = fmaf(a.x, e.x, acc.x);
+    acc.x = fmaf(-a.y, e.y, acc.x);
+    acc.y = fmaf(a.y, e.x, acc.y);
+    acc.y = fmaf(a.x, e.y, acc.y);
+}
 
 template <int OP>
 __global__ void __launch_bounds__(SF_MAXT) k_sfac_f(KP kp, int s0, int nsites, int tsg, int ngroups, int skipconv) {
@@ -251,34 +259,33 @@ __global__ void __launch_bounds__(SF_MAXT) k_sfac_f(KP kp, int s0, int nsites, i
     const int b = blockIdx.z;
     if (skipconv && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
     const int grp = blockIdx.y;
-    const int r0 = blockIdx.x * SF_RT;
-    const int nr = min(SF_RT, kp.nrun - r0);
-    const int L = kp.lmax, LZ = 2 * L + 1;
-    const int nkg = (LZ + SF_TK - 1) / SF_TK, KZP = nkg * SF_TK;
-    const int tid = threadIdx.x, rp = tid % SF_NRP, kg = tid / SF_NRP;
+    const int4 tile = kp.sftile[blockIdx.x];  // first ez slot, kz groups, runs, offset into sfrun
+    const int zb = tile.x, nkg = tile.y, nr = tile.z;
+    const int KZP = nkg * SF_TK;
+    const int L = kp.lmax;
+    const int tid = threadIdx.x, lane = tid % SF_RT, kg = tid / SF_RT;
     extern __shared__ float4 smf[];
     float2 *A = reinterpret_cast<float2 *>(smf);  // [TS][RT][M]
-    float2 *ez = A + SF_TS * SF_RT * M;            // [TS][KZP]
+    float2 *ez = A + SF_TS * SF_RT * M;            // [TS][KZP]: slots zb .. zb + KZP - 1
     float4 *wt = reinterpret_cast<float4 *>(ez + SF_TS * KZP);  // [TS]
     __shared__ int2 rxy[SF_RT];
     __shared__ float2 rkv[SF_RT];
     if (tid < SF_RT) {
         if (tid < nr) {
-            const KRun run = kp.runs[r0 + tid];
+            const int r = kp.sfrun[tile.w + tid];
+            const KRun run = kp.runs[r];
             rxy[tid] = make_int2(run.kx, run.ky);
-            rkv[tid] = kp.runkf[r0 + tid];
+            rkv[tid] = kp.runkf[r];
         } else {
             rxy[tid] = make_int2(0, 0);
             rkv[tid] = make_float2(0.f, 0.f);
         }
     }
-    float2 acc[SF_TR][SF_TK][M];
+    float2 acc[SF_TK][M];
 #pragma unroll
-    for (int i = 0; i < SF_TR; i++)
+    for (int j = 0; j < SF_TK; j++)
 #pragma unroll
-        for (int j = 0; j < SF_TK; j++)
-#pragma unroll
-            for (int m = 0; m < M; m++) acc[i][j][m] = make_float2(0.f, 0.f);
+        for (int m = 0; m < M; m++) acc[j][m] = make_float2(0.f, 0.f);
     const int gbeg = s0 + grp * tsg, gend = min(s0 + nsites, gbeg + tsg);
     for (int sb = gbeg; sb < gend; sb += SF_TS) {
         const int nloc = min(SF_TS, gend - sb);
@@ -290,14 +297,14 @@ __global__ void __launch_bounds__(SF_MAXT) k_sfac_f(KP kp, int s0, int nsites, i
                 if (OP == OP_Q)
                     w.x = (float)kp.pos[gs].w;
                 else
-                    w = make_float4((float)kp.dip[3 * gs], (float)kp.dip[3 * gs + 1], (float)kp.dip[3 * gs + 2], 0.f);
+                    w = kp.dipf[gs];  // FP32 copy written with every dipole update
             }
             wt[tid] = w;
         }
         for (int idx = tid; idx < SF_TS * KZP; idx += blockDim.x) {
-            const int site = idx / KZP, j = idx - site * KZP, kz = j - L;
+            const int site = idx / KZP, kz = zb + (idx - site * KZP) - L;
             float2 v = make_float2(0.f, 0.f);
-            if (site < nloc && j < LZ) {
+            if (site < nloc && kz <= L) {
                 v = tab_z<float>(kp, b, kz < 0 ? -kz : kz, sb + site);
                 if (kz < 0) v = cconj(v);
             }
@@ -305,7 +312,8 @@ __global__ void __launch_bounds__(SF_MAXT) k_sfac_f(KP kp, int s0, int nsites, i
         }
         __syncthreads();
         for (int idx = tid; idx < SF_TS * SF_RT; idx += blockDim.x) {
-            const int site = idx % SF_TS, r = idx / SF_TS;
+            // lane = run: the stores of a warp are contiguous (the table reads repeat few rows)
+            const int r = idx % SF_RT, site = idx / SF_RT;
             float2 a[M];
 #pragma unroll
             for (int m = 0; m < M; m++) a[m] = make_float2(0.f, 0.f);
@@ -329,53 +337,55 @@ __global__ void __launch_bounds__(SF_MAXT) k_sfac_f(KP kp, int s0, int nsites, i
                     a[M - 1] = make_float2(w.z * exy.x, w.z * exy.y);
                 }
             }
+            if (M == 2) {
+                *reinterpret_cast<float4 *>(A + (site * SF_RT + r) * M) = make_float4(a[0].x, a[0].y, a[M - 1].x, a[M - 1].y);
+            } else {
 #pragma unroll
-            for (int m = 0; m < M; m++) A[(site * SF_RT + r) * M + m] = a[m];
+                for (int m = 0; m < M; m++) A[(site * SF_RT + r) * M + m] = a[m];
+            }
         }
         __syncthreads();
         if (kg < nkg) {
             for (int site = 0; site < nloc; site++) {
-                float2 a[SF_TR][M], e[SF_TK];
-                const float2 *ap = A + (site * SF_RT + rp * SF_TR) * M;
+                float2 a[M], e[SF_TK];
+                const float2 *ap = A + (site * SF_RT + lane) * M;
+                if (M == 2) {
+                    const float4 v = *reinterpret_cast<const float4 *>(ap);
+                    a[0] = make_float2(v.x, v.y);
+                    a[M - 1] = make_float2(v.z, v.w);
+                } else {
 #pragma unroll
-                for (int i = 0; i < SF_TR; i++)
+                    for (int m = 0; m < M; m++) a[m] = ap[m];
+                }
+                const float4 *ep = reinterpret_cast<const float4 *>(ez + site * KZP + kg * SF_TK);
 #pragma unroll
-                    for (int m = 0; m < M; m++) a[i][m] = ap[i * M + m];
-                const float2 *ep = ez + site * KZP + kg * SF_TK;
+                for (int j = 0; j < SF_TK / 2; j++) {
+                    const float4 v = ep[j];
+                    e[2 * j] = make_float2(v.x, v.y);
+                    e[2 * j + 1] = make_float2(v.z, v.w);
+                }
+                // ewald.f90:37-39: coskr = cxy cz - sxy sz, sinkr = sxy cz + cxy sz
 #pragma unroll
-                for (int j = 0; j < SF_TK; j++) e[j] = ep[j];
+                for (int j = 0; j < SF_TK; j++)
 #pragma unroll
-                for (int i = 0; i < SF_TR; i++)
-#pragma unroll
-                    for (int j = 0; j < SF_TK; j++)
-#pragma unroll
-                        for (int m = 0; m < M; m++) {
-                            // ewald.f90:37-39: coskr = cxy cz - sxy sz, sinkr = sxy cz + cxy sz
-                            acc[i][j][m].x += a[i][m].x * e[j].x - a[i][m].y * e[j].y;
-                            acc[i][j][m].y += a[i][m].y * e[j].x + a[i][m].x * e[j].y;
-                        }
+                    for (int m = 0; m < M; m++) cmac(acc[j][m], a[m], e[j]);
             }
         }
     }
-    if (kg >= nkg) return;
+    if (kg >= nkg || lane >= nr) return;
+    const KRun run = kp.runs[kp.sfrun[tile.w + lane]];
 #pragma unroll
-    for (int i = 0; i < SF_TR; i++) {
-        const int r = rp * SF_TR + i;
-        if (r >= nr) continue;
-        const KRun run = kp.runs[r0 + r];
+    for (int j = 0; j < SF_TK; j++) {
+        const int kz = zb + kg * SF_TK + j - L;
+        if (kz < run.kzlo || kz >= run.kzlo + run.nkz) continue;
+        const int k = run.kbeg + kz - run.kzlo;
+        float2 *out = reinterpret_cast<float2 *>(kp.Spart) + (((size_t)b * ngroups + grp) * kp.nk + k) * NC;
+        if (OP == OP_MU) {
+            const float kzv = kp.kzf[k];
+            out[0] = make_float2(fmaf(kzv, acc[j][M - 1].x, acc[j][0].x), fmaf(kzv, acc[j][M - 1].y, acc[j][0].y));
+        } else {
 #pragma unroll
-        for (int j = 0; j < SF_TK; j++) {
-            const int kz = kg * SF_TK + j - L;
-            if (kz < run.kzlo || kz >= run.kzlo + run.nkz) continue;
-            const int k = run.kbeg + kz - run.kzlo;
-            float2 *out = reinterpret_cast<float2 *>(kp.Spart) + (((size_t)b * ngroups + grp) * kp.nk + k) * NC;
-            if (OP == OP_MU) {
-                const float kzv = kp.kzf[k];
-                out[0] = make_float2(acc[i][j][0].x + kzv * acc[i][j][M - 1].x, acc[i][j][0].y + kzv * acc[i][j][M - 1].y);
-            } else {
-#pragma unroll
-                for (int c = 0; c < NC; c++) out[c] = acc[i][j][c];
-            }
+            for (int c = 0; c < NC; c++) out[c] = acc[j][c];
         }
     }
 }
@@ -551,6 +561,181 @@ __global__ void __launch_bounds__(NT) k_field(KP kp, int s0, int s1) {
     }
 }
 
+// FP32 field pass of the mixed engine with the site's e^{i kz z} row held in registers, centred
+// at slot LM = LZM / 2 (slot LM + kz, |kz| <= lmax <= LM). Per chunk the weights are staged
+// densely as [run][slot] (zero outside the run's kz range). A run with kz in [-m, m] (every run
+// but kx = ky = 0) dispatches on m to a fully unrolled loop over exactly its 2m + 1 slots, so
+// each useful (site, k) costs one broadcast shared load and eight FP32 operations on register
+// operands: U0 = sum ez W, U1 = sum kz ez W (and V0..V2 with W2 = W_q + W_mu for QD). Same
+// slicing and FP64 per-chunk accumulation as k_field.
+constexpr int FF_NT = 128;
+constexpr int FF_RUNS = 64;  // runs per chunk (KChunk limit)
+
+struct FAcc {
+    float2 U0, U1, V0, V1, V2;
+};
+
+template <int MODE>
+PIMD_D void field_slot(const float2 &ez, float2 W, float2 W2, float kz, FAcc &a) {
+    const float2 t = make_float2(ez.x * W.x - ez.y * W.y, ez.y * W.x + ez.x * W.y);
+    a.U0.x += t.x;
+    a.U0.y += t.y;
+    a.U1.x = fmaf(kz, t.x, a.U1.x);
+    a.U1.y = fmaf(kz, t.y, a.U1.y);
+    if (MODE == F_QD) {
+        const float2 u = make_float2(ez.x * W2.x - ez.y * W2.y, ez.y * W2.x + ez.x * W2.y);
+        a.V0.x += u.x;
+        a.V0.y += u.y;
+        a.V1.x = fmaf(kz, u.x, a.V1.x);
+        a.V1.y = fmaf(kz, u.y, a.V1.y);
+        a.V2.x = fmaf(kz * kz, u.x, a.V2.x);
+        a.V2.y = fmaf(kz * kz, u.y, a.V2.y);
+    }
+}
+
+template <int MODE, int LZM, int MM>
+PIMD_D void field_sym(const float2 (&ez)[LZM], const float2 *w1, const float2 *w2, FAcc &a) {
+    constexpr int LM = LZM / 2;
+    if constexpr (MM <= LM) {
+#pragma unroll
+        for (int j = LM - MM; j <= LM + MM; j++)
+            field_slot<MODE>(ez[j], w1[j], MODE == F_QD ? w2[j] : make_float2(0.f, 0.f), (float)(j - LM), a);
+    }
+}
+
+template <int MODE, int LZM>
+__global__ void __launch_bounds__(FF_NT) k_field_f(KP kp, int s0, int s1) {
+    constexpr int LM = LZM / 2;
+    const int b = blockIdx.y, slice = blockIdx.z, nslice = gridDim.z;
+    if (MODE == F_D && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
+    const int s = s0 + blockIdx.x * FF_NT + threadIdx.x;
+    const bool valid = s < s1;
+    const int L = kp.lmax;
+    extern __shared__ float4 smf[];
+    float2 *Wd = reinterpret_cast<float2 *>(smf);  // [1 or 2 (QD)][FF_RUNS][LZM]
+    __shared__ int4 rinfo[FF_RUNS];                // kx, ky, first slot, last slot + 1
+    __shared__ float2 rkv[FF_RUNS];
+    float2 ez[LZM];
+#pragma unroll
+    for (int j = 0; j < LZM; j++) {
+        const int kz = j - LM;
+        float2 v = make_float2(0.f, 0.f);
+        if (valid && kz >= -L && kz <= L) {
+            v = tab_z<float>(kp, b, kz < 0 ? -kz : kz, s);
+            if (kz < 0) v = cconj(v);
+        }
+        ez[j] = v;
+    }
+    const size_t gs = (size_t)b * kp.S + (valid ? s : s0);
+    float qr = 0.f, mur[3] = {0.f, 0.f, 0.f};
+    bool isdip = false;
+    if (valid) {
+        qr = (float)kp.pos[gs].w;
+        isdip = s >= kp.fd && s < kp.ld;
+        if (MODE == F_QD && isdip) {
+            mur[0] = (float)kp.dip[3 * gs];
+            mur[1] = (float)kp.dip[3 * gs + 1];
+            mur[2] = (float)kp.dip[3 * gs + 2];
+        }
+    }
+    // the k-vector's z component is 2 pi kz / Lz; the loops accumulate with the integer kz
+    const float kzs = (float)(TWOPI * kp.boxi[2]);
+    double E[3] = {0, 0, 0}, phi = 0.0, G[3] = {0, 0, 0};
+    const int c0 = (int)((long)slice * kp.nchunk / nslice), c1 = (int)((long)(slice + 1) * kp.nchunk / nslice);
+    for (int chn = c0; chn < c1; chn++) {
+        const KChunk ch = kp.chunks[chn];
+        const int nr = ch.r1 - ch.r0;
+        __syncthreads();
+        if (threadIdx.x < nr) {
+            const KRun run = kp.runs[ch.r0 + threadIdx.x];
+            rinfo[threadIdx.x] = make_int4(run.kx, run.ky, run.kzlo + LM, run.kzlo + LM + run.nkz);
+            rkv[threadIdx.x] = kp.runkf[ch.r0 + threadIdx.x];
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nr * LZM; idx += FF_NT) {
+            const int rl = idx / LZM, j = idx - rl * LZM;
+            const int4 ri = rinfo[rl];
+            float2 w1 = make_float2(0.f, 0.f), w2 = w1;
+            if (j >= ri.z && j < ri.w) {
+                const int k = kp.runs[ch.r0 + rl].kbeg + (j - ri.z);
+                const float2 wq = kp.Wf[((size_t)b * 2) * kp.nk + k], wm = kp.Wf[((size_t)b * 2 + 1) * kp.nk + k];
+                w1 = (MODE == F_Q) ? wq : wm;
+                if (MODE == F_QD) w2 = make_float2(wq.x + wm.x, wq.y + wm.y);
+            }
+            Wd[idx] = w1;
+            if (MODE == F_QD) Wd[FF_RUNS * LZM + idx] = w2;
+        }
+        __syncthreads();
+        if (!valid) continue;
+        float cE[3] = {0.f, 0.f, 0.f}, cphi = 0.f, cG[3] = {0.f, 0.f, 0.f};
+        for (int rl = 0; rl < nr; rl++) {
+            const int4 ri = rinfo[rl];
+            const float2 kv = rkv[rl];
+            const float2 ex = tab_x<float>(kp, b, ri.x, s);
+            const float2 ey = tab_y<float>(kp, b, ri.y, s);
+            const float2 exy = make_float2(ex.x * ey.x - ex.y * ey.y, ex.y * ey.x + ex.x * ey.y);
+            FAcc a;
+            a.U0 = a.U1 = a.V0 = a.V1 = a.V2 = make_float2(0.f, 0.f);
+            const float2 *w1 = Wd + rl * LZM;
+            const float2 *w2 = Wd + FF_RUNS * LZM + rl * LZM;
+            const int m = LM - ri.z;
+            if (ri.z + ri.w == 2 * LM + 1) {  // kz in [-m, m]
+                switch (m) {
+#define PIMD_FF_CASE(MM) \
+    case MM: field_sym<MODE, LZM, MM>(ez, w1, w2, a); break;
+                    PIMD_FF_CASE(0) PIMD_FF_CASE(1) PIMD_FF_CASE(2) PIMD_FF_CASE(3) PIMD_FF_CASE(4)
+                    PIMD_FF_CASE(5) PIMD_FF_CASE(6) PIMD_FF_CASE(7) PIMD_FF_CASE(8) PIMD_FF_CASE(9)
+                    PIMD_FF_CASE(10) PIMD_FF_CASE(11) PIMD_FF_CASE(12) PIMD_FF_CASE(13) PIMD_FF_CASE(14)
+                    PIMD_FF_CASE(15) PIMD_FF_CASE(16) PIMD_FF_CASE(17) PIMD_FF_CASE(18) PIMD_FF_CASE(19)
+                    PIMD_FF_CASE(20) PIMD_FF_CASE(21) PIMD_FF_CASE(22) PIMD_FF_CASE(23) PIMD_FF_CASE(24)
+#undef PIMD_FF_CASE
+                    default: break;
+                }
+            } else {  // kx = ky = 0: kz >= 1 only
+#pragma unroll
+                for (int j = LM + 1; j < LZM; j++) {
+                    if (j >= ri.w) continue;
+                    field_slot<MODE>(ez[j], w1[j], MODE == F_QD ? w2[j] : make_float2(0.f, 0.f), (float)(j - LM), a);
+                }
+            }
+            const float2 z0 = cmul(exy, a.U0), z1 = cmul(exy, a.U1);
+            if (MODE == F_QD) {
+                cphi += z0.x;
+                cG[0] -= qr * z0.y * kv.x;
+                cG[1] -= qr * z0.y * kv.y;
+                cG[2] -= qr * z1.y * kzs;
+                if (isdip) {
+                    const float R0 = exy.x * a.V0.x - exy.y * a.V0.y;
+                    const float R1 = (exy.x * a.V1.x - exy.y * a.V1.y) * kzs;
+                    const float R2 = (exy.x * a.V2.x - exy.y * a.V2.y) * (kzs * kzs);
+                    const float aa = kv.x * mur[0] + kv.y * mur[1];
+                    cG[0] -= kv.x * (aa * R0 + mur[2] * R1);
+                    cG[1] -= kv.y * (aa * R0 + mur[2] * R1);
+                    cG[2] -= aa * R1 + mur[2] * R2;
+                }
+            } else {
+                cphi += z0.x;
+                cE[0] += z0.y * kv.x;
+                cE[1] += z0.y * kv.y;
+                cE[2] += z1.y * kzs;
+            }
+        }
+        phi += (double)cphi;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            E[c] += (double)cE[c];
+            G[c] += (double)cG[c];
+        }
+    }
+    if (valid) {
+        double4_32a *o = kp.Fpart + ((size_t)slice * kp.P + b) * (s1 - s0) + (s - s0);
+        if (MODE == F_QD)
+            *o = make_double4_32a(G[0], G[1], G[2], phi);
+        else
+            *o = make_double4_32a(E[0], E[1], E[2], phi);
+    }
+}
+
 // Sum the slices of k_field in order and apply the pass's epilogue, one thread per site.
 template <int MODE, int NT>
 __global__ void __launch_bounds__(NT) k_field_finish(KP kp, int s0, int s1, int nslice) {
@@ -609,6 +794,7 @@ __global__ void __launch_bounds__(NT) k_field_finish(KP kp, int s0, int s1, int 
                 kp.dip[3 * gs + c] = mn[c];
                 kp.Efdr[3 * gs + c] = 0.0;
             }
+            if (kp.dipf) kp.dipf[gs] = make_float4((float)mn[0], (float)mn[1], (float)mn[2], 0.f);
         }
         // reduce into acc[ACC_DSQ], acc[ACC_MUEFQ]
         __shared__ double red[NT / 32][2];
@@ -678,6 +864,7 @@ static int spass_groups(const Engine &E, int nsites) {
     int g = (int)((152L * 8 + per - 1) / per);
     if (g < 1) g = 1;
     if (g > ntile) g = ntile;
+    if (g > E.sp_cap) g = E.sp_cap;
     return g;
 }
 
@@ -698,22 +885,21 @@ static void run_spass_t(Engine &E, int s0, int nsites, int skipconv) {
 }
 
 // the mixed engine's register-tiled structure factor; site groups of whole 32-site tiles sized
-// for about 8 blocks of 160-320 threads per SM
+// for about 8 blocks per SM
 template <int OP>
 static void run_sfac_f(Engine &E, int s0, int nsites, int skipconv) {
     const KP &kp = E.kp;
     constexpr int M = (OP == OP_Q) ? 1 : (OP == OP_MU) ? 2 : 3;
-    const int LZ = 2 * kp.lmax + 1, nkg = (LZ + SF_TK - 1) / SF_TK, KZP = nkg * SF_TK;
-    const int rtiles = (kp.nrun + SF_RT - 1) / SF_RT;
     const int ntile = (nsites + SF_TS - 1) / SF_TS;
-    const long per = (long)rtiles * kp.P;
+    const long per = (long)E.sf_ntiles * kp.P;
     int ng = E.sf_groups > 0 ? E.sf_groups : (int)((152L * 8 + per - 1) / per);
-    ng = std::max(1, std::min(ng, ntile));
+    ng = std::max(1, std::min(std::min(ng, ntile), E.sp_cap));
     const int tsg = ((ntile + ng - 1) / ng) * SF_TS;
     const int ngr = (nsites + tsg - 1) / tsg;
+    const int KZP = E.sf_nkg_max * SF_TK;
     const size_t smem = sizeof(float2) * ((size_t)SF_TS * SF_RT * M + (size_t)SF_TS * KZP) + sizeof(float4) * SF_TS;
-    dim3 g(rtiles, ngr, kp.P);
-    k_sfac_f<OP><<<g, SF_NRP * nkg, smem, E.stream>>>(E.kp, s0, nsites, tsg, ngr, skipconv);
+    dim3 g(E.sf_ntiles, ngr, kp.P);
+    k_sfac_f<OP><<<g, SF_RT * E.sf_nkg_max, smem, E.stream>>>(E.kp, s0, nsites, tsg, ngr, skipconv);
     ++E.nlaunch;
     dim3 g2((kp.nk + 255) / 256, kp.P);
     k_sreduce<OP, float><<<g2, 256, 0, E.stream>>>(E.kp, ngr, skipconv);
@@ -723,7 +909,7 @@ static void run_sfac_f(Engine &E, int s0, int nsites, int skipconv) {
 template <int OP>
 static void run_spass(Engine &E, int s0, int nsites, int skipconv) {
     if (E.precision == PIMD_PREC_MIXED) {
-        if (E.sf_tiled && 2 * E.kp.lmax + 1 <= SF_TK * (SF_MAXT / SF_NRP))
+        if (E.sf_tiled && E.sf_nkg_max * SF_RT <= SF_MAXT)
             run_sfac_f<OP>(E, s0, nsites, skipconv);
         else
             run_spass_t<OP, float>(E, s0, nsites, skipconv);
@@ -748,9 +934,34 @@ static void launch_field_nt(Engine &E, int s0, int s1) {
     E.nlaunch += 2;
 }
 
+template <int MODE, int LZM>
+static void launch_field_f(Engine &E, int s0, int s1) {
+    const size_t smem = sizeof(float2) * ((MODE == F_QD) ? 2 : 1) * FF_RUNS * LZM;
+    const int sblocks = (s1 - s0 + FF_NT - 1) / FF_NT;
+    const long want = 8L * 152;
+    int ns = (int)((want + (long)sblocks * E.kp.P - 1) / ((long)sblocks * E.kp.P));
+    ns = std::max(1, std::min(ns, std::min(E.nchunk, E.max_slices)));
+    dim3 g(sblocks, E.kp.P, ns);
+    k_field_f<MODE, LZM><<<g, FF_NT, smem, E.stream>>>(E.kp, s0, s1);
+    dim3 g2((s1 - s0 + 127) / 128, E.kp.P);
+    k_field_finish<MODE, 128><<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns);
+    E.nlaunch += 2;
+}
+
 template <int MODE>
 static void run_field(Engine &E, int s0, int s1) {
     const int LZ = 2 * E.kp.lmax + 1;
+    if (E.precision == PIMD_PREC_MIXED && E.ff_regs && LZ <= 49) {
+        if (LZ <= 17)
+            launch_field_f<MODE, 17>(E, s0, s1);
+        else if (LZ <= 25)
+            launch_field_f<MODE, 25>(E, s0, s1);
+        else if (LZ <= 33)
+            launch_field_f<MODE, 33>(E, s0, s1);
+        else
+            launch_field_f<MODE, 49>(E, s0, s1);
+        return;
+    }
     if (E.precision == PIMD_PREC_MIXED) {
         if ((size_t)LZ * 128 * 8 <= 64 * 1024)
             launch_field_nt<MODE, 128, float>(E, s0, s1);
@@ -778,8 +989,45 @@ static void ewald_attrs() {
     cudaFuncSetAttribute(k_field<F_D, 64, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     cudaFuncSetAttribute(k_field<F_QD, 64, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
 }
+// Tiles of the register-tiled structure factor: runs sorted by kz extent (longest first), 32 per
+// tile; each tile records the first ez slot of its kz window and the number of kz groups.
+// Returns 0, or 1 if the device tables could not be allocated.
+static int sfac_tiles(Engine &E) {
+    KP &kp = E.kp;
+    std::vector<int> order(kp.nrun);
+    for (int r = 0; r < kp.nrun; r++) order[r] = r;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return E.h_runs[a].nkz > E.h_runs[b].nkz; });
+    std::vector<int4> tiles;
+    E.sf_nkg_max = 0;
+    for (int t0 = 0; t0 < kp.nrun; t0 += SF_RT) {
+        const int nr = std::min(SF_RT, kp.nrun - t0);
+        int lo = 1 << 30, hi = -(1 << 30);
+        for (int i = 0; i < nr; i++) {
+            const KRun &r = E.h_runs[order[t0 + i]];
+            lo = std::min(lo, r.kzlo);
+            hi = std::max(hi, r.kzlo + r.nkz - 1);
+        }
+        const int nkg = (hi - lo + 1 + SF_TK - 1) / SF_TK;
+        E.sf_nkg_max = std::max(E.sf_nkg_max, nkg);
+        tiles.push_back(make_int4(lo + kp.lmax, nkg, nr, t0));
+    }
+    E.sf_ntiles = (int)tiles.size();
+    int *d_order;
+    int4 *d_tiles;
+    if (cudaMalloc((void **)&d_order, sizeof(int) * kp.nrun) != cudaSuccess ||
+        cudaMalloc((void **)&d_tiles, sizeof(int4) * tiles.size()) != cudaSuccess)
+        return 1;
+    E.allocs.push_back(d_order);
+    E.allocs.push_back(d_tiles);
+    cudaMemcpy(d_order, order.data(), sizeof(int) * kp.nrun, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice);
+    kp.sfrun = d_order;
+    kp.sftile = d_tiles;
+    return 0;
+}
+
 void ewald_init(Engine &E) {
-    (void)E;
+    if (sfac_tiles(E) != 0) E.sf_tiled = false;  // allocation failed: untiled kernel
     ewald_attrs<double>();
     ewald_attrs<float>();
     cudaFuncSetAttribute(k_sfac_f<OP_Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(128) k_site_offsets(KP kp) {
     if (s >= kp.S) return;
     const int mol = s % kp.N;
     const size_t gs = (size_t)b * kp.S + s;
-    const double4_32a O = kp.pos[(size_t)b * kp.S + mol], R = kp.pos[gs], C = kp.posc[s];
+    const double4_32a O = kp.pos[(size_t)b * kp.S + mol], R = kp.pos[gs], C = posc_of(kp, b)[s];
     float4 d;
     if (s < kp.N) {
         d = make_float4(0.f, 0.f, 0.f, (float)R.w);
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(128) k_pair_qq_m(KP kp) {
             float d[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) d[c] = -sc * Rf[c];
-            const double4_32a ci = kp.posc[i], cj = kp.posc[j];
+            const double4_32a ci = posc_of(kp, b)[i], cj = posc_of(kp, b)[j];
             const float Rc[3] = {(float)min_image_rn(__dsub_rn(ci.x, cj.x), kp.box[0], kp.boxi[0]),
                                  (float)min_image_rn(__dsub_rn(ci.y, cj.y), kp.box[1], kp.boxi[1]),
                                  (float)min_image_rn(__dsub_rn(ci.z, cj.z), kp.box[2], kp.boxi[2])};
@@ -230,6 +230,7 @@ __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
     if (i >= N) return;
     if (kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
     const double *dip = kp.dip + (size_t)b * kp.S * 3;
+    const float4 *dipf = kp.dipf + (size_t)b * kp.S;
     const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
     const int e0 = kp.foff[(size_t)b * N + i];
     const int e1 = (i + 1 < N) ? kp.foff[(size_t)b * N + i + 1] : kp.fntot[b];
@@ -244,8 +245,8 @@ __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
         for (int isp = T::FDI; isp <= T::LDI; isp++)
 #pragma unroll
             for (int jsp = T::FDI; jsp <= T::LDI; jsp++, t++) {
-                const double *m = dip + 3 * ((jsp - 1) * N + j);
-                const float mx = (float)m[0], my = (float)m[1], mz = (float)m[2];
+                const float4 m = dipf[(jsp - 1) * N + j];
+                const float mx = m.x, my = m.y, mz = m.z;
                 const float *Tt = Te + 6 * t;
                 ei[isp][0] += Tt[0] * mx + Tt[3] * my + Tt[4] * mz;
                 ei[isp][1] += Tt[3] * mx + Tt[1] * my + Tt[5] * mz;

@@ -36,19 +36,6 @@ PIMD_D double gauss_from(unsigned a, unsigned b) {
     return sqrt(-2.0 * log(u1)) * cos(TWOPI * u2);
 }
 
-struct NMArgs {
-    int P, natoms;
-    const double *C;    // C(P,P) column-major: C[j + P*k] = C(j+1, k+1)
-    const double *A;    // [A11, A12, A21, A22, msf, c1, c2] x P
-    double massO, massH;
-    double delt, delt2, box0, boxi0;
-    int langevin, evolve;
-    const double *xi;   // (3, P, Natoms) standard normals, or null
-    unsigned long long seed, counter;
-    const int *tstep;   // device step word: when set, counter = 2 t + phase
-    int phase;
-};
-
 PIMD_D double noise(const NMArgs &a, int atom, int j, int c) {
     if (a.xi) return a.xi[c + 3 * j + (size_t)3 * a.P * atom];
     const unsigned long long idx = ((unsigned long long)atom * a.P + j) * 3 + c;
@@ -242,7 +229,7 @@ __global__ void k_md_sum(int P, const double *Upott, const double *virialt, cons
 }
 
 // ---------------------------------------------------------------------------------------
-static void nm_launch_shape(int P, int natoms, int *threads, int *blocks, size_t *smem) {
+void nm_launch_shape(int P, int natoms, int *threads, int *blocks, size_t *smem) {
     int G = 256 / (3 * P);
     if (G < 1) G = 1;
     *threads = ((G * 3 * P + 31) / 32) * 32;  // whole warps (the KE reduction shuffles)
@@ -264,7 +251,7 @@ static NMArgs nm_args(Engine &E, double massO, double massH) {
 }
 
 // NormalModes.f90:68-218
-static void nm_init_host(int P, double omegan, double delta, double setNMfreq, std::vector<double> &A11,
+void nm_init_host(int P, double omegan, double delta, double setNMfreq, std::vector<double> &A11,
                          std::vector<double> &A12, std::vector<double> &A21, std::vector<double> &A22,
                          std::vector<double> &om, std::vector<double> &msf, std::vector<double> &C) {
     A11.assign(P, 0);

@@ -58,17 +58,28 @@ PIMD_D double3 ld3(const double *p) { return make_double3(p[0], p[1], p[2]); }
 // ---------------------------------------------------------------------------------------
 // pot_ttm.f90:56-151 and 232-261: site layout, M sites, NASA PES + DMS charges, monomer
 // virials, self energy and intramolecular Ewald exclusions. One thread per (molecule, bead).
+// SITES_NL lanes share one molecule for the monomer PES and DMS polynomial sums (FP64, the
+// dominant cost); lane 0 of each group then finishes the molecule.
+constexpr int SITES_NL = 8;
+
 template <int MODEL>
 __global__ void __launch_bounds__(128) k_sites(KP kp) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = gt % SITES_NL;
     const int b = blockIdx.y;
     const int N = kp.N, S = kp.S;
+    const bool valid = gt / SITES_NL < N;
+    const int w = valid ? gt / SITES_NL : N - 1;  // the shuffles need every lane of the warp
+    __shared__ double fsh_all[128 / SITES_NL][48];
+    double *fsh = fsh_all[threadIdx.x / SITES_NL];
     double av[14];
 #pragma unroll
     for (int i = 0; i < 14; i++) av[i] = 0.0;
-    if (w < N) {
+    {
         const double *RR = kp.RRt + (size_t)b * kp.natoms * 3 + 9 * w;
-        const double *RC = kp.RRc + 9 * w;
+        const int rep = rep_of(kp, b);
+        const double *RC = kp.RRc + (size_t)rep * kp.natoms * 3 + 9 * w;
+        const bool first_bead = (b == 0) || (kp.brep && kp.brep[b - 1] != rep);
         double R[4][3], Rc[4][3];
 #pragma unroll
         for (int k = 0; k < 3; k++)
@@ -89,16 +100,17 @@ __global__ void __launch_bounds__(128) k_sites(KP kp) {
         }
         double dr1[3][3], e1 = 0.0;
         if (!kp.contraction) {
-            nasa_pot(R, kp.box, kp.boxi, dr1, &e1);
+            nasa_pot_lanes<SITES_NL>(R, kp.box, kp.boxi, dr1, &e1, lane, fsh);
         } else {
 #pragma unroll
             for (int k = 0; k < 3; k++)
 #pragma unroll
                 for (int c = 0; c < 3; c++) dr1[k][c] = 0.0;
         }
-        av[ACC_UMON] = e1;
         double q3[3], dq3[3][3][3];
-        nasa_dms(R, kp.box, kp.boxi, kp.dms1, kp.dms2, kp.dms3, q3, dq3);
+        nasa_dms_lanes<SITES_NL>(R, kp.box, kp.boxi, kp.dms1, kp.dms2, kp.dms3, q3, dq3, lane, fsh);
+        if (lane == 0 && valid) {
+        av[ACC_UMON] = e1;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             q3[k] *= CHARGECON;
@@ -195,7 +207,7 @@ __global__ void __launch_bounds__(128) k_sites(KP kp) {
         for (int k = 0; k < 4; k++) {
             const size_t s = (size_t)b * S + k * N + w;
             kp.pos[s] = make_double4_32a(R[k][0], R[k][1], R[k][2], q[k]);
-            if (b == 0) kp.posc[k * N + w] = make_double4_32a(Rc[k][0], Rc[k][1], Rc[k][2], 0.0);
+            if (first_bead) kp.posc[(size_t)rep * S + k * N + w] = make_double4_32a(Rc[k][0], Rc[k][1], Rc[k][2], 0.0);
             kp.F[s] = make_double4_32a(Ef[k][0], Ef[k][1], Ef[k][2], ph[k]);
 #pragma unroll
             for (int c = 0; c < 3; c++) {
@@ -204,6 +216,7 @@ __global__ void __launch_bounds__(128) k_sites(KP kp) {
                 kp.Efdr[3 * s + c] = 0.0;
             }
         }
+        }  // lane 0
     }
     block_reduce_add<14, 128>(av, kp.acc + (size_t)b * NACC);
 }
@@ -230,8 +243,8 @@ __global__ void __launch_bounds__(128) k_pair_qq(KP kp) {
         for (int k = 1; k <= 4; k++) {
             si[k] = pos[(k - 1) * N + i];
             sj[k] = pos[(k - 1) * N + j];
-            ci[k] = kp.posc[(k - 1) * N + i];
-            cj[k] = kp.posc[(k - 1) * N + j];
+            ci[k] = posc_of(kp, b)[(k - 1) * N + i];
+            cj[k] = posc_of(kp, b)[(k - 1) * N + j];
         }
         double Rij[3];
         Rij[0] = min_image_rn(__dsub_rn(si[1].x, sj[1].x), kp.box[0], kp.boxi[0]);
@@ -401,6 +414,7 @@ __global__ void __launch_bounds__(128) k_after_qq(KP kp) {
             kp.dip[3 * gs + 0] = mu[0];
             kp.dip[3 * gs + 1] = mu[1];
             kp.dip[3 * gs + 2] = mu[2];
+            if (kp.dipf) kp.dipf[gs] = make_float4((float)mu[0], (float)mu[1], (float)mu[2], 0.f);
         }
     }
     block_reduce_add<3, 128>(av, kp.acc + (size_t)b * NACC);  // slot 2 = ACC_UELEC2
@@ -610,7 +624,7 @@ __global__ void __launch_bounds__(128) k_pair_force(KP kp) {
                     gi[isp][c] += dij[c];
                     gj[jsp][c] -= dij[c];
                 }
-                const double4_32a ca = kp.posc[(isp - 1) * N + i], cb = kp.posc[(jsp - 1) * N + j];
+                const double4_32a ca = posc_of(kp, b)[(isp - 1) * N + i], cb = posc_of(kp, b)[(jsp - 1) * N + j];
                 const double Rc[3] = {ca.x - cb.x + Rw[0], ca.y - cb.y + Rw[1], ca.z - cb.z + Rw[2]};
                 av[ACC_VIRIALC] += Rc[0] * dij[0] + Rc[1] * dij[1] + Rc[2] * dij[2];
 #pragma unroll
@@ -641,7 +655,7 @@ __global__ void __launch_bounds__(128) k_pair_force(KP kp) {
 #pragma unroll
         for (int k = 1; k <= 4; k++) {
             s[k] = pos[(k - 1) * N + w];
-            c4[k] = kp.posc[(k - 1) * N + w];
+            c4[k] = posc_of(kp, b)[(k - 1) * N + w];
             const double3 m = ld3(dip + 3 * ((k - 1) * N + w));
             mu[k][0] = T::dip(k) ? m.x : 0.0;
             mu[k][1] = T::dip(k) ? m.y : 0.0;
@@ -725,7 +739,8 @@ __global__ void __launch_bounds__(128) k_finish(KP kp) {
             dg[0][c] = g[18 + 0 + c] * phH1 + g[18 + 3 + c] * phH2 + g[18 + 6 + c] * phM;
         }
         const double4_32a O = pos[w], H1 = pos[N + w], H2 = pos[2 * N + w], M = pos[3 * N + w];
-        const double4_32a Oc = kp.posc[w], H1c = kp.posc[N + w], H2c = kp.posc[2 * N + w];
+        const double4_32a *pc = posc_of(kp, b);
+        const double4_32a Oc = pc[w], H1c = pc[N + w], H2c = pc[2 * N + w];
         const double o[3] = {O.x, O.y, O.z}, h1[3] = {H1.x, H1.y, H1.z}, h2[3] = {H2.x, H2.y, H2.z};
         const double m[3] = {M.x, M.y, M.z};
         const double oc[3] = {Oc.x, Oc.y, Oc.z}, h1c[3] = {H1c.x, H1c.y, H1c.z}, h2c[3] = {H2c.x, H2c.y, H2c.z};
@@ -831,7 +846,7 @@ static int pair_blocks(const Engine &E) {
 }
 
 void launch_sites(Engine &E) {
-    dim3 g((E.kp.N + 127) / 128, E.kp.P);
+    dim3 g((E.kp.N * SITES_NL + 127) / 128, E.kp.P);
     DISPATCH_TTM(E, k_sites, g, 128);
 }
 

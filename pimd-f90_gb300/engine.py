@@ -71,6 +71,18 @@ SIGNATURES = {
     "pimd_md_step": [_V, ctypes.POINTER(MDParams), _D, _D, _D, _D, _D, _D, ctypes.c_int, _D],
     "pimd_peak_flops": [ctypes.c_int, ctypes.c_int, _D],
     "pimd_set_graph": [_V, ctypes.c_int],
+    "pimd_autotune": [_V, _V, _V],
+    "pimd_get_tuning": [_V, _I, ctypes.c_int],
+    "pimd_batch_create": [ctypes.POINTER(_V), ctypes.POINTER(Params), _V, ctypes.c_int, ctypes.POINTER(MDParams)],
+    "pimd_batch_destroy": [_V],
+    "pimd_batch_last_error": [_V],
+    "pimd_batch_info": [_V, _I, _I],
+    "pimd_batch_set_state": [_V, ctypes.c_int, _D, _D],
+    "pimd_batch_get_state": [_V, ctypes.c_int, _D, _D, _D, _D],
+    "pimd_batch_forces": [_V],
+    "pimd_batch_autotune": [_V],
+    "pimd_batch_step": [_V, ctypes.c_int],
+    "pimd_batch_sync": [_V],
     "pimd_graph_info": [_V, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
     "pimd_neighbors_noalloc": [_V, ctypes.c_int, _D, ctypes.c_double, _V, ctypes.c_int, _V, _V],
     "pimd_timers_reset": [_V, ctypes.c_int],
@@ -91,7 +103,8 @@ def load(path=LIB):
         for name, args in SIGNATURES.items():
             f = getattr(L, name)
             f.argtypes = args
-            f.restype = {"pimd_last_error": ctypes.c_char_p, "pimd_launch_count": ctypes.c_longlong}.get(name, ctypes.c_int)
+            f.restype = {"pimd_last_error": ctypes.c_char_p, "pimd_batch_last_error": ctypes.c_char_p,
+                         "pimd_launch_count": ctypes.c_longlong}.get(name, ctypes.c_int)
         _lib = L
     return _lib
 
@@ -125,6 +138,11 @@ def make_params(d, precision=PIMD_FP64, device=0):
     p.precision = int(d.get("precision", precision))
     p.device = int(d.get("device", device))
     return p
+
+
+class Replica(ctypes.Structure):
+    _fields_ = [("natoms", ctypes.c_int), ("nbeads", ctypes.c_int), ("box", ctypes.c_double * 3),
+                ("temp", ctypes.c_double)]
 
 
 class ForceEngine:
@@ -312,3 +330,79 @@ class ForceEngine:
             L.pimd_timers_get(self.h, i, buf, 64, ctypes.byref(ms), ctypes.byref(cnt))
             out[buf.value.decode()] = (ms.value, cnt.value)
         return out
+
+    # ---- autotuner ---------------------------------------------------------------------
+    def autotune(self, RRt_ptr=None, RRc_ptr=None):
+        """Pick the fastest launch shapes on the current (or given device) positions."""
+        self._check(load().pimd_autotune(self.h, RRt_ptr, RRc_ptr), "autotune")
+        return self.tuning()
+
+    def tuning(self):
+        k = (ctypes.c_int * 5)()
+        self._check(load().pimd_get_tuning(self.h, k, 5), "get_tuning")
+        return dict(sf_tiled=k[0], sf_groups=k[1], ff_regs=k[2], max_slices=k[3], nbr_block=k[4])
+
+
+class ReplicaBatch:
+    """Independent ring polymers of uneven sizes stepped together (one CUDA graph per step).
+
+    replicas: list of dicts with natoms, nbeads, box (3,), temp. common: engine parameters
+    shared by all (pot_model, rc, rc1, eps_ewald or alpha/nmax, polar settings)."""
+
+    def __init__(self, common, replicas, delt, massO, massH, langevin=1, seed=12345, precision=PIMD_FP64, device=0):
+        L = load()
+        p = make_params(dict(dict(natoms=3, nbeads=1, box=(1.0, 1.0, 1.0)), **common), precision, device)
+        arr = (Replica * len(replicas))()
+        for i, r in enumerate(replicas):
+            arr[i].natoms = int(r["natoms"])
+            arr[i].nbeads = int(r["nbeads"])
+            for c in range(3):
+                arr[i].box[c] = float(r["box"][c])
+            arr[i].temp = float(r["temp"])
+        mp = ForceEngine.md_params(delt, massO, massH, langevin, seed)
+        h = _V()
+        rc = L.pimd_batch_create(ctypes.byref(h), ctypes.byref(p), ctypes.cast(arr, _V), len(replicas), ctypes.byref(mp))
+        if rc:
+            raise PimdError("pimd_batch_create failed (%d: %s)" % (rc, ERRORS.get(rc, "?")))
+        self.h = h
+        self.replicas = [dict(r) for r in replicas]
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().pimd_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def _check(self, rc, what):
+        if rc:
+            msg = load().pimd_batch_last_error(self.h)
+            raise PimdError("%s failed (%d: %s): %s" % (what, rc, ERRORS.get(rc, "?"), msg.decode() if msg else ""))
+
+    def groups(self):
+        n = ctypes.c_int()
+        g = (ctypes.c_int * len(self.replicas))()
+        self._check(load().pimd_batch_info(self.h, ctypes.byref(n), g), "batch_info")
+        return n.value, list(g)
+
+    def set_state(self, r, RRt, PPt):
+        self._check(load().pimd_batch_set_state(self.h, r, _p(_f64(RRt)), _p(_f64(PPt))), "batch_set_state")
+
+    def get_state(self, r):
+        rep = self.replicas[r]
+        shape = (rep["nbeads"], rep["natoms"], 3)
+        R, P, G, o = np.zeros(shape), np.zeros(shape), np.zeros(shape), np.zeros(4)
+        self._check(load().pimd_batch_get_state(self.h, r, _p(R), _p(P), _p(G), _p(o)), "batch_get_state")
+        return R, P, G, o
+
+    def forces(self):
+        self._check(load().pimd_batch_forces(self.h), "batch_forces")
+
+    def autotune(self):
+        self._check(load().pimd_batch_autotune(self.h), "batch_autotune")
+
+    def step(self, nsteps=1):
+        self._check(load().pimd_batch_step(self.h, int(nsteps)), "batch_step")
+
+    def sync(self):
+        self._check(load().pimd_batch_sync(self.h), "batch_sync")
