@@ -128,9 +128,9 @@ def run_batch(args, pkg):
 def run_large(args, pkg):
     """TTM3-F 4096 H2O x 32 beads, L = 49.72 A, Rc = 9 A, |n| <= 24: steps/s per precision form."""
     res = {}
-    for name, prec, graph, steps in (("mixed_graph", pkg.engine.PIMD_MIXED, True, args.steps),
-                                     ("mixed", pkg.engine.PIMD_MIXED, False, args.steps),
-                                     ("fp64", pkg.engine.PIMD_FP64, False, max(2, min(args.steps, 5)))):
+    for name, prec, graph, steps in (("mixed", pkg.engine.PIMD_MIXED, False, args.steps),
+                                     ("mixed_graph", pkg.engine.PIMD_MIXED, True, args.steps),
+                                     ("fp64", pkg.engine.PIMD_FP64, False, max(2, min(args.steps, 4)))):
         r = run_gpu_arm(args, pkg, 0, 1, 0, prec, steps, graph=graph)
         res[name] = dict(steps_per_s=steps / (r["dev_ms"] / 1000.0), ms_per_step=r["dev_ms"] / steps, steps=steps,
                          dipole_iterations_mean=float(np.mean(r["niters"])), clocks=r["clocks"])

@@ -172,6 +172,41 @@ int pimd_set_graph(pimd_ctx *ctx, int enable);
 int pimd_graph_info(pimd_ctx *ctx, long long *captures, long long *launches);
 
 /* ---------------------------------------------------------------------------------------
+ * Differentiation form (TTM3-F, FP64 contexts). Model parameters theta, in this order, with the
+ * published TTM3-F values (pot_mod.f90:16-24) and NASA PES scale factors (nasa_mod.f90) as
+ * defaults: */
+enum {
+    PIMD_TH_POLAR_M = 0, /* polarisability of the M site (A^3)                          */
+    PIMD_TH_A_DD,        /* Thole damping, dipole-dipole                                 */
+    PIMD_TH_A_CC,        /* Thole damping, charge-charge and charge-dipole               */
+    PIMD_TH_VDW_C,       /* O-O C6 (C/r^6)                                               */
+    PIMD_TH_VDW_D,       /* O-O Born-Mayer prefactor (D exp(-E r))                       */
+    PIMD_TH_VDW_E,       /* O-O Born-Mayer exponent                                      */
+    PIMD_TH_DMS1,        /* TTM3-F charge corrections dms_param1..3 (nasa.f90:234-242)   */
+    PIMD_TH_DMS2,
+    PIMD_TH_DMS3,
+    PIMD_TH_GAMMA_M,     /* M-site placement / charge redistribution gamma               */
+    PIMD_TH_F5Z,         /* NASA PES scale factors f5z, fbasis, fcore, frest             */
+    PIMD_TH_FBASIS,
+    PIMD_TH_FCORE,
+    PIMD_TH_FREST,
+    PIMD_NTHETA
+};
+int pimd_get_theta(pimd_ctx *ctx, double *theta);
+int pimd_set_theta(pimd_ctx *ctx, const double *theta);
+/* Forward: the force call of pimd_full_bead_forces (host arrays) that also records every
+ * induced-dipole iteration for the backward. Needs the dipole predictor off at this step
+ * (guess_initdip = 0 or t <= 4). No counterpart in the reference. */
+int pimd_pot_forward(pimd_ctx *ctx, const double *RRt, const double *RRc, double *Upott, int t);
+/* Backward: for E = sum_k Ebar[k] Upot_k of the last forward, the exact derivative of the
+ * computed energies -- the induced dipoles as the forward computed them, after its own number of
+ * Jacobi-SOR iterations per bead, differentiated through those iterations by the transposed
+ * (adjoint) iteration, which reuses the symmetric dipole-field operator -- with respect to the
+ * positions, dRRt(3,Natoms,P), and to theta, dtheta[PIMD_NTHETA]. Pair geometry is recomputed,
+ * not stored. No counterpart in the reference. */
+int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *dtheta);
+
+/* ---------------------------------------------------------------------------------------
  * Tile-shape autotuner. Times force calls of this context on its current positions (device
  * RRt(3,Natoms,P) and RRc(3,Natoms) if given, else the last ones it was called with) for
  * candidate launch shapes -- site groups of the structure-factor kernels, k-slices of the field

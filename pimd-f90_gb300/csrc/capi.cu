@@ -6,6 +6,7 @@
 
 #include "../../include/pimd_gb300.h"
 #include "engine.h"
+#include "nasa_tables.h"
 
 namespace pimd {
 
@@ -261,6 +262,26 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
         const double r = std::pow(base[i], 1.0 / 6.0);
         pf[i] = spc ? 0.0 : 1.0 / (r * r * r);
     }
+    for (int i = 1; i <= 4; i++) E.polfac[i] = pf[i];
+    // the differentiable parameters start at the published values
+    E.theta[PIMD_TH_POLAR_M] = m.polarM;
+    E.theta[PIMD_TH_A_DD] = m.aDD;
+    E.theta[PIMD_TH_A_CC] = m.aCCaCD;
+    E.theta[PIMD_TH_VDW_C] = m.vdwC;
+    E.theta[PIMD_TH_VDW_D] = m.vdwD;
+    E.theta[PIMD_TH_VDW_E] = m.vdwE;
+    E.theta[PIMD_TH_DMS1] = m.dms1;
+    E.theta[PIMD_TH_DMS2] = m.dms2;
+    E.theta[PIMD_TH_DMS3] = m.dms3;
+    E.theta[PIMD_TH_GAMMA_M] = m.gammaM;
+    E.theta[PIMD_TH_F5Z] = PIMD_NASA_F5Z;
+    E.theta[PIMD_TH_FBASIS] = PIMD_NASA_FBASIS;
+    E.theta[PIMD_TH_FCORE] = PIMD_NASA_FCORE;
+    E.theta[PIMD_TH_FREST] = PIMD_NASA_FREST;
+    kp.nasa_f5z = PIMD_NASA_F5Z;
+    E.vdwA_model = m.vdwA;
+    E.vdwB_model = m.vdwB;
+    E.rc = p->rc;
     for (int i = 1; i <= 4; i++)
         for (int j = 1; j <= 4; j++) {
             kp.pt.apol_qq[i][j] = (m.aCCaCD * pf[i]) * pf[j];
@@ -329,6 +350,7 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
     pot_init_constants(E);
     ewald_init(E);
     neighbors_init(E);
+    if (kp.model == 3) adjoint_init(E);
     return cuda_check(E, cudaDeviceSynchronize(), "init");
 }
 
@@ -483,6 +505,7 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
     PHASE("ewald_sq", launch_ewald_sq(E));
     PHASE("ewald_fq", launch_ewald_fq(E));
     PHASE("after_qq", launch_after_qq(E));
+    if (E.tape_on) tape_record(E, 0);
     if (E.capturing) {
         int rc = capture_dipole_loop(E, mixed);
         if (rc) return rc;
@@ -491,6 +514,7 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
         int iter = 1;
         for (; iter <= kp.polar_maxiter; iter++) {
             dipole_iteration(E, mixed);
+            if (E.tape_on) tape_record(E, iter);
             if (check_every > 0 && (iter % check_every) == 0 && iter < kp.polar_maxiter) {
                 cudaMemcpyAsync(E.h_allconv, kp.allconv, sizeof(int), cudaMemcpyDeviceToHost, E.stream);
                 cudaError_t e = cudaStreamSynchronize(E.stream);
@@ -555,6 +579,9 @@ int pimd_destroy(pimd_ctx *ctx) {
     }
     if (E.h_allconv) cudaFreeHost(E.h_allconv);
     if (E.h_pin) cudaFreeHost(E.h_pin);
+    if (E.d_tape) cudaFree(E.d_tape);
+    if (E.d_phiq) cudaFree(E.d_phiq);
+    if (E.d_adj) cudaFree(E.d_adj);
     if (E.gexec) cudaGraphExecDestroy(E.gexec);
     if (E.body_stream) cudaStreamDestroy(E.body_stream);
     if (E.own_stream && E.stream) cudaStreamDestroy(E.stream);

@@ -202,6 +202,17 @@ PIMD_D void self2(double drsq, const EwC &e, double *ts1, double *ts2) {
     *ts2 = kr2 + ch2;
 }
 
+// dij of the dipole-dipole term: sum_ab di_a T_abc dj_b for the rank-3 Thole tensor
+// T_abc = 15 t3 R_a R_b R_c - 3 t2 (d_bc R_a + d_ac R_b + d_ab R_c)  (pot_ttm.f90:430-441)
+PIMD_D void dd_force(const double R[3], const double di[3], const double dj[3], double t2, double t3, double dij[3]) {
+    const double rdi = R[0] * di[0] + R[1] * di[1] + R[2] * di[2];
+    const double rdj = R[0] * dj[0] + R[1] * dj[1] + R[2] * dj[2];
+    const double didj = di[0] * dj[0] + di[1] * dj[1] + di[2] * dj[2];
+    const double a = 15.0 * t3 * rdi * rdj - 3.0 * t2 * didj;
+#pragma unroll
+    for (int c = 0; c < 3; c++) dij[c] += a * R[c] - 3.0 * t2 * (rdi * dj[c] + rdj * di[c]);
+}
+
 // ---------------------------------------------------------------------------------------
 // block-wide sum of NV doubles into per-bead accumulators (one atomic per value per block)
 template <int NV, int NT>

@@ -66,6 +66,8 @@ struct KP {
     double vdwA, vdwB, vdwC, vdwD, vdwE, shiftA, shiftB;
     double gammaM, polar[5], dms1, dms2, dms3, polar_sor, stath, factor, Uvdw_lrc;
     double qO, qH, roh0, th0, harmkb, harmka;
+    const double *c5z;   // NASA PES coefficients for non-default scale factors (null: published)
+    double nasa_f5z;     // NASA scale factor of deoh / phh1
     EwC ew;
     EwCf ewf;  // FP32 copy for the mixed engine
     PairTables pt;
@@ -164,6 +166,18 @@ struct Engine {
     cudaGraphExec_t gexec = nullptr;
     std::vector<const void *> gkey;
     long long graph_launches = 0, graph_captures = 0;
+    // differentiation form (adjoint.cu): model parameters theta and the forward's tape
+    double theta[PIMD_NTHETA];
+    double *d_c5z = nullptr;     // NASA coefficients for the current theta
+    bool tape_on = false;        // record the dipole iterations during the force call
+    int tape_kmax = 0;           // iterations the tape holds
+    double *d_tape = nullptr;    // [kmax + 1][P][N][3] dipoles of the dipole sites per iteration
+    double *d_phiq = nullptr;    // [P][S] charge-only potential after the charge phase
+    double *d_adj = nullptr;     // backward scratch
+    size_t adj_bytes = 0;
+    bool tape_valid = false;
+    double polfac[5] = {0, 0, 0, 0, 0};  // polfac^(-1/2) per site kind (potential.f90:244-245)
+    double vdwA_model = 0, vdwB_model = 0, rc = 0;
     // normal modes (filled by pimd_nm_init)
     int nm_P = 0;
     double *d_nmC = nullptr, *d_nmA = nullptr;  // C(P,P), [A11,A12,A21,A22,msf,c1,c2] x P
@@ -199,6 +213,15 @@ int create_context(Engine &E, const pimd_params *p, int nrep, const int *brep);
 void timer_begin(Engine &E, const char *name);
 void timer_end(Engine &E);
 int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt, double *virialct, double *virt9);
+
+// differentiation form (adjoint.cu)
+void tape_record(Engine &E, int iter);
+int apply_theta(Engine &E);
+void adjoint_init(Engine &E);
+void adj_structure_factor(Engine &E, const double *dipbuf, double2 *Sout, double *bacc);
+void adj_dipole_field(Engine &E, double2 *Sm_u, double *bacc, double *Dr);
+void adj_rec(Engine &E, int mode, const double *a, const double *bvec, const double2 *SA, const double2 *SB,
+             const double *ebw, double *grad, double *phi);
 
 // launchers (neighbors.cu)
 void neighbors_init(Engine &E);

@@ -1030,6 +1030,13 @@ void ewald_init(Engine &E) {
     if (sfac_tiles(E) != 0) E.sf_tiled = false;  // allocation failed: untiled kernel
     ewald_attrs<double>();
     ewald_attrs<float>();
+    // k_field_f stages [1 or 2][64 runs][LZM] complex weights: 50 KB for LZM = 49 in QD mode
+#define PIMD_FF_ATTR(MODE, LZM) cudaFuncSetAttribute(k_field_f<MODE, LZM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    PIMD_FF_ATTR(F_Q, 17) PIMD_FF_ATTR(F_D, 17) PIMD_FF_ATTR(F_QD, 17)
+    PIMD_FF_ATTR(F_Q, 25) PIMD_FF_ATTR(F_D, 25) PIMD_FF_ATTR(F_QD, 25)
+    PIMD_FF_ATTR(F_Q, 33) PIMD_FF_ATTR(F_D, 33) PIMD_FF_ATTR(F_QD, 33)
+    PIMD_FF_ATTR(F_Q, 49) PIMD_FF_ATTR(F_D, 49) PIMD_FF_ATTR(F_QD, 49)
+#undef PIMD_FF_ATTR
     cudaFuncSetAttribute(k_sfac_f<OP_Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     cudaFuncSetAttribute(k_sfac_f<OP_MU>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     cudaFuncSetAttribute(k_sfac_f<OP_DIP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
@@ -1041,6 +1048,139 @@ void launch_ewald_tables(Engine &E) {
         k_ewald_tables<float><<<g, 128, 0, E.stream>>>(E.kp);
     else
         k_ewald_tables<double><<<g, 128, 0, E.stream>>>(E.kp);
+    ++E.nlaunch;
+}
+
+// ---------------------------------------------------------------------------------------
+// Backward (adjoint) helpers of the differentiation form, FP64 engine only.
+
+// Structure factor of the dipole set dipbuf ([P][S][3], dipole sites filled) into Sout in the
+// forward's rotated form (-Im, Re) of sum_s (k.mu_s) e^{ik.r_s}; beads with bacc[ACC_CONV] != 0
+// are skipped.
+void adj_structure_factor(Engine &E, const double *dipbuf, double2 *Sout, double *bacc) {
+    const KP keep = E.kp;
+    E.kp.dip = const_cast<double *>(dipbuf);
+    E.kp.Sm = Sout;
+    E.kp.acc = bacc;
+    run_spass_t<OP_MU, double>(E, E.kp.fd, E.kp.ld - E.kp.fd, 1);
+    E.kp = keep;
+}
+
+// Dr[b][s] += reciprocal dipole field at the dipole sites from the structure factor Sm_u (the
+// forward's k_field<F_D> without the SOR update)
+__global__ void __launch_bounds__(128) k_adj_fsum(KP kp, int s0, int s1, int nslice, double *Dr) {
+    const int b = blockIdx.y, s = s0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= s1 || kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
+    double E[3] = {0, 0, 0};
+    for (int z = 0; z < nslice; z++) {
+        const double4_32a p = kp.Fpart[((size_t)z * kp.P + b) * (s1 - s0) + (s - s0)];
+        E[0] += p.x;
+        E[1] += p.y;
+        E[2] += p.z;
+    }
+    double *o = Dr + 3 * ((size_t)b * kp.S + s);
+    o[0] += E[0];
+    o[1] += E[1];
+    o[2] += E[2];
+}
+
+void adj_dipole_field(Engine &E, double2 *Sm_u, double *bacc, double *Dr) {
+    const KP keep = E.kp;
+    E.kp.Sm = Sm_u;
+    E.kp.acc = bacc;
+    const int s0 = E.kp.fd, s1 = E.kp.ld, NT = 128;
+    const int LZ = 2 * E.kp.lmax + 1;
+    const size_t smem = ((size_t)LZ * NT * 2 + (size_t)KCH * 5) * sizeof(double);
+    const int sblocks = (s1 - s0 + NT - 1) / NT;
+    int ns = (int)((4L * 152 + (long)sblocks * E.kp.P - 1) / ((long)sblocks * E.kp.P));
+    ns = std::max(1, std::min(ns, std::min(E.nchunk, E.max_slices)));
+    dim3 g(sblocks, E.kp.P, ns);
+    if ((size_t)LZ * 128 * 16 <= 64 * 1024)
+        k_field<F_D, 128, double><<<g, NT, smem, E.stream>>>(E.kp, s0, s1);
+    dim3 g2((s1 - s0 + 127) / 128, E.kp.P);
+    k_adj_fsum<<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns, Dr);
+    E.nlaunch += 2;
+    E.kp = keep;
+}
+
+// Reciprocal-space gradients of the backward, thread per site, FP64, direct sum over the
+// k-list (c_k = 4 pi A_k / V, S raw = sum (k.mu) e^{ik.r} or sum q e^{ik.r}):
+//   BIL  : d/dr_s [u^T D_rec v] = sum_k c_k k [(k.u_s) Im(e_s conj S_v) + (k.v_s) Im(e_s conj S_u)]
+//   CROSS: d/dr_s [nu^T E_q,rec] = sum_k c_k k (k.nu_s) Re(e_s conj S_q) (dipole sites)
+//                                 - q_s sum_k c_k k Re(e_s conj S_nu)    (charged sites)
+//          and the potential of the nu dipoles phi_s = -sum_k c_k Im(e_s conj S_nu).
+// Derived from the forward's field formula E_s = sum_k c_k k Im(e_s conj S) (ewald.f90:45-49,
+// 114-117): the k-space operator is the Hessian of a quadratic form, so these are exact.
+enum { ADJ_BIL = 0, ADJ_CROSS = 1 };
+template <int MODE>
+__global__ void __launch_bounds__(128) k_adj_rec(KP kp, int s0, int s1, const double *a, const double *bvec,
+                                                 const double2 *SA, const double2 *SB, const double *ebw,
+                                                 double *grad, double *phi) {
+    const int b = blockIdx.y, s = s0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= s1 || ebw[b] == 0.0) return;
+    const size_t gs = (size_t)b * kp.S + s;
+    const double q = kp.pos[gs].w;
+    const bool isdip = s >= kp.fd && s < kp.ld;
+    double av[3] = {0, 0, 0}, bv[3] = {0, 0, 0};
+    if (isdip) {
+        for (int c = 0; c < 3; c++) {
+            av[c] = a[3 * gs + c];
+            if (MODE == ADJ_BIL) bv[c] = bvec[3 * gs + c];
+        }
+    }
+    double G[3] = {0, 0, 0}, ph = 0.0;
+    for (int r = 0; r < kp.nrun; r++) {
+        const KRun run = kp.runs[r];
+        const double2 ex = tab_x<double>(kp, b, run.kx, s);
+        const double2 ey = tab_y<double>(kp, b, run.ky, s);
+        const double2 exy = make_double2(ex.x * ey.x - ex.y * ey.y, ex.y * ey.x + ex.x * ey.y);
+        for (int j = 0; j < run.nkz; j++) {
+            const int k = run.kbeg + j, kz = run.kzlo + j;
+            double2 z = tab_z<double>(kp, b, kz < 0 ? -kz : kz, s);
+            if (kz < 0) z = cconj(z);
+            const double2 e = cmul(exy, z);
+            const double4_32a ki = kp.kinfo[k];
+            const double kv[3] = {ki.x, ki.y, ki.z}, ck = ki.w;
+            if (MODE == ADJ_BIL) {
+                if (!isdip) continue;
+                // raw S from the rotated (-Im, Re) form: raw = (y, -x)
+                const double2 su = SA[(size_t)b * kp.nk + k], sv = SB[(size_t)b * kp.nk + k];
+                const double2 cu = make_double2(su.y, su.x), cv = make_double2(sv.y, sv.x);  // conj(raw)
+                const double imv = e.x * cv.y + e.y * cv.x, imu = e.x * cu.y + e.y * cu.x;
+                const double ku = kv[0] * av[0] + kv[1] * av[1] + kv[2] * av[2];
+                const double kw = kv[0] * bv[0] + kv[1] * bv[1] + kv[2] * bv[2];
+                const double f = ck * (ku * imv + kw * imu);
+                for (int c = 0; c < 3; c++) G[c] += f * kv[c];
+            } else {
+                if (isdip) {
+                    const double2 sq = kp.Sq[(size_t)b * kp.nk + k];  // raw charge structure factor
+                    const double re = e.x * sq.x + e.y * sq.y;          // Re(e conj Sq)
+                    const double kn = kv[0] * av[0] + kv[1] * av[1] + kv[2] * av[2];
+                    for (int c = 0; c < 3; c++) G[c] += ck * kn * re * kv[c];
+                }
+                if (q != 0.0) {
+                    const double2 sn = SA[(size_t)b * kp.nk + k];
+                    const double2 cn = make_double2(sn.y, sn.x);  // conj(raw S_nu)
+                    const double re = e.x * cn.x - e.y * cn.y, im = e.x * cn.y + e.y * cn.x;
+                    for (int c = 0; c < 3; c++) G[c] -= q * ck * re * kv[c];
+                    ph -= ck * im;
+                }
+            }
+        }
+    }
+    const double w = ebw[b];  // per-bead scale (0: bead inactive)
+    for (int c = 0; c < 3; c++) grad[3 * gs + c] += w * G[c];
+    if (MODE == ADJ_CROSS && phi) phi[gs] += w * ph;
+}
+
+void adj_rec(Engine &E, int mode, const double *a, const double *bvec, const double2 *SA, const double2 *SB,
+             const double *ebw, double *grad, double *phi) {
+    const int s0 = (mode == ADJ_BIL) ? E.kp.fd : 0, s1 = (mode == ADJ_BIL) ? E.kp.ld : E.kp.S;
+    dim3 g((s1 - s0 + 127) / 128, E.kp.P);
+    if (mode == ADJ_BIL)
+        k_adj_rec<ADJ_BIL><<<g, 128, 0, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
+    else
+        k_adj_rec<ADJ_CROSS><<<g, 128, 0, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
     ++E.nlaunch;
 }
 

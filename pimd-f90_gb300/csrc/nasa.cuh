@@ -1,7 +1,6 @@
 // nasa.cuh -- Partridge-Schwenke water monomer PES and dipole-moment surface on the device.
 // Restates pot_ttm/nasa.f90:2-103 (pot_nasa) and :105-293 (dms_nasa) in FP64; one thread
-// evaluates one molecule (nasa_pot / nasa_dms) or NL lanes share one (the _lanes variants).
-// Coefficient tables live in constant memory (all threads of a warp
+// evaluates one molecule. Coefficient tables live in constant memory (all threads of a warp
 // read the same term at the same time, so the reads are broadcasts).
 #pragma once
 #include "common.cuh"
@@ -9,14 +8,41 @@
 
 namespace pimd {
 
-__constant__ double c_c5z[245];
-__constant__ double c_coefD[84];
-__constant__ unsigned char c_idx[245][3];
-__constant__ unsigned char c_idxD[84][3];
+// Per translation unit (each .cu that includes this header has its own copy in its own device
+// module): nasa_upload_constants() fills this unit's copy.
+static __constant__ double c_c5z[245];
+static __constant__ double c_coefD[84];
+static __constant__ unsigned char c_idx[245][3];
+static __constant__ unsigned char c_idxD[84][3];
+
+// c5z = f5z C5ZA + fbasis CBASIS + fcore CCORE + frest CREST (nasa_mod.f90) and the index tables
+static inline void nasa_upload_constants() {
+    double c5z[245];
+    for (int j = 0; j < 245; j++)
+        c5z[j] = PIMD_NASA_F5Z * PIMD_NASA_C5ZA[j] + PIMD_NASA_FBASIS * PIMD_NASA_CBASIS[j] +
+                 PIMD_NASA_FCORE * PIMD_NASA_CCORE[j] + PIMD_NASA_FREST * PIMD_NASA_CREST[j];
+    unsigned char idx[245][3], idxD[84][3];
+    for (int j = 0; j < 245; j++) {
+        idx[j][0] = (unsigned char)PIMD_NASA_IDX1[j];
+        idx[j][1] = (unsigned char)PIMD_NASA_IDX2[j];
+        idx[j][2] = (unsigned char)PIMD_NASA_IDX3[j];
+    }
+    for (int j = 0; j < 84; j++) {
+        idxD[j][0] = (unsigned char)PIMD_NASA_IDXD1[j];
+        idxD[j][1] = (unsigned char)PIMD_NASA_IDXD2[j];
+        idxD[j][2] = (unsigned char)PIMD_NASA_IDXD3[j];
+    }
+    cudaMemcpyToSymbol(c_c5z, c5z, sizeof(c5z));
+    cudaMemcpyToSymbol(c_coefD, PIMD_NASA_COEFD, sizeof(double) * 84);
+    cudaMemcpyToSymbol(c_idx, idx, sizeof(idx));
+    cudaMemcpyToSymbol(c_idxD, idxD, sizeof(idxD));
+}
 
 // r1[atom][comp]: atoms O, H1, H2. Returns energy (kcal/mol) and gradient dr1[atom][comp].
+// c5zg: the 245 combined coefficients when the four scale factors differ from the published
+// ones (null: the constant-memory table), f5z: the CCSD(T)/5Z scale factor of deoh and phh1.
 PIMD_D void nasa_pot(const double r1[3][3], const double box[3], const double boxi[3], double dr1[3][3],
-                     double *e1) {
+                     double *e1, const double *c5zg = nullptr, double f5z = PIMD_NASA_F5Z) {
     double ROH1[3], ROH2[3], RHH[3];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
@@ -30,8 +56,8 @@ PIMD_D void nasa_pot(const double r1[3][3], const double box[3], const double bo
     const double costh = (ROH1[0] * ROH2[0] + ROH1[1] * ROH2[1] + ROH1[2] * ROH2[2]) / (dROH1 * dROH2);
     const double reoh = PIMD_NASA_REOH, b1 = PIMD_NASA_B1, roh = PIMD_NASA_ROH, alphaoh = PIMD_NASA_ALPHAOH,
                  phh2 = PIMD_NASA_PHH2;
-    const double deoh = PIMD_NASA_F5Z * PIMD_NASA_DEOHA;
-    const double phh1 = (PIMD_NASA_F5Z * PIMD_NASA_PHH1A) * exp(phh2);
+    const double deoh = f5z * PIMD_NASA_DEOHA;
+    const double phh1 = (f5z * PIMD_NASA_PHH1A) * exp(phh2);
     const double costhe = -.24780227221366464506;
     const double exp1 = exp(-alphaoh * (dROH1 - roh));
     const double exp2 = exp(-alphaoh * (dROH2 - roh));
@@ -54,14 +80,14 @@ PIMD_D void nasa_pot(const double r1[3][3], const double box[3], const double bo
     double sum0 = 0, sum1 = 0, sum2 = 0, sum3 = 0;
     for (int j = 1; j < 245; j++) {
         const int inI = c_idx[j][0], inJ = c_idx[j][1], inK = c_idx[j][2];
-        const double c = c_c5z[j];
+        const double c = c5zg ? c5zg[j] : c_c5z[j];
         const double sym = f1[inI] * f2[inJ] + f1[inJ] * f2[inI];
         sum0 += c * sym * f3[inK];
         sum1 += c * ((double)(inI - 1) * f1[inI - 1] * f2[inJ] + (double)(inJ - 1) * f1[inJ - 1] * f2[inI]) * f3[inK];
         sum2 += c * ((double)(inJ - 1) * f1[inI] * f2[inJ - 1] + (double)(inI - 1) * f1[inJ] * f2[inI - 1]) * f3[inK];
         sum3 += c * sym * (double)(inK - 1) * f3[inK - 1];
     }
-    const double Vc = 2.0 * c_c5z[0] + efac * sum0;
+    const double Vc = 2.0 * (c5zg ? c5zg[0] : c_c5z[0]) + efac * sum0;
     *e1 = ((Va + Vb + Vc) + 0.44739574026257) * 0.00285914375100642899;
     const double dVcdr1 = (-2.0 * b1 * efac * (dROH1 - reoh) * sum0 + efac * sum1 / reoh) / dROH1;
     const double dVcdr2 = (-2.0 * b1 * efac * (dROH2 - reoh) * sum0 + efac * sum2 / reoh) / dROH2;
@@ -193,138 +219,6 @@ PIMD_D void nasa_dms(const double r1[3][3], const double box[3], const double bo
         dp2dr2 += cf * ((double)(inI - 1) * f1[inJ] * f2[inI - 1] * f3[inK]);
         dp2dcabc += cf * ((double)(inK - 1) * f1[inJ] * f2[inI] * f3[inK - 1]);
     }
-    nasa_dms_finish(ROH1, ROH2, dROH1, dROH2, costh, efac, P1, P2, dp1dr1, dp1dr2, dp1dcabc, dp2dr1, dp2dr2, dp2dcabc,
-                    PL1, PL2, dms1, dms2, dms3, q3, gradq);
-}
-
-// ---------------------------------------------------------------------------------------
-// Lane-split variants: NL consecutive lanes of a warp evaluate one molecule. The powers of the
-// three internal coordinates go to the molecule's shared-memory row fsh[48] (f1, f2, f3), each
-// lane sums every NL-th polynomial term, and butterfly shuffles inside the lane group combine
-// the partial sums, so every lane ends with the molecule's full result. All 32 lanes of the
-// warp must call these together.
-template <int NL>
-PIMD_D void nasa_powers(double x1, double x2, double x3, int lane, double *fsh) {
-    __syncwarp();
-    if (lane < 3) {
-        const double x = lane == 0 ? x1 : (lane == 1 ? x2 : x3);
-        double *f = fsh + 16 * lane;
-        f[0] = 0.0;
-        f[1] = 1.0;
-        for (int j = 2; j <= 15; j++) f[j] = f[j - 1] * x;
-    }
-    __syncwarp();
-}
-
-template <int NL>
-PIMD_D double group_sum(double v) {
-#pragma unroll
-    for (int o = NL / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-template <int NL>
-PIMD_D void nasa_pot_lanes(const double r1[3][3], const double box[3], const double boxi[3], double dr1[3][3],
-                           double *e1, int lane, double *fsh) {
-    double ROH1[3], ROH2[3], RHH[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        ROH1[c] = min_image_rn(__dsub_rn(r1[1][c], r1[0][c]), box[c], boxi[c]);
-        ROH2[c] = min_image_rn(__dsub_rn(r1[2][c], r1[0][c]), box[c], boxi[c]);
-        RHH[c] = min_image_rn(__dsub_rn(r1[1][c], r1[2][c]), box[c], boxi[c]);
-    }
-    const double dROH1 = sqrt(ROH1[0] * ROH1[0] + ROH1[1] * ROH1[1] + ROH1[2] * ROH1[2]);
-    const double dROH2 = sqrt(ROH2[0] * ROH2[0] + ROH2[1] * ROH2[1] + ROH2[2] * ROH2[2]);
-    const double dRHH = sqrt(RHH[0] * RHH[0] + RHH[1] * RHH[1] + RHH[2] * RHH[2]);
-    const double costh = (ROH1[0] * ROH2[0] + ROH1[1] * ROH2[1] + ROH1[2] * ROH2[2]) / (dROH1 * dROH2);
-    const double reoh = PIMD_NASA_REOH, b1 = PIMD_NASA_B1, roh = PIMD_NASA_ROH, alphaoh = PIMD_NASA_ALPHAOH,
-                 phh2 = PIMD_NASA_PHH2;
-    const double deoh = PIMD_NASA_F5Z * PIMD_NASA_DEOHA;
-    const double phh1 = (PIMD_NASA_F5Z * PIMD_NASA_PHH1A) * exp(phh2);
-    const double costhe = -.24780227221366464506;
-    const double exp1 = exp(-alphaoh * (dROH1 - roh));
-    const double exp2 = exp(-alphaoh * (dROH2 - roh));
-    const double Va = deoh * (exp1 * (exp1 - 2.0) + exp2 * (exp2 - 2.0));
-    const double Vb = phh1 * exp(-phh2 * dRHH);
-    const double dVa1 = 2.0 * alphaoh * deoh * exp1 * (1.0 - exp1) / dROH1;
-    const double dVa2 = 2.0 * alphaoh * deoh * exp2 * (1.0 - exp2) / dROH2;
-    const double dVb = -phh2 * Vb / dRHH;
-    const double x1 = (dROH1 - reoh) / reoh, x2 = (dROH2 - reoh) / reoh, x3 = costh - costhe;
-    nasa_powers<NL>(x1, x2, x3, lane, fsh);
-    const double *f1 = fsh, *f2 = fsh + 16, *f3 = fsh + 32;
-    const double efac = exp(-b1 * ((dROH1 - reoh) * (dROH1 - reoh) + (dROH2 - reoh) * (dROH2 - reoh)));
-    double sum0 = 0, sum1 = 0, sum2 = 0, sum3 = 0;
-    for (int j = 1 + lane; j < 245; j += NL) {
-        const int inI = c_idx[j][0], inJ = c_idx[j][1], inK = c_idx[j][2];
-        const double c = c_c5z[j];
-        const double sym = f1[inI] * f2[inJ] + f1[inJ] * f2[inI];
-        sum0 += c * sym * f3[inK];
-        sum1 += c * ((double)(inI - 1) * f1[inI - 1] * f2[inJ] + (double)(inJ - 1) * f1[inJ - 1] * f2[inI]) * f3[inK];
-        sum2 += c * ((double)(inJ - 1) * f1[inI] * f2[inJ - 1] + (double)(inI - 1) * f1[inJ] * f2[inI - 1]) * f3[inK];
-        sum3 += c * sym * (double)(inK - 1) * f3[inK - 1];
-    }
-    sum0 = group_sum<NL>(sum0);
-    sum1 = group_sum<NL>(sum1);
-    sum2 = group_sum<NL>(sum2);
-    sum3 = group_sum<NL>(sum3);
-    const double Vc = 2.0 * c_c5z[0] + efac * sum0;
-    *e1 = ((Va + Vb + Vc) + 0.44739574026257) * 0.00285914375100642899;
-    const double dVcdr1 = (-2.0 * b1 * efac * (dROH1 - reoh) * sum0 + efac * sum1 / reoh) / dROH1;
-    const double dVcdr2 = (-2.0 * b1 * efac * (dROH2 - reoh) * sum0 + efac * sum2 / reoh) / dROH2;
-    const double dVcdcth = efac * sum3;
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        double g1 = dVa1 * ROH1[c] + dVb * RHH[c] + dVcdr1 * ROH1[c] +
-                    dVcdcth * (ROH2[c] / (dROH1 * dROH2) - costh * ROH1[c] / (dROH1 * dROH1));
-        double g2 = dVa2 * ROH2[c] - dVb * RHH[c] + dVcdr2 * ROH2[c] +
-                    dVcdcth * (ROH1[c] / (dROH1 * dROH2) - costh * ROH2[c] / (dROH2 * dROH2));
-        dr1[1][c] = g1 * .00285914375100642899;
-        dr1[2][c] = g2 * .00285914375100642899;
-        dr1[0][c] = -(g1 + g2) * .00285914375100642899;
-    }
-}
-
-// dms_nasa with the 84-term sums split over NL lanes (same outputs as nasa_dms)
-template <int NL>
-PIMD_D void nasa_dms_lanes(const double r1[3][3], const double box[3], const double boxi[3], double dms1, double dms2,
-                           double dms3, double q3[3], double gradq[3][3][3], int lane, double *fsh) {
-    const double reoh = PIMD_NASA_REOH, b1D = PIMD_NASA_B1D, costhe = -.24780227221366464506;
-    double ROH1[3], ROH2[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        ROH1[c] = min_image_rn(__dsub_rn(r1[1][c], r1[0][c]), box[c], boxi[c]);
-        ROH2[c] = min_image_rn(__dsub_rn(r1[2][c], r1[0][c]), box[c], boxi[c]);
-    }
-    const double dROH1 = sqrt(ROH1[0] * ROH1[0] + ROH1[1] * ROH1[1] + ROH1[2] * ROH1[2]);
-    const double dROH2 = sqrt(ROH2[0] * ROH2[0] + ROH2[1] * ROH2[1] + ROH2[2] * ROH2[2]);
-    const double costh = (ROH1[0] * ROH2[0] + ROH1[1] * ROH2[1] + ROH1[2] * ROH2[2]) / (dROH1 * dROH2);
-    const double efac = exp(-b1D * ((dROH1 - reoh) * (dROH1 - reoh) + (dROH2 - reoh) * (dROH2 - reoh)));
-    const double x1 = (dROH1 - reoh) / reoh, x2 = (dROH2 - reoh) / reoh, x3 = costh - costhe;
-    nasa_powers<NL>(x1, x2, x3, lane, fsh);
-    const double *f1 = fsh, *f2 = fsh + 16, *f3 = fsh + 32;
-    double P1 = 0, P2 = 0;
-    const double PL1 = costh, PL2 = 0.5 * (3.0 * PL1 * PL1 - 1.0);
-    double dp1dr1 = 0, dp1dr2 = 0, dp1dcabc = 0, dp2dr1 = 0, dp2dr2 = 0, dp2dcabc = 0;
-    for (int j = 1 + lane; j < 84; j += NL) {
-        const int inI = c_idxD[j][0], inJ = c_idxD[j][1], inK = c_idxD[j][2];
-        const double cf = c_coefD[j];
-        P1 += cf * f1[inI] * f2[inJ] * f3[inK];
-        P2 += cf * f1[inJ] * f2[inI] * f3[inK];
-        dp1dr1 += cf * ((double)(inI - 1) * f1[inI - 1] * f2[inJ] * f3[inK]);
-        dp1dr2 += cf * ((double)(inJ - 1) * f1[inI] * f2[inJ - 1] * f3[inK]);
-        dp1dcabc += cf * ((double)(inK - 1) * f1[inI] * f2[inJ] * f3[inK - 1]);
-        dp2dr1 += cf * ((double)(inJ - 1) * f1[inJ - 1] * f2[inI] * f3[inK]);
-        dp2dr2 += cf * ((double)(inI - 1) * f1[inJ] * f2[inI - 1] * f3[inK]);
-        dp2dcabc += cf * ((double)(inK - 1) * f1[inJ] * f2[inI] * f3[inK - 1]);
-    }
-    P1 = group_sum<NL>(P1);
-    P2 = group_sum<NL>(P2);
-    dp1dr1 = group_sum<NL>(dp1dr1);
-    dp1dr2 = group_sum<NL>(dp1dr2);
-    dp1dcabc = group_sum<NL>(dp1dcabc);
-    dp2dr1 = group_sum<NL>(dp2dr1);
-    dp2dr2 = group_sum<NL>(dp2dr2);
-    dp2dcabc = group_sum<NL>(dp2dcabc);
     nasa_dms_finish(ROH1, ROH2, dROH1, dROH2, costh, efac, P1, P2, dp1dr1, dp1dr2, dp1dcabc, dp2dr1, dp2dr2, dp2dcabc,
                     PL1, PL2, dms1, dms2, dms3, q3, gradq);
 }

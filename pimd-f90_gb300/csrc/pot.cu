@@ -32,25 +32,8 @@ struct TT {
 };
 
 void pot_init_constants(Engine &E) {
-    double c5z[245];
-    for (int j = 0; j < 245; j++)
-        c5z[j] = PIMD_NASA_F5Z * PIMD_NASA_C5ZA[j] + PIMD_NASA_FBASIS * PIMD_NASA_CBASIS[j] +
-                 PIMD_NASA_FCORE * PIMD_NASA_CCORE[j] + PIMD_NASA_FREST * PIMD_NASA_CREST[j];
-    unsigned char idx[245][3], idxD[84][3];
-    for (int j = 0; j < 245; j++) {
-        idx[j][0] = (unsigned char)PIMD_NASA_IDX1[j];
-        idx[j][1] = (unsigned char)PIMD_NASA_IDX2[j];
-        idx[j][2] = (unsigned char)PIMD_NASA_IDX3[j];
-    }
-    for (int j = 0; j < 84; j++) {
-        idxD[j][0] = (unsigned char)PIMD_NASA_IDXD1[j];
-        idxD[j][1] = (unsigned char)PIMD_NASA_IDXD2[j];
-        idxD[j][2] = (unsigned char)PIMD_NASA_IDXD3[j];
-    }
-    cudaMemcpyToSymbol(c_c5z, c5z, sizeof(c5z));
-    cudaMemcpyToSymbol(c_coefD, PIMD_NASA_COEFD, sizeof(double) * 84);
-    cudaMemcpyToSymbol(c_idx, idx, sizeof(idx));
-    cudaMemcpyToSymbol(c_idxD, idxD, sizeof(idxD));
+    (void)E;
+    nasa_upload_constants();
 }
 
 PIMD_D double3 ld3(const double *p) { return make_double3(p[0], p[1], p[2]); }
@@ -58,24 +41,15 @@ PIMD_D double3 ld3(const double *p) { return make_double3(p[0], p[1], p[2]); }
 // ---------------------------------------------------------------------------------------
 // pot_ttm.f90:56-151 and 232-261: site layout, M sites, NASA PES + DMS charges, monomer
 // virials, self energy and intramolecular Ewald exclusions. One thread per (molecule, bead).
-// SITES_NL lanes share one molecule for the monomer PES and DMS polynomial sums (FP64, the
-// dominant cost); lane 0 of each group then finishes the molecule.
-constexpr int SITES_NL = 8;
-
 template <int MODEL>
 __global__ void __launch_bounds__(128) k_sites(KP kp) {
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = gt % SITES_NL;
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
     const int b = blockIdx.y;
     const int N = kp.N, S = kp.S;
-    const bool valid = gt / SITES_NL < N;
-    const int w = valid ? gt / SITES_NL : N - 1;  // the shuffles need every lane of the warp
-    __shared__ double fsh_all[128 / SITES_NL][48];
-    double *fsh = fsh_all[threadIdx.x / SITES_NL];
     double av[14];
 #pragma unroll
     for (int i = 0; i < 14; i++) av[i] = 0.0;
-    {
+    if (w < N) {
         const double *RR = kp.RRt + (size_t)b * kp.natoms * 3 + 9 * w;
         const int rep = rep_of(kp, b);
         const double *RC = kp.RRc + (size_t)rep * kp.natoms * 3 + 9 * w;
@@ -100,17 +74,16 @@ __global__ void __launch_bounds__(128) k_sites(KP kp) {
         }
         double dr1[3][3], e1 = 0.0;
         if (!kp.contraction) {
-            nasa_pot_lanes<SITES_NL>(R, kp.box, kp.boxi, dr1, &e1, lane, fsh);
+            nasa_pot(R, kp.box, kp.boxi, dr1, &e1, kp.c5z, kp.nasa_f5z);
         } else {
 #pragma unroll
             for (int k = 0; k < 3; k++)
 #pragma unroll
                 for (int c = 0; c < 3; c++) dr1[k][c] = 0.0;
         }
-        double q3[3], dq3[3][3][3];
-        nasa_dms_lanes<SITES_NL>(R, kp.box, kp.boxi, kp.dms1, kp.dms2, kp.dms3, q3, dq3, lane, fsh);
-        if (lane == 0 && valid) {
         av[ACC_UMON] = e1;
+        double q3[3], dq3[3][3][3];
+        nasa_dms(R, kp.box, kp.boxi, kp.dms1, kp.dms2, kp.dms3, q3, dq3);
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             q3[k] *= CHARGECON;
@@ -216,7 +189,6 @@ __global__ void __launch_bounds__(128) k_sites(KP kp) {
                 kp.Efdr[3 * s + c] = 0.0;
             }
         }
-        }  // lane 0
     }
     block_reduce_add<14, 128>(av, kp.acc + (size_t)b * NACC);
 }
@@ -527,16 +499,6 @@ __global__ void k_set_step(int *dstep, int t) {
 }
 
 // ---------------------------------------------------------------------------------------
-// dij of the dipole-dipole term: sum_ab di_a T_abc dj_b for the rank-3 Thole tensor
-// T_abc = 15 t3 R_a R_b R_c - 3 t2 (d_bc R_a + d_ac R_b + d_ab R_c)  (pot_ttm.f90:430-441)
-PIMD_D void dd_force(const double R[3], const double di[3], const double dj[3], double t2, double t3, double dij[3]) {
-    const double rdi = R[0] * di[0] + R[1] * di[1] + R[2] * di[2];
-    const double rdj = R[0] * dj[0] + R[1] * dj[1] + R[2] * dj[2];
-    const double didj = di[0] * dj[0] + di[1] * dj[1] + di[2] * dj[2];
-    const double a = 15.0 * t3 * rdi * rdj - 3.0 * t2 * didj;
-#pragma unroll
-    for (int c = 0; c < 3; c++) dij[c] += a * R[c] - 3.0 * t2 * (rdi * dj[c] + rdj * di[c]);
-}
 
 // pot_ttm.f90:399-542: real-space forces on charges and dipoles (charge-dipole and
 // dipole-dipole), the dipole part of phi, and the intramolecular terms.
@@ -846,7 +808,7 @@ static int pair_blocks(const Engine &E) {
 }
 
 void launch_sites(Engine &E) {
-    dim3 g((E.kp.N * SITES_NL + 127) / 128, E.kp.P);
+    dim3 g((E.kp.N + 127) / 128, E.kp.P);
     DISPATCH_TTM(E, k_sites, g, 128);
 }
 

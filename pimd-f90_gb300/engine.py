@@ -23,6 +23,11 @@ ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "neighbour list overflow", 
           5: "out of device memory", 6: "call-order violation"}
 
 
+# parameter vector of the differentiation form (include/pimd_gb300.h PIMD_TH_*)
+THETA_NAMES = ["polar_M", "a_dd", "a_cc", "vdw_C", "vdw_D", "vdw_E", "dms1", "dms2", "dms3", "gamma_M", "nasa_f5z",
+               "nasa_fbasis", "nasa_fcore", "nasa_frest"]
+
+
 class PimdError(RuntimeError):
     pass
 
@@ -72,6 +77,10 @@ SIGNATURES = {
     "pimd_peak_flops": [ctypes.c_int, ctypes.c_int, _D],
     "pimd_set_graph": [_V, ctypes.c_int],
     "pimd_autotune": [_V, _V, _V],
+    "pimd_get_theta": [_V, _D],
+    "pimd_set_theta": [_V, _D],
+    "pimd_pot_forward": [_V, _D, _D, _D, ctypes.c_int],
+    "pimd_pot_backward": [_V, _D, _D, _D],
     "pimd_get_tuning": [_V, _I, ctypes.c_int],
     "pimd_batch_create": [ctypes.POINTER(_V), ctypes.POINTER(Params), _V, ctypes.c_int, ctypes.POINTER(MDParams)],
     "pimd_batch_destroy": [_V],
@@ -330,6 +339,30 @@ class ForceEngine:
             L.pimd_timers_get(self.h, i, buf, 64, ctypes.byref(ms), ctypes.byref(cnt))
             out[buf.value.decode()] = (ms.value, cnt.value)
         return out
+
+    # ---- differentiation form ----------------------------------------------------------
+    def get_theta(self):
+        th = np.zeros(len(THETA_NAMES))
+        self._check(load().pimd_get_theta(self.h, _p(th)), "get_theta")
+        return th
+
+    def set_theta(self, theta):
+        self._check(load().pimd_set_theta(self.h, _p(_f64(theta))), "set_theta")
+
+    def pot_forward(self, RRt, RRc, t=1):
+        """Energies Upott (P,) of all beads, recording the dipole iterations for pot_backward."""
+        RRt, RRc = _f64(RRt), _f64(RRc)
+        U = np.zeros(self.P)
+        self._check(load().pimd_pot_forward(self.h, _p(RRt), _p(RRc), _p(U), int(t)), "pot_forward")
+        return U
+
+    def pot_backward(self, ebar):
+        """dE/dRRt (P, Natoms, 3) and dE/dtheta for E = sum_k ebar[k] Upot_k of the last forward."""
+        ebar = _f64(ebar)
+        g = np.zeros((self.P, self.natoms, 3))
+        dth = np.zeros(len(THETA_NAMES))
+        self._check(load().pimd_pot_backward(self.h, _p(ebar), _p(g), _p(dth)), "pot_backward")
+        return g, dth
 
     # ---- autotuner ---------------------------------------------------------------------
     def autotune(self, RRt_ptr=None, RRc_ptr=None):

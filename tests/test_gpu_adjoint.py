@@ -1,0 +1,96 @@
+"""GPU tests of the differentiation form (TTM3-F, FP64): the adjoint backward against central
+finite differences of the forward's own energies, in positions and in every parameter theta,
+and against the analytic forces when the dipoles are converged.
+
+The finite differences use a fixed number of dipole iterations (polar_eps = 0), so the energy
+is a smooth function of positions and parameters. Tolerances (normwise, relative to the largest
+gradient component): positions 2e-5 (h = 1e-5 A; the A&S erfc and the NR Q(2/3,x) of the
+reference make the analytic derivative consistent with the energy only to ~1e-7 relative per
+term); parameters 1e-4 relative (h = 1e-4 relative: smaller steps drown in the ~1e-12 rounding
+noise of the energy's FP64 atomic sums)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def case(pkg, nw=32, P=2, K=6, eps=0.0, seed=31):
+    c = pkg.waterbox.make_config("ttm3f_512x32", nw=nw, P=P, seed=seed)
+    L = c["params"]["box"][0]
+    rc = min(9.0, L / 2 - 0.01)
+    p = dict(c["params"], rc=rc, rc1=0.8 * rc, alpha=3.2 / rc, nmax=7, polar_maxiter=K, polar_eps=eps,
+             guess_initdip=0)
+    return c, p
+
+
+def energy(eng, RRt, RRc, ebar):
+    U = eng.pot_forward(RRt, RRc)
+    return float(np.dot(ebar, U))
+
+
+def test_adjoint_position_gradient_matches_fd(pkg, engine_lib):
+    c, p = case(pkg)
+    eng = pkg.ForceEngine(p)
+    ebar = np.array([1.0, 0.5])
+    RRt, RRc = c["RRt"].copy(), c["RRc"]
+    energy(eng, RRt, RRc, ebar)
+    g, _ = eng.pot_backward(ebar)
+    scale = np.abs(g).max()
+    h = 1e-5
+    rng = np.random.default_rng(2)
+    worst = 0.0
+    for _ in range(12):
+        b, a, k = int(rng.integers(2)), int(rng.integers(p["natoms"])), int(rng.integers(3))
+        Rp, Rm = RRt.copy(), RRt.copy()
+        Rp[b, a, k] += h
+        Rm[b, a, k] -= h
+        fd = (energy(eng, Rp, RRc, ebar) - energy(eng, Rm, RRc, ebar)) / (2 * h)
+        worst = max(worst, abs(fd - g[b, a, k]) / scale)
+    assert worst < 2e-5, worst
+
+
+def test_adjoint_theta_gradient_matches_fd(pkg, engine_lib):
+    c, p = case(pkg, P=1)
+    eng = pkg.ForceEngine(p)
+    ebar = np.array([1.0])
+    RRt, RRc = c["RRt"], c["RRc"]
+    energy(eng, RRt, RRc, ebar)
+    _, dth = eng.pot_backward(ebar)
+    th0 = eng.get_theta()
+    names = pkg.engine.THETA_NAMES
+    bad = []
+    for i, name in enumerate(names):
+        h = 1e-4 * max(abs(th0[i]), 1e-3)
+        tp, tm = th0.copy(), th0.copy()
+        tp[i] += h
+        tm[i] -= h
+        eng.set_theta(tp)
+        ep = energy(eng, RRt, RRc, ebar)
+        eng.set_theta(tm)
+        em = energy(eng, RRt, RRc, ebar)
+        eng.set_theta(th0)
+        fd = (ep - em) / (2 * h)
+        if abs(fd - dth[i]) > 1e-4 * max(abs(fd), 1e-6 * abs(ep)):
+            bad.append((name, fd, dth[i]))
+    assert not bad, bad
+
+
+def test_adjoint_equals_analytic_forces_when_converged(pkg, orc, engine_lib):
+    """With converged dipoles (1e-12) and no force-only vdW switch (rc1 = rc) the exact
+    derivative of the energy equals the reference's analytic gradient (Hellmann-Feynman) to the
+    ~1e-7 consistency of its A&S erfc / NR Q(2/3,x)."""
+    c, p = case(pkg, P=2, K=200, eps=1e-12)
+    p["rc1"] = p["rc"]
+    eng = pkg.ForceEngine(p)
+    ebar = np.ones(2)
+    eng.pot_forward(c["RRt"], c["RRc"])
+    g, _ = eng.pot_backward(ebar)
+    ref = orc.full_bead_forces(p, c["RRt"], c["RRc"])["dRRt"]
+    assert np.abs(g - ref).max() < 1e-5 * np.abs(ref).max()
+
+
+def test_backward_requires_forward(pkg, engine_lib):
+    c, p = case(pkg, P=1)
+    eng = pkg.ForceEngine(p)
+    with pytest.raises(pkg.engine.PimdError):
+        eng.pot_backward(np.ones(1))
