@@ -145,10 +145,31 @@ def workload(pkg, name):
     return c, p
 
 
+# DRAM bytes (read + write) of one mixed ewald_std_dd call at the headline workload, from one
+# ncu capture of the three kernels (profiles/ewald_dd_kernels_ttm3f_512x32.md): 5.4 + 6.1 + 6.6 MB
+DD_TRAFFIC_BYTES = 18.1e6
+
+
 def flops_ewald_dd(nk, ndip, P):
     """Algorithmic flops of one ewald_std_dd call for P beads (ewald.f90:56-119): 22 per
     (k-vector, dipole site), the per-unit count of the reference's loop body."""
     return 22.0 * nk * ndip * P
+
+
+def reduce_max(value, device, world):
+    """The job's time is the slowest rank's: max over ranks (no-op for one rank)."""
+    if world <= 1:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(rank):
+    """Each rank is an independent replica: its own Langevin stream."""
+    return 20261203 + rank
 
 
 # ---------------------------------------------------------------------------------------
@@ -233,7 +254,7 @@ def run_gpu_arm(args, pkg, rank, world, local, precision, steps, graph=False):
     omegan = pkg.waterbox.KB_AMU * TEMP * P / pkg.waterbox.HBAR
     eng.nm_init(P, omegan, delt)
     eng.langevin_init(delt / 2, 0, 0.1, P * TEMP)
-    mp = eng.md_params(delt, c["massO"], c["massH"], langevin=1, seed=20261203 + rank)
+    mp = eng.md_params(delt, c["massO"], c["massH"], langevin=1, seed=replica_seed(rank))
     # device-resident MD state
     RRt = torch.from_numpy(c["RRt"]).to(dev)
     PPt = torch.from_numpy(c["PPt"]).to(dev)
@@ -277,11 +298,7 @@ def run_gpu_arm(args, pkg, rank, world, local, precision, steps, graph=False):
     graph_launches = eng.graph_info()[1]
     timers = eng.timers()
     eng.timers_reset(False)
-    dev_ms = sum(step_ms)
-    if world > 1:
-        tt = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        dev_ms = float(tt.item())
+    dev_ms = reduce_max(sum(step_ms), dev, world)
     out = out4.cpu().numpy()
     # e2e: the host-array C-ABI step, copies in and out every step
     hR, hP, hG = RRt.cpu().numpy().copy(), PPt.cpu().numpy().copy(), dRRt.cpu().numpy().copy()
@@ -351,7 +368,17 @@ def main():
         print(json.dumps(line))
         return 0
 
-    pkg.build_lib.build()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", rank=rank, world_size=world)
+        if local == 0:  # one build per node; the other ranks load what it wrote
+            pkg.build_lib.build()
+        dist.barrier()
+    else:
+        pkg.build_lib.build()
     if args.batch:
         run_batch(args, pkg)
         return 0
@@ -359,10 +386,6 @@ def main():
         args.config = "ttm3f_4096x32"
         run_large(args, pkg)
         return 0
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", rank=rank, world_size=world)
     # the FP64 engine is the comparison arm: at most 40 timed steps (~2.5 s)
     steps64 = min(args.steps, 40)
     res64 = run_gpu_arm(args, pkg, rank, world, local, pkg.engine.PIMD_FP64, steps64)
@@ -424,8 +447,9 @@ def main():
         accuracy=ferr,
         e2e=dict(value=res["e2e_steps"] / res["e2e_s"], unit="steps/s", h2d_bytes_per_step=res["h2d"],
                  d2h_bytes_per_step=res["d2h"]),
-        roofline=dict(kernel="ewald_std_dd (k_spass<MU,f32> + k_sreduce + k_field<D,f32>)", bound="fp32-pipe",
-                      achieved=ach, peak=peak32, unit="TFLOP/s", frac=(ach / peak32) if ach else None, traffic=None,
+        roofline=dict(kernel="ewald_std_dd (k_sfac_f<MU> + k_field_f<D> + k_field_finish<D>)", bound="fp32-pipe",
+                      achieved=ach, peak=peak32, unit="TFLOP/s", frac=(ach / peak32) if ach else None,
+                      traffic=DD_TRAFFIC_BYTES, traffic_unit="bytes per call",
                       peak_source="measured in-run: FP32 FMA-throughput kernel (MEASURED_PEAKS.json has no FP32 figure)"),
         cpu_baseline=cpu,
         clocks=res["clocks"],

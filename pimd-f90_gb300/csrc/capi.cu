@@ -323,7 +323,7 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
         (rc = dalloc(E, &kp.tab, P * kp.ntab * S)) || (rc = dalloc(E, &kp.Spart, P * maxgroups * kp.nk * 3)) ||
         (rc = dalloc(E, &kp.Sq, P * kp.nk)) || (rc = dalloc(E, &kp.Sm, P * kp.nk)) || (rc = dalloc(E, &kp.Sdip, P * kp.nk * 3)) ||
         (rc = dalloc(E, &kp.acc, P * NACC)) || (rc = dalloc(E, &kp.err, 1)) || (rc = dalloc(E, &kp.allconv, 1)) ||
-        (rc = dalloc(E, &kp.dstep, 2)) ||
+        (rc = dalloc(E, &kp.dstep, 2)) || (rc = dalloc(E, &kp.fin_counter, 1)) ||
         (rc = dalloc(E, &kp.nbrtmp, P * N)) || (rc = dalloc(E, &E.d_out, 3 * P + 16)) ||
         (rc = dalloc(E, &kp.Fpart, (size_t)E.max_slices * P * S)))
         return rc;
@@ -341,6 +341,7 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
     cudaMemset(kp.err, 0, sizeof(unsigned));
     if ((rc = cuda_check(E, cudaMallocHost((void **)&E.h_allconv, sizeof(int)), "cudaMallocHost"))) return rc;
     cudaMemset(kp.dstep, 0, sizeof(int) * 2);
+    cudaMemset(kp.fin_counter, 0, sizeof(unsigned));
     if (nrep > 1) {
         int *d_brep;
         if ((rc = dalloc(E, &d_brep, P))) return rc;
@@ -429,12 +430,12 @@ static void dipole_iteration(Engine &E, bool mixed) {
     else
         PHASE("dd_real", launch_dd_real(E));
     PHASE("dd_smu", launch_ewald_smu(E));
-    PHASE("dd_update", launch_dd_update(E));
-    PHASE("dd_check", launch_dd_check(E));
+    PHASE("dd_update", launch_dd_update(E));  // includes the convergence test (last block)
 }
 
 // While capturing a CUDA graph: the dipole iterations become a conditional while node whose
-// body is one iteration; k_dd_check sets the condition on the device, so the loop runs with
+// body is one iteration; the convergence test in the field pass's last block sets the condition
+// on the device, so the loop runs with
 // no host round trip and stops at convergence (or polar_maxiter) exactly like the host loop.
 static int capture_dipole_loop(Engine &E, bool mixed) {
     cudaStreamCaptureStatus st;

@@ -108,6 +108,7 @@ struct KP {
                                   // polymers (null: one replica); RRc and posc are per replica
     int nrep;                     // replicas in this context (>= 1)
     int *dstep;                   // [0] MD step t of the force call, [1] dipole iterations done
+    unsigned *fin_counter;        // blocks done in the dipole field pass (fused convergence test)
     unsigned long long cond;      // CUDA-graph conditional handle of the dipole loop (0: host loop)
 };
 
@@ -141,6 +142,7 @@ struct Engine {
     int sf_groups = 0;     // site groups of k_sfac_f (0: sized from the SM count)
     int sf_ntiles = 0, sf_nkg_max = 0;  // run tiles of k_sfac_f and the largest kz-group count
     int sp_cap = 1;        // site groups the structure-factor partial buffer (Spart) holds
+    int mu_pending_groups = 0;  // dipole structure factor left in k_sfac_f partials for k_field_f
     bool ff_regs = true;   // mixed engine: field passes with the kz row in registers (k_field_f)
     bool nbr_block = true; // one-launch neighbour lists per bead for N <= 1024 (k_nbr_block)
     size_t cap = 0;
@@ -233,7 +235,6 @@ void launch_pair_qq(Engine &E);
 void launch_after_qq(Engine &E);
 void launch_dd_real(Engine &E);
 void launch_dd_update(Engine &E);
-void launch_dd_check(Engine &E);
 void launch_set_step(Engine &E, int t);
 void launch_pair_force(Engine &E);
 void launch_finish(Engine &E);

@@ -18,6 +18,7 @@
 // partials and chunk partials are added in FP64.
 #include <algorithm>
 
+#include "dipole_check.cuh"
 #include "engine.h"
 
 namespace pimd {
@@ -603,8 +604,12 @@ PIMD_D void field_sym(const float2 (&ez)[LZM], const float2 *w1, const float2 *w
     }
 }
 
+// With mu_ngroups > 0 (F_D) the dipole structure factor is still in per-site-group partials
+// (k_sfac_f without its reduction): the staging adds them in FP64 in group order -- the k_sreduce
+// arithmetic -- and the blocks with blockIdx.x == 0 also store Sm and the FP32 weights for the
+// later passes, which saves a launch per dipole iteration.
 template <int MODE, int LZM>
-__global__ void __launch_bounds__(FF_NT) k_field_f(KP kp, int s0, int s1) {
+__global__ void __launch_bounds__(FF_NT) k_field_f(KP kp, int s0, int s1, int mu_ngroups) {
     constexpr int LM = LZM / 2;
     const int b = blockIdx.y, slice = blockIdx.z, nslice = gridDim.z;
     if (MODE == F_D && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
@@ -658,9 +663,25 @@ __global__ void __launch_bounds__(FF_NT) k_field_f(KP kp, int s0, int s1) {
             float2 w1 = make_float2(0.f, 0.f), w2 = w1;
             if (j >= ri.z && j < ri.w) {
                 const int k = kp.runs[ch.r0 + rl].kbeg + (j - ri.z);
-                const float2 wq = kp.Wf[((size_t)b * 2) * kp.nk + k], wm = kp.Wf[((size_t)b * 2 + 1) * kp.nk + k];
-                w1 = (MODE == F_Q) ? wq : wm;
-                if (MODE == F_QD) w2 = make_float2(wq.x + wm.x, wq.y + wm.y);
+                if (MODE == F_D && mu_ngroups > 0) {
+                    const float2 *part = reinterpret_cast<const float2 *>(kp.Spart);
+                    double sx = 0.0, sy = 0.0;
+                    for (int g = 0; g < mu_ngroups; g++) {
+                        const float2 v = part[((size_t)b * mu_ngroups + g) * kp.nk + k];
+                        sx += (double)v.x;
+                        sy += (double)v.y;
+                    }
+                    const double w = kp.kinfo[k].w;  // Sm = (-Im, Re) of the sum; W = w conj(Sm)
+                    w1 = make_float2((float)(-w * sy), (float)(-w * sx));
+                    if (blockIdx.x == 0) {
+                        kp.Sm[(size_t)b * kp.nk + k] = make_double2(-sy, sx);
+                        kp.Wf[((size_t)b * 2 + 1) * kp.nk + k] = w1;
+                    }
+                } else {
+                    const float2 wq = kp.Wf[((size_t)b * 2) * kp.nk + k], wm = kp.Wf[((size_t)b * 2 + 1) * kp.nk + k];
+                    w1 = (MODE == F_Q) ? wq : wm;
+                    if (MODE == F_QD) w2 = make_float2(wq.x + wm.x, wq.y + wm.y);
+                }
             }
             Wd[idx] = w1;
             if (MODE == F_QD) Wd[FF_RUNS * LZM + idx] = w2;
@@ -737,11 +758,29 @@ __global__ void __launch_bounds__(FF_NT) k_field_f(KP kp, int s0, int s1) {
 }
 
 // Sum the slices of k_field in order and apply the pass's epilogue, one thread per site.
+// F_D also runs the iteration's convergence test (dipole_check.cuh) in whichever block finishes
+// last (a device counter, reset by that block), so an iteration needs no separate launch.
 template <int MODE, int NT>
 __global__ void __launch_bounds__(NT) k_field_finish(KP kp, int s0, int s1, int nslice) {
     const int b = blockIdx.y;
     const int iter = kp.dstep[1] + 1;  // dipole iteration of this update (F_D)
-    if (MODE == F_D && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
+    const bool done = MODE == F_D && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0;
+    if (done) {  // converged bead: no update, but the block still counts towards the test
+        if (kp.fin_counter) {
+            __shared__ bool last0;
+            if (threadIdx.x == 0) {
+                __threadfence();
+                last0 = atomicAdd(kp.fin_counter, 1u) == gridDim.x * gridDim.y - 1;
+            }
+            __syncthreads();
+            if (last0) {
+                __threadfence();
+                dd_check_block(kp, kp.polar_eps);
+                if (threadIdx.x == 0) *kp.fin_counter = 0u;
+            }
+        }
+        return;
+    }
     const int s = s0 + blockIdx.x * NT + threadIdx.x;
     const bool valid = s < s1;
     const size_t gs = (size_t)b * kp.S + (valid ? s : s0);
@@ -811,6 +850,20 @@ __global__ void __launch_bounds__(NT) k_field_finish(KP kp, int s0, int s1, int 
             double t = 0;
             for (int w = 0; w < NT / 32; w++) t += red[w][threadIdx.x];
             atomicAdd(kp.acc + (size_t)b * NACC + ACC_DSQ + threadIdx.x, t);
+        }
+        if (kp.fin_counter) {
+            __shared__ bool last;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                __threadfence();  // this block's sums are visible before it counts
+                last = atomicAdd(kp.fin_counter, 1u) == gridDim.x * gridDim.y - 1;
+            }
+            __syncthreads();
+            if (last) {
+                __threadfence();
+                dd_check_block(kp, kp.polar_eps);
+                if (threadIdx.x == 0) *kp.fin_counter = 0u;
+            }
         }
     }
 }
@@ -901,6 +954,12 @@ static void run_sfac_f(Engine &E, int s0, int nsites, int skipconv) {
     dim3 g(E.sf_ntiles, ngr, kp.P);
     k_sfac_f<OP><<<g, SF_RT * E.sf_nkg_max, smem, E.stream>>>(E.kp, s0, nsites, tsg, ngr, skipconv);
     ++E.nlaunch;
+    // the dipole iteration's structure factor is reduced by the register-row field pass that
+    // follows (k_field_f<F_D>); every other one here
+    if (OP == OP_MU && E.ff_regs && 2 * kp.lmax + 1 <= 49) {
+        E.mu_pending_groups = ngr;
+        return;
+    }
     dim3 g2((kp.nk + 255) / 256, kp.P);
     k_sreduce<OP, float><<<g2, 256, 0, E.stream>>>(E.kp, ngr, skipconv);
     ++E.nlaunch;
@@ -942,7 +1001,9 @@ static void launch_field_f(Engine &E, int s0, int s1) {
     int ns = (int)((want + (long)sblocks * E.kp.P - 1) / ((long)sblocks * E.kp.P));
     ns = std::max(1, std::min(ns, std::min(E.nchunk, E.max_slices)));
     dim3 g(sblocks, E.kp.P, ns);
-    k_field_f<MODE, LZM><<<g, FF_NT, smem, E.stream>>>(E.kp, s0, s1);
+    const int mu_ngroups = (MODE == F_D) ? E.mu_pending_groups : 0;
+    k_field_f<MODE, LZM><<<g, FF_NT, smem, E.stream>>>(E.kp, s0, s1, mu_ngroups);
+    if (MODE == F_D) E.mu_pending_groups = 0;
     dim3 g2((s1 - s0 + 127) / 128, E.kp.P);
     k_field_finish<MODE, 128><<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns);
     E.nlaunch += 2;

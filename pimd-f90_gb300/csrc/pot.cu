@@ -462,35 +462,6 @@ __global__ void __launch_bounds__(128) k_dd_real(KP kp) {
     }
 }
 
-// pot_ttm.f90:379-385: convergence test per bead after an update. The iteration number comes
-// from the device step word; the kernel advances it, and inside a CUDA graph it sets the
-// conditional of the dipole loop (continue while some bead is not converged).
-__global__ void k_dd_check(KP kp, double eps) {
-    __shared__ int nconv;
-    const int iter = kp.dstep[1] + 1;
-    if (threadIdx.x == 0) nconv = 0;
-    __syncthreads();
-    for (int b = threadIdx.x; b < kp.P; b += blockDim.x) {
-        double *a = kp.acc + (size_t)b * NACC;
-        if (a[ACC_CONV] == 0.0) {
-            const double dd = kp.stath * sqrt(a[ACC_DSQ]);
-            a[ACC_UIND] = -0.5 * a[ACC_MUEFQ];
-            a[ACC_NITER] = (double)iter;
-            a[ACC_DELTADIP] = dd;
-            if (dd < eps || iter >= kp.polar_maxiter) a[ACC_CONV] = (dd < eps) ? 1.0 : 2.0;
-            a[ACC_DSQ] = 0.0;
-            a[ACC_MUEFQ] = 0.0;
-        }
-        if (a[ACC_CONV] != 0.0) atomicAdd(&nconv, 1);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        *kp.allconv = (nconv == kp.P) ? 1 : 0;
-        kp.dstep[1] = iter;
-        if (kp.cond) cudaGraphSetConditional(kp.cond, nconv == kp.P ? 0u : 1u);
-    }
-}
-
 __global__ void k_set_step(int *dstep, int t) {
     if (threadIdx.x == 0) {
         dstep[0] = t;
@@ -832,9 +803,6 @@ void launch_dd_real(Engine &E) {
     DISPATCH_TTM(E, k_dd_real, g, 128);
 }
 
-void launch_dd_check(Engine &E) {
-    k_dd_check<<<1, 256, 0, E.stream>>>(E.kp, E.kp.polar_eps); ++E.nlaunch;
-}
 
 void launch_pair_force(Engine &E) {
     dim3 g(pair_blocks(E), E.kp.P);
