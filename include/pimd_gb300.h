@@ -216,7 +216,8 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
  * No counterpart in the reference. */
 int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc);
 /* The chosen shapes: [tiled structure factors, site groups (0 = sized from the SM count),
- * register-row field kernels, max k-slices, one-launch neighbour lists]; n >= 5. */
+ * register-row field kernels, max k-slices, one-launch neighbour lists] and, when n >= 6,
+ * [wave-quantised split counts]; n >= 5. */
 int pimd_get_tuning(pimd_ctx *ctx, int *knobs, int n);
 
 /* ---------------------------------------------------------------------------------------

@@ -335,6 +335,23 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
             (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd * 6)) || (rc = dalloc(E, &kp.Wf, P * 2 * (size_t)kp.nk)) || (rc = dalloc(E, &kp.dipf, P * S)))
             return rc;
     }
+    // cell lists for boxes beyond the one-block neighbour kernel (cells of width >= Rc + 1e-3 A)
+    kp.cl_ncell = 0;
+    if (N > 1024) {
+        bool ok = true;
+        for (int d = 0; d < 3; d++) {
+            kp.cl_n[d] = (int)std::floor(p->box[d] / (p->rc + 1e-3));
+            ok = ok && kp.cl_n[d] >= 4;
+        }
+        if (ok) {
+            kp.cl_ncell = kp.cl_n[0] * kp.cl_n[1] * kp.cl_n[2];
+            if ((rc = dalloc(E, &kp.cl_mol, P * N)) || (rc = dalloc(E, &kp.cl_posf, P * N)) ||
+                (rc = dalloc(E, &kp.cl_cnt, P * (size_t)kp.cl_ncell)) ||
+                (rc = dalloc(E, &kp.cl_start, P * (size_t)(kp.cl_ncell + 1))) || (rc = dalloc(E, &kp.cl_list, P * N)) ||
+                (rc = dalloc(E, &kp.cl_row, P * N * 256)) || (rc = dalloc(E, &kp.cl_rowlen, P * N)))
+                return rc;
+        }
+    }
     cudaMemset(kp.txdip, 0, sizeof(double) * P * 4 * S * 3);
     cudaMemset(kp.Sm, 0, sizeof(double2) * P * kp.nk);
     if (kp.Wf) cudaMemset(kp.Wf, 0, sizeof(float2) * P * 2 * kp.nk);
@@ -863,7 +880,8 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         int *v;
         std::vector<int> cand;
     };
-    int sf_tiled = E.sf_tiled, ff_regs = E.ff_regs, nbr_block = E.nbr_block;
+    int sf_tiled = E.sf_tiled, ff_regs = E.ff_regs, nbr_block = E.nbr_block, wave = E.wave_shapes;
+    int nbr_cells = E.nbr_cells;
     std::vector<Knob> knobs;
     const bool mixed = E.precision == PIMD_MIXED && E.kp.model < 4;
     if (mixed) {
@@ -871,12 +889,16 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         knobs.push_back({&E.sf_groups, {0, 4, 8, 16, 32}});
         knobs.push_back({&ff_regs, {1, 0}});
     }
+    knobs.push_back({&wave, {1, 0}});
     knobs.push_back({&E.max_slices, {16, 8, 4, 2}});
     knobs.push_back({&nbr_block, {1, 0}});
+    if (E.kp.cl_ncell > 0) knobs.push_back({&nbr_cells, {1, 0}});
     auto apply = [&]() {
         E.sf_tiled = sf_tiled != 0;
         E.ff_regs = ff_regs != 0;
         E.nbr_block = nbr_block != 0;
+        E.wave_shapes = wave != 0;
+        E.nbr_cells = nbr_cells != 0;
     };
     int rc = PIMD_OK;
     float best;
@@ -915,6 +937,7 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     k[2] = E.ff_regs;
     k[3] = E.max_slices;
     k[4] = E.nbr_block;
+    if (n >= 6) k[5] = E.wave_shapes;
     return PIMD_OK;
 }
 

@@ -101,6 +101,13 @@ struct KP {
     float *Tf;             // [P][fcap][ndd][6] FP32 dipole tensors of the full list
     int fcap;
     double4_32a *Fpart;    // [slices][P][S] per-k-slice partial fields of the Ewald field passes
+    // cell lists of large boxes (N > 1024, >= 4 cells of width >= Rc per edge)
+    int cl_n[3], cl_ncell;     // cells per edge, cells (0: no cell lists)
+    int *cl_mol;               // [P][N] cell of each molecule
+    float4 *cl_posf;           // [P][N] FP32 O sites wrapped into the box
+    int *cl_cnt, *cl_start;    // [P][ncell] counts, [P][ncell + 1] starts
+    int *cl_list;              // [P][N] molecules ordered by cell
+    int *cl_row, *cl_rowlen;   // [P][N][256] sorted full rows, [P][N] their lengths
     double *acc;
     unsigned *err;
     int *allconv;
@@ -142,9 +149,10 @@ struct Engine {
     int sf_groups = 0;     // site groups of k_sfac_f (0: sized from the SM count)
     int sf_ntiles = 0, sf_nkg_max = 0;  // run tiles of k_sfac_f and the largest kz-group count
     int sp_cap = 1;        // site groups the structure-factor partial buffer (Spart) holds
-    int mu_pending_groups = 0;  // dipole structure factor left in k_sfac_f partials for k_field_f
     bool ff_regs = true;   // mixed engine: field passes with the kz row in registers (k_field_f)
     bool nbr_block = true; // one-launch neighbour lists per bead for N <= 1024 (k_nbr_block)
+    bool nbr_cells = true; // cell lists for N > 1024 when the box holds >= 4 cells per edge
+    bool wave_shapes = true;  // k-slices / site groups chosen by wave quantisation (occupancy API)
     size_t cap = 0;
     std::vector<KRun> h_runs;
     std::vector<KChunk> h_chunks;

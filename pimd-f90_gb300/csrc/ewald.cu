@@ -604,12 +604,8 @@ PIMD_D void field_sym(const float2 (&ez)[LZM], const float2 *w1, const float2 *w
     }
 }
 
-// With mu_ngroups > 0 (F_D) the dipole structure factor is still in per-site-group partials
-// (k_sfac_f without its reduction): the staging adds them in FP64 in group order -- the k_sreduce
-// arithmetic -- and the blocks with blockIdx.x == 0 also store Sm and the FP32 weights for the
-// later passes, which saves a launch per dipole iteration.
 template <int MODE, int LZM>
-__global__ void __launch_bounds__(FF_NT) k_field_f(KP kp, int s0, int s1, int mu_ngroups) {
+__global__ void __launch_bounds__(FF_NT) k_field_f(KP kp, int s0, int s1) {
     constexpr int LM = LZM / 2;
     const int b = blockIdx.y, slice = blockIdx.z, nslice = gridDim.z;
     if (MODE == F_D && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
@@ -663,25 +659,9 @@ __global__ void __launch_bounds__(FF_NT) k_field_f(KP kp, int s0, int s1, int mu
             float2 w1 = make_float2(0.f, 0.f), w2 = w1;
             if (j >= ri.z && j < ri.w) {
                 const int k = kp.runs[ch.r0 + rl].kbeg + (j - ri.z);
-                if (MODE == F_D && mu_ngroups > 0) {
-                    const float2 *part = reinterpret_cast<const float2 *>(kp.Spart);
-                    double sx = 0.0, sy = 0.0;
-                    for (int g = 0; g < mu_ngroups; g++) {
-                        const float2 v = part[((size_t)b * mu_ngroups + g) * kp.nk + k];
-                        sx += (double)v.x;
-                        sy += (double)v.y;
-                    }
-                    const double w = kp.kinfo[k].w;  // Sm = (-Im, Re) of the sum; W = w conj(Sm)
-                    w1 = make_float2((float)(-w * sy), (float)(-w * sx));
-                    if (blockIdx.x == 0) {
-                        kp.Sm[(size_t)b * kp.nk + k] = make_double2(-sy, sx);
-                        kp.Wf[((size_t)b * 2 + 1) * kp.nk + k] = w1;
-                    }
-                } else {
-                    const float2 wq = kp.Wf[((size_t)b * 2) * kp.nk + k], wm = kp.Wf[((size_t)b * 2 + 1) * kp.nk + k];
-                    w1 = (MODE == F_Q) ? wq : wm;
-                    if (MODE == F_QD) w2 = make_float2(wq.x + wm.x, wq.y + wm.y);
-                }
+                const float2 wq = kp.Wf[((size_t)b * 2) * kp.nk + k], wm = kp.Wf[((size_t)b * 2 + 1) * kp.nk + k];
+                w1 = (MODE == F_Q) ? wq : wm;
+                if (MODE == F_QD) w2 = make_float2(wq.x + wm.x, wq.y + wm.y);
             }
             Wd[idx] = w1;
             if (MODE == F_QD) Wd[FF_RUNS * LZM + idx] = w2;
@@ -945,21 +925,22 @@ static void run_sfac_f(Engine &E, int s0, int nsites, int skipconv) {
     constexpr int M = (OP == OP_Q) ? 1 : (OP == OP_MU) ? 2 : 3;
     const int ntile = (nsites + SF_TS - 1) / SF_TS;
     const long per = (long)E.sf_ntiles * kp.P;
-    int ng = E.sf_groups > 0 ? E.sf_groups : (int)((152L * 8 + per - 1) / per);
-    ng = std::max(1, std::min(std::min(ng, ntile), E.sp_cap));
-    const int tsg = ((ntile + ng - 1) / ng) * SF_TS;
-    const int ngr = (nsites + tsg - 1) / tsg;
     const int KZP = E.sf_nkg_max * SF_TK;
     const size_t smem = sizeof(float2) * ((size_t)SF_TS * SF_RT * M + (size_t)SF_TS * KZP) + sizeof(float4) * SF_TS;
+    const int gmax = std::max(1, std::min(ntile, E.sp_cap));
+    int ng;
+    if (E.sf_groups > 0)
+        ng = E.sf_groups;
+    else if (E.wave_shapes)
+        ng = wave_split(E, k_sfac_f<OP>, SF_RT * E.sf_nkg_max, smem, per, gmax);
+    else
+        ng = (int)((152L * 8 + per - 1) / per);
+    ng = std::max(1, std::min(ng, gmax));
+    const int tsg = ((ntile + ng - 1) / ng) * SF_TS;
+    const int ngr = (nsites + tsg - 1) / tsg;
     dim3 g(E.sf_ntiles, ngr, kp.P);
     k_sfac_f<OP><<<g, SF_RT * E.sf_nkg_max, smem, E.stream>>>(E.kp, s0, nsites, tsg, ngr, skipconv);
     ++E.nlaunch;
-    // the dipole iteration's structure factor is reduced by the register-row field pass that
-    // follows (k_field_f<F_D>); every other one here
-    if (OP == OP_MU && E.ff_regs && 2 * kp.lmax + 1 <= 49) {
-        E.mu_pending_groups = ngr;
-        return;
-    }
     dim3 g2((kp.nk + 255) / 256, kp.P);
     k_sreduce<OP, float><<<g2, 256, 0, E.stream>>>(E.kp, ngr, skipconv);
     ++E.nlaunch;
@@ -975,6 +956,39 @@ static void run_spass(Engine &E, int s0, int nsites, int skipconv) {
     } else {
         run_spass_t<OP, double>(E, s0, nsites, skipconv);
     }
+}
+
+// Launch shapes by wave quantisation. A grid of B blocks with R resident per SM runs in
+// ceil(B / (SMs R)) waves; when the split count c divides the work (each block does ~1/c of it),
+// the time goes as waves(c) / c. Pick the c in [1, cmax] that minimises it (ties: smallest c,
+// fewest partials to add afterwards). R comes from the occupancy calculator for the kernel.
+static int sm_count(const Engine &E) {
+    static int cached[64] = {0};
+    const int d = E.device & 63;
+    if (!cached[d]) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, E.device);
+        cached[d] = n > 0 ? n : 152;
+    }
+    return cached[d];
+}
+
+template <typename K>
+static int wave_split(const Engine &E, K kernel, int threads, size_t smem, long base_blocks, int cmax) {
+    int R = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&R, kernel, threads, smem);
+    const long slots = (long)sm_count(E) * std::max(R, 1);
+    int best = 1;
+    double best_t = 1e300;
+    for (int c = 1; c <= std::max(1, cmax); c++) {
+        const long waves = (base_blocks * c + slots - 1) / slots;
+        const double t = (double)waves / c;
+        if (t < best_t - 1e-12) {
+            best_t = t;
+            best = c;
+        }
+    }
+    return best;
 }
 
 template <int MODE, int NT, typename R>
@@ -997,13 +1011,12 @@ template <int MODE, int LZM>
 static void launch_field_f(Engine &E, int s0, int s1) {
     const size_t smem = sizeof(float2) * ((MODE == F_QD) ? 2 : 1) * FF_RUNS * LZM;
     const int sblocks = (s1 - s0 + FF_NT - 1) / FF_NT;
-    const long want = 8L * 152;
-    int ns = (int)((want + (long)sblocks * E.kp.P - 1) / ((long)sblocks * E.kp.P));
-    ns = std::max(1, std::min(ns, std::min(E.nchunk, E.max_slices)));
+    const int cmax = std::min(E.nchunk, E.max_slices);
+    const int ns = E.wave_shapes ? wave_split(E, k_field_f<MODE, LZM>, FF_NT, smem, (long)sblocks * E.kp.P, cmax)
+                                 : std::max(1, std::min((int)((8L * 152 + (long)sblocks * E.kp.P - 1) /
+                                                              ((long)sblocks * E.kp.P)), cmax));
     dim3 g(sblocks, E.kp.P, ns);
-    const int mu_ngroups = (MODE == F_D) ? E.mu_pending_groups : 0;
-    k_field_f<MODE, LZM><<<g, FF_NT, smem, E.stream>>>(E.kp, s0, s1, mu_ngroups);
-    if (MODE == F_D) E.mu_pending_groups = 0;
+    k_field_f<MODE, LZM><<<g, FF_NT, smem, E.stream>>>(E.kp, s0, s1);
     dim3 g2((s1 - s0 + 127) / 128, E.kp.P);
     k_field_finish<MODE, 128><<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns);
     E.nlaunch += 2;

@@ -216,6 +216,164 @@ __global__ void __launch_bounds__(NB_MAXN) k_nbr_block(KP kp) {
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// Boxes of more than NB_MAXN molecules with at least 4 cells of width >= Rc per edge: cell lists.
+// The O sites of a bead are binned into cells; a warp owns row i, tests the members of the 27
+// surrounding cells (FP32 prefilter, FP64 near the cutoff: the same decisions as above), collects
+// the hits of the full row in shared memory and sorts them by j (bitonic), so the half and full
+// lists written afterwards are the reference's lists bit for bit.
+constexpr int CL_ROWCAP = 256;  // neighbours of one molecule in the full list (about 100 at water density and 9 A)
+
+__global__ void __launch_bounds__(128) k_cell_bin(KP kp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (i >= kp.N) return;
+    const double4_32a o = kp.pos[(size_t)b * kp.S + i];
+    const double x[3] = {o.x, o.y, o.z};
+    int c[3];
+    float w[3];
+    for (int d = 0; d < 3; d++) {
+        const double xw = x[d] - kp.box[d] * round(x[d] * kp.boxi[d]);  // in [-L/2, L/2]
+        w[d] = (float)xw;
+        int ci = (int)floor((xw * kp.boxi[d] + 0.5) * kp.cl_n[d]);
+        c[d] = min(max(ci, 0), kp.cl_n[d] - 1);
+    }
+    const int cell = (c[2] * kp.cl_n[1] + c[1]) * kp.cl_n[0] + c[0];
+    kp.cl_mol[(size_t)b * kp.N + i] = cell;
+    kp.cl_posf[(size_t)b * kp.N + i] = make_float4(w[0], w[1], w[2], 0.f);
+    atomicAdd(kp.cl_cnt + (size_t)b * kp.cl_ncell + cell, 1);
+}
+
+// exclusive scan of the cell counts into cell starts, one block per bead; resets the counts
+__global__ void __launch_bounds__(1024) k_cell_scan(KP kp) {
+    __shared__ int part[1024];
+    const int b = blockIdx.x, nt = blockDim.x, nc = kp.cl_ncell;
+    const int per = (nc + nt - 1) / nt, c0 = threadIdx.x * per, c1 = min(nc, c0 + per);
+    int *cnt = kp.cl_cnt + (size_t)b * nc, *start = kp.cl_start + (size_t)b * (nc + 1);
+    int s = 0;
+    for (int c = c0; c < c1; c++) s += cnt[c];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int d = 1; d < nt; d <<= 1) {
+        const int v = (threadIdx.x >= d) ? part[threadIdx.x - d] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int base = part[threadIdx.x] - s;
+    for (int c = c0; c < c1; c++) {
+        start[c] = base;
+        base += cnt[c];
+        cnt[c] = 0;
+    }
+    if (threadIdx.x == nt - 1) start[nc] = part[nt - 1];
+}
+
+__global__ void __launch_bounds__(128) k_cell_fill(KP kp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (i >= kp.N) return;
+    const int cell = kp.cl_mol[(size_t)b * kp.N + i];
+    const int slot = atomicAdd(kp.cl_cnt + (size_t)b * kp.cl_ncell + cell, 1);
+    kp.cl_list[(size_t)b * kp.N + kp.cl_start[(size_t)b * (kp.cl_ncell + 1) + cell] + slot] = i;
+}
+
+// warp per (row, bead): sorted full row into cl_row, counts of the half / full rows
+template <bool FULL>
+__global__ void __launch_bounds__(128) k_cell_rows(KP kp) {
+    __shared__ int buf[4][CL_ROWCAP];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, b = blockIdx.y;
+    if (i >= kp.N) return;
+    int *row = buf[wib];
+    const float4 *pf = kp.cl_posf + (size_t)b * kp.N;
+    const double4_32a *O = kp.pos + (size_t)b * kp.S;
+    const float4 fi = pf[i];
+    const double4_32a di = O[i];
+    const float rc2f = (float)kp.rc2;
+    const float3 Lf = make_float3((float)kp.box[0], (float)kp.box[1], (float)kp.box[2]);
+    const float3 Lif = make_float3((float)kp.boxi[0], (float)kp.boxi[1], (float)kp.boxi[2]);
+    const int ci = kp.cl_mol[(size_t)b * kp.N + i];
+    const int c0 = ci % kp.cl_n[0], c1 = (ci / kp.cl_n[0]) % kp.cl_n[1], c2 = ci / (kp.cl_n[0] * kp.cl_n[1]);
+    const int *start = kp.cl_start + (size_t)b * (kp.cl_ncell + 1);
+    const int *list = kp.cl_list + (size_t)b * kp.N;
+    int n = 0;
+    for (int d = 0; d < 27; d++) {
+        const int x = (c0 + d % 3 - 1 + kp.cl_n[0]) % kp.cl_n[0];
+        const int y = (c1 + (d / 3) % 3 - 1 + kp.cl_n[1]) % kp.cl_n[1];
+        const int z = (c2 + d / 9 - 1 + kp.cl_n[2]) % kp.cl_n[2];
+        const int cell = (z * kp.cl_n[1] + y) * kp.cl_n[0] + x;
+        const int m0 = start[cell], m1 = start[cell + 1];
+        for (int m = m0; m < m1; m += 32) {
+            const int mm = m + lane;
+            const int j = mm < m1 ? list[mm] : -1;
+            const bool hit = j >= 0 && j != i && oo_test_sm(fi, pf[max(j, 0)], di, O[max(j, 0)], kp, rc2f, Lf, Lif);
+            const unsigned msk = __ballot_sync(0xffffffffu, hit);
+            if (hit) {
+                const int slot = n + __popc(msk & ((1u << lane) - 1u));
+                if (slot < CL_ROWCAP) row[slot] = j;
+            }
+            n += __popc(msk);
+        }
+    }
+    if (n > CL_ROWCAP) {
+        if (lane == 0) atomicOr(kp.err, 1u);
+        n = CL_ROWCAP;
+    }
+    for (int s = n + lane; s < CL_ROWCAP; s += 32) row[s] = 0x7fffffff;
+    __syncwarp();
+    // bitonic sort of the row (ascending j)
+    for (int k = 2; k <= CL_ROWCAP; k <<= 1)
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int t = lane; t < CL_ROWCAP; t += 32) {
+                const int p = t ^ jj;
+                if (p > t) {
+                    const int a = row[t], c = row[p];
+                    const bool up = (t & k) == 0;
+                    if ((a > c) == up) {
+                        row[t] = c;
+                        row[p] = a;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    int nh = 0;
+    int *out = kp.cl_row + ((size_t)b * kp.N + i) * CL_ROWCAP;
+    for (int s = lane; s < n; s += 32) {
+        out[s] = row[s];
+        nh += row[s] > i;
+    }
+    for (int o = 16; o > 0; o >>= 1) nh += __shfl_xor_sync(0xffffffffu, nh, o);
+    if (lane == 0) {
+        kp.cl_rowlen[(size_t)b * kp.N + i] = n;
+        kp.nbrtmp[(size_t)b * kp.N + i] = nh;  // scanned into half-list offsets
+        if (FULL) kp.foff[(size_t)b * kp.N + i] = n;
+    }
+}
+
+// copy the sorted rows into the compact half list (and full list) at the scanned offsets
+template <bool FULL>
+__global__ void __launch_bounds__(128) k_cell_copy(KP kp) {
+    const int lane = threadIdx.x & 31;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, b = blockIdx.y;
+    if (i >= kp.N) return;
+    const int *row = kp.cl_row + ((size_t)b * kp.N + i) * CL_ROWCAP;
+    const int oh = kp.nbrtmp[(size_t)b * kp.N + i];
+    const int of = FULL ? kp.foff[(size_t)b * kp.N + i] : 0;
+    const int nf = FULL ? ((i + 1 < kp.N) ? kp.foff[(size_t)b * kp.N + i + 1] : kp.fntot[b]) - of : 0;
+    const int nh_end = (i + 1 < kp.N) ? kp.nbrtmp[(size_t)b * kp.N + i + 1] : kp.npair[b];
+    const int nh = nh_end - oh;
+    // the row's first entry with j > i: the full row minus the half row
+    const int n = kp.cl_rowlen[(size_t)b * kp.N + i];
+    int2 *ph = kp.pairs + (size_t)b * kp.cap;
+    int2 *pfl = reinterpret_cast<int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
+    for (int s = lane; s < n; s += 32) {
+        const int j = row[s];
+        const int sh = s - (n - nh);  // the j > i entries are the last nh of the sorted row
+        if (sh >= 0 && oh + sh < kp.cap) ph[oh + sh] = make_int2(i, j);
+        if (FULL && s < nf && of + s < kp.fcap) pfl[of + s] = make_int2(i, j);
+    }
+}
+
 template <bool FULL, bool PRE>
 static void build_list(Engine &E, int *cnt, int *tot, int cap) {
     KP &kp = E.kp;
@@ -229,6 +387,26 @@ static void build_list(Engine &E, int *cnt, int *tot, int cap) {
 // half list for every engine; the mixed engine adds the full list (row offsets in foff)
 void launch_neighbors(Engine &E) {
     KP &kp = E.kp;
+    if (kp.N > NB_MAXN && kp.cl_ncell > 0 && E.nbr_cells) {
+        const bool full = E.precision == PIMD_PREC_MIXED;
+        cudaMemsetAsync(kp.cl_cnt, 0, sizeof(int) * (size_t)kp.P * kp.cl_ncell, E.stream);
+        dim3 g1((kp.N + 127) / 128, kp.P), gw((kp.N * 32 + 127) / 128, kp.P);
+        k_cell_bin<<<g1, 128, 0, E.stream>>>(kp);
+        k_cell_scan<<<kp.P, 1024, 0, E.stream>>>(kp);
+        k_cell_fill<<<g1, 128, 0, E.stream>>>(kp);
+        if (full)
+            k_cell_rows<true><<<gw, 128, 0, E.stream>>>(kp);
+        else
+            k_cell_rows<false><<<gw, 128, 0, E.stream>>>(kp);
+        k_scan_counts<<<kp.P, 1024, 0, E.stream>>>(kp.nbrtmp, kp.npair, kp.N, kp.cap, kp.err);
+        if (full) k_scan_counts<<<kp.P, 1024, 0, E.stream>>>(kp.foff, kp.fntot, kp.N, kp.fcap, kp.err);
+        if (full)
+            k_cell_copy<true><<<gw, 128, 0, E.stream>>>(kp);
+        else
+            k_cell_copy<false><<<gw, 128, 0, E.stream>>>(kp);
+        E.nlaunch += full ? 7 : 6;
+        return;
+    }
     if (kp.N <= NB_MAXN && E.nbr_block) {
         const int nt = ((kp.N + 31) / 32) * 32 < 256 ? 256 : ((kp.N + 31) / 32) * 32;
         const size_t smem = (sizeof(double4_32a) + sizeof(float4) + 2 * sizeof(int)) * (size_t)kp.N;

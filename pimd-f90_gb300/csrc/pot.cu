@@ -41,8 +41,12 @@ PIMD_D double3 ld3(const double *p) { return make_double3(p[0], p[1], p[2]); }
 // ---------------------------------------------------------------------------------------
 // pot_ttm.f90:56-151 and 232-261: site layout, M sites, NASA PES + DMS charges, monomer
 // virials, self energy and intramolecular Ewald exclusions. One thread per (molecule, bead).
+// 32-thread blocks: one molecule per thread is FP64-latency-bound at this occupancy (about 3
+// warps per SM at 512 x 32), so the warps are spread over every SM rather than packed 4 per block.
+constexpr int SITES_NT = 32;
+
 template <int MODEL>
-__global__ void __launch_bounds__(128) k_sites(KP kp) {
+__global__ void __launch_bounds__(SITES_NT) k_sites(KP kp) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     const int b = blockIdx.y;
     const int N = kp.N, S = kp.S;
@@ -190,7 +194,7 @@ __global__ void __launch_bounds__(128) k_sites(KP kp) {
             }
         }
     }
-    block_reduce_add<14, 128>(av, kp.acc + (size_t)b * NACC);
+    block_reduce_add<14, SITES_NT>(av, kp.acc + (size_t)b * NACC);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -779,8 +783,8 @@ static int pair_blocks(const Engine &E) {
 }
 
 void launch_sites(Engine &E) {
-    dim3 g((E.kp.N + 127) / 128, E.kp.P);
-    DISPATCH_TTM(E, k_sites, g, 128);
+    dim3 g((E.kp.N + SITES_NT - 1) / SITES_NT, E.kp.P);
+    DISPATCH_TTM(E, k_sites, g, SITES_NT);
 }
 
 void launch_pair_qq(Engine &E) {

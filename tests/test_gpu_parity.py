@@ -172,3 +172,18 @@ def test_mixed_headline_and_convergence(pkg, orc, engine_lib):
         e = eng.energies(k)
         assert e["niter"] < p["polar_maxiter"] and e["deltadip"] < p["polar_eps"]
         assert abs(e["niter"] - r["niter"]) <= 2
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_cell_list_neighbours_large_box(pkg, orc, engine_lib, precision):
+    """1800 molecules (L = 37.8 A, 4 cells of >= 9 A per edge): the cell-list build gives the
+    reference's list bit for bit, and the forces follow (FP64 1e-10; mixed 1e-4 relative)."""
+    c = pkg.waterbox.make_config("ttm3f_512x32", nw=1800, P=1)
+    p = dict(c["params"], rc=9.0, rc1=7.2, alpha=0.39, nmax=6, polar_maxiter=8, polar_eps=0.0)
+    eng = pkg.ForceEngine(p, precision=precision)
+    got = eng.full_bead_forces(c["RRt"], c["RRc"])
+    o = orc.Oracle(p)
+    assert np.array_equal(eng.neighbors(0), o.neighbors(c["RRt"][0]))
+    r = o.pot_ttm(c["RRt"][0], c["RRc"])
+    tol = RTOL if precision == 0 else 1e-4
+    assert rel(got["dRRt"][0], r["dRR"]) < tol
