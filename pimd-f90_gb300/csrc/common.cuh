@@ -236,4 +236,27 @@ PIMD_D void block_reduce_add(double (&v)[NV], double *dst) {
     __syncthreads();
 }
 
+// The same for per-thread FP32 partials (the mixed engine's pair kernels, about one pair per
+// thread): warp sums in FP32, then the warps' sums added in FP64 -- no FP64 arithmetic per lane.
+template <int NV, int NT>
+PIMD_D void block_reduce_add_f(float (&v)[NV], double *dst) {
+    __shared__ double red[NT / 32][NV];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        float x = v[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) red[warp][i] = (double)x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double s = 0;
+#pragma unroll
+        for (int w = 0; w < NT / 32; w++) s += red[w][threadIdx.x];
+        if (s != 0.0) atomicAdd(dst + threadIdx.x, s);
+    }
+    __syncthreads();
+}
+
 }  // namespace pimd

@@ -67,9 +67,9 @@ __global__ void __launch_bounds__(128) k_pair_qq_m(KP kp) {
     const float Li[3] = {(float)kp.boxi[0], (float)kp.boxi[1], (float)kp.boxi[2]};
     const float vA = kp.vdwA, vB = kp.vdwB, vC = kp.vdwC, vD = kp.vdwD, vE = kp.vdwE;
     const float sA = kp.shiftA, sB = kp.shiftB, r1 = kp.rc1;
-    double av[14];
+    float av[14];  // per-thread FP32 partials, reduced in FP64 per warp (block_reduce_add_f)
 #pragma unroll
-    for (int i = 0; i < 14; i++) av[i] = 0.0;
+    for (int i = 0; i < 14; i++) av[i] = 0.f;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
         const int2 ij = kp.pairs[(size_t)b * kp.cap + p];
         const int i = ij.x, j = ij.y;
@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(128) k_pair_qq_m(KP kp) {
             const float dRij = sqrtf(dRsq);
             const float R2i = 1.f / dRsq, R4i = R2i * R2i, R6i = R4i * R2i, R8i = R6i * R2i;
             const float tv = vD * __expf(-vE * dRij);
-            av[ACC_UVDW] += (double)(R6i * ((vA * R6i + vB * R4i) + vC) + tv);
+            av[ACC_UVDW] += R6i * ((vA * R6i + vB * R4i) + vC) + tv;
             const float xr = dRij - r1;
             const float sc = R8i * 6.f * vC + tv * vE / dRij + sA * (xr * xr) + sB * (xr * xr * xr);
             float d[3];
@@ -107,11 +107,11 @@ __global__ void __launch_bounds__(128) k_pair_qq_m(KP kp) {
                 atomicAdd(dRi + c, (double)d[c]);
                 atomicAdd(dRj + c, -(double)d[c]);
             }
-            av[ACC_VIRIALC] += (double)(Rc[0] * d[0] + Rc[1] * d[1] + Rc[2] * d[2]);
+            av[ACC_VIRIALC] += Rc[0] * d[0] + Rc[1] * d[1] + Rc[2] * d[2];
 #pragma unroll
             for (int col = 0; col < 3; col++)
 #pragma unroll
-                for (int c = 0; c < 3; c++) av[ACC_VIRT + c + 3 * col] += (double)(d[col] * Rf[c]);
+                for (int c = 0; c < 3; c++) av[ACC_VIRT + c + 3 * col] += d[col] * Rf[c];
         }
         float Fi[5][4], Fj[5][4];
 #pragma unroll
@@ -153,9 +153,9 @@ __global__ void __launch_bounds__(128) k_pair_qq_m(KP kp) {
                 }
             }
         }
-        av[ACC_VIRIALC] += (double)vc;
+        av[ACC_VIRIALC] += vc;
 #pragma unroll
-        for (int q = 0; q < 9; q++) av[ACC_VIRT + q] += (double)vt[q];
+        for (int q = 0; q < 9; q++) av[ACC_VIRT + q] += vt[q];
         if (err) atomicOr(kp.err, err);
         double4_32a *Fb = kp.F + (size_t)b * kp.S;
 #pragma unroll
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(128) k_pair_qq_m(KP kp) {
             }
         }
     }
-    block_reduce_add<14, 128>(av, kp.acc + (size_t)b * NACC);
+    block_reduce_add_f<14, 128>(av, kp.acc + (size_t)b * NACC);
 }
 
 // FP32 Thole-smeared dipole tensors for every entry (i, j) of the full neighbour list,
@@ -311,9 +311,9 @@ __global__ void __launch_bounds__(128) k_pair_force_m(KP kp) {
     const bool same_a = kp.same_acd != 0;
     const float L[3] = {(float)kp.box[0], (float)kp.box[1], (float)kp.box[2]};
     const float Li[3] = {(float)kp.boxi[0], (float)kp.boxi[1], (float)kp.boxi[2]};
-    double av[14];
+    float av[14];  // per-thread FP32 partials, reduced in FP64 per warp (block_reduce_add_f)
 #pragma unroll
-    for (int i = 0; i < 14; i++) av[i] = 0.0;
+    for (int i = 0; i < 14; i++) av[i] = 0.f;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
         const int2 ij = kp.pairs[(size_t)b * kp.cap + p];
         const int i = ij.x, j = ij.y;
@@ -392,9 +392,9 @@ __global__ void __launch_bounds__(128) k_pair_force_m(KP kp) {
                     for (int c = 0; c < 3; c++) vt[c + 3 * col] += dij[c] * Rs[col];
             }
         }
-        av[ACC_VIRIALC] += (double)vc;
+        av[ACC_VIRIALC] += vc;
 #pragma unroll
-        for (int q = 0; q < 9; q++) av[ACC_VIRT + q] += (double)vt[q];
+        for (int q = 0; q < 9; q++) av[ACC_VIRT + q] += vt[q];
 #pragma unroll
         for (int k = 1; k <= 4; k++) {
             if (MODEL != 2 && k == 1) continue;
@@ -468,9 +468,9 @@ __global__ void __launch_bounds__(128) k_pair_force_m(KP kp) {
 #pragma unroll
                     for (int c = 0; c < 3; c++) vt[c + 3 * col] += dij[c] * Rs[col];
             }
-        av[ACC_VIRIALC] += (double)vc;
+        av[ACC_VIRIALC] += vc;
 #pragma unroll
-        for (int q = 0; q < 9; q++) av[ACC_VIRT + q] += (double)vt[q];
+        for (int q = 0; q < 9; q++) av[ACC_VIRT + q] += vt[q];
 #pragma unroll
         for (int k = 1; k <= 4; k++) {
 #pragma unroll
@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(128) k_pair_force_m(KP kp) {
             if (k != 1) atomicAdd(&Fb[(k - 1) * N + w].w, (double)ph[k]);
         }
     }
-    block_reduce_add<14, 128>(av, kp.acc + (size_t)b * NACC);
+    block_reduce_add_f<14, 128>(av, kp.acc + (size_t)b * NACC);
 }
 
 // ---------------------------------------------------------------------------------------
