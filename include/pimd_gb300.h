@@ -209,15 +209,17 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
 /* ---------------------------------------------------------------------------------------
  * Tile-shape autotuner. Times force calls of this context on its current positions (device
  * RRt(3,Natoms,P) and RRc(3,Natoms) if given, else the last ones it was called with) for
- * candidate launch shapes -- site groups of the structure-factor kernels, k-slices of the field
- * passes, register-tiled vs. generic Ewald kernels, one-launch vs. three-launch neighbour lists
+ * candidate launch shapes -- tensor-core vs. FP32-pipe dipole structure factors, site groups of
+ * the structure-factor kernels, k-slices of the field passes, register-tiled vs. generic Ewald
+ * kernels, one-launch vs. three-launch neighbour lists
  * -- by coordinate descent, and keeps the fastest. Results change only by FP32 summation order.
  * Call before MD starts (it overwrites the dipole predictor history) and before graph capture.
  * No counterpart in the reference. */
 int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc);
 /* The chosen shapes: [tiled structure factors, site groups (0 = sized from the SM count),
  * register-row field kernels, max k-slices, one-launch neighbour lists] and, when n >= 6,
- * [wave-quantised split counts]; n >= 5. */
+ * [wave-quantised split counts], when n >= 7 [tensor-core (tcgen05) dipole structure factor
+ * in use]; n >= 5. */
 int pimd_get_tuning(pimd_ctx *ctx, int *knobs, int n);
 
 /* ---------------------------------------------------------------------------------------

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpimd_gb300.so")
-SOURCES = ["capi.cu", "neighbors.cu", "pot.cu", "ewald.cu", "mixed.cu", "nm.cu", "peak.cu", "noalloc.cu", "spc.cu", "md_batch.cu", "adjoint.cu"]
+SOURCES = ["capi.cu", "neighbors.cu", "pot.cu", "ewald.cu", "mixed.cu", "nm.cu", "peak.cu", "noalloc.cu", "spc.cu", "md_batch.cu", "adjoint.cu", "ewald_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -559,6 +559,7 @@ static int read_err(Engine &E) {
     if (e != cudaSuccess) return cuda_check(E, e, "force call");
     if (err & 1u) return fail(E, PIMD_ERR_NEIGHBOR_OVERFLOW, "neighbour list capacity exceeded");
     if (err & 4u) return fail(E, PIMD_ERR_GAMMQ, "gammq2_3 did not converge");
+    if (err & 8u) return fail(E, PIMD_ERR_CUDA, "tensor-core structure factor: pipeline wait timed out");
     return PIMD_OK;
 }
 
@@ -881,10 +882,11 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         std::vector<int> cand;
     };
     int sf_tiled = E.sf_tiled, ff_regs = E.ff_regs, nbr_block = E.nbr_block, wave = E.wave_shapes;
-    int nbr_cells = E.nbr_cells;
+    int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc;
     std::vector<Knob> knobs;
     const bool mixed = E.precision == PIMD_MIXED && E.kp.model < 4;
     if (mixed) {
+        if (E.tc_ready) knobs.push_back({&sf_tc, {1, 0}});
         knobs.push_back({&sf_tiled, {1, 0}});
         knobs.push_back({&E.sf_groups, {0, 4, 8, 16, 32}});
         knobs.push_back({&ff_regs, {1, 0}});
@@ -899,6 +901,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         E.nbr_block = nbr_block != 0;
         E.wave_shapes = wave != 0;
         E.nbr_cells = nbr_cells != 0;
+        E.sf_tc = sf_tc != 0;
     };
     int rc = PIMD_OK;
     float best;
@@ -938,6 +941,7 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     k[3] = E.max_slices;
     k[4] = E.nbr_block;
     if (n >= 6) k[5] = E.wave_shapes;
+    if (n >= 7) k[6] = E.sf_tc && E.tc_ready;
     return PIMD_OK;
 }
 

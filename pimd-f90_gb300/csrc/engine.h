@@ -153,6 +153,14 @@ struct Engine {
     bool nbr_block = true; // one-launch neighbour lists per bead for N <= 1024 (k_nbr_block)
     bool nbr_cells = true; // cell lists for N > 1024 when the box holds >= 4 cells per edge
     bool wave_shapes = true;  // k-slices / site groups chosen by wave quantisation (occupancy API)
+    // tensor-core (tcgen05, 3xTF32) dipole structure factor of the mixed engine (ewald_tc.cu)
+    bool sf_tc = true;        // use it when tc_ready
+    bool tc_ready = false;    // tiles built and the table tensor map encoded
+    int tc_ntile = 0, tc_ntg = 0, tc_nrows = 0, tc_jmax = 0, tc_tgmax = 0;
+    const int4 *d_tctile = nullptr;  // per M tile: TMEM column offset in its group, N, J, first run slot
+    const int *d_tcrun = nullptr;    // [tiles][32] run of each tile slot (-1: padding)
+    const int4 *d_tcgrp = nullptr;   // per tile group: first tile, tiles, TMEM columns
+    alignas(64) unsigned char tc_map[128];  // CUtensorMap of the FP32 tables tabf
     size_t cap = 0;
     std::vector<KRun> h_runs;
     std::vector<KChunk> h_chunks;
@@ -260,6 +268,10 @@ void launch_ewald_fq(Engine &E);
 void launch_ewald_smu(Engine &E);
 void launch_ewald_qd(Engine &E);
 void launch_ewald_pw(Engine &E);
+// tensor-core structure factor (ewald_tc.cu): setup once per context, then per call the
+// launch writes Spart partials and returns the number of site groups (0: not applicable)
+void tc_init(Engine &E);
+int launch_sfac_tc(Engine &E, int s0, int nsites, int skipconv);
 // launchers (spc.cu): q-SPC/Fw and SPC/F
 void launch_sites_spc(Engine &E);
 void launch_pair_spc(Engine &E);

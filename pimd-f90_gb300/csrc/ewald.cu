@@ -948,6 +948,16 @@ static void run_sfac_f(Engine &E, int s0, int nsites, int skipconv) {
 
 template <int OP>
 static void run_spass(Engine &E, int s0, int nsites, int skipconv) {
+    if (OP == OP_MU && E.precision == PIMD_PREC_MIXED) {
+        // tensor-core structure factor (ewald_tc.cu) when the context supports it
+        const int ngr = launch_sfac_tc(E, s0, nsites, skipconv);
+        if (ngr > 0) {
+            dim3 g2((E.kp.nk + 255) / 256, E.kp.P);
+            k_sreduce<OP, float><<<g2, 256, 0, E.stream>>>(E.kp, ngr, skipconv);
+            ++E.nlaunch;
+            return;
+        }
+    }
     if (E.precision == PIMD_PREC_MIXED) {
         if (E.sf_tiled && E.sf_nkg_max * SF_RT <= SF_MAXT)
             run_sfac_f<OP>(E, s0, nsites, skipconv);
@@ -1102,6 +1112,7 @@ static int sfac_tiles(Engine &E) {
 
 void ewald_init(Engine &E) {
     if (sfac_tiles(E) != 0) E.sf_tiled = false;  // allocation failed: untiled kernel
+    tc_init(E);
     ewald_attrs<double>();
     ewald_attrs<float>();
     // k_field_f stages [1 or 2][64 runs][LZM] complex weights: 50 KB for LZM = 49 in QD mode

@@ -1,0 +1,119 @@
+// Fifth-generation tensor-core (tcgen05) building blocks for sm_103a, written as inline PTX:
+// shared-memory matrix descriptors, the kind::tf32 instruction descriptor, TMEM allocation,
+// the single-thread MMA issue, its completion through an mbarrier, and TMEM -> register loads.
+//
+// Operand layout used throughout (K-major, no swizzle): a "core matrix" is 8 rows x 16 bytes
+// (8 rows x 4 TF32 values) stored as 128 contiguous bytes, row i at byte 16 i. An operand tile
+// of R rows x K values is a grid of (R/8) x (K/4) core matrices; the descriptor names the byte
+// distance between core matrices adjacent along K (leading byte offset) and along the rows
+// (stride byte offset). One kind::tf32 MMA consumes K = 8, i.e. two core matrices along K.
+// The accumulator of an M = 128 MMA is TMEM lanes 0..127 (row m -> lane m), one 32-bit column
+// per output column; warp w of the CTA may read lanes 32 (w % 4) .. 32 (w % 4) + 31 only.
+#pragma once
+#include <cstdint>
+
+#ifndef PIMD_D
+#define PIMD_D __device__ __forceinline__
+#endif
+
+namespace umma {
+
+PIMD_D uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Byte offset of element (r, k) of a K-major operand tile with `kcm` core matrices along K,
+// laid out K-fastest: lbo = 128, sbo = 128 kcm.
+PIMD_D int kmajor_off(int r, int k, int kcm) { return (((r >> 3) * kcm + (k >> 2)) << 7) + ((r & 7) << 4) + ((k & 3) << 2); }
+
+// Shared-memory matrix descriptor: start address, leading / stride byte offsets (all >> 4),
+// descriptor version 1 (bits 46-47), base offset 0, layout type 0 = no swizzle (bits 61-63).
+PIMD_D uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor of kind::tf32 with F32 accumulation, A and B K-major, dense:
+// D format (bits 4-5) = 1 (F32), A/B formats (bits 7-9, 10-12) = 2 (TF32), N >> 3 at bit 17,
+// M >> 4 at bit 24. M = 128 takes N = 16 .. 256 in steps of 16.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// TMEM allocation (one whole warp executes each of these; ncols a power of two >= 32)
+PIMD_D void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols) : "memory");
+}
+PIMD_D void tmem_relinquish() { asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory"); }
+PIMD_D void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// D[tmem] (+)= A[smem] x B[smem]^T, issued by one thread; accumulate = 0 overwrites D
+PIMD_D void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// The mbarrier completes one arrival when every MMA issued so far by this thread has finished
+PIMD_D void commit(uint64_t *mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
+PIMD_D void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+PIMD_D void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// generic-proxy shared-memory writes made visible to the tensor core's (async-proxy) reads
+PIMD_D void fence_smem_to_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+PIMD_D void mbar_init(uint64_t *m, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Wait until the phase with the given parity has completed, for at most ~`max_cycles` SM
+// cycles. Returns 0 on completion, 1 on timeout (the caller records an error and carries on).
+PIMD_D int mbar_wait(uint64_t *m, uint32_t parity, long long max_cycles) {
+    const uint32_t a = smem_u32(m);
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return 0;
+        if (clock64() - t0 > max_cycles) return 1;
+    }
+}
+
+// 32 TMEM lanes x 8 consecutive columns -> 8 registers per thread (thread i <- lane base + i),
+// with the wait for the load inside the same statement so no use can move above it.
+PIMD_D void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r0, r1, r2, r3, r4, r5, r6, r7;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3), "=r"(r4), "=r"(r5), "=r"(r6), "=r"(r7)
+        : "r"(taddr)
+        : "memory");
+    v[0] = __uint_as_float(r0); v[1] = __uint_as_float(r1); v[2] = __uint_as_float(r2); v[3] = __uint_as_float(r3);
+    v[4] = __uint_as_float(r4); v[5] = __uint_as_float(r5); v[6] = __uint_as_float(r6); v[7] = __uint_as_float(r7);
+}
+
+// Round to TF32 (nearest, ties away; low 13 mantissa bits cleared)
+PIMD_D float to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// x = hi + lo with hi, lo TF32: hi*hi' + hi*lo' + lo*hi' carries ~22 mantissa bits
+PIMD_D void split_tf32(float x, float &hi, float &lo) {
+    hi = to_tf32(x);
+    lo = to_tf32(x - hi);
+}
+
+}  // namespace umma
