@@ -312,7 +312,7 @@ def run_gpu_arm(args, pkg, rank, world, local, precision, steps, graph=False):
     res = dict(dev_ms=dev_ms, step_ms=step_ms, wall=wall, timers=timers, niters=niters, clocks=clk.summary(),
                launches=launches, graph_launches=graph_launches,
                out=out.tolist(), nk=nk, alpha=alpha, P=P, nw=nw, e2e_s=e2e_s, e2e_steps=e2e_steps,
-               h2d=3 * hR.nbytes, d2h=3 * hR.nbytes + 4 * 8 + hR.shape[1] * 24)
+               h2d=3 * hR.nbytes, d2h=3 * hR.nbytes + 4 * 8 + hR.shape[1] * 24, tuning=eng.tuning())
     eng.close()
     return res
 
@@ -434,6 +434,7 @@ def main():
                     precision="mixed", polar_eps=POLAR["polar_eps"], predictor=True, dt_fs=DT_FS,
                     l2="256 MB buffer written between timed steps", parallelism="replicas" if world > 1 else "1 GPU",
                     execution="one CUDA graph per MD step (dipole loop as a conditional while node)",
+                    tensor_core_structure_factor=bool(res["tuning"]["sf_tc"]),
                     dipole_iterations_mean=float(np.mean(res["niters"])),
                     fp64_dipole_iterations_mean=float(np.mean(res64["niters"]))),
         fp64=dict(value=fp64_value, steps=steps64, ms_per_step=res64["dev_ms"] / steps64,

@@ -155,11 +155,13 @@ struct Engine {
     bool wave_shapes = true;  // k-slices / site groups chosen by wave quantisation (occupancy API)
     // tensor-core (tcgen05, 3xTF32) dipole structure factor of the mixed engine (ewald_tc.cu)
     bool sf_tc = true;        // use it when tc_ready
-    bool tc_ready = false;    // tiles built and the table tensor map encoded
-    int tc_ntile = 0, tc_ntg = 0, tc_nrows = 0, tc_jmax = 0, tc_tgmax = 0;
-    const int4 *d_tctile = nullptr;  // per M tile: TMEM column offset in its group, N, J, first run slot
-    const int *d_tcrun = nullptr;    // [tiles][32] run of each tile slot (-1: padding)
-    const int4 *d_tcgrp = nullptr;   // per tile group: first tile, tiles, TMEM columns
+    bool tc_ready = false;    // run groups built and the table tensor map encoded
+    int tc_ntg = 0, tc_ncolmax = 0, tc_nabuf = 0;
+    const int4 *d_tcslot = nullptr;   // per run slot: run, local k offset, kzlo, nkz
+    const float2 *d_tcskv = nullptr;  // per run slot: FP32 (k_x, k_y)
+    const void *d_tcgrp = nullptr;    // per run group (TcGroup): slots, columns, kz rows, k-vectors
+    const int *d_tckloc = nullptr;    // k-vector of each local index, group after group
+    const float *d_tckzv = nullptr;   // FP32 k_z component by kz + lmax
     alignas(64) unsigned char tc_map[128];  // CUtensorMap of the FP32 tables tabf
     size_t cap = 0;
     std::vector<KRun> h_runs;
@@ -268,8 +270,8 @@ void launch_ewald_fq(Engine &E);
 void launch_ewald_smu(Engine &E);
 void launch_ewald_qd(Engine &E);
 void launch_ewald_pw(Engine &E);
-// tensor-core structure factor (ewald_tc.cu): setup once per context, then per call the
-// launch writes Spart partials and returns the number of site groups (0: not applicable)
+// tensor-core structure factor (ewald_tc.cu): setup once per context; per call the launch
+// writes Sm and the dipole weights Wf and returns 1, or returns 0 (not applicable)
 void tc_init(Engine &E);
 int launch_sfac_tc(Engine &E, int s0, int nsites, int skipconv);
 // launchers (spc.cu): q-SPC/Fw and SPC/F

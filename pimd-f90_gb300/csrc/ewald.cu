@@ -949,14 +949,8 @@ static void run_sfac_f(Engine &E, int s0, int nsites, int skipconv) {
 template <int OP>
 static void run_spass(Engine &E, int s0, int nsites, int skipconv) {
     if (OP == OP_MU && E.precision == PIMD_PREC_MIXED) {
-        // tensor-core structure factor (ewald_tc.cu) when the context supports it
-        const int ngr = launch_sfac_tc(E, s0, nsites, skipconv);
-        if (ngr > 0) {
-            dim3 g2((E.kp.nk + 255) / 256, E.kp.P);
-            k_sreduce<OP, float><<<g2, 256, 0, E.stream>>>(E.kp, ngr, skipconv);
-            ++E.nlaunch;
-            return;
-        }
+        // tensor-core structure factor (ewald_tc.cu), which also writes Sm and Wf
+        if (launch_sfac_tc(E, s0, nsites, skipconv)) return;
     }
     if (E.precision == PIMD_PREC_MIXED) {
         if (E.sf_tiled && E.sf_nkg_max * SF_RT <= SF_MAXT)

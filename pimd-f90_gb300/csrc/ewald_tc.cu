@@ -1,33 +1,39 @@
 // Tensor-core (tcgen05) dipole structure factor of the mixed engine:
 //   S(k) = sum_s (k.mu_s) e^{i k.r_s}            (ewald.f90:99-108, the per-iteration ewald_std_dd sum)
-// over the dipole sites of every bead, as 3xTF32 GEMMs with FP32 accumulators in TMEM.
+// over the dipole sites of every bead, as 3xTF32 GEMMs with FP32 accumulators in TMEM, followed
+// by the FP64 sum over site groups and the FP32 field weights (k_sreduce's job) in the same launch.
 //
 // Formulation. For a run (kx, ky) with kz in [kzlo, kzlo + nkz) and a site s, e^{ik.r} =
-// exy(s) ez(s, kz) with exy = ex(kx) ey(ky) (ewald.f90:30-31). Writing
-//   A0 = (kx mu_x + ky mu_y) exy,   A1 = mu_z exy,   S(kz) = G0(kz) + kz G1(kz),
-//   Gi(kz) = sum_s Ai(s) ez(s, kz),
-// and ez(-j) = conj ez(j) = c_j - i s_j, every Gi(+-j) follows from the four real sums
-//   Ar.c_j, Ar.s_j, Ai.c_j, Ai.s_j   (j = |kz| >= 0):
-//   G(+j) = (Ar.c - Ai.s) + i (Ar.s + Ai.c),   G(-j) = (Ar.c + Ai.s) + i (Ai.c - Ar.s).
-// So one real GEMM per bead, D[(run, component)][(j, cos|sin)] = sum_s A[.][s] B[.][s], with four
-// components (A0 re, A0 im, A1 re, A1 im) per run, gives every k-vector: half the products of
-// the direct complex sum over kz in [-m, m]. Rows of an M = 128 tile hold 32 runs (runs sorted by
-// kz extent, so a tile's N = 2 (max |kz| + 1), rounded up to 16, is tight); row = 32 component
-// + run slot, so the A stores of a warp fill whole 128-byte lines.
+// exy(s) ez(s, kz) with exy = ex(kx) ey(ky) (ewald.f90:30-31), and
+//   S(kz) = kx Gx(kz) + ky Gy(kz) + kz Gz(kz),   Gc(kz) = sum_s mu_c(s) exy(s) ez(s, kz).
+// With ez(-j) = conj ez(j) = c_j - i s_j, every Gc(+-j) follows from four real sums over s,
+//   Re.c = sum Re(exy) mu_c c_j,  Re.s,  Im.c,  Im.s :
+//   Gc(+j) = (Re.c - Im.s) + i (Re.s + Im.c),   Gc(-j) = (Re.c + Im.s) + i (Im.c - Re.s),
+// so one real GEMM per bead gives every k-vector:
+//   D[(c, j, cos|sin)][(run, Re|Im)] = sum_s Z[(c, j, cos|sin)][s] X[(run, Re|Im)][s],
+//   Z = mu_c(s) (c_j(s) | s_j(s)),   X = Re|Im exy(s, run).
+// The M side holds 6 (max |kz| + 1) <= 128 rows, the N side two columns per run (<= 256 runs,
+// two MMAs of N <= 256 per K step). A tcgen05 MMA costs about the same for any N <= 256 on this
+// part, so the wide, run-dependent operand goes on N; each K step of 8 sites is three MMAs
+// (hi.hi + hi.lo + lo.hi of the TF32 split) per N half.
 //
-// Pipeline of one CTA (a bead, a group of consecutive sites, a group of <= 8 tiles):
-//   * TMA (cp.async.bulk.tensor.2d, two boxes of 16 sites x all ntab rows, 128-byte swizzle)
-//     brings the FP32 tables of 32 sites into a double-buffered stage, completing on an mbarrier;
-//   * per 8 sites (one kind::tf32 K step) all threads build A (the tiles' 4 x 32 rows) and B
-//     (ez cos/sin rows) in the canonical no-swizzle K-major layout, split into TF32 hi + lo;
-//   * one thread issues hi.hi + hi.lo + lo.hi per tile into the tile's TMEM columns and commits
-//     to the buffer's mbarrier, so the MMAs of step i run while step i + 1 is built;
-//   * the epilogue reads TMEM (tcgen05.ld), combines the four components of each run through
-//     shared memory and writes the FP32 partial S of every k of its runs to Spart, which
-//     k_sreduce adds in FP64 in a fixed order, as for the other structure-factor kernels.
-// Every mbarrier wait is bounded (~0.13 s); after a timeout the CTA stops issuing work, waits
-// (bounded) for its MMAs in flight, frees its TMEM and returns, and bit 8 of the context's error
-// word is set.
+// A CTA owns one bead, one group of <= 256 runs and one group of consecutive sites; the site
+// groups of a (bead, run group) form a thread-block cluster. Warp roles:
+//   * producer warp: per 32-site stage, TMA (cp.async.bulk.tensor.2d, two boxes of 16 sites x all
+//     ntab table rows, 128-byte swizzle) plus a bulk copy of the 32 FP32 dipoles, completing on an
+//     mbarrier;
+//   * 14 builder warps: per 8 sites build X (exy of every run) and Z (mu_c ez) in the canonical
+//     no-swizzle K-major layout, split into TF32 hi + lo, into one of three buffers;
+//   * MMA warp: one thread issues the MMAs into TMEM and commits to the buffer's mbarrier, which
+//     releases the buffer to the builders.
+// Only mbarriers connect the roles, so building, copying and MMAs overlap. The epilogue reads
+// TMEM (tcgen05.ld) 32 runs at a time, combines each k-vector's 12 sums, and keeps the CTA's FP32
+// partial S in shared memory; after a cluster barrier each CTA adds the partials of all CTAs of
+// its cluster over a slice of the k-vectors (distributed shared memory, FP64, site groups in
+// order as k_sreduce does) and writes Sm and the FP32 weights Wf.
+// Every mbarrier wait is bounded (~0.13 s); after a timeout a role stops, the CTA waits (bounded)
+// for its copies and MMAs in flight, frees its TMEM, still meets its cluster barriers, and bit 8
+// of the context's error word is set.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <algorithm>
@@ -38,41 +44,51 @@
 
 namespace pimd {
 
-constexpr int TC_NT = 256;     // threads per CTA (8 warps)
-constexpr int TC_RUNS = 32;    // runs per M tile (4 rows each)
-constexpr int TC_TGMAX = 8;    // M tiles per CTA
-constexpr int TC_SS = 32;      // sites per table stage (two TMA boxes)
-constexpr int TC_KS = 8;       // sites per MMA step
+constexpr int TC_NB = 14;                 // builder warps
+constexpr int TC_MMA_WARP = TC_NB;        // MMA-issuing warp (then the producer warp)
+constexpr int TC_NT = (TC_NB + 2) * 32;   // 512 threads
+constexpr int TC_SS = 32;                 // sites per table stage
+constexpr int TC_KS = 8;                  // sites per MMA step (32 bytes of K)
+constexpr int TC_NABUF_MAX = 3;           // operand buffers
+constexpr int TC_CLMAX = 8;               // site groups per cluster (portable cluster size)
+constexpr int TC_MAXRUN = 256;            // runs per group: 512 TMEM columns
+constexpr int TC_CH = 32;                 // runs per epilogue chunk
+constexpr int TC_LD = 2 * TC_CH + 4;      // staging row pitch (floats)
 constexpr long long TC_WAIT = 1LL << 28;  // cycles before a wait gives up (~0.13 s)
 
+struct TcGroup {
+    int p0, nr, ncol, jm, nkl, kgoff, pad0, pad1;  // slots, runs, MMA columns, kz rows, k-vectors
+};
+
 struct TcArgs {
-    const int4 *tile;  // coff, N, J, first slot in run
-    const int *run;    // [tiles][32]
-    const int4 *grp;   // t0, nt, ncols
-    int ntg;           // tile groups
-    int ngroups;       // site groups
-    int sbase;         // first site of group 0 (multiple of 32, <= s_lo)
-    int s_lo, s_hi;    // dipole sites [s_lo, s_hi)
-    int tsg;           // sites per group (multiple of 32)
-    int nrows;         // B rows (max N over tiles)
-    int jmax;          // ez rows used (max J over tiles)
+    const int4 *slot;     // per slot: run, local k offset, kzlo, nkz
+    const float2 *skv;    // per slot: FP32 (k_x, k_y)
+    const TcGroup *grp;
+    const int *kloc;      // k-vector of each local index
+    const float *kzv;     // k_z by kz + lmax
+    int sbase;            // first site of site group 0 (multiple of 32, <= s_lo)
+    int s_lo, s_hi;       // dipole sites [s_lo, s_hi)
+    int tsg;              // sites per group (multiple of 32)
+    int ncolmax;          // max MMA columns over run groups
+    int nabuf;            // operand buffers
     int skipconv;
 };
 
 // Shared-memory carve-up (bytes from a 1024-aligned base), used by the kernel and the launcher.
-// A table stage is two TMA boxes of 16 sites x ntab rows, each written with the 128-byte swizzle
-// (16-byte chunk c of row r lands at chunk c ^ (r & 7)), so loads of the same sites from
-// different rows fall in different banks.
+// A table stage holds two TMA boxes of 16 sites x ntab rows, each written with the 128-byte
+// swizzle (16-byte chunk c of row r lands at chunk c ^ (r & 7), so loads of the same sites from
+// different rows fall in different banks), followed by the stage's 32 dipoles. An operand
+// buffer holds Z hi, Z lo (128 rows x 8 sites each) and X hi, X lo (ncolmax rows x 8 sites).
 struct TcSmem {
-    int boxb, stage, A, B, mu, total, astride;
-    __host__ __device__ TcSmem(int ntab, int tg, int nrows) {
+    int boxb, mu, stage, buf, xoff, bufstride, total;
+    __host__ __device__ TcSmem(int ntab, int ncolmax, int nabuf) {
         boxb = ((ntab * 128 + 1023) / 1024) * 1024;
-        stage = 2 * boxb;
-        A = 2 * stage;                     // [2 buffers][hi tiles | lo tiles][4 KB]
-        astride = 2 * tg * 4096;
-        B = A + 2 * astride;               // [2 buffers][hi | lo][nrows][32 B]
-        mu = B + 2 * 2 * nrows * 32;       // [2][32] float4
-        total = mu + 2 * TC_SS * 16 + 1024;  // + alignment slack of the dynamic base
+        mu = 2 * boxb;
+        stage = ((mu + TC_SS * 16 + 1023) / 1024) * 1024;
+        buf = 2 * stage;
+        xoff = 2 * 128 * 32;
+        bufstride = xoff + 2 * ncolmax * 32;
+        total = buf + nabuf * bufstride + 1024;  // + alignment slack of the dynamic base
     }
 };
 
@@ -93,140 +109,141 @@ PIMD_D void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_
         "l"((unsigned long long)map), "r"(x), "r"(y), "r"(umma::smem_u32(bar))
         : "memory");
 }
+// contiguous global -> shared copy (addresses 16-byte aligned, bytes a multiple of 16)
+PIMD_D void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     umma::smem_u32(dst)),
+                 "l"((unsigned long long)src), "r"(bytes), "r"(umma::smem_u32(bar))
+                 : "memory");
+}
 PIMD_D void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(umma::smem_u32(bar)), "r"(bytes) : "memory");
+}
+PIMD_D void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(umma::smem_u32(bar)) : "memory");
+}
+PIMD_D void cluster_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+PIMD_D uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+PIMD_D float2 ld_cluster_f2(uint32_t local_addr, uint32_t rank) {
+    uint32_t ra;
+    float2 v;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(local_addr), "r"(rank));
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(ra) : "memory");
+    return v;
 }
 // TF32 split by truncation: hi keeps the top 10 mantissa bits, lo = x - hi exactly
 PIMD_D void split_t(float x, float &hi, float &lo) {
     hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
     lo = x - hi;
 }
+// byte offset of (row n, site k) in a K-major operand of 8 sites (two core matrices along K)
+PIMD_D int opoff(int n, int k) { return umma::kmajor_off(n, k, TC_KS / 4); }
 
 __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CUtensorMap tmap, KP kp, TcArgs a) {
-    const int b = blockIdx.y;
+    const int grp = blockIdx.x, tg = blockIdx.y, b = blockIdx.z;
+    // the whole cluster (same bead) leaves together
     if (a.skipconv && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
-    const int tg = blockIdx.x % a.ntg, grp = blockIdx.x / a.ntg;
-    const int4 gi = a.grp[tg];
-    const int t0 = gi.x, nt = gi.y;
-    const uint32_t ncols = (uint32_t)gi.z;
+    const TcGroup G = a.grp[tg];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const TcSmem L(kp.ntab, TC_TGMAX, a.nrows);
+    const TcSmem L(kp.ntab, a.ncolmax, a.nabuf);
     extern __shared__ __align__(1024) unsigned char sm_raw[];
     // the swizzle pattern follows shared-memory address bits 7-9: align the base to 1024 bytes
     unsigned char *sm = sm_raw + ((1024u - (umma::smem_u32(sm_raw) & 1023u)) & 1023u);
-    __shared__ uint64_t tbar[2], mbar[2];
+    __shared__ uint64_t tfull[2], tempty[2], afull[TC_NABUF_MAX], aempty[TC_NABUF_MAX];
     __shared__ uint32_t tslot;
-    __shared__ int4 stile[TC_TGMAX];
-    float4 *smu = reinterpret_cast<float4 *>(sm + L.mu);
+    __shared__ int4 sslot[TC_MAXRUN];
+    __shared__ float2 sskv[TC_MAXRUN];
+    __shared__ float skz[256];
 
     const int g0 = a.sbase + grp * a.tsg;
     const int g1 = min(a.s_hi, g0 + a.tsg);
-    const int nstage = (g1 - g0 + TC_SS - 1) / TC_SS;
+    const int nstage = max(0, (g1 - g0 + TC_SS - 1) / TC_SS);
+    const int nsub = nstage * (TC_SS / TC_KS);
     const int yrow = kp.hmax + 1;            // first ey row (ky = 0)
     const int zrow = yrow + kp.kmax + 1;     // first ez row (kz = 0)
-    const uint32_t box_tx = (uint32_t)(kp.ntab * 128);
+    const int nab = a.nabuf, jm = G.jm, nr = G.nr;
+    const int xlo = a.ncolmax * 32;          // X lo after X hi
 
-    // per-thread A items (tile, run slot q, site quad h), at most two: rows 32 c + q of the tile
-    int it_n = 0;
-    int it_off[2], it_xr[2], it_yr[2], it_h[2];
-    float it_kx[2], it_ky[2], it_ys[2];
-    bool it_ok[2];
-#pragma unroll
-    for (int u = 0; u < 2; u++) {
-        const int it = tid + u * TC_NT;
-        it_ok[u] = false;
-        it_off[u] = it_xr[u] = it_yr[u] = it_h[u] = 0;
-        it_kx[u] = it_ky[u] = 0.f;
-        it_ys[u] = 1.f;
-        if (it >= nt * 64) continue;
-        it_n = u + 1;
-        const int t = it >> 6, q = (it >> 1) & 31, h = it & 1;
-        const int4 ti = a.tile[t0 + t];
-        const int r = a.run[ti.w + q];
-        // byte offset of (row q, K quad h) in tile t of the hi operand; component c adds 1024 c
-        it_off[u] = t * 4096 + (((q >> 3) * 2 + h) << 7) + ((q & 7) << 4);
-        it_h[u] = h;
-        if (r >= 0) {
-            const KRun run = kp.runs[r];
-            const float2 kv = kp.runkf[r];
-            it_ok[u] = true;
-            it_xr[u] = run.kx;
-            it_yr[u] = yrow + (run.ky < 0 ? -run.ky : run.ky);
-            it_ys[u] = run.ky < 0 ? -1.f : 1.f;
-            it_kx[u] = kv.x;
-            it_ky[u] = kv.y;
-        }
+    if (tid < nr) {
+        sslot[tid] = a.slot[G.p0 + tid];
+        sskv[tid] = a.skv[G.p0 + tid];
     }
-    if (tid < nt) stile[tid] = a.tile[t0 + tid];
-
-    if (warp == 0) umma::tmem_alloc(&tslot, ncols);
+    if (tid < 2 * kp.lmax + 1) skz[tid] = a.kzv[tid];
+    if (warp == 0) umma::tmem_alloc(&tslot, 512);
     if (tid == 0) {
-        umma::mbar_init(&tbar[0], 1);
-        umma::mbar_init(&tbar[1], 1);
-        umma::mbar_init(&mbar[0], 1);
-        umma::mbar_init(&mbar[1], 1);
+        for (int i = 0; i < 2; i++) {
+            umma::mbar_init(&tfull[i], 1);
+            umma::mbar_init(&tempty[i], TC_NB);
+        }
+        for (int i = 0; i < nab; i++) {
+            umma::mbar_init(&afull[i], TC_NB);
+            umma::mbar_init(&aempty[i], 1);
+        }
     }
-    {   // B rows n >= 2 jmax stay zero in both buffers (hi and lo)
-        const int per = a.nrows * 8, pad0 = 2 * a.jmax;
-        float *Bf = reinterpret_cast<float *>(sm + L.B);
-        for (int i = tid; i < 4 * per; i += TC_NT) {
-            const int f = i % per;
+    // padding stays zero in every buffer: Z rows >= 6 jm, X rows (columns of D) >= 2 nr
+    for (int bi = 0; bi < nab; bi++) {
+        float *Zf = reinterpret_cast<float *>(sm + L.buf + bi * L.bufstride);
+        float *Xf = reinterpret_cast<float *>(sm + L.buf + bi * L.bufstride + L.xoff);
+        for (int i = tid; i < 2 * 128 * TC_KS; i += TC_NT) {
+            const int f = i % (128 * TC_KS);
             const int n = ((f >> 5) >> 1) * 8 + ((f & 31) >> 2);
-            if (n >= pad0) Bf[i] = 0.f;
+            if (n >= 6 * jm) Zf[i] = 0.f;
+        }
+        for (int i = tid; i < 2 * a.ncolmax * TC_KS; i += TC_NT) {
+            const int f = i % (a.ncolmax * TC_KS);
+            const int n = ((f >> 5) >> 1) * 8 + ((f & 31) >> 2);
+            if (n >= 2 * nr) Xf[i] = 0.f;
         }
     }
-    auto load_mu = [&](int stage, int buf) {
-        if (tid < TC_SS) {
-            const int s = g0 + stage * TC_SS + tid;
-            float4 m = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (s >= a.s_lo && s < g1) m = kp.dipf[(size_t)b * kp.S + s];
-            smu[buf * TC_SS + tid] = m;
-        }
-    };
-    auto load_tab = [&](int stage, int buf) {  // thread 0
-        uint64_t *bar = &tbar[buf];
-        unsigned char *dst = sm + buf * L.stage;
-        const int x = 2 * (g0 + stage * TC_SS);
-        mbar_expect_tx(bar, 2 * box_tx);
-        tma_load_2d(dst, &tmap, x, b * kp.ntab, bar);
-        tma_load_2d(dst + L.boxb, &tmap, x + 2 * 16, b * kp.ntab, bar);
-    };
-    load_mu(0, 0);
+    umma::fence_smem_to_async();
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
     const uint32_t tm = tslot;
-    if (tid == 0) load_tab(0, 0);
-    int issued = 1, landed = 0;  // table stages requested / seen complete
     uint32_t err = 0;
-    bool bad = false;  // a wait timed out somewhere in the CTA: stop issuing, free TMEM, return
-    int sub = 0;
-    const uint32_t idesc_base = umma::idesc_tf32(128, 16) & ~(0x3Fu << 17);
-    for (int ts = 0; ts < nstage && !bad; ts++) {
-        const int tb = ts & 1;
-        if (ts + 1 < nstage) {  // both buffers of stage ts - 1 were last read before the last barrier
-            if (tid == 0) load_tab(ts + 1, tb ^ 1);
-            load_mu(ts + 1, tb ^ 1);
-            issued = ts + 2;
-        }
-        {
-            const int to = umma::mbar_wait(&tbar[tb], (uint32_t)((ts >> 1) & 1), TC_WAIT);
-            err |= (uint32_t)to;
-            if (!to) landed = ts + 1;
-        }
-        const unsigned char *tab = sm + tb * L.stage;
-        const float4 *mus = smu + tb * TC_SS;
-        for (int ks = 0; ks < TC_SS / TC_KS; ks++, sub++) {
-            const int ab = sub & 1;
-            if (sub >= 2) err |= (uint32_t)umma::mbar_wait(&mbar[ab], (uint32_t)(((sub - 2) >> 1) & 1), TC_WAIT);
-            unsigned char *Ab = sm + L.A + ab * L.astride;
-            unsigned char *Bb = sm + L.B + ab * 2 * a.nrows * 32;
-            const int so = ks * TC_KS;
+
+    if (warp < TC_NB) {
+        // ---------------- builders: X = exy of every run (4 sites per item), Z = mu_c ez
+        const int bt = tid;  // 0 .. 32 TC_NB - 1
+        int it_n = 0, it_off[2], it_xr[2], it_yr[2], it_h[2];
+        float it_ys[2];
 #pragma unroll
-            for (int u = 0; u < 2; u++) {
-                if (u >= it_n) break;
-                float4 c[4];
-                if (it_ok[u]) {
+        for (int u = 0; u < 2; u++) {
+            const int it = bt + u * 32 * TC_NB;
+            it_off[u] = it_xr[u] = it_yr[u] = it_h[u] = 0;
+            it_ys[u] = 1.f;
+            if (it >= 2 * nr) continue;
+            it_n = u + 1;
+            const int p = it >> 1, h = it & 1;
+            const KRun run = kp.runs[sslot[p].x];
+            it_off[u] = opoff(2 * p, 4 * h);  // Re row; the Im row 2 p + 1 is 16 bytes further
+            it_h[u] = h;
+            it_xr[u] = run.kx;
+            it_yr[u] = yrow + (run.ky < 0 ? -run.ky : run.ky);
+            it_ys[u] = run.ky < 0 ? -1.f : 1.f;
+        }
+        const bool zit = bt < jm * TC_KS;
+        const int zj = bt >> 3, zk = bt & 7;
+        for (int ts = 0; ts < nstage && !err; ts++) {
+            const int tb = ts & 1;
+            err |= (uint32_t)umma::mbar_wait(&tfull[tb], (uint32_t)((ts >> 1) & 1), TC_WAIT);
+            const unsigned char *tab = sm + tb * L.stage;
+            const float4 *mus = reinterpret_cast<const float4 *>(tab + L.mu);
+            const int sfirst = g0 + ts * TC_SS;
+            for (int ks = 0; ks < TC_SS / TC_KS && !err; ks++) {
+                const int sub = ts * (TC_SS / TC_KS) + ks, ab = sub % nab, use = sub / nab;
+                if (use > 0) err |= (uint32_t)umma::mbar_wait(&aempty[ab], (uint32_t)((use - 1) & 1), TC_WAIT);
+                unsigned char *Bf = sm + L.buf + ab * L.bufstride;
+                const int so = ks * TC_KS;
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    if (u >= it_n) break;
                     const int sq = so + 4 * it_h[u];
                     const float4 x01 = *tab_chunk(tab, L.boxb, it_xr[u], sq);
                     const float4 x23 = *tab_chunk(tab, L.boxb, it_xr[u], sq + 2);
@@ -235,130 +252,168 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
                     const float ys = it_ys[u];
                     const float ex[4][2] = {{x01.x, x01.y}, {x01.z, x01.w}, {x23.x, x23.y}, {x23.z, x23.w}};
                     const float ey[4][2] = {{y01.x, ys * y01.y}, {y01.z, ys * y01.w}, {y23.x, ys * y23.y}, {y23.z, ys * y23.w}};
-                    float v[4][4];
+                    float re[4], im[4];
 #pragma unroll
                     for (int i = 0; i < 4; i++) {
-                        const float4 m = mus[sq + i];
                         // ewald.f90:30-31: coskxky = cx cy - sx sy, sinkxky = sx cy + cx sy
-                        const float er = ex[i][0] * ey[i][0] - ex[i][1] * ey[i][1];
-                        const float ei = ex[i][1] * ey[i][0] + ex[i][0] * ey[i][1];
-                        const float t = fmaf(it_kx[u], m.x, it_ky[u] * m.y);  // k.mu without k_z
-                        v[0][i] = t * er;
-                        v[1][i] = t * ei;
-                        v[2][i] = m.z * er;
-                        v[3][i] = m.z * ei;
+                        re[i] = ex[i][0] * ey[i][0] - ex[i][1] * ey[i][1];
+                        im[i] = ex[i][1] * ey[i][0] + ex[i][0] * ey[i][1];
                     }
-#pragma unroll
-                    for (int cc = 0; cc < 4; cc++) c[cc] = make_float4(v[cc][0], v[cc][1], v[cc][2], v[cc][3]);
-                } else {
-#pragma unroll
-                    for (int cc = 0; cc < 4; cc++) c[cc] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    float4 rh, rl, ih, il;
+                    split_t(re[0], rh.x, rl.x);
+                    split_t(re[1], rh.y, rl.y);
+                    split_t(re[2], rh.z, rl.z);
+                    split_t(re[3], rh.w, rl.w);
+                    split_t(im[0], ih.x, il.x);
+                    split_t(im[1], ih.y, il.y);
+                    split_t(im[2], ih.z, il.z);
+                    split_t(im[3], ih.w, il.w);
+                    unsigned char *xp = Bf + L.xoff + it_off[u];
+                    *reinterpret_cast<float4 *>(xp) = rh;
+                    *reinterpret_cast<float4 *>(xp + 16) = ih;
+                    *reinterpret_cast<float4 *>(xp + xlo) = rl;
+                    *reinterpret_cast<float4 *>(xp + xlo + 16) = il;
                 }
+                if (zit) {
+                    const int s = sfirst + so + zk;
+                    float4 m = mus[so + zk];
+                    if (s < a.s_lo || s >= g1) m = make_float4(0.f, 0.f, 0.f, 0.f);
+                    const float2 z = tab_elem(tab, L.boxb, zrow + zj, so + zk);
+                    const float mc[3] = {m.x, m.y, m.z};
+                    float *Zh = reinterpret_cast<float *>(Bf);
+                    float *Zl = reinterpret_cast<float *>(Bf + 128 * 32);
 #pragma unroll
-                for (int cc = 0; cc < 4; cc++) {
-                    float4 hi, lo;
-                    split_t(c[cc].x, hi.x, lo.x);
-                    split_t(c[cc].y, hi.y, lo.y);
-                    split_t(c[cc].z, hi.z, lo.z);
-                    split_t(c[cc].w, hi.w, lo.w);
-                    *reinterpret_cast<float4 *>(Ab + it_off[u] + cc * 1024) = hi;
-                    *reinterpret_cast<float4 *>(Ab + nt * 4096 + it_off[u] + cc * 1024) = lo;
+                    for (int c = 0; c < 3; c++) {
+                        const int row = (c * jm + zj) * 2;
+                        const int o0 = opoff(row, zk) >> 2, o1 = opoff(row + 1, zk) >> 2;
+                        float hi, lo;
+                        split_t(mc[c] * z.x, hi, lo);
+                        Zh[o0] = hi;
+                        Zl[o0] = lo;
+                        split_t(mc[c] * z.y, hi, lo);
+                        Zh[o1] = hi;
+                        Zl[o1] = lo;
+                    }
                 }
+                umma::fence_smem_to_async();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&afull[ab]);
             }
-            // B rows 2j (cos) and 2j + 1 (sin) of ez, K = the step's 8 sites
-            if (tid < a.jmax * TC_KS) {
-                const int j = tid >> 3, k = tid & 7;
-                const float2 z = tab_elem(tab, L.boxb, zrow + j, so + k);
-                float *Bh = reinterpret_cast<float *>(Bb);
-                float *Bl = Bh + a.nrows * 8;
-                const int n0 = 2 * j, n1 = 2 * j + 1;
-                const int o0 = (umma::kmajor_off(n0, k, 2)) >> 2;
-                const int o1 = (umma::kmajor_off(n1, k, 2)) >> 2;
-                float hi, lo;
-                split_t(z.x, hi, lo);
-                Bh[o0] = hi;
-                Bl[o0] = lo;
-                split_t(z.y, hi, lo);
-                Bh[o1] = hi;
-                Bl[o1] = lo;
-            }
-            umma::fence_smem_to_async();
-            if (__syncthreads_or((int)err)) {
-                bad = true;
-                break;
-            }
-            if (tid == 0) {
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[tb]);
+        }
+    } else if (warp == TC_MMA_WARP) {
+        // ---------------- MMA issue (one thread): D[128][ncol] += Z X^T, two N halves
+        if (lane == 0) {
+            const uint32_t idesc_base = umma::idesc_tf32(128, 16) & ~(0x3Fu << 17);
+            for (int sub = 0; sub < nsub && !err; sub++) {
+                const int ab = sub % nab, use = sub / nab;
+                err |= (uint32_t)umma::mbar_wait(&afull[ab], (uint32_t)(use & 1), TC_WAIT);
+                if (err) break;
                 umma::fence_after_sync();
-                const uint32_t aH = umma::smem_u32(Ab), aL = aH + nt * 4096;
-                const uint32_t bH = umma::smem_u32(Bb), bL = bH + a.nrows * 32;
-                const uint64_t db_h = umma::sdesc(bH, 128, 256), db_l = umma::sdesc(bL, 128, 256);
-                for (int t = 0; t < nt; t++) {
-                    const int4 ti = stile[t];
-                    const uint32_t id = idesc_base | ((uint32_t)(ti.y >> 3) << 17);
-                    const uint32_t d = tm + (uint32_t)ti.x;
-                    const uint64_t da_h = umma::sdesc(aH + t * 4096, 128, 256), da_l = umma::sdesc(aL + t * 4096, 128, 256);
-                    umma::mma_tf32(d, da_h, db_h, id, sub > 0);
-                    umma::mma_tf32(d, da_h, db_l, id, 1);
-                    umma::mma_tf32(d, da_l, db_h, id, 1);
+                const uint32_t zH = umma::smem_u32(sm + L.buf + ab * L.bufstride), zL = zH + 128 * 32;
+                const uint32_t xH = zH + L.xoff, xL = xH + xlo;
+                const uint64_t dz_h = umma::sdesc(zH, 128, 256), dz_l = umma::sdesc(zL, 128, 256);
+                for (int nt = 0; nt * 256 < G.ncol; nt++) {
+                    const int N = min(256, G.ncol - nt * 256);
+                    const uint32_t id = idesc_base | ((uint32_t)(N >> 3) << 17);
+                    const uint32_t d = tm + (uint32_t)(nt * 256);
+                    // rows 256 nt.. of X: 32 row groups of 256 bytes per half
+                    const uint64_t dx_h = umma::sdesc(xH + nt * 8192, 128, 256), dx_l = umma::sdesc(xL + nt * 8192, 128, 256);
+                    umma::mma_tf32(d, dz_h, dx_h, id, sub > 0);
+                    umma::mma_tf32(d, dz_h, dx_l, id, 1);
+                    umma::mma_tf32(d, dz_l, dx_h, id, 1);
                 }
-                umma::commit(&mbar[ab]);
+                umma::commit(&aempty[ab]);
             }
         }
+    } else {
+        // ---------------- producer: tables + dipoles of each 32-site stage by TMA
+        if (lane == 0) {
+            const uint32_t box_tx = (uint32_t)(kp.ntab * 128);
+            int issued = 0, landed = 0;
+            for (int ts = 0; ts < nstage && !err; ts++) {
+                const int tb = ts & 1;
+                if (ts >= 2) {
+                    // buffer tb: all builder warps done with stage ts - 2, whose copy has landed
+                    err |= (uint32_t)umma::mbar_wait(&tempty[tb], (uint32_t)(((ts - 2) >> 1) & 1), TC_WAIT);
+                    if (err) break;
+                    landed = ts - 1;
+                }
+                const int sfirst = g0 + ts * TC_SS;
+                unsigned char *dst = sm + tb * L.stage;
+                const int nmu = min(TC_SS, kp.S - sfirst);  // dipoles inside this bead's rows
+                const uint32_t mub = (uint32_t)nmu * 16u;
+                mbar_expect_tx(&tfull[tb], 2 * box_tx + mub);
+                tma_load_2d(dst, &tmap, 2 * sfirst, b * kp.ntab, &tfull[tb]);
+                tma_load_2d(dst + L.boxb, &tmap, 2 * sfirst + 32, b * kp.ntab, &tfull[tb]);
+                bulk_load(dst + L.mu, kp.dipf + (size_t)b * kp.S + sfirst, mub, &tfull[tb]);
+                issued = ts + 1;
+            }
+            // the builders saw every copy land unless something timed out: then wait here
+            for (int w = landed; w < issued && err; w++) umma::mbar_wait(&tfull[w & 1], (uint32_t)((w >> 1) & 1), TC_WAIT);
+        }
     }
-    // all MMAs done: the last commit tracks every earlier MMA of the issuing thread
-    if (sub > 0) {
-        const int last = sub - 1;
-        int to = umma::mbar_wait(&mbar[last & 1], (uint32_t)((last >> 1) & 1), TC_WAIT);
-        if (to) to = umma::mbar_wait(&mbar[last & 1], (uint32_t)((last >> 1) & 1), TC_WAIT);
+
+    // ---------------- all MMAs done: the last commit tracks every earlier MMA of the issuing thread
+    if (nsub > 0) {
+        const int last = nsub - 1;
+        int to = umma::mbar_wait(&aempty[last % nab], (uint32_t)((last / nab) & 1), TC_WAIT);
+        if (to) to = umma::mbar_wait(&aempty[last % nab], (uint32_t)((last / nab) & 1), TC_WAIT);
         err |= (uint32_t)to;
     }
-    // table copies still in flight after a timeout land before the CTA leaves
-    for (int w = landed; w < issued && err; w++) umma::mbar_wait(&tbar[w & 1], (uint32_t)((w >> 1) & 1), TC_WAIT);
     umma::fence_after_sync();
-    bad = __syncthreads_or((int)err) != 0;
-    // epilogue, one tile at a time through shared memory (the A buffers are free now)
-    float *stg = reinterpret_cast<float *>(sm + L.A);
-    float2 *part = reinterpret_cast<float2 *>(kp.Spart) + ((size_t)b * a.ngroups + grp) * kp.nk;
-    for (int t = 0; t < nt && !bad; t++) {
-        const int4 ti = stile[t];
-        const int N = ti.y, J = ti.z, ld = N + 4;
-        const int lq = warp & 3, half = warp >> 2, ncol = N / 2;
-        for (int c0 = half * ncol; c0 < (half + 1) * ncol; c0 += 8) {
+    const bool bad = __syncthreads_or((int)err) != 0;
+
+    // epilogue: TMEM -> shared, 32 runs (64 columns) at a time -> partial S of every k of the group
+    float *stg = reinterpret_cast<float *>(sm);                       // [128][TC_LD]
+    float2 *pt = reinterpret_cast<float2 *>(sm + 128 * TC_LD * 4);    // [nkl]
+    for (int ch = 0; ch * TC_CH < nr && !bad; ch++) {
+        {
+            const int lq = warp & 3, part = warp >> 2;  // 4 lane quarters x 4 column quarters
+            const int c0 = ch * 2 * TC_CH + 16 * part;
             float v[8];
-            if (sub > 0) {
-                umma::tmem_ld8(tm + ((uint32_t)(32 * lq) << 16) + (uint32_t)(ti.x + c0), v);
-            } else {
+            float *row = stg + (32 * lq + lane) * TC_LD + 16 * part;
 #pragma unroll
-                for (int j = 0; j < 8; j++) v[j] = 0.f;
+            for (int hh = 0; hh < 2; hh++) {
+                if (nsub > 0) {
+                    umma::tmem_ld8(tm + ((uint32_t)(32 * lq) << 16) + (uint32_t)(c0 + 8 * hh), v);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 8; j++) v[j] = 0.f;
+                }
+                *reinterpret_cast<float4 *>(row + 8 * hh) = make_float4(v[0], v[1], v[2], v[3]);
+                *reinterpret_cast<float4 *>(row + 8 * hh + 4) = make_float4(v[4], v[5], v[6], v[7]);
             }
-            float *row = stg + (32 * lq + lane) * ld + c0;
-            *reinterpret_cast<float4 *>(row) = make_float4(v[0], v[1], v[2], v[3]);
-            *reinterpret_cast<float4 *>(row + 4) = make_float4(v[4], v[5], v[6], v[7]);
         }
         __syncthreads();
-        for (int i = tid; i < TC_RUNS * J; i += TC_NT) {
-            const int q = i / J, j = i - q * J;
-            const int r = a.run[ti.w + q];
-            if (r < 0) continue;
-            const KRun run = kp.runs[r];
-            // (x, y) = (A.c_j, A.s_j) of the four components
-            const float2 p0r = *reinterpret_cast<const float2 *>(stg + (0 * 32 + q) * ld + 2 * j);
-            const float2 p0i = *reinterpret_cast<const float2 *>(stg + (1 * 32 + q) * ld + 2 * j);
-            const float2 p1r = *reinterpret_cast<const float2 *>(stg + (2 * 32 + q) * ld + 2 * j);
-            const float2 p1i = *reinterpret_cast<const float2 *>(stg + (3 * 32 + q) * ld + 2 * j);
-            if (j >= run.kzlo && j < run.kzlo + run.nkz) {
-                const int k = run.kbeg + j - run.kzlo;
-                const float kz = kp.kzf[k];
-                const float g0r = p0r.x - p0i.y, g0i = p0r.y + p0i.x;
-                const float g1r = p1r.x - p1i.y, g1i = p1r.y + p1i.x;
-                part[k] = make_float2(fmaf(kz, g1r, g0r), fmaf(kz, g1i, g0i));
+        for (int i = tid; i < TC_CH * jm; i += TC_NT) {
+            const int q = i % TC_CH, j = i / TC_CH, p = ch * TC_CH + q;
+            if (p >= nr) continue;
+            const int4 sl = sslot[p];  // run, local offset, kzlo, nkz
+            const bool plus = j >= sl.z && j < sl.z + sl.w;
+            const bool minus = j > 0 && -j >= sl.z && -j < sl.z + sl.w;
+            if (!plus && !minus) continue;
+            float2 gp[3], gm[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const int rc = (c * jm + j) * 2;
+                // (x, y) = (Re exy, Im exy) against mu_c c_j (row rc) and mu_c s_j (row rc + 1)
+                const float2 dc = *reinterpret_cast<const float2 *>(stg + rc * TC_LD + 2 * q);
+                const float2 ds = *reinterpret_cast<const float2 *>(stg + (rc + 1) * TC_LD + 2 * q);
+                gp[c] = make_float2(dc.x - ds.y, ds.x + dc.y);
+                gm[c] = make_float2(dc.x + ds.y, dc.y - ds.x);
             }
-            if (j > 0 && -j >= run.kzlo && -j < run.kzlo + run.nkz) {
-                const int k = run.kbeg - j - run.kzlo;
-                const float kz = kp.kzf[k];
-                const float g0r = p0r.x + p0i.y, g0i = p0i.x - p0r.y;
-                const float g1r = p1r.x + p1i.y, g1i = p1i.x - p1r.y;
-                part[k] = make_float2(fmaf(kz, g1r, g0r), fmaf(kz, g1i, g0i));
+            const float2 kv = sskv[p];
+            if (plus) {
+                const float kz = skz[kp.lmax + j];
+                pt[sl.y + j - sl.z] = make_float2(fmaf(kz, gp[2].x, fmaf(kv.y, gp[1].x, kv.x * gp[0].x)),
+                                                  fmaf(kz, gp[2].y, fmaf(kv.y, gp[1].y, kv.x * gp[0].y)));
+            }
+            if (minus) {
+                const float kz = skz[kp.lmax - j];
+                pt[sl.y - j - sl.z] = make_float2(fmaf(kz, gm[2].x, fmaf(kv.y, gm[1].x, kv.x * gm[0].x)),
+                                                  fmaf(kz, gm[2].y, fmaf(kv.y, gm[1].y, kv.x * gm[0].y)));
             }
         }
         __syncthreads();
@@ -367,10 +422,31 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     __syncthreads();
     if (warp == 0) {
         umma::fence_after_sync();
-        umma::tmem_dealloc(tm, ncols);
+        umma::tmem_dealloc(tm, 512);
         umma::tmem_relinquish();
     }
-    if (err && tid == 0) atomicOr(kp.err, 8u);
+    // cluster: add the partials of all site groups over this CTA's slice of the k-vectors
+    // (FP64, groups in order, as k_sreduce<OP_MU>), then Sm = (-Im, Re) and the FP32 weights
+    cluster_sync();
+    if (!bad) {
+        const int cr = (int)cluster_rank(), cn = gridDim.x;
+        const int i0 = (int)((long)cr * G.nkl / cn), i1 = (int)((long)(cr + 1) * G.nkl / cn);
+        const uint32_t pbase = umma::smem_u32(pt);
+        for (int i = i0 + tid; i < i1; i += TC_NT) {
+            double sx = 0.0, sy = 0.0;
+            for (int c = 0; c < cn; c++) {
+                const float2 v = ld_cluster_f2(pbase + 8u * (uint32_t)i, (uint32_t)c);
+                sx += (double)v.x;
+                sy += (double)v.y;
+            }
+            const int k = a.kloc[G.kgoff + i];
+            kp.Sm[(size_t)b * kp.nk + k] = make_double2(-sy, sx);
+            const double w = kp.kinfo[k].w;
+            kp.Wf[((size_t)b * 2 + 1) * kp.nk + k] = make_float2((float)(w * -sy), (float)(-w * sx));
+        }
+    }
+    cluster_sync();  // remote reads done before any CTA of the cluster leaves
+    if (bad && tid == 0) atomicOr(kp.err, 8u);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -393,78 +469,102 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 void tc_init(Engine &E) {
     E.tc_ready = false;
     KP &kp = E.kp;
-    if (E.precision != PIMD_MIXED || kp.ld <= kp.fd || !kp.tabf || !kp.dipf) return;
-    // TMA rules: row pitch S x 8 bytes a multiple of 16, box rows <= 256
-    if ((kp.S & 1) || kp.ntab > 256) return;
+    if (E.precision != PIMD_MIXED || kp.ld <= kp.fd || !kp.tabf || !kp.dipf || !kp.Wf) return;
+    // TMA rules: row pitch S x 8 bytes a multiple of 16, box rows <= 256; kz table <= 256
+    if ((kp.S & 1) || kp.ntab > 256 || 2 * kp.lmax + 1 > 256) return;
     int major = 0;
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, E.device);
     if (major != 10) return;
     PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
     if (!enc) return;
-    // runs sorted by their largest |kz| (longest first), 32 per M tile
+    // the FP32 k_z of a k-vector depends on kz alone
+    std::vector<float> kzv(2 * kp.lmax + 1, 0.f);
+    std::vector<int> kzseen(2 * kp.lmax + 1, 0);
+    for (int r = 0; r < kp.nrun; r++) {
+        const KRun &run = E.h_runs[r];
+        for (int j = 0; j < run.nkz; j++) {
+            const int kz = run.kzlo + j, k = run.kbeg + j;
+            const float v = (float)E.h_kvec[3 * k + 2];
+            if (kzseen[kz + kp.lmax] && kzv[kz + kp.lmax] != v) return;
+            kzseen[kz + kp.lmax] = 1;
+            kzv[kz + kp.lmax] = v;
+        }
+    }
+    // runs sorted by their largest |kz| (longest first), groups of <= 256 runs, 6 (max |kz| + 1)
+    // Z rows per group <= 128
     std::vector<int> order(kp.nrun), jr(kp.nrun);
     for (int r = 0; r < kp.nrun; r++) {
         const KRun &run = E.h_runs[r];
-        const int lo = run.kzlo, hi = run.kzlo + run.nkz - 1;
-        jr[r] = std::max(std::abs(lo), std::abs(hi)) + 1;
+        jr[r] = std::max(std::abs(run.kzlo), std::abs(run.kzlo + run.nkz - 1)) + 1;
         order[r] = r;
     }
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return jr[x] > jr[y]; });
-    const int T = (kp.nrun + TC_RUNS - 1) / TC_RUNS;
-    std::vector<int4> tiles(T), groups;
-    std::vector<int> slots((size_t)T * TC_RUNS, -1);
-    int jmax = 1, nrows = 16;
-    for (int t = 0; t < T; t++) {
-        int J = 1;
-        for (int q = 0; q < TC_RUNS && t * TC_RUNS + q < kp.nrun; q++) {
-            const int r = order[t * TC_RUNS + q];
-            slots[(size_t)t * TC_RUNS + q] = r;
-            J = std::max(J, jr[r]);
+    std::vector<int4> slots(kp.nrun);
+    std::vector<float2> skv(kp.nrun);
+    std::vector<TcGroup> groups;
+    std::vector<int> kloc;
+    std::vector<float2> runkf(kp.nrun);
+    for (int r = 0; r < kp.nrun; r++)
+        runkf[r] = make_float2((float)E.h_kvec[3 * E.h_runs[r].kbeg], (float)E.h_kvec[3 * E.h_runs[r].kbeg + 1]);
+    int ncolmax = 16, nklmax = 0;
+    for (int p0 = 0; p0 < kp.nrun; p0 += TC_MAXRUN) {
+        TcGroup g{p0, std::min(TC_MAXRUN, kp.nrun - p0), 0, jr[order[p0]], 0, (int)kloc.size(), 0, 0};
+        if (6 * g.jm > 128) return;
+        g.ncol = ((2 * g.nr + 15) / 16) * 16;
+        for (int p = p0; p < p0 + g.nr; p++) {
+            const int r = order[p];
+            const KRun &run = E.h_runs[r];
+            slots[p] = make_int4(r, g.nkl, run.kzlo, run.nkz);
+            skv[p] = runkf[r];
+            for (int j = 0; j < run.nkz; j++) kloc.push_back(run.kbeg + j);
+            g.nkl += run.nkz;
         }
-        const int N = ((2 * J + 15) / 16) * 16;
-        if (N > 256) return;
-        tiles[t] = make_int4(0, N, J, t * TC_RUNS);
-        jmax = std::max(jmax, J);
-        nrows = std::max(nrows, N);
+        groups.push_back(g);
+        ncolmax = std::max(ncolmax, g.ncol);
+        nklmax = std::max(nklmax, g.nkl);
     }
-    // tile groups of <= 8 tiles whose TMEM columns fit in 512
-    for (int t = 0; t < T;) {
-        int cols = 0, n = 0;
-        while (t + n < T && n < TC_TGMAX && cols + tiles[t + n].y <= 512) {
-            tiles[t + n].x = cols;
-            cols += tiles[t + n].y;
-            n++;
-        }
-        if (n == 0) return;
-        int pw = 32;
-        while (pw < cols) pw *= 2;
-        groups.push_back(make_int4(t, n, pw, 0));
-        t += n;
-    }
-    if (jmax * TC_KS > TC_NT) return;
-    const TcSmem L(kp.ntab, TC_TGMAX, nrows);
-    if (L.total > 200 * 1024) return;
-    // one limit for every context (the attribute belongs to the function, not the context)
-    if (cudaFuncSetAttribute(k_sfac_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess) {
+    if ((int)kloc.size() != kp.nk) return;
+    // dynamic shared memory available: the opt-in limit minus the kernel's static part
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, E.device);
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, k_sfac_tc) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
-    int4 *d_tiles = nullptr, *d_groups = nullptr;
-    int *d_slots = nullptr;
-    if (cudaMalloc((void **)&d_tiles, sizeof(int4) * T) != cudaSuccess ||
-        cudaMalloc((void **)&d_groups, sizeof(int4) * groups.size()) != cudaSuccess ||
-        cudaMalloc((void **)&d_slots, sizeof(int) * slots.size()) != cudaSuccess) {
+    const int dmax = optin - (int)fa.sharedSizeBytes;
+    // operand buffers: three when they fit, else two
+    int nabuf = TC_NABUF_MAX;
+    while (nabuf > 2 && TcSmem(kp.ntab, ncolmax, nabuf).total > dmax) nabuf--;
+    const TcSmem L(kp.ntab, ncolmax, nabuf);
+    if (L.total > dmax) return;
+    // the epilogue's staging tile and partial S reuse the table and operand regions
+    if (128 * TC_LD * 4 + 8 * nklmax > L.total - 1024) return;
+    if (cudaFuncSetAttribute(k_sfac_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, dmax) != cudaSuccess) {
         cudaGetLastError();
-        if (d_tiles) cudaFree(d_tiles);
-        if (d_groups) cudaFree(d_groups);
         return;
     }
-    E.allocs.push_back(d_tiles);
-    E.allocs.push_back(d_groups);
-    E.allocs.push_back(d_slots);
-    cudaMemcpy(d_tiles, tiles.data(), sizeof(int4) * T, cudaMemcpyHostToDevice);
-    cudaMemcpy(d_groups, groups.data(), sizeof(int4) * groups.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(d_slots, slots.data(), sizeof(int) * slots.size(), cudaMemcpyHostToDevice);
+    int4 *d_slots = nullptr;
+    float2 *d_skv = nullptr;
+    TcGroup *d_groups = nullptr;
+    int *d_kloc = nullptr;
+    float *d_kzv = nullptr;
+    if (cudaMalloc((void **)&d_slots, sizeof(int4) * slots.size()) != cudaSuccess ||
+        cudaMalloc((void **)&d_skv, sizeof(float2) * skv.size()) != cudaSuccess ||
+        cudaMalloc((void **)&d_groups, sizeof(TcGroup) * groups.size()) != cudaSuccess ||
+        cudaMalloc((void **)&d_kloc, sizeof(int) * kloc.size()) != cudaSuccess ||
+        cudaMalloc((void **)&d_kzv, sizeof(float) * kzv.size()) != cudaSuccess) {
+        cudaGetLastError();
+        for (void *p : {(void *)d_slots, (void *)d_skv, (void *)d_groups, (void *)d_kloc, (void *)d_kzv})
+            if (p) cudaFree(p);
+        return;
+    }
+    for (void *p : {(void *)d_slots, (void *)d_skv, (void *)d_groups, (void *)d_kloc, (void *)d_kzv}) E.allocs.push_back(p);
+    cudaMemcpy(d_slots, slots.data(), sizeof(int4) * slots.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_skv, skv.data(), sizeof(float2) * skv.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_groups, groups.data(), sizeof(TcGroup) * groups.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_kloc, kloc.data(), sizeof(int) * kloc.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_kzv, kzv.data(), sizeof(float) * kzv.size(), cudaMemcpyHostToDevice);
     // tables [P][ntab][S] float2 as a 2-D FP32 tensor (x = 2 S values, y = P ntab rows); a box
     // is 16 sites (128 bytes) x ntab rows, written to shared memory with the 128-byte swizzle
     CUtensorMap *map = reinterpret_cast<CUtensorMap *>(E.tc_map);
@@ -475,47 +575,68 @@ void tc_init(Engine &E) {
     if (enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, kp.tabf, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return;
-    E.d_tctile = d_tiles;
+    E.d_tcslot = d_slots;
+    E.d_tcskv = d_skv;
     E.d_tcgrp = d_groups;
-    E.d_tcrun = d_slots;
-    E.tc_ntile = T;
+    E.d_tckloc = d_kloc;
+    E.d_tckzv = d_kzv;
     E.tc_ntg = (int)groups.size();
-    E.tc_nrows = nrows;
-    E.tc_jmax = jmax;
-    E.tc_tgmax = TC_TGMAX;
+    E.tc_ncolmax = ncolmax;
+    E.tc_nabuf = nabuf;
     E.tc_ready = true;
 }
 
+// Returns 1 when the launch wrote Sm and the dipole weights Wf (no k_sreduce needed), else 0.
 int launch_sfac_tc(Engine &E, int s0, int nsites, int skipconv) {
     if (!E.tc_ready || !E.sf_tc || nsites <= 0) return 0;
     const KP &kp = E.kp;
     TcArgs a;
-    a.tile = E.d_tctile;
-    a.run = E.d_tcrun;
-    a.grp = E.d_tcgrp;
-    a.ntg = E.tc_ntg;
+    a.slot = E.d_tcslot;
+    a.skv = E.d_tcskv;
+    a.grp = reinterpret_cast<const TcGroup *>(E.d_tcgrp);
+    a.kloc = E.d_tckloc;
+    a.kzv = E.d_tckzv;
     a.sbase = s0 & ~(TC_SS - 1);  // TMA x coordinate 2 sbase: 256-byte aligned
     a.s_lo = s0;
     a.s_hi = s0 + nsites;
-    a.nrows = E.tc_nrows;
-    a.jmax = E.tc_jmax;
+    a.ncolmax = E.tc_ncolmax;
+    a.nabuf = E.tc_nabuf;
     a.skipconv = skipconv;
-    // one CTA per SM (shared memory), one wave: site groups of whole 32-site stages
+    // one CTA per SM (shared memory); site groups (= cluster size) so that one wave fills the GPU
+    static int nsm_cache[64] = {0};
+    int &nsm = nsm_cache[E.device & 63];
+    if (!nsm) {
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, E.device);
+        if (nsm <= 0) nsm = 152;
+    }
     const int nst = (a.s_hi - a.sbase + TC_SS - 1) / TC_SS;
     const long per = (long)E.tc_ntg * kp.P;
-    int nsm = 0;
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, E.device);
-    int ng = (int)std::max(1L, (long)std::max(nsm, 1) / per);
-    ng = std::max(1, std::min(ng, std::min(nst, E.sp_cap)));
+    int ng = (int)std::max(1L, (long)nsm / per);
+    ng = std::max(1, std::min(ng, std::min(nst, TC_CLMAX)));
     const int spg = (nst + ng - 1) / ng;
     a.tsg = spg * TC_SS;
-    a.ngroups = (nst + spg - 1) / spg;
-    const TcSmem L(kp.ntab, TC_TGMAX, a.nrows);
-    dim3 g(E.tc_ntg * a.ngroups, kp.P);
+    ng = (nst + spg - 1) / spg;
+    const TcSmem L(kp.ntab, a.ncolmax, a.nabuf);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ng, E.tc_ntg, kp.P);
+    cfg.blockDim = dim3(TC_NT);
+    cfg.dynamicSmemBytes = L.total;
+    cfg.stream = E.stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = ng;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
     const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(E.tc_map);
-    k_sfac_tc<<<g, TC_NT, L.total, E.stream>>>(*map, kp, a);
+    if (cudaLaunchKernelEx(&cfg, k_sfac_tc, *map, kp, a) != cudaSuccess) {
+        cudaGetLastError();
+        E.sf_tc = false;  // e.g. no room for the cluster: the FP32-pipe kernel from now on
+        return 0;
+    }
     ++E.nlaunch;
-    return a.ngroups;
+    return 1;
 }
 
 }  // namespace pimd

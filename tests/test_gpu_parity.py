@@ -158,6 +158,19 @@ def test_mixed_error_budget_small(pkg, orc, engine_lib, model):
     assert np.array_equal(eng.neighbors(0), o.neighbors(c["RRt"][0]))
 
 
+@pytest.mark.parametrize("model", [3, 2])
+def test_tensor_core_structure_factor_active(pkg, orc, engine_lib, model):
+    """The mixed engine's dipole structure factor runs on the tcgen05 kernel (a silent fallback
+    to the FP32-pipe kernel fails here) and stays inside the mixed error budget."""
+    c, p = small_case(pkg, model, nw=64, P=4, polar_maxiter=40)
+    eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_MIXED)
+    got = eng.full_bead_forces(c["RRt"], c["RRc"], t=1)
+    assert eng.tuning()["sf_tc"] == 1
+    ref = orc.full_bead_forces(p, c["RRt"], c["RRc"], t=1)
+    assert rms_rel(got["dRRt"], ref["dRRt"]) < 1e-5
+    assert rms_rel(got["dip_momIt"], ref["dip_momIt"]) < 1e-5
+
+
 def test_mixed_headline_and_convergence(pkg, orc, engine_lib):
     """TTM3-F 512 H2O x 32 beads: force RMS error <= 1e-4 relative, and the induced dipoles
     converge to the 1e-8 threshold (deterministic FP32 field, FP64 residual)."""
