@@ -160,7 +160,7 @@ struct Engine {
     const int4 *d_tcslot = nullptr;   // per run slot: run, local k offset, kzlo, nkz
     const float2 *d_tcskv = nullptr;  // per run slot: FP32 (k_x, k_y)
     const void *d_tcgrp = nullptr;    // per run group (TcGroup): slots, columns, kz rows, k-vectors
-    const int *d_tckloc = nullptr;    // k-vector of each local index, group after group
+    const void *d_tckloc = nullptr;   // (k-vector, weight) of each local index, group after group
     const float *d_tckzv = nullptr;   // FP32 k_z component by kz + lmax
     alignas(64) unsigned char tc_map[128];  // CUtensorMap of the FP32 tables tabf
     size_t cap = 0;

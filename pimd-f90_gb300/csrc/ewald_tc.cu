@@ -1,7 +1,8 @@
 // Tensor-core (tcgen05) dipole structure factor of the mixed engine:
 //   S(k) = sum_s (k.mu_s) e^{i k.r_s}            (ewald.f90:99-108, the per-iteration ewald_std_dd sum)
-// over the dipole sites of every bead, as 3xTF32 GEMMs with FP32 accumulators in TMEM, followed
-// by the FP64 sum over site groups and the FP32 field weights (k_sreduce's job) in the same launch.
+// over the dipole sites of every bead, as GEMMs on FP16 hi + lo splits (hi.hi + hi.lo + lo.hi,
+// ~22-bit operands) with FP32 accumulators in TMEM, followed by the sum over site groups and the
+// FP32 field weights (k_sreduce's job) in the same launch.
 //
 // Formulation. For a run (kx, ky) with kz in [kzlo, kzlo + nkz) and a site s, e^{ik.r} =
 // exy(s) ez(s, kz) with exy = ex(kx) ey(ky) (ewald.f90:30-31), and
@@ -14,23 +15,25 @@
 //   Z = mu_c(s) (c_j(s) | s_j(s)),   X = Re|Im exy(s, run).
 // The M side holds 6 (max |kz| + 1) <= 128 rows, the N side two columns per run (<= 256 runs,
 // two MMAs of N <= 256 per K step). A tcgen05 MMA costs about the same for any N <= 256 on this
-// part, so the wide, run-dependent operand goes on N; each K step of 8 sites is three MMAs
-// (hi.hi + hi.lo + lo.hi of the TF32 split) per N half.
+// part (measured: ~200 cycles for M = 128 and 32 bytes of K), so the wide, run-dependent operand
+// goes on N, and kind::f16 (16 sites per 32 bytes of K) halves the MMAs per site of kind::tf32;
+// each K step of 16 sites is three MMAs per N half. Z is scaled by 2^6 (exact) so that small
+// mu_c ez values keep normal FP16 lo parts; the epilogue takes the scale out.
 //
 // A CTA owns one bead, one group of <= 256 runs and one group of consecutive sites; the site
 // groups of a (bead, run group) form a thread-block cluster. Warp roles:
 //   * producer warp: per 32-site stage, TMA (cp.async.bulk.tensor.2d, two boxes of 16 sites x all
 //     ntab table rows, 128-byte swizzle) plus a bulk copy of the 32 FP32 dipoles, completing on an
 //     mbarrier;
-//   * 14 builder warps: per 8 sites build X (exy of every run) and Z (mu_c ez) in the canonical
-//     no-swizzle K-major layout, split into TF32 hi + lo, into one of three buffers;
+//   * 14 builder warps: per 16 sites build X (exy of every run) and Z (mu_c ez) in the canonical
+//     no-swizzle K-major layout, split into FP16 hi + lo, into one of three buffers;
 //   * MMA warp: one thread issues the MMAs into TMEM and commits to the buffer's mbarrier, which
 //     releases the buffer to the builders.
 // Only mbarriers connect the roles, so building, copying and MMAs overlap. The epilogue reads
 // TMEM (tcgen05.ld) 32 runs at a time, combines each k-vector's 12 sums, and keeps the CTA's FP32
 // partial S in shared memory; after a cluster barrier each CTA adds the partials of all CTAs of
-// its cluster over a slice of the k-vectors (distributed shared memory, FP64, site groups in
-// order as k_sreduce does) and writes Sm and the FP32 weights Wf.
+// its cluster over a slice of the k-vectors (distributed shared memory, FP32, site groups in a
+// fixed order) and writes Sm and the FP32 weights Wf.
 // Every mbarrier wait is bounded (~0.13 s); after a timeout a role stops, the CTA waits (bounded)
 // for its copies and MMAs in flight, frees its TMEM, still meets its cluster barriers, and bit 8
 // of the context's error word is set.
@@ -38,6 +41,8 @@
 #include <cudaTypedefs.h>
 #include <algorithm>
 #include <vector>
+
+#include <cuda_fp16.h>
 
 #include "engine.h"
 #include "umma.cuh"
@@ -48,7 +53,8 @@ constexpr int TC_NB = 14;                 // builder warps
 constexpr int TC_MMA_WARP = TC_NB;        // MMA-issuing warp (then the producer warp)
 constexpr int TC_NT = (TC_NB + 2) * 32;   // 512 threads
 constexpr int TC_SS = 32;                 // sites per table stage
-constexpr int TC_KS = 8;                  // sites per MMA step (32 bytes of K)
+constexpr int TC_KS = 16;                 // sites per MMA step (kind::f16: 32 bytes of K)
+constexpr float TC_ZS = 64.f;             // power-of-two scale of Z (keeps small mu_c ez normal in FP16)
 constexpr int TC_NABUF_MAX = 3;           // operand buffers
 constexpr int TC_CLMAX = 8;               // site groups per cluster (portable cluster size)
 constexpr int TC_MAXRUN = 256;            // runs per group: 512 TMEM columns
@@ -60,11 +66,17 @@ struct TcGroup {
     int p0, nr, ncol, jm, nkl, kgoff, pad0, pad1;  // slots, runs, MMA columns, kz rows, k-vectors
 };
 
+// k-vector of a local index and its 4 pi Ak / V
+struct TcKW {
+    int k;
+    float w;
+};
+
 struct TcArgs {
-    const int4 *slot;     // per slot: run, local k offset, kzlo, nkz
+    const int4 *slot;     // per slot: kx + 256 (ky + 128), local k offset, kzlo, nkz
     const float2 *skv;    // per slot: FP32 (k_x, k_y)
     const TcGroup *grp;
-    const int *kloc;      // k-vector of each local index
+    const TcKW *kw;       // k-vector and weight of each local index
     const float *kzv;     // k_z by kz + lmax
     int sbase;            // first site of site group 0 (multiple of 32, <= s_lo)
     int s_lo, s_hi;       // dipole sites [s_lo, s_hi)
@@ -78,7 +90,7 @@ struct TcArgs {
 // A table stage holds two TMA boxes of 16 sites x ntab rows, each written with the 128-byte
 // swizzle (16-byte chunk c of row r lands at chunk c ^ (r & 7), so loads of the same sites from
 // different rows fall in different banks), followed by the stage's 32 dipoles. An operand
-// buffer holds Z hi, Z lo (128 rows x 8 sites each) and X hi, X lo (ncolmax rows x 8 sites).
+// buffer holds Z hi, Z lo (128 rows x 16 FP16 sites each) and X hi, X lo (ncolmax rows x 16 sites).
 struct TcSmem {
     int boxb, mu, stage, buf, xoff, bufstride, total;
     __host__ __device__ TcSmem(int ntab, int ncolmax, int nabuf) {
@@ -134,16 +146,26 @@ PIMD_D float2 ld_cluster_f2(uint32_t local_addr, uint32_t rank) {
     uint32_t ra;
     float2 v;
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(local_addr), "r"(rank));
-    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(ra) : "memory");
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(ra));
     return v;
 }
-// TF32 split by truncation: hi keeps the top 10 mantissa bits, lo = x - hi exactly
-PIMD_D void split_t(float x, float &hi, float &lo) {
-    hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
-    lo = x - hi;
+// Eight FP32 values as FP16 hi + lo (x = hi + lo to ~22 bits): two 16-byte rows of 8 halves
+PIMD_D void split8_h(const float (&x)[8], uint4 &hi, uint4 &lo) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const __half2 hh = __floats2half2_rn(x[2 * i], x[2 * i + 1]);
+        const float2 hf = __half22float2(hh);
+        const __half2 ll = __floats2half2_rn(x[2 * i] - hf.x, x[2 * i + 1] - hf.y);
+        h[i] = *reinterpret_cast<const uint32_t *>(&hh);
+        l[i] = *reinterpret_cast<const uint32_t *>(&ll);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
-// byte offset of (row n, site k) in a K-major operand of 8 sites (two core matrices along K)
-PIMD_D int opoff(int n, int k) { return umma::kmajor_off(n, k, TC_KS / 4); }
+// byte offset of the 16-byte chunk c (sites 8 c .. 8 c + 7) of row n in a K-major operand of 16
+// FP16 sites (two core matrices along K)
+PIMD_D int rowchunk(int n, int c) { return (((n >> 3) * 2 + c) << 7) + ((n & 7) << 4); }
 
 __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CUtensorMap tmap, KP kp, TcArgs a) {
     const int grp = blockIdx.x, tg = blockIdx.y, b = blockIdx.z;
@@ -186,19 +208,15 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
             umma::mbar_init(&aempty[i], 1);
         }
     }
-    // padding stays zero in every buffer: Z rows >= 6 jm, X rows (columns of D) >= 2 nr
-    for (int bi = 0; bi < nab; bi++) {
-        float *Zf = reinterpret_cast<float *>(sm + L.buf + bi * L.bufstride);
-        float *Xf = reinterpret_cast<float *>(sm + L.buf + bi * L.bufstride + L.xoff);
-        for (int i = tid; i < 2 * 128 * TC_KS; i += TC_NT) {
-            const int f = i % (128 * TC_KS);
-            const int n = ((f >> 5) >> 1) * 8 + ((f & 31) >> 2);
-            if (n >= 6 * jm) Zf[i] = 0.f;
-        }
-        for (int i = tid; i < 2 * a.ncolmax * TC_KS; i += TC_NT) {
-            const int f = i % (a.ncolmax * TC_KS);
-            const int n = ((f >> 5) >> 1) * 8 + ((f & 31) >> 2);
-            if (n >= 2 * nr) Xf[i] = 0.f;
+    {   // padding stays zero in every buffer (hi and lo): Z rows >= 6 jm, X rows >= 2 nr
+        const int zp = 128 - 6 * jm, xp = G.ncol - 2 * nr;
+        for (int i = tid; i < nab * 2 * (zp + xp) * 2; i += TC_NT) {
+            const int q = i & 1, rr = i >> 1;
+            const int row = rr % (zp + xp), hl = (rr / (zp + xp)) & 1, bi = rr / (2 * (zp + xp));
+            unsigned char *B0 = sm + L.buf + bi * L.bufstride;
+            unsigned char *dst = row < zp ? B0 + hl * 128 * 32 + rowchunk(6 * jm + row, q)
+                                          : B0 + L.xoff + hl * a.ncolmax * 32 + rowchunk(2 * nr + row - zp, q);
+            *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
     }
     umma::fence_smem_to_async();
@@ -209,27 +227,31 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     uint32_t err = 0;
 
     if (warp < TC_NB) {
-        // ---------------- builders: X = exy of every run (4 sites per item), Z = mu_c ez
+        // ---------------- builders: X = exy of every run (8 sites per item), Z = mu_c ez
         const int bt = tid;  // 0 .. 32 TC_NB - 1
-        int it_n = 0, it_off[2], it_xr[2], it_yr[2], it_h[2];
+        int it_n = 0, it_off[2], it_xr[2], it_yr[2], it_o[2];
         float it_ys[2];
 #pragma unroll
         for (int u = 0; u < 2; u++) {
             const int it = bt + u * 32 * TC_NB;
-            it_off[u] = it_xr[u] = it_yr[u] = it_h[u] = 0;
+            it_off[u] = it_xr[u] = it_yr[u] = it_o[u] = 0;
             it_ys[u] = 1.f;
             if (it >= 2 * nr) continue;
             it_n = u + 1;
-            const int p = it >> 1, h = it & 1;
-            const KRun run = kp.runs[sslot[p].x];
-            it_off[u] = opoff(2 * p, 4 * h);  // Re row; the Im row 2 p + 1 is 16 bytes further
-            it_h[u] = h;
-            it_xr[u] = run.kx;
-            it_yr[u] = yrow + (run.ky < 0 ? -run.ky : run.ky);
-            it_ys[u] = run.ky < 0 ? -1.f : 1.f;
+            const int p = it >> 1, o = it & 1;
+            const int kxy = sslot[p].x, kx = kxy & 255, ky = (kxy >> 8) - 128;
+            it_off[u] = rowchunk(2 * p, o);  // Re row; the Im row 2 p + 1 is 16 bytes further
+            it_o[u] = o;
+            it_xr[u] = kx;
+            it_yr[u] = yrow + (ky < 0 ? -ky : ky);
+            it_ys[u] = ky < 0 ? -1.f : 1.f;
         }
-        const bool zit = bt < jm * TC_KS;
-        const int zj = bt >> 3, zk = bt & 7;
+        // Z items: one row (c, j, cos|sin) x 8 sites, on the threads from the last one down
+        const int zi = 32 * TC_NB - 1 - bt;
+        const bool zit = zi < 6 * jm * 2;
+        const int zrow_ = zi >> 1, zo = zi & 1;
+        const int zc = zrow_ / (2 * jm), zj = (zrow_ >> 1) % jm, zcs = zrow_ & 1;
+        const int zoff = rowchunk(zrow_, zo);
         for (int ts = 0; ts < nstage && !err; ts++) {
             const int tb = ts & 1;
             err |= (uint32_t)umma::mbar_wait(&tfull[tb], (uint32_t)((ts >> 1) & 1), TC_WAIT);
@@ -244,56 +266,47 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
 #pragma unroll
                 for (int u = 0; u < 2; u++) {
                     if (u >= it_n) break;
-                    const int sq = so + 4 * it_h[u];
-                    const float4 x01 = *tab_chunk(tab, L.boxb, it_xr[u], sq);
-                    const float4 x23 = *tab_chunk(tab, L.boxb, it_xr[u], sq + 2);
-                    const float4 y01 = *tab_chunk(tab, L.boxb, it_yr[u], sq);
-                    const float4 y23 = *tab_chunk(tab, L.boxb, it_yr[u], sq + 2);
+                    const int sq = so + 8 * it_o[u];
                     const float ys = it_ys[u];
-                    const float ex[4][2] = {{x01.x, x01.y}, {x01.z, x01.w}, {x23.x, x23.y}, {x23.z, x23.w}};
-                    const float ey[4][2] = {{y01.x, ys * y01.y}, {y01.z, ys * y01.w}, {y23.x, ys * y23.y}, {y23.z, ys * y23.w}};
-                    float re[4], im[4];
+                    float re[8], im[8];
 #pragma unroll
-                    for (int i = 0; i < 4; i++) {
+                    for (int h = 0; h < 4; h++) {
+                        const float4 xx = *tab_chunk(tab, L.boxb, it_xr[u], sq + 2 * h);
+                        const float4 yy = *tab_chunk(tab, L.boxb, it_yr[u], sq + 2 * h);
                         // ewald.f90:30-31: coskxky = cx cy - sx sy, sinkxky = sx cy + cx sy
-                        re[i] = ex[i][0] * ey[i][0] - ex[i][1] * ey[i][1];
-                        im[i] = ex[i][1] * ey[i][0] + ex[i][0] * ey[i][1];
+                        re[2 * h] = xx.x * yy.x - xx.y * (ys * yy.y);
+                        im[2 * h] = xx.y * yy.x + xx.x * (ys * yy.y);
+                        re[2 * h + 1] = xx.z * yy.z - xx.w * (ys * yy.w);
+                        im[2 * h + 1] = xx.w * yy.z + xx.z * (ys * yy.w);
                     }
-                    float4 rh, rl, ih, il;
-                    split_t(re[0], rh.x, rl.x);
-                    split_t(re[1], rh.y, rl.y);
-                    split_t(re[2], rh.z, rl.z);
-                    split_t(re[3], rh.w, rl.w);
-                    split_t(im[0], ih.x, il.x);
-                    split_t(im[1], ih.y, il.y);
-                    split_t(im[2], ih.z, il.z);
-                    split_t(im[3], ih.w, il.w);
+                    uint4 rh, rl, ih, il;
+                    split8_h(re, rh, rl);
+                    split8_h(im, ih, il);
                     unsigned char *xp = Bf + L.xoff + it_off[u];
-                    *reinterpret_cast<float4 *>(xp) = rh;
-                    *reinterpret_cast<float4 *>(xp + 16) = ih;
-                    *reinterpret_cast<float4 *>(xp + xlo) = rl;
-                    *reinterpret_cast<float4 *>(xp + xlo + 16) = il;
+                    *reinterpret_cast<uint4 *>(xp) = rh;
+                    *reinterpret_cast<uint4 *>(xp + 16) = ih;
+                    *reinterpret_cast<uint4 *>(xp + xlo) = rl;
+                    *reinterpret_cast<uint4 *>(xp + xlo + 16) = il;
                 }
                 if (zit) {
-                    const int s = sfirst + so + zk;
-                    float4 m = mus[so + zk];
-                    if (s < a.s_lo || s >= g1) m = make_float4(0.f, 0.f, 0.f, 0.f);
-                    const float2 z = tab_elem(tab, L.boxb, zrow + zj, so + zk);
-                    const float mc[3] = {m.x, m.y, m.z};
-                    float *Zh = reinterpret_cast<float *>(Bf);
-                    float *Zl = reinterpret_cast<float *>(Bf + 128 * 32);
+                    const int sq = so + 8 * zo;
+                    float v[8];
 #pragma unroll
-                    for (int c = 0; c < 3; c++) {
-                        const int row = (c * jm + zj) * 2;
-                        const int o0 = opoff(row, zk) >> 2, o1 = opoff(row + 1, zk) >> 2;
-                        float hi, lo;
-                        split_t(mc[c] * z.x, hi, lo);
-                        Zh[o0] = hi;
-                        Zl[o0] = lo;
-                        split_t(mc[c] * z.y, hi, lo);
-                        Zh[o1] = hi;
-                        Zl[o1] = lo;
+                    for (int h = 0; h < 4; h++) {
+                        const float4 zz = *tab_chunk(tab, L.boxb, zrow + zj, sq + 2 * h);
+#pragma unroll
+                        for (int e = 0; e < 2; e++) {
+                            const int i = 2 * h + e, s = sfirst + sq + i;
+                            const float4 m = mus[sq + i];
+                            const float mc = zc == 0 ? m.x : (zc == 1 ? m.y : m.z);
+                            const float zv = e == 0 ? (zcs ? zz.y : zz.x) : (zcs ? zz.w : zz.z);
+                            v[i] = (s < a.s_lo || s >= g1) ? 0.f : TC_ZS * mc * zv;
+                        }
                     }
+                    uint4 hi, lo;
+                    split8_h(v, hi, lo);
+                    *reinterpret_cast<uint4 *>(Bf + zoff) = hi;
+                    *reinterpret_cast<uint4 *>(Bf + 128 * 32 + zoff) = lo;
                 }
                 umma::fence_smem_to_async();
                 __syncwarp();
@@ -305,7 +318,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     } else if (warp == TC_MMA_WARP) {
         // ---------------- MMA issue (one thread): D[128][ncol] += Z X^T, two N halves
         if (lane == 0) {
-            const uint32_t idesc_base = umma::idesc_tf32(128, 16) & ~(0x3Fu << 17);
+            const uint32_t idesc_base = umma::idesc_f16(128, 16) & ~(0x3Fu << 17);
             for (int sub = 0; sub < nsub && !err; sub++) {
                 const int ab = sub % nab, use = sub / nab;
                 err |= (uint32_t)umma::mbar_wait(&afull[ab], (uint32_t)(use & 1), TC_WAIT);
@@ -320,9 +333,9 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
                     const uint32_t d = tm + (uint32_t)(nt * 256);
                     // rows 256 nt.. of X: 32 row groups of 256 bytes per half
                     const uint64_t dx_h = umma::sdesc(xH + nt * 8192, 128, 256), dx_l = umma::sdesc(xL + nt * 8192, 128, 256);
-                    umma::mma_tf32(d, dz_h, dx_h, id, sub > 0);
-                    umma::mma_tf32(d, dz_h, dx_l, id, 1);
-                    umma::mma_tf32(d, dz_l, dx_h, id, 1);
+                    umma::mma_f16(d, dz_h, dx_h, id, sub > 0);
+                    umma::mma_f16(d, dz_h, dx_l, id, 1);
+                    umma::mma_f16(d, dz_l, dx_h, id, 1);
                 }
                 umma::commit(&aempty[ab]);
             }
@@ -365,6 +378,16 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     umma::fence_after_sync();
     const bool bad = __syncthreads_or((int)err) != 0;
 
+    // this CTA's slice of the cluster reduction; its (k, w) pairs are fetched now, under the epilogue
+    const int cr = (int)cluster_rank(), cn = gridDim.x;
+    const int i0 = (int)((long)cr * G.nkl / cn), i1 = (int)((long)(cr + 1) * G.nkl / cn);
+    constexpr int TC_PF = 4;
+    TcKW pf[TC_PF];
+#pragma unroll
+    for (int u = 0; u < TC_PF; u++) {
+        const int i = i0 + tid + u * TC_NT;
+        pf[u] = i < i1 ? a.kw[G.kgoff + i] : TcKW{0, 0.f};
+    }
     // epilogue: TMEM -> shared, 32 runs (64 columns) at a time -> partial S of every k of the group
     float *stg = reinterpret_cast<float *>(sm);                       // [128][TC_LD]
     float2 *pt = reinterpret_cast<float2 *>(sm + 128 * TC_LD * 4);    // [nkl]
@@ -404,14 +427,15 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
                 gp[c] = make_float2(dc.x - ds.y, ds.x + dc.y);
                 gm[c] = make_float2(dc.x + ds.y, dc.y - ds.x);
             }
-            const float2 kv = sskv[p];
+            const float2 kv = make_float2(sskv[p].x * (1.f / TC_ZS), sskv[p].y * (1.f / TC_ZS));
+            const float kzs = 1.f / TC_ZS;
             if (plus) {
-                const float kz = skz[kp.lmax + j];
+                const float kz = skz[kp.lmax + j] * kzs;
                 pt[sl.y + j - sl.z] = make_float2(fmaf(kz, gp[2].x, fmaf(kv.y, gp[1].x, kv.x * gp[0].x)),
                                                   fmaf(kz, gp[2].y, fmaf(kv.y, gp[1].y, kv.x * gp[0].y)));
             }
             if (minus) {
-                const float kz = skz[kp.lmax - j];
+                const float kz = skz[kp.lmax - j] * kzs;
                 pt[sl.y - j - sl.z] = make_float2(fmaf(kz, gm[2].x, fmaf(kv.y, gm[1].x, kv.x * gm[0].x)),
                                                   fmaf(kz, gm[2].y, fmaf(kv.y, gm[1].y, kv.x * gm[0].y)));
             }
@@ -426,24 +450,33 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
         umma::tmem_relinquish();
     }
     // cluster: add the partials of all site groups over this CTA's slice of the k-vectors
-    // (FP64, groups in order, as k_sreduce<OP_MU>), then Sm = (-Im, Re) and the FP32 weights
+    // (groups in order), then Sm = (-Im, Re) and the FP32 weights 4 pi Ak / V conj(S)
     cluster_sync();
     if (!bad) {
-        const int cr = (int)cluster_rank(), cn = gridDim.x;
-        const int i0 = (int)((long)cr * G.nkl / cn), i1 = (int)((long)(cr + 1) * G.nkl / cn);
         const uint32_t pbase = umma::smem_u32(pt);
-        for (int i = i0 + tid; i < i1; i += TC_NT) {
-            double sx = 0.0, sy = 0.0;
-            for (int c = 0; c < cn; c++) {
-                const float2 v = ld_cluster_f2(pbase + 8u * (uint32_t)i, (uint32_t)c);
-                sx += (double)v.x;
-                sy += (double)v.y;
-            }
-            const int k = a.kloc[G.kgoff + i];
-            kp.Sm[(size_t)b * kp.nk + k] = make_double2(-sy, sx);
-            const double w = kp.kinfo[k].w;
-            kp.Wf[((size_t)b * 2 + 1) * kp.nk + k] = make_float2((float)(w * -sy), (float)(-w * sx));
+        auto reduce_one = [&](int i, const TcKW &kw) {
+            float2 v[TC_CLMAX];
+#pragma unroll
+            for (int c = 0; c < TC_CLMAX; c++)
+                if (c < cn) v[c] = ld_cluster_f2(pbase + 8u * (uint32_t)i, (uint32_t)c);
+            // FP32 in a fixed order: FP64 arithmetic is slow on this part, and the partials carry
+            // only the split operands' ~2^-21 anyway
+            float sx = 0.f, sy = 0.f;
+#pragma unroll
+            for (int c = 0; c < TC_CLMAX; c++)
+                if (c < cn) {
+                    sx += v[c].x;
+                    sy += v[c].y;
+                }
+            kp.Sm[(size_t)b * kp.nk + kw.k] = make_double2(-(double)sy, (double)sx);
+            kp.Wf[((size_t)b * 2 + 1) * kp.nk + kw.k] = make_float2(-kw.w * sy, -kw.w * sx);
+        };
+#pragma unroll
+        for (int u = 0; u < TC_PF; u++) {
+            const int i = i0 + tid + u * TC_NT;
+            if (i < i1) reduce_one(i, pf[u]);
         }
+        for (int i = i0 + tid + TC_PF * TC_NT; i < i1; i += TC_NT) reduce_one(i, a.kw[G.kgoff + i]);
     }
     cluster_sync();  // remote reads done before any CTA of the cluster leaves
     if (bad && tid == 0) atomicOr(kp.err, 8u);
@@ -502,7 +535,7 @@ void tc_init(Engine &E) {
     std::vector<int4> slots(kp.nrun);
     std::vector<float2> skv(kp.nrun);
     std::vector<TcGroup> groups;
-    std::vector<int> kloc;
+    std::vector<TcKW> kloc;
     std::vector<float2> runkf(kp.nrun);
     for (int r = 0; r < kp.nrun; r++)
         runkf[r] = make_float2((float)E.h_kvec[3 * E.h_runs[r].kbeg], (float)E.h_kvec[3 * E.h_runs[r].kbeg + 1]);
@@ -514,9 +547,9 @@ void tc_init(Engine &E) {
         for (int p = p0; p < p0 + g.nr; p++) {
             const int r = order[p];
             const KRun &run = E.h_runs[r];
-            slots[p] = make_int4(r, g.nkl, run.kzlo, run.nkz);
+            slots[p] = make_int4(run.kx + 256 * (run.ky + 128), g.nkl, run.kzlo, run.nkz);
             skv[p] = runkf[r];
-            for (int j = 0; j < run.nkz; j++) kloc.push_back(run.kbeg + j);
+            for (int j = 0; j < run.nkz; j++) kloc.push_back(TcKW{run.kbeg + j, (float)(FOURPI * E.h_Ak[run.kbeg + j] / kp.volume)});
             g.nkl += run.nkz;
         }
         groups.push_back(g);
@@ -547,12 +580,12 @@ void tc_init(Engine &E) {
     int4 *d_slots = nullptr;
     float2 *d_skv = nullptr;
     TcGroup *d_groups = nullptr;
-    int *d_kloc = nullptr;
+    TcKW *d_kloc = nullptr;
     float *d_kzv = nullptr;
     if (cudaMalloc((void **)&d_slots, sizeof(int4) * slots.size()) != cudaSuccess ||
         cudaMalloc((void **)&d_skv, sizeof(float2) * skv.size()) != cudaSuccess ||
         cudaMalloc((void **)&d_groups, sizeof(TcGroup) * groups.size()) != cudaSuccess ||
-        cudaMalloc((void **)&d_kloc, sizeof(int) * kloc.size()) != cudaSuccess ||
+        cudaMalloc((void **)&d_kloc, sizeof(TcKW) * kloc.size()) != cudaSuccess ||
         cudaMalloc((void **)&d_kzv, sizeof(float) * kzv.size()) != cudaSuccess) {
         cudaGetLastError();
         for (void *p : {(void *)d_slots, (void *)d_skv, (void *)d_groups, (void *)d_kloc, (void *)d_kzv})
@@ -563,7 +596,7 @@ void tc_init(Engine &E) {
     cudaMemcpy(d_slots, slots.data(), sizeof(int4) * slots.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(d_skv, skv.data(), sizeof(float2) * skv.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(d_groups, groups.data(), sizeof(TcGroup) * groups.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(d_kloc, kloc.data(), sizeof(int) * kloc.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(d_kloc, kloc.data(), sizeof(TcKW) * kloc.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(d_kzv, kzv.data(), sizeof(float) * kzv.size(), cudaMemcpyHostToDevice);
     // tables [P][ntab][S] float2 as a 2-D FP32 tensor (x = 2 S values, y = P ntab rows); a box
     // is 16 sites (128 bytes) x ntab rows, written to shared memory with the 128-byte swizzle
@@ -594,7 +627,7 @@ int launch_sfac_tc(Engine &E, int s0, int nsites, int skipconv) {
     a.slot = E.d_tcslot;
     a.skv = E.d_tcskv;
     a.grp = reinterpret_cast<const TcGroup *>(E.d_tcgrp);
-    a.kloc = E.d_tckloc;
+    a.kw = reinterpret_cast<const TcKW *>(E.d_tckloc);
     a.kzv = E.d_tckzv;
     a.sbase = s0 & ~(TC_SS - 1);  // TMA x coordinate 2 sbase: 256-byte aligned
     a.s_lo = s0;
