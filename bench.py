@@ -435,6 +435,7 @@ def main():
                     l2="256 MB buffer written between timed steps", parallelism="replicas" if world > 1 else "1 GPU",
                     execution="one CUDA graph per MD step (dipole loop as a conditional while node)",
                     tensor_core_structure_factor=bool(res["tuning"]["sf_tc"]),
+                    tensor_core_field_pass=bool(res["tuning"]["ff_tc"]),
                     dipole_iterations_mean=float(np.mean(res["niters"])),
                     fp64_dipole_iterations_mean=float(np.mean(res64["niters"]))),
         fp64=dict(value=fp64_value, steps=steps64, ms_per_step=res64["dev_ms"] / steps64,

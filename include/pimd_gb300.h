@@ -219,7 +219,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc);
 /* The chosen shapes: [tiled structure factors, site groups (0 = sized from the SM count),
  * register-row field kernels, max k-slices, one-launch neighbour lists] and, when n >= 6,
  * [wave-quantised split counts], when n >= 7 [tensor-core (tcgen05) dipole structure factor
- * in use]; n >= 5. */
+ * in use], when n >= 8 [tensor-core dipole field pass in use]; n >= 5. */
 int pimd_get_tuning(pimd_ctx *ctx, int *knobs, int n);
 
 /* ---------------------------------------------------------------------------------------

@@ -882,11 +882,12 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         std::vector<int> cand;
     };
     int sf_tiled = E.sf_tiled, ff_regs = E.ff_regs, nbr_block = E.nbr_block, wave = E.wave_shapes;
-    int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc;
+    int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc, ff_tc = E.ff_tc;
     std::vector<Knob> knobs;
     const bool mixed = E.precision == PIMD_MIXED && E.kp.model < 4;
     if (mixed) {
         if (E.tc_ready) knobs.push_back({&sf_tc, {1, 0}});
+        if (E.tf_ready) knobs.push_back({&ff_tc, {1, 0}});
         knobs.push_back({&sf_tiled, {1, 0}});
         knobs.push_back({&E.sf_groups, {0, 4, 8, 16, 32}});
         knobs.push_back({&ff_regs, {1, 0}});
@@ -902,6 +903,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         E.wave_shapes = wave != 0;
         E.nbr_cells = nbr_cells != 0;
         E.sf_tc = sf_tc != 0;
+        E.ff_tc = ff_tc != 0;
     };
     int rc = PIMD_OK;
     float best;
@@ -942,6 +944,7 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     k[4] = E.nbr_block;
     if (n >= 6) k[5] = E.wave_shapes;
     if (n >= 7) k[6] = E.sf_tc && E.tc_ready;
+    if (n >= 8) k[7] = E.ff_tc && E.tf_ready;
     return PIMD_OK;
 }
 

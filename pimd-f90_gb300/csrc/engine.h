@@ -162,6 +162,10 @@ struct Engine {
     const void *d_tcgrp = nullptr;    // per run group (TcGroup): slots, columns, kz rows, k-vectors
     const void *d_tckloc = nullptr;   // (k-vector, weight) of each local index, group after group
     const float *d_tckzv = nullptr;   // FP32 k_z component by kz + lmax
+    bool ff_tc = true;                // tensor-core dipole field pass (k_field_tc) when tf_ready
+    bool tf_ready = false;
+    int tf_nr = 0, tf_jm = 0, tf_ncol = 0, tf_kq = 0;
+    const int2 *d_tfkpm = nullptr;    // per (run slot, j): k-vectors of kz = +j, -j
     alignas(64) unsigned char tc_map[128];  // CUtensorMap of the FP32 tables tabf
     size_t cap = 0;
     std::vector<KRun> h_runs;
@@ -274,6 +278,8 @@ void launch_ewald_pw(Engine &E);
 // writes Sm and the dipole weights Wf and returns 1, or returns 0 (not applicable)
 void tc_init(Engine &E);
 int launch_sfac_tc(Engine &E, int s0, int nsites, int skipconv);
+// tensor-core dipole field (ewald_tc.cu): k-slice 0 of Fpart at [s0, s1); 1 when launched
+int launch_field_tc(Engine &E, int s0, int s1);
 // launchers (spc.cu): q-SPC/Fw and SPC/F
 void launch_sites_spc(Engine &E);
 void launch_pair_spc(Engine &E);

@@ -1029,6 +1029,13 @@ static void launch_field_f(Engine &E, int s0, int s1) {
 template <int MODE>
 static void run_field(Engine &E, int s0, int s1) {
     const int LZ = 2 * E.kp.lmax + 1;
+    if (MODE == F_D && E.precision == PIMD_PREC_MIXED && launch_field_tc(E, s0, s1)) {
+        // tensor-core field pass (ewald_tc.cu): one k-slice, then the FP64 SOR update and test
+        dim3 g2((s1 - s0 + 127) / 128, E.kp.P);
+        k_field_finish<MODE, 128><<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, 1);
+        ++E.nlaunch;
+        return;
+    }
     if (E.precision == PIMD_PREC_MIXED && E.ff_regs && LZ <= 49) {
         if (LZ <= 17)
             launch_field_f<MODE, 17>(E, s0, s1);

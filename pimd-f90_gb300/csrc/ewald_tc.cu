@@ -483,6 +483,234 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
 }
 
 // ---------------------------------------------------------------------------------------
+// Tensor-core dipole field of the mixed engine (the per-iteration k_field_f<F_D> sum,
+// ewald.f90:114-117): at every dipole site s of a bead,
+//   E_x,y(s) = sum_run k_x,y Im(exy(s) T0(s)),   E_z(s) = sum_run Im(exy(s) T1(s)),
+//   T0(s) = sum_kz W(kz) ez(s, kz),   T1(s) = sum_kz k_z W(kz) ez(s, kz),
+// with W the FP32 weights 4 pi Ak / V conj(S) of the run's k-vectors. Folding +-j as in the
+// structure factor (W+ = W(+j), W- = W(-j), Wp = W+ + W-, Wm = W+ - W-):
+//   T0 = sum_j (Wp.x c_j - Wm.y s_j) + i (Wp.y c_j + Wm.x s_j)
+//   T1 = sum_j k_z(j) [(Wm.x c_j - Wp.y s_j) + i (Wm.y c_j + Wp.x s_j)]
+// so T0, T1 of every run at every site are one GEMM per bead,
+//   D[s][(run, T0re|T0im|T1re|T1im)] = sum_q Q[s][q] V[(run, comp)][q],  q = (j, cos|sin),
+// with the sites on M (128 per CTA), 4 columns per run on N and only 2 (max |kz| + 1) terms on
+// K (FP16 hi + lo split, three MMAs per 16-term K step). The epilogue contracts each TMEM row
+// with exy(s, run) from the TMA-staged tables, 16 warps = 4 lane quarters x 4 run quarters, and
+// writes the field at the CTA's sites as k-slice 0 of Fpart for k_field_finish<F_D>. V is built
+// by every CTA of a bead from Wf (scaled by 2^10, exact, to keep small weights normal in FP16).
+constexpr int TF_NT = 512;
+constexpr int TF_SITES = 128;             // sites per CTA (M)
+constexpr float TF_WS = 1024.f;           // power-of-two scale of V
+
+struct TfArgs {
+    const int4 *slot;     // per run slot: packed kx/ky, local k offset, kzlo, nkz
+    const float2 *skv;    // per run slot: FP32 (k_x, k_y)
+    const int2 *kpm;      // per (slot, j): k-vector of kz = +j and of kz = -j (-1: none)
+    const float *kzv;     // k_z by kz + lmax
+    int nr, ncol, kq, jm; // runs, V rows (4 nr rounded to 16), K terms (multiple of 16), kz rows
+    int sbase, s_lo, s_hi;
+};
+
+struct TfSmem {
+    int boxb, A, B, total;
+    __host__ __device__ TfSmem(int ntab, int ncol, int kq) {
+        boxb = ((ntab * 128 + 1023) / 1024) * 1024;
+        A = 8 * boxb;                      // tables of 128 sites: 8 TMA boxes of 16 sites
+        B = A + 2 * TF_SITES * kq * 2;     // Q hi, lo: 128 rows x kq halves
+        total = B + 2 * ncol * kq * 2 + 1024;  // V hi, lo: ncol rows x kq halves
+    }
+};
+
+// byte offset of half q of row n in a K-major operand of kq halves (kq / 8 core matrices along K)
+PIMD_D int hoff(int n, int q, int kcm) { return (((n >> 3) * kcm + (q >> 3)) << 7) + ((n & 7) << 4) + ((q & 7) << 1); }
+PIMD_D uint32_t pack_h2(float a, float b, float &ra, float &rb) {
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 f = __half22float2(h);
+    ra = a - f.x;
+    rb = b - f.y;
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+// (a, b) -> hi, lo half pairs
+PIMD_D void split2_h(float a, float b, uint32_t &hi, uint32_t &lo) {
+    float ra, rb;
+    hi = pack_h2(a, b, ra, rb);
+    const __half2 l = __floats2half2_rn(ra, rb);
+    lo = *reinterpret_cast<const uint32_t *>(&l);
+}
+
+__global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ CUtensorMap tmap, KP kp, TfArgs a) {
+    const int t = blockIdx.x, b = blockIdx.y;
+    if (kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;  // converged bead, as k_field_f<F_D>
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const TfSmem L(kp.ntab, a.ncol, a.kq);
+    extern __shared__ __align__(1024) unsigned char sm_raw[];
+    unsigned char *sm = sm_raw + ((1024u - (umma::smem_u32(sm_raw) & 1023u)) & 1023u);
+    __shared__ uint64_t tbar, mbar;
+    __shared__ uint32_t tslot;
+    __shared__ int4 sslot[TC_MAXRUN];
+    __shared__ float2 sskv[TC_MAXRUN];
+    const int sb = a.sbase + t * TF_SITES;
+    const int kcm = a.kq / 8, nr = a.nr, jm = a.jm;
+    const int yrow = kp.hmax + 1, zrow = yrow + kp.kmax + 1;
+    if (tid < nr) {
+        sslot[tid] = a.slot[tid];
+        sskv[tid] = make_float2(a.skv[tid].x * (1.f / TF_WS), a.skv[tid].y * (1.f / TF_WS));
+    }
+    if (warp == 0) umma::tmem_alloc(&tslot, 512);
+    if (tid == 0) {
+        umma::mbar_init(&tbar, 1);
+        umma::mbar_init(&mbar, 1);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tm = tslot;
+    if (tid == 0) {
+        const uint32_t box_tx = (uint32_t)(kp.ntab * 128);
+        mbar_expect_tx(&tbar, 8 * box_tx);
+        for (int i = 0; i < 8; i++) tma_load_2d(sm + i * L.boxb, &tmap, 2 * (sb + 16 * i), b * kp.ntab, &tbar);
+    }
+    // V = the run weights (while the tables land): rows 4 p + comp, halves (2 j, 2 j + 1)
+    unsigned char *Vh = sm + L.B, *Vl = Vh + a.ncol * a.kq * 2;
+    const float2 *W = kp.Wf + ((size_t)b * 2 + 1) * kp.nk;
+    for (int it = tid; it < nr * jm; it += TF_NT) {
+        const int p = it / jm, j = it - p * jm;
+        const int2 km = a.kpm[it];
+        const float2 wpl = km.x >= 0 ? W[km.x] : make_float2(0.f, 0.f);
+        const float2 wmi = km.y >= 0 ? W[km.y] : make_float2(0.f, 0.f);
+        const float2 wp = make_float2(TF_WS * (wpl.x + wmi.x), TF_WS * (wpl.y + wmi.y));
+        const float2 wm = make_float2(TF_WS * (wpl.x - wmi.x), TF_WS * (wpl.y - wmi.y));
+        const float kz = a.kzv[kp.lmax + j];
+        // (cos, sin) coefficients of T0re, T0im, T1re, T1im
+        const float cv[4][2] = {{wp.x, -wm.y}, {wp.y, wm.x}, {kz * wm.x, -kz * wp.y}, {kz * wm.y, kz * wp.x}};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            uint32_t hi, lo;
+            split2_h(cv[c][0], cv[c][1], hi, lo);
+            const int o = hoff(4 * p + c, 2 * j, kcm);
+            *reinterpret_cast<uint32_t *>(Vh + o) = hi;
+            *reinterpret_cast<uint32_t *>(Vl + o) = lo;
+        }
+    }
+    // zero padding: V rows >= 4 nr, V and Q halves >= 2 jm
+    for (int it = tid; it < (a.ncol - 4 * nr) * (a.kq / 2); it += TF_NT) {
+        const int n = 4 * nr + it / (a.kq / 2), q = 2 * (it % (a.kq / 2));
+        *reinterpret_cast<uint32_t *>(Vh + hoff(n, q, kcm)) = 0u;
+        *reinterpret_cast<uint32_t *>(Vl + hoff(n, q, kcm)) = 0u;
+    }
+    const int kpad = (a.kq - 2 * jm) / 2;
+    for (int it = tid; it < 4 * nr * kpad; it += TF_NT) {
+        const int n = it / kpad, q = 2 * jm + 2 * (it % kpad);
+        *reinterpret_cast<uint32_t *>(Vh + hoff(n, q, kcm)) = 0u;
+        *reinterpret_cast<uint32_t *>(Vl + hoff(n, q, kcm)) = 0u;
+    }
+    unsigned char *Qh = sm + L.A, *Ql = Qh + TF_SITES * a.kq * 2;
+    for (int it = tid; it < TF_SITES * kpad; it += TF_NT) {
+        const int n = it / kpad, q = 2 * jm + 2 * (it % kpad);
+        *reinterpret_cast<uint32_t *>(Qh + hoff(n, q, kcm)) = 0u;
+        *reinterpret_cast<uint32_t *>(Ql + hoff(n, q, kcm)) = 0u;
+    }
+    uint32_t err = (uint32_t)umma::mbar_wait(&tbar, 0, TC_WAIT);
+    // Q = ez rows of the CTA's sites: halves (2 j, 2 j + 1) = (c_j, s_j)
+    for (int it = tid; it < TF_SITES * jm; it += TF_NT) {
+        const int s = it % TF_SITES, j = it / TF_SITES;
+        const float2 z = tab_elem(sm, L.boxb, zrow + j, s);
+        uint32_t hi, lo;
+        split2_h(z.x, z.y, hi, lo);
+        const int o = hoff(s, 2 * j, kcm);
+        *reinterpret_cast<uint32_t *>(Qh + o) = hi;
+        *reinterpret_cast<uint32_t *>(Ql + o) = lo;
+    }
+    umma::fence_smem_to_async();
+    umma::fence_before_sync();
+    const bool bad0 = __syncthreads_or((int)err) != 0;
+    umma::fence_after_sync();
+    // two passes of <= 512 TMEM columns (N tiles of 256 V rows = 64 runs)
+    const int ntile = (a.ncol + 255) / 256;
+    float Ex = 0.f, Ey = 0.f, Ez = 0.f;
+    const int lq = warp & 3, part = warp >> 2, sl = 32 * lq + lane;
+    bool bad = bad0;
+    for (int pass = 0; pass * 2 < ntile && !bad; pass++) {
+        if (tid == 0) {
+            const uint32_t idesc_base = umma::idesc_f16(128, 16) & ~(0x3Fu << 17);
+            const uint32_t qh = umma::smem_u32(Qh), ql = umma::smem_u32(Ql);
+            const uint32_t vh = umma::smem_u32(Vh), vl = umma::smem_u32(Vl);
+            for (int nt = 2 * pass; nt < min(ntile, 2 * pass + 2); nt++) {
+                const int N = min(256, a.ncol - 256 * nt);
+                const uint32_t id = idesc_base | ((uint32_t)(N >> 3) << 17);
+                const uint32_t d = tm + (uint32_t)(256 * (nt - 2 * pass));
+                const uint32_t vo = (uint32_t)(nt * 32 * kcm * 128);  // 256 rows = 32 row groups
+                for (int ks = 0; ks < a.kq / 16; ks++) {
+                    const uint64_t dq_h = umma::sdesc(qh + ks * 256, 128, kcm * 128), dq_l = umma::sdesc(ql + ks * 256, 128, kcm * 128);
+                    const uint64_t dv_h = umma::sdesc(vh + vo + ks * 256, 128, kcm * 128), dv_l = umma::sdesc(vl + vo + ks * 256, 128, kcm * 128);
+                    umma::mma_f16(d, dq_h, dv_h, id, ks > 0);
+                    umma::mma_f16(d, dq_h, dv_l, id, 1);
+                    umma::mma_f16(d, dq_l, dv_h, id, 1);
+                }
+            }
+            umma::commit(&mbar);
+        }
+        __syncwarp();
+        int to = umma::mbar_wait(&mbar, (uint32_t)(pass & 1), TC_WAIT);
+        if (to) to = umma::mbar_wait(&mbar, (uint32_t)(pass & 1), TC_WAIT);
+        umma::fence_after_sync();
+        bad = __syncthreads_or(to) != 0;
+        if (bad) break;
+        // runs of this pass: 128 (4 run quarters of 32), two per 8-column TMEM load
+        const int r0 = 128 * pass;
+        for (int pp = 0; pp < 32; pp += 2) {
+            const int p = r0 + 32 * part + pp;
+            if (p >= nr) break;
+            float v[8];
+            umma::tmem_ld8(tm + ((uint32_t)(32 * lq) << 16) + (uint32_t)(4 * (p - r0)), v);
+#pragma unroll
+            for (int e = 0; e < 2; e++) {
+                if (p + e >= nr) break;
+                const int kxy = sslot[p + e].x, kx = kxy & 255, ky = (kxy >> 8) - 128;
+                const float2 ex = tab_elem(sm, L.boxb, kx, sl);
+                float2 ey = tab_elem(sm, L.boxb, yrow + (ky < 0 ? -ky : ky), sl);
+                if (ky < 0) ey.y = -ey.y;
+                // ewald.f90:30-31: coskxky = cx cy - sx sy, sinkxky = sx cy + cx sy
+                const float er = ex.x * ey.x - ex.y * ey.y, ei = ex.y * ey.x + ex.x * ey.y;
+                const float t0 = fmaf(er, v[4 * e + 1], ei * v[4 * e + 0]);  // Im(exy T0)
+                const float t1 = fmaf(er, v[4 * e + 3], ei * v[4 * e + 2]);  // Im(exy T1)
+                const float2 kv = sskv[p + e];
+                Ex = fmaf(kv.x, t0, Ex);
+                Ey = fmaf(kv.y, t0, Ey);
+                Ez = fmaf(1.f / TF_WS, t1, Ez);
+            }
+        }
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+    }
+    // the four run quarters of each site, in order; k-slice 0 of Fpart
+    float *red = reinterpret_cast<float *>(Qh);  // [4][128][3]
+    red[(part * TF_SITES + sl) * 3 + 0] = Ex;
+    red[(part * TF_SITES + sl) * 3 + 1] = Ey;
+    red[(part * TF_SITES + sl) * 3 + 2] = Ez;
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        umma::fence_after_sync();
+        umma::tmem_dealloc(tm, 512);
+        umma::tmem_relinquish();
+    }
+    if (tid < TF_SITES && !bad) {
+        const int s = sb + tid;
+        if (s >= a.s_lo && s < a.s_hi) {
+            float e[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int q4 = 0; q4 < 4; q4++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) e[c] += red[(q4 * TF_SITES + tid) * 3 + c];
+            kp.Fpart[(size_t)b * (a.s_hi - a.s_lo) + (s - a.s_lo)] = make_double4_32a(e[0], e[1], e[2], 0.0);
+        }
+    }
+    if (bad && tid == 0) atomicOr(kp.err, 8u);
+}
+
+// ---------------------------------------------------------------------------------------
 // host side
 
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -617,6 +845,63 @@ void tc_init(Engine &E) {
     E.tc_ncolmax = ncolmax;
     E.tc_nabuf = nabuf;
     E.tc_ready = true;
+    // field kernel: one run group; per (slot, j) the k-vectors of kz = +j and -j
+    E.tf_ready = false;
+    if (groups.size() != 1) return;
+    const int nr = groups[0].nr, jm = groups[0].jm;
+    const int ncolf = ((4 * nr + 15) / 16) * 16, kq = ((2 * jm + 15) / 16) * 16;
+    if (TfSmem(kp.ntab, ncolf, kq).total > dmax || kp.ntab > 128) return;
+    if (cudaFuncSetAttribute(k_field_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, dmax) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    std::vector<int2> kpm((size_t)nr * jm, make_int2(-1, -1));
+    for (int p = 0; p < nr; p++) {
+        const KRun &run = E.h_runs[order[p]];
+        for (int j = 0; j < jm; j++) {
+            int2 v = make_int2(-1, -1);
+            if (j >= run.kzlo && j < run.kzlo + run.nkz) v.x = run.kbeg + j - run.kzlo;
+            if (j > 0 && -j >= run.kzlo && -j < run.kzlo + run.nkz) v.y = run.kbeg - j - run.kzlo;
+            kpm[(size_t)p * jm + j] = v;
+        }
+    }
+    int2 *d_kpm = nullptr;
+    if (cudaMalloc((void **)&d_kpm, sizeof(int2) * kpm.size()) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    E.allocs.push_back(d_kpm);
+    cudaMemcpy(d_kpm, kpm.data(), sizeof(int2) * kpm.size(), cudaMemcpyHostToDevice);
+    E.d_tfkpm = d_kpm;
+    E.tf_nr = nr;
+    E.tf_jm = jm;
+    E.tf_ncol = ncolf;
+    E.tf_kq = kq;
+    E.tf_ready = true;
+}
+
+// Dipole field at the sites [s0, s1) into k-slice 0 of Fpart; 1 when launched, else 0.
+int launch_field_tc(Engine &E, int s0, int s1) {
+    if (!E.tc_ready || !E.tf_ready || !E.ff_tc || s1 <= s0) return 0;
+    const KP &kp = E.kp;
+    TfArgs a;
+    a.slot = E.d_tcslot;
+    a.skv = E.d_tcskv;
+    a.kpm = E.d_tfkpm;
+    a.kzv = E.d_tckzv;
+    a.nr = E.tf_nr;
+    a.ncol = E.tf_ncol;
+    a.kq = E.tf_kq;
+    a.jm = E.tf_jm;
+    a.sbase = s0 & ~(TC_SS - 1);  // TMA x coordinates 2 (sbase + 16 i): 128-byte aligned
+    a.s_lo = s0;
+    a.s_hi = s1;
+    const TfSmem L(kp.ntab, a.ncol, a.kq);
+    dim3 g((s1 - a.sbase + TF_SITES - 1) / TF_SITES, kp.P);
+    const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(E.tc_map);
+    k_field_tc<<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
+    ++E.nlaunch;
+    return 1;
 }
 
 // Returns 1 when the launch wrote Sm and the dipole weights Wf (no k_sreduce needed), else 0.

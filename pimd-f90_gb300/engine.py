@@ -371,10 +371,10 @@ class ForceEngine:
         return self.tuning()
 
     def tuning(self):
-        k = (ctypes.c_int * 7)()
-        self._check(load().pimd_get_tuning(self.h, k, 7), "get_tuning")
+        k = (ctypes.c_int * 8)()
+        self._check(load().pimd_get_tuning(self.h, k, 8), "get_tuning")
         return dict(sf_tiled=k[0], sf_groups=k[1], ff_regs=k[2], max_slices=k[3], nbr_block=k[4], wave_shapes=k[5],
-                    sf_tc=k[6])
+                    sf_tc=k[6], ff_tc=k[7])
 
 
 class ReplicaBatch:
