@@ -35,4 +35,70 @@ PIMD_D void dd_check_block(const KP &kp, double eps) {
     }
 }
 
+// pot_ttm.f90:371-381: Efd = Efd_real + Efd_rec + Efq + factor mu and the SOR update (FP64) of
+// the dipole at site s of bead b, with E this iteration's reciprocal field at the site;
+// av += (|mu_new - mu|^2 (|mu_new|^2 on the first iteration), mu_new . Efq).
+PIMD_D void dd_sor_site(const KP &kp, int b, int s, const double (&E)[3], int iter, double (&av)[2]) {
+    const size_t gs = (size_t)b * kp.S + s;
+    double mu[3];
+    mu[0] = kp.dip[3 * gs];
+    mu[1] = kp.dip[3 * gs + 1];
+    mu[2] = kp.dip[3 * gs + 2];
+    const double4_32a f = kp.F[gs];
+    const double efq[3] = {f.x, f.y, f.z};
+    const int kind = s / kp.N + 1;
+    const double pol = kp.polar_sor * kp.polar[kind];
+    double mn[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const double efd = (kp.Efdr[3 * gs + c] + E[c]) + efq[c] + kp.factor * mu[c];
+        mn[c] = (1.0 - kp.polar_sor) * mu[c] + pol * efd;
+        const double dd = (iter == 1) ? mn[c] : mn[c] - mu[c];
+        av[0] += dd * dd;
+        av[1] += mn[c] * efq[c];
+        kp.dip[3 * gs + c] = mn[c];
+        kp.Efdr[3 * gs + c] = 0.0;
+    }
+    if (kp.dipf) kp.dipf[gs] = make_float4((float)mn[0], (float)mn[1], (float)mn[2], 0.f);
+}
+
+// End of a dipole-update block: its sums go into the bead's acc[ACC_DSQ], acc[ACC_MUEFQ] (when
+// add), then the block counts itself and the last block of the launch runs the convergence
+// test (a device counter, reset by that block). Every thread of every block of the launch calls
+// this exactly once; blocks of converged beads call it with add = false.
+template <int NT>
+PIMD_D void dd_block_end(const KP &kp, int b, const double (&av)[2], bool add) {
+    if (add) {
+        __shared__ double red[NT / 32][2];
+        const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+        for (int i = 0; i < 2; i++) {
+            double x = av[i];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) red[wp][i] = x;
+        }
+        __syncthreads();
+        if (threadIdx.x < 2) {
+            double t = 0;
+            for (int w = 0; w < NT / 32; w++) t += red[w][threadIdx.x];
+            atomicAdd(kp.acc + (size_t)b * NACC + ACC_DSQ + threadIdx.x, t);
+        }
+    }
+    if (kp.fin_counter) {
+        __shared__ bool last;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();  // this block's sums are visible before it counts
+            last = atomicAdd(kp.fin_counter, 1u) == gridDim.x * gridDim.y - 1;
+        }
+        __syncthreads();
+        if (last) {
+            __threadfence();
+            dd_check_block(kp, kp.polar_eps);
+            if (threadIdx.x == 0) *kp.fin_counter = 0u;
+        }
+    }
+}
+
 }  // namespace pimd

@@ -278,7 +278,7 @@ void launch_ewald_pw(Engine &E);
 // writes Sm and the dipole weights Wf and returns 1, or returns 0 (not applicable)
 void tc_init(Engine &E);
 int launch_sfac_tc(Engine &E, int s0, int nsites, int skipconv);
-// tensor-core dipole field (ewald_tc.cu): k-slice 0 of Fpart at [s0, s1); 1 when launched
+// tensor-core dipole field, SOR update and convergence test (ewald_tc.cu); 1 when launched
 int launch_field_tc(Engine &E, int s0, int s1);
 // launchers (spc.cu): q-SPC/Fw and SPC/F
 void launch_sites_spc(Engine &E);

@@ -746,19 +746,8 @@ __global__ void __launch_bounds__(NT) k_field_finish(KP kp, int s0, int s1, int 
     const int iter = kp.dstep[1] + 1;  // dipole iteration of this update (F_D)
     const bool done = MODE == F_D && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0;
     if (done) {  // converged bead: no update, but the block still counts towards the test
-        if (kp.fin_counter) {
-            __shared__ bool last0;
-            if (threadIdx.x == 0) {
-                __threadfence();
-                last0 = atomicAdd(kp.fin_counter, 1u) == gridDim.x * gridDim.y - 1;
-            }
-            __syncthreads();
-            if (last0) {
-                __threadfence();
-                dd_check_block(kp, kp.polar_eps);
-                if (threadIdx.x == 0) *kp.fin_counter = 0u;
-            }
-        }
+        const double zero[2] = {0.0, 0.0};
+        dd_block_end<NT>(kp, b, zero, false);
         return;
     }
     const int s = s0 + blockIdx.x * NT + threadIdx.x;
@@ -793,58 +782,8 @@ __global__ void __launch_bounds__(NT) k_field_finish(KP kp, int s0, int s1, int 
     } else {
         // pot_ttm.f90:371-381 Efd = Efd_real + Efd_rec + Efq + factor mu; SOR update (FP64)
         double av[2] = {0.0, 0.0};
-        double mu[3] = {0, 0, 0};
-        if (valid) {
-            mu[0] = kp.dip[3 * gs];
-            mu[1] = kp.dip[3 * gs + 1];
-            mu[2] = kp.dip[3 * gs + 2];
-            const double4_32a f = kp.F[gs];
-            const double efq[3] = {f.x, f.y, f.z};
-            const int kind = s / kp.N + 1;
-            const double pol = kp.polar_sor * kp.polar[kind];
-            double mn[3];
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                const double efd = (kp.Efdr[3 * gs + c] + E[c]) + efq[c] + kp.factor * mu[c];
-                mn[c] = (1.0 - kp.polar_sor) * mu[c] + pol * efd;
-                const double dd = (iter == 1) ? mn[c] : mn[c] - mu[c];
-                av[0] += dd * dd;
-                av[1] += mn[c] * efq[c];
-                kp.dip[3 * gs + c] = mn[c];
-                kp.Efdr[3 * gs + c] = 0.0;
-            }
-            if (kp.dipf) kp.dipf[gs] = make_float4((float)mn[0], (float)mn[1], (float)mn[2], 0.f);
-        }
-        // reduce into acc[ACC_DSQ], acc[ACC_MUEFQ]
-        __shared__ double red[NT / 32][2];
-        const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-#pragma unroll
-        for (int i = 0; i < 2; i++) {
-            double x = av[i];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            if (lane == 0) red[wp][i] = x;
-        }
-        __syncthreads();
-        if (threadIdx.x < 2) {
-            double t = 0;
-            for (int w = 0; w < NT / 32; w++) t += red[w][threadIdx.x];
-            atomicAdd(kp.acc + (size_t)b * NACC + ACC_DSQ + threadIdx.x, t);
-        }
-        if (kp.fin_counter) {
-            __shared__ bool last;
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                __threadfence();  // this block's sums are visible before it counts
-                last = atomicAdd(kp.fin_counter, 1u) == gridDim.x * gridDim.y - 1;
-            }
-            __syncthreads();
-            if (last) {
-                __threadfence();
-                dd_check_block(kp, kp.polar_eps);
-                if (threadIdx.x == 0) *kp.fin_counter = 0u;
-            }
-        }
+        if (valid) dd_sor_site(kp, b, s, E, iter, av);
+        dd_block_end<NT>(kp, b, av, true);
     }
 }
 
@@ -1029,13 +968,8 @@ static void launch_field_f(Engine &E, int s0, int s1) {
 template <int MODE>
 static void run_field(Engine &E, int s0, int s1) {
     const int LZ = 2 * E.kp.lmax + 1;
-    if (MODE == F_D && E.precision == PIMD_PREC_MIXED && launch_field_tc(E, s0, s1)) {
-        // tensor-core field pass (ewald_tc.cu): one k-slice, then the FP64 SOR update and test
-        dim3 g2((s1 - s0 + 127) / 128, E.kp.P);
-        k_field_finish<MODE, 128><<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, 1);
-        ++E.nlaunch;
-        return;
-    }
+    // tensor-core field pass with the SOR update and convergence test (ewald_tc.cu)
+    if (MODE == F_D && E.precision == PIMD_PREC_MIXED && launch_field_tc(E, s0, s1)) return;
     if (E.precision == PIMD_PREC_MIXED && E.ff_regs && LZ <= 49) {
         if (LZ <= 17)
             launch_field_f<MODE, 17>(E, s0, s1);

@@ -44,6 +44,7 @@
 
 #include <cuda_fp16.h>
 
+#include "dipole_check.cuh"
 #include "engine.h"
 #include "umma.cuh"
 
@@ -494,10 +495,12 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
 // so T0, T1 of every run at every site are one GEMM per bead,
 //   D[s][(run, T0re|T0im|T1re|T1im)] = sum_q Q[s][q] V[(run, comp)][q],  q = (j, cos|sin),
 // with the sites on M (128 per CTA), 4 columns per run on N and only 2 (max |kz| + 1) terms on
-// K (FP16 hi + lo split, three MMAs per 16-term K step). The epilogue contracts each TMEM row
-// with exy(s, run) from the TMA-staged tables, 16 warps = 4 lane quarters x 4 run quarters, and
-// writes the field at the CTA's sites as k-slice 0 of Fpart for k_field_finish<F_D>. V is built
-// by every CTA of a bead from Wf (scaled by 2^10, exact, to keep small weights normal in FP16).
+// K (FP16 hi + lo split, three MMAs per 16-term K step). V is built by every CTA of a bead from
+// the bead's weights Wf (one bulk copy into shared memory; scaled by 2^10, exact, to keep small
+// weights normal in FP16). The epilogue contracts each TMEM row with exy(s, run) from the
+// TMA-staged tables (16 warps = 4 lane quarters x 4 run quarters), then applies the iteration's
+// FP64 SOR update at the CTA's dipole sites and the convergence test in the last CTA
+// (dipole_check.cuh, as k_field_finish<F_D> does).
 constexpr int TF_NT = 512;
 constexpr int TF_SITES = 128;             // sites per CTA (M)
 constexpr float TF_WS = 1024.f;           // power-of-two scale of V
@@ -512,12 +515,13 @@ struct TfArgs {
 };
 
 struct TfSmem {
-    int boxb, A, B, total;
-    __host__ __device__ TfSmem(int ntab, int ncol, int kq) {
+    int boxb, A, B, W, total;
+    __host__ __device__ TfSmem(int ntab, int ncol, int kq, int nk) {
         boxb = ((ntab * 128 + 1023) / 1024) * 1024;
         A = 8 * boxb;                      // tables of 128 sites: 8 TMA boxes of 16 sites
         B = A + 2 * TF_SITES * kq * 2;     // Q hi, lo: 128 rows x kq halves
-        total = B + 2 * ncol * kq * 2 + 1024;  // V hi, lo: ncol rows x kq halves
+        W = B + 2 * ncol * kq * 2;         // V hi, lo: ncol rows x kq halves
+        total = W + ((nk * 8 + 127) / 128) * 128 + 1024;  // the bead's weights Wf
     }
 };
 
@@ -540,12 +544,18 @@ PIMD_D void split2_h(float a, float b, uint32_t &hi, uint32_t &lo) {
 
 __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ CUtensorMap tmap, KP kp, TfArgs a) {
     const int t = blockIdx.x, b = blockIdx.y;
-    if (kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;  // converged bead, as k_field_f<F_D>
+    const int iter = kp.dstep[1] + 1;  // dipole iteration of this update
+    if (kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) {
+        // converged bead: no update, but the block still counts towards the convergence test
+        const double zero[2] = {0.0, 0.0};
+        dd_block_end<TF_NT>(kp, b, zero, false);
+        return;
+    }
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const TfSmem L(kp.ntab, a.ncol, a.kq);
+    const TfSmem L(kp.ntab, a.ncol, a.kq, kp.nk);
     extern __shared__ __align__(1024) unsigned char sm_raw[];
     unsigned char *sm = sm_raw + ((1024u - (umma::smem_u32(sm_raw) & 1023u)) & 1023u);
-    __shared__ uint64_t tbar, mbar;
+    __shared__ uint64_t tbar, wbar, mbar;
     __shared__ uint32_t tslot;
     __shared__ int4 sslot[TC_MAXRUN];
     __shared__ float2 sskv[TC_MAXRUN];
@@ -559,6 +569,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     if (warp == 0) umma::tmem_alloc(&tslot, 512);
     if (tid == 0) {
         umma::mbar_init(&tbar, 1);
+        umma::mbar_init(&wbar, 1);
         umma::mbar_init(&mbar, 1);
     }
     umma::fence_before_sync();
@@ -566,13 +577,35 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     umma::fence_after_sync();
     const uint32_t tm = tslot;
     if (tid == 0) {
+        const uint32_t wbytes = (uint32_t)kp.nk * 8u;
+        mbar_expect_tx(&wbar, wbytes);
+        bulk_load(sm + L.W, kp.Wf + ((size_t)b * 2 + 1) * kp.nk, wbytes, &wbar);
         const uint32_t box_tx = (uint32_t)(kp.ntab * 128);
         mbar_expect_tx(&tbar, 8 * box_tx);
         for (int i = 0; i < 8; i++) tma_load_2d(sm + i * L.boxb, &tmap, 2 * (sb + 16 * i), b * kp.ntab, &tbar);
     }
-    // V = the run weights (while the tables land): rows 4 p + comp, halves (2 j, 2 j + 1)
     unsigned char *Vh = sm + L.B, *Vl = Vh + a.ncol * a.kq * 2;
-    const float2 *W = kp.Wf + ((size_t)b * 2 + 1) * kp.nk;
+    unsigned char *Qh = sm + L.A, *Ql = Qh + TF_SITES * a.kq * 2;
+    const int kpad = (a.kq - 2 * jm) / 2;
+    // zero padding: V rows >= 4 nr, V and Q halves >= 2 jm
+    for (int it = tid; it < (a.ncol - 4 * nr) * (a.kq / 2); it += TF_NT) {
+        const int n = 4 * nr + it / (a.kq / 2), q = 2 * (it % (a.kq / 2));
+        *reinterpret_cast<uint32_t *>(Vh + hoff(n, q, kcm)) = 0u;
+        *reinterpret_cast<uint32_t *>(Vl + hoff(n, q, kcm)) = 0u;
+    }
+    for (int it = tid; it < 4 * nr * kpad; it += TF_NT) {
+        const int n = it / kpad, q = 2 * jm + 2 * (it % kpad);
+        *reinterpret_cast<uint32_t *>(Vh + hoff(n, q, kcm)) = 0u;
+        *reinterpret_cast<uint32_t *>(Vl + hoff(n, q, kcm)) = 0u;
+    }
+    for (int it = tid; it < TF_SITES * kpad; it += TF_NT) {
+        const int n = it / kpad, q = 2 * jm + 2 * (it % kpad);
+        *reinterpret_cast<uint32_t *>(Qh + hoff(n, q, kcm)) = 0u;
+        *reinterpret_cast<uint32_t *>(Ql + hoff(n, q, kcm)) = 0u;
+    }
+    // V = the run weights: rows 4 p + comp, halves (2 j, 2 j + 1)
+    uint32_t err = (uint32_t)umma::mbar_wait(&wbar, 0, TC_WAIT);
+    const float2 *W = reinterpret_cast<const float2 *>(sm + L.W);
     for (int it = tid; it < nr * jm; it += TF_NT) {
         const int p = it / jm, j = it - p * jm;
         const int2 km = a.kpm[it];
@@ -592,25 +625,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
             *reinterpret_cast<uint32_t *>(Vl + o) = lo;
         }
     }
-    // zero padding: V rows >= 4 nr, V and Q halves >= 2 jm
-    for (int it = tid; it < (a.ncol - 4 * nr) * (a.kq / 2); it += TF_NT) {
-        const int n = 4 * nr + it / (a.kq / 2), q = 2 * (it % (a.kq / 2));
-        *reinterpret_cast<uint32_t *>(Vh + hoff(n, q, kcm)) = 0u;
-        *reinterpret_cast<uint32_t *>(Vl + hoff(n, q, kcm)) = 0u;
-    }
-    const int kpad = (a.kq - 2 * jm) / 2;
-    for (int it = tid; it < 4 * nr * kpad; it += TF_NT) {
-        const int n = it / kpad, q = 2 * jm + 2 * (it % kpad);
-        *reinterpret_cast<uint32_t *>(Vh + hoff(n, q, kcm)) = 0u;
-        *reinterpret_cast<uint32_t *>(Vl + hoff(n, q, kcm)) = 0u;
-    }
-    unsigned char *Qh = sm + L.A, *Ql = Qh + TF_SITES * a.kq * 2;
-    for (int it = tid; it < TF_SITES * kpad; it += TF_NT) {
-        const int n = it / kpad, q = 2 * jm + 2 * (it % kpad);
-        *reinterpret_cast<uint32_t *>(Qh + hoff(n, q, kcm)) = 0u;
-        *reinterpret_cast<uint32_t *>(Ql + hoff(n, q, kcm)) = 0u;
-    }
-    uint32_t err = (uint32_t)umma::mbar_wait(&tbar, 0, TC_WAIT);
+    err |= (uint32_t)umma::mbar_wait(&tbar, 0, TC_WAIT);
     // Q = ez rows of the CTA's sites: halves (2 j, 2 j + 1) = (c_j, s_j)
     for (int it = tid; it < TF_SITES * jm; it += TF_NT) {
         const int s = it % TF_SITES, j = it / TF_SITES;
@@ -696,6 +711,8 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         umma::tmem_dealloc(tm, 512);
         umma::tmem_relinquish();
     }
+    // the iteration's FP64 SOR update at the CTA's dipole sites, then the block's end
+    double av[2] = {0.0, 0.0};
     if (tid < TF_SITES && !bad) {
         const int s = sb + tid;
         if (s >= a.s_lo && s < a.s_hi) {
@@ -704,10 +721,12 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
             for (int q4 = 0; q4 < 4; q4++)
 #pragma unroll
                 for (int c = 0; c < 3; c++) e[c] += red[(q4 * TF_SITES + tid) * 3 + c];
-            kp.Fpart[(size_t)b * (a.s_hi - a.s_lo) + (s - a.s_lo)] = make_double4_32a(e[0], e[1], e[2], 0.0);
+            const double E[3] = {(double)e[0], (double)e[1], (double)e[2]};
+            dd_sor_site(kp, b, s, E, iter, av);
         }
     }
     if (bad && tid == 0) atomicOr(kp.err, 8u);
+    dd_block_end<TF_NT>(kp, b, av, !bad);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -850,8 +869,15 @@ void tc_init(Engine &E) {
     if (groups.size() != 1) return;
     const int nr = groups[0].nr, jm = groups[0].jm;
     const int ncolf = ((4 * nr + 15) / 16) * 16, kq = ((2 * jm + 15) / 16) * 16;
-    if (TfSmem(kp.ntab, ncolf, kq).total > dmax || kp.ntab > 128) return;
-    if (cudaFuncSetAttribute(k_field_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, dmax) != cudaSuccess) {
+    cudaFuncAttributes fb;
+    if (cudaFuncGetAttributes(&fb, k_field_tc) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    const int dmaxf = optin - (int)fb.sharedSizeBytes;
+    // the weights arrive by one bulk copy: 8 nk bytes, a multiple of 16
+    if (TfSmem(kp.ntab, ncolf, kq, kp.nk).total > dmaxf || kp.ntab > 128 || (kp.nk & 1)) return;
+    if (cudaFuncSetAttribute(k_field_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
@@ -880,7 +906,8 @@ void tc_init(Engine &E) {
     E.tf_ready = true;
 }
 
-// Dipole field at the sites [s0, s1) into k-slice 0 of Fpart; 1 when launched, else 0.
+// Dipole field, SOR update and convergence test of one iteration at the dipole sites [s0, s1)
+// (k_field_f<F_D> + k_field_finish<F_D>); 1 when launched, else 0.
 int launch_field_tc(Engine &E, int s0, int s1) {
     if (!E.tc_ready || !E.tf_ready || !E.ff_tc || s1 <= s0) return 0;
     const KP &kp = E.kp;
@@ -896,7 +923,7 @@ int launch_field_tc(Engine &E, int s0, int s1) {
     a.sbase = s0 & ~(TC_SS - 1);  // TMA x coordinates 2 (sbase + 16 i): 128-byte aligned
     a.s_lo = s0;
     a.s_hi = s1;
-    const TfSmem L(kp.ntab, a.ncol, a.kq);
+    const TfSmem L(kp.ntab, a.ncol, a.kq, kp.nk);
     dim3 g((s1 - a.sbase + TF_SITES - 1) / TF_SITES, kp.P);
     const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(E.tc_map);
     k_field_tc<<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
