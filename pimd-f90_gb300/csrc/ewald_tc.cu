@@ -24,13 +24,15 @@
 // groups of a (bead, run group) form a thread-block cluster. Warp roles:
 //   * producer warp: per 32-site stage, TMA (cp.async.bulk.tensor.2d, two boxes of 16 sites x all
 //     ntab table rows, 128-byte swizzle) plus a bulk copy of the 32 FP32 dipoles, completing on an
-//     mbarrier;
-//   * 14 builder warps: per 16 sites build X (exy of every run) and Z (mu_c ez) in the canonical
-//     no-swizzle K-major layout, split into FP16 hi + lo, into one of three buffers;
+//     mbarrier; it then turns the dipoles into scaled, masked per-component rows and releases the
+//     stage to the builders;
+//   * 16 builder warps: per 16 sites build X (exy of every run, one item per thread) and Z
+//     (mu_c ez, on the threads without an X item) in the canonical no-swizzle K-major layout,
+//     split into FP16 hi + lo, into one of three buffers;
 //   * MMA warp: one thread issues the MMAs into TMEM and commits to the buffer's mbarrier, which
 //     releases the buffer to the builders.
 // Only mbarriers connect the roles, so building, copying and MMAs overlap. The epilogue reads
-// TMEM (tcgen05.ld) 32 runs at a time, combines each k-vector's 12 sums, and keeps the CTA's FP32
+// TMEM (tcgen05.ld) 64 runs at a time, combines each k-vector's 12 sums, and keeps the CTA's FP32
 // partial S in shared memory; after a cluster barrier each CTA adds the partials of all CTAs of
 // its cluster over a slice of the k-vectors (distributed shared memory, FP32, site groups in a
 // fixed order) and writes Sm and the FP32 weights Wf.
@@ -50,16 +52,18 @@
 
 namespace pimd {
 
-constexpr int TC_NB = 14;                 // builder warps
+constexpr int TC_NB = 16;                 // builder warps
 constexpr int TC_MMA_WARP = TC_NB;        // MMA-issuing warp (then the producer warp)
-constexpr int TC_NT = (TC_NB + 2) * 32;   // 512 threads
+constexpr int TC_NT = (TC_NB + 2) * 32;   // 576 threads
 constexpr int TC_SS = 32;                 // sites per table stage
 constexpr int TC_KS = 16;                 // sites per MMA step (kind::f16: 32 bytes of K)
 constexpr float TC_ZS = 64.f;             // power-of-two scale of Z (keeps small mu_c ez normal in FP16)
 constexpr int TC_NABUF_MAX = 3;           // operand buffers
+constexpr int TC_NST = 4;                 // table stage buffers (a CTA's 128 sites at 512 x 32)
+constexpr int TC_ZMAX = 4;                // Z items per builder thread (6 (|kz|max + 1) x 2 <= 256)
 constexpr int TC_CLMAX = 8;               // site groups per cluster (portable cluster size)
 constexpr int TC_MAXRUN = 256;            // runs per group: 512 TMEM columns
-constexpr int TC_CH = 32;                 // runs per epilogue chunk
+constexpr int TC_CH = 64;                 // runs per epilogue chunk
 constexpr int TC_LD = 2 * TC_CH + 4;      // staging row pitch (floats)
 constexpr long long TC_WAIT = 1LL << 28;  // cycles before a wait gives up (~0.13 s)
 
@@ -90,15 +94,17 @@ struct TcArgs {
 // Shared-memory carve-up (bytes from a 1024-aligned base), used by the kernel and the launcher.
 // A table stage holds two TMA boxes of 16 sites x ntab rows, each written with the 128-byte
 // swizzle (16-byte chunk c of row r lands at chunk c ^ (r & 7), so loads of the same sites from
-// different rows fall in different banks), followed by the stage's 32 dipoles. An operand
+// different rows fall in different banks), followed by the stage's 32 dipoles (as copied, then
+// as 3 rows of 2^6 mu_c with the sites outside the group zeroed). An operand
 // buffer holds Z hi, Z lo (128 rows x 16 FP16 sites each) and X hi, X lo (ncolmax rows x 16 sites).
 struct TcSmem {
-    int boxb, mu, stage, buf, xoff, bufstride, total;
+    int boxb, mu, muz, stage, buf, xoff, bufstride, total;
     __host__ __device__ TcSmem(int ntab, int ncolmax, int nabuf) {
         boxb = ((ntab * 128 + 1023) / 1024) * 1024;
         mu = 2 * boxb;
-        stage = ((mu + TC_SS * 16 + 1023) / 1024) * 1024;
-        buf = 2 * stage;
+        muz = mu + TC_SS * 16;
+        stage = ((muz + 3 * TC_SS * 4 + 1023) / 1024) * 1024;
+        buf = TC_NST * stage;
         xoff = 2 * 128 * 32;
         bufstride = xoff + 2 * ncolmax * 32;
         total = buf + nabuf * bufstride + 1024;  // + alignment slack of the dynamic base
@@ -178,7 +184,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     extern __shared__ __align__(1024) unsigned char sm_raw[];
     // the swizzle pattern follows shared-memory address bits 7-9: align the base to 1024 bytes
     unsigned char *sm = sm_raw + ((1024u - (umma::smem_u32(sm_raw) & 1023u)) & 1023u);
-    __shared__ uint64_t tfull[2], tempty[2], afull[TC_NABUF_MAX], aempty[TC_NABUF_MAX];
+    __shared__ uint64_t tfull[TC_NST], mfull[TC_NST], tempty[TC_NST], afull[TC_NABUF_MAX], aempty[TC_NABUF_MAX];
     __shared__ uint32_t tslot;
     __shared__ int4 sslot[TC_MAXRUN];
     __shared__ float2 sskv[TC_MAXRUN];
@@ -188,8 +194,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     const int g1 = min(a.s_hi, g0 + a.tsg);
     const int nstage = max(0, (g1 - g0 + TC_SS - 1) / TC_SS);
     const int nsub = nstage * (TC_SS / TC_KS);
-    const int yrow = kp.hmax + 1;            // first ey row (ky = 0)
-    const int zrow = yrow + kp.kmax + 1;     // first ez row (kz = 0)
+    const int yrow = kp.hmax + 1;            // first ey row (ky = 0); ez rows follow the ky rows
     const int nab = a.nabuf, jm = G.jm, nr = G.nr;
     const int xlo = a.ncolmax * 32;          // X lo after X hi
 
@@ -199,15 +204,30 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     }
     if (tid < 2 * kp.lmax + 1) skz[tid] = a.kzv[tid];
     if (warp == 0) umma::tmem_alloc(&tslot, 512);
+    // table stage ts of this group: TMA boxes of the tables and a bulk copy of the dipoles
+    const uint32_t box_tx = (uint32_t)(kp.ntab * 128);
+    auto issue_stage = [&](int ts) {
+        const int sfirst = g0 + ts * TC_SS, tb = ts % TC_NST;
+        unsigned char *dst = sm + tb * L.stage;
+        const int nmu = min(TC_SS, kp.S - sfirst);  // dipoles inside this bead's rows
+        const uint32_t mub = (uint32_t)nmu * 16u;
+        mbar_expect_tx(&tfull[tb], 2 * box_tx + mub);
+        tma_load_2d(dst, &tmap, 2 * sfirst, b * kp.ntab, &tfull[tb]);
+        tma_load_2d(dst + L.boxb, &tmap, 2 * sfirst + 32, b * kp.ntab, &tfull[tb]);
+        bulk_load(dst + L.mu, kp.dipf + (size_t)b * kp.S + sfirst, mub, &tfull[tb]);
+    };
     if (tid == 0) {
-        for (int i = 0; i < 2; i++) {
+        for (int i = 0; i < TC_NST; i++) {
             umma::mbar_init(&tfull[i], 1);
+            umma::mbar_init(&mfull[i], 1);
             umma::mbar_init(&tempty[i], TC_NB);
         }
         for (int i = 0; i < nab; i++) {
             umma::mbar_init(&afull[i], TC_NB);
             umma::mbar_init(&aempty[i], 1);
         }
+        // the first stages go out now, under the rest of the set-up
+        for (int ts = 0; ts < min(nstage, TC_NST); ts++) issue_stage(ts);
     }
     {   // padding stays zero in every buffer (hi and lo): Z rows >= 6 jm, X rows >= 2 nr
         const int zp = 128 - 6 * jm, xp = G.ncol - 2 * nr;
@@ -247,18 +267,29 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
             it_yr[u] = yrow + (ky < 0 ? -ky : ky);
             it_ys[u] = ky < 0 ? -1.f : 1.f;
         }
-        // Z items: one row (c, j, cos|sin) x 8 sites, on the threads from the last one down
-        const int zi = 32 * TC_NB - 1 - bt;
-        const bool zit = zi < 6 * jm * 2;
-        const int zrow_ = zi >> 1, zo = zi & 1;
-        const int zc = zrow_ / (2 * jm), zj = (zrow_ >> 1) % jm, zcs = zrow_ & 1;
-        const int zoff = rowchunk(zrow_, zo);
+        // Z items: one row (c, j, cos|sin) x 8 sites each, on the whole warps after the X items
+        // (else on the last warp), at most TC_ZMAX per thread; row decoded once here
+        const int nzi = 6 * jm * 2;
+        const int zwarps = max(1, TC_NB - (2 * nr + 31) / 32), zthreads = 32 * zwarps, zbase = 32 * TC_NB - zthreads;
+        int zn = 0, zoff[TC_ZMAX], zmo[TC_ZMAX], zer[TC_ZMAX], zcs[TC_ZMAX], zq[TC_ZMAX];
+#pragma unroll
+        for (int u = 0; u < TC_ZMAX; u++) {
+            const int zi = bt - zbase + u * zthreads;
+            zoff[u] = zmo[u] = zer[u] = zcs[u] = zq[u] = 0;
+            if (bt < zbase || zi >= nzi) continue;
+            zn = u + 1;
+            const int zr = zi >> 1, c = zr / (2 * jm);
+            zoff[u] = rowchunk(zr, zi & 1);
+            zmo[u] = c * TC_SS + 8 * (zi & 1);         // component row of muz, first site
+            zer[u] = yrow + kp.kmax + 1 + ((zr >> 1) % jm);  // ez row of j
+            zcs[u] = zr & 1;
+            zq[u] = 8 * (zi & 1);
+        }
         for (int ts = 0; ts < nstage && !err; ts++) {
-            const int tb = ts & 1;
-            err |= (uint32_t)umma::mbar_wait(&tfull[tb], (uint32_t)((ts >> 1) & 1), TC_WAIT);
+            const int tb = ts % TC_NST;
+            err |= (uint32_t)umma::mbar_wait(&mfull[tb], (uint32_t)((ts / TC_NST) & 1), TC_WAIT);
             const unsigned char *tab = sm + tb * L.stage;
-            const float4 *mus = reinterpret_cast<const float4 *>(tab + L.mu);
-            const int sfirst = g0 + ts * TC_SS;
+            const float *muz = reinterpret_cast<const float *>(tab + L.muz);
             for (int ks = 0; ks < TC_SS / TC_KS && !err; ks++) {
                 const int sub = ts * (TC_SS / TC_KS) + ks, ab = sub % nab, use = sub / nab;
                 if (use > 0) err |= (uint32_t)umma::mbar_wait(&aempty[ab], (uint32_t)((use - 1) & 1), TC_WAIT);
@@ -289,25 +320,24 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
                     *reinterpret_cast<uint4 *>(xp + xlo) = rl;
                     *reinterpret_cast<uint4 *>(xp + xlo + 16) = il;
                 }
-                if (zit) {
-                    const int sq = so + 8 * zo;
+#pragma unroll
+                for (int u = 0; u < TC_ZMAX; u++) {
+                    if (u >= zn) break;
+                    const int sq = so + zq[u];
+                    const float4 m0 = *reinterpret_cast<const float4 *>(muz + zmo[u] + so);
+                    const float4 m1 = *reinterpret_cast<const float4 *>(muz + zmo[u] + so + 4);
+                    const float mc[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
                     float v[8];
 #pragma unroll
                     for (int h = 0; h < 4; h++) {
-                        const float4 zz = *tab_chunk(tab, L.boxb, zrow + zj, sq + 2 * h);
-#pragma unroll
-                        for (int e = 0; e < 2; e++) {
-                            const int i = 2 * h + e, s = sfirst + sq + i;
-                            const float4 m = mus[sq + i];
-                            const float mc = zc == 0 ? m.x : (zc == 1 ? m.y : m.z);
-                            const float zv = e == 0 ? (zcs ? zz.y : zz.x) : (zcs ? zz.w : zz.z);
-                            v[i] = (s < a.s_lo || s >= g1) ? 0.f : TC_ZS * mc * zv;
-                        }
+                        const float4 zz = *tab_chunk(tab, L.boxb, zer[u], sq + 2 * h);
+                        v[2 * h] = mc[2 * h] * (zcs[u] ? zz.y : zz.x);
+                        v[2 * h + 1] = mc[2 * h + 1] * (zcs[u] ? zz.w : zz.z);
                     }
                     uint4 hi, lo;
                     split8_h(v, hi, lo);
-                    *reinterpret_cast<uint4 *>(Bf + zoff) = hi;
-                    *reinterpret_cast<uint4 *>(Bf + 128 * 32 + zoff) = lo;
+                    *reinterpret_cast<uint4 *>(Bf + zoff[u]) = hi;
+                    *reinterpret_cast<uint4 *>(Bf + 128 * 32 + zoff[u]) = lo;
                 }
                 umma::fence_smem_to_async();
                 __syncwarp();
@@ -342,31 +372,39 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
             }
         }
     } else {
-        // ---------------- producer: tables + dipoles of each 32-site stage by TMA
-        if (lane == 0) {
-            const uint32_t box_tx = (uint32_t)(kp.ntab * 128);
-            int issued = 0, landed = 0;
-            for (int ts = 0; ts < nstage && !err; ts++) {
-                const int tb = ts & 1;
-                if (ts >= 2) {
-                    // buffer tb: all builder warps done with stage ts - 2, whose copy has landed
-                    err |= (uint32_t)umma::mbar_wait(&tempty[tb], (uint32_t)(((ts - 2) >> 1) & 1), TC_WAIT);
-                    if (err) break;
-                    landed = ts - 1;
-                }
-                const int sfirst = g0 + ts * TC_SS;
-                unsigned char *dst = sm + tb * L.stage;
-                const int nmu = min(TC_SS, kp.S - sfirst);  // dipoles inside this bead's rows
-                const uint32_t mub = (uint32_t)nmu * 16u;
-                mbar_expect_tx(&tfull[tb], 2 * box_tx + mub);
-                tma_load_2d(dst, &tmap, 2 * sfirst, b * kp.ntab, &tfull[tb]);
-                tma_load_2d(dst + L.boxb, &tmap, 2 * sfirst + 32, b * kp.ntab, &tfull[tb]);
-                bulk_load(dst + L.mu, kp.dipf + (size_t)b * kp.S + sfirst, mub, &tfull[tb]);
-                issued = ts + 1;
+        // ---------------- producer: as each table stage lands, the dipoles as 3 component rows
+        // (2^6 mu_c, zero outside [s_lo, g1)) for the builders; stages beyond the first TC_NST are
+        // copied into a buffer once all builder warps are done with its previous stage
+        int issued = min(nstage, TC_NST), landed = 0;
+        for (int ts = 0; ts < nstage && !err; ts++) {
+            const int tb = ts % TC_NST;
+            err |= (uint32_t)umma::mbar_wait(&tfull[tb], (uint32_t)((ts / TC_NST) & 1), TC_WAIT);
+            if (err) break;
+            landed = ts + 1;
+            unsigned char *dst = sm + tb * L.stage;
+            {
+                const int s = g0 + ts * TC_SS + lane;
+                const float4 m = reinterpret_cast<const float4 *>(dst + L.mu)[lane];
+                const bool in = s >= a.s_lo && s < g1;
+                float *muz = reinterpret_cast<float *>(dst + L.muz);
+                muz[lane] = in ? TC_ZS * m.x : 0.f;
+                muz[TC_SS + lane] = in ? TC_ZS * m.y : 0.f;
+                muz[2 * TC_SS + lane] = in ? TC_ZS * m.z : 0.f;
             }
-            // the builders saw every copy land unless something timed out: then wait here
-            for (int w = landed; w < issued && err; w++) umma::mbar_wait(&tfull[w & 1], (uint32_t)((w >> 1) & 1), TC_WAIT);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&mfull[tb]);
+            const int tr = ts + TC_NST - 1;  // refill the buffer of stage ts - 1
+            if (ts >= 1 && tr < nstage) {
+                err |= (uint32_t)umma::mbar_wait(&tempty[tr % TC_NST], (uint32_t)(((ts - 1) / TC_NST) & 1), TC_WAIT);
+                if (err) break;
+                if (lane == 0) issue_stage(tr);
+                issued = tr + 1;
+                __syncwarp();
+            }
         }
+        // copies still in flight after a timeout land before the CTA leaves
+        for (int w = landed; w < issued && err; w++)
+            umma::mbar_wait(&tfull[w % TC_NST], (uint32_t)((w / TC_NST) & 1), TC_WAIT);
     }
 
     // ---------------- all MMAs done: the last commit tracks every earlier MMA of the issuing thread
@@ -389,17 +427,17 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
         const int i = i0 + tid + u * TC_NT;
         pf[u] = i < i1 ? a.kw[G.kgoff + i] : TcKW{0, 0.f};
     }
-    // epilogue: TMEM -> shared, 32 runs (64 columns) at a time -> partial S of every k of the group
+    // epilogue: TMEM -> shared, 64 runs (128 columns) at a time -> partial S of every k of the group
     float *stg = reinterpret_cast<float *>(sm);                       // [128][TC_LD]
     float2 *pt = reinterpret_cast<float2 *>(sm + 128 * TC_LD * 4);    // [nkl]
     for (int ch = 0; ch * TC_CH < nr && !bad; ch++) {
-        {
+        if (warp < 16) {
             const int lq = warp & 3, part = warp >> 2;  // 4 lane quarters x 4 column quarters
-            const int c0 = ch * 2 * TC_CH + 16 * part;
+            const int c0 = ch * 2 * TC_CH + 32 * part;
             float v[8];
-            float *row = stg + (32 * lq + lane) * TC_LD + 16 * part;
+            float *row = stg + (32 * lq + lane) * TC_LD + 32 * part;
 #pragma unroll
-            for (int hh = 0; hh < 2; hh++) {
+            for (int hh = 0; hh < 4; hh++) {
                 if (nsub > 0) {
                     umma::tmem_ld8(tm + ((uint32_t)(32 * lq) << 16) + (uint32_t)(c0 + 8 * hh), v);
                 } else {
@@ -790,6 +828,10 @@ void tc_init(Engine &E) {
     for (int p0 = 0; p0 < kp.nrun; p0 += TC_MAXRUN) {
         TcGroup g{p0, std::min(TC_MAXRUN, kp.nrun - p0), 0, jr[order[p0]], 0, (int)kloc.size(), 0, 0};
         if (6 * g.jm > 128) return;
+        {   // the builders' Z items fit TC_ZMAX per thread (the kernel's split of warps)
+            const int zw = std::max(1, TC_NB - (2 * g.nr + 31) / 32);
+            if ((12 * g.jm + 32 * zw - 1) / (32 * zw) > TC_ZMAX) return;
+        }
         g.ncol = ((2 * g.nr + 15) / 16) * 16;
         for (int p = p0; p < p0 + g.nr; p++) {
             const int r = order[p];
