@@ -35,31 +35,46 @@ PIMD_D void dd_check_block(const KP &kp, double eps) {
     }
 }
 
+// The FP64 inputs of one dipole site's SOR update (fetched early by callers that can hide the
+// latency).
+struct DdSite {
+    double mu[3], efq[3], efdr[3], pol;
+};
+PIMD_D void dd_sor_load(const KP &kp, int b, int s, DdSite &d) {
+    const size_t gs = (size_t)b * kp.S + s;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        d.mu[c] = kp.dip[3 * gs + c];
+        d.efdr[c] = kp.Efdr[3 * gs + c];
+    }
+    const double4_32a f = kp.F[gs];
+    d.efq[0] = f.x;
+    d.efq[1] = f.y;
+    d.efq[2] = f.z;
+    d.pol = kp.polar_sor * kp.polar[s / kp.N + 1];
+}
 // pot_ttm.f90:371-381: Efd = Efd_real + Efd_rec + Efq + factor mu and the SOR update (FP64) of
 // the dipole at site s of bead b, with E this iteration's reciprocal field at the site;
 // av += (|mu_new - mu|^2 (|mu_new|^2 on the first iteration), mu_new . Efq).
-PIMD_D void dd_sor_site(const KP &kp, int b, int s, const double (&E)[3], int iter, double (&av)[2]) {
+PIMD_D void dd_sor_apply(const KP &kp, int b, int s, const DdSite &d, const double (&E)[3], int iter, double (&av)[2]) {
     const size_t gs = (size_t)b * kp.S + s;
-    double mu[3];
-    mu[0] = kp.dip[3 * gs];
-    mu[1] = kp.dip[3 * gs + 1];
-    mu[2] = kp.dip[3 * gs + 2];
-    const double4_32a f = kp.F[gs];
-    const double efq[3] = {f.x, f.y, f.z};
-    const int kind = s / kp.N + 1;
-    const double pol = kp.polar_sor * kp.polar[kind];
     double mn[3];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        const double efd = (kp.Efdr[3 * gs + c] + E[c]) + efq[c] + kp.factor * mu[c];
-        mn[c] = (1.0 - kp.polar_sor) * mu[c] + pol * efd;
-        const double dd = (iter == 1) ? mn[c] : mn[c] - mu[c];
+        const double efd = (d.efdr[c] + E[c]) + d.efq[c] + kp.factor * d.mu[c];
+        mn[c] = (1.0 - kp.polar_sor) * d.mu[c] + d.pol * efd;
+        const double dd = (iter == 1) ? mn[c] : mn[c] - d.mu[c];
         av[0] += dd * dd;
-        av[1] += mn[c] * efq[c];
+        av[1] += mn[c] * d.efq[c];
         kp.dip[3 * gs + c] = mn[c];
         kp.Efdr[3 * gs + c] = 0.0;
     }
     if (kp.dipf) kp.dipf[gs] = make_float4((float)mn[0], (float)mn[1], (float)mn[2], 0.f);
+}
+PIMD_D void dd_sor_site(const KP &kp, int b, int s, const double (&E)[3], int iter, double (&av)[2]) {
+    DdSite d;
+    dd_sor_load(kp, b, s, d);
+    dd_sor_apply(kp, b, s, d, E, iter, av);
 }
 
 // End of a dipole-update block: its sums go into the bead's acc[ACC_DSQ], acc[ACC_MUEFQ] (when

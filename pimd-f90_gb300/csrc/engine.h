@@ -164,7 +164,7 @@ struct Engine {
     const float *d_tckzv = nullptr;   // FP32 k_z component by kz + lmax
     bool ff_tc = true;                // tensor-core dipole field pass (k_field_tc) when tf_ready
     bool tf_ready = false;
-    int tf_nr = 0, tf_jm = 0, tf_ncol = 0, tf_kq = 0;
+    int tf_nr = 0, tf_nph = 0, tf_jm = 0, tf_ncol = 0, tf_kq = 0;
     const int2 *d_tfkpm = nullptr;    // per (run slot, j): k-vectors of kz = +j, -j
     alignas(64) unsigned char tc_map[128];  // CUtensorMap of the FP32 tables tabf
     size_t cap = 0;

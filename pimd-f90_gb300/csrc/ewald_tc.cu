@@ -531,12 +531,14 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
 //   T0 = sum_j (Wp.x c_j - Wm.y s_j) + i (Wp.y c_j + Wm.x s_j)
 //   T1 = sum_j k_z(j) [(Wm.x c_j - Wp.y s_j) + i (Wm.y c_j + Wp.x s_j)]
 // so T0, T1 of every run at every site are one GEMM per bead,
-//   D[s][(run, T0re|T0im|T1re|T1im)] = sum_q Q[s][q] V[(run, comp)][q],  q = (j, cos|sin),
-// with the sites on M (128 per CTA), 4 columns per run on N and only 2 (max |kz| + 1) terms on
-// K (FP16 hi + lo split, three MMAs per 16-term K step). V is built by every CTA of a bead from
+//   D[s][(run, comp)] = sum_q Q[s][q] V[(run, comp)][q],  comp = T0re|T0im|T1re|T1im,  q = (j, cos|sin),
+// with the sites on M (128 per CTA), runs x components on N (two passes of half the runs, each
+// component-major in <= 512 TMEM columns) and only 2 (max |kz| + 1) terms on K (FP16 hi + lo
+// split, three MMAs per 16-term K step). V is built by every CTA of a bead from
 // the bead's weights Wf (one bulk copy into shared memory; scaled by 2^10, exact, to keep small
 // weights normal in FP16). The epilogue contracts each TMEM row with exy(s, run) from the
-// TMA-staged tables (16 warps = 4 lane quarters x 4 run quarters), then applies the iteration's
+// TMA-staged tables (16 warps = 4 lane quarters x 4 run quarters, 16 runs x 4 components per
+// TMEM wait), then applies the iteration's
 // FP64 SOR update at the CTA's dipole sites and the convergence test in the last CTA
 // (dipole_check.cuh, as k_field_finish<F_D> does).
 constexpr int TF_NT = 512;
@@ -548,7 +550,7 @@ struct TfArgs {
     const float2 *skv;    // per run slot: FP32 (k_x, k_y)
     const int2 *kpm;      // per (slot, j): k-vector of kz = +j and of kz = -j (-1: none)
     const float *kzv;     // k_z by kz + lmax
-    int nr, ncol, kq, jm; // runs, V rows (4 nr rounded to 16), K terms (multiple of 16), kz rows
+    int nr, nph, ncol, kq, jm;  // runs, runs per pass (rounded up to 8), V rows (8 nph), K terms (x16), kz rows
     int sbase, s_lo, s_hi;
 };
 
@@ -563,26 +565,12 @@ struct TfSmem {
     }
 };
 
-// byte offset of half q of row n in a K-major operand of kq halves (kq / 8 core matrices along K)
-PIMD_D int hoff(int n, int q, int kcm) { return (((n >> 3) * kcm + (q >> 3)) << 7) + ((n & 7) << 4) + ((q & 7) << 1); }
-PIMD_D uint32_t pack_h2(float a, float b, float &ra, float &rb) {
-    const __half2 h = __floats2half2_rn(a, b);
-    const float2 f = __half22float2(h);
-    ra = a - f.x;
-    rb = b - f.y;
-    return *reinterpret_cast<const uint32_t *>(&h);
-}
-// (a, b) -> hi, lo half pairs
-PIMD_D void split2_h(float a, float b, uint32_t &hi, uint32_t &lo) {
-    float ra, rb;
-    hi = pack_h2(a, b, ra, rb);
-    const __half2 l = __floats2half2_rn(ra, rb);
-    lo = *reinterpret_cast<const uint32_t *>(&l);
-}
+// byte offset of the 16-byte chunk jc (halves 8 jc .. 8 jc + 7) of row n in a K-major operand
+// with kcm core matrices along K
+PIMD_D int rowchunk_k(int n, int jc, int kcm) { return (((n >> 3) * kcm + jc) << 7) + ((n & 7) << 4); }
 
 __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ CUtensorMap tmap, KP kp, TfArgs a) {
     const int t = blockIdx.x, b = blockIdx.y;
-    const int iter = kp.dstep[1] + 1;  // dipole iteration of this update
     if (kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) {
         // converged bead: no update, but the block still counts towards the convergence test
         const double zero[2] = {0.0, 0.0};
@@ -598,23 +586,11 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     __shared__ int4 sslot[TC_MAXRUN];
     __shared__ float2 sskv[TC_MAXRUN];
     const int sb = a.sbase + t * TF_SITES;
-    const int kcm = a.kq / 8, nr = a.nr, jm = a.jm;
-    const int yrow = kp.hmax + 1, zrow = yrow + kp.kmax + 1;
-    if (tid < nr) {
-        sslot[tid] = a.slot[tid];
-        sskv[tid] = make_float2(a.skv[tid].x * (1.f / TF_WS), a.skv[tid].y * (1.f / TF_WS));
-    }
-    if (warp == 0) umma::tmem_alloc(&tslot, 512);
+    // the copies go out first: the bead's weights (one bulk copy) and the tables of 128 sites
     if (tid == 0) {
         umma::mbar_init(&tbar, 1);
         umma::mbar_init(&wbar, 1);
         umma::mbar_init(&mbar, 1);
-    }
-    umma::fence_before_sync();
-    __syncthreads();
-    umma::fence_after_sync();
-    const uint32_t tm = tslot;
-    if (tid == 0) {
         const uint32_t wbytes = (uint32_t)kp.nk * 8u;
         mbar_expect_tx(&wbar, wbytes);
         bulk_load(sm + L.W, kp.Wf + ((size_t)b * 2 + 1) * kp.nk, wbytes, &wbar);
@@ -622,77 +598,103 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         mbar_expect_tx(&tbar, 8 * box_tx);
         for (int i = 0; i < 8; i++) tma_load_2d(sm + i * L.boxb, &tmap, 2 * (sb + 16 * i), b * kp.ntab, &tbar);
     }
+    const int iter = kp.dstep[1] + 1;  // dipole iteration of this update
+    const int kcm = a.kq / 8, nr = a.nr, nph = a.nph, jm = a.jm;
+    const int yrow = kp.hmax + 1, zrow = yrow + kp.kmax + 1;
+    if (tid < nr) {
+        sslot[tid] = a.slot[tid];
+        sskv[tid] = make_float2(a.skv[tid].x * (1.f / TF_WS), a.skv[tid].y * (1.f / TF_WS));
+    }
+    if (warp == 0) umma::tmem_alloc(&tslot, 512);
+    // the SOR inputs of the CTA's dipole sites, fetched now
+    const int s_own = sb + tid;
+    const bool own = tid < TF_SITES && s_own >= a.s_lo && s_own < a.s_hi;
+    DdSite din;
+    if (own) dd_sor_load(kp, b, s_own, din);
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tm = tslot;
     unsigned char *Vh = sm + L.B, *Vl = Vh + a.ncol * a.kq * 2;
     unsigned char *Qh = sm + L.A, *Ql = Qh + TF_SITES * a.kq * 2;
-    const int kpad = (a.kq - 2 * jm) / 2;
-    // zero padding: V rows >= 4 nr, V and Q halves >= 2 jm
-    for (int it = tid; it < (a.ncol - 4 * nr) * (a.kq / 2); it += TF_NT) {
-        const int n = 4 * nr + it / (a.kq / 2), q = 2 * (it % (a.kq / 2));
-        *reinterpret_cast<uint32_t *>(Vh + hoff(n, q, kcm)) = 0u;
-        *reinterpret_cast<uint32_t *>(Vl + hoff(n, q, kcm)) = 0u;
-    }
-    for (int it = tid; it < 4 * nr * kpad; it += TF_NT) {
-        const int n = it / kpad, q = 2 * jm + 2 * (it % kpad);
-        *reinterpret_cast<uint32_t *>(Vh + hoff(n, q, kcm)) = 0u;
-        *reinterpret_cast<uint32_t *>(Vl + hoff(n, q, kcm)) = 0u;
-    }
-    for (int it = tid; it < TF_SITES * kpad; it += TF_NT) {
-        const int n = it / kpad, q = 2 * jm + 2 * (it % kpad);
-        *reinterpret_cast<uint32_t *>(Qh + hoff(n, q, kcm)) = 0u;
-        *reinterpret_cast<uint32_t *>(Ql + hoff(n, q, kcm)) = 0u;
-    }
-    // V = the run weights: rows 4 p + comp, halves (2 j, 2 j + 1)
+    // V = the run weights: run p = pass nph + pl, component c at row pass 4 nph + c nph + pl;
+    // 8 halves (4 j) per item, zero for p >= nr and j >= jm
     uint32_t err = (uint32_t)umma::mbar_wait(&wbar, 0, TC_WAIT);
     const float2 *W = reinterpret_cast<const float2 *>(sm + L.W);
-    for (int it = tid; it < nr * jm; it += TF_NT) {
-        const int p = it / jm, j = it - p * jm;
-        const int2 km = a.kpm[it];
-        const float2 wpl = km.x >= 0 ? W[km.x] : make_float2(0.f, 0.f);
-        const float2 wmi = km.y >= 0 ? W[km.y] : make_float2(0.f, 0.f);
-        const float2 wp = make_float2(TF_WS * (wpl.x + wmi.x), TF_WS * (wpl.y + wmi.y));
-        const float2 wm = make_float2(TF_WS * (wpl.x - wmi.x), TF_WS * (wpl.y - wmi.y));
-        const float kz = a.kzv[kp.lmax + j];
-        // (cos, sin) coefficients of T0re, T0im, T1re, T1im
-        const float cv[4][2] = {{wp.x, -wm.y}, {wp.y, wm.x}, {kz * wm.x, -kz * wp.y}, {kz * wm.y, kz * wp.x}};
+    for (int it = tid; it < 2 * nph * kcm; it += TF_NT) {
+        const int p = it % (2 * nph), jc = it / (2 * nph);
+        const int vrow = (p / nph) * 4 * nph + (p % nph);
+        float v[4][8];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int j = 4 * jc + e;
+            float2 wp = make_float2(0.f, 0.f), wm = wp;
+            float kz = 0.f;
+            if (p < nr && j < jm) {
+                const int2 km = a.kpm[p * jm + j];
+                const float2 wpl = km.x >= 0 ? W[km.x] : make_float2(0.f, 0.f);
+                const float2 wmi = km.y >= 0 ? W[km.y] : make_float2(0.f, 0.f);
+                wp = make_float2(TF_WS * (wpl.x + wmi.x), TF_WS * (wpl.y + wmi.y));
+                wm = make_float2(TF_WS * (wpl.x - wmi.x), TF_WS * (wpl.y - wmi.y));
+                kz = a.kzv[kp.lmax + j];
+            }
+            // (cos, sin) coefficients of T0re, T0im, T1re, T1im
+            v[0][2 * e] = wp.x;
+            v[0][2 * e + 1] = -wm.y;
+            v[1][2 * e] = wp.y;
+            v[1][2 * e + 1] = wm.x;
+            v[2][2 * e] = kz * wm.x;
+            v[2][2 * e + 1] = -kz * wp.y;
+            v[3][2 * e] = kz * wm.y;
+            v[3][2 * e + 1] = kz * wp.x;
+        }
 #pragma unroll
         for (int c = 0; c < 4; c++) {
-            uint32_t hi, lo;
-            split2_h(cv[c][0], cv[c][1], hi, lo);
-            const int o = hoff(4 * p + c, 2 * j, kcm);
-            *reinterpret_cast<uint32_t *>(Vh + o) = hi;
-            *reinterpret_cast<uint32_t *>(Vl + o) = lo;
+            uint4 hi, lo;
+            split8_h(v[c], hi, lo);
+            const int o = rowchunk_k(vrow + c * nph, jc, kcm);
+            *reinterpret_cast<uint4 *>(Vh + o) = hi;
+            *reinterpret_cast<uint4 *>(Vl + o) = lo;
         }
     }
+    // Q = ez rows of the CTA's sites, 8 halves (4 j: c_j, s_j) per item, zero for j >= jm
     err |= (uint32_t)umma::mbar_wait(&tbar, 0, TC_WAIT);
-    // Q = ez rows of the CTA's sites: halves (2 j, 2 j + 1) = (c_j, s_j)
-    for (int it = tid; it < TF_SITES * jm; it += TF_NT) {
-        const int s = it % TF_SITES, j = it / TF_SITES;
-        const float2 z = tab_elem(sm, L.boxb, zrow + j, s);
-        uint32_t hi, lo;
-        split2_h(z.x, z.y, hi, lo);
-        const int o = hoff(s, 2 * j, kcm);
-        *reinterpret_cast<uint32_t *>(Qh + o) = hi;
-        *reinterpret_cast<uint32_t *>(Ql + o) = lo;
+    for (int it = tid; it < TF_SITES * kcm; it += TF_NT) {
+        const int s = it % TF_SITES, jc = it / TF_SITES;
+        float v[8];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int j = 4 * jc + e;
+            const float2 z = j < jm ? tab_elem(sm, L.boxb, zrow + j, s) : make_float2(0.f, 0.f);
+            v[2 * e] = z.x;
+            v[2 * e + 1] = z.y;
+        }
+        uint4 hi, lo;
+        split8_h(v, hi, lo);
+        const int o = rowchunk_k(s, jc, kcm);
+        *reinterpret_cast<uint4 *>(Qh + o) = hi;
+        *reinterpret_cast<uint4 *>(Ql + o) = lo;
     }
     umma::fence_smem_to_async();
     umma::fence_before_sync();
     const bool bad0 = __syncthreads_or((int)err) != 0;
     umma::fence_after_sync();
-    // two passes of <= 512 TMEM columns (N tiles of 256 V rows = 64 runs)
-    const int ntile = (a.ncol + 255) / 256;
+    // two passes of nph runs, 4 nph <= 512 TMEM columns each: column c nph + pl for component c
+    // of the pass's run pl
     float Ex = 0.f, Ey = 0.f, Ez = 0.f;
     const int lq = warp & 3, part = warp >> 2, sl = 32 * lq + lane;
+    const int q4 = nph / 4;  // runs per run quarter
     bool bad = bad0;
-    for (int pass = 0; pass * 2 < ntile && !bad; pass++) {
+    for (int pass = 0; pass < 2 && !bad; pass++) {
         if (tid == 0) {
             const uint32_t idesc_base = umma::idesc_f16(128, 16) & ~(0x3Fu << 17);
             const uint32_t qh = umma::smem_u32(Qh), ql = umma::smem_u32(Ql);
             const uint32_t vh = umma::smem_u32(Vh), vl = umma::smem_u32(Vl);
-            for (int nt = 2 * pass; nt < min(ntile, 2 * pass + 2); nt++) {
-                const int N = min(256, a.ncol - 256 * nt);
+            for (int c0 = 0; c0 < 4 * nph; c0 += 256) {
+                const int N = min(256, 4 * nph - c0);
                 const uint32_t id = idesc_base | ((uint32_t)(N >> 3) << 17);
-                const uint32_t d = tm + (uint32_t)(256 * (nt - 2 * pass));
-                const uint32_t vo = (uint32_t)(nt * 32 * kcm * 128);  // 256 rows = 32 row groups
+                const uint32_t d = tm + (uint32_t)c0;
+                const uint32_t vo = (uint32_t)(((pass * 4 * nph + c0) >> 3) * kcm * 128);  // row group of V
                 for (int ks = 0; ks < a.kq / 16; ks++) {
                     const uint64_t dq_h = umma::sdesc(qh + ks * 256, 128, kcm * 128), dq_l = umma::sdesc(ql + ks * 256, 128, kcm * 128);
                     const uint64_t dv_h = umma::sdesc(vh + vo + ks * 256, 128, kcm * 128), dv_l = umma::sdesc(vl + vo + ks * 256, 128, kcm * 128);
@@ -709,25 +711,25 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         umma::fence_after_sync();
         bad = __syncthreads_or(to) != 0;
         if (bad) break;
-        // runs of this pass: 128 (4 run quarters of 32), two per 8-column TMEM load
-        const int r0 = 128 * pass;
-        for (int pp = 0; pp < 32; pp += 2) {
-            const int p = r0 + 32 * part + pp;
-            if (p >= nr) break;
-            float v[8];
-            umma::tmem_ld8(tm + ((uint32_t)(32 * lq) << 16) + (uint32_t)(4 * (p - r0)), v);
+        // this warp's run quarter in groups of 16 runs x 4 components (one TMEM wait each)
+        for (int pl0 = part * q4; pl0 < (part + 1) * q4; pl0 += 16) {
+            if (pass * nph + pl0 >= nr) break;
+            float v[64];
+            const uint32_t tl = tm + ((uint32_t)(32 * lq) << 16) + (uint32_t)pl0;
+            umma::tmem_ld16x4(tl, tl + (uint32_t)nph, tl + (uint32_t)(2 * nph), tl + (uint32_t)(3 * nph), v);
 #pragma unroll
-            for (int e = 0; e < 2; e++) {
-                if (p + e >= nr) break;
-                const int kxy = sslot[p + e].x, kx = kxy & 255, ky = (kxy >> 8) - 128;
+            for (int e = 0; e < 16; e++) {
+                const int pl = pl0 + e, p = pass * nph + pl;
+                if (pl >= (part + 1) * q4 || p >= nr) break;
+                const int kxy = sslot[p].x, kx = kxy & 255, ky = (kxy >> 8) - 128;
                 const float2 ex = tab_elem(sm, L.boxb, kx, sl);
                 float2 ey = tab_elem(sm, L.boxb, yrow + (ky < 0 ? -ky : ky), sl);
                 if (ky < 0) ey.y = -ey.y;
                 // ewald.f90:30-31: coskxky = cx cy - sx sy, sinkxky = sx cy + cx sy
                 const float er = ex.x * ey.x - ex.y * ey.y, ei = ex.y * ey.x + ex.x * ey.y;
-                const float t0 = fmaf(er, v[4 * e + 1], ei * v[4 * e + 0]);  // Im(exy T0)
-                const float t1 = fmaf(er, v[4 * e + 3], ei * v[4 * e + 2]);  // Im(exy T1)
-                const float2 kv = sskv[p + e];
+                const float t0 = fmaf(er, v[16 + e], ei * v[e]);       // Im(exy T0)
+                const float t1 = fmaf(er, v[48 + e], ei * v[32 + e]);  // Im(exy T1)
+                const float2 kv = sskv[p];
                 Ex = fmaf(kv.x, t0, Ex);
                 Ey = fmaf(kv.y, t0, Ey);
                 Ez = fmaf(1.f / TF_WS, t1, Ez);
@@ -737,7 +739,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         __syncthreads();
         umma::fence_after_sync();
     }
-    // the four run quarters of each site, in order; k-slice 0 of Fpart
+    // the four run quarters of each site, in order
     float *red = reinterpret_cast<float *>(Qh);  // [4][128][3]
     red[(part * TF_SITES + sl) * 3 + 0] = Ex;
     red[(part * TF_SITES + sl) * 3 + 1] = Ey;
@@ -751,17 +753,14 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     }
     // the iteration's FP64 SOR update at the CTA's dipole sites, then the block's end
     double av[2] = {0.0, 0.0};
-    if (tid < TF_SITES && !bad) {
-        const int s = sb + tid;
-        if (s >= a.s_lo && s < a.s_hi) {
-            float e[3] = {0.f, 0.f, 0.f};
+    if (own && !bad) {
+        float e[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-            for (int q4 = 0; q4 < 4; q4++)
+        for (int q4 = 0; q4 < 4; q4++)
 #pragma unroll
-                for (int c = 0; c < 3; c++) e[c] += red[(q4 * TF_SITES + tid) * 3 + c];
-            const double E[3] = {(double)e[0], (double)e[1], (double)e[2]};
-            dd_sor_site(kp, b, s, E, iter, av);
-        }
+            for (int c = 0; c < 3; c++) e[c] += red[(q4 * TF_SITES + tid) * 3 + c];
+        const double E[3] = {(double)e[0], (double)e[1], (double)e[2]};
+        dd_sor_apply(kp, b, s_own, din, E, iter, av);
     }
     if (bad && tid == 0) atomicOr(kp.err, 8u);
     dd_block_end<TF_NT>(kp, b, av, !bad);
@@ -910,7 +909,10 @@ void tc_init(Engine &E) {
     E.tf_ready = false;
     if (groups.size() != 1) return;
     const int nr = groups[0].nr, jm = groups[0].jm;
-    const int ncolf = ((4 * nr + 15) / 16) * 16, kq = ((2 * jm + 15) / 16) * 16;
+    // two passes of nph runs (a multiple of 8) x 4 components in TMEM, plus the columns the last
+    // 16-run load of a run quarter reaches past the pass
+    const int nph = ((nr + 1) / 2 + 7) / 8 * 8, ncolf = 8 * nph, kq = ((2 * jm + 15) / 16) * 16;
+    if (4 * nph + 16 > 512) return;
     cudaFuncAttributes fb;
     if (cudaFuncGetAttributes(&fb, k_field_tc) != cudaSuccess) {
         cudaGetLastError();
@@ -942,6 +944,7 @@ void tc_init(Engine &E) {
     cudaMemcpy(d_kpm, kpm.data(), sizeof(int2) * kpm.size(), cudaMemcpyHostToDevice);
     E.d_tfkpm = d_kpm;
     E.tf_nr = nr;
+    E.tf_nph = nph;
     E.tf_jm = jm;
     E.tf_ncol = ncolf;
     E.tf_kq = kq;
@@ -959,6 +962,7 @@ int launch_field_tc(Engine &E, int s0, int s1) {
     a.kpm = E.d_tfkpm;
     a.kzv = E.d_tckzv;
     a.nr = E.tf_nr;
+    a.nph = E.tf_nph;
     a.ncol = E.tf_ncol;
     a.kq = E.tf_kq;
     a.jm = E.tf_jm;
