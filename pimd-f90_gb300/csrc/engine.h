@@ -156,6 +156,7 @@ struct Engine {
     // tensor-core (tcgen05, 3xTF32) dipole structure factor of the mixed engine (ewald_tc.cu)
     bool sf_tc = true;        // use it when tc_ready
     bool tc_ready = false;    // run groups built and the table tensor map encoded
+    bool tc_dip_ok = false;   // the dipole-component sums (three partials per k) fit too
     int tc_ntg = 0, tc_ncolmax = 0, tc_nabuf = 0;
     const int4 *d_tcslot = nullptr;   // per run slot: run, local k offset, kzlo, nkz
     const float2 *d_tcskv = nullptr;  // per run slot: FP32 (k_x, k_y)
@@ -274,12 +275,14 @@ void launch_ewald_fq(Engine &E);
 void launch_ewald_smu(Engine &E);
 void launch_ewald_qd(Engine &E);
 void launch_ewald_pw(Engine &E);
-// tensor-core structure factor (ewald_tc.cu): setup once per context; per call the launch
-// writes Sm and the dipole weights Wf and returns 1, or returns 0 (not applicable)
+// tensor-core structure factors (ewald_tc.cu): setup once per context; per call the launch
+// writes the sums of op (OP_Q: Sq + charge weights, OP_MU: Sm + dipole weights, OP_DIP: Sdip)
+// and returns 1, or returns 0 (not applicable)
 void tc_init(Engine &E);
-int launch_sfac_tc(Engine &E, int s0, int nsites, int skipconv);
-// tensor-core dipole field, SOR update and convergence test (ewald_tc.cu); 1 when launched
-int launch_field_tc(Engine &E, int s0, int s1);
+int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv);
+// tensor-core field passes (ewald_tc.cu): mode F_D (dipole field, SOR update, convergence test)
+// or F_Q (charge field and potential into F); 1 when launched
+int launch_field_tc(Engine &E, int mode, int s0, int s1);
 // launchers (spc.cu): q-SPC/Fw and SPC/F
 void launch_sites_spc(Engine &E);
 void launch_pair_spc(Engine &E);

@@ -887,10 +887,8 @@ static void run_sfac_f(Engine &E, int s0, int nsites, int skipconv) {
 
 template <int OP>
 static void run_spass(Engine &E, int s0, int nsites, int skipconv) {
-    if (OP == OP_MU && E.precision == PIMD_PREC_MIXED) {
-        // tensor-core structure factor (ewald_tc.cu), which also writes Sm and Wf
-        if (launch_sfac_tc(E, s0, nsites, skipconv)) return;
-    }
+    // tensor-core structure factors (ewald_tc.cu), which also write Sq/Sm/Sdip and the weights
+    if (E.precision == PIMD_PREC_MIXED && launch_sfac_tc(E, OP, s0, nsites, skipconv)) return;
     if (E.precision == PIMD_PREC_MIXED) {
         if (E.sf_tiled && E.sf_nkg_max * SF_RT <= SF_MAXT)
             run_sfac_f<OP>(E, s0, nsites, skipconv);
@@ -968,8 +966,9 @@ static void launch_field_f(Engine &E, int s0, int s1) {
 template <int MODE>
 static void run_field(Engine &E, int s0, int s1) {
     const int LZ = 2 * E.kp.lmax + 1;
-    // tensor-core field pass with the SOR update and convergence test (ewald_tc.cu)
-    if (MODE == F_D && E.precision == PIMD_PREC_MIXED && launch_field_tc(E, s0, s1)) return;
+    // tensor-core field passes (ewald_tc.cu): dipole field with the SOR update and convergence
+    // test, and the charge field and potential
+    if (MODE != F_QD && E.precision == PIMD_PREC_MIXED && launch_field_tc(E, MODE, s0, s1)) return;
     if (E.precision == PIMD_PREC_MIXED && E.ff_regs && LZ <= 49) {
         if (LZ <= 17)
             launch_field_f<MODE, 17>(E, s0, s1);

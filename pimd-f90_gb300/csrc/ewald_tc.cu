@@ -67,6 +67,11 @@ constexpr int TC_CH = 64;                 // runs per epilogue chunk
 constexpr int TC_LD = 2 * TC_CH + 4;      // staging row pitch (floats)
 constexpr long long TC_WAIT = 1LL << 28;  // cycles before a wait gives up (~0.13 s)
 
+// structure-factor sums (values as in ewald.cu): charge q e, dipole (k.mu) e, dipole components mu_c e
+enum { TC_OP_Q = 0, TC_OP_MU = 1, TC_OP_DIP = 2 };
+// field passes (values as in ewald.cu): charge field and potential, dipole field + SOR update
+enum { TF_Q = 0, TF_D = 1 };
+
 struct TcGroup {
     int p0, nr, ncol, jm, nkl, kgoff, pad0, pad1;  // slots, runs, MMA columns, kz rows, k-vectors
 };
@@ -174,7 +179,11 @@ PIMD_D void split8_h(const float (&x)[8], uint4 &hi, uint4 &lo) {
 // FP16 sites (two core matrices along K)
 PIMD_D int rowchunk(int n, int c) { return (((n >> 3) * 2 + c) << 7) + ((n & 7) << 4); }
 
+template <int OP>
 __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CUtensorMap tmap, KP kp, TcArgs a) {
+    // Z components: q (charges) or mu_x, mu_y, mu_z; partial sums per k: S, or the three G_c
+    constexpr int NCZ = (OP == TC_OP_Q) ? 1 : 3;
+    constexpr int NPT = (OP == TC_OP_DIP) ? 3 : 1;
     const int grp = blockIdx.x, tg = blockIdx.y, b = blockIdx.z;
     // the whole cluster (same bead) leaves together
     if (a.skipconv && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
@@ -214,7 +223,8 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
         mbar_expect_tx(&tfull[tb], 2 * box_tx + mub);
         tma_load_2d(dst, &tmap, 2 * sfirst, b * kp.ntab, &tfull[tb]);
         tma_load_2d(dst + L.boxb, &tmap, 2 * sfirst + 32, b * kp.ntab, &tfull[tb]);
-        bulk_load(dst + L.mu, kp.dipf + (size_t)b * kp.S + sfirst, mub, &tfull[tb]);
+        const float4 *wsrc = (OP == TC_OP_Q) ? kp.posf : kp.dipf;  // (offset, q) or (mu, 0)
+        bulk_load(dst + L.mu, wsrc + (size_t)b * kp.S + sfirst, mub, &tfull[tb]);
     };
     if (tid == 0) {
         for (int i = 0; i < TC_NST; i++) {
@@ -230,12 +240,12 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
         for (int ts = 0; ts < min(nstage, TC_NST); ts++) issue_stage(ts);
     }
     {   // padding stays zero in every buffer (hi and lo): Z rows >= 6 jm, X rows >= 2 nr
-        const int zp = 128 - 6 * jm, xp = G.ncol - 2 * nr;
+        const int zp = 128 - 2 * NCZ * jm, xp = G.ncol - 2 * nr;
         for (int i = tid; i < nab * 2 * (zp + xp) * 2; i += TC_NT) {
             const int q = i & 1, rr = i >> 1;
             const int row = rr % (zp + xp), hl = (rr / (zp + xp)) & 1, bi = rr / (2 * (zp + xp));
             unsigned char *B0 = sm + L.buf + bi * L.bufstride;
-            unsigned char *dst = row < zp ? B0 + hl * 128 * 32 + rowchunk(6 * jm + row, q)
+            unsigned char *dst = row < zp ? B0 + hl * 128 * 32 + rowchunk(2 * NCZ * jm + row, q)
                                           : B0 + L.xoff + hl * a.ncolmax * 32 + rowchunk(2 * nr + row - zp, q);
             *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
@@ -269,7 +279,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
         }
         // Z items: one row (c, j, cos|sin) x 8 sites each, on the whole warps after the X items
         // (else on the last warp), at most TC_ZMAX per thread; row decoded once here
-        const int nzi = 6 * jm * 2;
+        const int nzi = 2 * NCZ * jm * 2;
         const int zwarps = max(1, TC_NB - (2 * nr + 31) / 32), zthreads = 32 * zwarps, zbase = 32 * TC_NB - zthreads;
         int zn = 0, zoff[TC_ZMAX], zmo[TC_ZMAX], zer[TC_ZMAX], zcs[TC_ZMAX], zq[TC_ZMAX];
 #pragma unroll
@@ -387,9 +397,13 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
                 const float4 m = reinterpret_cast<const float4 *>(dst + L.mu)[lane];
                 const bool in = s >= a.s_lo && s < g1;
                 float *muz = reinterpret_cast<float *>(dst + L.muz);
-                muz[lane] = in ? TC_ZS * m.x : 0.f;
-                muz[TC_SS + lane] = in ? TC_ZS * m.y : 0.f;
-                muz[2 * TC_SS + lane] = in ? TC_ZS * m.z : 0.f;
+                if (OP == TC_OP_Q) {
+                    muz[lane] = in ? TC_ZS * m.w : 0.f;
+                } else {
+                    muz[lane] = in ? TC_ZS * m.x : 0.f;
+                    muz[TC_SS + lane] = in ? TC_ZS * m.y : 0.f;
+                    muz[2 * TC_SS + lane] = in ? TC_ZS * m.z : 0.f;
+                }
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&mfull[tb]);
@@ -456,9 +470,9 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
             const bool plus = j >= sl.z && j < sl.z + sl.w;
             const bool minus = j > 0 && -j >= sl.z && -j < sl.z + sl.w;
             if (!plus && !minus) continue;
-            float2 gp[3], gm[3];
+            float2 gp[NCZ], gm[NCZ];
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
+            for (int c = 0; c < NCZ; c++) {
                 const int rc = (c * jm + j) * 2;
                 // (x, y) = (Re exy, Im exy) against mu_c c_j (row rc) and mu_c s_j (row rc + 1)
                 const float2 dc = *reinterpret_cast<const float2 *>(stg + rc * TC_LD + 2 * q);
@@ -466,17 +480,26 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
                 gp[c] = make_float2(dc.x - ds.y, ds.x + dc.y);
                 gm[c] = make_float2(dc.x + ds.y, dc.y - ds.x);
             }
-            const float2 kv = make_float2(sskv[p].x * (1.f / TC_ZS), sskv[p].y * (1.f / TC_ZS));
-            const float kzs = 1.f / TC_ZS;
-            if (plus) {
-                const float kz = skz[kp.lmax + j] * kzs;
-                pt[sl.y + j - sl.z] = make_float2(fmaf(kz, gp[2].x, fmaf(kv.y, gp[1].x, kv.x * gp[0].x)),
-                                                  fmaf(kz, gp[2].y, fmaf(kv.y, gp[1].y, kv.x * gp[0].y)));
-            }
-            if (minus) {
-                const float kz = skz[kp.lmax - j] * kzs;
-                pt[sl.y - j - sl.z] = make_float2(fmaf(kz, gm[2].x, fmaf(kv.y, gm[1].x, kv.x * gm[0].x)),
-                                                  fmaf(kz, gm[2].y, fmaf(kv.y, gm[1].y, kv.x * gm[0].y)));
+            const float zs = 1.f / TC_ZS;
+            if (OP == TC_OP_MU) {
+                const float2 kv = make_float2(sskv[p].x * zs, sskv[p].y * zs);
+                if (plus) {
+                    const float kz = skz[kp.lmax + j] * zs;
+                    pt[sl.y + j - sl.z] = make_float2(fmaf(kz, gp[NCZ - 1].x, fmaf(kv.y, gp[1 % NCZ].x, kv.x * gp[0].x)),
+                                                      fmaf(kz, gp[NCZ - 1].y, fmaf(kv.y, gp[1 % NCZ].y, kv.x * gp[0].y)));
+                }
+                if (minus) {
+                    const float kz = skz[kp.lmax - j] * zs;
+                    pt[sl.y - j - sl.z] = make_float2(fmaf(kz, gm[NCZ - 1].x, fmaf(kv.y, gm[1 % NCZ].x, kv.x * gm[0].x)),
+                                                      fmaf(kz, gm[NCZ - 1].y, fmaf(kv.y, gm[1 % NCZ].y, kv.x * gm[0].y)));
+                }
+            } else {
+                // charges: S itself; dipole components: the three G_c
+#pragma unroll
+                for (int c = 0; c < NPT; c++) {
+                    if (plus) pt[NPT * (sl.y + j - sl.z) + c] = make_float2(zs * gp[c].x, zs * gp[c].y);
+                    if (minus) pt[NPT * (sl.y - j - sl.z) + c] = make_float2(zs * gm[c].x, zs * gm[c].y);
+                }
             }
         }
         __syncthreads();
@@ -494,21 +517,31 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     if (!bad) {
         const uint32_t pbase = umma::smem_u32(pt);
         auto reduce_one = [&](int i, const TcKW &kw) {
-            float2 v[TC_CLMAX];
 #pragma unroll
-            for (int c = 0; c < TC_CLMAX; c++)
-                if (c < cn) v[c] = ld_cluster_f2(pbase + 8u * (uint32_t)i, (uint32_t)c);
-            // FP32 in a fixed order: FP64 arithmetic is slow on this part, and the partials carry
-            // only the split operands' ~2^-21 anyway
-            float sx = 0.f, sy = 0.f;
+            for (int e = 0; e < NPT; e++) {
+                float2 v[TC_CLMAX];
 #pragma unroll
-            for (int c = 0; c < TC_CLMAX; c++)
-                if (c < cn) {
-                    sx += v[c].x;
-                    sy += v[c].y;
+                for (int c = 0; c < TC_CLMAX; c++)
+                    if (c < cn) v[c] = ld_cluster_f2(pbase + 8u * (uint32_t)(NPT * i + e), (uint32_t)c);
+                // FP32 in a fixed order: FP64 arithmetic is slow on this part, and the partials
+                // carry only the split operands' ~2^-21 anyway
+                float sx = 0.f, sy = 0.f;
+#pragma unroll
+                for (int c = 0; c < TC_CLMAX; c++)
+                    if (c < cn) {
+                        sx += v[c].x;
+                        sy += v[c].y;
+                    }
+                if (OP == TC_OP_MU) {  // (-Im, Re) as the reference's rQm, iQm (ewald.f90:106-107)
+                    kp.Sm[(size_t)b * kp.nk + kw.k] = make_double2(-(double)sy, (double)sx);
+                    kp.Wf[((size_t)b * 2 + 1) * kp.nk + kw.k] = make_float2(-kw.w * sy, -kw.w * sx);
+                } else if (OP == TC_OP_Q) {
+                    kp.Sq[(size_t)b * kp.nk + kw.k] = make_double2((double)sx, (double)sy);
+                    kp.Wf[((size_t)b * 2) * kp.nk + kw.k] = make_float2(kw.w * sx, -kw.w * sy);
+                } else {
+                    kp.Sdip[((size_t)b * kp.nk + kw.k) * 3 + e] = make_double2((double)sx, (double)sy);
                 }
-            kp.Sm[(size_t)b * kp.nk + kw.k] = make_double2(-(double)sy, (double)sx);
-            kp.Wf[((size_t)b * 2 + 1) * kp.nk + kw.k] = make_float2(-kw.w * sy, -kw.w * sx);
+            }
         };
 #pragma unroll
         for (int u = 0; u < TC_PF; u++) {
@@ -569,9 +602,10 @@ struct TfSmem {
 // with kcm core matrices along K
 PIMD_D int rowchunk_k(int n, int jc, int kcm) { return (((n >> 3) * kcm + jc) << 7) + ((n & 7) << 4); }
 
+template <int MODE>
 __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ CUtensorMap tmap, KP kp, TfArgs a) {
     const int t = blockIdx.x, b = blockIdx.y;
-    if (kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) {
+    if (MODE == TF_D && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) {
         // converged bead: no update, but the block still counts towards the convergence test
         const double zero[2] = {0.0, 0.0};
         dd_block_end<TF_NT>(kp, b, zero, false);
@@ -593,7 +627,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         umma::mbar_init(&mbar, 1);
         const uint32_t wbytes = (uint32_t)kp.nk * 8u;
         mbar_expect_tx(&wbar, wbytes);
-        bulk_load(sm + L.W, kp.Wf + ((size_t)b * 2 + 1) * kp.nk, wbytes, &wbar);
+        bulk_load(sm + L.W, kp.Wf + ((size_t)b * 2 + (MODE == TF_D ? 1 : 0)) * kp.nk, wbytes, &wbar);
         const uint32_t box_tx = (uint32_t)(kp.ntab * 128);
         mbar_expect_tx(&tbar, 8 * box_tx);
         for (int i = 0; i < 8; i++) tma_load_2d(sm + i * L.boxb, &tmap, 2 * (sb + 16 * i), b * kp.ntab, &tbar);
@@ -610,7 +644,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     const int s_own = sb + tid;
     const bool own = tid < TF_SITES && s_own >= a.s_lo && s_own < a.s_hi;
     DdSite din;
-    if (own) dd_sor_load(kp, b, s_own, din);
+    if (MODE == TF_D && own) dd_sor_load(kp, b, s_own, din);
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
@@ -681,7 +715,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     umma::fence_after_sync();
     // two passes of nph runs, 4 nph <= 512 TMEM columns each: column c nph + pl for component c
     // of the pass's run pl
-    float Ex = 0.f, Ey = 0.f, Ez = 0.f;
+    float Ex = 0.f, Ey = 0.f, Ez = 0.f, phi = 0.f;
     const int lq = warp & 3, part = warp >> 2, sl = 32 * lq + lane;
     const int q4 = nph / 4;  // runs per run quarter
     bool bad = bad0;
@@ -733,6 +767,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
                 Ex = fmaf(kv.x, t0, Ex);
                 Ey = fmaf(kv.y, t0, Ey);
                 Ez = fmaf(1.f / TF_WS, t1, Ez);
+                if (MODE == TF_Q) phi = fmaf(1.f / TF_WS, fmaf(er, v[e], -ei * v[16 + e]), phi);  // Re(exy T0)
             }
         }
         umma::fence_before_sync();
@@ -740,10 +775,11 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         umma::fence_after_sync();
     }
     // the four run quarters of each site, in order
-    float *red = reinterpret_cast<float *>(Qh);  // [4][128][3]
-    red[(part * TF_SITES + sl) * 3 + 0] = Ex;
-    red[(part * TF_SITES + sl) * 3 + 1] = Ey;
-    red[(part * TF_SITES + sl) * 3 + 2] = Ez;
+    float *red = reinterpret_cast<float *>(Qh);  // [4][128][4]
+    red[(part * TF_SITES + sl) * 4 + 0] = Ex;
+    red[(part * TF_SITES + sl) * 4 + 1] = Ey;
+    red[(part * TF_SITES + sl) * 4 + 2] = Ez;
+    red[(part * TF_SITES + sl) * 4 + 3] = phi;
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 0) {
@@ -751,18 +787,33 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         umma::tmem_dealloc(tm, 512);
         umma::tmem_relinquish();
     }
+    float e[4] = {0.f, 0.f, 0.f, 0.f};
+    if (own && !bad) {
+#pragma unroll
+        for (int rq = 0; rq < 4; rq++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) e[c] += red[(rq * TF_SITES + tid) * 4 + c];
+    }
+    if (bad && tid == 0) atomicOr(kp.err, 8u);
+    if (MODE == TF_Q) {
+        // ewald.f90:45-49 as k_field_finish<F_Q>: Efq += E, phi += (charged sites)
+        if (own && !bad) {
+            const size_t gs = (size_t)b * kp.S + s_own;
+            double4_32a f = kp.F[gs];
+            f.x += (double)e[0];
+            f.y += (double)e[1];
+            f.z += (double)e[2];
+            if (s_own >= kp.fq) f.w += (double)e[3];
+            kp.F[gs] = f;
+        }
+        return;
+    }
     // the iteration's FP64 SOR update at the CTA's dipole sites, then the block's end
     double av[2] = {0.0, 0.0};
     if (own && !bad) {
-        float e[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-        for (int q4 = 0; q4 < 4; q4++)
-#pragma unroll
-            for (int c = 0; c < 3; c++) e[c] += red[(q4 * TF_SITES + tid) * 3 + c];
         const double E[3] = {(double)e[0], (double)e[1], (double)e[2]};
         dd_sor_apply(kp, b, s_own, din, E, iter, av);
     }
-    if (bad && tid == 0) atomicOr(kp.err, 8u);
     dd_block_end<TF_NT>(kp, b, av, !bad);
 }
 
@@ -848,12 +899,14 @@ void tc_init(Engine &E) {
     // dynamic shared memory available: the opt-in limit minus the kernel's static part
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, E.device);
-    cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, k_sfac_tc) != cudaSuccess) {
+    cudaFuncAttributes fa, fq, fd;
+    if (cudaFuncGetAttributes(&fa, k_sfac_tc<TC_OP_MU>) != cudaSuccess ||
+        cudaFuncGetAttributes(&fq, k_sfac_tc<TC_OP_Q>) != cudaSuccess ||
+        cudaFuncGetAttributes(&fd, k_sfac_tc<TC_OP_DIP>) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
-    const int dmax = optin - (int)fa.sharedSizeBytes;
+    const int dmax = optin - (int)std::max(fa.sharedSizeBytes, std::max(fq.sharedSizeBytes, fd.sharedSizeBytes));
     // operand buffers: three when they fit, else two
     int nabuf = TC_NABUF_MAX;
     while (nabuf > 2 && TcSmem(kp.ntab, ncolmax, nabuf).total > dmax) nabuf--;
@@ -861,10 +914,14 @@ void tc_init(Engine &E) {
     if (L.total > dmax) return;
     // the epilogue's staging tile and partial S reuse the table and operand regions
     if (128 * TC_LD * 4 + 8 * nklmax > L.total - 1024) return;
-    if (cudaFuncSetAttribute(k_sfac_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, dmax) != cudaSuccess) {
+    if (cudaFuncSetAttribute(k_sfac_tc<TC_OP_MU>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_sfac_tc<TC_OP_Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmax) != cudaSuccess ||
+        cudaFuncSetAttribute(k_sfac_tc<TC_OP_DIP>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmax) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
+    // the component sums keep three partials per k-vector
+    E.tc_dip_ok = 128 * TC_LD * 4 + 3 * 8 * nklmax <= L.total - 1024;
     int4 *d_slots = nullptr;
     float2 *d_skv = nullptr;
     TcGroup *d_groups = nullptr;
@@ -913,15 +970,16 @@ void tc_init(Engine &E) {
     // 16-run load of a run quarter reaches past the pass
     const int nph = ((nr + 1) / 2 + 7) / 8 * 8, ncolf = 8 * nph, kq = ((2 * jm + 15) / 16) * 16;
     if (4 * nph + 16 > 512) return;
-    cudaFuncAttributes fb;
-    if (cudaFuncGetAttributes(&fb, k_field_tc) != cudaSuccess) {
+    cudaFuncAttributes fb, fb2;
+    if (cudaFuncGetAttributes(&fb, k_field_tc<TF_D>) != cudaSuccess || cudaFuncGetAttributes(&fb2, k_field_tc<TF_Q>) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
-    const int dmaxf = optin - (int)fb.sharedSizeBytes;
+    const int dmaxf = optin - (int)std::max(fb.sharedSizeBytes, fb2.sharedSizeBytes);
     // the weights arrive by one bulk copy: 8 nk bytes, a multiple of 16
     if (TfSmem(kp.ntab, ncolf, kq, kp.nk).total > dmaxf || kp.ntab > 128 || (kp.nk & 1)) return;
-    if (cudaFuncSetAttribute(k_field_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess) {
+    if (cudaFuncSetAttribute(k_field_tc<TF_D>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess ||
+        cudaFuncSetAttribute(k_field_tc<TF_Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
@@ -951,9 +1009,10 @@ void tc_init(Engine &E) {
     E.tf_ready = true;
 }
 
-// Dipole field, SOR update and convergence test of one iteration at the dipole sites [s0, s1)
-// (k_field_f<F_D> + k_field_finish<F_D>); 1 when launched, else 0.
-int launch_field_tc(Engine &E, int s0, int s1) {
+// mode TF_D: dipole field, SOR update and convergence test of one iteration at the dipole sites
+// [s0, s1) (k_field_f<F_D> + k_field_finish<F_D>); TF_Q: charge field and potential added to F at
+// [s0, s1) (k_field_f<F_Q> + k_field_finish<F_Q>). 1 when launched, else 0.
+int launch_field_tc(Engine &E, int mode, int s0, int s1) {
     if (!E.tc_ready || !E.tf_ready || !E.ff_tc || s1 <= s0) return 0;
     const KP &kp = E.kp;
     TfArgs a;
@@ -972,14 +1031,18 @@ int launch_field_tc(Engine &E, int s0, int s1) {
     const TfSmem L(kp.ntab, a.ncol, a.kq, kp.nk);
     dim3 g((s1 - a.sbase + TF_SITES - 1) / TF_SITES, kp.P);
     const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(E.tc_map);
-    k_field_tc<<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
+    if (mode == TF_D)
+        k_field_tc<TF_D><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
+    else
+        k_field_tc<TF_Q><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
     ++E.nlaunch;
     return 1;
 }
 
-// Returns 1 when the launch wrote Sm and the dipole weights Wf (no k_sreduce needed), else 0.
-int launch_sfac_tc(Engine &E, int s0, int nsites, int skipconv) {
-    if (!E.tc_ready || !E.sf_tc || nsites <= 0) return 0;
+// Returns 1 when the launch wrote the structure factor of `op` (Sq and the charge weights, Sm
+// and the dipole weights, or Sdip; no k_sreduce needed), else 0.
+int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv) {
+    if (!E.tc_ready || !E.sf_tc || nsites <= 0 || (op == TC_OP_DIP && !E.tc_dip_ok)) return 0;
     const KP &kp = E.kp;
     TcArgs a;
     a.slot = E.d_tcslot;
@@ -1021,7 +1084,14 @@ int launch_sfac_tc(Engine &E, int s0, int nsites, int skipconv) {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(E.tc_map);
-    if (cudaLaunchKernelEx(&cfg, k_sfac_tc, *map, kp, a) != cudaSuccess) {
+    cudaError_t e = cudaErrorInvalidValue;
+    if (op == TC_OP_MU)
+        e = cudaLaunchKernelEx(&cfg, k_sfac_tc<TC_OP_MU>, *map, kp, a);
+    else if (op == TC_OP_Q)
+        e = cudaLaunchKernelEx(&cfg, k_sfac_tc<TC_OP_Q>, *map, kp, a);
+    else
+        e = cudaLaunchKernelEx(&cfg, k_sfac_tc<TC_OP_DIP>, *map, kp, a);
+    if (e != cudaSuccess) {
         cudaGetLastError();
         E.sf_tc = false;  // e.g. no room for the cluster: the FP32-pipe kernel from now on
         return 0;
