@@ -9,6 +9,7 @@
 // tests in FP32 and repeats the FP64 test only within 1e-4 of the cutoff, which gives the same
 // decisions. The mixed engine also builds the full list (all j != i) for its dipole gather.
 #include "engine.h"
+#include "umma.cuh"
 
 namespace pimd {
 
@@ -131,10 +132,17 @@ PIMD_D int block_exscan(int v, int *ex, int *wsum) {
     return total;
 }
 
+// One bead per thread-block cluster: CTA r of the cluster owns rows [r N / n, (r + 1) N / n) and
+// every CTA holds all N O sites in shared memory. Row offsets are the exclusive scan over the
+// bead's rows: within a CTA a block scan, across the cluster the totals of the lower-ranked CTAs
+// read from their shared memory, so the lists are the same whatever the cluster size.
 template <bool FULL>
 __global__ void __launch_bounds__(NB_MAXN) k_nbr_block(KP kp) {
     extern __shared__ double4_32a sO[];
-    const int N = kp.N, b = blockIdx.x;
+    const int ncl = (int)umma::cluster_size(), cr = (int)umma::cluster_rank();
+    const int N = kp.N, b = blockIdx.x / ncl;
+    const int r0 = cr * N / ncl, r1 = (cr + 1) * N / ncl;
+    __shared__ int ctot[2];
     float4 *sf = reinterpret_cast<float4 *>(sO + N);
     int *oh = reinterpret_cast<int *>(sf + N), *of = oh + N;
     __shared__ int wsum[32];
@@ -152,7 +160,7 @@ __global__ void __launch_bounds__(NB_MAXN) k_nbr_block(KP kp) {
     const float3 Lf = make_float3((float)kp.box[0], (float)kp.box[1], (float)kp.box[2]);
     const float3 Lif = make_float3((float)kp.boxi[0], (float)kp.boxi[1], (float)kp.boxi[2]);
     __syncthreads();
-    for (int i = w; i < N; i += nw) {
+    for (int i = r0 + w; i < r1; i += nw) {
         const float4 fi = sf[i];
         const double4_32a di = sO[i];
         int nh = 0, nf = 0;
@@ -169,31 +177,42 @@ __global__ void __launch_bounds__(NB_MAXN) k_nbr_block(KP kp) {
         }
     }
     __syncthreads();
-    // row offsets (N <= blockDim.x: one row per thread)
-    const int t = threadIdx.x;
-    int ch = (t < N) ? oh[t] : 0, cf = (t < N) ? of[t] : 0, eh, ef;
+    // row offsets (this CTA's rows <= blockDim.x: one row per thread), then the lower CTAs' totals
+    const int t = threadIdx.x, nrow = r1 - r0;
+    int ch = (t < nrow) ? oh[r0 + t] : 0, cf = (t < nrow) ? of[r0 + t] : 0, eh, ef = 0;
     const int toth = block_exscan(ch, &eh, wsum);
     const int totf = FULL ? block_exscan(cf, &ef, wsum) : 0;
-    if (t < N) {
-        oh[t] = eh;
-        kp.nbrtmp[(size_t)b * N + t] = eh;
+    if (t == 0) {
+        ctot[0] = toth;
+        ctot[1] = totf;
+    }
+    umma::cluster_barrier();
+    int bh = 0, bf = 0;
+    for (int c = 0; c < cr; c++) {
+        bh += umma::ld_cluster_s32(&ctot[0], (uint32_t)c);
+        if (FULL) bf += umma::ld_cluster_s32(&ctot[1], (uint32_t)c);
+    }
+    umma::cluster_barrier();  // the totals are read before any CTA of the cluster leaves
+    if (t < nrow) {
+        oh[r0 + t] = bh + eh;
+        kp.nbrtmp[(size_t)b * N + r0 + t] = bh + eh;
         if (FULL) {
-            of[t] = ef;
-            kp.foff[(size_t)b * N + t] = ef;
+            of[r0 + t] = bf + ef;
+            kp.foff[(size_t)b * N + r0 + t] = bf + ef;
         }
     }
-    if (t == 0) {
-        kp.npair[b] = min(toth, kp.cap);
-        if (toth > kp.cap) atomicOr(kp.err, 1u);
+    if (t == 0 && cr == ncl - 1) {
+        kp.npair[b] = min(bh + toth, kp.cap);
+        if (bh + toth > kp.cap) atomicOr(kp.err, 1u);
         if (FULL) {
-            kp.fntot[b] = min(totf, kp.fcap);
-            if (totf > kp.fcap) atomicOr(kp.err, 1u);
+            kp.fntot[b] = min(bf + totf, kp.fcap);
+            if (bf + totf > kp.fcap) atomicOr(kp.err, 1u);
         }
     }
     __syncthreads();
     int2 *ph = kp.pairs + (size_t)b * kp.cap;
     int2 *pf = reinterpret_cast<int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
-    for (int i = w; i < N; i += nw) {
+    for (int i = r0 + w; i < r1; i += nw) {
         const float4 fi = sf[i];
         const double4_32a di = sO[i];
         int h = oh[i], f = FULL ? of[i] : 0;
@@ -410,10 +429,30 @@ void launch_neighbors(Engine &E) {
     if (kp.N <= NB_MAXN && E.nbr_block) {
         const int nt = ((kp.N + 31) / 32) * 32 < 256 ? 256 : ((kp.N + 31) / 32) * 32;
         const size_t smem = (sizeof(double4_32a) + sizeof(float4) + 2 * sizeof(int)) * (size_t)kp.N;
+        // a cluster of up to 4 CTAs per bead so that the beads cover the GPU
+        static int nsm_cache[64] = {0};
+        int &nsm = nsm_cache[E.device & 63];
+        if (!nsm) {
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, E.device);
+            if (nsm <= 0) nsm = 152;
+        }
+        const int ncl = std::max(1, std::min(4, std::min(nsm / std::max(kp.P, 1), kp.N / 32)));
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(ncl * kp.P);
+        cfg.blockDim = dim3(nt);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = E.stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = ncl;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
         if (E.precision == PIMD_PREC_MIXED)
-            k_nbr_block<true><<<kp.P, nt, smem, E.stream>>>(kp);
+            cudaLaunchKernelEx(&cfg, k_nbr_block<true>, kp);
         else
-            k_nbr_block<false><<<kp.P, nt, smem, E.stream>>>(kp);
+            cudaLaunchKernelEx(&cfg, k_nbr_block<false>, kp);
         ++E.nlaunch;
         return;
     }

@@ -169,4 +169,28 @@ PIMD_D void split_tf32(float x, float &hi, float &lo) {
     lo = to_tf32(x - hi);
 }
 
+// Thread-block cluster helpers (a launch without a cluster attribute is clusters of one CTA)
+PIMD_D uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+PIMD_D uint32_t cluster_size() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+// every thread of every CTA of the cluster: arrive (release) and wait (acquire)
+PIMD_D void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// a 32-bit value at this CTA's shared address `local` in the shared memory of CTA `rank`
+PIMD_D int ld_cluster_s32(const void *local, uint32_t rank) {
+    uint32_t ra;
+    int v;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_u32(local)), "r"(rank));
+    asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(ra));
+    return v;
+}
+
 }  // namespace umma
