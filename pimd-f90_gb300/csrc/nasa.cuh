@@ -14,6 +14,41 @@ static __constant__ double c_c5z[245];
 static __constant__ double c_coefD[84];
 static __constant__ unsigned char c_idx[245][3];
 static __constant__ unsigned char c_idxD[84][3];
+// The sums of pot_nasa (terms 1..244) and dms_nasa (terms 1..83) regrouped by the powers (i, j)
+// of x1, x2: per group, slots k = n .. 1 (descending, for Horner in x3) hold the term with
+// power k of f3, or -1 where the table has none. Group: i, j, first slot, slots.
+constexpr int NASA_PG = 32, NASA_PS = 256, NASA_DG = 32, NASA_DS = 128;
+static __constant__ unsigned char c_pg[NASA_PG][4];
+static __constant__ short c_ps[NASA_PS];
+static __constant__ unsigned char c_dg[NASA_DG][4];
+static __constant__ short c_ds[NASA_DS];
+static __constant__ int c_ngrp[2];  // groups of the PES and of the DMS
+
+// group terms j0 .. j1 - 1 of an (i, j, k) table by (i, j); returns the group count (-1: too many)
+static inline int nasa_group(const int *I, const int *J, const int *K, int j0, int j1, unsigned char (*grp)[4], short *slot,
+                             int maxg, int maxs) {
+    int ng = 0, ns = 0;
+    for (int a = 1; a <= 16; a++)
+        for (int b = 1; b <= 16; b++) {
+            int kmax = 0;
+            for (int t = j0; t < j1; t++)
+                if (I[t] == a && J[t] == b) kmax = K[t] > kmax ? K[t] : kmax;
+            if (!kmax) continue;
+            if (ng >= maxg || ns + kmax > maxs) return -1;
+            grp[ng][0] = (unsigned char)a;
+            grp[ng][1] = (unsigned char)b;
+            grp[ng][2] = (unsigned char)ns;
+            grp[ng][3] = (unsigned char)kmax;
+            for (int k = kmax; k >= 1; k--) {
+                short js = -1;
+                for (int t = j0; t < j1; t++)
+                    if (I[t] == a && J[t] == b && K[t] == k) js = (short)t;
+                slot[ns++] = js;
+            }
+            ng++;
+        }
+    return ng;
+}
 
 // c5z = f5z C5ZA + fbasis CBASIS + fcore CCORE + frest CREST (nasa_mod.f90) and the index tables
 static inline void nasa_upload_constants() {
@@ -36,6 +71,18 @@ static inline void nasa_upload_constants() {
     cudaMemcpyToSymbol(c_coefD, PIMD_NASA_COEFD, sizeof(double) * 84);
     cudaMemcpyToSymbol(c_idx, idx, sizeof(idx));
     cudaMemcpyToSymbol(c_idxD, idxD, sizeof(idxD));
+    unsigned char pg[NASA_PG][4] = {}, dg[NASA_DG][4] = {};
+    short ps[NASA_PS], ds[NASA_DS];
+    for (int i = 0; i < NASA_PS; i++) ps[i] = -1;
+    for (int i = 0; i < NASA_DS; i++) ds[i] = -1;
+    int ng[2];
+    ng[0] = nasa_group(PIMD_NASA_IDX1, PIMD_NASA_IDX2, PIMD_NASA_IDX3, 1, 245, pg, ps, NASA_PG, NASA_PS);
+    ng[1] = nasa_group(PIMD_NASA_IDXD1, PIMD_NASA_IDXD2, PIMD_NASA_IDXD3, 1, 84, dg, ds, NASA_DG, NASA_DS);
+    cudaMemcpyToSymbol(c_pg, pg, sizeof(pg));
+    cudaMemcpyToSymbol(c_ps, ps, sizeof(ps));
+    cudaMemcpyToSymbol(c_dg, dg, sizeof(dg));
+    cudaMemcpyToSymbol(c_ds, ds, sizeof(ds));
+    cudaMemcpyToSymbol(c_ngrp, ng, sizeof(ng));
 }
 
 // r1[atom][comp]: atoms O, H1, H2. Returns energy (kcal/mol) and gradient dr1[atom][comp].
@@ -77,15 +124,24 @@ PIMD_D void nasa_pot(const double r1[3][3], const double box[3], const double bo
         f3[j] = f3[j - 1] * x3;
     }
     const double efac = exp(-b1 * ((dROH1 - reoh) * (dROH1 - reoh) + (dROH2 - reoh) * (dROH2 - reoh)));
+    // sum0 = sum_t c_t sym_t f3[k_t], sum3 its x3-derivative, sum1, sum2 the x1-, x2-derivatives
+    // (nasa.f90:62-72): per (i, j) group the k-sum is a polynomial in x3, evaluated by Horner
+    // together with its derivative, so each term costs two FMAs
     double sum0 = 0, sum1 = 0, sum2 = 0, sum3 = 0;
-    for (int j = 1; j < 245; j++) {
-        const int inI = c_idx[j][0], inJ = c_idx[j][1], inK = c_idx[j][2];
-        const double c = c5zg ? c5zg[j] : c_c5z[j];
+    for (int g = 0; g < c_ngrp[0]; g++) {
+        const int inI = c_pg[g][0], inJ = c_pg[g][1], s0 = c_pg[g][2], n = c_pg[g][3];
+        double pk = 0.0, dpk = 0.0;
+        for (int t = 0; t < n; t++) {
+            const int j = c_ps[s0 + t];
+            const double c = j < 0 ? 0.0 : (c5zg ? c5zg[j] : c_c5z[j]);
+            dpk = dpk * x3 + pk;
+            pk = pk * x3 + c;
+        }
         const double sym = f1[inI] * f2[inJ] + f1[inJ] * f2[inI];
-        sum0 += c * sym * f3[inK];
-        sum1 += c * ((double)(inI - 1) * f1[inI - 1] * f2[inJ] + (double)(inJ - 1) * f1[inJ - 1] * f2[inI]) * f3[inK];
-        sum2 += c * ((double)(inJ - 1) * f1[inI] * f2[inJ - 1] + (double)(inI - 1) * f1[inJ] * f2[inI - 1]) * f3[inK];
-        sum3 += c * sym * (double)(inK - 1) * f3[inK - 1];
+        sum0 += sym * pk;
+        sum1 += ((double)(inI - 1) * f1[inI - 1] * f2[inJ] + (double)(inJ - 1) * f1[inJ - 1] * f2[inI]) * pk;
+        sum2 += ((double)(inJ - 1) * f1[inI] * f2[inJ - 1] + (double)(inI - 1) * f1[inJ] * f2[inI - 1]) * pk;
+        sum3 += sym * dpk;
     }
     const double Vc = 2.0 * (c5zg ? c5zg[0] : c_c5z[0]) + efac * sum0;
     *e1 = ((Va + Vb + Vc) + 0.44739574026257) * 0.00285914375100642899;
@@ -207,17 +263,24 @@ PIMD_D void nasa_dms(const double r1[3][3], const double box[3], const double bo
     double P1 = 0, P2 = 0;
     const double PL1 = costh, PL2 = 0.5 * (3.0 * PL1 * PL1 - 1.0);
     double dp1dr1 = 0, dp1dr2 = 0, dp1dcabc = 0, dp2dr1 = 0, dp2dr2 = 0, dp2dcabc = 0;
-    for (int j = 1; j < 84; j++) {
-        const int inI = c_idxD[j][0], inJ = c_idxD[j][1], inK = c_idxD[j][2];
-        const double cf = c_coefD[j];
-        P1 += cf * f1[inI] * f2[inJ] * f3[inK];
-        P2 += cf * f1[inJ] * f2[inI] * f3[inK];
-        dp1dr1 += cf * ((double)(inI - 1) * f1[inI - 1] * f2[inJ] * f3[inK]);
-        dp1dr2 += cf * ((double)(inJ - 1) * f1[inI] * f2[inJ - 1] * f3[inK]);
-        dp1dcabc += cf * ((double)(inK - 1) * f1[inI] * f2[inJ] * f3[inK - 1]);
-        dp2dr1 += cf * ((double)(inJ - 1) * f1[inJ - 1] * f2[inI] * f3[inK]);
-        dp2dr2 += cf * ((double)(inI - 1) * f1[inJ] * f2[inI - 1] * f3[inK]);
-        dp2dcabc += cf * ((double)(inK - 1) * f1[inJ] * f2[inI] * f3[inK - 1]);
+    // nasa.f90:229-241 regrouped by (i, j) with Horner in x3, as in nasa_pot
+    for (int g = 0; g < c_ngrp[1]; g++) {
+        const int inI = c_dg[g][0], inJ = c_dg[g][1], s0 = c_dg[g][2], n = c_dg[g][3];
+        double qk = 0.0, dqk = 0.0;
+        for (int t = 0; t < n; t++) {
+            const int j = c_ds[s0 + t];
+            dqk = dqk * x3 + qk;
+            qk = qk * x3 + (j < 0 ? 0.0 : c_coefD[j]);
+        }
+        const double a = f1[inI] * f2[inJ], bb = f1[inJ] * f2[inI];
+        P1 += a * qk;
+        P2 += bb * qk;
+        dp1dr1 += (double)(inI - 1) * f1[inI - 1] * f2[inJ] * qk;
+        dp1dr2 += (double)(inJ - 1) * f1[inI] * f2[inJ - 1] * qk;
+        dp1dcabc += a * dqk;
+        dp2dr1 += (double)(inJ - 1) * f1[inJ - 1] * f2[inI] * qk;
+        dp2dr2 += (double)(inI - 1) * f1[inJ] * f2[inI - 1] * qk;
+        dp2dcabc += bb * dqk;
     }
     nasa_dms_finish(ROH1, ROH2, dROH1, dROH2, costh, efac, P1, P2, dp1dr1, dp1dr2, dp1dcabc, dp2dr1, dp2dr2, dp2dcabc,
                     PL1, PL2, dms1, dms2, dms3, q3, gradq);
