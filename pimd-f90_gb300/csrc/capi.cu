@@ -201,6 +201,7 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
     for (int c = 0; c < 3; c++) {
         kp.box[c] = p->box[c];
         kp.boxi[c] = 1.0 / p->box[c];
+        kp.boxq[c] = (float)(p->box[c] * 0x1p-32);
     }
     kp.volume = p->box[0] * p->box[1] * p->box[2];
     kp.rc2 = p->rc * p->rc;
@@ -332,7 +333,8 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
         if ((rc = dalloc(E, &kp.tabf, P * kp.ntab * S)) || (rc = dalloc(E, &kp.posf, P * S)) ||
             (rc = dalloc(E, &kp.rhof, P * S)) || (rc = dalloc(E, &kp.fcnt, P * N)) || (rc = dalloc(E, &kp.foff, P * N)) ||
             (rc = dalloc(E, &kp.fnbr, P * (size_t)kp.fcap * 2)) || (rc = dalloc(E, &kp.fntot, P)) ||
-            (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd * 6)) || (rc = dalloc(E, &kp.Wf, P * 2 * (size_t)kp.nk)) || (rc = dalloc(E, &kp.dipf, P * S)))
+            (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd * 6)) || (rc = dalloc(E, &kp.Wf, P * 2 * (size_t)kp.nk)) || (rc = dalloc(E, &kp.dipf, P * S)) ||
+            (rc = dalloc(E, &kp.ofix, P * N)) || (rc = dalloc(E, &kp.orawf, P * N)))
             return rc;
     }
     // cell lists for boxes beyond the one-block neighbour kernel (cells of width >= Rc + 1e-3 A)
@@ -367,6 +369,7 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
     }
     pot_init_constants(E);
     ewald_init(E);
+    if (E.precision == PIMD_MIXED && (rc = cuda_check(E, mixed_init(E), "mixed tables"))) return rc;
     neighbors_init(E);
     if (kp.model == 3) adjoint_init(E);
     return cuda_check(E, cudaDeviceSynchronize(), "init");

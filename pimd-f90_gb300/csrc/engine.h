@@ -63,6 +63,7 @@ struct KP {
     int contraction, guess, t, polar_maxiter, same_acd;
     double polar_eps;
     double box[3], boxi[3], volume, rc2, rc1;
+    float boxq[3];  // box / 2^32 (FP32): the length of one unit of ofix
     double vdwA, vdwB, vdwC, vdwD, vdwE, shiftA, shiftB;
     double gammaM, polar[5], dms1, dms2, dms3, polar_sor, stath, factor, Uvdw_lrc;
     double qO, qH, roh0, th0, harmkb, harmka;
@@ -94,6 +95,10 @@ struct KP {
     float2 *tabf;          // [P][ntab][S] FP32 copies of the FP64 recurrence tables
     float4 *posf;          // [P][S] (site - own O (min image), q)
     float4 *rhof;          // [P][S] centroid site - own bead O (raw difference)
+    uint4 *ofix;           // [P][N] O sites as 32-bit fractions of the box edges: the wrapping
+                           // unsigned difference of two of them is the minimum image
+    float4 *orawf;         // [P][N] O sites (unwrapped) in FP32: force-phase centroid-virial lever
+    float4 *gq23;          // [GQ_N] cubic pieces of h(u) = Gamma(2/3) Q(2/3, u^3) exp(u^3) (mixed.cu)
     float4 *dipf;          // [P][S] FP32 copy of the induced dipoles (written with every update)
     int *fcnt, *foff;      // [P][N] full neighbour list counts / offsets
     int *fnbr;             // [P][fcap] full neighbour list (j ascending per i)
@@ -263,6 +268,7 @@ void launch_pair_force(Engine &E);
 void launch_finish(Engine &E);
 void launch_totals(Engine &E, double *Upott, double *virialt, double *virialct, double *virt9);
 // launchers (mixed.cu): FP32 pair arithmetic, FP64 accumulation
+cudaError_t mixed_init(Engine &E);  // FP32 lookup tables of the mixed engine
 void launch_site_offsets(Engine &E);
 void launch_pair_qq_m(Engine &E);
 void launch_dd_real_m(Engine &E);

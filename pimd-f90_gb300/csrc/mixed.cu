@@ -1,18 +1,22 @@
 // mixed.cu -- mixed-precision real-space kernels of the TTM force call (pot_ttm.f90:159-542).
 //
 // Site-pair arithmetic (screened/Thole-smeared tensors, vdW, charge-dipole and dipole-dipole
-// terms) runs in FP32; energies, virials, fields and gradients are accumulated in FP64.
-// Site-pair separations are never formed from absolute FP32 coordinates: each site keeps
-// its offset from its own molecule's O (min-imaged in FP64, stored FP32) and each molecule
-// pair its O-O minimum-image vector (FP64, the same bits as the neighbour list), so
+// terms) runs in FP32; energies, virials, fields and gradients are accumulated in FP64 per
+// molecule or per block. Site-pair separations are never formed from absolute FP32 coordinates:
+// each site keeps its offset from its own molecule's O (min-imaged in FP64, stored FP32) and
+// each O site its position as 32-bit fractions of the box edges, so that the O-O minimum image
+// is one wrapping integer difference per component (exact) and one rounding to FP32:
 //   R_s(i) - R_s'(j) = R_OO(ij) + delta_s(i) - delta_s'(j)        (then wrapped in FP32).
 // The centroid-virial separations of the reference (raw centroid differences, see
 // pot_ttm.f90:217 and :468) are rebuilt the same way from rho_s = Rc_s - R_O (FP64 difference
 // stored FP32).
 //
-// The real-space dipole field of the iterations is a gather over a full neighbour list with
-// cached FP32 tensors: deterministic, so the FP64 SOR residual converges below 1e-8 without
-// atomic-order noise.
+// Every pair kernel is a gather over the full neighbour list (a group of lanes per molecule,
+// fixed order, one plain FP64 add per output row): deterministic, no FP64 atomics, no FP64
+// arithmetic per pair, so the FP64 SOR residual of the dipole iterations converges below 1e-8
+// without atomic-order noise. Each unordered pair is evaluated from both ends.
+#include <cmath>
+
 #include "engine.h"
 
 namespace pimd {
@@ -34,7 +38,100 @@ struct TM {
 PIMD_D float wrapf(float v, float L, float Li) { return v - L * rintf(v * Li); }
 
 // ---------------------------------------------------------------------------------------
-// per-site offsets: delta = site - own O (min image), rho = centroid site - own bead O (raw)
+// Q(2/3, x) of the Thole-smeared charge pairs (smear.f90:2-34 calls math.f90:188-285 with
+// x = a r^3) without the iterative series / continued fraction. With u = a^(1/3) r,
+//   G(u) = Gamma(2/3) Q(2/3, u^3) = 3 int_u^inf s exp(-s^3) ds,
+// and h(u) = G(u) exp(u^3) is smooth on [0, inf) with h(0) = Gamma(2/3), h ~ 1/u for large u,
+// and h'(u) = 3u^2 h(u) - 3u. The table holds h as cubic Hermite pieces on a grid of 1/32
+// (interpolation error below 1e-8 relative, under FP32 rounding); the kernel forms
+// ra g23 Q = ra exp(-a r^3) h(ra r) from the exp(-a r^3) it already has. Beyond u = 4.5
+// exp(-u^3) is below the FP32 range and the term vanishes. Values of h come from the same
+// series / continued fraction evaluated in FP64 to 1e-16 at engine creation.
+constexpr int GQ_PER_UNIT = 32;
+constexpr int GQ_N = 144;  // u in [0, 4.5)
+
+static double gq_h_host(double u) {
+    const double a = 2.0 / 3.0;
+    if (u <= 0.0) return std::tgamma(a);
+    const double x = u * u * u;
+    if (x < a + 1.0) {  // P(a, x) by its series
+        double ap = a, sum = 1.0 / a, del = sum;
+        for (int n = 0; n < 2000 && std::fabs(del) > std::fabs(sum) * 1e-17; n++) {
+            ap += 1.0;
+            del *= x / ap;
+            sum += del;
+        }
+        const double P = sum * std::exp(-x + a * std::log(x) - std::lgamma(a));
+        return std::tgamma(a) * (1.0 - P) * std::exp(x);
+    }
+    // Q(a, x) = exp(-x) x^a cf / Gamma(a) by the modified Lentz continued fraction, so h = x^a cf
+    const double tiny = 1e-300;
+    double b = x + 1.0 - a, c = 1.0 / tiny, d = 1.0 / b, h = d;
+    for (int i = 1; i < 2000; i++) {
+        const double an = -i * (i - a);
+        b += 2.0;
+        d = an * d + b;
+        if (std::fabs(d) < tiny) d = tiny;
+        c = b + an / c;
+        if (std::fabs(c) < tiny) c = tiny;
+        d = 1.0 / d;
+        const double del = d * c;
+        h *= del;
+        if (std::fabs(del - 1.0) < 1e-16) break;
+    }
+    return std::pow(x, a) * h;
+}
+
+cudaError_t mixed_init(Engine &E) {
+    float4 tab[GQ_N];
+    const double du = 1.0 / GQ_PER_UNIT;
+    for (int k = 0; k < GQ_N; k++) {
+        const double u0 = k * du, u1 = (k + 1) * du;
+        const double h0 = gq_h_host(u0), h1 = gq_h_host(u1);
+        const double d0 = (3.0 * u0 * u0 * h0 - 3.0 * u0) * du, d1 = (3.0 * u1 * u1 * h1 - 3.0 * u1) * du;
+        tab[k] = make_float4((float)h0, (float)d0, (float)(3.0 * (h1 - h0) - 2.0 * d0 - d1),
+                             (float)(2.0 * (h0 - h1) + d0 + d1));
+    }
+    cudaError_t e = cudaMalloc((void **)&E.kp.gq23, sizeof(tab));
+    if (e == cudaSuccess) E.allocs.push_back(E.kp.gq23);
+    if (e == cudaSuccess) e = cudaMemcpy(E.kp.gq23, tab, sizeof(tab), cudaMemcpyHostToDevice);
+    return e;
+}
+
+// ra g23 Q(2/3, a r^3) = ra exp1 h(ra r), exp1 = exp(-a r^3)
+PIMD_D float gq_h(const float4 *tab, float u) {
+    const float x = u * (float)GQ_PER_UNIT;
+    const int k = min((int)x, GQ_N - 1);
+    const float t = fminf(x - (float)k, 1.f);
+    const float4 c = __ldg(tab + k);
+    return c.x + t * (c.y + t * (c.z + t * c.w));
+}
+
+// smear01<float> (smear.f90:2-34) with the tabulated Q(2/3, x)
+PIMD_D void smear01_m(float drsq, float a_pol12, float ra, const EwCf &e, const float4 *gq, float *ts0, float *ts1) {
+    const float dd = sqrtf(drsq);
+    const float dri = 1.f / dd;
+    const float drsqi = dri * dri;
+    const float expon = expf(-(e.a2 * drsq));
+    const float er = erfc_as<float>(e.aewald * dd);
+    float t0 = er * dri;
+    float t1 = (t0 + e.cts1 * expon) * drsqi;
+    if (drsq < 25.f) {
+        const float rA3 = dd * drsq * a_pol12;
+        const float exp1 = expf(-rA3);
+        const float ch1 = -dri * drsqi;
+        const float sr1 = (1.f - exp1) * dri * drsqi;
+        t1 = t1 + ch1 + sr1;
+        t0 = t0 - exp1 * dri + ra * exp1 * gq_h(gq, ra * dd);
+    }
+    *ts0 = t0;
+    *ts1 = t1;
+}
+
+// ---------------------------------------------------------------------------------------
+// per-site offsets: delta = site - own O (min image), rho = centroid site - own bead O (raw);
+// per molecule the O site as fractions of the box edges in 32-bit fixed point (ofix) and in
+// FP32 (orawf, unwrapped)
 __global__ void __launch_bounds__(128) k_site_offsets(KP kp) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     if (s >= kp.S) return;
@@ -44,6 +141,16 @@ __global__ void __launch_bounds__(128) k_site_offsets(KP kp) {
     float4 d;
     if (s < kp.N) {
         d = make_float4(0.f, 0.f, 0.f, (float)R.w);
+        const double o[3] = {O.x, O.y, O.z};
+        unsigned u[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const double t = o[c] * kp.boxi[c];
+            // fraction in [0, 1) times 2^32; a round-up to 2^32 wraps to 0, the same point
+            u[c] = (unsigned)(unsigned long long)__double2ll_rn((t - floor(t)) * 0x1p32);
+        }
+        kp.ofix[(size_t)b * kp.N + s] = make_uint4(u[0], u[1], u[2], 0u);
+        kp.orawf[(size_t)b * kp.N + s] = make_float4((float)O.x, (float)O.y, (float)O.z, 0.f);
     } else {
         d = make_float4((float)min_image_rn(__dsub_rn(R.x, O.x), kp.box[0], kp.boxi[0]),
                         (float)min_image_rn(__dsub_rn(R.y, O.y), kp.box[1], kp.boxi[1]),
@@ -53,127 +160,162 @@ __global__ void __launch_bounds__(128) k_site_offsets(KP kp) {
     kp.rhof[gs] = make_float4((float)(C.x - O.x), (float)(C.y - O.y), (float)(C.z - O.z), 0.f);
 }
 
+// O_i - O_j, minimum image, from the fixed-point sites: the unsigned difference wraps modulo the
+// box, read as signed it is the nearest image; one rounding to FP32 (relative 2^-24) and the scale
+PIMD_D void oo_min_image(const KP &kp, uint4 oi, uint4 oj, float R[3]) {
+    R[0] = (float)(int)(oi.x - oj.x) * kp.boxq[0];
+    R[1] = (float)(int)(oi.y - oj.y) * kp.boxq[1];
+    R[2] = (float)(int)(oi.z - oj.z) * kp.boxq[2];
+}
+
+// sum over the QL lanes of one molecule's group (QL divides 32; every lane of the warp calls it)
+template <int QL>
+PIMD_D float group_sum(float v) {
+#pragma unroll
+    for (int o = QL / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// lanes per molecule of the gather kernels (two molecules per warp)
+constexpr int QL = 16;
+
 // ---------------------------------------------------------------------------------------
-// pot_ttm.f90:159-228 in FP32 pair arithmetic (vdW + screened/Thole charge-charge)
+// pot_ttm.f90:159-228 in FP32 pair arithmetic (vdW + screened/Thole charge-charge), as a
+// gather over the full neighbour list: QL lanes per molecule i stride over its entries (i, j)
+// and accumulate only i's side -- the fields and potentials at i's sites from j's charges and
+// i's share of the vdW gradient; j's side is accumulated when j gathers i. Every unordered pair
+// is visited twice, so energies and virials are added with weight 1/2. No atomics per entry: the
+// group's sums are added once to the F and dR rows k_sites initialised (deterministic).
 template <int MODEL>
 __global__ void __launch_bounds__(128) k_pair_qq_m(KP kp) {
     using T = TM<MODEL>;
     const int b = blockIdx.y, N = kp.N;
-    const int np = kp.npair[b];
-    const double4_32a *pos = kp.pos + (size_t)b * kp.S;
+    const int sub = threadIdx.x & (QL - 1);
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) / QL;
     const float4 *pf = kp.posf + (size_t)b * kp.S;
     const float4 *rh = kp.rhof + (size_t)b * kp.S;
+    const uint4 *of = kp.ofix + (size_t)b * N;
+    const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
     const float L[3] = {(float)kp.box[0], (float)kp.box[1], (float)kp.box[2]};
     const float Li[3] = {(float)kp.boxi[0], (float)kp.boxi[1], (float)kp.boxi[2]};
     const float vA = kp.vdwA, vB = kp.vdwB, vC = kp.vdwC, vD = kp.vdwD, vE = kp.vdwE;
     const float sA = kp.shiftA, sB = kp.shiftB, r1 = kp.rc1;
-    float av[14];  // per-thread FP32 partials, reduced in FP64 per warp (block_reduce_add_f)
+    float av[14];  // per-lane FP32 partials, reduced in FP64 per warp (block_reduce_add_f)
 #pragma unroll
-    for (int i = 0; i < 14; i++) av[i] = 0.f;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
-        const int2 ij = kp.pairs[(size_t)b * kp.cap + p];
-        const int i = ij.x, j = ij.y;
-        const double4_32a Oi = pos[i], Oj = pos[j];
-        float Rf[3];
-        Rf[0] = (float)min_image_rn(__dsub_rn(Oi.x, Oj.x), kp.box[0], kp.boxi[0]);
-        Rf[1] = (float)min_image_rn(__dsub_rn(Oi.y, Oj.y), kp.box[1], kp.boxi[1]);
-        Rf[2] = (float)min_image_rn(__dsub_rn(Oi.z, Oj.z), kp.box[2], kp.boxi[2]);
-        float4 di[5], dj[5], ri[5], rj[5];
+    for (int q = 0; q < 14; q++) av[q] = 0.f;
+    float Fi[5][4], gR[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 5; k++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) Fi[k][c] = 0.f;
+    if (i < N) {
+        // row bounds clamped to the stored length (offsets run past it when the list overflowed)
+        const int ne = kp.fntot[b];
+        const int e0 = min(kp.foff[(size_t)b * N + i], ne);
+        const int e1 = (i + 1 < N) ? min(kp.foff[(size_t)b * N + i + 1], ne) : ne;
+        const uint4 oi = of[i];
+        float4 di[5], ri[5];
 #pragma unroll
         for (int k = 1; k <= 4; k++) {
             di[k] = pf[(k - 1) * N + i];
-            dj[k] = pf[(k - 1) * N + j];
             ri[k] = rh[(k - 1) * N + i];
-            rj[k] = rh[(k - 1) * N + j];
         }
-        {  // van der Waals, O-O (pot_ttm.f90:168-190)
-            const float dRsq = Rf[0] * Rf[0] + Rf[1] * Rf[1] + Rf[2] * Rf[2];
-            const float dRij = sqrtf(dRsq);
-            const float R2i = 1.f / dRsq, R4i = R2i * R2i, R6i = R4i * R2i, R8i = R6i * R2i;
-            const float tv = vD * __expf(-vE * dRij);
-            av[ACC_UVDW] += R6i * ((vA * R6i + vB * R4i) + vC) + tv;
-            const float xr = dRij - r1;
-            const float sc = R8i * 6.f * vC + tv * vE / dRij + sA * (xr * xr) + sB * (xr * xr * xr);
-            float d[3];
-#pragma unroll
-            for (int c = 0; c < 3; c++) d[c] = -sc * Rf[c];
-            const double4_32a ci = posc_of(kp, b)[i], cj = posc_of(kp, b)[j];
-            const float Rc[3] = {(float)min_image_rn(__dsub_rn(ci.x, cj.x), kp.box[0], kp.boxi[0]),
-                                 (float)min_image_rn(__dsub_rn(ci.y, cj.y), kp.box[1], kp.boxi[1]),
-                                 (float)min_image_rn(__dsub_rn(ci.z, cj.z), kp.box[2], kp.boxi[2])};
-            double *dRi = kp.dR + 3 * ((size_t)b * kp.S + i), *dRj = kp.dR + 3 * ((size_t)b * kp.S + j);
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                atomicAdd(dRi + c, (double)d[c]);
-                atomicAdd(dRj + c, -(double)d[c]);
-            }
-            av[ACC_VIRIALC] += Rc[0] * d[0] + Rc[1] * d[1] + Rc[2] * d[2];
-#pragma unroll
-            for (int col = 0; col < 3; col++)
-#pragma unroll
-                for (int c = 0; c < 3; c++) av[ACC_VIRT + c + 3 * col] += d[col] * Rf[c];
-        }
-        float Fi[5][4], Fj[5][4];
-#pragma unroll
-        for (int k = 0; k < 5; k++)
-#pragma unroll
-            for (int c = 0; c < 4; c++) Fi[k][c] = Fj[k][c] = 0.f;
         float vt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, vc = 0.f;
-        unsigned err = 0;
+        for (int e = e0 + sub; e < e1; e += QL) {
+            const int j = fl[e].y;
+            float Rf[3];
+            oo_min_image(kp, oi, of[j], Rf);
+            float4 dj[5], rj[5];
 #pragma unroll
-        for (int isp = 1; isp <= 4; isp++) {
-#pragma unroll
-            for (int jsp = 1; jsp <= 4; jsp++) {
-                if (!T::qq_active(isp, jsp)) continue;
-                const float Rs[3] = {wrapf(Rf[0] + di[isp].x - dj[jsp].x, L[0], Li[0]),
-                                     wrapf(Rf[1] + di[isp].y - dj[jsp].y, L[1], Li[1]),
-                                     wrapf(Rf[2] + di[isp].z - dj[jsp].z, L[2], Li[2])};
-                const float d2 = Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2];
-                float ts0, ts1;
-                smear01<float>(d2, (float)kp.pt.apol_qq[isp][jsp], (float)kp.pt.ra_qq[isp][jsp], kp.ewf, &ts0, &ts1, &err);
-                const float qi = di[isp].w, qj = dj[jsp].w;
+            for (int k = 1; k <= 4; k++) {
+                dj[k] = pf[(k - 1) * N + j];
+                rj[k] = rh[(k - 1) * N + j];
+            }
+            {  // van der Waals, O-O (pot_ttm.f90:168-190)
+                const float dRsq = Rf[0] * Rf[0] + Rf[1] * Rf[1] + Rf[2] * Rf[2];
+                const float dRij = sqrtf(dRsq);
+                const float R2i = 1.f / dRsq, R4i = R2i * R2i, R6i = R4i * R2i, R8i = R6i * R2i;
+                const float tv = vD * __expf(-vE * dRij);
+                av[ACC_UVDW] += R6i * ((vA * R6i + vB * R4i) + vC) + tv;
+                const float xr = dRij - r1;
+                const float sc = R8i * 6.f * vC + tv * vE / dRij + sA * (xr * xr) + sB * (xr * xr * xr);
+                float d[3];
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    Fi[isp][c] += ts1 * qj * Rs[c];
-                    Fj[jsp][c] -= ts1 * qi * Rs[c];
+                    d[c] = -sc * Rf[c];
+                    gR[c] += d[c];
                 }
-                Fi[isp][3] += ts0 * qj;
-                Fj[jsp][3] += ts0 * qi;
-                if (T::chg(isp) && T::chg(jsp)) {
-                    float d[3];
+                // centroid O-O minimum image: Rc_i - Rc_j = (O_i - O_j) + rho_i - rho_j
+                const float Rc[3] = {wrapf(Rf[0] + ri[1].x - rj[1].x, L[0], Li[0]),
+                                     wrapf(Rf[1] + ri[1].y - rj[1].y, L[1], Li[1]),
+                                     wrapf(Rf[2] + ri[1].z - rj[1].z, L[2], Li[2])};
+                vc += Rc[0] * d[0] + Rc[1] * d[1] + Rc[2] * d[2];
 #pragma unroll
-                    for (int c = 0; c < 3; c++) d[c] = -ts1 * qi * qj * Rs[c];
-                    const float Rc[3] = {Rf[0] + ri[isp].x - rj[jsp].x, Rf[1] + ri[isp].y - rj[jsp].y,
-                                         Rf[2] + ri[isp].z - rj[jsp].z};
-                    vc += Rc[0] * d[0] + Rc[1] * d[1] + Rc[2] * d[2];
+                for (int col = 0; col < 3; col++)
 #pragma unroll
-                    for (int col = 0; col < 3; col++)
+                    for (int c = 0; c < 3; c++) vt[c + 3 * col] += d[col] * Rf[c];
+            }
 #pragma unroll
-                        for (int c = 0; c < 3; c++) vt[c + 3 * col] += d[col] * Rs[c];
+            for (int isp = 1; isp <= 4; isp++) {
+#pragma unroll
+                for (int jsp = 2; jsp <= 4; jsp++) {  // j's charged sites
+                    if (!T::qq_active(isp, jsp)) continue;
+                    const float Rs[3] = {wrapf(Rf[0] + di[isp].x - dj[jsp].x, L[0], Li[0]),
+                                         wrapf(Rf[1] + di[isp].y - dj[jsp].y, L[1], Li[1]),
+                                         wrapf(Rf[2] + di[isp].z - dj[jsp].z, L[2], Li[2])};
+                    const float d2 = Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2];
+                    float ts0, ts1;
+                    smear01_m(d2, (float)kp.pt.apol_qq[isp][jsp], (float)kp.pt.ra_qq[isp][jsp], kp.ewf, kp.gq23, &ts0, &ts1);
+                    const float qj = dj[jsp].w;
+#pragma unroll
+                    for (int c = 0; c < 3; c++) Fi[isp][c] += ts1 * qj * Rs[c];
+                    Fi[isp][3] += ts0 * qj;
+                    if (T::chg(isp)) {
+                        const float qi = di[isp].w;
+                        float d[3];
+#pragma unroll
+                        for (int c = 0; c < 3; c++) d[c] = -ts1 * qi * qj * Rs[c];
+                        const float Rc[3] = {Rf[0] + ri[isp].x - rj[jsp].x, Rf[1] + ri[isp].y - rj[jsp].y,
+                                             Rf[2] + ri[isp].z - rj[jsp].z};
+                        vc += Rc[0] * d[0] + Rc[1] * d[1] + Rc[2] * d[2];
+#pragma unroll
+                        for (int col = 0; col < 3; col++)
+#pragma unroll
+                            for (int c = 0; c < 3; c++) vt[c + 3 * col] += d[col] * Rs[c];
+                    }
                 }
             }
         }
         av[ACC_VIRIALC] += vc;
 #pragma unroll
         for (int q = 0; q < 9; q++) av[ACC_VIRT + q] += vt[q];
-        if (err) atomicOr(kp.err, err);
+    }
+    // group sums of i's side (all lanes take part; lanes of i >= N hold zeros)
+#pragma unroll
+    for (int k = 1; k <= 4; k++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) Fi[k][c] = group_sum<QL>(Fi[k][c]);
+#pragma unroll
+    for (int c = 0; c < 3; c++) gR[c] = group_sum<QL>(gR[c]);
+    if (i < N && sub == 0) {
         double4_32a *Fb = kp.F + (size_t)b * kp.S;
 #pragma unroll
         for (int k = 1; k <= 4; k++) {
             if (MODEL != 2 && k == 1) continue;
-            double *fi = reinterpret_cast<double *>(Fb + (k - 1) * N + i);
-            double *fj = reinterpret_cast<double *>(Fb + (k - 1) * N + j);
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                atomicAdd(fi + c, (double)Fi[k][c]);
-                atomicAdd(fj + c, (double)Fj[k][c]);
-            }
-            if (k != 1) {
-                atomicAdd(fi + 3, (double)Fi[k][3]);
-                atomicAdd(fj + 3, (double)Fj[k][3]);
-            }
+            double4_32a f = Fb[(k - 1) * N + i];
+            f.x += (double)Fi[k][0];
+            f.y += (double)Fi[k][1];
+            f.z += (double)Fi[k][2];
+            if (k != 1) f.w += (double)Fi[k][3];
+            Fb[(k - 1) * N + i] = f;
         }
+        double *dRi = kp.dR + 3 * ((size_t)b * kp.S + i);
+#pragma unroll
+        for (int c = 0; c < 3; c++) dRi[c] += (double)gR[c];
     }
+    // each unordered pair was visited from both ends
+#pragma unroll
+    for (int q = 0; q < 14; q++) av[q] *= 0.5f;
     block_reduce_add_f<14, 128>(av, kp.acc + (size_t)b * NACC);
 }
 
@@ -184,17 +326,15 @@ __global__ void __launch_bounds__(128) k_dd_tensors_m(KP kp) {
     using T = TM<MODEL>;
     const int b = blockIdx.y, N = kp.N;
     const int ne = kp.fntot[b];
-    const double4_32a *pos = kp.pos + (size_t)b * kp.S;
+    const uint4 *of = kp.ofix + (size_t)b * N;
     const float4 *pf = kp.posf + (size_t)b * kp.S;
     const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
     const float L[3] = {(float)kp.box[0], (float)kp.box[1], (float)kp.box[2]};
     const float Li[3] = {(float)kp.boxi[0], (float)kp.boxi[1], (float)kp.boxi[2]};
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
         const int2 ij = fl[e];
-        const double4_32a Oi = pos[ij.x], Oj = pos[ij.y];
-        const float Rf[3] = {(float)min_image_rn(__dsub_rn(Oi.x, Oj.x), kp.box[0], kp.boxi[0]),
-                             (float)min_image_rn(__dsub_rn(Oi.y, Oj.y), kp.box[1], kp.boxi[1]),
-                             (float)min_image_rn(__dsub_rn(Oi.z, Oj.z), kp.box[2], kp.boxi[2])};
+        float Rf[3];
+        oo_min_image(kp, of[ij.x], of[ij.y], Rf);
         float *Te = kp.Tf + ((size_t)b * kp.fcap + e) * kp.ndd * 6;
         int t = 0;
 #pragma unroll
@@ -232,8 +372,9 @@ __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
     const double *dip = kp.dip + (size_t)b * kp.S * 3;
     const float4 *dipf = kp.dipf + (size_t)b * kp.S;
     const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
-    const int e0 = kp.foff[(size_t)b * N + i];
-    const int e1 = (i + 1 < N) ? kp.foff[(size_t)b * N + i + 1] : kp.fntot[b];
+    const int ne = kp.fntot[b];  // offsets run past the stored length when the list overflowed
+    const int e0 = min(kp.foff[(size_t)b * N + i], ne);
+    const int e1 = (i + 1 < N) ? min(kp.foff[(size_t)b * N + i + 1], ne) : ne;
     float ei[5][3];
 #pragma unroll
     for (int k = 0; k < 5; k++) ei[k][0] = ei[k][1] = ei[k][2] = 0.f;
@@ -296,186 +437,176 @@ PIMD_D void dd_force_f(const float R[3], const float di[3], const float dj[3], f
     for (int c = 0; c < 3; c++) dij[c] += a * R[c] - 3.f * t2 * (rdi * dj[c] + rdj * di[c]);
 }
 
-// pot_ttm.f90:399-542 in FP32 pair arithmetic, FP64 accumulation
+// pot_ttm.f90:399-542 in FP32 pair arithmetic, as a gather like k_pair_qq_m: QL lanes per
+// molecule i over its full-list entries accumulate i's side (gradients at i's sites, the
+// potentials at i's sites from j's dipoles) with virials at weight 1/2, then lane 0 of the group
+// adds the intramolecular terms (pot_ttm.f90:482-542) before the group sums go into dR and F.w.
 template <int MODEL>
 __global__ void __launch_bounds__(128) k_pair_force_m(KP kp) {
     using T = TM<MODEL>;
     const int b = blockIdx.y, N = kp.N;
-    const int np = kp.npair[b];
-    const double4_32a *pos = kp.pos + (size_t)b * kp.S;
+    const int sub = threadIdx.x & (QL - 1);
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) / QL;
     const float4 *pf = kp.posf + (size_t)b * kp.S;
     const float4 *rh = kp.rhof + (size_t)b * kp.S;
-    const double *dip = kp.dip + (size_t)b * kp.S * 3;
-    double *dR = kp.dR + (size_t)b * kp.S * 3;
-    double4_32a *Fb = kp.F + (size_t)b * kp.S;
+    const float4 *mf = kp.dipf + (size_t)b * kp.S;
+    const uint4 *of = kp.ofix + (size_t)b * N;
+    const float4 *orw = kp.orawf + (size_t)b * N;
+    const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
     const bool same_a = kp.same_acd != 0;
     const float L[3] = {(float)kp.box[0], (float)kp.box[1], (float)kp.box[2]};
     const float Li[3] = {(float)kp.boxi[0], (float)kp.boxi[1], (float)kp.boxi[2]};
-    float av[14];  // per-thread FP32 partials, reduced in FP64 per warp (block_reduce_add_f)
+    float av[14];  // per-lane FP32 partials, reduced in FP64 per warp (block_reduce_add_f)
 #pragma unroll
-    for (int i = 0; i < 14; i++) av[i] = 0.f;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
-        const int2 ij = kp.pairs[(size_t)b * kp.cap + p];
-        const int i = ij.x, j = ij.y;
-        const double4_32a Oi = pos[i], Oj = pos[j];
-        double Rd[3], Cd[3];
-        Rd[0] = min_image_rn(__dsub_rn(Oi.x, Oj.x), kp.box[0], kp.boxi[0]);
-        Rd[1] = min_image_rn(__dsub_rn(Oi.y, Oj.y), kp.box[1], kp.boxi[1]);
-        Rd[2] = min_image_rn(__dsub_rn(Oi.z, Oj.z), kp.box[2], kp.boxi[2]);
-        // raw O-O difference plus the wrapped Rij0 of pot_ttm.f90:406-407 (centroid virial)
-        const double Raw[3] = {Oi.x - Oj.x, Oi.y - Oj.y, Oi.z - Oj.z};
+    for (int q = 0; q < 14; q++) av[q] = 0.f;
+    float gi[5][3], pi[5];
 #pragma unroll
-        for (int c = 0; c < 3; c++) Cd[c] = Raw[c] + min_image_rn(Rd[c] - Raw[c], kp.box[c], kp.boxi[c]);
-        const float Rf[3] = {(float)Rd[0], (float)Rd[1], (float)Rd[2]};
-        const float Cf[3] = {(float)Cd[0], (float)Cd[1], (float)Cd[2]};
-        float gi[5][3], gj[5][3], pi[5], pj[5];
+    for (int k = 0; k < 5; k++) gi[k][0] = gi[k][1] = gi[k][2] = pi[k] = 0.f;
+    if (i < N) {
+        // row bounds clamped to the stored length (offsets run past it when the list overflowed)
+        const int ne = kp.fntot[b];
+        const int e0 = min(kp.foff[(size_t)b * N + i], ne);
+        const int e1 = (i + 1 < N) ? min(kp.foff[(size_t)b * N + i + 1], ne) : ne;
+        const uint4 oi = of[i];
+        const float4 owi = orw[i];
+        float4 si[5], ri[5];
+        float mi[5][3];
 #pragma unroll
-        for (int k = 0; k < 5; k++) {
-            gi[k][0] = gi[k][1] = gi[k][2] = gj[k][0] = gj[k][1] = gj[k][2] = 0.f;
-            pi[k] = pj[k] = 0.f;
+        for (int k = 1; k <= 4; k++) {
+            si[k] = pf[(k - 1) * N + i];
+            ri[k] = rh[(k - 1) * N + i];
+            const float4 m = T::dip(k) ? mf[(k - 1) * N + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            mi[k][0] = m.x, mi[k][1] = m.y, mi[k][2] = m.z;
         }
         float vt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, vc = 0.f;
+        for (int e = e0 + sub; e < e1; e += QL) {
+            const int j = fl[e].y;
+            float Rf[3];
+            oo_min_image(kp, oi, of[j], Rf);
+            // raw O-O difference: the force phase's centroid virial uses unwrapped centroid
+            // differences (its Rij0 is wrapped to zero, pot_ttm.f90:406-407 and :468)
+            const float4 owj = orw[j];
+            const float Cf[3] = {owi.x - owj.x, owi.y - owj.y, owi.z - owj.z};
 #pragma unroll
-        for (int isp = 1; isp <= 4; isp++) {
+            for (int isp = 1; isp <= 4; isp++) {
 #pragma unroll
-            for (int jsp = 1; jsp <= 4; jsp++) {
-                if (!T::f_active(isp, jsp)) continue;
-                const float4 a = pf[(isp - 1) * N + i], c4 = pf[(jsp - 1) * N + j];
-                const float Rs[3] = {wrapf(Rf[0] + a.x - c4.x, L[0], Li[0]), wrapf(Rf[1] + a.y - c4.y, L[1], Li[1]),
-                                     wrapf(Rf[2] + a.z - c4.z, L[2], Li[2])};
-                const float d2 = Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2];
-                const float qi = a.w, qj = c4.w;
-                float di[3] = {0, 0, 0}, dj[3] = {0, 0, 0};
-                if (T::dip(isp)) {
-                    const double *m = dip + 3 * ((isp - 1) * N + i);
-                    di[0] = (float)m[0], di[1] = (float)m[1], di[2] = (float)m[2];
-                }
-                if (T::dip(jsp)) {
-                    const double *m = dip + 3 * ((jsp - 1) * N + j);
-                    dj[0] = (float)m[0], dj[1] = (float)m[1], dj[2] = (float)m[2];
-                }
-                float qd[3];
-#pragma unroll
-                for (int c = 0; c < 3; c++) qd[c] = qj * di[c] - qi * dj[c];
-                const float qd2 = qd[0] * qd[0] + qd[1] * qd[1] + qd[2] * qd[2];
-                float dij[3] = {0, 0, 0};
-                float ts1 = 0.f, ts2 = 0.f;
-                bool have = false;
-                if (T::dip(isp) && T::dip(jsp)) {
-                    float t1, t2, t3;
-                    smear3<float>(d2, (float)kp.pt.apol_dd[isp][jsp], kp.ewf, &t1, &t2, &t3);
-                    dd_force_f(Rs, di, dj, t2, t3, dij);
-                    if (same_a) {
-                        ts1 = t1, ts2 = t2;
-                        have = true;
+                for (int jsp = 1; jsp <= 4; jsp++) {
+                    if (!T::f_active(isp, jsp)) continue;
+                    const float4 c4 = pf[(jsp - 1) * N + j];
+                    const float Rs[3] = {wrapf(Rf[0] + si[isp].x - c4.x, L[0], Li[0]),
+                                         wrapf(Rf[1] + si[isp].y - c4.y, L[1], Li[1]),
+                                         wrapf(Rf[2] + si[isp].z - c4.z, L[2], Li[2])};
+                    const float d2 = Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2];
+                    const float qi = si[isp].w, qj = c4.w;
+                    float dj[3] = {0, 0, 0};
+                    if (T::dip(jsp)) {
+                        const float4 m = mf[(jsp - 1) * N + j];
+                        dj[0] = m.x, dj[1] = m.y, dj[2] = m.z;
                     }
+                    const float *di = mi[isp];
+                    float qd[3];
+#pragma unroll
+                    for (int c = 0; c < 3; c++) qd[c] = qj * di[c] - qi * dj[c];
+                    const float qd2 = qd[0] * qd[0] + qd[1] * qd[1] + qd[2] * qd[2];
+                    float dij[3] = {0, 0, 0};
+                    float ts1 = 0.f, ts2 = 0.f;
+                    bool have = false;
+                    if (T::dip(isp) && T::dip(jsp)) {
+                        float t1, t2, t3;
+                        smear3<float>(d2, (float)kp.pt.apol_dd[isp][jsp], kp.ewf, &t1, &t2, &t3);
+                        dd_force_f(Rs, di, dj, t2, t3, dij);
+                        if (same_a) {
+                            ts1 = t1, ts2 = t2;
+                            have = true;
+                        }
+                    }
+                    if (qd2 > 1.e-9f) {
+                        if (!have) smear2<float>(d2, (float)kp.pt.apol_cd[isp][jsp], kp.ewf, &ts1, &ts2);
+                        const float rq = Rs[0] * qd[0] + Rs[1] * qd[1] + Rs[2] * qd[2];
+#pragma unroll
+                        for (int c = 0; c < 3; c++) dij[c] += 3.f * ts2 * rq * Rs[c] - ts1 * qd[c];
+                        if (isp != 1) pi[isp] += ts1 * (Rs[0] * dj[0] + Rs[1] * dj[1] + Rs[2] * dj[2]);
+                    }
+#pragma unroll
+                    for (int c = 0; c < 3; c++) gi[isp][c] += dij[c];
+                    const float4 rb = rh[(jsp - 1) * N + j];
+                    const float Rc[3] = {Cf[0] + ri[isp].x - rb.x, Cf[1] + ri[isp].y - rb.y, Cf[2] + ri[isp].z - rb.z};
+                    vc += Rc[0] * dij[0] + Rc[1] * dij[1] + Rc[2] * dij[2];
+#pragma unroll
+                    for (int col = 0; col < 3; col++)
+#pragma unroll
+                        for (int c = 0; c < 3; c++) vt[c + 3 * col] += dij[c] * Rs[col];
                 }
-                if (qd2 > 1.e-9f) {
-                    if (!have) smear2<float>(d2, (float)kp.pt.apol_cd[isp][jsp], kp.ewf, &ts1, &ts2);
+            }
+        }
+        // each unordered pair was visited from both ends
+        av[ACC_VIRIALC] += 0.5f * vc;
+#pragma unroll
+        for (int q = 0; q < 9; q++) av[ACC_VIRT + q] += 0.5f * vt[q];
+        if (sub == 0) {  // intramolecular (pot_ttm.f90:482-542)
+            float vt1[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, vc1 = 0.f;
+#pragma unroll
+            for (int isp = 1; isp <= 3; isp++)
+#pragma unroll
+                for (int jsp = isp + 1; jsp <= 4; jsp++) {
+                    const float Rs[3] = {si[isp].x - si[jsp].x, si[isp].y - si[jsp].y, si[isp].z - si[jsp].z};
+                    const float Rc[3] = {wrapf(ri[isp].x - ri[jsp].x, L[0], Li[0]), wrapf(ri[isp].y - ri[jsp].y, L[1], Li[1]),
+                                         wrapf(ri[isp].z - ri[jsp].z, L[2], Li[2])};
+                    const float d2 = Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2];
+                    float dij[3] = {0, 0, 0};
+                    if (T::dip(isp) && T::dip(jsp)) {
+                        float t1, t2, t3;
+                        smear3<float>(d2, (float)kp.pt.apol_dd[isp][jsp], kp.ewf, &t1, &t2, &t3);
+                        dd_force_f(Rs, mi[isp], mi[jsp], t2, t3, dij);
+                    }
+                    const float qi = si[isp].w, qj = si[jsp].w;
+                    float qd[3];
+#pragma unroll
+                    for (int c = 0; c < 3; c++) qd[c] = qj * mi[isp][c] - qi * mi[jsp][c];
+                    // self2 (smear.f90:133-156) in FP32
+                    const float dd = sqrtf(d2), drsqi = 1.f / d2, dri = sqrtf(drsqi);
+                    const float expon = __expf(-(kp.ewf.a2 * d2));
+                    const float kr0 = erfc_as<float>(kp.ewf.aewald * dd) * dri;
+                    const float kr1 = (kr0 + kp.ewf.cts1 * expon) * drsqi;
+                    const float kr2 = (kr1 + kp.ewf.cts2 * expon) * drsqi;
+                    const float ch1 = -dri * drsqi, ch2 = ch1 * drsqi;
+                    const float ts1 = kr1 + ch1, ts2 = kr2 + ch2;
                     const float rq = Rs[0] * qd[0] + Rs[1] * qd[1] + Rs[2] * qd[2];
 #pragma unroll
                     for (int c = 0; c < 3; c++) dij[c] += 3.f * ts2 * rq * Rs[c] - ts1 * qd[c];
-                    if (isp != 1) pi[isp] += ts1 * (Rs[0] * dj[0] + Rs[1] * dj[1] + Rs[2] * dj[2]);
-                    if (jsp != 1) pj[jsp] -= ts1 * (Rs[0] * di[0] + Rs[1] * di[1] + Rs[2] * di[2]);
+                    pi[isp] += ts1 * (Rs[0] * mi[jsp][0] + Rs[1] * mi[jsp][1] + Rs[2] * mi[jsp][2]);
+                    pi[jsp] -= ts1 * (Rs[0] * mi[isp][0] + Rs[1] * mi[isp][1] + Rs[2] * mi[isp][2]);
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        gi[isp][c] += dij[c];
+                        gi[jsp][c] -= dij[c];
+                    }
+                    vc1 += Rc[0] * dij[0] + Rc[1] * dij[1] + Rc[2] * dij[2];
+#pragma unroll
+                    for (int col = 0; col < 3; col++)
+#pragma unroll
+                        for (int c = 0; c < 3; c++) vt1[c + 3 * col] += dij[c] * Rs[col];
                 }
+            av[ACC_VIRIALC] += vc1;
 #pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    gi[isp][c] += dij[c];
-                    gj[jsp][c] -= dij[c];
-                }
-                const float4 ra = rh[(isp - 1) * N + i], rb = rh[(jsp - 1) * N + j];
-                const float Rc[3] = {Cf[0] + ra.x - rb.x, Cf[1] + ra.y - rb.y, Cf[2] + ra.z - rb.z};
-                vc += Rc[0] * dij[0] + Rc[1] * dij[1] + Rc[2] * dij[2];
-#pragma unroll
-                for (int col = 0; col < 3; col++)
-#pragma unroll
-                    for (int c = 0; c < 3; c++) vt[c + 3 * col] += dij[c] * Rs[col];
-            }
-        }
-        av[ACC_VIRIALC] += vc;
-#pragma unroll
-        for (int q = 0; q < 9; q++) av[ACC_VIRT + q] += vt[q];
-#pragma unroll
-        for (int k = 1; k <= 4; k++) {
-            if (MODEL != 2 && k == 1) continue;
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                atomicAdd(dR + 3 * ((k - 1) * N + i) + c, (double)gi[k][c]);
-                atomicAdd(dR + 3 * ((k - 1) * N + j) + c, (double)gj[k][c]);
-            }
-            if (k != 1) {
-                atomicAdd(&Fb[(k - 1) * N + i].w, (double)pi[k]);
-                atomicAdd(&Fb[(k - 1) * N + j].w, (double)pj[k]);
-            }
+            for (int q = 0; q < 9; q++) av[ACC_VIRT + q] += vt1[q];
         }
     }
-    // intramolecular (pot_ttm.f90:482-542), one molecule per thread
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < N; w += gridDim.x * blockDim.x) {
-        float4 s[5], r4[5];
-        float mu[5][3];
+    // group sums of i's side (all lanes take part; lanes of i >= N hold zeros)
 #pragma unroll
-        for (int k = 1; k <= 4; k++) {
-            s[k] = pf[(k - 1) * N + w];
-            r4[k] = rh[(k - 1) * N + w];
-            const double *m = dip + 3 * ((k - 1) * N + w);
-            mu[k][0] = T::dip(k) ? (float)m[0] : 0.f;
-            mu[k][1] = T::dip(k) ? (float)m[1] : 0.f;
-            mu[k][2] = T::dip(k) ? (float)m[2] : 0.f;
-        }
-        float g[5][3], ph[5];
+    for (int k = 1; k <= 4; k++) {
 #pragma unroll
-        for (int k = 0; k < 5; k++) g[k][0] = g[k][1] = g[k][2] = ph[k] = 0.f;
-        float vt[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, vc = 0.f;
-#pragma unroll
-        for (int isp = 1; isp <= 3; isp++)
-#pragma unroll
-            for (int jsp = isp + 1; jsp <= 4; jsp++) {
-                const float Rs[3] = {s[isp].x - s[jsp].x, s[isp].y - s[jsp].y, s[isp].z - s[jsp].z};
-                const float Rc[3] = {wrapf(r4[isp].x - r4[jsp].x, L[0], Li[0]), wrapf(r4[isp].y - r4[jsp].y, L[1], Li[1]),
-                                     wrapf(r4[isp].z - r4[jsp].z, L[2], Li[2])};
-                const float d2 = Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2];
-                float dij[3] = {0, 0, 0};
-                if (T::dip(isp) && T::dip(jsp)) {
-                    float t1, t2, t3;
-                    smear3<float>(d2, (float)kp.pt.apol_dd[isp][jsp], kp.ewf, &t1, &t2, &t3);
-                    dd_force_f(Rs, mu[isp], mu[jsp], t2, t3, dij);
-                }
-                const float qi = s[isp].w, qj = s[jsp].w;
-                float qd[3];
-#pragma unroll
-                for (int c = 0; c < 3; c++) qd[c] = qj * mu[isp][c] - qi * mu[jsp][c];
-                // self2 (smear.f90:133-156) in FP32
-                const float dd = sqrtf(d2), drsqi = 1.f / d2, dri = sqrtf(drsqi);
-                const float expon = __expf(-(kp.ewf.a2 * d2));
-                const float kr0 = erfc_as<float>(kp.ewf.aewald * dd) * dri;
-                const float kr1 = (kr0 + kp.ewf.cts1 * expon) * drsqi;
-                const float kr2 = (kr1 + kp.ewf.cts2 * expon) * drsqi;
-                const float ch1 = -dri * drsqi, ch2 = ch1 * drsqi;
-                const float ts1 = kr1 + ch1, ts2 = kr2 + ch2;
-                const float rq = Rs[0] * qd[0] + Rs[1] * qd[1] + Rs[2] * qd[2];
-#pragma unroll
-                for (int c = 0; c < 3; c++) dij[c] += 3.f * ts2 * rq * Rs[c] - ts1 * qd[c];
-                ph[isp] += ts1 * (Rs[0] * mu[jsp][0] + Rs[1] * mu[jsp][1] + Rs[2] * mu[jsp][2]);
-                ph[jsp] -= ts1 * (Rs[0] * mu[isp][0] + Rs[1] * mu[isp][1] + Rs[2] * mu[isp][2]);
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    g[isp][c] += dij[c];
-                    g[jsp][c] -= dij[c];
-                }
-                vc += Rc[0] * dij[0] + Rc[1] * dij[1] + Rc[2] * dij[2];
-#pragma unroll
-                for (int col = 0; col < 3; col++)
-#pragma unroll
-                    for (int c = 0; c < 3; c++) vt[c + 3 * col] += dij[c] * Rs[col];
-            }
-        av[ACC_VIRIALC] += vc;
-#pragma unroll
-        for (int q = 0; q < 9; q++) av[ACC_VIRT + q] += vt[q];
+        for (int c = 0; c < 3; c++) gi[k][c] = group_sum<QL>(gi[k][c]);
+        if (k != 1) pi[k] = group_sum<QL>(pi[k]);
+    }
+    if (i < N && sub == 0) {
+        double *dR = kp.dR + (size_t)b * kp.S * 3;
+        double4_32a *Fb = kp.F + (size_t)b * kp.S;
 #pragma unroll
         for (int k = 1; k <= 4; k++) {
 #pragma unroll
-            for (int c = 0; c < 3; c++) atomicAdd(dR + 3 * ((k - 1) * N + w) + c, (double)g[k][c]);
-            if (k != 1) atomicAdd(&Fb[(k - 1) * N + w].w, (double)ph[k]);
+            for (int c = 0; c < 3; c++) dR[3 * ((k - 1) * N + i) + c] += (double)gi[k][c];
+            if (k != 1) Fb[(k - 1) * N + i].w += (double)pi[k];
         }
     }
     block_reduce_add_f<14, 128>(av, kp.acc + (size_t)b * NACC);
@@ -505,7 +636,7 @@ void launch_site_offsets(Engine &E) {
 }
 
 void launch_pair_qq_m(Engine &E) {
-    dim3 g(pair_blocks_m(E, 64), E.kp.P);
+    dim3 g((E.kp.N * QL + 127) / 128, E.kp.P);
     DISPATCH_M(E, k_pair_qq_m, g, 128);
     dim3 g2(pair_blocks_m(E, 128), E.kp.P);
     DISPATCH_M(E, k_dd_tensors_m, g2, 128);
@@ -517,7 +648,7 @@ void launch_dd_real_m(Engine &E) {
 }
 
 void launch_pair_force_m(Engine &E) {
-    dim3 g(pair_blocks_m(E, 64), E.kp.P);
+    dim3 g((E.kp.N * QL + 127) / 128, E.kp.P);
     DISPATCH_M(E, k_pair_force_m, g, 128);
 }
 
