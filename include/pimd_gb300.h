@@ -219,8 +219,15 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc);
 /* The chosen shapes: [tiled structure factors, site groups (0 = sized from the SM count),
  * register-row field kernels, max k-slices, one-launch neighbour lists] and, when n >= 6,
  * [wave-quantised split counts], when n >= 7 [tensor-core (tcgen05) dipole structure factor
- * in use], when n >= 8 [tensor-core dipole field pass in use]; n >= 5. */
+ * in use], when n >= 8 [tensor-core dipole field pass in use], when n >= 9 [real-space dipole
+ * field on a second stream beside the structure factor (mixed engine)]; n >= 5. */
 int pimd_get_tuning(pimd_ctx *ctx, int *knobs, int n);
+/* Sets the shapes in the order pimd_get_tuning reports them (n >= 5; the first n are set),
+ * e.g. to reuse an earlier autotune result without timing again. Tensor-core paths are used
+ * only where available whatever their knob says. Site groups must lie in [0, 1024] and max
+ * k-slices in [1, 16] (else PIMD_ERR_ARG). A captured MD-step graph is captured again at the
+ * next step. No counterpart in the reference. */
+int pimd_set_tuning(pimd_ctx *ctx, const int *knobs, int n);
 
 /* ---------------------------------------------------------------------------------------
  * Batches of independent ring polymers (replicas) of uneven sizes: each replica has its own

@@ -445,6 +445,21 @@ void timer_end(Engine &E) {
 // One induced-dipole iteration (pot_ttm.f90:298-390): real-space dipole field, ewald_std_dd
 // structure factor, field + SOR update, convergence test.
 static void dipole_iteration(Engine &E, bool mixed) {
+    if (mixed && E.aux_stream && E.dd_overlap) {
+        // the real-space field runs on the second stream beside the structure factor (both only
+        // read the iteration's dipoles); the field + SOR pass waits for both
+        cudaEventRecord(E.ev_fork, E.stream);
+        cudaStreamWaitEvent(E.aux_stream, E.ev_fork, 0);
+        PHASE("dd_smu", launch_ewald_smu(E));
+        cudaStream_t keep = E.stream;
+        E.stream = E.aux_stream;
+        PHASE("dd_real", launch_dd_real_m(E));
+        E.stream = keep;
+        cudaEventRecord(E.ev_join, E.aux_stream);
+        cudaStreamWaitEvent(E.stream, E.ev_join, 0);
+        PHASE("dd_update", launch_dd_update(E));  // includes the convergence test (last block)
+        return;
+    }
     if (mixed)
         PHASE("dd_real", launch_dd_real_m(E));
     else
@@ -606,6 +621,9 @@ int pimd_destroy(pimd_ctx *ctx) {
     if (E.d_adj) cudaFree(E.d_adj);
     if (E.gexec) cudaGraphExecDestroy(E.gexec);
     if (E.body_stream) cudaStreamDestroy(E.body_stream);
+    if (E.aux_stream) cudaStreamDestroy(E.aux_stream);
+    if (E.ev_fork) cudaEventDestroy(E.ev_fork);
+    if (E.ev_join) cudaEventDestroy(E.ev_join);
     if (E.own_stream && E.stream) cudaStreamDestroy(E.stream);
     delete ctx;
     return PIMD_OK;
@@ -885,7 +903,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         std::vector<int> cand;
     };
     int sf_tiled = E.sf_tiled, ff_regs = E.ff_regs, nbr_block = E.nbr_block, wave = E.wave_shapes;
-    int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc, ff_tc = E.ff_tc;
+    int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc, ff_tc = E.ff_tc, dd_overlap = E.dd_overlap;
     std::vector<Knob> knobs;
     const bool mixed = E.precision == PIMD_MIXED && E.kp.model < 4;
     if (mixed) {
@@ -894,6 +912,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         knobs.push_back({&sf_tiled, {1, 0}});
         knobs.push_back({&E.sf_groups, {0, 4, 8, 16, 32}});
         knobs.push_back({&ff_regs, {1, 0}});
+        if (E.aux_stream) knobs.push_back({&dd_overlap, {1, 0}});
     }
     knobs.push_back({&wave, {1, 0}});
     knobs.push_back({&E.max_slices, {16, 8, 4, 2}});
@@ -907,6 +926,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         E.nbr_cells = nbr_cells != 0;
         E.sf_tc = sf_tc != 0;
         E.ff_tc = ff_tc != 0;
+        E.dd_overlap = dd_overlap != 0;
     };
     int rc = PIMD_OK;
     float best;
@@ -930,6 +950,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
     }
     // the Fpart buffer holds max_slices slices: never exceed the allocated 16
     E.max_slices = std::min(E.max_slices, 16);
+    E.gkey.clear();  // a captured MD-step graph holds the old launches: capture again
     E.timers.on = timers_on;
     const double *kr = saved.RRt, *kc = saved.RRc;
     E.kp.RRt = kr;
@@ -948,6 +969,24 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     if (n >= 6) k[5] = E.wave_shapes;
     if (n >= 7) k[6] = E.sf_tc && E.tc_ready;
     if (n >= 8) k[7] = E.ff_tc && E.tf_ready;
+    if (n >= 9) k[8] = E.dd_overlap && E.aux_stream != nullptr && E.precision == PIMD_MIXED;
+    return PIMD_OK;
+}
+
+int pimd_set_tuning(pimd_ctx *ctx, const int *k, int n) {
+    if (!ctx || !k || n < 5) return PIMD_ERR_ARG;
+    if (k[1] < 0 || k[1] > 1024 || k[3] < 1 || k[3] > 16) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    E.sf_tiled = k[0] != 0;
+    E.sf_groups = k[1];
+    E.ff_regs = k[2] != 0;
+    E.max_slices = k[3];
+    E.nbr_block = k[4] != 0;
+    if (n >= 6) E.wave_shapes = k[5] != 0;
+    if (n >= 7) E.sf_tc = k[6] != 0;
+    if (n >= 8) E.ff_tc = k[7] != 0;
+    if (n >= 9) E.dd_overlap = k[8] != 0;
+    E.gkey.clear();  // a captured MD-step graph holds the old launches: capture again
     return PIMD_OK;
 }
 

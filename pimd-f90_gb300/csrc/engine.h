@@ -158,6 +158,7 @@ struct Engine {
     bool nbr_block = true; // one-launch neighbour lists per bead for N <= 1024 (k_nbr_block)
     bool nbr_cells = true; // cell lists for N > 1024 when the box holds >= 4 cells per edge
     bool wave_shapes = true;  // k-slices / site groups chosen by wave quantisation (occupancy API)
+    bool dd_overlap = true;   // mixed engine: real-space dipole field beside the structure factor
     // tensor-core (tcgen05, 3xTF32) dipole structure factor of the mixed engine (ewald_tc.cu)
     bool sf_tc = true;        // use it when tc_ready
     bool tc_ready = false;    // run groups built and the table tensor map encoded
@@ -193,6 +194,10 @@ struct Engine {
     bool graph_mode = false;
     bool capturing = false;
     cudaStream_t body_stream = nullptr;
+    // mixed engine: a second stream on which the real-space dipole field of an iteration runs
+    // beside the structure factor (fork / join events; branches of the graph when captured)
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaGraphExec_t gexec = nullptr;
     std::vector<const void *> gkey;
     long long graph_launches = 0, graph_captures = 0;

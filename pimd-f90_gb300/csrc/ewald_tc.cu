@@ -1076,13 +1076,23 @@ int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv) {
     cfg.blockDim = dim3(TC_NT);
     cfg.dynamicSmemBytes = L.total;
     cfg.stream = E.stream;
-    cudaLaunchAttribute at[1];
+    // the highest stream priority: the mixed engine's real-space dipole field runs beside this
+    // kernel on a second stream and must not hold the SMs its clusters wait for
+    static int prio_cache[64] = {0}, prio_set[64] = {0};
+    if (!prio_set[E.device & 63]) {
+        int least = 0, greatest = 0;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess) prio_cache[E.device & 63] = greatest;
+        prio_set[E.device & 63] = 1;
+    }
+    cudaLaunchAttribute at[2];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = ng;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
+    at[1].id = cudaLaunchAttributePriority;
+    at[1].val.priority = prio_cache[E.device & 63];
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = 2;
     const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(E.tc_map);
     cudaError_t e = cudaErrorInvalidValue;
     if (op == TC_OP_MU)

@@ -82,6 +82,7 @@ static double gq_h_host(double u) {
     return std::pow(x, a) * h;
 }
 
+// FP32 tables and the second stream of the mixed engine
 cudaError_t mixed_init(Engine &E) {
     float4 tab[GQ_N];
     const double du = 1.0 / GQ_PER_UNIT;
@@ -92,7 +93,10 @@ cudaError_t mixed_init(Engine &E) {
         tab[k] = make_float4((float)h0, (float)d0, (float)(3.0 * (h1 - h0) - 2.0 * d0 - d1),
                              (float)(2.0 * (h0 - h1) + d0 + d1));
     }
-    cudaError_t e = cudaMalloc((void **)&E.kp.gq23, sizeof(tab));
+    cudaError_t e = cudaStreamCreateWithFlags(&E.aux_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&E.kp.gq23, sizeof(tab));
     if (e == cudaSuccess) E.allocs.push_back(E.kp.gq23);
     if (e == cudaSuccess) e = cudaMemcpy(E.kp.gq23, tab, sizeof(tab), cudaMemcpyHostToDevice);
     return e;

@@ -82,6 +82,7 @@ SIGNATURES = {
     "pimd_pot_forward": [_V, _D, _D, _D, ctypes.c_int],
     "pimd_pot_backward": [_V, _D, _D, _D],
     "pimd_get_tuning": [_V, _I, ctypes.c_int],
+    "pimd_set_tuning": [_V, _I, ctypes.c_int],
     "pimd_batch_create": [ctypes.POINTER(_V), ctypes.POINTER(Params), _V, ctypes.c_int, ctypes.POINTER(MDParams)],
     "pimd_batch_destroy": [_V],
     "pimd_batch_last_error": [_V],
@@ -370,11 +371,26 @@ class ForceEngine:
         self._check(load().pimd_autotune(self.h, RRt_ptr, RRc_ptr), "autotune")
         return self.tuning()
 
+    TUNING_KEYS = ("sf_tiled", "sf_groups", "ff_regs", "max_slices", "nbr_block", "wave_shapes", "sf_tc", "ff_tc",
+                   "dd_overlap")
+
     def tuning(self):
-        k = (ctypes.c_int * 8)()
-        self._check(load().pimd_get_tuning(self.h, k, 8), "get_tuning")
-        return dict(sf_tiled=k[0], sf_groups=k[1], ff_regs=k[2], max_slices=k[3], nbr_block=k[4], wave_shapes=k[5],
-                    sf_tc=k[6], ff_tc=k[7])
+        n = len(self.TUNING_KEYS)
+        k = (ctypes.c_int * n)()
+        self._check(load().pimd_get_tuning(self.h, k, n), "get_tuning")
+        return {name: k[i] for i, name in enumerate(self.TUNING_KEYS)}
+
+    def set_tuning(self, **knobs):
+        """Set launch-shape knobs by name (the keys of tuning()); the others keep their values."""
+        cur = self.tuning()
+        unknown = set(knobs) - set(cur)
+        if unknown:
+            raise ValueError("unknown tuning knobs: %s" % sorted(unknown))
+        cur.update({k: int(v) for k, v in knobs.items()})
+        n = len(self.TUNING_KEYS)
+        k = (ctypes.c_int * n)(*[cur[name] for name in self.TUNING_KEYS])
+        self._check(load().pimd_set_tuning(self.h, k, n), "set_tuning")
+        return self.tuning()
 
 
 class ReplicaBatch:
