@@ -232,6 +232,8 @@ struct NMArgs {
     unsigned long long seed, counter;
     const int *tstep;   // device step word: when set, counter = 2 t + phase
     int phase;
+    int fast;           // mixed engine: fused multiply-add mode transforms and FP32 Box-Muller
+                        // draws (FP64 state, not bit-identical to the sequentially rounded sums)
 };
 __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt, double *RRc);
 __global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk);

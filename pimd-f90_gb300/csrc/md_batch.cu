@@ -93,6 +93,7 @@ static NMArgs replica_args(const pimd_batch *bt, const BatchReplica &r, const En
     a.evolve = r.P > 1;
     a.seed = r.seed;
     a.tstep = E.kp.dstep;
+    a.fast = E.precision == PIMD_MIXED;
     return a;
 }
 

@@ -36,6 +36,14 @@ PIMD_D double gauss_from(unsigned a, unsigned b) {
     return sqrt(-2.0 * log(u1)) * cos(TWOPI * u2);
 }
 
+// the same draw with FP32 logarithm and cosine (the mixed engine): u1 keeps its full range
+// (2^-32 ... 1, tails to 6.66 sigma), the value differs from gauss_from by FP32 rounding only
+PIMD_D double gauss_from_f(unsigned a, unsigned b) {
+    const float u1 = ((float)a + 1.0f) * 2.3283064365386963e-10f;
+    const float u2 = (float)b * 2.3283064365386963e-10f;
+    return (double)(sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2));
+}
+
 PIMD_D double noise(const NMArgs &a, int atom, int j, int c) {
     if (a.xi) return a.xi[c + 3 * j + (size_t)3 * a.P * atom];
     const unsigned long long idx = ((unsigned long long)atom * a.P + j) * 3 + c;
@@ -43,12 +51,17 @@ PIMD_D double noise(const NMArgs &a, int atom, int j, int c) {
                                            : a.counter;
     const uint4 r = philox4x32(make_uint4((unsigned)idx, (unsigned)(idx >> 32), (unsigned)ctr, (unsigned)(ctr >> 32)),
                                make_uint2((unsigned)a.seed, (unsigned)(a.seed >> 32)));
-    return gauss_from(r.x, r.y);
+    return a.fast ? gauss_from_f(r.x, r.y) : gauss_from(r.x, r.y);
 }
 
-// x~_j = sum_k C(j,k) x_k  (real2NM) or x_j = sum_k C(k,j) x~_k (NM2real), rounded per op
-PIMD_D double nm_row(const double *Cs, const double *v, int P, int j, int c, bool fwd) {
+// x~_j = sum_k C(j,k) x_k  (real2NM) or x_j = sum_k C(k,j) x~_k (NM2real), rounded per op,
+// or (fast) one fused multiply-add per term: half the FP64 instructions
+PIMD_D double nm_row(const double *Cs, const double *v, int P, int j, int c, bool fwd, bool fast = false) {
     double s = 0.0;
+    if (fast) {
+        for (int k = 0; k < P; k++) s = fma(fwd ? Cs[j + P * k] : Cs[k + P * j], v[3 * k + c], s);
+        return s;
+    }
     for (int k = 0; k < P; k++) {
         const double ck = fwd ? Cs[j + P * k] : Cs[k + P * j];
         s = __dadd_rn(s, __dmul_rn(ck, v[3 * k + c]));
@@ -59,7 +72,7 @@ PIMD_D double nm_row(const double *Cs, const double *v, int P, int j, int c, boo
 // Langevin_NM on one atom's momenta held in shared memory p[3P] (group-local).
 PIMD_D void langevin_atom(const NMArgs &a, const double *Cs, double *p, double *tr, int atom, int j, int c,
                           bool active) {
-    if (active) tr[3 * j + c] = nm_row(Cs, p, a.P, j, c, true);
+    if (active) tr[3 * j + c] = nm_row(Cs, p, a.P, j, c, true, a.fast);
     __syncthreads();
     if (active) {
         const double m = (atom % 3 == 0) ? a.massO : a.massH;
@@ -68,7 +81,7 @@ PIMD_D void langevin_atom(const NMArgs &a, const double *Cs, double *p, double *
         tr[3 * j + c] = __dadd_rn(__dmul_rn(c1, tr[3 * j + c]), __dmul_rn(c2, __dmul_rn(sqrtmass, noise(a, atom, j, c))));
     }
     __syncthreads();
-    if (active) p[3 * j + c] = nm_row(Cs, tr, a.P, j, c, false);
+    if (active) p[3 * j + c] = nm_row(Cs, tr, a.P, j, c, false, a.fast);
     __syncthreads();
 }
 
@@ -96,8 +109,8 @@ __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt,
     if (a.evolve) {
         double xt = 0, pt = 0;
         if (active) {
-            xt = nm_row(Cs, x, P, j, c, true);
-            pt = nm_row(Cs, p, P, j, c, true);
+            xt = nm_row(Cs, x, P, j, c, true, a.fast);
+            pt = nm_row(Cs, p, P, j, c, true, a.fast);
         }
         __syncthreads();
         if (active) {
@@ -110,8 +123,8 @@ __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt,
         __syncthreads();
         double xr = 0, pr = 0;
         if (active) {
-            xr = nm_row(Cs, tr, P, j, c, false);
-            pr = nm_row(Cs, x, P, j, c, false);
+            xr = nm_row(Cs, tr, P, j, c, false, a.fast);
+            pr = nm_row(Cs, x, P, j, c, false, a.fast);
         }
         __syncthreads();
         if (active) {
@@ -436,6 +449,7 @@ static int md_step_enqueue(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt,
     a.tstep = E.kp.dstep;
     a.phase = 0;
     a.xi = xi1;
+    a.fast = E.precision == PIMD_MIXED;
     int threads, blocks;
     size_t smem;
     nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
