@@ -159,6 +159,21 @@ static int setup_kspace(Engine &E, const pimd_params *p) {
     if ((rc = dalloc(E, &d_runkf, kp.nrun)) || (rc = dalloc(E, &d_kzf, kp.nk))) return rc;
     cudaMemcpy(d_runkf, runkf.data(), sizeof(float2) * kp.nrun, cudaMemcpyHostToDevice);
     cudaMemcpy(d_kzf, kzf.data(), sizeof(float) * kp.nk, cudaMemcpyHostToDevice);
+    // per k-vector (k_x, k_y, k_z, Ak) and 2 / k^2 + 1 / (2 alpha^2) in FP32 (mixed reciprocal virial)
+    std::vector<float4> kvirf(kp.nk);
+    std::vector<float> kc2f(kp.nk);
+    for (int k = 0; k < kp.nk; k++) {
+        const double kx = E.h_kvec[3 * k], ky = E.h_kvec[3 * k + 1], kz = E.h_kvec[3 * k + 2];
+        kvirf[k] = make_float4((float)kx, (float)ky, (float)kz, (float)E.h_Ak[k]);
+        kc2f[k] = (float)(2.0 / (kx * kx + ky * ky + kz * kz) + 0.5 / (kp.ew.aewald * kp.ew.aewald));
+    }
+    float4 *d_kvirf;
+    float *d_kc2f;
+    if ((rc = dalloc(E, &d_kvirf, kp.nk)) || (rc = dalloc(E, &d_kc2f, kp.nk))) return rc;
+    cudaMemcpy(d_kvirf, kvirf.data(), sizeof(float4) * kp.nk, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_kc2f, kc2f.data(), sizeof(float) * kp.nk, cudaMemcpyHostToDevice);
+    kp.kvirf = d_kvirf;
+    kp.kc2f = d_kc2f;
     kp.runkf = d_runkf;
     kp.kzf = d_kzf;
     kp.runs = d_runs;

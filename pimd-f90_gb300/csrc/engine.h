@@ -87,6 +87,8 @@ struct KP {
     const int2 *kidx;      // (run index, kz) of each k-vector
     const float2 *runkf;   // FP32 (kx, ky) components of each run's k-vectors (mixed engine)
     const float *kzf;      // FP32 kz component of each k-vector (mixed engine)
+    const float4 *kvirf;   // FP32 (k_x, k_y, k_z, Ak) of each k-vector (mixed engine)
+    const float *kc2f;     // FP32 2 / k^2 + 1 / (2 alpha^2) of each k-vector (mixed engine)
     float2 *Wf;            // [P][2][nk] FP32 field weights 4pi Ak/V conj(S): slot 0 charge, 1 dipole
     const int *sfrun;      // runs in the order of the structure-factor tiles (sorted by nkz)
     const int4 *sftile;    // per tile: first ez slot, kz groups, runs, offset into sfrun

@@ -91,6 +91,33 @@ __global__ void __launch_bounds__(128) k_ewald_tables(KP kp) {
     }
 }
 
+// The FP32 tables of the mixed engine without the FP64 recurrence: the site's coordinate as a
+// 32-bit fraction u of the box edge (wrapped, rounded once from FP64), n u modulo 2^32 is the
+// exact phase fraction of harmonic n (a wrapping integer multiply), read as signed it is the
+// angle pi ph / 2^31 in [-pi, pi) for sincospif. Each entry carries only FP32 rounding (of the
+// phase and of the sine and cosine), like the rounded FP64 recurrence it replaces.
+__global__ void __launch_bounds__(128) k_ewald_tables_m(KP kp) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (s >= kp.S) return;
+    const double4_32a r = kp.pos[(size_t)b * kp.S + s];
+    const double xyz[3] = {r.x, r.y, r.z};
+    const int nmx[3] = {kp.hmax, kp.kmax, kp.lmax};
+    int off = 0;
+    float2 *T = kp.tabf + (size_t)b * kp.ntab * kp.S + s;
+    for (int d = 0; d < 3; d++) {
+        const double t = xyz[d] * kp.boxi[d];
+        const unsigned u = (unsigned)(unsigned long long)__double2ll_rn((t - floor(t)) * 0x1p32);
+        T[(size_t)off * kp.S] = make_float2(1.f, 0.f);
+        for (int n = 1; n <= nmx[d]; n++) {
+            const int ph = (int)(u * (unsigned)n);
+            float sn, cs;
+            sincospif((float)ph * 0x1p-31f, &sn, &cs);
+            T[(size_t)(off + n) * kp.S] = make_float2(cs, sn);
+        }
+        off += nmx[d] + 1;
+    }
+}
+
 // k-vector components in the arithmetic type of the phase sums: FP64 from kinfo, FP32 from
 // the precomputed FP32 tables (no double-to-float conversion inside the mixed kernels)
 template <typename R>
@@ -829,6 +856,60 @@ __global__ void __launch_bounds__(128) k_qd_virial(KP kp) {
     block_reduce_add<14, 128>(av, kp.acc + (size_t)b * NACC);
 }
 
+// The same in FP32 per k-vector (the mixed engine): structure factors rounded from FP64 once,
+// per-k constants precomputed, warp sums in FP32 and block sums in FP64 (block_reduce_add_f).
+template <bool DIP>
+__global__ void __launch_bounds__(128) k_qd_virial_m(KP kp, float sc) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    float av[14];
+#pragma unroll
+    for (int i = 0; i < 14; i++) av[i] = 0.f;
+    if (k < kp.nk) {
+        const float4 q = kp.kvirf[k];
+        const float kv[3] = {q.x, q.y, q.z};
+        const float coeff2 = kp.kc2f[k];
+        const double2 sq = kp.Sq[(size_t)b * kp.nk + k];
+        const double2 sm = DIP ? kp.Sm[(size_t)b * kp.nk + k] : make_double2(0.0, 0.0);
+        const float rQqm = (float)(sq.x + sm.x), iQqm = (float)(sq.y + sm.y);
+        const float Ureck = q.w * (rQqm * rQqm + iQqm * iQqm);
+        float rdip[3] = {0.f, 0.f, 0.f}, idip[3] = {0.f, 0.f, 0.f};
+        if (DIP) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const double2 d = kp.Sdip[((size_t)b * kp.nk + k) * 3 + c];
+                rdip[c] = -(float)d.y;
+                idip[c] = (float)d.x;
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int bb = 0; bb < 3; bb++) {
+                const float v = ((a == bb) ? Ureck : 0.f) - Ureck * coeff2 * kv[a] * kv[bb];
+                const float v1 = 2.f * q.w * kv[a] * (rQqm * rdip[bb] + iQqm * idip[bb]);
+                av[ACC_VIRT + a + 3 * bb] = sc * (v + v1);
+            }
+        if (DIP) av[ACC_VIRIALC] = av[ACC_VIRT + 0] + av[ACC_VIRT + 4] + av[ACC_VIRT + 8];
+    }
+    block_reduce_add_f<14, 128>(av, kp.acc + (size_t)b * NACC);
+}
+
+static void launch_qd_virial(Engine &E, bool dip) {
+    dim3 g((E.kp.nk + 127) / 128, E.kp.P);
+    if (E.precision == PIMD_PREC_MIXED && E.kp.kvirf) {
+        const float sc = (float)(-0.5 * FOURPI / E.kp.volume);
+        if (dip)
+            k_qd_virial_m<true><<<g, 128, 0, E.stream>>>(E.kp, sc);
+        else
+            k_qd_virial_m<false><<<g, 128, 0, E.stream>>>(E.kp, sc);
+    } else if (dip) {
+        k_qd_virial<true><<<g, 128, 0, E.stream>>>(E.kp);
+    } else {
+        k_qd_virial<false><<<g, 128, 0, E.stream>>>(E.kp);
+    }
+    ++E.nlaunch;
+}
+
 // ---------------------------------------------------------------------------------------
 static int spass_groups(const Engine &E, int nsites) {
     const int ntile = (nsites + SP_TS - 1) / SP_TS;
@@ -1064,7 +1145,7 @@ void ewald_init(Engine &E) {
 void launch_ewald_tables(Engine &E) {
     dim3 g((E.kp.S + 127) / 128, E.kp.P);
     if (E.precision == PIMD_PREC_MIXED)
-        k_ewald_tables<float><<<g, 128, 0, E.stream>>>(E.kp);
+        k_ewald_tables_m<<<g, 128, 0, E.stream>>>(E.kp);
     else
         k_ewald_tables<double><<<g, 128, 0, E.stream>>>(E.kp);
     ++E.nlaunch;
@@ -1216,9 +1297,7 @@ void launch_dd_update(Engine &E) { run_field<F_D>(E, E.kp.fd, E.kp.ld); }
 // ewald_std_qd
 void launch_ewald_qd(Engine &E) {
     run_spass<OP_DIP>(E, E.kp.fd, E.kp.ld - E.kp.fd, 0);
-    dim3 g((E.kp.nk + 127) / 128, E.kp.P);
-    k_qd_virial<true><<<g, 128, 0, E.stream>>>(E.kp);
-    ++E.nlaunch;
+    launch_qd_virial(E, true);
     run_field<F_QD>(E, field_s0(E), E.kp.S);
 }
 // ewald_pw_std_qq (ewald.f90:230-291): charge structure factor over all sites, field and
@@ -1226,9 +1305,7 @@ void launch_ewald_qd(Engine &E) {
 void launch_ewald_pw(Engine &E) {
     launch_ewald_sq(E);
     launch_ewald_fq(E);
-    dim3 g((E.kp.nk + 127) / 128, E.kp.P);
-    k_qd_virial<false><<<g, 128, 0, E.stream>>>(E.kp);
-    ++E.nlaunch;
+    launch_qd_virial(E, false);
 }
 
 }  // namespace pimd
