@@ -174,6 +174,8 @@ struct Engine {
     bool ff_tc = true;                // tensor-core dipole field pass (k_field_tc) when tf_ready
     bool tf_ready = false;
     int tf_nr = 0, tf_nph = 0, tf_jm = 0, tf_ncol = 0, tf_kq = 0;
+    bool tf_qd_ready = false;         // the force-pass modes (charge / dipole halves of ewald_std_qd)
+    int tf_nphd = 0, tf_ncold = 0;    // runs per pass and V rows of the dipole-force mode
     const int2 *d_tfkpm = nullptr;    // per (run slot, j): k-vectors of kz = +j, -j
     alignas(64) unsigned char tc_map[128];  // CUtensorMap of the FP32 tables tabf
     size_t cap = 0;
@@ -298,6 +300,7 @@ int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv);
 // tensor-core field passes (ewald_tc.cu): mode F_D (dipole field, SOR update, convergence test)
 // or F_Q (charge field and potential into F); 1 when launched
 int launch_field_tc(Engine &E, int mode, int s0, int s1);
+int launch_field_qd_tc(Engine &E, int s0, int s1);  // ewald_std_qd force pass on the tensor cores
 // launchers (spc.cu): q-SPC/Fw and SPC/F
 void launch_sites_spc(Engine &E);
 void launch_pair_spc(Engine &E);

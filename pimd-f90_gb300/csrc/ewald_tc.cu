@@ -69,8 +69,10 @@ constexpr long long TC_WAIT = 1LL << 28;  // cycles before a wait gives up (~0.1
 
 // structure-factor sums (values as in ewald.cu): charge q e, dipole (k.mu) e, dipole components mu_c e
 enum { TC_OP_Q = 0, TC_OP_MU = 1, TC_OP_DIP = 2 };
-// field passes (values as in ewald.cu): charge field and potential, dipole field + SOR update
-enum { TF_Q = 0, TF_D = 1 };
+// field passes (values as in ewald.cu): charge field and potential, dipole field + SOR update,
+// and the two halves of the force pass ewald_std_qd: TF_QG the charge force and potential from
+// the dipole structure factor, TF_DG the dipole force from the total (charge + dipole) one
+enum { TF_Q = 0, TF_D = 1, TF_QG = 2, TF_DG = 3 };
 
 struct TcGroup {
     int p0, nr, ncol, jm, nkl, kgoff, pad0, pad1;  // slots, runs, MMA columns, kz rows, k-vectors
@@ -589,12 +591,12 @@ struct TfArgs {
 
 struct TfSmem {
     int boxb, A, B, W, total;
-    __host__ __device__ TfSmem(int ntab, int ncol, int kq, int nk) {
+    __host__ __device__ TfSmem(int ntab, int ncol, int kq, int nk, int nslot = 1) {
         boxb = ((ntab * 128 + 1023) / 1024) * 1024;
         A = 8 * boxb;                      // tables of 128 sites: 8 TMA boxes of 16 sites
         B = A + 2 * TF_SITES * kq * 2;     // Q hi, lo: 128 rows x kq halves
         W = B + 2 * ncol * kq * 2;         // V hi, lo: ncol rows x kq halves
-        total = W + ((nk * 8 + 127) / 128) * 128 + 1024;  // the bead's weights Wf
+        total = W + ((nslot * nk * 8 + 127) / 128) * 128 + 1024;  // the bead's weights Wf (1 or 2 slots)
     }
 };
 
@@ -604,6 +606,10 @@ PIMD_D int rowchunk_k(int n, int jc, int kcm) { return (((n >> 3) * kcm + jc) <<
 
 template <int MODE>
 __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ CUtensorMap tmap, KP kp, TfArgs a) {
+    // TF_DG: 6 components per run (T0, T1 and T2 = sum kz^2 W ez, complex), V rebuilt for each
+    // pass of nph runs; the other modes: 4 components, V of both passes built once
+    constexpr bool DG = MODE == TF_DG;
+    constexpr int NC = DG ? 6 : 4;
     const int t = blockIdx.x, b = blockIdx.y;
     if (MODE == TF_D && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) {
         // converged bead: no update, but the block still counts towards the convergence test
@@ -612,7 +618,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         return;
     }
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const TfSmem L(kp.ntab, a.ncol, a.kq, kp.nk);
+    const TfSmem L(kp.ntab, a.ncol, a.kq, kp.nk, DG ? 2 : 1);
     extern __shared__ __align__(1024) unsigned char sm_raw[];
     unsigned char *sm = sm_raw + ((1024u - (umma::smem_u32(sm_raw) & 1023u)) & 1023u);
     __shared__ uint64_t tbar, wbar, mbar;
@@ -625,19 +631,23 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         umma::mbar_init(&tbar, 1);
         umma::mbar_init(&wbar, 1);
         umma::mbar_init(&mbar, 1);
-        const uint32_t wbytes = (uint32_t)kp.nk * 8u;
+        // weight slots: charge (0), dipole (1); TF_DG takes both (adjacent in Wf)
+        const int slot = (MODE == TF_D || MODE == TF_QG) ? 1 : 0;
+        const uint32_t wbytes = (uint32_t)kp.nk * 8u * (DG ? 2u : 1u);
         mbar_expect_tx(&wbar, wbytes);
-        bulk_load(sm + L.W, kp.Wf + ((size_t)b * 2 + (MODE == TF_D ? 1 : 0)) * kp.nk, wbytes, &wbar);
+        bulk_load(sm + L.W, kp.Wf + ((size_t)b * 2 + slot) * kp.nk, wbytes, &wbar);
         const uint32_t box_tx = (uint32_t)(kp.ntab * 128);
         mbar_expect_tx(&tbar, 8 * box_tx);
         for (int i = 0; i < 8; i++) tma_load_2d(sm + i * L.boxb, &tmap, 2 * (sb + 16 * i), b * kp.ntab, &tbar);
     }
     const int iter = kp.dstep[1] + 1;  // dipole iteration of this update
     const int kcm = a.kq / 8, nr = a.nr, nph = a.nph, jm = a.jm;
+    const int npass = DG ? (nr + nph - 1) / nph : 2;
     const int yrow = kp.hmax + 1, zrow = yrow + kp.kmax + 1;
     if (tid < nr) {
         sslot[tid] = a.slot[tid];
-        sskv[tid] = make_float2(a.skv[tid].x * (1.f / TF_WS), a.skv[tid].y * (1.f / TF_WS));
+        const float ws = DG ? 1.f : 1.f / TF_WS;  // TF_DG scales its sums once at the end
+        sskv[tid] = make_float2(a.skv[tid].x * ws, a.skv[tid].y * ws);
     }
     if (warp == 0) umma::tmem_alloc(&tslot, 512);
     // the SOR inputs of the CTA's dipole sites, fetched now
@@ -651,45 +661,61 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     const uint32_t tm = tslot;
     unsigned char *Vh = sm + L.B, *Vl = Vh + a.ncol * a.kq * 2;
     unsigned char *Qh = sm + L.A, *Ql = Qh + TF_SITES * a.kq * 2;
-    // V = the run weights: run p = pass nph + pl, component c at row pass 4 nph + c nph + pl;
-    // 8 halves (4 j) per item, zero for p >= nr and j >= jm
     uint32_t err = (uint32_t)umma::mbar_wait(&wbar, 0, TC_WAIT);
     const float2 *W = reinterpret_cast<const float2 *>(sm + L.W);
-    for (int it = tid; it < 2 * nph * kcm; it += TF_NT) {
-        const int p = it % (2 * nph), jc = it / (2 * nph);
-        const int vrow = (p / nph) * 4 * nph + (p % nph);
-        float v[4][8];
+    // V of runs [p0, p0 + nrow): run p0 + pl, component c at row vrow0 + c nrow + pl; 8 halves
+    // (4 j) per item, zero for runs >= nr and j >= jm
+    auto build_v = [&](int p0, int nrow, int vrow0) {
+        for (int it = tid; it < nrow * kcm; it += TF_NT) {
+            const int pl = it % nrow, jc = it / nrow, p = p0 + pl;
+            float v[NC][8];
 #pragma unroll
-        for (int e = 0; e < 4; e++) {
-            const int j = 4 * jc + e;
-            float2 wp = make_float2(0.f, 0.f), wm = wp;
-            float kz = 0.f;
-            if (p < nr && j < jm) {
-                const int2 km = a.kpm[p * jm + j];
-                const float2 wpl = km.x >= 0 ? W[km.x] : make_float2(0.f, 0.f);
-                const float2 wmi = km.y >= 0 ? W[km.y] : make_float2(0.f, 0.f);
-                wp = make_float2(TF_WS * (wpl.x + wmi.x), TF_WS * (wpl.y + wmi.y));
-                wm = make_float2(TF_WS * (wpl.x - wmi.x), TF_WS * (wpl.y - wmi.y));
-                kz = a.kzv[kp.lmax + j];
+            for (int e = 0; e < 4; e++) {
+                const int j = 4 * jc + e;
+                float2 wp = make_float2(0.f, 0.f), wm = wp;
+                float kz = 0.f;
+                if (p < nr && j < jm) {
+                    const int2 km = a.kpm[p * jm + j];
+                    float2 wpl = km.x >= 0 ? W[km.x] : make_float2(0.f, 0.f);
+                    float2 wmi = km.y >= 0 ? W[km.y] : make_float2(0.f, 0.f);
+                    if (DG) {  // total weights W_q + W_mu
+                        if (km.x >= 0) wpl = make_float2(wpl.x + W[kp.nk + km.x].x, wpl.y + W[kp.nk + km.x].y);
+                        if (km.y >= 0) wmi = make_float2(wmi.x + W[kp.nk + km.y].x, wmi.y + W[kp.nk + km.y].y);
+                    }
+                    wp = make_float2(TF_WS * (wpl.x + wmi.x), TF_WS * (wpl.y + wmi.y));
+                    wm = make_float2(TF_WS * (wpl.x - wmi.x), TF_WS * (wpl.y - wmi.y));
+                    kz = a.kzv[kp.lmax + j];
+                }
+                // (cos, sin) coefficients of T0re, T0im, T1re, T1im (, T2re, T2im)
+                v[0][2 * e] = wp.x;
+                v[0][2 * e + 1] = -wm.y;
+                v[1][2 * e] = wp.y;
+                v[1][2 * e + 1] = wm.x;
+                v[2][2 * e] = kz * wm.x;
+                v[2][2 * e + 1] = -kz * wp.y;
+                v[3][2 * e] = kz * wm.y;
+                v[3][2 * e + 1] = kz * wp.x;
+                if constexpr (DG) {
+                    const float k2 = kz * kz;
+                    v[4][2 * e] = k2 * wp.x;
+                    v[4][2 * e + 1] = -k2 * wm.y;
+                    v[5][2 * e] = k2 * wp.y;
+                    v[5][2 * e + 1] = k2 * wm.x;
+                }
             }
-            // (cos, sin) coefficients of T0re, T0im, T1re, T1im
-            v[0][2 * e] = wp.x;
-            v[0][2 * e + 1] = -wm.y;
-            v[1][2 * e] = wp.y;
-            v[1][2 * e + 1] = wm.x;
-            v[2][2 * e] = kz * wm.x;
-            v[2][2 * e + 1] = -kz * wp.y;
-            v[3][2 * e] = kz * wm.y;
-            v[3][2 * e + 1] = kz * wp.x;
-        }
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-            uint4 hi, lo;
-            split8_h(v[c], hi, lo);
-            const int o = rowchunk_k(vrow + c * nph, jc, kcm);
-            *reinterpret_cast<uint4 *>(Vh + o) = hi;
-            *reinterpret_cast<uint4 *>(Vl + o) = lo;
+            for (int c = 0; c < NC; c++) {
+                uint4 hi, lo;
+                split8_h(v[c], hi, lo);
+                const int o = rowchunk_k(vrow0 + c * nrow + pl, jc, kcm);
+                *reinterpret_cast<uint4 *>(Vh + o) = hi;
+                *reinterpret_cast<uint4 *>(Vl + o) = lo;
+            }
         }
+    };
+    if (!DG) {  // both passes: pass q's rows from q 4 nph
+        build_v(0, nph, 0);
+        build_v(nph, nph, 4 * nph);
     }
     // Q = ez rows of the CTA's sites, 8 halves (4 j: c_j, s_j) per item, zero for j >= jm
     err |= (uint32_t)umma::mbar_wait(&tbar, 0, TC_WAIT);
@@ -709,26 +735,35 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         *reinterpret_cast<uint4 *>(Qh + o) = hi;
         *reinterpret_cast<uint4 *>(Ql + o) = lo;
     }
-    umma::fence_smem_to_async();
-    umma::fence_before_sync();
-    const bool bad0 = __syncthreads_or((int)err) != 0;
-    umma::fence_after_sync();
-    // two passes of nph runs, 4 nph <= 512 TMEM columns each: column c nph + pl for component c
+    // passes of nph runs, NC nph <= 512 TMEM columns each: column c nph + pl for component c
     // of the pass's run pl
     float Ex = 0.f, Ey = 0.f, Ez = 0.f, phi = 0.f;
     const int lq = warp & 3, part = warp >> 2, sl = 32 * lq + lane;
     const int q4 = nph / 4;  // runs per run quarter
-    bool bad = bad0;
-    for (int pass = 0; pass < 2 && !bad; pass++) {
+    // TF_DG: the dipole of the epilogue lane's site (scaled by nothing; zero outside the range)
+    float mu[3] = {0.f, 0.f, 0.f};
+    if (DG && sb + sl >= a.s_lo && sb + sl < a.s_hi) {
+        const float4 m = kp.dipf[(size_t)b * kp.S + sb + sl];
+        mu[0] = m.x, mu[1] = m.y, mu[2] = m.z;
+    }
+    bool bad = err != 0;
+    for (int pass = 0; pass < npass; pass++) {
+        if (DG) build_v(pass * nph, nph, 0);
+        umma::fence_smem_to_async();
+        umma::fence_before_sync();
+        bad = __syncthreads_or((int)bad) != 0;
+        umma::fence_after_sync();
+        if (bad) break;
         if (tid == 0) {
             const uint32_t idesc_base = umma::idesc_f16(128, 16) & ~(0x3Fu << 17);
             const uint32_t qh = umma::smem_u32(Qh), ql = umma::smem_u32(Ql);
             const uint32_t vh = umma::smem_u32(Vh), vl = umma::smem_u32(Vl);
-            for (int c0 = 0; c0 < 4 * nph; c0 += 256) {
-                const int N = min(256, 4 * nph - c0);
+            for (int c0 = 0; c0 < NC * nph; c0 += 256) {
+                const int N = min(256, NC * nph - c0);
                 const uint32_t id = idesc_base | ((uint32_t)(N >> 3) << 17);
                 const uint32_t d = tm + (uint32_t)c0;
-                const uint32_t vo = (uint32_t)(((pass * 4 * nph + c0) >> 3) * kcm * 128);  // row group of V
+                const int vr = (DG ? 0 : pass * 4 * nph) + c0;  // first V row of the MMA
+                const uint32_t vo = (uint32_t)((vr >> 3) * kcm * 128);
                 for (int ks = 0; ks < a.kq / 16; ks++) {
                     const uint64_t dq_h = umma::sdesc(qh + ks * 256, 128, kcm * 128), dq_l = umma::sdesc(ql + ks * 256, 128, kcm * 128);
                     const uint64_t dv_h = umma::sdesc(vh + vo + ks * 256, 128, kcm * 128), dv_l = umma::sdesc(vl + vo + ks * 256, 128, kcm * 128);
@@ -745,12 +780,14 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         umma::fence_after_sync();
         bad = __syncthreads_or(to) != 0;
         if (bad) break;
-        // this warp's run quarter in groups of 16 runs x 4 components (one TMEM wait each)
+        // this warp's run quarter in groups of 16 runs x 4 (6) components (one TMEM wait each)
         for (int pl0 = part * q4; pl0 < (part + 1) * q4; pl0 += 16) {
             if (pass * nph + pl0 >= nr) break;
             float v[64];
             const uint32_t tl = tm + ((uint32_t)(32 * lq) << 16) + (uint32_t)pl0;
             umma::tmem_ld16x4(tl, tl + (uint32_t)nph, tl + (uint32_t)(2 * nph), tl + (uint32_t)(3 * nph), v);
+            float w[32];
+            if constexpr (DG) umma::tmem_ld16x2(tl + (uint32_t)(4 * nph), tl + (uint32_t)(5 * nph), w);
 #pragma unroll
             for (int e = 0; e < 16; e++) {
                 const int pl = pl0 + e, p = pass * nph + pl;
@@ -761,18 +798,35 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
                 if (ky < 0) ey.y = -ey.y;
                 // ewald.f90:30-31: coskxky = cx cy - sx sy, sinkxky = sx cy + cx sy
                 const float er = ex.x * ey.x - ex.y * ey.y, ei = ex.y * ey.x + ex.x * ey.y;
-                const float t0 = fmaf(er, v[16 + e], ei * v[e]);       // Im(exy T0)
-                const float t1 = fmaf(er, v[48 + e], ei * v[32 + e]);  // Im(exy T1)
                 const float2 kv = sskv[p];
-                Ex = fmaf(kv.x, t0, Ex);
-                Ey = fmaf(kv.y, t0, Ey);
-                Ez = fmaf(1.f / TF_WS, t1, Ez);
-                if (MODE == TF_Q) phi = fmaf(1.f / TF_WS, fmaf(er, v[e], -ei * v[16 + e]), phi);  // Re(exy T0)
+                if constexpr (DG) {
+                    // sum_k k (k . mu) Re(e W) with the run's kz sums (ewald.f90:146-187)
+                    const float R0 = fmaf(er, v[e], -ei * v[16 + e]);       // Re(exy T0)
+                    const float R1 = fmaf(er, v[32 + e], -ei * v[48 + e]);  // Re(exy T1)
+                    const float R2 = fmaf(er, w[e], -ei * w[16 + e]);       // Re(exy T2)
+                    const float aa = kv.x * mu[0] + kv.y * mu[1];
+                    const float tt = fmaf(aa, R0, mu[2] * R1);
+                    Ex = fmaf(-kv.x, tt, Ex);
+                    Ey = fmaf(-kv.y, tt, Ey);
+                    Ez -= fmaf(aa, R1, mu[2] * R2);
+                } else {
+                    const float t0 = fmaf(er, v[16 + e], ei * v[e]);       // Im(exy T0)
+                    const float t1 = fmaf(er, v[48 + e], ei * v[32 + e]);  // Im(exy T1)
+                    Ex = fmaf(kv.x, t0, Ex);
+                    Ey = fmaf(kv.y, t0, Ey);
+                    Ez = fmaf(1.f / TF_WS, t1, Ez);
+                    if (MODE == TF_Q || MODE == TF_QG) phi = fmaf(1.f / TF_WS, fmaf(er, v[e], -ei * v[16 + e]), phi);  // Re(exy T0)
+                }
             }
         }
         umma::fence_before_sync();
         __syncthreads();
         umma::fence_after_sync();
+    }
+    if (DG) {
+        Ex *= 1.f / TF_WS;
+        Ey *= 1.f / TF_WS;
+        Ez *= 1.f / TF_WS;
     }
     // the four run quarters of each site, in order
     float *red = reinterpret_cast<float *>(Qh);  // [4][128][4]
@@ -805,6 +859,19 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
             f.z += (double)e[2];
             if (s_own >= kp.fq) f.w += (double)e[3];
             kp.F[gs] = f;
+        }
+        return;
+    }
+    if (MODE == TF_QG || MODE == TF_DG) {
+        // as k_field_finish<F_QD>: dR += -q E (charge part) or the dipole force; phi of the
+        // dipole structure factor at the charged sites
+        if (own && !bad) {
+            const size_t gs = (size_t)b * kp.S + s_own;
+            const double q = MODE == TF_QG ? kp.pos[gs].w : -1.0;
+            kp.dR[3 * gs + 0] -= q * (double)e[0];
+            kp.dR[3 * gs + 1] -= q * (double)e[1];
+            kp.dR[3 * gs + 2] -= q * (double)e[2];
+            if (MODE == TF_QG && s_own >= kp.fq) kp.F[gs].w += (double)e[3];
         }
         return;
     }
@@ -970,16 +1037,21 @@ void tc_init(Engine &E) {
     // 16-run load of a run quarter reaches past the pass
     const int nph = ((nr + 1) / 2 + 7) / 8 * 8, ncolf = 8 * nph, kq = ((2 * jm + 15) / 16) * 16;
     if (4 * nph + 16 > 512) return;
-    cudaFuncAttributes fb, fb2;
-    if (cudaFuncGetAttributes(&fb, k_field_tc<TF_D>) != cudaSuccess || cudaFuncGetAttributes(&fb2, k_field_tc<TF_Q>) != cudaSuccess) {
+    cudaFuncAttributes fb[4];
+    if (cudaFuncGetAttributes(&fb[0], k_field_tc<TF_Q>) != cudaSuccess || cudaFuncGetAttributes(&fb[1], k_field_tc<TF_D>) != cudaSuccess ||
+        cudaFuncGetAttributes(&fb[2], k_field_tc<TF_QG>) != cudaSuccess || cudaFuncGetAttributes(&fb[3], k_field_tc<TF_DG>) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
-    const int dmaxf = optin - (int)std::max(fb.sharedSizeBytes, fb2.sharedSizeBytes);
+    size_t fstat = 0;
+    for (int i = 0; i < 4; i++) fstat = std::max(fstat, fb[i].sharedSizeBytes);
+    const int dmaxf = optin - (int)fstat;
     // the weights arrive by one bulk copy: 8 nk bytes, a multiple of 16
     if (TfSmem(kp.ntab, ncolf, kq, kp.nk).total > dmaxf || kp.ntab > 128 || (kp.nk & 1)) return;
     if (cudaFuncSetAttribute(k_field_tc<TF_D>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess ||
-        cudaFuncSetAttribute(k_field_tc<TF_Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess) {
+        cudaFuncSetAttribute(k_field_tc<TF_Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess ||
+        cudaFuncSetAttribute(k_field_tc<TF_QG>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess ||
+        cudaFuncSetAttribute(k_field_tc<TF_DG>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess) {
         cudaGetLastError();
         return;
     }
@@ -1007,11 +1079,19 @@ void tc_init(Engine &E) {
     E.tf_ncol = ncolf;
     E.tf_kq = kq;
     E.tf_ready = true;
+    // dipole-force mode: 6 components per run, passes of nphd runs (a multiple of 8) with
+    // 6 nphd + 16 <= 512 TMEM columns, V of one pass at a time, both weight slots resident
+    const int npd = (nr + 79) / 80;
+    const int nphd = ((nr + npd - 1) / npd + 7) / 8 * 8, ncold = 6 * nphd;
+    E.tf_qd_ready = 6 * nphd + 16 <= 512 && TfSmem(kp.ntab, ncold, kq, kp.nk, 2).total <= dmaxf;
+    E.tf_nphd = nphd;
+    E.tf_ncold = ncold;
 }
 
 // mode TF_D: dipole field, SOR update and convergence test of one iteration at the dipole sites
 // [s0, s1) (k_field_f<F_D> + k_field_finish<F_D>); TF_Q: charge field and potential added to F at
-// [s0, s1) (k_field_f<F_Q> + k_field_finish<F_Q>). 1 when launched, else 0.
+// [s0, s1) (k_field_f<F_Q> + k_field_finish<F_Q>); TF_QG, TF_DG: the halves of the force pass
+// (launch_field_qd_tc). 1 when launched, else 0.
 int launch_field_tc(Engine &E, int mode, int s0, int s1) {
     if (!E.tc_ready || !E.tf_ready || !E.ff_tc || s1 <= s0) return 0;
     const KP &kp = E.kp;
@@ -1028,14 +1108,32 @@ int launch_field_tc(Engine &E, int mode, int s0, int s1) {
     a.sbase = s0 & ~(TC_SS - 1);  // TMA x coordinates 2 (sbase + 16 i): 128-byte aligned
     a.s_lo = s0;
     a.s_hi = s1;
-    const TfSmem L(kp.ntab, a.ncol, a.kq, kp.nk);
+    if (mode == TF_DG) {
+        a.nph = E.tf_nphd;
+        a.ncol = E.tf_ncold;
+    }
+    const TfSmem L(kp.ntab, a.ncol, a.kq, kp.nk, mode == TF_DG ? 2 : 1);
     dim3 g((s1 - a.sbase + TF_SITES - 1) / TF_SITES, kp.P);
     const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(E.tc_map);
     if (mode == TF_D)
         k_field_tc<TF_D><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
-    else
+    else if (mode == TF_Q)
         k_field_tc<TF_Q><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
+    else if (mode == TF_QG)
+        k_field_tc<TF_QG><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
+    else
+        k_field_tc<TF_DG><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
     ++E.nlaunch;
+    return 1;
+}
+
+// ewald_std_qd's force pass (k_field_f<F_QD> + k_field_finish<F_QD>) as two tensor-core passes:
+// the charge force -q E and potential from the dipole structure factor at [s0, s1), then the
+// dipole force at the dipole sites from the total structure factor. 1 when launched, else 0.
+int launch_field_qd_tc(Engine &E, int s0, int s1) {
+    if (!E.tc_ready || !E.tf_ready || !E.tf_qd_ready || !E.ff_tc || s1 <= s0) return 0;
+    launch_field_tc(E, TF_QG, s0, s1);
+    if (E.kp.ld > E.kp.fd) launch_field_tc(E, TF_DG, E.kp.fd, E.kp.ld);
     return 1;
 }
 
