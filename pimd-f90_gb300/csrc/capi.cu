@@ -985,6 +985,7 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     if (n >= 7) k[6] = E.sf_tc && E.tc_ready;
     if (n >= 8) k[7] = E.ff_tc && E.tf_ready;
     if (n >= 9) k[8] = E.dd_overlap && E.aux_stream != nullptr && E.precision == PIMD_MIXED;
+    if (n >= 10) k[9] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
     return PIMD_OK;
 }
 

@@ -373,17 +373,18 @@ class ForceEngine:
 
     TUNING_KEYS = ("sf_tiled", "sf_groups", "ff_regs", "max_slices", "nbr_block", "wave_shapes", "sf_tc", "ff_tc",
                    "dd_overlap")
+    TUNING_REPORTS = ("qd_tc",)  # read-only: tensor-core force pass in use
 
     def tuning(self):
-        n = len(self.TUNING_KEYS)
+        n = len(self.TUNING_KEYS) + len(self.TUNING_REPORTS)
         k = (ctypes.c_int * n)()
         self._check(load().pimd_get_tuning(self.h, k, n), "get_tuning")
-        return {name: k[i] for i, name in enumerate(self.TUNING_KEYS)}
+        return {name: k[i] for i, name in enumerate(self.TUNING_KEYS + self.TUNING_REPORTS)}
 
     def set_tuning(self, **knobs):
         """Set launch-shape knobs by name (the keys of tuning()); the others keep their values."""
         cur = self.tuning()
-        unknown = set(knobs) - set(cur)
+        unknown = set(knobs) - set(self.TUNING_KEYS)
         if unknown:
             raise ValueError("unknown tuning knobs: %s" % sorted(unknown))
         cur.update({k: int(v) for k, v in knobs.items()})

@@ -165,10 +165,18 @@ def test_tensor_core_structure_factor_active(pkg, orc, engine_lib, model):
     c, p = small_case(pkg, model, nw=64, P=4, polar_maxiter=40)
     eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_MIXED)
     got = eng.full_bead_forces(c["RRt"], c["RRc"], t=1)
-    assert eng.tuning()["sf_tc"] == 1 and eng.tuning()["ff_tc"] == 1
+    tun = eng.tuning()
+    assert tun["sf_tc"] == 1 and tun["ff_tc"] == 1 and tun["qd_tc"] == 1
     ref = orc.full_bead_forces(p, c["RRt"], c["RRc"], t=1)
     assert rms_rel(got["dRRt"], ref["dRRt"]) < 1e-5
     assert rms_rel(got["dip_momIt"], ref["dip_momIt"]) < 1e-5
+    assert np.abs(got["virialt"] - ref["virialt"]).max() < 1e-5 * np.abs(ref["virialt"]).max() + 1e-3
+    # the field passes (dipole, charge, force) on the FP32 pipe instead agree within the budget
+    eng.set_tuning(ff_tc=0)
+    alt = eng.full_bead_forces(c["RRt"], c["RRc"], t=1)
+    assert eng.tuning()["qd_tc"] == 0
+    assert rms_rel(alt["dRRt"], got["dRRt"]) < 1e-5
+    eng.close()
 
 
 def test_mixed_headline_and_convergence(pkg, orc, engine_lib):
