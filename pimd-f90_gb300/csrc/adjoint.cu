@@ -46,6 +46,7 @@ int apply_theta(Engine &E) {
     kp.vdwC = th[PIMD_TH_VDW_C];
     kp.vdwD = th[PIMD_TH_VDW_D];
     kp.vdwE = th[PIMD_TH_VDW_E];
+    kp_float_tables(kp);
     kp.dms1 = th[PIMD_TH_DMS1];
     kp.dms2 = th[PIMD_TH_DMS2];
     kp.dms3 = th[PIMD_TH_DMS3];

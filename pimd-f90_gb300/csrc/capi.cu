@@ -312,6 +312,7 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
     kp.ew.cts2 = 4.0 * a * a * a / (3.0 * SQPI);
     kp.ew.cts3 = 8.0 * (a * a * a * a * a) / (15.0 * SQPI);
     kp.ewf = EwCf{(float)kp.ew.aewald, (float)kp.ew.a2, (float)kp.ew.cts1, (float)kp.ew.cts2, (float)kp.ew.cts3};
+    kp_float_tables(kp);
     kp.stath = DEBYE / CHARGECON / std::sqrt((double)kp.natoms);
     kp.factor = 4.0 * (a * a * a) / (3.0 * std::sqrt(PI));
     // neighbour-list capacity: 3x the expected O-O pairs, at most all pairs

@@ -44,6 +44,15 @@ struct PairTables {
     double apol_cd[5][5];  // aCCaCD * polfac(i) * polfac(j)
 };
 
+// FP32 copies of the pair constants for the mixed engine's pair kernels (converted once on the
+// host, so no FP64-to-FP32 conversion -- an FP64-pipe instruction -- sits in a pair loop)
+struct PairTablesF {
+    float apol_qq[5][5], ra_qq[5][5], apol_dd[5][5], apol_cd[5][5];
+    float vdw[5];            // vdwA .. vdwE
+    float shiftA, shiftB, rc1;
+    float box[3], boxi[3];
+};
+
 // k-space run: a maximal block of consecutive k-vectors with equal (kx, ky); kz runs over
 // [kzlo, kzlo + nkz). kbeg is the index of the first k-vector of the run.
 struct KRun {
@@ -65,6 +74,7 @@ struct KP {
     double box[3], boxi[3], volume, rc2, rc1;
     float boxq[3];  // box / 2^32 (FP32): the length of one unit of ofix
     double vdwA, vdwB, vdwC, vdwD, vdwE, shiftA, shiftB;
+    PairTablesF ptf;  // FP32 copies of pt, the vdW constants and the box (kp_float_tables)
     double gammaM, polar[5], dms1, dms2, dms3, polar_sor, stath, factor, Uvdw_lrc;
     double qO, qH, roh0, th0, harmkb, harmka;
     const double *c5z;   // NASA PES coefficients for non-default scale factors (null: published)
@@ -125,6 +135,26 @@ struct KP {
     unsigned *fin_counter;        // blocks done in the dipole field pass (fused convergence test)
     unsigned long long cond;      // CUDA-graph conditional handle of the dipole loop (0: host loop)
 };
+
+// refresh kp.ptf from the FP64 constants (after they are set or changed)
+inline void kp_float_tables(KP &kp) {
+    for (int i = 0; i < 5; i++)
+        for (int j = 0; j < 5; j++) {
+            kp.ptf.apol_qq[i][j] = (float)kp.pt.apol_qq[i][j];
+            kp.ptf.ra_qq[i][j] = (float)kp.pt.ra_qq[i][j];
+            kp.ptf.apol_dd[i][j] = (float)kp.pt.apol_dd[i][j];
+            kp.ptf.apol_cd[i][j] = (float)kp.pt.apol_cd[i][j];
+        }
+    const double v[5] = {kp.vdwA, kp.vdwB, kp.vdwC, kp.vdwD, kp.vdwE};
+    for (int i = 0; i < 5; i++) kp.ptf.vdw[i] = (float)v[i];
+    kp.ptf.shiftA = (float)kp.shiftA;
+    kp.ptf.shiftB = (float)kp.shiftB;
+    kp.ptf.rc1 = (float)kp.rc1;
+    for (int c = 0; c < 3; c++) {
+        kp.ptf.box[c] = (float)kp.box[c];
+        kp.ptf.boxi[c] = (float)kp.boxi[c];
+    }
+}
 
 // replica of bead b and its centroid sites (posc[replica][S])
 PIMD_HD int rep_of(const KP &kp, int b) { return kp.brep ? kp.brep[b] : 0; }

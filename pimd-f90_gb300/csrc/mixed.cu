@@ -200,10 +200,10 @@ __global__ void __launch_bounds__(128) k_pair_qq_m(KP kp) {
     const float4 *rh = kp.rhof + (size_t)b * kp.S;
     const uint4 *of = kp.ofix + (size_t)b * N;
     const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
-    const float L[3] = {(float)kp.box[0], (float)kp.box[1], (float)kp.box[2]};
-    const float Li[3] = {(float)kp.boxi[0], (float)kp.boxi[1], (float)kp.boxi[2]};
-    const float vA = kp.vdwA, vB = kp.vdwB, vC = kp.vdwC, vD = kp.vdwD, vE = kp.vdwE;
-    const float sA = kp.shiftA, sB = kp.shiftB, r1 = kp.rc1;
+    const float L[3] = {kp.ptf.box[0], kp.ptf.box[1], kp.ptf.box[2]};
+    const float Li[3] = {kp.ptf.boxi[0], kp.ptf.boxi[1], kp.ptf.boxi[2]};
+    const float vA = kp.ptf.vdw[0], vB = kp.ptf.vdw[1], vC = kp.ptf.vdw[2], vD = kp.ptf.vdw[3], vE = kp.ptf.vdw[4];
+    const float sA = kp.ptf.shiftA, sB = kp.ptf.shiftB, r1 = kp.ptf.rc1;
     float av[14];  // per-lane FP32 partials, reduced in FP64 per warp (block_reduce_add_f)
 #pragma unroll
     for (int q = 0; q < 14; q++) av[q] = 0.f;
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(128) k_pair_qq_m(KP kp) {
                                          wrapf(Rf[2] + di[isp].z - dj[jsp].z, L[2], Li[2])};
                     const float d2 = Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2];
                     float ts0, ts1;
-                    smear01_m(d2, (float)kp.pt.apol_qq[isp][jsp], (float)kp.pt.ra_qq[isp][jsp], kp.ewf, kp.gq23, &ts0, &ts1);
+                    smear01_m(d2, kp.ptf.apol_qq[isp][jsp], kp.ptf.ra_qq[isp][jsp], kp.ewf, kp.gq23, &ts0, &ts1);
                     const float qj = dj[jsp].w;
 #pragma unroll
                     for (int c = 0; c < 3; c++) Fi[isp][c] += ts1 * qj * Rs[c];
@@ -333,8 +333,8 @@ __global__ void __launch_bounds__(128) k_dd_tensors_m(KP kp) {
     const uint4 *of = kp.ofix + (size_t)b * N;
     const float4 *pf = kp.posf + (size_t)b * kp.S;
     const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
-    const float L[3] = {(float)kp.box[0], (float)kp.box[1], (float)kp.box[2]};
-    const float Li[3] = {(float)kp.boxi[0], (float)kp.boxi[1], (float)kp.boxi[2]};
+    const float L[3] = {kp.ptf.box[0], kp.ptf.box[1], kp.ptf.box[2]};
+    const float Li[3] = {kp.ptf.boxi[0], kp.ptf.boxi[1], kp.ptf.boxi[2]};
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
         const int2 ij = fl[e];
         float Rf[3];
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(128) k_dd_tensors_m(KP kp) {
                 const float Rs[3] = {wrapf(Rf[0] + a.x - c.x, L[0], Li[0]), wrapf(Rf[1] + a.y - c.y, L[1], Li[1]),
                                      wrapf(Rf[2] + a.z - c.z, L[2], Li[2])};
                 float t1, t2;
-                smear2<float>(Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2], (float)kp.pt.apol_dd[isp][jsp], kp.ewf, &t1, &t2);
+                smear2<float>(Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2], kp.ptf.apol_dd[isp][jsp], kp.ewf, &t1, &t2);
                 const float t3 = 3.f * t2;
                 Te[6 * t + 0] = t3 * Rs[0] * Rs[0] - t1;
                 Te[6 * t + 1] = t3 * Rs[1] * Rs[1] - t1;
@@ -458,8 +458,8 @@ __global__ void __launch_bounds__(128) k_pair_force_m(KP kp) {
     const float4 *orw = kp.orawf + (size_t)b * N;
     const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
     const bool same_a = kp.same_acd != 0;
-    const float L[3] = {(float)kp.box[0], (float)kp.box[1], (float)kp.box[2]};
-    const float Li[3] = {(float)kp.boxi[0], (float)kp.boxi[1], (float)kp.boxi[2]};
+    const float L[3] = {kp.ptf.box[0], kp.ptf.box[1], kp.ptf.box[2]};
+    const float Li[3] = {kp.ptf.boxi[0], kp.ptf.boxi[1], kp.ptf.boxi[2]};
     float av[14];  // per-lane FP32 partials, reduced in FP64 per warp (block_reduce_add_f)
 #pragma unroll
     for (int q = 0; q < 14; q++) av[q] = 0.f;
@@ -517,7 +517,7 @@ __global__ void __launch_bounds__(128) k_pair_force_m(KP kp) {
                     bool have = false;
                     if (T::dip(isp) && T::dip(jsp)) {
                         float t1, t2, t3;
-                        smear3<float>(d2, (float)kp.pt.apol_dd[isp][jsp], kp.ewf, &t1, &t2, &t3);
+                        smear3<float>(d2, kp.ptf.apol_dd[isp][jsp], kp.ewf, &t1, &t2, &t3);
                         dd_force_f(Rs, di, dj, t2, t3, dij);
                         if (same_a) {
                             ts1 = t1, ts2 = t2;
@@ -525,7 +525,7 @@ __global__ void __launch_bounds__(128) k_pair_force_m(KP kp) {
                         }
                     }
                     if (qd2 > 1.e-9f) {
-                        if (!have) smear2<float>(d2, (float)kp.pt.apol_cd[isp][jsp], kp.ewf, &ts1, &ts2);
+                        if (!have) smear2<float>(d2, kp.ptf.apol_cd[isp][jsp], kp.ewf, &ts1, &ts2);
                         const float rq = Rs[0] * qd[0] + Rs[1] * qd[1] + Rs[2] * qd[2];
 #pragma unroll
                         for (int c = 0; c < 3; c++) dij[c] += 3.f * ts2 * rq * Rs[c] - ts1 * qd[c];
@@ -560,7 +560,7 @@ __global__ void __launch_bounds__(128) k_pair_force_m(KP kp) {
                     float dij[3] = {0, 0, 0};
                     if (T::dip(isp) && T::dip(jsp)) {
                         float t1, t2, t3;
-                        smear3<float>(d2, (float)kp.pt.apol_dd[isp][jsp], kp.ewf, &t1, &t2, &t3);
+                        smear3<float>(d2, kp.ptf.apol_dd[isp][jsp], kp.ewf, &t1, &t2, &t3);
                         dd_force_f(Rs, mi[isp], mi[jsp], t2, t3, dij);
                     }
                     const float qi = si[isp].w, qj = si[jsp].w;

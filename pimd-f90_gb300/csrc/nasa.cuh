@@ -12,6 +12,8 @@ namespace pimd {
 // module): nasa_upload_constants() fills this unit's copy.
 static __constant__ double c_c5z[245];
 static __constant__ double c_coefD[84];
+static __constant__ float c_c5zf[245];  // FP32 copies for the mixed engine's polynomial sums
+static __constant__ float c_coefDf[84];
 static __constant__ unsigned char c_idx[245][3];
 static __constant__ unsigned char c_idxD[84][3];
 // The sums of pot_nasa (terms 1..244) and dms_nasa (terms 1..83) regrouped by the powers (i, j)
@@ -69,6 +71,11 @@ static inline void nasa_upload_constants() {
     }
     cudaMemcpyToSymbol(c_c5z, c5z, sizeof(c5z));
     cudaMemcpyToSymbol(c_coefD, PIMD_NASA_COEFD, sizeof(double) * 84);
+    float c5zf[245], coefDf[84];
+    for (int j = 0; j < 245; j++) c5zf[j] = (float)c5z[j];
+    for (int j = 0; j < 84; j++) coefDf[j] = (float)PIMD_NASA_COEFD[j];
+    cudaMemcpyToSymbol(c_c5zf, c5zf, sizeof(c5zf));
+    cudaMemcpyToSymbol(c_coefDf, coefDf, sizeof(coefDf));
     cudaMemcpyToSymbol(c_idx, idx, sizeof(idx));
     cudaMemcpyToSymbol(c_idxD, idxD, sizeof(idxD));
     unsigned char pg[NASA_PG][4] = {}, dg[NASA_DG][4] = {};
@@ -85,11 +92,55 @@ static inline void nasa_upload_constants() {
     cudaMemcpyToSymbol(c_ngrp, ng, sizeof(ng));
 }
 
+// The PES polynomial sums (nasa.f90:62-72) in the arithmetic type S: sum0 = sum_t c_t sym_t
+// f3[k_t], sum3 its x3-derivative, sum1, sum2 the x1-, x2-derivatives. Per (i, j) group the
+// k-sum is a polynomial in x3, evaluated by Horner together with its derivative (two FMAs per
+// term). S = float (the mixed engine, published coefficients only) keeps the rest of the
+// monomer in FP64: the sums carry about 1e-7 relative error into the gradient.
+template <typename S>
+PIMD_D void nasa_pot_sums(double x1d, double x2d, double x3d, const double *c5zg, double &s0d, double &s1d, double &s2d,
+                          double &s3d) {
+    const S x1 = (S)x1d, x2 = (S)x2d, x3 = (S)x3d;
+    S f1[16], f2[16];
+    f1[0] = f2[0] = S(0);
+    f1[1] = f2[1] = S(1);
+#pragma unroll
+    for (int j = 2; j <= 15; j++) {
+        f1[j] = f1[j - 1] * x1;
+        f2[j] = f2[j - 1] * x2;
+    }
+    S sum0 = 0, sum1 = 0, sum2 = 0, sum3 = 0;
+    for (int g = 0; g < c_ngrp[0]; g++) {
+        const int inI = c_pg[g][0], inJ = c_pg[g][1], s0 = c_pg[g][2], n = c_pg[g][3];
+        S pk = S(0), dpk = S(0);
+        for (int t = 0; t < n; t++) {
+            const int j = c_ps[s0 + t];
+            S c;
+            if (sizeof(S) == sizeof(float))
+                c = j < 0 ? S(0) : (S)c_c5zf[j];
+            else
+                c = j < 0 ? S(0) : (S)(c5zg ? c5zg[j] : c_c5z[j]);
+            dpk = dpk * x3 + pk;
+            pk = pk * x3 + c;
+        }
+        const S sym = f1[inI] * f2[inJ] + f1[inJ] * f2[inI];
+        sum0 += sym * pk;
+        sum1 += ((S)(inI - 1) * f1[inI - 1] * f2[inJ] + (S)(inJ - 1) * f1[inJ - 1] * f2[inI]) * pk;
+        sum2 += ((S)(inJ - 1) * f1[inI] * f2[inJ - 1] + (S)(inI - 1) * f1[inJ] * f2[inI - 1]) * pk;
+        sum3 += sym * dpk;
+    }
+    s0d = (double)sum0;
+    s1d = (double)sum1;
+    s2d = (double)sum2;
+    s3d = (double)sum3;
+}
+
 // r1[atom][comp]: atoms O, H1, H2. Returns energy (kcal/mol) and gradient dr1[atom][comp].
 // c5zg: the 245 combined coefficients when the four scale factors differ from the published
 // ones (null: the constant-memory table), f5z: the CCSD(T)/5Z scale factor of deoh and phh1.
+// fsum: polynomial sums in FP32 (ignored with c5zg).
 PIMD_D void nasa_pot(const double r1[3][3], const double box[3], const double boxi[3], double dr1[3][3],
-                     double *e1, const double *c5zg = nullptr, double f5z = PIMD_NASA_F5Z) {
+                     double *e1, const double *c5zg = nullptr, double f5z = PIMD_NASA_F5Z, bool fsum = false) {
     double ROH1[3], ROH2[3], RHH[3];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
@@ -114,35 +165,12 @@ PIMD_D void nasa_pot(const double r1[3][3], const double box[3], const double bo
     const double dVa2 = 2.0 * alphaoh * deoh * exp2 * (1.0 - exp2) / dROH2;
     const double dVb = -phh2 * Vb / dRHH;
     const double x1 = (dROH1 - reoh) / reoh, x2 = (dROH2 - reoh) / reoh, x3 = costh - costhe;
-    double f1[16], f2[16], f3[16];
-    f1[0] = f2[0] = f3[0] = 0.0;
-    f1[1] = f2[1] = f3[1] = 1.0;
-#pragma unroll
-    for (int j = 2; j <= 15; j++) {
-        f1[j] = f1[j - 1] * x1;
-        f2[j] = f2[j - 1] * x2;
-        f3[j] = f3[j - 1] * x3;
-    }
     const double efac = exp(-b1 * ((dROH1 - reoh) * (dROH1 - reoh) + (dROH2 - reoh) * (dROH2 - reoh)));
-    // sum0 = sum_t c_t sym_t f3[k_t], sum3 its x3-derivative, sum1, sum2 the x1-, x2-derivatives
-    // (nasa.f90:62-72): per (i, j) group the k-sum is a polynomial in x3, evaluated by Horner
-    // together with its derivative, so each term costs two FMAs
-    double sum0 = 0, sum1 = 0, sum2 = 0, sum3 = 0;
-    for (int g = 0; g < c_ngrp[0]; g++) {
-        const int inI = c_pg[g][0], inJ = c_pg[g][1], s0 = c_pg[g][2], n = c_pg[g][3];
-        double pk = 0.0, dpk = 0.0;
-        for (int t = 0; t < n; t++) {
-            const int j = c_ps[s0 + t];
-            const double c = j < 0 ? 0.0 : (c5zg ? c5zg[j] : c_c5z[j]);
-            dpk = dpk * x3 + pk;
-            pk = pk * x3 + c;
-        }
-        const double sym = f1[inI] * f2[inJ] + f1[inJ] * f2[inI];
-        sum0 += sym * pk;
-        sum1 += ((double)(inI - 1) * f1[inI - 1] * f2[inJ] + (double)(inJ - 1) * f1[inJ - 1] * f2[inI]) * pk;
-        sum2 += ((double)(inJ - 1) * f1[inI] * f2[inJ - 1] + (double)(inI - 1) * f1[inJ] * f2[inI - 1]) * pk;
-        sum3 += sym * dpk;
-    }
+    double sum0, sum1, sum2, sum3;
+    if (fsum && !c5zg)
+        nasa_pot_sums<float>(x1, x2, x3, nullptr, sum0, sum1, sum2, sum3);
+    else
+        nasa_pot_sums<double>(x1, x2, x3, c5zg, sum0, sum1, sum2, sum3);
     const double Vc = 2.0 * (c5zg ? c5zg[0] : c_c5z[0]) + efac * sum0;
     *e1 = ((Va + Vb + Vc) + 0.44739574026257) * 0.00285914375100642899;
     const double dVcdr1 = (-2.0 * b1 * efac * (dROH1 - reoh) * sum0 + efac * sum1 / reoh) / dROH1;
@@ -235,10 +263,52 @@ PIMD_D void nasa_dms_finish(const double ROH1[3], const double ROH2[3], double d
     }
 }
 
+// The DMS polynomial sums (nasa.f90:229-241) regrouped by (i, j) with Horner in x3, as in
+// nasa_pot_sums, in the arithmetic type S: P1, P2 and their x1-, x2- and x3-derivatives.
+template <typename S>
+PIMD_D void nasa_dms_sums(double x1d, double x2d, double x3d, double (&out)[8]) {
+    const S x1 = (S)x1d, x2 = (S)x2d, x3 = (S)x3d;
+    S f1[16], f2[16];
+    f1[0] = f2[0] = S(0);
+    f1[1] = f2[1] = S(1);
+#pragma unroll
+    for (int j = 2; j <= 15; j++) {
+        f1[j] = f1[j - 1] * x1;
+        f2[j] = f2[j - 1] * x2;
+    }
+    S P1 = 0, P2 = 0, dp1dr1 = 0, dp1dr2 = 0, dp1dcabc = 0, dp2dr1 = 0, dp2dr2 = 0, dp2dcabc = 0;
+    for (int g = 0; g < c_ngrp[1]; g++) {
+        const int inI = c_dg[g][0], inJ = c_dg[g][1], s0 = c_dg[g][2], n = c_dg[g][3];
+        S qk = S(0), dqk = S(0);
+        for (int t = 0; t < n; t++) {
+            const int j = c_ds[s0 + t];
+            S c;
+            if (sizeof(S) == sizeof(float))
+                c = j < 0 ? S(0) : (S)c_coefDf[j];
+            else
+                c = j < 0 ? S(0) : (S)c_coefD[j];
+            dqk = dqk * x3 + qk;
+            qk = qk * x3 + c;
+        }
+        const S a = f1[inI] * f2[inJ], bb = f1[inJ] * f2[inI];
+        P1 += a * qk;
+        P2 += bb * qk;
+        dp1dr1 += (S)(inI - 1) * f1[inI - 1] * f2[inJ] * qk;
+        dp1dr2 += (S)(inJ - 1) * f1[inI] * f2[inJ - 1] * qk;
+        dp1dcabc += a * dqk;
+        dp2dr1 += (S)(inJ - 1) * f1[inJ - 1] * f2[inI] * qk;
+        dp2dr2 += (S)(inI - 1) * f1[inJ] * f2[inI - 1] * qk;
+        dp2dcabc += bb * dqk;
+    }
+    const S r[8] = {P1, P2, dp1dr1, dp1dr2, dp1dcabc, dp2dr1, dp2dr2, dp2dcabc};
+#pragma unroll
+    for (int i = 0; i < 8; i++) out[i] = (double)r[i];
+}
+
 // dms_nasa: site charges q3 (O, H1, H2) in e and gradq[a][b][c] = d q_b / d x_{a,c}
 // with a = H1, H2, O (the reference's gradq(a, b, c) ordering).
 PIMD_D void nasa_dms(const double r1[3][3], const double box[3], const double boxi[3], double dms1, double dms2,
-                     double dms3, double q3[3], double gradq[3][3][3]) {
+                     double dms3, double q3[3], double gradq[3][3][3], bool fsum = false) {
     const double reoh = PIMD_NASA_REOH, b1D = PIMD_NASA_B1D, costhe = -.24780227221366464506;
     double ROH1[3], ROH2[3];
 #pragma unroll
@@ -251,37 +321,14 @@ PIMD_D void nasa_dms(const double r1[3][3], const double box[3], const double bo
     const double costh = (ROH1[0] * ROH2[0] + ROH1[1] * ROH2[1] + ROH1[2] * ROH2[2]) / (dROH1 * dROH2);
     const double efac = exp(-b1D * ((dROH1 - reoh) * (dROH1 - reoh) + (dROH2 - reoh) * (dROH2 - reoh)));
     const double x1 = (dROH1 - reoh) / reoh, x2 = (dROH2 - reoh) / reoh, x3 = costh - costhe;
-    double f1[16], f2[16], f3[16];
-    f1[0] = f2[0] = f3[0] = 0.0;
-    f1[1] = f2[1] = f3[1] = 1.0;
-#pragma unroll
-    for (int j = 2; j <= 15; j++) {
-        f1[j] = f1[j - 1] * x1;
-        f2[j] = f2[j - 1] * x2;
-        f3[j] = f3[j - 1] * x3;
-    }
-    double P1 = 0, P2 = 0;
     const double PL1 = costh, PL2 = 0.5 * (3.0 * PL1 * PL1 - 1.0);
-    double dp1dr1 = 0, dp1dr2 = 0, dp1dcabc = 0, dp2dr1 = 0, dp2dr2 = 0, dp2dcabc = 0;
-    // nasa.f90:229-241 regrouped by (i, j) with Horner in x3, as in nasa_pot
-    for (int g = 0; g < c_ngrp[1]; g++) {
-        const int inI = c_dg[g][0], inJ = c_dg[g][1], s0 = c_dg[g][2], n = c_dg[g][3];
-        double qk = 0.0, dqk = 0.0;
-        for (int t = 0; t < n; t++) {
-            const int j = c_ds[s0 + t];
-            dqk = dqk * x3 + qk;
-            qk = qk * x3 + (j < 0 ? 0.0 : c_coefD[j]);
-        }
-        const double a = f1[inI] * f2[inJ], bb = f1[inJ] * f2[inI];
-        P1 += a * qk;
-        P2 += bb * qk;
-        dp1dr1 += (double)(inI - 1) * f1[inI - 1] * f2[inJ] * qk;
-        dp1dr2 += (double)(inJ - 1) * f1[inI] * f2[inJ - 1] * qk;
-        dp1dcabc += a * dqk;
-        dp2dr1 += (double)(inJ - 1) * f1[inJ - 1] * f2[inI] * qk;
-        dp2dr2 += (double)(inI - 1) * f1[inJ] * f2[inI - 1] * qk;
-        dp2dcabc += bb * dqk;
-    }
+    double sums[8];
+    if (fsum)
+        nasa_dms_sums<float>(x1, x2, x3, sums);
+    else
+        nasa_dms_sums<double>(x1, x2, x3, sums);
+    const double P1 = sums[0], P2 = sums[1], dp1dr1 = sums[2], dp1dr2 = sums[3], dp1dcabc = sums[4], dp2dr1 = sums[5],
+                 dp2dr2 = sums[6], dp2dcabc = sums[7];
     nasa_dms_finish(ROH1, ROH2, dROH1, dROH2, costh, efac, P1, P2, dp1dr1, dp1dr2, dp1dcabc, dp2dr1, dp2dr2, dp2dcabc,
                     PL1, PL2, dms1, dms2, dms3, q3, gradq);
 }

@@ -45,7 +45,8 @@ PIMD_D double3 ld3(const double *p) { return make_double3(p[0], p[1], p[2]); }
 // warps per SM at 512 x 32), so the warps are spread over every SM rather than packed 4 per block.
 constexpr int SITES_NT = 32;
 
-template <int MODEL>
+// FSUM: the NASA polynomial sums in FP32 (the mixed engine)
+template <int MODEL, bool FSUM>
 __global__ void __launch_bounds__(SITES_NT) k_sites(KP kp) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     const int b = blockIdx.y;
@@ -78,7 +79,7 @@ __global__ void __launch_bounds__(SITES_NT) k_sites(KP kp) {
         }
         double dr1[3][3], e1 = 0.0;
         if (!kp.contraction) {
-            nasa_pot(R, kp.box, kp.boxi, dr1, &e1, kp.c5z, kp.nasa_f5z);
+            nasa_pot(R, kp.box, kp.boxi, dr1, &e1, kp.c5z, kp.nasa_f5z, FSUM);
         } else {
 #pragma unroll
             for (int k = 0; k < 3; k++)
@@ -87,7 +88,7 @@ __global__ void __launch_bounds__(SITES_NT) k_sites(KP kp) {
         }
         av[ACC_UMON] = e1;
         double q3[3], dq3[3][3][3];
-        nasa_dms(R, kp.box, kp.boxi, kp.dms1, kp.dms2, kp.dms3, q3, dq3);
+        nasa_dms(R, kp.box, kp.boxi, kp.dms1, kp.dms2, kp.dms3, q3, dq3, FSUM);
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             q3[k] *= CHARGECON;
@@ -784,7 +785,19 @@ static int pair_blocks(const Engine &E) {
 
 void launch_sites(Engine &E) {
     dim3 g((E.kp.N + SITES_NT - 1) / SITES_NT, E.kp.P);
-    DISPATCH_TTM(E, k_sites, g, SITES_NT);
+    const bool f = E.precision == PIMD_PREC_MIXED;
+    if (E.kp.model == 2) {
+        if (f)
+            k_sites<2, true><<<g, SITES_NT, 0, E.stream>>>(E.kp);
+        else
+            k_sites<2, false><<<g, SITES_NT, 0, E.stream>>>(E.kp);
+    } else {
+        if (f)
+            k_sites<3, true><<<g, SITES_NT, 0, E.stream>>>(E.kp);
+        else
+            k_sites<3, false><<<g, SITES_NT, 0, E.stream>>>(E.kp);
+    }
+    ++E.nlaunch;
 }
 
 void launch_pair_qq(Engine &E) {
