@@ -80,23 +80,26 @@ PIMD_D void dd_sor_site(const KP &kp, int b, int s, const double (&E)[3], int it
 // End of a dipole-update block: its sums go into the bead's acc[ACC_DSQ], acc[ACC_MUEFQ] (when
 // add), then the block counts itself and the last block of the launch runs the convergence
 // test (a device counter, reset by that block). Every thread of every block of the launch calls
-// this exactly once; blocks of converged beads call it with add = false.
-template <int NT>
+// this exactly once; blocks of converged beads call it with add = false. Only the first NWA
+// warps may hold nonzero sums (the others skip the FP64 shuffles; the totals are unchanged).
+template <int NT, int NWA = NT / 32>
 PIMD_D void dd_block_end(const KP &kp, int b, const double (&av)[2], bool add) {
     if (add) {
-        __shared__ double red[NT / 32][2];
+        __shared__ double red[NWA][2];
         const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+        if (wp < NWA) {
 #pragma unroll
-        for (int i = 0; i < 2; i++) {
-            double x = av[i];
+            for (int i = 0; i < 2; i++) {
+                double x = av[i];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            if (lane == 0) red[wp][i] = x;
+                for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                if (lane == 0) red[wp][i] = x;
+            }
         }
         __syncthreads();
         if (threadIdx.x < 2) {
             double t = 0;
-            for (int w = 0; w < NT / 32; w++) t += red[w][threadIdx.x];
+            for (int w = 0; w < NWA; w++) t += red[w][threadIdx.x];
             atomicAdd(kp.acc + (size_t)b * NACC + ACC_DSQ + threadIdx.x, t);
         }
     }

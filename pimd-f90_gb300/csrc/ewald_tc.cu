@@ -650,6 +650,22 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         sskv[tid] = make_float2(a.skv[tid].x * ws, a.skv[tid].y * ws);
     }
     if (warp == 0) umma::tmem_alloc(&tslot, 512);
+    // the (k(+j), k(-j)) pairs and k_z of a V item (run p0 + it % nrow, j = 4 (it / nrow) + e):
+    // this thread's first item of each early V build is fetched now, before the weights land
+    auto fetch_km = [&](int p0, int nrow, int it, int2 (&km)[4], float (&kz)[4]) {
+        const int p = p0 + it % nrow, jc = it / nrow;
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int j = 4 * jc + e;
+            const bool ok = it < nrow * kcm && p < nr && j < jm;
+            km[e] = ok ? a.kpm[p * jm + j] : make_int2(-1, -1);
+            kz[e] = ok ? a.kzv[kp.lmax + j] : 0.f;
+        }
+    };
+    int2 km0[4], km1[4];
+    float kz0[4], kz1[4];
+    fetch_km(0, nph, tid, km0, kz0);
+    fetch_km(DG ? 0 : nph, nph, tid, km1, kz1);
     // the SOR inputs of the CTA's dipole sites, fetched now
     const int s_own = sb + tid;
     const bool own = tid < TF_SITES && s_own >= a.s_lo && s_own < a.s_hi;
@@ -665,26 +681,31 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     const float2 *W = reinterpret_cast<const float2 *>(sm + L.W);
     // V of runs [p0, p0 + nrow): run p0 + pl, component c at row vrow0 + c nrow + pl; 8 halves
     // (4 j) per item, zero for runs >= nr and j >= jm
-    auto build_v = [&](int p0, int nrow, int vrow0) {
+    auto build_v = [&](int p0, int nrow, int vrow0, const int2 (&kmf)[4], const float (&kzf)[4]) {
         for (int it = tid; it < nrow * kcm; it += TF_NT) {
-            const int pl = it % nrow, jc = it / nrow, p = p0 + pl;
+            const int pl = it % nrow, jc = it / nrow;
+            int2 km[4];
+            float kzz[4];
+            if (it == tid) {
+#pragma unroll
+                for (int e = 0; e < 4; e++) km[e] = kmf[e], kzz[e] = kzf[e];
+            } else {
+                fetch_km(p0, nrow, it, km, kzz);
+            }
             float v[NC][8];
 #pragma unroll
             for (int e = 0; e < 4; e++) {
-                const int j = 4 * jc + e;
                 float2 wp = make_float2(0.f, 0.f), wm = wp;
-                float kz = 0.f;
-                if (p < nr && j < jm) {
-                    const int2 km = a.kpm[p * jm + j];
-                    float2 wpl = km.x >= 0 ? W[km.x] : make_float2(0.f, 0.f);
-                    float2 wmi = km.y >= 0 ? W[km.y] : make_float2(0.f, 0.f);
+                const float kz = kzz[e];
+                {
+                    float2 wpl = km[e].x >= 0 ? W[km[e].x] : make_float2(0.f, 0.f);
+                    float2 wmi = km[e].y >= 0 ? W[km[e].y] : make_float2(0.f, 0.f);
                     if (DG) {  // total weights W_q + W_mu
-                        if (km.x >= 0) wpl = make_float2(wpl.x + W[kp.nk + km.x].x, wpl.y + W[kp.nk + km.x].y);
-                        if (km.y >= 0) wmi = make_float2(wmi.x + W[kp.nk + km.y].x, wmi.y + W[kp.nk + km.y].y);
+                        if (km[e].x >= 0) wpl = make_float2(wpl.x + W[kp.nk + km[e].x].x, wpl.y + W[kp.nk + km[e].x].y);
+                        if (km[e].y >= 0) wmi = make_float2(wmi.x + W[kp.nk + km[e].y].x, wmi.y + W[kp.nk + km[e].y].y);
                     }
                     wp = make_float2(TF_WS * (wpl.x + wmi.x), TF_WS * (wpl.y + wmi.y));
                     wm = make_float2(TF_WS * (wpl.x - wmi.x), TF_WS * (wpl.y - wmi.y));
-                    kz = a.kzv[kp.lmax + j];
                 }
                 // (cos, sin) coefficients of T0re, T0im, T1re, T1im (, T2re, T2im)
                 v[0][2 * e] = wp.x;
@@ -714,8 +735,8 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         }
     };
     if (!DG) {  // both passes: pass q's rows from q 4 nph
-        build_v(0, nph, 0);
-        build_v(nph, nph, 4 * nph);
+        build_v(0, nph, 0, km0, kz0);
+        build_v(nph, nph, 4 * nph, km1, kz1);
     }
     // Q = ez rows of the CTA's sites, 8 halves (4 j: c_j, s_j) per item, zero for j >= jm
     err |= (uint32_t)umma::mbar_wait(&tbar, 0, TC_WAIT);
@@ -748,7 +769,14 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     }
     bool bad = err != 0;
     for (int pass = 0; pass < npass; pass++) {
-        if (DG) build_v(pass * nph, nph, 0);
+        if (DG) {
+            if (pass == 0) {
+                build_v(0, nph, 0, km0, kz0);
+            } else {
+                fetch_km(pass * nph, nph, tid, km1, kz1);
+                build_v(pass * nph, nph, 0, km1, kz1);
+            }
+        }
         umma::fence_smem_to_async();
         umma::fence_before_sync();
         bad = __syncthreads_or((int)bad) != 0;
@@ -881,7 +909,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         const double E[3] = {(double)e[0], (double)e[1], (double)e[2]};
         dd_sor_apply(kp, b, s_own, din, E, iter, av);
     }
-    dd_block_end<TF_NT>(kp, b, av, !bad);
+    dd_block_end<TF_NT, TF_SITES / 32>(kp, b, av, !bad);  // own sites: threads < TF_SITES
 }
 
 // ---------------------------------------------------------------------------------------
