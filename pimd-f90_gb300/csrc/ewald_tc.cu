@@ -623,7 +623,9 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     unsigned char *sm = sm_raw + ((1024u - (umma::smem_u32(sm_raw) & 1023u)) & 1023u);
     __shared__ uint64_t tbar, wbar, mbar;
     __shared__ uint32_t tslot;
-    __shared__ int4 sslot[TC_MAXRUN];
+    // per run: byte offsets of the ex and ey table rows in a stage and their swizzle keys (16 x
+    // (row & 7)); bit 0 of the ey key: ky < 0 (conjugate ey)
+    __shared__ int4 sroff[TC_MAXRUN];
     __shared__ float2 sskv[TC_MAXRUN];
     const int sb = a.sbase + t * TF_SITES;
     // the copies go out first: the bead's weights (one bulk copy) and the tables of 128 sites
@@ -645,7 +647,9 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     const int npass = DG ? (nr + nph - 1) / nph : 2;
     const int yrow = kp.hmax + 1, zrow = yrow + kp.kmax + 1;
     if (tid < nr) {
-        sslot[tid] = a.slot[tid];
+        const int kxy = a.slot[tid].x, kx = kxy & 255, ky = (kxy >> 8) - 128;
+        const int ry = yrow + (ky < 0 ? -ky : ky);
+        sroff[tid] = make_int4(kx * 128, (kx & 7) << 4, ry * 128, ((ry & 7) << 4) | (ky < 0 ? 1 : 0));
         const float ws = DG ? 1.f : 1.f / TF_WS;  // TF_DG scales its sums once at the end
         sskv[tid] = make_float2(a.skv[tid].x * ws, a.skv[tid].y * ws);
     }
@@ -761,6 +765,10 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     float Ex = 0.f, Ey = 0.f, Ez = 0.f, phi = 0.f;
     const int lq = warp & 3, part = warp >> 2, sl = 32 * lq + lane;
     const int q4 = nph / 4;  // runs per run quarter
+    // the epilogue lane's site in the staged tables: its box and float2 slot, and its 16-byte
+    // chunk (before the swizzle) times 16
+    const unsigned char *tsite = sm + (sl >> 4) * L.boxb + (sl & 1) * 8;
+    const int cs4 = ((sl & 15) >> 1) << 4;
     // TF_DG: the dipole of the epilogue lane's site (scaled by nothing; zero outside the range)
     float mu[3] = {0.f, 0.f, 0.f};
     if (DG && sb + sl >= a.s_lo && sb + sl < a.s_hi) {
@@ -820,10 +828,11 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
             for (int e = 0; e < 16; e++) {
                 const int pl = pl0 + e, p = pass * nph + pl;
                 if (pl >= (part + 1) * q4 || p >= nr) break;
-                const int kxy = sslot[p].x, kx = kxy & 255, ky = (kxy >> 8) - 128;
-                const float2 ex = tab_elem(sm, L.boxb, kx, sl);
-                float2 ey = tab_elem(sm, L.boxb, yrow + (ky < 0 ? -ky : ky), sl);
-                if (ky < 0) ey.y = -ey.y;
+                // tab_elem(sm, boxb, row, sl) with the run's row offsets and keys precomputed
+                const int4 ro = sroff[p];
+                const float2 ex = *reinterpret_cast<const float2 *>(tsite + ro.x + (cs4 ^ ro.y));
+                float2 ey = *reinterpret_cast<const float2 *>(tsite + ro.z + (cs4 ^ (ro.w & ~1)));
+                if (ro.w & 1) ey.y = -ey.y;
                 // ewald.f90:30-31: coskxky = cx cy - sx sy, sinkxky = sx cy + cx sy
                 const float er = ex.x * ey.x - ex.y * ey.y, ei = ex.y * ey.x + ex.x * ey.y;
                 const float2 kv = sskv[p];
