@@ -96,6 +96,8 @@ struct TcArgs {
     int ncolmax;          // max MMA columns over run groups
     int nabuf;            // operand buffers
     int skipconv;
+    uint4 *xcache;        // X operand blocks of the dipole sites (null: no cache), see k_sfac_tc
+    int xsub, xblock;     // 16-site blocks per bead and run group, bytes per block
 };
 
 // Shared-memory carve-up (bytes from a 1024-aligned base), used by the kernel and the launcher.
@@ -140,6 +142,16 @@ PIMD_D void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      umma::smem_u32(dst)),
                  "l"((unsigned long long)src), "r"(bytes), "r"(umma::smem_u32(bar))
+                 : "memory");
+}
+// the same with an L2 evict-first policy (data read once per kernel that should not displace
+// the working set of the other kernels)
+PIMD_D void bulk_load_stream(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+                     umma::smem_u32(dst)),
+                 "l"((unsigned long long)src), "r"(bytes), "r"(umma::smem_u32(bar)), "l"(pol)
                  : "memory");
 }
 PIMD_D void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
@@ -196,6 +208,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     // the swizzle pattern follows shared-memory address bits 7-9: align the base to 1024 bytes
     unsigned char *sm = sm_raw + ((1024u - (umma::smem_u32(sm_raw) & 1023u)) & 1023u);
     __shared__ uint64_t tfull[TC_NST], mfull[TC_NST], tempty[TC_NST], afull[TC_NABUF_MAX], aempty[TC_NABUF_MAX];
+    __shared__ uint64_t xfull[TC_NABUF_MAX];  // a cached X block has landed in the buffer
     __shared__ uint32_t tslot;
     __shared__ int4 sslot[TC_MAXRUN];
     __shared__ float2 sskv[TC_MAXRUN];
@@ -208,6 +221,15 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     const int yrow = kp.hmax + 1;            // first ey row (ky = 0); ez rows follow the ky rows
     const int nab = a.nabuf, jm = G.jm, nr = G.nr;
     const int xlo = a.ncolmax * 32;          // X lo after X hi
+    // X = exy(site, run) depends on the positions only, so the dipole structure factor of the
+    // iterations builds it once per force call: the first iteration (no iteration done yet)
+    // builds and stores it (xm 1), later ones load it by bulk copies (xm 2) and build only Z.
+    // A block holds the X rows [0, 2 nr) rounded to 8-row groups, hi then lo, in the operand
+    // layout; the cache is zeroed once, so the rows past 2 nr stay zero.
+    const int xm = (OP == TC_OP_MU && a.xcache) ? (kp.dstep[1] == 0 ? 1 : 2) : 0;
+    const int xbytes = ((2 * nr + 7) / 8) * 256;
+    uint4 *xc = xm ? a.xcache + ((size_t)(b * gridDim.y + tg) * a.xsub + (g0 - a.sbase) / TC_KS) * (a.xblock / 16)
+                   : nullptr;
 
     if (tid < nr) {
         sslot[tid] = a.slot[G.p0 + tid];
@@ -237,6 +259,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
         for (int i = 0; i < nab; i++) {
             umma::mbar_init(&afull[i], TC_NB);
             umma::mbar_init(&aempty[i], 1);
+            umma::mbar_init(&xfull[i], 1);
         }
         // the first stages go out now, under the rest of the set-up
         for (int ts = 0; ts < min(nstage, TC_NST); ts++) issue_stage(ts);
@@ -269,7 +292,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
             const int it = bt + u * 32 * TC_NB;
             it_off[u] = it_xr[u] = it_yr[u] = it_o[u] = 0;
             it_ys[u] = 1.f;
-            if (it >= 2 * nr) continue;
+            if (it >= 2 * nr || xm == 2) continue;
             it_n = u + 1;
             const int p = it >> 1, o = it & 1;
             const int kxy = sslot[p].x, kx = kxy & 255, ky = (kxy >> 8) - 128;
@@ -282,7 +305,8 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
         // Z items: one row (c, j, cos|sin) x 8 sites each, on the whole warps after the X items
         // (else on the last warp), at most TC_ZMAX per thread; row decoded once here
         const int nzi = 2 * NCZ * jm * 2;
-        const int zwarps = max(1, TC_NB - (2 * nr + 31) / 32), zthreads = 32 * zwarps, zbase = 32 * TC_NB - zthreads;
+        const int zwarps = xm == 2 ? TC_NB : max(1, TC_NB - (2 * nr + 31) / 32);
+        const int zthreads = 32 * zwarps, zbase = 32 * TC_NB - zthreads;
         int zn = 0, zoff[TC_ZMAX], zmo[TC_ZMAX], zer[TC_ZMAX], zcs[TC_ZMAX], zq[TC_ZMAX];
 #pragma unroll
         for (int u = 0; u < TC_ZMAX; u++) {
@@ -307,6 +331,12 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
                 if (use > 0) err |= (uint32_t)umma::mbar_wait(&aempty[ab], (uint32_t)((use - 1) & 1), TC_WAIT);
                 unsigned char *Bf = sm + L.buf + ab * L.bufstride;
                 const int so = ks * TC_KS;
+                uint4 *xb = xm ? xc + (size_t)sub * (a.xblock / 16) : nullptr;  // this block in the cache
+                if (xm == 2 && bt == 0) {
+                    mbar_expect_tx(&xfull[ab], 2u * (uint32_t)xbytes);
+                    bulk_load_stream(Bf + L.xoff, xb, (uint32_t)xbytes, &xfull[ab]);
+                    bulk_load_stream(Bf + L.xoff + xlo, xb + xbytes / 16, (uint32_t)xbytes, &xfull[ab]);
+                }
 #pragma unroll
                 for (int u = 0; u < 2; u++) {
                     if (u >= it_n) break;
@@ -331,6 +361,13 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
                     *reinterpret_cast<uint4 *>(xp + 16) = ih;
                     *reinterpret_cast<uint4 *>(xp + xlo) = rl;
                     *reinterpret_cast<uint4 *>(xp + xlo + 16) = il;
+                    if (xm == 1) {
+                        uint4 *g = xb + it_off[u] / 16;
+                        g[0] = rh;
+                        g[1] = ih;
+                        g[xbytes / 16] = rl;
+                        g[xbytes / 16 + 1] = il;
+                    }
                 }
 #pragma unroll
                 for (int u = 0; u < TC_ZMAX; u++) {
@@ -365,6 +402,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
             for (int sub = 0; sub < nsub && !err; sub++) {
                 const int ab = sub % nab, use = sub / nab;
                 err |= (uint32_t)umma::mbar_wait(&afull[ab], (uint32_t)(use & 1), TC_WAIT);
+                if (xm == 2) err |= (uint32_t)umma::mbar_wait(&xfull[ab], (uint32_t)(use & 1), TC_WAIT);
                 if (err) break;
                 umma::fence_after_sync();
                 const uint32_t zH = umma::smem_u32(sm + L.buf + ab * L.bufstride), zL = zH + 128 * 32;
@@ -1062,6 +1100,27 @@ void tc_init(Engine &E) {
     E.d_tcgrp = d_groups;
     E.d_tckloc = d_kloc;
     E.d_tckzv = d_kzv;
+    // X-operand cache of the dipole sites (k_sfac_tc, TC_OP_MU): per bead and run group, one
+    // block per 16 sites from the first site group's base, hi and lo rows [0, 2 nr) rounded to
+    // 8-row groups; zero-filled once (the padding rows are never written)
+    E.d_tcx = nullptr;
+    if (kp.ld > kp.fd) {
+        int xb = 0;
+        for (const TcGroup &g : groups) xb = std::max(xb, ((2 * g.nr + 7) / 8) * 256);
+        const int sbase = kp.fd & ~(TC_SS - 1);
+        const int xsub = (kp.ld - sbase + TC_SS - 1) / TC_SS * (TC_SS / TC_KS);  // whole table stages
+        const size_t bytes = (size_t)kp.P * groups.size() * xsub * 2 * xb;
+        void *d_x = nullptr;
+        if (cudaMalloc(&d_x, bytes) == cudaSuccess) {
+            E.allocs.push_back(d_x);
+            cudaMemset(d_x, 0, bytes);
+            E.d_tcx = d_x;
+            E.tc_xsub = xsub;
+            E.tc_xblock = 2 * xb;
+        } else {
+            cudaGetLastError();
+        }
+    }
     E.tc_ntg = (int)groups.size();
     E.tc_ncolmax = ncolmax;
     E.tc_nabuf = nabuf;
@@ -1191,6 +1250,11 @@ int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv) {
     a.ncolmax = E.tc_ncolmax;
     a.nabuf = E.tc_nabuf;
     a.skipconv = skipconv;
+    // the iterations' dipole structure factor caches X (its site range is the cached one)
+    const bool xok = op == TC_OP_MU && E.d_tcx && E.tc_xcache && s0 == kp.fd && nsites == kp.ld - kp.fd;
+    a.xcache = xok ? reinterpret_cast<uint4 *>(E.d_tcx) : nullptr;
+    a.xsub = E.tc_xsub;
+    a.xblock = E.tc_xblock;
     // one CTA per SM (shared memory); site groups (= cluster size) so that one wave fills the GPU
     static int nsm_cache[64] = {0};
     int &nsm = nsm_cache[E.device & 63];
