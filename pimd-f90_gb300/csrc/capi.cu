@@ -919,7 +919,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         std::vector<int> cand;
     };
     int sf_tiled = E.sf_tiled, ff_regs = E.ff_regs, nbr_block = E.nbr_block, wave = E.wave_shapes;
-    int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc, ff_tc = E.ff_tc, dd_overlap = E.dd_overlap;
+    int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc, ff_tc = E.ff_tc, dd_overlap = E.dd_overlap, xcache = E.tc_xcache;
     std::vector<Knob> knobs;
     const bool mixed = E.precision == PIMD_MIXED && E.kp.model < 4;
     if (mixed) {
@@ -929,6 +929,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         knobs.push_back({&E.sf_groups, {0, 4, 8, 16, 32}});
         knobs.push_back({&ff_regs, {1, 0}});
         if (E.aux_stream) knobs.push_back({&dd_overlap, {1, 0}});
+        if (E.d_tcx) knobs.push_back({&xcache, {1, 0}});
     }
     knobs.push_back({&wave, {1, 0}});
     knobs.push_back({&E.max_slices, {16, 8, 4, 2}});
@@ -943,6 +944,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         E.sf_tc = sf_tc != 0;
         E.ff_tc = ff_tc != 0;
         E.dd_overlap = dd_overlap != 0;
+        E.tc_xcache = xcache != 0;
     };
     int rc = PIMD_OK;
     float best;
@@ -986,7 +988,8 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     if (n >= 7) k[6] = E.sf_tc && E.tc_ready;
     if (n >= 8) k[7] = E.ff_tc && E.tf_ready;
     if (n >= 9) k[8] = E.dd_overlap && E.aux_stream != nullptr && E.precision == PIMD_MIXED;
-    if (n >= 10) k[9] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
+    if (n >= 10) k[9] = E.tc_xcache && E.d_tcx != nullptr && E.sf_tc && E.tc_ready;
+    if (n >= 11) k[10] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
     return PIMD_OK;
 }
 
@@ -1003,6 +1006,7 @@ int pimd_set_tuning(pimd_ctx *ctx, const int *k, int n) {
     if (n >= 7) E.sf_tc = k[6] != 0;
     if (n >= 8) E.ff_tc = k[7] != 0;
     if (n >= 9) E.dd_overlap = k[8] != 0;
+    if (n >= 10) E.tc_xcache = k[9] != 0;
     E.gkey.clear();  // a captured MD-step graph holds the old launches: capture again
     return PIMD_OK;
 }

@@ -171,6 +171,13 @@ def test_tensor_core_structure_factor_active(pkg, orc, engine_lib, model):
     assert rms_rel(got["dRRt"], ref["dRRt"]) < 1e-5
     assert rms_rel(got["dip_momIt"], ref["dip_momIt"]) < 1e-5
     assert np.abs(got["virialt"] - ref["virialt"]).max() < 1e-5 * np.abs(ref["virialt"]).max() + 1e-3
+    assert tun["x_cache"] == 1
+    # building X in every iteration (no cache) is the same arithmetic: equal up to the FP64
+    # atomic order of the block sums
+    eng.set_tuning(x_cache=0)
+    nocache = eng.full_bead_forces(c["RRt"], c["RRc"], t=1)
+    assert eng.tuning()["x_cache"] == 0
+    assert rms_rel(nocache["dRRt"], got["dRRt"]) < 1e-9
     # the field passes (dipole, charge, force) on the FP32 pipe instead agree within the budget
     eng.set_tuning(ff_tc=0)
     alt = eng.full_bead_forces(c["RRt"], c["RRc"], t=1)
