@@ -156,6 +156,12 @@ inline void kp_float_tables(KP &kp) {
     }
 }
 
+// acc[ACC_CONV] != 0.0 (bead b's dipoles converged) tested on the bits, without an FP64 compare
+PIMD_D bool bead_converged(const KP &kp, int b) {
+    const unsigned long long u = reinterpret_cast<const unsigned long long *>(kp.acc)[(size_t)b * NACC + ACC_CONV];
+    return (u & 0x7fffffffffffffffULL) != 0ULL;
+}
+
 // replica of bead b and its centroid sites (posc[replica][S])
 PIMD_HD int rep_of(const KP &kp, int b) { return kp.brep ? kp.brep[b] : 0; }
 PIMD_HD const double4_32a *posc_of(const KP &kp, int b) { return kp.posc + (size_t)rep_of(kp, b) * kp.S; }

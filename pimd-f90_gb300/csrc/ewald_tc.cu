@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     constexpr int NPT = (OP == TC_OP_DIP) ? 3 : 1;
     const int grp = blockIdx.x, tg = blockIdx.y, b = blockIdx.z;
     // the whole cluster (same bead) leaves together
-    if (a.skipconv && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
+    if (a.skipconv && bead_converged(kp, b)) return;
     const TcGroup G = a.grp[tg];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const TcSmem L(kp.ntab, a.ncolmax, a.nabuf);
@@ -649,7 +649,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     constexpr bool DG = MODE == TF_DG;
     constexpr int NC = DG ? 6 : 4;
     const int t = blockIdx.x, b = blockIdx.y;
-    if (MODE == TF_D && kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) {
+    if (MODE == TF_D && bead_converged(kp, b)) {
         // converged bead: no update, but the block still counts towards the convergence test
         const double zero[2] = {0.0, 0.0};
         dd_block_end<TF_NT>(kp, b, zero, false);

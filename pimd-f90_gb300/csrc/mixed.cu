@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
     const int lane = threadIdx.x & 31;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, b = blockIdx.y, N = kp.N;
     if (i >= N) return;
-    if (kp.acc[(size_t)b * NACC + ACC_CONV] != 0.0) return;
+    if (bead_converged(kp, b)) return;
     const double *dip = kp.dip + (size_t)b * kp.S * 3;
     const float4 *dipf = kp.dipf + (size_t)b * kp.S;
     const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
@@ -407,6 +407,15 @@ __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
             ei[k][c] = v;
         }
+    double *Ef = kp.Efdr + (size_t)b * kp.S * 3;
+    if (MODEL != 2) {  // every lane holds the sums: lanes 0-2 store one component each
+        if (lane < 3) {
+#pragma unroll
+            for (int k = T::FDI; k <= T::LDI; k++)
+                Ef[3 * ((k - 1) * N + i) + lane] = (double)(lane == 0 ? ei[k][0] : lane == 1 ? ei[k][1] : ei[k][2]);
+        }
+        return;
+    }
     if (lane != 0) return;
     if (MODEL == 2) {  // intramolecular O-H1, O-H2, H1-H2 from the FP64 per-molecule cache
         const double *Tw = kp.Tself + ((size_t)b * N + i) * 18;
@@ -425,7 +434,6 @@ __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
                 ei[c + 1][2] += (float)(Tt[4] * ma[0] + Tt[5] * ma[1] + Tt[2] * ma[2]);
             }
     }
-    double *Ef = kp.Efdr + (size_t)b * kp.S * 3;
 #pragma unroll
     for (int k = T::FDI; k <= T::LDI; k++)
 #pragma unroll
