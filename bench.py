@@ -146,8 +146,9 @@ def workload(pkg, name):
 
 
 # DRAM bytes (read + write) of one mixed ewald_std_dd call at the headline workload, from one
-# ncu capture of its two kernels (k_sfac_tc 5.5 MB + k_field_tc 6.1 MB, cold cache)
-DD_TRAFFIC_BYTES = 11.6e6
+# ncu capture of its two kernels (k_sfac_tc 34.8 MB -- the tables plus the cached X operand,
+# 31.5 MB, loaded evict-first -- and k_field_tc 7.4 MB, cold cache)
+DD_TRAFFIC_BYTES = 42.3e6
 
 
 def tensor_flops_dd(nmax, ndip, P):
