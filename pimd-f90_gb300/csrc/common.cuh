@@ -119,19 +119,37 @@ PIMD_D void smear01(R drsq, R a_pol12, R ra, const EC &e, R *ts0, R *ts1, unsign
     *ts1 = t1;
 }
 
+// dd = r, dri = 1/r from r^2, and exp: FP64 as the reference (sqrt, divide, exp); FP32 (the mixed
+// engine) by the hardware reciprocal square root and exp2 (a few ulp, below the FP32 noise of
+// the pair sums)
+template <typename R>
+PIMD_D void rinv(R drsq, R &dd, R &dri);
+template <>
+PIMD_D void rinv<double>(double drsq, double &dd, double &dri) {
+    dd = sqrt(drsq);
+    dri = 1.0 / dd;
+}
+template <>
+PIMD_D void rinv<float>(float drsq, float &dd, float &dri) {
+    dri = rsqrtf(drsq);
+    dd = drsq * dri;
+}
+PIMD_D double exp_p(double x) { return exp(x); }
+PIMD_D float exp_p(float x) { return __expf(x); }
+
 // smear.f90:36-69 PBCsmear2
 template <typename R, typename EC>
 PIMD_D void smear2(R drsq, R a_pol12, const EC &e, R *ts1, R *ts2) {
-    R dd = sqrt(drsq);
-    R dri = R(1) / dd;
+    R dd, dri;
+    rinv<R>(drsq, dd, dri);
     R drsqi = dri * dri;
-    R expon = exp(-(R(e.a2) * drsq));
+    R expon = exp_p(-(R(e.a2) * drsq));
     R er = erfc_as<R>(R(e.aewald) * dd);
     R t1 = (er * dri + R(e.cts1) * expon) * drsqi;
     R t2 = (t1 + R(e.cts2) * expon) * drsqi;
     if (drsq < R(25)) {
         R rA3 = (dd * drsq) * a_pol12;
-        R exp1 = exp(-rA3);
+        R exp1 = exp_p(-rA3);
         R ch1 = -dri * drsqi;
         R ch2 = ch1 * drsqi;
         R sr1 = (R(1) - exp1) * dri * drsqi;
@@ -146,17 +164,17 @@ PIMD_D void smear2(R drsq, R a_pol12, const EC &e, R *ts1, R *ts2) {
 // smear.f90:71-107 PBCsmear3
 template <typename R, typename EC>
 PIMD_D void smear3(R drsq, R a_pol12, const EC &e, R *ts1, R *ts2, R *ts3) {
-    R dd = sqrt(drsq);
-    R dri = R(1) / dd;
+    R dd, dri;
+    rinv<R>(drsq, dd, dri);
     R drsqi = dri * dri;
-    R expon = exp(-(R(e.a2) * drsq));
+    R expon = exp_p(-(R(e.a2) * drsq));
     R er = erfc_as<R>(R(e.aewald) * dd);
     R t1 = (er * dri + R(e.cts1) * expon) * drsqi;
     R t2 = (t1 + R(e.cts2) * expon) * drsqi;
     R t3 = (t2 + R(e.cts3) * expon) * drsqi;
     if (drsq < R(25)) {
         R rA3 = (dd * drsq) * a_pol12;
-        R exp1 = exp(-rA3);
+        R exp1 = exp_p(-rA3);
         R ch1 = -dri * drsqi;
         R ch2 = ch1 * drsqi;
         R ch3 = ch2 * drsqi;

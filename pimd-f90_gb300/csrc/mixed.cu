@@ -113,16 +113,16 @@ PIMD_D float gq_h(const float4 *tab, float u) {
 
 // smear01<float> (smear.f90:2-34) with the tabulated Q(2/3, x)
 PIMD_D void smear01_m(float drsq, float a_pol12, float ra, const EwCf &e, const float4 *gq, float *ts0, float *ts1) {
-    const float dd = sqrtf(drsq);
-    const float dri = 1.f / dd;
+    float dd, dri;
+    rinv<float>(drsq, dd, dri);
     const float drsqi = dri * dri;
-    const float expon = expf(-(e.a2 * drsq));
+    const float expon = __expf(-(e.a2 * drsq));
     const float er = erfc_as<float>(e.aewald * dd);
     float t0 = er * dri;
     float t1 = (t0 + e.cts1 * expon) * drsqi;
     if (drsq < 25.f) {
         const float rA3 = dd * drsq * a_pol12;
-        const float exp1 = expf(-rA3);
+        const float exp1 = __expf(-rA3);
         const float ch1 = -dri * drsqi;
         const float sr1 = (1.f - exp1) * dri * drsqi;
         t1 = t1 + ch1 + sr1;
@@ -576,7 +576,9 @@ __global__ void __launch_bounds__(128) k_pair_force_m(KP kp) {
 #pragma unroll
                     for (int c = 0; c < 3; c++) qd[c] = qj * mi[isp][c] - qi * mi[jsp][c];
                     // self2 (smear.f90:133-156) in FP32
-                    const float dd = sqrtf(d2), drsqi = 1.f / d2, dri = sqrtf(drsqi);
+                    float dd, dri;
+                    rinv<float>(d2, dd, dri);
+                    const float drsqi = dri * dri;
                     const float expon = __expf(-(kp.ewf.a2 * d2));
                     const float kr0 = erfc_as<float>(kp.ewf.aewald * dd) * dri;
                     const float kr1 = (kr0 + kp.ewf.cts1 * expon) * drsqi;
