@@ -40,15 +40,19 @@ PIMD_D double3 ld3(const double *p) { return make_double3(p[0], p[1], p[2]); }
 
 // ---------------------------------------------------------------------------------------
 // pot_ttm.f90:56-151 and 232-261: site layout, M sites, NASA PES + DMS charges, monomer
-// virials, self energy and intramolecular Ewald exclusions. One thread per (molecule, bead).
-// 32-thread blocks: one molecule per thread is FP64-latency-bound at this occupancy (about 3
-// warps per SM at 512 x 32), so the warps are spread over every SM rather than packed 4 per block.
-constexpr int SITES_NT = 32;
+// virials, self energy and intramolecular Ewald exclusions. Two threads per (molecule, bead),
+// in two warps of a 64-thread block (32 molecules): the first warp evaluates the PES
+// (nasa_pot), the monomer virial and the gradient rows; the second the DMS charges (nasa_dms),
+// their gradients, the site rows, the self energy and the intramolecular exclusions. The two
+// halves share no data, so the FP64-latency-bound chain of a molecule is split in two; about 7
+// warps per SM at 512 x 32, spread over every SM.
+constexpr int SITES_NT = 64;
 
 // FSUM: the NASA polynomial sums in FP32 (the mixed engine)
 template <int MODEL, bool FSUM>
 __global__ void __launch_bounds__(SITES_NT) k_sites(KP kp) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    const int w = blockIdx.x * (SITES_NT / 2) + (threadIdx.x & 31);
+    const bool pes = threadIdx.x < 32;  // warp-uniform roles
     const int b = blockIdx.y;
     const int N = kp.N, S = kp.S;
     double av[14];
@@ -77,121 +81,128 @@ __global__ void __launch_bounds__(SITES_NT) k_sites(KP kp) {
             r2 = min_image_rn(__dsub_rn(Rc[2][c], Rc[0][c]), kp.box[c], kp.boxi[c]);
             Rc[3][c] = __dadd_rn(__dmul_rn(hg, __dadd_rn(r1, r2)), Rc[0][c]);
         }
-        double dr1[3][3], e1 = 0.0;
-        if (!kp.contraction) {
-            nasa_pot(R, kp.box, kp.boxi, dr1, &e1, kp.c5z, kp.nasa_f5z, FSUM);
-        } else {
+        if (pes) {
+            double dr1[3][3], e1 = 0.0;
+            if (!kp.contraction) {
+                nasa_pot(R, kp.box, kp.boxi, dr1, &e1, kp.c5z, kp.nasa_f5z, FSUM);
+            } else {
 #pragma unroll
-            for (int k = 0; k < 3; k++)
+                for (int k = 0; k < 3; k++)
 #pragma unroll
-                for (int c = 0; c < 3; c++) dr1[k][c] = 0.0;
-        }
-        av[ACC_UMON] = e1;
-        double q3[3], dq3[3][3][3];
-        nasa_dms(R, kp.box, kp.boxi, kp.dms1, kp.dms2, kp.dms3, q3, dq3, FSUM);
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            q3[k] *= CHARGECON;
-            kp.chg[(size_t)b * kp.natoms + 3 * w + k] = q3[k];
-        }
-        if (!kp.contraction) {
-            double roh1[3], roh2[3], rc1[3], rc2[3];
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                roh1[c] = min_image_rn(__dsub_rn(R[1][c], R[0][c]), kp.box[c], kp.boxi[c]);
-                roh2[c] = min_image_rn(__dsub_rn(R[2][c], R[0][c]), kp.box[c], kp.boxi[c]);
-                rc1[c] = min_image_rn(__dsub_rn(Rc[1][c], Rc[0][c]), kp.box[c], kp.boxi[c]);
-                rc2[c] = min_image_rn(__dsub_rn(Rc[2][c], Rc[0][c]), kp.box[c], kp.boxi[c]);
+                    for (int c = 0; c < 3; c++) dr1[k][c] = 0.0;
             }
-#pragma unroll
-            for (int col = 0; col < 3; col++)
-#pragma unroll
-                for (int c = 0; c < 3; c++) av[ACC_VIRT + c + 3 * col] += roh1[c] * dr1[1][col] + roh2[c] * dr1[2][col];
-            av[ACC_VIRIALC] += (rc1[0] * dr1[1][0] + rc1[1] * dr1[1][1] + rc1[2] * dr1[1][2]) +
-                               (rc2[0] * dr1[2][0] + rc2[1] * dr1[2][1] + rc2[2] * dr1[2][2]);
-        }
-        const double tmp = 0.5 * kp.gammaM / (1.0 - kp.gammaM);
-        double q[4];
-        q[0] = 0.0;
-        q[1] = q3[1] + tmp * (q3[1] + q3[2]);
-        q[2] = q3[2] + tmp * (q3[1] + q3[2]);
-        q[3] = q3[0] / (1.0 - kp.gammaM);
-        double *g = kp.grdq + ((size_t)b * N + w) * 27;
-#pragma unroll
-        for (int a = 0; a < 3; a++)
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                const double s01 = dq3[a][0][c] * CHARGECON + dq3[a][1][c] * CHARGECON;
-                g[9 * a + 0 + c] = dq3[a][0][c] * CHARGECON + tmp * s01;
-                g[9 * a + 3 + c] = dq3[a][1][c] * CHARGECON + tmp * s01;
-                g[9 * a + 6 + c] = dq3[a][2][c] * CHARGECON - 2.0 * tmp * s01;
-            }
-        // self energy and intramolecular exclusions (pot_ttm.f90:232-261)
-        double Ef[4][3], ph[4];
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            ph[k] = (k == 0) ? 0.0 : -kp.ew.aewald * TSP * q[k];
-            Ef[k][0] = Ef[k][1] = Ef[k][2] = 0.0;
-        }
-#pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-            for (int j = i + 1; j < 4; j++) {
-                double Rs[3], Rcs[3];
+            av[ACC_UMON] = e1;
+            if (!kp.contraction) {
+                double roh1[3], roh2[3], rc1[3], rc2[3];
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    Rs[c] = min_image_rn(__dsub_rn(R[i][c], R[j][c]), kp.box[c], kp.boxi[c]);
-                    Rcs[c] = min_image_rn(__dsub_rn(Rc[i][c], Rc[j][c]), kp.box[c], kp.boxi[c]);
+                    roh1[c] = min_image_rn(__dsub_rn(R[1][c], R[0][c]), kp.box[c], kp.boxi[c]);
+                    roh2[c] = min_image_rn(__dsub_rn(R[2][c], R[0][c]), kp.box[c], kp.boxi[c]);
+                    rc1[c] = min_image_rn(__dsub_rn(Rc[1][c], Rc[0][c]), kp.box[c], kp.boxi[c]);
+                    rc2[c] = min_image_rn(__dsub_rn(Rc[2][c], Rc[0][c]), kp.box[c], kp.boxi[c]);
                 }
-                double ts0, ts1;
-                self1(dot3_rn(Rs[0], Rs[1], Rs[2]), kp.ew, &ts0, &ts1);
-                ph[i] += ts0 * q[j];
-                ph[j] += ts0 * q[i];
-                double d[3];
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    Ef[i][c] += ts1 * q[j] * Rs[c];
-                    Ef[j][c] -= ts1 * q[i] * Rs[c];
-                    d[c] = -ts1 * q[i] * q[j] * Rs[c];
-                }
-                av[ACC_VIRIALC] += Rcs[0] * d[0] + Rcs[1] * d[1] + Rcs[2] * d[2];
 #pragma unroll
                 for (int col = 0; col < 3; col++)
 #pragma unroll
-                    for (int c = 0; c < 3; c++) av[ACC_VIRT + c + 3 * col] += d[col] * Rs[c];
+                    for (int c = 0; c < 3; c++) av[ACC_VIRT + c + 3 * col] += roh1[c] * dr1[1][col] + roh2[c] * dr1[2][col];
+                av[ACC_VIRIALC] += (rc1[0] * dr1[1][0] + rc1[1] * dr1[1][1] + rc1[2] * dr1[1][2]) +
+                                   (rc2[0] * dr1[2][0] + rc2[1] * dr1[2][1] + rc2[2] * dr1[2][2]);
             }
-        // TTM2.1-F intramolecular dipole tensors (pot_ttm.f90:344-365), cached per molecule
-        if (MODEL == 2) {
-            int t = 0;
 #pragma unroll
-            for (int i = 0; i < 2; i++)
+            for (int k = 0; k < 4; k++) {
+                const size_t s = (size_t)b * S + k * N + w;
 #pragma unroll
-                for (int j = i + 1; j < 3; j++, t++) {
-                    double Rs[3];
-#pragma unroll
-                    for (int c = 0; c < 3; c++) Rs[c] = min_image_rn(__dsub_rn(R[i][c], R[j][c]), kp.box[c], kp.boxi[c]);
-                    double t1, t2;
-                    smear2<double>(dot3_rn(Rs[0], Rs[1], Rs[2]), kp.pt.apol_dd[i + 1][j + 1], kp.ew, &t1, &t2);
-                    double *T = kp.Tself + (((size_t)b * N + w) * 3 + t) * 6;
-                    T[0] = 3.0 * t2 * Rs[0] * Rs[0] - t1;
-                    T[1] = 3.0 * t2 * Rs[1] * Rs[1] - t1;
-                    T[2] = 3.0 * t2 * Rs[2] * Rs[2] - t1;
-                    T[3] = 3.0 * t2 * Rs[0] * Rs[1];
-                    T[4] = 3.0 * t2 * Rs[0] * Rs[2];
-                    T[5] = 3.0 * t2 * Rs[1] * Rs[2];
+                for (int c = 0; c < 3; c++) {
+                    kp.dR[3 * s + c] = (k < 3) ? dr1[k][c] : 0.0;
+                    kp.dip[3 * s + c] = 0.0;
+                    kp.Efdr[3 * s + c] = 0.0;
                 }
-        }
+            }
+        } else {
+            double q3[3], dq3[3][3][3];
+            nasa_dms(R, kp.box, kp.boxi, kp.dms1, kp.dms2, kp.dms3, q3, dq3, FSUM);
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const size_t s = (size_t)b * S + k * N + w;
-            kp.pos[s] = make_double4_32a(R[k][0], R[k][1], R[k][2], q[k]);
-            if (first_bead) kp.posc[(size_t)rep * S + k * N + w] = make_double4_32a(Rc[k][0], Rc[k][1], Rc[k][2], 0.0);
-            kp.F[s] = make_double4_32a(Ef[k][0], Ef[k][1], Ef[k][2], ph[k]);
+            for (int k = 0; k < 3; k++) {
+                q3[k] *= CHARGECON;
+                kp.chg[(size_t)b * kp.natoms + 3 * w + k] = q3[k];
+            }
+            const double tmp = 0.5 * kp.gammaM / (1.0 - kp.gammaM);
+            double q[4];
+            q[0] = 0.0;
+            q[1] = q3[1] + tmp * (q3[1] + q3[2]);
+            q[2] = q3[2] + tmp * (q3[1] + q3[2]);
+            q[3] = q3[0] / (1.0 - kp.gammaM);
+            double *g = kp.grdq + ((size_t)b * N + w) * 27;
 #pragma unroll
-            for (int c = 0; c < 3; c++) {
-                kp.dR[3 * s + c] = (k < 3) ? dr1[k][c] : 0.0;
-                kp.dip[3 * s + c] = 0.0;
-                kp.Efdr[3 * s + c] = 0.0;
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const double s01 = dq3[a][0][c] * CHARGECON + dq3[a][1][c] * CHARGECON;
+                    g[9 * a + 0 + c] = dq3[a][0][c] * CHARGECON + tmp * s01;
+                    g[9 * a + 3 + c] = dq3[a][1][c] * CHARGECON + tmp * s01;
+                    g[9 * a + 6 + c] = dq3[a][2][c] * CHARGECON - 2.0 * tmp * s01;
+                }
+            // self energy and intramolecular exclusions (pot_ttm.f90:232-261)
+            double Ef[4][3], ph[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                ph[k] = (k == 0) ? 0.0 : -kp.ew.aewald * TSP * q[k];
+                Ef[k][0] = Ef[k][1] = Ef[k][2] = 0.0;
+            }
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = i + 1; j < 4; j++) {
+                    double Rs[3], Rcs[3];
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        Rs[c] = min_image_rn(__dsub_rn(R[i][c], R[j][c]), kp.box[c], kp.boxi[c]);
+                        Rcs[c] = min_image_rn(__dsub_rn(Rc[i][c], Rc[j][c]), kp.box[c], kp.boxi[c]);
+                    }
+                    double ts0, ts1;
+                    self1(dot3_rn(Rs[0], Rs[1], Rs[2]), kp.ew, &ts0, &ts1);
+                    ph[i] += ts0 * q[j];
+                    ph[j] += ts0 * q[i];
+                    double d[3];
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {
+                        Ef[i][c] += ts1 * q[j] * Rs[c];
+                        Ef[j][c] -= ts1 * q[i] * Rs[c];
+                        d[c] = -ts1 * q[i] * q[j] * Rs[c];
+                    }
+                    av[ACC_VIRIALC] += Rcs[0] * d[0] + Rcs[1] * d[1] + Rcs[2] * d[2];
+#pragma unroll
+                    for (int col = 0; col < 3; col++)
+#pragma unroll
+                        for (int c = 0; c < 3; c++) av[ACC_VIRT + c + 3 * col] += d[col] * Rs[c];
+                }
+            // TTM2.1-F intramolecular dipole tensors (pot_ttm.f90:344-365), cached per molecule
+            if (MODEL == 2) {
+                int t = 0;
+#pragma unroll
+                for (int i = 0; i < 2; i++)
+#pragma unroll
+                    for (int j = i + 1; j < 3; j++, t++) {
+                        double Rs[3];
+#pragma unroll
+                        for (int c = 0; c < 3; c++) Rs[c] = min_image_rn(__dsub_rn(R[i][c], R[j][c]), kp.box[c], kp.boxi[c]);
+                        double t1, t2;
+                        smear2<double>(dot3_rn(Rs[0], Rs[1], Rs[2]), kp.pt.apol_dd[i + 1][j + 1], kp.ew, &t1, &t2);
+                        double *T = kp.Tself + (((size_t)b * N + w) * 3 + t) * 6;
+                        T[0] = 3.0 * t2 * Rs[0] * Rs[0] - t1;
+                        T[1] = 3.0 * t2 * Rs[1] * Rs[1] - t1;
+                        T[2] = 3.0 * t2 * Rs[2] * Rs[2] - t1;
+                        T[3] = 3.0 * t2 * Rs[0] * Rs[1];
+                        T[4] = 3.0 * t2 * Rs[0] * Rs[2];
+                        T[5] = 3.0 * t2 * Rs[1] * Rs[2];
+                    }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const size_t s = (size_t)b * S + k * N + w;
+                kp.pos[s] = make_double4_32a(R[k][0], R[k][1], R[k][2], q[k]);
+                if (first_bead) kp.posc[(size_t)rep * S + k * N + w] = make_double4_32a(Rc[k][0], Rc[k][1], Rc[k][2], 0.0);
+                kp.F[s] = make_double4_32a(Ef[k][0], Ef[k][1], Ef[k][2], ph[k]);
             }
         }
     }
@@ -784,7 +795,7 @@ static int pair_blocks(const Engine &E) {
 }
 
 void launch_sites(Engine &E) {
-    dim3 g((E.kp.N + SITES_NT - 1) / SITES_NT, E.kp.P);
+    dim3 g((2 * E.kp.N + SITES_NT - 1) / SITES_NT, E.kp.P);
     const bool f = E.precision == PIMD_PREC_MIXED;
     if (E.kp.model == 2) {
         if (f)
