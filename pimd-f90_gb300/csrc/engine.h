@@ -266,7 +266,8 @@ struct Engine {
 // (nm.cu); a context with several replicas launches them once per replica.
 struct NMArgs {
     int P, natoms;
-    const double *C;    // C(P,P) column-major: C[j + P*k] = C(j+1, k+1)
+    const double *C;    // C(P,P) column-major: C[j + P*k] = C(j+1, k+1); then the same as FP32
+                        // pairs (hi, lo) with hi + lo = C to 2^-48 (float2[P*P], fast transforms)
     const double *A;    // [A11, A12, A21, A22, msf, c1, c2] x P
     double massO, massH;
     double delt, delt2, box0, boxi0;
@@ -283,6 +284,7 @@ __global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk)
 __global__ void k_md_sum(int P, const double *Upott, const double *virialt, const double *virialct, const double *uk,
                          double *out4);
 void nm_launch_shape(int P, int natoms, int *threads, int *blocks, size_t *smem);
+void nm_pair_copy(const std::vector<double> &C, std::vector<double> &out);  // C then its FP32 pairs
 void nm_init_host(int P, double omegan, double delta, double setNMfreq, std::vector<double> &A11,
                   std::vector<double> &A12, std::vector<double> &A21, std::vector<double> &A22,
                   std::vector<double> &om, std::vector<double> &msf, std::vector<double> &C);

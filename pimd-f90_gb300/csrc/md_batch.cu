@@ -263,8 +263,10 @@ int pimd_batch_create(pimd_batch **out, const pimd_params *common, const pimd_re
             A[5 * r.P + j] = c1;
             A[6 * r.P + j] = std::sqrt(KB_AMU * r.P * r.temp) * std::sqrt(1 - c1 * c1);
         }
-        if ((rc = balloc(bt, &r.d_C, C.size())) || (rc = balloc(bt, &r.d_A, A.size()))) break;
-        cudaMemcpy(r.d_C, C.data(), sizeof(double) * C.size(), cudaMemcpyHostToDevice);
+        std::vector<double> CP;
+        nm_pair_copy(C, CP);  // C, then its FP32 pairs for the mixed engine's transforms
+        if ((rc = balloc(bt, &r.d_C, CP.size())) || (rc = balloc(bt, &r.d_A, A.size()))) break;
+        cudaMemcpy(r.d_C, CP.data(), sizeof(double) * CP.size(), cudaMemcpyHostToDevice);
         cudaMemcpy(r.d_A, A.data(), sizeof(double) * A.size(), cudaMemcpyHostToDevice);
     }
     if (!rc) rc = bcuda(bt, cudaDeviceSynchronize(), "batch set-up");

@@ -69,9 +69,51 @@ PIMD_D double nm_row(const double *Cs, const double *v, int P, int j, int c, boo
     return s;
 }
 
+// The fast (mixed-engine) transforms in FP32 pairs on the FP32 pipe: x = hi + lo (hi = fp32(x),
+// lo = fp32(x - hi), 48 bits), and each output a compensated dot product (TwoProduct by FMA,
+// TwoSum; Ogita-Rump-Oishi Dot2) over the pairs of C and of the group's vector, then one
+// FP64 sum: about twice-FP32 accuracy (~1e-14 relative for the orthogonal C) for a few FP64
+// operations per element instead of P fused multiply-adds. Intrinsics keep every rounding.
+PIMD_D float2 to_pair(double x) {
+    const float h = __double2float_rn(x);
+    return make_float2(h, __double2float_rn(x - (double)h));
+}
+PIMD_D double nm_row_pair(const float2 *Cf, const float2 *vf, int P, int j, int c, bool fwd) {
+    float s = 0.f, comp = 0.f;
+    for (int k = 0; k < P; k++) {
+        const float2 ck = fwd ? Cf[j + P * k] : Cf[k + P * j];
+        const float2 vk = vf[3 * k + c];
+        const float ph = __fmul_rn(ck.x, vk.x);
+        float pe = __fmaf_rn(ck.x, vk.x, -ph);
+        pe = __fmaf_rn(ck.x, vk.y, __fmaf_rn(ck.y, vk.x, pe));
+        const float t = __fadd_rn(s, ph);
+        const float z = __fsub_rn(t, s);
+        comp = __fadd_rn(comp, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(ph, z)), pe));
+        s = t;
+    }
+    return (double)s + (double)comp;
+}
+
 // Langevin_NM on one atom's momenta held in shared memory p[3P] (group-local).
 PIMD_D void langevin_atom(const NMArgs &a, const double *Cs, double *p, double *tr, int atom, int j, int c,
-                          bool active) {
+                          bool active, const float2 *Cf = nullptr, float2 *vf = nullptr) {
+    if (a.fast) {  // the same steps on FP32 pairs (vf: the group's vector as pairs)
+        if (active) vf[3 * j + c] = to_pair(p[3 * j + c]);
+        __syncthreads();
+        double t = 0.0;
+        if (active) t = nm_row_pair(Cf, vf, a.P, j, c, true);
+        __syncthreads();
+        if (active) {
+            const double m = (atom % 3 == 0) ? a.massO : a.massH;
+            const double sqrtmass = sqrt(m * a.A[4 * a.P + j]);
+            const double c1 = a.A[5 * a.P + j], c2 = a.A[6 * a.P + j];
+            vf[3 * j + c] = to_pair(c1 * t + c2 * (sqrtmass * noise(a, atom, j, c)));
+        }
+        __syncthreads();
+        if (active) p[3 * j + c] = nm_row_pair(Cf, vf, a.P, j, c, false);
+        __syncthreads();
+        return;
+    }
     if (active) tr[3 * j + c] = nm_row(Cs, p, a.P, j, c, true, a.fast);
     __syncthreads();
     if (active) {
@@ -94,7 +136,14 @@ __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt,
     const int atom = blockIdx.x * G + g;
     double *Cs = sh;
     double *x = Cs + P * P + g * 9 * P, *p = x + 3 * P, *tr = p + 3 * P;
-    for (int i = threadIdx.x; i < P * P; i += blockDim.x) Cs[i] = a.C[i];
+    // fast transforms: C as FP32 pairs after the FP64 layout, and two pair vectors per group
+    float2 *Cf = reinterpret_cast<float2 *>(sh + P * P + G * 9 * P), *vf = Cf + P * P + g * 6 * P;
+    for (int i = threadIdx.x; i < P * P; i += blockDim.x) {
+        if (a.fast)
+            Cf[i] = reinterpret_cast<const float2 *>(a.C + P * P)[i];
+        else
+            Cs[i] = a.C[i];
+    }
     const bool active = g < G && atom < a.natoms;
     const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
     if (active) {
@@ -102,11 +151,36 @@ __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt,
         p[3 * j + c] = PPt[gi];
     }
     __syncthreads();
-    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active);
+    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active, Cf, vf);
     if (active) p[3 * j + c] = __dsub_rn(p[3 * j + c], __dmul_rn(__dmul_rn(MASSCON, dRRt[gi]), a.delt2));
     __syncthreads();
     const double m = (atom % 3 == 0) ? a.massO : a.massH;
-    if (a.evolve) {
+    if (a.evolve && a.fast) {  // EvolveRing on FP32 pairs: vf holds x, vf + 3P holds p
+        float2 *vx = vf, *vp = vf + 3 * P;
+        if (active) {
+            vx[3 * j + c] = to_pair(x[3 * j + c]);
+            vp[3 * j + c] = to_pair(p[3 * j + c]);
+        }
+        __syncthreads();
+        double xt = 0, pt = 0;
+        if (active) {
+            xt = nm_row_pair(Cf, vx, P, j, c, true);
+            pt = nm_row_pair(Cf, vp, P, j, c, true);
+        }
+        __syncthreads();
+        if (active) {
+            const double A11 = a.A[j], A12 = a.A[P + j], A21 = a.A[2 * P + j], A22 = a.A[3 * P + j], msf = a.A[4 * P + j];
+            vx[3 * j + c] = to_pair(A11 * xt + (A12 * pt) / (m * msf));
+            vp[3 * j + c] = to_pair(A21 * m * msf * xt + A22 * pt);
+        }
+        __syncthreads();
+        if (active) {
+            const double xr = nm_row_pair(Cf, vx, P, j, c, false), pr = nm_row_pair(Cf, vp, P, j, c, false);
+            x[3 * j + c] = xr;
+            p[3 * j + c] = pr;
+        }
+        __syncthreads();
+    } else if (a.evolve) {
         double xt = 0, pt = 0;
         if (active) {
             xt = nm_row(Cs, x, P, j, c, true, a.fast);
@@ -159,12 +233,18 @@ __global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk)
     const int atom = blockIdx.x * G + g;
     double *Cs = sh;
     double *p = Cs + P * P + g * 9 * P, *tr = p + 3 * P;
-    for (int i = threadIdx.x; i < P * P; i += blockDim.x) Cs[i] = a.C[i];
+    float2 *Cf = reinterpret_cast<float2 *>(sh + P * P + G * 9 * P), *vf = Cf + P * P + g * 6 * P;
+    for (int i = threadIdx.x; i < P * P; i += blockDim.x) {
+        if (a.fast)
+            Cf[i] = reinterpret_cast<const float2 *>(a.C + P * P)[i];
+        else
+            Cs[i] = a.C[i];
+    }
     const bool active = g < G && atom < a.natoms;
     const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
     if (active) p[3 * j + c] = __dsub_rn(PPt[gi], __dmul_rn(__dmul_rn(MASSCON, dRRt[gi]), a.delt2));
     __syncthreads();
-    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active);
+    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active, Cf, vf);
     double ke = 0.0;
     if (active) {
         PPt[gi] = p[3 * j + c];
@@ -247,7 +327,19 @@ void nm_launch_shape(int P, int natoms, int *threads, int *blocks, size_t *smem)
     if (G < 1) G = 1;
     *threads = ((G * 3 * P + 31) / 32) * 32;  // whole warps (the KE reduction shuffles)
     *blocks = (natoms + G - 1) / G;
-    *smem = sizeof(double) * ((size_t)P * P + (size_t)G * 9 * P);
+    // FP64 C and vectors, then C and two vectors per group as FP32 pairs (fast transforms)
+    *smem = sizeof(double) * ((size_t)P * P + (size_t)G * 9 * P) + sizeof(float2) * ((size_t)P * P + (size_t)G * 6 * P);
+}
+
+void nm_pair_copy(const std::vector<double> &C, std::vector<double> &out) {
+    out = C;
+    out.resize(2 * C.size());
+    float *f = reinterpret_cast<float *>(out.data() + C.size());
+    for (size_t i = 0; i < C.size(); i++) {
+        const float h = (float)C[i];
+        f[2 * i] = h;
+        f[2 * i + 1] = (float)(C[i] - (double)h);
+    }
 }
 
 static NMArgs nm_args(Engine &E, double massO, double massH) {
@@ -336,7 +428,7 @@ int pimd_nm_init(pimd_ctx *ctx, int P, double omegan, double delta, double setNM
     if (E.nm_P != P) {
         if (E.d_nmC) cudaFree(E.d_nmC);
         if (E.d_nmA) cudaFree(E.d_nmA);
-        if (cudaMalloc((void **)&E.d_nmC, sizeof(double) * P * P) != cudaSuccess ||
+        if (cudaMalloc((void **)&E.d_nmC, sizeof(double) * 2 * P * P) != cudaSuccess ||
             cudaMalloc((void **)&E.d_nmA, sizeof(double) * 7 * P) != cudaSuccess)
             return PIMD_ERR_NOMEM;
         E.nm_P = P;
@@ -353,7 +445,9 @@ int pimd_nm_init(pimd_ctx *ctx, int P, double omegan, double delta, double setNM
     }
     E.h_nm = A;
     E.h_nm.insert(E.h_nm.end(), om.begin(), om.end());
-    cudaMemcpy(E.d_nmC, CC.data(), sizeof(double) * P * P, cudaMemcpyHostToDevice);
+    std::vector<double> CP;
+    nm_pair_copy(CC, CP);
+    cudaMemcpy(E.d_nmC, CP.data(), sizeof(double) * CP.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(E.d_nmA, A.data(), sizeof(double) * 7 * P, cudaMemcpyHostToDevice);
     auto out = [&](double *dst, const std::vector<double> &v) {
         if (dst) std::memcpy(dst, v.data(), sizeof(double) * v.size());
