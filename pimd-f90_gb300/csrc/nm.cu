@@ -252,7 +252,15 @@ __global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk)
         ke = (1.0 / m) * p[3 * j + c] * p[3 * j + c];
     }
     for (int o = 16; o > 0; o >>= 1) ke += __shfl_xor_sync(0xffffffffu, ke, o);
-    if ((threadIdx.x & 31) == 0 && uk) atomicAdd(uk, 0.5 * ke);
+    // the block's warps in order, then one atomic per block (not per warp: one address)
+    __shared__ double wke[32];
+    if ((threadIdx.x & 31) == 0) wke[threadIdx.x >> 5] = ke;
+    __syncthreads();
+    if (threadIdx.x == 0 && uk) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += wke[w];
+        atomicAdd(uk, 0.5 * t);
+    }
 }
 
 // EvolveRing alone for every atom (no kick, no thermostat)
