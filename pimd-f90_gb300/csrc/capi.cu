@@ -919,7 +919,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         std::vector<int> cand;
     };
     int sf_tiled = E.sf_tiled, ff_regs = E.ff_regs, nbr_block = E.nbr_block, wave = E.wave_shapes;
-    int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc, ff_tc = E.ff_tc, dd_overlap = E.dd_overlap, xcache = E.tc_xcache;
+    int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc, ff_tc = E.ff_tc, dd_overlap = E.dd_overlap, xcache = E.tc_xcache, pdl = E.tc_pdl;
     std::vector<Knob> knobs;
     const bool mixed = E.precision == PIMD_MIXED && E.kp.model < 4;
     if (mixed) {
@@ -930,6 +930,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         knobs.push_back({&ff_regs, {1, 0}});
         if (E.aux_stream) knobs.push_back({&dd_overlap, {1, 0}});
         if (E.d_tcx) knobs.push_back({&xcache, {1, 0}});
+        if (E.tf_ready) knobs.push_back({&pdl, {1, 0}});
     }
     knobs.push_back({&wave, {1, 0}});
     knobs.push_back({&E.max_slices, {16, 8, 4, 2}});
@@ -945,6 +946,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         E.ff_tc = ff_tc != 0;
         E.dd_overlap = dd_overlap != 0;
         E.tc_xcache = xcache != 0;
+        E.tc_pdl = pdl != 0;
     };
     int rc = PIMD_OK;
     float best;
@@ -989,7 +991,8 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     if (n >= 8) k[7] = E.ff_tc && E.tf_ready;
     if (n >= 9) k[8] = E.dd_overlap && E.aux_stream != nullptr && E.precision == PIMD_MIXED;
     if (n >= 10) k[9] = E.tc_xcache && E.d_tcx != nullptr && E.sf_tc && E.tc_ready;
-    if (n >= 11) k[10] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
+    if (n >= 11) k[10] = E.tc_pdl && E.ff_tc && E.tf_ready && E.sf_tc && E.tc_ready;
+    if (n >= 12) k[11] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
     return PIMD_OK;
 }
 
@@ -1007,6 +1010,7 @@ int pimd_set_tuning(pimd_ctx *ctx, const int *k, int n) {
     if (n >= 8) E.ff_tc = k[7] != 0;
     if (n >= 9) E.dd_overlap = k[8] != 0;
     if (n >= 10) E.tc_xcache = k[9] != 0;
+    if (n >= 11) E.tc_pdl = k[10] != 0;
     E.gkey.clear();  // a captured MD-step graph holds the old launches: capture again
     return PIMD_OK;
 }

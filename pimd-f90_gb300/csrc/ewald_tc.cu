@@ -154,6 +154,11 @@ PIMD_D void bulk_load_stream(void *dst, const void *src, uint32_t bytes, uint64_
                  "l"((unsigned long long)src), "r"(bytes), "r"(umma::smem_u32(bar)), "l"(pol)
                  : "memory");
 }
+// programmatic dependent launch: the next kernel of the stream may start (its CTAs wait with
+// pdl_wait before they read what this grid writes); pdl_wait returns once the previous grid
+// has completed and its writes are visible (a no-op without the launch attribute)
+PIMD_D void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+PIMD_D void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 PIMD_D void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(umma::smem_u32(bar)), "r"(bytes) : "memory");
 }
@@ -279,6 +284,8 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
+    // the iteration's field pass may start its set-up (tables, Q) on the SMs this grid leaves free
+    pdl_launch_dependents();
     const uint32_t tm = tslot;
     uint32_t err = 0;
 
@@ -625,6 +632,7 @@ struct TfArgs {
     const float *kzv;     // k_z by kz + lmax
     int nr, nph, ncol, kq, jm;  // runs, runs per pass (rounded up to 8), V rows (8 nph), K terms (x16), kz rows
     int sbase, s_lo, s_hi;
+    int pdl;  // launched as a programmatic dependent of the structure factor (pdl_wait before W)
 };
 
 struct TfSmem {
@@ -672,10 +680,12 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         umma::mbar_init(&wbar, 1);
         umma::mbar_init(&mbar, 1);
         // weight slots: charge (0), dipole (1); TF_DG takes both (adjacent in Wf)
-        const int slot = (MODE == TF_D || MODE == TF_QG) ? 1 : 0;
-        const uint32_t wbytes = (uint32_t)kp.nk * 8u * (DG ? 2u : 1u);
-        mbar_expect_tx(&wbar, wbytes);
-        bulk_load(sm + L.W, kp.Wf + ((size_t)b * 2 + slot) * kp.nk, wbytes, &wbar);
+        if (!a.pdl) {
+            const int slot = (MODE == TF_D || MODE == TF_QG) ? 1 : 0;
+            const uint32_t wbytes = (uint32_t)kp.nk * 8u * (DG ? 2u : 1u);
+            mbar_expect_tx(&wbar, wbytes);
+            bulk_load(sm + L.W, kp.Wf + ((size_t)b * 2 + slot) * kp.nk, wbytes, &wbar);
+        }
         const uint32_t box_tx = (uint32_t)(kp.ntab * 128);
         mbar_expect_tx(&tbar, 8 * box_tx);
         for (int i = 0; i < 8; i++) tma_load_2d(sm + i * L.boxb, &tmap, 2 * (sb + 16 * i), b * kp.ntab, &tbar);
@@ -708,18 +718,47 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     float kz0[4], kz1[4];
     fetch_km(0, nph, tid, km0, kz0);
     fetch_km(DG ? 0 : nph, nph, tid, km1, kz1);
-    // the SOR inputs of the CTA's dipole sites, fetched now
-    const int s_own = sb + tid;
-    const bool own = tid < TF_SITES && s_own >= a.s_lo && s_own < a.s_hi;
-    DdSite din;
-    if (MODE == TF_D && own) dd_sor_load(kp, b, s_own, din);
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
     const uint32_t tm = tslot;
     unsigned char *Vh = sm + L.B, *Vl = Vh + a.ncol * a.kq * 2;
     unsigned char *Qh = sm + L.A, *Ql = Qh + TF_SITES * a.kq * 2;
-    uint32_t err = (uint32_t)umma::mbar_wait(&wbar, 0, TC_WAIT);
+    // Q = ez rows of the CTA's sites, 8 halves (4 j: c_j, s_j) per item, zero for j >= jm
+    uint32_t err = (uint32_t)umma::mbar_wait(&tbar, 0, TC_WAIT);
+    for (int it = tid; it < TF_SITES * kcm; it += TF_NT) {
+        const int s = it % TF_SITES, jc = it / TF_SITES;
+        float v[8];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int j = 4 * jc + e;
+            const float2 z = j < jm ? tab_elem(sm, L.boxb, zrow + j, s) : make_float2(0.f, 0.f);
+            v[2 * e] = z.x;
+            v[2 * e + 1] = z.y;
+        }
+        uint4 hi, lo;
+        split8_h(v, hi, lo);
+        const int o = rowchunk_k(s, jc, kcm);
+        *reinterpret_cast<uint4 *>(Qh + o) = hi;
+        *reinterpret_cast<uint4 *>(Ql + o) = lo;
+    }
+    // everything above reads only the positions; from here on the structure factor's weights
+    // and the iteration's dipoles and fields (a programmatic launch waits for them here)
+    if (a.pdl) {
+        pdl_wait();
+        if (tid == 0) {
+            const int slot = (MODE == TF_D || MODE == TF_QG) ? 1 : 0;
+            const uint32_t wbytes = (uint32_t)kp.nk * 8u * (DG ? 2u : 1u);
+            mbar_expect_tx(&wbar, wbytes);
+            bulk_load(sm + L.W, kp.Wf + ((size_t)b * 2 + slot) * kp.nk, wbytes, &wbar);
+        }
+    }
+    // the SOR inputs of the CTA's dipole sites
+    const int s_own = sb + tid;
+    const bool own = tid < TF_SITES && s_own >= a.s_lo && s_own < a.s_hi;
+    DdSite din;
+    if (MODE == TF_D && own) dd_sor_load(kp, b, s_own, din);
+    err |= (uint32_t)umma::mbar_wait(&wbar, 0, TC_WAIT);
     const float2 *W = reinterpret_cast<const float2 *>(sm + L.W);
     // V of runs [p0, p0 + nrow): run p0 + pl, component c at row vrow0 + c nrow + pl; 8 halves
     // (4 j) per item, zero for runs >= nr and j >= jm
@@ -779,24 +818,6 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     if (!DG) {  // both passes: pass q's rows from q 4 nph
         build_v(0, nph, 0, km0, kz0);
         build_v(nph, nph, 4 * nph, km1, kz1);
-    }
-    // Q = ez rows of the CTA's sites, 8 halves (4 j: c_j, s_j) per item, zero for j >= jm
-    err |= (uint32_t)umma::mbar_wait(&tbar, 0, TC_WAIT);
-    for (int it = tid; it < TF_SITES * kcm; it += TF_NT) {
-        const int s = it % TF_SITES, jc = it / TF_SITES;
-        float v[8];
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-            const int j = 4 * jc + e;
-            const float2 z = j < jm ? tab_elem(sm, L.boxb, zrow + j, s) : make_float2(0.f, 0.f);
-            v[2 * e] = z.x;
-            v[2 * e + 1] = z.y;
-        }
-        uint4 hi, lo;
-        split8_h(v, hi, lo);
-        const int o = rowchunk_k(s, jc, kcm);
-        *reinterpret_cast<uint4 *>(Qh + o) = hi;
-        *reinterpret_cast<uint4 *>(Ql + o) = lo;
     }
     // passes of nph runs, NC nph <= 512 TMEM columns each: column c nph + pl for component c
     // of the pass's run pl
@@ -1211,6 +1232,29 @@ int launch_field_tc(Engine &E, int mode, int s0, int s1) {
     const TfSmem L(kp.ntab, a.ncol, a.kq, kp.nk, mode == TF_DG ? 2 : 1);
     dim3 g((s1 - a.sbase + TF_SITES - 1) / TF_SITES, kp.P);
     const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(E.tc_map);
+    a.pdl = 0;
+    if (mode == TF_D && E.tc_pdl && E.sf_tc) {
+        // a programmatic dependent of the iteration's structure factor: its set-up (tables,
+        // Q) runs while that grid finishes; it waits (pdl_wait) before reading the weights
+        a.pdl = 1;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = g;
+        cfg.blockDim = dim3(TF_NT);
+        cfg.dynamicSmemBytes = L.total;
+        cfg.stream = E.stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        if (cudaLaunchKernelEx(&cfg, k_field_tc<TF_D>, *map, kp, a) == cudaSuccess) {
+            ++E.nlaunch;
+            return 1;
+        }
+        cudaGetLastError();
+        a.pdl = 0;
+        E.tc_pdl = false;  // not available: plain launches from now on
+    }
     if (mode == TF_D)
         k_field_tc<TF_D><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
     else if (mode == TF_Q)
