@@ -514,7 +514,10 @@ static int capture_dipole_loop(Engine &E, bool mixed) {
     cudaStream_t keep = E.stream;
     E.stream = E.body_stream;
     E.kp.cond = h;
-    dipole_iteration(E, mixed);
+    // iterations per body: 2 halves the conditional's relaunches; an iteration after every bead
+    // has converged is empty (each kernel returns at the bead's flag, the test leaves the
+    // per-bead counts alone)
+    for (int u = 0; u < std::max(1, E.loop_unroll); u++) dipole_iteration(E, mixed);
     E.kp.cond = 0;
     E.stream = keep;
     cudaGraph_t out = nullptr;
@@ -992,7 +995,8 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     if (n >= 9) k[8] = E.dd_overlap && E.aux_stream != nullptr && E.precision == PIMD_MIXED;
     if (n >= 10) k[9] = E.tc_xcache && E.d_tcx != nullptr && E.sf_tc && E.tc_ready;
     if (n >= 11) k[10] = E.tc_pdl && E.ff_tc && E.tf_ready && E.sf_tc && E.tc_ready;
-    if (n >= 12) k[11] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
+    if (n >= 12) k[11] = E.loop_unroll;
+    if (n >= 13) k[12] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
     return PIMD_OK;
 }
 
@@ -1011,6 +1015,10 @@ int pimd_set_tuning(pimd_ctx *ctx, const int *k, int n) {
     if (n >= 9) E.dd_overlap = k[8] != 0;
     if (n >= 10) E.tc_xcache = k[9] != 0;
     if (n >= 11) E.tc_pdl = k[10] != 0;
+    if (n >= 12) {
+        if (k[11] < 1 || k[11] > 4) return PIMD_ERR_ARG;
+        E.loop_unroll = k[11];
+    }
     E.gkey.clear();  // a captured MD-step graph holds the old launches: capture again
     return PIMD_OK;
 }

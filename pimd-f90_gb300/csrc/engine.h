@@ -211,6 +211,7 @@ struct Engine {
     int tc_xsub = 0, tc_xblock = 0;   // 16-site blocks per bead and run group, bytes per block
     bool tc_xcache = true;            // use the X cache in the dipole iterations
     bool tc_pdl = true;               // field pass as a programmatic dependent launch
+    int loop_unroll = 2;              // dipole iterations per body of the graph's conditional loop
     bool ff_tc = true;                // tensor-core dipole field pass (k_field_tc) when tf_ready
     bool tf_ready = false;
     int tf_nr = 0, tf_nph = 0, tf_jm = 0, tf_ncol = 0, tf_kq = 0;
