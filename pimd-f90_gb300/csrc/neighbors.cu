@@ -145,6 +145,9 @@ __global__ void __launch_bounds__(NB_MAXN) k_nbr_block(KP kp) {
     __shared__ int ctot[2];
     float4 *sf = reinterpret_cast<float4 *>(sO + N);
     int *oh = reinterpret_cast<int *>(sf + N), *of = oh + N;
+    // the count pass keeps each row's hit masks (one word per 32 candidates) for the fill pass
+    const int nch = (N + 31) / 32;
+    unsigned *mk = reinterpret_cast<unsigned *>(of + N);
     __shared__ int wsum[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const double4_32a *O = kp.pos + (size_t)b * kp.S;
@@ -170,6 +173,7 @@ __global__ void __launch_bounds__(NB_MAXN) k_nbr_block(KP kp) {
             const unsigned m = __ballot_sync(0xffffffffu, hit), mh = __ballot_sync(0xffffffffu, hit && j > i);
             nf += __popc(m);
             nh += __popc(mh);
+            if (lane == 0) mk[(i - r0) * nch + (j0 >> 5)] = m;
         }
         if (lane == 0) {
             oh[i] = nh;
@@ -213,13 +217,13 @@ __global__ void __launch_bounds__(NB_MAXN) k_nbr_block(KP kp) {
     int2 *ph = kp.pairs + (size_t)b * kp.cap;
     int2 *pf = reinterpret_cast<int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
     for (int i = r0 + w; i < r1; i += nw) {
-        const float4 fi = sf[i];
-        const double4_32a di = sO[i];
         int h = oh[i], f = FULL ? of[i] : 0;
         for (int j0 = FULL ? 0 : ((i + 1) & ~31); j0 < N; j0 += 32) {
             const int j = j0 + lane;
-            const bool hit = j < N && j != i && (FULL || j > i) && oo_test_sm(fi, sf[j], di, sO[j], kp, rc2f, Lf, Lif);
-            const unsigned m = __ballot_sync(0xffffffffu, hit), mh = __ballot_sync(0xffffffffu, hit && j > i);
+            const unsigned m = mk[(i - r0) * nch + (j0 >> 5)];  // the count pass's tests
+            const bool hit = (m >> lane) & 1u;
+            const int d = i - j0;  // lanes above d have j > i
+            const unsigned mh = m & (d < 0 ? 0xffffffffu : (d >= 31 ? 0u : (0xffffffffu << (d + 1))));
             const unsigned below = (1u << lane) - 1u;
             if (hit && j > i) {
                 const int slot = h + __popc(mh & below);
@@ -428,7 +432,7 @@ void launch_neighbors(Engine &E) {
     }
     if (kp.N <= NB_MAXN && E.nbr_block) {
         const int nt = ((kp.N + 31) / 32) * 32 < 256 ? 256 : ((kp.N + 31) / 32) * 32;
-        const size_t smem = (sizeof(double4_32a) + sizeof(float4) + 2 * sizeof(int)) * (size_t)kp.N;
+        size_t smem = (sizeof(double4_32a) + sizeof(float4) + 2 * sizeof(int)) * (size_t)kp.N;
         // a cluster of up to 4 CTAs per bead so that the beads cover the GPU
         static int nsm_cache[64] = {0};
         int &nsm = nsm_cache[E.device & 63];
@@ -437,6 +441,8 @@ void launch_neighbors(Engine &E) {
             if (nsm <= 0) nsm = 152;
         }
         const int ncl = std::max(1, std::min(4, std::min(nsm / std::max(kp.P, 1), kp.N / 32)));
+        // + the hit masks of a CTA's rows (at most 128 KB at N = 1024 in one CTA)
+        smem += sizeof(unsigned) * (size_t)((kp.N + ncl - 1) / ncl + 1) * ((kp.N + 31) / 32);
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(ncl * kp.P);
         cfg.blockDim = dim3(nt);
@@ -469,7 +475,7 @@ void launch_neighbors(Engine &E) {
 namespace pimd {
 void neighbors_init(Engine &E) {
     (void)E;
-    cudaFuncSetAttribute(k_nbr_block<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-    cudaFuncSetAttribute(k_nbr_block<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+    cudaFuncSetAttribute(k_nbr_block<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_nbr_block<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
 }  // namespace pimd
