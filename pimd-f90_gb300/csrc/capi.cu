@@ -207,6 +207,7 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
     KP &kp = E.kp;
     std::memset(&kp, 0, sizeof(kp));
     kp.model = p->pot_model;
+    kp.fx_s0 = (kp.model == 3) ? kp.N : 0;  // the first site of the charge field passes
     kp.natoms = p->natoms;
     kp.N = p->natoms / 3;
     kp.S = (spc ? 3 : 4) * kp.N;  // potential.f90:53-80: no M site in the SPC models
@@ -350,7 +351,7 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
             (rc = dalloc(E, &kp.rhof, P * S)) || (rc = dalloc(E, &kp.fcnt, P * N)) || (rc = dalloc(E, &kp.foff, P * N)) ||
             (rc = dalloc(E, &kp.fnbr, P * (size_t)kp.fcap * 2)) || (rc = dalloc(E, &kp.fntot, P)) ||
             (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd * 6)) || (rc = dalloc(E, &kp.Wf, P * 2 * (size_t)kp.nk)) || (rc = dalloc(E, &kp.dipf, P * S)) ||
-            (rc = dalloc(E, &kp.ofix, P * N)) || (rc = dalloc(E, &kp.orawf, P * N)))
+            (rc = dalloc(E, &kp.ofix, P * N)) || (rc = dalloc(E, &kp.orawf, P * N)) || (rc = dalloc(E, &kp.Fx, P * S)))
             return rc;
     }
     // cell lists for boxes beyond the one-block neighbour kernel (cells of width >= Rc + 1e-3 A)
@@ -461,18 +462,18 @@ void timer_end(Engine &E) {
 // One induced-dipole iteration (pot_ttm.f90:298-390): real-space dipole field, ewald_std_dd
 // structure factor, field + SOR update, convergence test.
 static void dipole_iteration(Engine &E, bool mixed) {
-    if (mixed && E.aux_stream && E.dd_overlap) {
+    if (mixed && E.loop_aux && E.dd_overlap) {
         // the real-space field runs on the second stream beside the structure factor (both only
         // read the iteration's dipoles); the field + SOR pass waits for both
-        cudaEventRecord(E.ev_fork, E.stream);
-        cudaStreamWaitEvent(E.aux_stream, E.ev_fork, 0);
+        cudaEventRecord(E.loop_fork, E.stream);
+        cudaStreamWaitEvent(E.loop_aux, E.loop_fork, 0);
         PHASE("dd_smu", launch_ewald_smu(E));
         cudaStream_t keep = E.stream;
-        E.stream = E.aux_stream;
+        E.stream = E.loop_aux;
         PHASE("dd_real", launch_dd_real_m(E));
         E.stream = keep;
-        cudaEventRecord(E.ev_join, E.aux_stream);
-        cudaStreamWaitEvent(E.stream, E.ev_join, 0);
+        cudaEventRecord(E.loop_join, E.loop_aux);
+        cudaStreamWaitEvent(E.stream, E.loop_join, 0);
         PHASE("dd_update", launch_dd_update(E));  // includes the convergence test (last block)
         return;
     }
@@ -548,18 +549,44 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
         return cuda_check(E, cudaGetLastError(), "force kernels");
     }
     PHASE("sites", launch_sites(E));
+    // mixed engine with the tensor-core field passes: the reciprocal charge passes run on the
+    // second stream beside the neighbour list and the charge pair gather, and the force pass
+    // beside the force pair gather; their field / gradient sums go to the scratch Fx, which
+    // k_after_qq and k_finish add (the pair kernels update F and dR in place)
+    const bool ovl = mixed && E.ewald_overlap && E.aux_stream && kp.Fx && E.tc_ready && E.tf_ready && E.ff_tc;
+    const bool ovq = ovl, ovf = ovl && E.tf_qd_ready;
+    kp.fx_mode = 0;
     if (mixed) {
         PHASE("site_offsets", launch_site_offsets(E));
+        if (ovq) {
+            cudaEventRecord(E.ev_fork, E.stream);
+            cudaStreamWaitEvent(E.aux_stream, E.ev_fork, 0);
+            cudaStream_t keep = E.stream;
+            E.stream = E.aux_stream;
+            kp.fx_mode = 1;
+            PHASE("ewald_tables", launch_ewald_tables(E));
+            PHASE("ewald_sq", launch_ewald_sq(E));
+            PHASE("ewald_fq", launch_ewald_fq(E));
+            kp.fx_mode = 0;
+            E.stream = keep;
+            cudaEventRecord(E.ev_join, E.aux_stream);
+        }
         PHASE("neighbors", launch_neighbors(E));
         PHASE("pair_qq", launch_pair_qq_m(E));
     } else {
         PHASE("neighbors", launch_neighbors(E));
         PHASE("pair_qq", launch_pair_qq(E));
     }
-    PHASE("ewald_tables", launch_ewald_tables(E));
-    PHASE("ewald_sq", launch_ewald_sq(E));
-    PHASE("ewald_fq", launch_ewald_fq(E));
+    if (ovq) {
+        cudaStreamWaitEvent(E.stream, E.ev_join, 0);
+        kp.fx_mode = 1;
+    } else {
+        PHASE("ewald_tables", launch_ewald_tables(E));
+        PHASE("ewald_sq", launch_ewald_sq(E));
+        PHASE("ewald_fq", launch_ewald_fq(E));
+    }
     PHASE("after_qq", launch_after_qq(E));
+    kp.fx_mode = 0;
     if (E.tape_on) tape_record(E, 0);
     if (E.capturing) {
         int rc = capture_dipole_loop(E, mixed);
@@ -579,12 +606,28 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
         }
         E.last_niter_max = std::min(iter, kp.polar_maxiter);
     }
-    if (mixed)
+    if (ovf) {
+        cudaEventRecord(E.ev_fork, E.stream);
+        cudaStreamWaitEvent(E.aux_stream, E.ev_fork, 0);
+        cudaStream_t keep = E.stream;
+        E.stream = E.aux_stream;
+        kp.fx_mode = 2;
+        PHASE("ewald_qd", launch_ewald_qd(E));
+        kp.fx_mode = 0;
+        E.stream = keep;
+        cudaEventRecord(E.ev_join, E.aux_stream);
         PHASE("pair_force", launch_pair_force_m(E));
-    else
-        PHASE("pair_force", launch_pair_force(E));
-    PHASE("ewald_qd", launch_ewald_qd(E));
+        cudaStreamWaitEvent(E.stream, E.ev_join, 0);
+        kp.fx_mode = 2;
+    } else {
+        if (mixed)
+            PHASE("pair_force", launch_pair_force_m(E));
+        else
+            PHASE("pair_force", launch_pair_force(E));
+        PHASE("ewald_qd", launch_ewald_qd(E));
+    }
     PHASE("finish", launch_finish(E));
+    kp.fx_mode = 0;
     PHASE("totals", launch_totals(E, Upott, virialt, virialct, virt9));
     return cuda_check(E, cudaGetLastError(), "force kernels");
 }
@@ -643,6 +686,9 @@ int pimd_destroy(pimd_ctx *ctx) {
     if (E.aux_stream) cudaStreamDestroy(E.aux_stream);
     if (E.ev_fork) cudaEventDestroy(E.ev_fork);
     if (E.ev_join) cudaEventDestroy(E.ev_join);
+    if (E.loop_aux) cudaStreamDestroy(E.loop_aux);
+    if (E.loop_fork) cudaEventDestroy(E.loop_fork);
+    if (E.loop_join) cudaEventDestroy(E.loop_join);
     if (E.own_stream && E.stream) cudaStreamDestroy(E.stream);
     delete ctx;
     return PIMD_OK;
@@ -922,7 +968,8 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         std::vector<int> cand;
     };
     int sf_tiled = E.sf_tiled, ff_regs = E.ff_regs, nbr_block = E.nbr_block, wave = E.wave_shapes;
-    int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc, ff_tc = E.ff_tc, dd_overlap = E.dd_overlap, xcache = E.tc_xcache, pdl = E.tc_pdl;
+    int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc, ff_tc = E.ff_tc, dd_overlap = E.dd_overlap, xcache = E.tc_xcache, pdl = E.tc_pdl,
+        ewo = E.ewald_overlap;
     std::vector<Knob> knobs;
     const bool mixed = E.precision == PIMD_MIXED && E.kp.model < 4;
     if (mixed) {
@@ -931,9 +978,10 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         knobs.push_back({&sf_tiled, {1, 0}});
         knobs.push_back({&E.sf_groups, {0, 4, 8, 16, 32}});
         knobs.push_back({&ff_regs, {1, 0}});
-        if (E.aux_stream) knobs.push_back({&dd_overlap, {1, 0}});
+        if (E.loop_aux) knobs.push_back({&dd_overlap, {1, 0}});
         if (E.d_tcx) knobs.push_back({&xcache, {1, 0}});
         if (E.tf_ready) knobs.push_back({&pdl, {1, 0}});
+        if (E.kp.Fx) knobs.push_back({&ewo, {1, 0}});
     }
     knobs.push_back({&wave, {1, 0}});
     knobs.push_back({&E.max_slices, {16, 8, 4, 2}});
@@ -950,6 +998,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         E.dd_overlap = dd_overlap != 0;
         E.tc_xcache = xcache != 0;
         E.tc_pdl = pdl != 0;
+        E.ewald_overlap = ewo != 0;
     };
     int rc = PIMD_OK;
     float best;
@@ -992,11 +1041,12 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     if (n >= 6) k[5] = E.wave_shapes;
     if (n >= 7) k[6] = E.sf_tc && E.tc_ready;
     if (n >= 8) k[7] = E.ff_tc && E.tf_ready;
-    if (n >= 9) k[8] = E.dd_overlap && E.aux_stream != nullptr && E.precision == PIMD_MIXED;
+    if (n >= 9) k[8] = E.dd_overlap && E.loop_aux != nullptr && E.precision == PIMD_MIXED;
     if (n >= 10) k[9] = E.tc_xcache && E.d_tcx != nullptr && E.sf_tc && E.tc_ready;
     if (n >= 11) k[10] = E.tc_pdl && E.ff_tc && E.tf_ready && E.sf_tc && E.tc_ready;
     if (n >= 12) k[11] = E.loop_unroll;
-    if (n >= 13) k[12] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
+    if (n >= 13) k[12] = E.ewald_overlap && E.aux_stream != nullptr && E.kp.Fx != nullptr;
+    if (n >= 14) k[13] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
     return PIMD_OK;
 }
 
@@ -1019,6 +1069,7 @@ int pimd_set_tuning(pimd_ctx *ctx, const int *k, int n) {
         if (k[11] < 1 || k[11] > 4) return PIMD_ERR_ARG;
         E.loop_unroll = k[11];
     }
+    if (n >= 13) E.ewald_overlap = k[12] != 0;
     E.gkey.clear();  // a captured MD-step graph holds the old launches: capture again
     return PIMD_OK;
 }

@@ -110,6 +110,11 @@ struct KP {
     uint4 *ofix;           // [P][N] O sites as 32-bit fractions of the box edges: the wrapping
                            // unsigned difference of two of them is the minimum image
     float4 *orawf;         // [P][N] O sites (unwrapped) in FP32: force-phase centroid-virial lever
+    double4_32a *Fx;       // [P][S] reciprocal charge field / force-pass sums when those passes run
+                           // beside the pair kernels (mixed engine): (x, y, z, potential)
+    int fx_mode;           // bit 0: the charge field is in Fx (k_after_qq adds it to F); bit 1: the
+                           // force pass is in Fx (k_finish adds it to dR and the potentials)
+    int fx_s0;             // first site the tensor-core passes write (sites below are not in Fx)
     float4 *gq23;          // [GQ_N] cubic pieces of h(u) = Gamma(2/3) Q(2/3, u^3) exp(u^3) (mixed.cu)
     float4 *dipf;          // [P][S] FP32 copy of the induced dipoles (written with every update)
     int *fcnt, *foff;      // [P][N] full neighbour list counts / offsets
@@ -212,6 +217,7 @@ struct Engine {
     bool tc_xcache = true;            // use the X cache in the dipole iterations
     bool tc_pdl = true;               // field pass as a programmatic dependent launch
     int loop_unroll = 2;              // dipole iterations per body of the graph's conditional loop
+    bool ewald_overlap = true;        // reciprocal charge / force passes beside the pair gathers
     bool ff_tc = true;                // tensor-core dipole field pass (k_field_tc) when tf_ready
     bool tf_ready = false;
     int tf_nr = 0, tf_nph = 0, tf_jm = 0, tf_ncol = 0, tf_kq = 0;
@@ -243,6 +249,10 @@ struct Engine {
     // beside the structure factor (fork / join events; branches of the graph when captured)
     cudaStream_t aux_stream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // the dipole iterations' own pair (inside a graph they are captured into the conditional
+    // loop's body, a graph of its own, which must not share a stream with the outer capture)
+    cudaStream_t loop_aux = nullptr;
+    cudaEvent_t loop_fork = nullptr, loop_join = nullptr;
     cudaGraphExec_t gexec = nullptr;
     std::vector<const void *> gkey;
     long long graph_launches = 0, graph_captures = 0;

@@ -945,6 +945,29 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
             for (int c = 0; c < 4; c++) e[c] += red[(rq * TF_SITES + tid) * 4 + c];
     }
     if (bad && tid == 0) atomicOr(kp.err, 8u);
+    if (MODE == TF_Q && (kp.fx_mode & 1)) {  // into the scratch (this pass runs beside the pair kernels)
+        if (own && !bad)
+            kp.Fx[(size_t)b * kp.S + s_own] =
+                make_double4_32a((double)e[0], (double)e[1], (double)e[2], s_own >= kp.fq ? (double)e[3] : 0.0);
+        return;
+    }
+    if ((MODE == TF_QG || MODE == TF_DG) && (kp.fx_mode & 2)) {
+        if (own && !bad) {
+            const size_t gs = (size_t)b * kp.S + s_own;
+            if (MODE == TF_QG) {
+                const double q = kp.pos[gs].w;
+                kp.Fx[gs] = make_double4_32a(-q * (double)e[0], -q * (double)e[1], -q * (double)e[2],
+                                             s_own >= kp.fq ? (double)e[3] : 0.0);
+            } else {
+                double4_32a f = kp.Fx[gs];
+                f.x += (double)e[0];
+                f.y += (double)e[1];
+                f.z += (double)e[2];
+                kp.Fx[gs] = f;
+            }
+        }
+        return;
+    }
     if (MODE == TF_Q) {
         // ewald.f90:45-49 as k_field_finish<F_Q>: Efq += E, phi += (charged sites)
         if (own && !bad) {

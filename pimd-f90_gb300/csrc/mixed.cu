@@ -96,6 +96,9 @@ cudaError_t mixed_init(Engine &E) {
     cudaError_t e = cudaStreamCreateWithFlags(&E.aux_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E.loop_aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.loop_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.loop_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void **)&E.kp.gq23, sizeof(tab));
     if (e == cudaSuccess) E.allocs.push_back(E.kp.gq23);
     if (e == cudaSuccess) e = cudaMemcpy(E.kp.gq23, tab, sizeof(tab), cudaMemcpyHostToDevice);

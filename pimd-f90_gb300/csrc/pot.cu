@@ -376,7 +376,15 @@ __global__ void __launch_bounds__(128) k_after_qq(KP kp) {
     double av[3] = {0.0, 0.0, 0.0};
     if (s < kp.S) {
         const size_t gs = (size_t)b * kp.S + s;
-        const double4_32a F = kp.F[gs];
+        double4_32a F = kp.F[gs];
+        if ((kp.fx_mode & 1) && s >= kp.fx_s0) {  // the reciprocal charge field from its scratch
+            const double4_32a x = kp.Fx[gs];
+            F.x += x.x;
+            F.y += x.y;
+            F.z += x.z;
+            F.w += x.w;
+            kp.F[gs] = F;
+        }
         const double q = kp.pos[gs].w;
         if (s >= kp.N) {
             kp.dR[3 * gs + 0] -= q * F.x;
@@ -678,7 +686,22 @@ __global__ void __launch_bounds__(128) k_finish(KP kp) {
         const double4_32a *pos = kp.pos + base;
         const double4_32a *Fb = kp.F + base;
         double *dR = kp.dR + 3 * base;
-        const double phH1 = Fb[N + w].w, phH2 = Fb[2 * N + w].w, phM = Fb[3 * N + w].w;
+        double phH1 = Fb[N + w].w, phH2 = Fb[2 * N + w].w, phM = Fb[3 * N + w].w;
+        if (kp.fx_mode & 2) {  // the force pass's sums from its scratch (sites from fx_s0 on)
+            const double4_32a *X = kp.Fx + base;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int s = k * N + w;
+                if (s < kp.fx_s0) continue;
+                const double4_32a x = X[s];
+                dR[3 * s + 0] += x.x;
+                dR[3 * s + 1] += x.y;
+                dR[3 * s + 2] += x.z;
+                if (k == 1) phH1 += x.w;
+                if (k == 2) phH2 += x.w;
+                if (k == 3) phM += x.w;
+            }
+        }
         const double *g = kp.grdq + ((size_t)b * N + w) * 27;
         double dg[3][3];
 #pragma unroll

@@ -105,16 +105,17 @@ def test_autotune_keeps_results(pkg, engine_lib):
     a = eng.full_bead_forces(c["RRt"], c["RRc"], t=0)
     tuned = eng.autotune()
     assert set(tuned) == {"sf_tiled", "sf_groups", "ff_regs", "max_slices", "nbr_block", "wave_shapes", "sf_tc", "ff_tc",
-                          "dd_overlap", "x_cache", "pdl", "loop_unroll", "qd_tc"}
+                          "dd_overlap", "x_cache", "pdl", "loop_unroll", "ewald_overlap", "qd_tc"}
     assert 1 <= tuned["max_slices"] <= 16
     b = eng.full_bead_forces(c["RRt"], c["RRc"], t=0)
     assert rel(b["dRRt"], a["dRRt"]) < 1e-6
     assert rel(b["Upott"], a["Upott"]) < 1e-6
-    # pinned shapes: the real-space field beside the structure factor or after it is the same
-    # arithmetic in the same order (equal up to the FP64 atomic order of the block sums)
+    # pinned shapes: the passes on a second stream or in line, the field pass as a programmatic
+    # dependent or a plain launch, are the same arithmetic in the same order (equal up to the
+    # FP64 atomic order of the block sums)
     runs = []
     for ov in (0, 1):
-        assert eng.set_tuning(dd_overlap=ov, pdl=ov)["dd_overlap"] == ov
+        assert eng.set_tuning(dd_overlap=ov, pdl=ov, ewald_overlap=ov)["ewald_overlap"] == ov
         runs.append(eng.full_bead_forces(c["RRt"], c["RRc"], t=0))
     assert rel(runs[0]["dRRt"], runs[1]["dRRt"]) < 1e-7
     with pytest.raises(ValueError):
