@@ -226,9 +226,11 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc);
  * the structure factor (its set-up overlaps that grid's end)], when n >= 12 [dipole iterations
  * per body of the CUDA graph's conditional loop, 1-4], when n >= 13 [the reciprocal charge and
  * force passes on a second stream beside the pair kernels (mixed engine)], when n >= 14
- * [tensor-core force pass in use (follows the field-pass knob; reported only)]; n >= 5. */
+ * [real-space dipole tensors formed inside each iteration rather than cached per list entry
+ * (mixed engine)], when n >= 15 [tensor-core force pass in use (follows the field-pass knob;
+ * reported only)]; n >= 5. */
 int pimd_get_tuning(pimd_ctx *ctx, int *knobs, int n);
-/* Sets the shapes in the order pimd_get_tuning reports them (n >= 5; the first n up to 13 are
+/* Sets the shapes in the order pimd_get_tuning reports them (n >= 5; the first n up to 14 are
  * set, later entries are reports only),
  * e.g. to reuse an earlier autotune result without timing again. Tensor-core paths are used
  * only where available whatever their knob says. Site groups must lie in [0, 1024] and max

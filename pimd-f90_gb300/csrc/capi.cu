@@ -207,9 +207,9 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
     KP &kp = E.kp;
     std::memset(&kp, 0, sizeof(kp));
     kp.model = p->pot_model;
-    kp.fx_s0 = (kp.model == 3) ? kp.N : 0;  // the first site of the charge field passes
     kp.natoms = p->natoms;
     kp.N = p->natoms / 3;
+    kp.fx_s0 = (kp.model == 3) ? kp.N : 0;  // the first site of the charge field passes
     kp.S = (spc ? 3 : 4) * kp.N;  // potential.f90:53-80: no M site in the SPC models
     kp.fq = spc ? 0 : kp.N;
     kp.P = p->nbeads;
@@ -969,7 +969,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
     };
     int sf_tiled = E.sf_tiled, ff_regs = E.ff_regs, nbr_block = E.nbr_block, wave = E.wave_shapes;
     int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc, ff_tc = E.ff_tc, dd_overlap = E.dd_overlap, xcache = E.tc_xcache, pdl = E.tc_pdl,
-        ewo = E.ewald_overlap;
+        ewo = E.ewald_overlap, otf = E.dd_otf;
     std::vector<Knob> knobs;
     const bool mixed = E.precision == PIMD_MIXED && E.kp.model < 4;
     if (mixed) {
@@ -982,6 +982,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         if (E.d_tcx) knobs.push_back({&xcache, {1, 0}});
         if (E.tf_ready) knobs.push_back({&pdl, {1, 0}});
         if (E.kp.Fx) knobs.push_back({&ewo, {1, 0}});
+        knobs.push_back({&otf, {1, 0}});
     }
     knobs.push_back({&wave, {1, 0}});
     knobs.push_back({&E.max_slices, {16, 8, 4, 2}});
@@ -999,6 +1000,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         E.tc_xcache = xcache != 0;
         E.tc_pdl = pdl != 0;
         E.ewald_overlap = ewo != 0;
+        E.dd_otf = otf != 0;
     };
     int rc = PIMD_OK;
     float best;
@@ -1046,7 +1048,8 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     if (n >= 11) k[10] = E.tc_pdl && E.ff_tc && E.tf_ready && E.sf_tc && E.tc_ready;
     if (n >= 12) k[11] = E.loop_unroll;
     if (n >= 13) k[12] = E.ewald_overlap && E.aux_stream != nullptr && E.kp.Fx != nullptr;
-    if (n >= 14) k[13] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
+    if (n >= 14) k[13] = E.dd_otf && E.precision == PIMD_MIXED;
+    if (n >= 15) k[14] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
     return PIMD_OK;
 }
 
@@ -1070,6 +1073,7 @@ int pimd_set_tuning(pimd_ctx *ctx, const int *k, int n) {
         E.loop_unroll = k[11];
     }
     if (n >= 13) E.ewald_overlap = k[12] != 0;
+    if (n >= 14) E.dd_otf = k[13] != 0;
     E.gkey.clear();  // a captured MD-step graph holds the old launches: capture again
     return PIMD_OK;
 }

@@ -218,6 +218,7 @@ struct Engine {
     bool tc_pdl = true;               // field pass as a programmatic dependent launch
     int loop_unroll = 2;              // dipole iterations per body of the graph's conditional loop
     bool ewald_overlap = true;        // reciprocal charge / force passes beside the pair gathers
+    bool dd_otf = false;              // real-space dipole tensors formed in each iteration (no cache)
     bool ff_tc = true;                // tensor-core dipole field pass (k_field_tc) when tf_ready
     bool tf_ready = false;
     int tf_nr = 0, tf_nph = 0, tf_jm = 0, tf_ncol = 0, tf_kq = 0;

@@ -369,7 +369,11 @@ __global__ void __launch_bounds__(128) k_dd_tensors_m(KP kp) {
 // real-space dipole field of one iteration: gather over the full list, one warp per
 // molecule, lanes striding over its entries, butterfly reduction in a fixed order
 // (deterministic); writes Efdr (pot_ttm.f90:311-365)
-template <int MODEL>
+// OTF: the tensors formed on the fly from the O fixed-point sites and site offsets (FP32 smear2,
+// T mu = 3 t2 (R . mu) R - t1 mu) instead of loaded from the per-entry cache: more arithmetic, no
+// 39 MB stream per iteration competing with the structure factor for DRAM (512 H2O x 32 beads,
+// TTM3-F: 27 us against 18 us cached, so the cache is the default; the autotuner tries both)
+template <int MODEL, bool OTF>
 __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
     using T = TM<MODEL>;
     const int lane = threadIdx.x & 31;
@@ -385,7 +389,38 @@ __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
     float ei[5][3];
 #pragma unroll
     for (int k = 0; k < 5; k++) ei[k][0] = ei[k][1] = ei[k][2] = 0.f;
-    for (int e = e0 + lane; e < e1; e += 32) {
+    if (OTF) {
+        const float4 *pf = kp.posf + (size_t)b * kp.S;
+        const uint4 *of = kp.ofix + (size_t)b * N;
+        const float L[3] = {kp.ptf.box[0], kp.ptf.box[1], kp.ptf.box[2]};
+        const float Li[3] = {kp.ptf.boxi[0], kp.ptf.boxi[1], kp.ptf.boxi[2]};
+        const uint4 oi = of[i];
+        float4 si[5];
+#pragma unroll
+        for (int k = T::FDI; k <= T::LDI; k++) si[k] = pf[(k - 1) * N + i];
+        for (int e = e0 + lane; e < e1; e += 32) {
+            const int j = fl[e].y;
+            float Rf[3];
+            oo_min_image(kp, oi, of[j], Rf);
+#pragma unroll
+            for (int jsp = T::FDI; jsp <= T::LDI; jsp++) {
+                const float4 c = pf[(jsp - 1) * N + j];
+                const float4 m = dipf[(jsp - 1) * N + j];
+#pragma unroll
+                for (int isp = T::FDI; isp <= T::LDI; isp++) {
+                    const float Rs[3] = {wrapf(Rf[0] + si[isp].x - c.x, L[0], Li[0]), wrapf(Rf[1] + si[isp].y - c.y, L[1], Li[1]),
+                                         wrapf(Rf[2] + si[isp].z - c.z, L[2], Li[2])};
+                    float t1, t2;
+                    smear2<float>(Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2], kp.ptf.apol_dd[isp][jsp], kp.ewf, &t1, &t2);
+                    const float rm = 3.f * t2 * (Rs[0] * m.x + Rs[1] * m.y + Rs[2] * m.z);
+                    ei[isp][0] += rm * Rs[0] - t1 * m.x;
+                    ei[isp][1] += rm * Rs[1] - t1 * m.y;
+                    ei[isp][2] += rm * Rs[2] - t1 * m.z;
+                }
+            }
+        }
+    }
+    for (int e = e0 + lane; e < e1 && !OTF; e += 32) {
         const int j = fl[e].y;
         const float *Te = kp.Tf + ((size_t)b * kp.fcap + e) * kp.ndd * 6;
         int t = 0;
@@ -655,13 +690,19 @@ void launch_site_offsets(Engine &E) {
 void launch_pair_qq_m(Engine &E) {
     dim3 g((E.kp.N * QL + 127) / 128, E.kp.P);
     DISPATCH_M(E, k_pair_qq_m, g, 128);
-    dim3 g2(pair_blocks_m(E, 128), E.kp.P);
-    DISPATCH_M(E, k_dd_tensors_m, g2, 128);
+    if (!E.dd_otf) {
+        dim3 g2(pair_blocks_m(E, 128), E.kp.P);
+        DISPATCH_M(E, k_dd_tensors_m, g2, 128);
+    }
 }
 
 void launch_dd_real_m(Engine &E) {
     dim3 g((E.kp.N * 32 + 127) / 128, E.kp.P);
-    DISPATCH_M(E, k_dd_real_m, g, 128);
+    if (E.kp.model == 2)
+        E.dd_otf ? k_dd_real_m<2, true><<<g, 128, 0, E.stream>>>(E.kp) : k_dd_real_m<2, false><<<g, 128, 0, E.stream>>>(E.kp);
+    else
+        E.dd_otf ? k_dd_real_m<3, true><<<g, 128, 0, E.stream>>>(E.kp) : k_dd_real_m<3, false><<<g, 128, 0, E.stream>>>(E.kp);
+    ++E.nlaunch;
 }
 
 void launch_pair_force_m(Engine &E) {

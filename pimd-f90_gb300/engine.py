@@ -372,7 +372,7 @@ class ForceEngine:
         return self.tuning()
 
     TUNING_KEYS = ("sf_tiled", "sf_groups", "ff_regs", "max_slices", "nbr_block", "wave_shapes", "sf_tc", "ff_tc",
-                   "dd_overlap", "x_cache", "pdl", "loop_unroll", "ewald_overlap")
+                   "dd_overlap", "x_cache", "pdl", "loop_unroll", "ewald_overlap", "dd_otf")
     TUNING_REPORTS = ("qd_tc",)  # read-only: tensor-core force pass in use
 
     def tuning(self):

@@ -105,7 +105,7 @@ def test_autotune_keeps_results(pkg, engine_lib):
     a = eng.full_bead_forces(c["RRt"], c["RRc"], t=0)
     tuned = eng.autotune()
     assert set(tuned) == {"sf_tiled", "sf_groups", "ff_regs", "max_slices", "nbr_block", "wave_shapes", "sf_tc", "ff_tc",
-                          "dd_overlap", "x_cache", "pdl", "loop_unroll", "ewald_overlap", "qd_tc"}
+                          "dd_overlap", "x_cache", "pdl", "loop_unroll", "ewald_overlap", "dd_otf", "qd_tc"}
     assert 1 <= tuned["max_slices"] <= 16
     b = eng.full_bead_forces(c["RRt"], c["RRc"], t=0)
     assert rel(b["dRRt"], a["dRRt"]) < 1e-6
@@ -118,6 +118,13 @@ def test_autotune_keeps_results(pkg, engine_lib):
         assert eng.set_tuning(dd_overlap=ov, pdl=ov, ewald_overlap=ov)["ewald_overlap"] == ov
         runs.append(eng.full_bead_forces(c["RRt"], c["RRc"], t=0))
     assert rel(runs[0]["dRRt"], runs[1]["dRRt"]) < 1e-7
+    # real-space dipole tensors cached per list entry or formed in each iteration: the same
+    # FP32 terms contracted in another order
+    otf = []
+    for v in (0, 1):
+        assert eng.set_tuning(dd_otf=v)["dd_otf"] == v
+        otf.append(eng.full_bead_forces(c["RRt"], c["RRc"], t=0))
+    assert rel(otf[0]["dRRt"], otf[1]["dRRt"]) < 1e-6
     with pytest.raises(ValueError):
         eng.set_tuning(no_such_knob=1)
     eng.close()
