@@ -54,6 +54,8 @@ def parse():
                     help="TTM3-F 4096 H2O x 32 beads (|n| <= 24) steps/s for FP64, mixed and mixed+graph")
     ap.add_argument("--profile-force", choices=["fp64", "mixed"],
                     help="run two force calls of the workload and exit (the case profiled with ncu)")
+    ap.add_argument("--profile-md", choices=["fp64", "mixed"],
+                    help="run three eager MD steps of the workload and exit (integrator kernels under ncu)")
     return ap.parse_args()
 
 
@@ -64,6 +66,22 @@ def profile_force(pkg, which):
     for t in (1, 2):
         r = eng.full_bead_forces(c["RRt"], c["RRc"], t=t)
     print(json.dumps(dict(profile_force=which, Upot=float(r["Upot"]), niter=eng.energies(0)["niter"])))
+    eng.close()
+
+
+def profile_md(pkg, which):
+    c, p = workload(pkg, CONFIG)
+    prec = pkg.engine.PIMD_MIXED if which == "mixed" else pkg.engine.PIMD_FP64
+    eng = pkg.ForceEngine(p, precision=prec)
+    P = p["nbeads"]
+    delt = DT_FS / 1000.0
+    eng.nm_init(P, pkg.waterbox.KB_AMU * TEMP * P / pkg.waterbox.HBAR, delt)
+    eng.langevin_init(delt / 2, 0, 0.1, P * TEMP)
+    mp = eng.md_params(delt, c["massO"], c["massH"], langevin=1, seed=replica_seed(0))
+    RRt, PPt, dRRt = c["RRt"].copy(), c["PPt"].copy(), np.zeros_like(c["RRt"])
+    for t in (1, 2, 3):
+        out, _ = eng.md_step(mp, RRt, PPt, dRRt, t)
+    print(json.dumps(dict(profile_md=which, Upot=float(out[0]), uk=float(out[3]))))
     eng.close()
 
 
@@ -368,6 +386,10 @@ def main():
     if args.profile_force:
         pkg.build_lib.build()
         profile_force(pkg, args.profile_force)
+        return 0
+    if args.profile_md:
+        pkg.build_lib.build()
+        profile_md(pkg, args.profile_md)
         return 0
     if args.impl == "reference":
         if rank != 0:

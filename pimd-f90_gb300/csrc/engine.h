@@ -281,7 +281,7 @@ struct NMArgs {
     int P, natoms;
     const double *C;    // C(P,P) column-major: C[j + P*k] = C(j+1, k+1); then the same as FP32
                         // pairs (hi, lo) with hi + lo = C to 2^-48 (float2[P*P], fast transforms)
-    const double *A;    // [A11, A12, A21, A22, msf, c1, c2] x P
+    const double *A;    // [A11, A12, A21, A22, msf, c1, c2, A12 / msf, A21 msf, c2 sqrt(msf)] x P
     double massO, massH;
     double delt, delt2, box0, boxi0;
     int langevin, evolve;
@@ -289,14 +289,23 @@ struct NMArgs {
     unsigned long long seed, counter;
     const int *tstep;   // device step word: when set, counter = 2 t + phase
     int phase;
-    int fast;           // mixed engine: fused multiply-add mode transforms and FP32 Box-Muller
-                        // draws (FP64 state, not bit-identical to the sequentially rounded sums)
+    int fast;           // mixed engine: the MD-step kernels in FP32-pair arithmetic with FP32
+                        // Box-Muller draws (FP64 state, not bit-identical to the FP64 kernels)
+    double mass[2], minv[2], msqrt[2];  // O, H: m, 1/m, sqrt(m) (filled by nm_fast_args)
+    float2 kick;                        // MASSCON dt/2 as an FP32 pair
+    float2 hminv[2], pinv, boxf;        // 1/(2m) of O, H; 1/P; box edge (pairs)
+    float boxif;                        // 1/box edge
 };
 __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt, double *RRc);
 __global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk);
 __global__ void k_md_sum(int P, const double *Upott, const double *virialt, const double *virialct, const double *uk,
                          double *out4);
 void nm_launch_shape(int P, int natoms, int *threads, int *blocks, size_t *smem);
+void nm_smem_optin(int P);
+void nm_extend_A(std::vector<double> &A, int P);
+void nm_fast_args(NMArgs &a);
+void nm_launch_md_pre(const NMArgs &a, cudaStream_t st, double *RRt, double *PPt, const double *dRRt, double *RRc);
+void nm_launch_md_post(const NMArgs &a, cudaStream_t st, double *PPt, const double *dRRt, double *uk);
 void nm_pair_copy(const std::vector<double> &C, std::vector<double> &out);  // C then its FP32 pairs
 void nm_init_host(int P, double omegan, double delta, double setNMfreq, std::vector<double> &A11,
                   std::vector<double> &A12, std::vector<double> &A21, std::vector<double> &A22,

@@ -105,11 +105,8 @@ static int enqueue_group_step(pimd_batch *bt, BatchGroup &g) {
         const BatchReplica &r = bt->reps[ri];
         NMArgs a = replica_args(bt, r, E);
         a.phase = 0;
-        int threads, blocks;
-        size_t smem;
-        nm_launch_shape(r.P, r.natoms, &threads, &blocks, &smem);
-        k_md_pre<<<blocks, threads, smem, E.stream>>>(a, g.RRt + r.bead0 * na3, g.PPt + r.bead0 * na3,
-                                                      g.dRRt + r.bead0 * na3, g.RRc + r.local * na3);
+        nm_launch_md_pre(a, E.stream, g.RRt + r.bead0 * na3, g.PPt + r.bead0 * na3, g.dRRt + r.bead0 * na3,
+                         g.RRc + r.local * na3);
         ++E.nlaunch;
     }
     double *d = E.d_out;  // Upott, virialt, virialct of all beads of the group
@@ -120,10 +117,7 @@ static int enqueue_group_step(pimd_batch *bt, BatchGroup &g) {
         const BatchReplica &r = bt->reps[ri];
         NMArgs a = replica_args(bt, r, E);
         a.phase = 1;
-        int threads, blocks;
-        size_t smem;
-        nm_launch_shape(r.P, r.natoms, &threads, &blocks, &smem);
-        k_md_post<<<blocks, threads, smem, E.stream>>>(a, g.PPt + r.bead0 * na3, g.dRRt + r.bead0 * na3, g.uk + r.local);
+        nm_launch_md_post(a, E.stream, g.PPt + r.bead0 * na3, g.dRRt + r.bead0 * na3, g.uk + r.local);
         k_md_sum<<<1, 32, 0, E.stream>>>(r.P, d + r.bead0, d + g.Ptot + r.bead0, d + 2 * g.Ptot + r.bead0, g.uk + r.local,
                                          bt->d_out4 + 4 * (size_t)ri);
         E.nlaunch += 2;
@@ -263,10 +257,12 @@ int pimd_batch_create(pimd_batch **out, const pimd_params *common, const pimd_re
             A[5 * r.P + j] = c1;
             A[6 * r.P + j] = std::sqrt(KB_AMU * r.P * r.temp) * std::sqrt(1 - c1 * c1);
         }
+        nm_extend_A(A, r.P);
         std::vector<double> CP;
         nm_pair_copy(C, CP);  // C, then its FP32 pairs for the mixed engine's transforms
         if ((rc = balloc(bt, &r.d_C, CP.size())) || (rc = balloc(bt, &r.d_A, A.size()))) break;
         cudaMemcpy(r.d_C, CP.data(), sizeof(double) * CP.size(), cudaMemcpyHostToDevice);
+        nm_smem_optin(r.P);
         cudaMemcpy(r.d_A, A.data(), sizeof(double) * A.size(), cudaMemcpyHostToDevice);
     }
     if (!rc) rc = bcuda(bt, cudaDeviceSynchronize(), "batch set-up");

@@ -36,14 +36,6 @@ PIMD_D double gauss_from(unsigned a, unsigned b) {
     return sqrt(-2.0 * log(u1)) * cos(TWOPI * u2);
 }
 
-// the same draw with FP32 logarithm and cosine (the mixed engine): u1 keeps its full range
-// (2^-32 ... 1, tails to 6.66 sigma), the value differs from gauss_from by FP32 rounding only
-PIMD_D double gauss_from_f(unsigned a, unsigned b) {
-    const float u1 = ((float)a + 1.0f) * 2.3283064365386963e-10f;
-    const float u2 = (float)b * 2.3283064365386963e-10f;
-    return (double)(sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2));
-}
-
 PIMD_D double noise(const NMArgs &a, int atom, int j, int c) {
     if (a.xi) return a.xi[c + 3 * j + (size_t)3 * a.P * atom];
     const unsigned long long idx = ((unsigned long long)atom * a.P + j) * 3 + c;
@@ -51,37 +43,117 @@ PIMD_D double noise(const NMArgs &a, int atom, int j, int c) {
                                            : a.counter;
     const uint4 r = philox4x32(make_uint4((unsigned)idx, (unsigned)(idx >> 32), (unsigned)ctr, (unsigned)(ctr >> 32)),
                                make_uint2((unsigned)a.seed, (unsigned)(a.seed >> 32)));
-    return a.fast ? gauss_from_f(r.x, r.y) : gauss_from(r.x, r.y);
+    return gauss_from(r.x, r.y);
 }
 
-// x~_j = sum_k C(j,k) x_k  (real2NM) or x_j = sum_k C(k,j) x~_k (NM2real), rounded per op,
-// or (fast) one fused multiply-add per term: half the FP64 instructions
-PIMD_D double nm_row(const double *Cs, const double *v, int P, int j, int c, bool fwd, bool fast = false) {
+// C(j,k) sits in shared memory at Cs[j + (P + 1) k]: the padded column keeps the rows of
+// NM2real (threads of a warp at different j, same k) on different banks
+__host__ __device__ inline int nm_ld(int P) { return P + 1; }
+template <typename T>
+PIMD_D void nm_load_C(T *Cs, const T *C, int P) {
+    for (int i = threadIdx.x; i < P * P; i += blockDim.x) Cs[i % P + nm_ld(P) * (i / P)] = C[i];
+}
+
+// x~_j = sum_k C(j,k) x_k  (real2NM) or x_j = sum_k C(k,j) x~_k (NM2real), rounded per op
+PIMD_D double nm_row(const double *Cs, const double *v, int P, int j, int c, bool fwd) {
+    const int L = nm_ld(P);
     double s = 0.0;
-    if (fast) {
-        for (int k = 0; k < P; k++) s = fma(fwd ? Cs[j + P * k] : Cs[k + P * j], v[3 * k + c], s);
-        return s;
-    }
     for (int k = 0; k < P; k++) {
-        const double ck = fwd ? Cs[j + P * k] : Cs[k + P * j];
+        const double ck = fwd ? Cs[j + L * k] : Cs[k + L * j];
         s = __dadd_rn(s, __dmul_rn(ck, v[3 * k + c]));
     }
     return s;
 }
 
-// The fast (mixed-engine) transforms in FP32 pairs on the FP32 pipe: x = hi + lo (hi = fp32(x),
-// lo = fp32(x - hi), 48 bits), and each output a compensated dot product (TwoProduct by FMA,
-// TwoSum; Ogita-Rump-Oishi Dot2) over the pairs of C and of the group's vector, then one
-// FP64 sum: about twice-FP32 accuracy (~1e-14 relative for the orthogonal C) for a few FP64
-// operations per element instead of P fused multiply-adds. Intrinsics keep every rounding.
-PIMD_D float2 to_pair(double x) {
-    const float h = __double2float_rn(x);
-    return make_float2(h, __double2float_rn(x - (double)h));
+// Langevin_NM on one atom's momenta held in shared memory p[3P] (group-local).
+PIMD_D void langevin_atom(const NMArgs &a, const double *Cs, double *p, double *tr, int atom, int j, int c,
+                          bool active) {
+    if (active) tr[3 * j + c] = nm_row(Cs, p, a.P, j, c, true);
+    __syncthreads();
+    if (active) {
+        const double m = (atom % 3 == 0) ? a.massO : a.massH;
+        const double sqrtmass = sqrt(m * a.A[4 * a.P + j]);
+        const double c1 = a.A[5 * a.P + j], c2 = a.A[6 * a.P + j];
+        tr[3 * j + c] = __dadd_rn(__dmul_rn(c1, tr[3 * j + c]), __dmul_rn(c2, __dmul_rn(sqrtmass, noise(a, atom, j, c))));
+    }
+    __syncthreads();
+    if (active) p[3 * j + c] = nm_row(Cs, tr, a.P, j, c, false);
+    __syncthreads();
 }
-PIMD_D double nm_row_pair(const float2 *Cf, const float2 *vf, int P, int j, int c, bool fwd) {
+
+// ---- the mixed engine's integrator: FP32-pair (double-float) arithmetic ----------------------
+// The FP64 state enters and leaves as pairs x = h + l by bit operations (h: the mantissa cut to
+// 24 bits, l: the remaining 29 bits rounded to FP32, ~2^-48 relative), so the step issues almost
+// no FP64 instruction (this part runs FP64 at 1/64 of the FP32 rate). Error-free transforms:
+// TwoSum (Knuth), Fast2Sum (Dekker), TwoProduct by FMA; pair sum and product after Joldes,
+// Muller and Popescu, ACM TOMS 44 (2017), Algorithm 6 (AccurateDWPlusDW, <= 3u^2) and the
+// FMA product (DWTimesDW, ~5u^2). Intrinsics keep every rounding.
+struct dfl {
+    float h, l;
+};
+PIMD_D dfl two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+PIMD_D dfl fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+PIMD_D dfl df_add(dfl a, dfl b) {
+    const dfl s = two_sum(a.h, b.h), t = two_sum(a.l, b.l);
+    const dfl v = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
+    return fast_two_sum(v.h, __fadd_rn(t.l, v.l));
+}
+PIMD_D dfl df_neg(dfl a) { return {-a.h, -a.l}; }
+PIMD_D dfl df_mul(dfl a, dfl b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e));
+    return fast_two_sum(p, e);
+}
+// double -> pair by bit operations only (a branch to conversion instructions would be
+// predicated and issued on every lane): exact to 2^-48 for 2^-70 <= |x| < 2^101; smaller
+// magnitudes (zero included) give a signed zero, larger ones and NaN an infinity / NaN
+PIMD_D dfl df_split(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned hw = (unsigned)(u >> 32), lw = (unsigned)u;
+    const int eb = (int)((hw >> 20) & 0x7ffu) - 1023;
+    const unsigned sign = hw & 0x80000000u;
+    if (eb < -70) return {__uint_as_float(sign), 0.f};
+    if (eb > 100) return {__uint_as_float(sign | 0x7f800000u | ((eb == 1024 && ((hw & 0xfffffu) | lw)) ? 0x400000u : 0u)), 0.f};
+    const float h = __uint_as_float(sign | ((unsigned)(eb + 127) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29));
+    const float l = __fmul_rn(__uint2float_rn(lw & 0x1fffffffu), __uint_as_float((unsigned)(eb + 75) << 23));
+    return {h, __uint_as_float(__float_as_uint(l) | sign)};
+}
+// float -> double by bit operations (exact for every input)
+PIMD_D double f2d_bits(float f) {
+    const unsigned b = __float_as_uint(f), e = (b >> 23) & 0xffu;
+    const unsigned long long sg = (unsigned long long)(b & 0x80000000u) << 32;
+    unsigned m = b & 0x7fffffu, ed;
+    if (e == 255) {
+        ed = 0x7ffu;
+    } else if (e != 0) {
+        ed = e + 896;
+    } else if (m == 0) {
+        ed = 0;
+    } else {  // subnormal: normalise the mantissa
+        const int n = __clz(m) - 8;
+        m = (m << n) & 0x7fffffu;
+        ed = 897 - n;
+    }
+    return __longlong_as_double((long long)(sg | ((unsigned long long)ed << 52) | ((unsigned long long)m << 29)));
+}
+PIMD_D double df_double(dfl a) { return f2d_bits(a.h) + f2d_bits(a.l); }
+PIMD_D dfl df_f(float2 v) { return {v.x, v.y}; }
+PIMD_D float2 df_store(dfl a) { return make_float2(a.h, a.l); }
+
+// Dot2 over the pairs of C and of the group's vector (as nm_row_pair), result as a pair
+PIMD_D dfl nm_row_df(const float2 *Cf, const float2 *vf, int P, int j, int c, bool fwd) {
+    const int L = nm_ld(P);
     float s = 0.f, comp = 0.f;
+#pragma unroll 4
     for (int k = 0; k < P; k++) {
-        const float2 ck = fwd ? Cf[j + P * k] : Cf[k + P * j];
+        const float2 ck = fwd ? Cf[j + L * k] : Cf[k + L * j];
         const float2 vk = vf[3 * k + c];
         const float ph = __fmul_rn(ck.x, vk.x);
         float pe = __fmaf_rn(ck.x, vk.x, -ph);
@@ -91,40 +163,186 @@ PIMD_D double nm_row_pair(const float2 *Cf, const float2 *vf, int P, int j, int 
         comp = __fadd_rn(comp, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(ph, z)), pe));
         s = t;
     }
-    return (double)s + (double)comp;
+    return two_sum(s, comp);
 }
 
-// Langevin_NM on one atom's momenta held in shared memory p[3P] (group-local).
-PIMD_D void langevin_atom(const NMArgs &a, const double *Cs, double *p, double *tr, int atom, int j, int c,
-                          bool active, const float2 *Cf = nullptr, float2 *vf = nullptr) {
-    if (a.fast) {  // the same steps on FP32 pairs (vf: the group's vector as pairs)
-        if (active) vf[3 * j + c] = to_pair(p[3 * j + c]);
-        __syncthreads();
-        double t = 0.0;
-        if (active) t = nm_row_pair(Cf, vf, a.P, j, c, true);
-        __syncthreads();
+// per-bead constants of the fast kernels as pairs in shared memory: A11, A22, c1 (P each), then
+// per atom type (O, H) A12 / (m msf), A21 m msf, c2 sqrt(m msf) (2 x 3P); from A's rows 7-9
+// (A12 / msf, A21 msf, c2 sqrt(msf)) and the host-computed 1/m, m, sqrt(m) of NMArgs
+PIMD_D void nm_fast_consts(const NMArgs &a, float2 *kf) {
+    const int P = a.P;
+    for (int i = threadIdx.x; i < 3 * P; i += blockDim.x) {
+        const int row = i / P, j = i % P;
+        kf[i] = df_store(df_split(a.A[(row == 0 ? 0 : row == 1 ? 3 : 5) * P + j]));
+        for (int ty = 0; ty < 2; ty++) {
+            const double f = row == 0 ? a.minv[ty] : row == 1 ? a.mass[ty] : a.msqrt[ty];
+            const dfl v = df_mul(df_split(a.A[(7 + row) * P + j]), df_split(f));
+            kf[3 * P + ty * 3 * P + i] = df_store(v);
+        }
+    }
+}
+
+PIMD_D float gauss_f(unsigned a, unsigned b) {
+    const float u1 = ((float)a + 1.0f) * 2.3283064365386963e-10f;
+    const float u2 = (float)b * 2.3283064365386963e-10f;
+    return sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+}
+PIMD_D dfl noise_df(const NMArgs &a, int atom, int j, int c) {
+    if (a.xi) return df_split(a.xi[c + 3 * j + (size_t)3 * a.P * atom]);
+    const unsigned long long idx = ((unsigned long long)atom * a.P + j) * 3 + c;
+    const unsigned long long ctr = a.tstep ? 2ull * (unsigned long long)(long long)a.tstep[0] + (unsigned long long)a.phase
+                                           : a.counter;
+    const uint4 r = philox4x32(make_uint4((unsigned)idx, (unsigned)(idx >> 32), (unsigned)ctr, (unsigned)(ctr >> 32)),
+                               make_uint2((unsigned)a.seed, (unsigned)(a.seed >> 32)));
+    return {gauss_f(r.x, r.y), 0.f};
+}
+
+// Langevin_NM on the group's momenta as pairs (vp: the group's pair vector, pp: this thread's)
+PIMD_D dfl langevin_df(const NMArgs &a, const float2 *Cf, const float2 *kf, float2 *vp, dfl pp, int atom, int j, int c,
+                       bool active) {
+    const int P = a.P, ty = (atom % 3 == 0) ? 0 : 1;
+    if (active) vp[3 * j + c] = df_store(pp);
+    __syncthreads();
+    dfl t{0.f, 0.f};
+    if (active) t = nm_row_df(Cf, vp, P, j, c, true);
+    __syncthreads();
+    if (active)
+        vp[3 * j + c] = df_store(df_add(df_mul(df_f(kf[2 * P + j]), t), df_mul(df_f(kf[3 * P + ty * 3 * P + 2 * P + j]),
+                                                                                 noise_df(a, atom, j, c))));
+    __syncthreads();
+    if (active) pp = nm_row_df(Cf, vp, P, j, c, false);
+    __syncthreads();
+    return pp;
+}
+
+// shared memory of the fast kernels: padded C and the constants as pairs, then per group two
+// pair vectors and the centroid's image shift (3 floats, padded to 2 float2)
+PIMD_D void nm_fast_layout(int P, int g, float2 *&Cf, float2 *&kf, float2 *&vx, float2 *&vp, float *&nsh) {
+    extern __shared__ double sh[];
+    Cf = reinterpret_cast<float2 *>(sh);
+    kf = Cf + nm_ld(P) * P;
+    vx = kf + 9 * P + g * (6 * P + 2);
+    vp = vx + 3 * P;
+    nsh = reinterpret_cast<float *>(vp + 3 * P);
+}
+size_t nm_fast_smem(int P, int G) { return sizeof(float2) * ((size_t)nm_ld(P) * P + 9 * (size_t)P + (size_t)G * (6 * P + 2)); }
+
+void nm_fast_args(NMArgs &a) {
+    const double m[2] = {a.massO, a.massH};
+    for (int t = 0; t < 2; t++) {
+        a.mass[t] = m[t];
+        a.minv[t] = 1.0 / m[t];
+        a.msqrt[t] = std::sqrt(m[t]);
+    }
+    auto pair = [](double v) {
+        const float h = (float)v;
+        return make_float2(h, (float)(v - (double)h));
+    };
+    a.kick = pair(MASSCON * a.delt2);
+    a.hminv[0] = pair(0.5 / a.massO);
+    a.hminv[1] = pair(0.5 / a.massH);
+    a.pinv = pair(1.0 / a.P);
+    a.boxf = pair(a.box0);
+    a.boxif = (float)a.boxi0;
+}
+
+__global__ void k_md_pre_fast(NMArgs a, double *RRt, double *PPt, const double *dRRt, double *RRc) {
+    const int P = a.P, G = blockDim.x / (3 * P);
+    const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
+    const int atom = blockIdx.x * G + g;
+    float2 *Cf, *kf, *vx, *vp;
+    float *nsh;
+    nm_fast_layout(P, min(g, G - 1), Cf, kf, vx, vp, nsh);
+    nm_load_C(Cf, reinterpret_cast<const float2 *>(a.C + P * P), P);
+    nm_fast_consts(a, kf);
+    const bool active = g < G && atom < a.natoms;
+    const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
+    dfl px{0.f, 0.f}, pp{0.f, 0.f}, pg{0.f, 0.f};
+    if (active) {
+        px = df_split(RRt[gi]);
+        pp = df_split(PPt[gi]);
+        pg = df_split(dRRt[gi]);
+    }
+    __syncthreads();
+    if (a.langevin) pp = langevin_df(a, Cf, kf, vp, pp, atom, j, c, active);
+    pp = df_add(pp, df_neg(df_mul(df_f(a.kick), pg)));  // p -= MASSCON dt/2 dV/dx
+    const int ty = (atom % 3 == 0) ? 0 : 1;
+    if (a.evolve) {
         if (active) {
-            const double m = (atom % 3 == 0) ? a.massO : a.massH;
-            const double sqrtmass = sqrt(m * a.A[4 * a.P + j]);
-            const double c1 = a.A[5 * a.P + j], c2 = a.A[6 * a.P + j];
-            vf[3 * j + c] = to_pair(c1 * t + c2 * (sqrtmass * noise(a, atom, j, c)));
+            vx[3 * j + c] = df_store(px);
+            vp[3 * j + c] = df_store(pp);
         }
         __syncthreads();
-        if (active) p[3 * j + c] = nm_row_pair(Cf, vf, a.P, j, c, false);
+        dfl xt{0.f, 0.f}, pt{0.f, 0.f};
+        if (active) {
+            xt = nm_row_df(Cf, vx, P, j, c, true);
+            pt = nm_row_df(Cf, vp, P, j, c, true);
+        }
         __syncthreads();
-        return;
+        if (active) {
+            const float2 *kt = kf + 3 * P + ty * 3 * P;
+            vx[3 * j + c] = df_store(df_add(df_mul(df_f(kf[j]), xt), df_mul(df_f(kt[j]), pt)));
+            vp[3 * j + c] = df_store(df_add(df_mul(df_f(kt[P + j]), xt), df_mul(df_f(kf[P + j]), pt)));
+        }
+        __syncthreads();
+        if (active) {
+            px = nm_row_df(Cf, vx, P, j, c, false);
+            pp = nm_row_df(Cf, vp, P, j, c, false);
+        }
+    } else if (active) {  // P = 1: free flight
+        px = df_add(px, df_mul(pp, df_split(a.delt * a.minv[ty])));
     }
-    if (active) tr[3 * j + c] = nm_row(Cs, p, a.P, j, c, true, a.fast);
+    __syncthreads();  // the transforms have read vx
+    if (active) vx[3 * j + c] = df_store(px);
+    __syncthreads();
+    // centroid (main_stuff.f90:107-125) in pair arithmetic, its image from the FP32 value (any
+    // whole number of boxes is a valid shift; the molecule moves as a whole)
+    if (active && j == 0) {
+        dfl sum{0.f, 0.f};
+        for (int k = 0; k < P; k++) sum = df_add(sum, df_f(vx[3 * k + c]));
+        const dfl rc = df_mul(sum, df_f(a.pinv));
+        const float n = rintf(__fmul_rn(rc.h, a.boxif));
+        const dfl rs = df_add(rc, df_neg(df_mul(df_f(a.boxf), dfl{n, 0.f})));
+        RRc[3 * atom + c] = df_double(rs);
+        nsh[c] = n;
+    }
     __syncthreads();
     if (active) {
-        const double m = (atom % 3 == 0) ? a.massO : a.massH;
-        const double sqrtmass = sqrt(m * a.A[4 * a.P + j]);
-        const double c1 = a.A[5 * a.P + j], c2 = a.A[6 * a.P + j];
-        tr[3 * j + c] = __dadd_rn(__dmul_rn(c1, tr[3 * j + c]), __dmul_rn(c2, __dmul_rn(sqrtmass, noise(a, atom, j, c))));
+        RRt[gi] = df_double(df_add(px, df_neg(df_mul(df_f(a.boxf), dfl{nsh[c], 0.f}))));
+        PPt[gi] = df_double(pp);
     }
+}
+
+__global__ void k_md_post_fast(NMArgs a, double *PPt, const double *dRRt, double *uk) {
+    const int P = a.P, G = blockDim.x / (3 * P);
+    const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
+    const int atom = blockIdx.x * G + g;
+    float2 *Cf, *kf, *vx, *vp;
+    float *nsh;
+    nm_fast_layout(P, min(g, G - 1), Cf, kf, vx, vp, nsh);
+    nm_load_C(Cf, reinterpret_cast<const float2 *>(a.C + P * P), P);
+    nm_fast_consts(a, kf);
+    const bool active = g < G && atom < a.natoms;
+    const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
+    dfl pp{0.f, 0.f};
+    if (active) pp = df_add(df_split(PPt[gi]), df_neg(df_mul(df_f(a.kick), df_split(dRRt[gi]))));
     __syncthreads();
-    if (active) p[3 * j + c] = nm_row(Cs, tr, a.P, j, c, false, a.fast);
+    if (a.langevin) pp = langevin_df(a, Cf, kf, vp, pp, atom, j, c, active);
+    dfl ke{0.f, 0.f};
+    if (active) {
+        PPt[gi] = df_double(pp);
+        ke = df_mul(df_mul(pp, pp), df_f(a.hminv[(atom % 3 == 0) ? 0 : 1]));
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        ke = df_add(ke, dfl{__shfl_xor_sync(0xffffffffu, ke.h, o), __shfl_xor_sync(0xffffffffu, ke.l, o)});
+    __shared__ double wke[32];
+    if ((threadIdx.x & 31) == 0) wke[threadIdx.x >> 5] = df_double(ke);
     __syncthreads();
+    if (threadIdx.x == 0 && uk) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += wke[w];
+        atomicAdd(uk, t);
+    }
 }
 
 // MD.f90:40-73 up to the force call: Langevin, half kick, EvolveRing (or free flight for
@@ -135,15 +353,8 @@ __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt,
     const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
     const int atom = blockIdx.x * G + g;
     double *Cs = sh;
-    double *x = Cs + P * P + g * 9 * P, *p = x + 3 * P, *tr = p + 3 * P;
-    // fast transforms: C as FP32 pairs after the FP64 layout, and two pair vectors per group
-    float2 *Cf = reinterpret_cast<float2 *>(sh + P * P + G * 9 * P), *vf = Cf + P * P + g * 6 * P;
-    for (int i = threadIdx.x; i < P * P; i += blockDim.x) {
-        if (a.fast)
-            Cf[i] = reinterpret_cast<const float2 *>(a.C + P * P)[i];
-        else
-            Cs[i] = a.C[i];
-    }
+    double *x = Cs + nm_ld(P) * P + g * 9 * P, *p = x + 3 * P, *tr = p + 3 * P;
+    nm_load_C(Cs, a.C, P);
     const bool active = g < G && atom < a.natoms;
     const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
     if (active) {
@@ -151,40 +362,15 @@ __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt,
         p[3 * j + c] = PPt[gi];
     }
     __syncthreads();
-    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active, Cf, vf);
+    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active);
     if (active) p[3 * j + c] = __dsub_rn(p[3 * j + c], __dmul_rn(__dmul_rn(MASSCON, dRRt[gi]), a.delt2));
     __syncthreads();
     const double m = (atom % 3 == 0) ? a.massO : a.massH;
-    if (a.evolve && a.fast) {  // EvolveRing on FP32 pairs: vf holds x, vf + 3P holds p
-        float2 *vx = vf, *vp = vf + 3 * P;
-        if (active) {
-            vx[3 * j + c] = to_pair(x[3 * j + c]);
-            vp[3 * j + c] = to_pair(p[3 * j + c]);
-        }
-        __syncthreads();
+    if (a.evolve) {
         double xt = 0, pt = 0;
         if (active) {
-            xt = nm_row_pair(Cf, vx, P, j, c, true);
-            pt = nm_row_pair(Cf, vp, P, j, c, true);
-        }
-        __syncthreads();
-        if (active) {
-            const double A11 = a.A[j], A12 = a.A[P + j], A21 = a.A[2 * P + j], A22 = a.A[3 * P + j], msf = a.A[4 * P + j];
-            vx[3 * j + c] = to_pair(A11 * xt + (A12 * pt) / (m * msf));
-            vp[3 * j + c] = to_pair(A21 * m * msf * xt + A22 * pt);
-        }
-        __syncthreads();
-        if (active) {
-            const double xr = nm_row_pair(Cf, vx, P, j, c, false), pr = nm_row_pair(Cf, vp, P, j, c, false);
-            x[3 * j + c] = xr;
-            p[3 * j + c] = pr;
-        }
-        __syncthreads();
-    } else if (a.evolve) {
-        double xt = 0, pt = 0;
-        if (active) {
-            xt = nm_row(Cs, x, P, j, c, true, a.fast);
-            pt = nm_row(Cs, p, P, j, c, true, a.fast);
+            xt = nm_row(Cs, x, P, j, c, true);
+            pt = nm_row(Cs, p, P, j, c, true);
         }
         __syncthreads();
         if (active) {
@@ -197,8 +383,8 @@ __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt,
         __syncthreads();
         double xr = 0, pr = 0;
         if (active) {
-            xr = nm_row(Cs, tr, P, j, c, false, a.fast);
-            pr = nm_row(Cs, x, P, j, c, false, a.fast);
+            xr = nm_row(Cs, tr, P, j, c, false);
+            pr = nm_row(Cs, x, P, j, c, false);
         }
         __syncthreads();
         if (active) {
@@ -232,19 +418,13 @@ __global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk)
     const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
     const int atom = blockIdx.x * G + g;
     double *Cs = sh;
-    double *p = Cs + P * P + g * 9 * P, *tr = p + 3 * P;
-    float2 *Cf = reinterpret_cast<float2 *>(sh + P * P + G * 9 * P), *vf = Cf + P * P + g * 6 * P;
-    for (int i = threadIdx.x; i < P * P; i += blockDim.x) {
-        if (a.fast)
-            Cf[i] = reinterpret_cast<const float2 *>(a.C + P * P)[i];
-        else
-            Cs[i] = a.C[i];
-    }
+    double *p = Cs + nm_ld(P) * P + g * 9 * P, *tr = p + 3 * P;
+    nm_load_C(Cs, a.C, P);
     const bool active = g < G && atom < a.natoms;
     const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
     if (active) p[3 * j + c] = __dsub_rn(PPt[gi], __dmul_rn(__dmul_rn(MASSCON, dRRt[gi]), a.delt2));
     __syncthreads();
-    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active, Cf, vf);
+    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active);
     double ke = 0.0;
     if (active) {
         PPt[gi] = p[3 * j + c];
@@ -270,8 +450,8 @@ __global__ void k_evolve(NMArgs a, double *RRt, double *PPt) {
     const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
     const int atom = blockIdx.x * G + g;
     double *Cs = sh;
-    double *x = Cs + P * P + g * 9 * P, *p = x + 3 * P, *tr = p + 3 * P;
-    for (int i = threadIdx.x; i < P * P; i += blockDim.x) Cs[i] = a.C[i];
+    double *x = Cs + nm_ld(P) * P + g * 9 * P, *p = x + 3 * P, *tr = p + 3 * P;
+    nm_load_C(Cs, a.C, P);
     const bool active = g < G && atom < a.natoms;
     const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
     if (active) {
@@ -304,8 +484,8 @@ __global__ void k_langevin(NMArgs a, double *PPt) {
     const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
     const int atom = blockIdx.x * G + g;
     double *Cs = sh;
-    double *p = Cs + P * P + g * 9 * P, *tr = p + 3 * P;
-    for (int i = threadIdx.x; i < P * P; i += blockDim.x) Cs[i] = a.C[i];
+    double *p = Cs + nm_ld(P) * P + g * 9 * P, *tr = p + 3 * P;
+    nm_load_C(Cs, a.C, P);
     const bool active = g < G && atom < a.natoms;
     const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
     if (active) p[3 * j + c] = PPt[gi];
@@ -335,8 +515,60 @@ void nm_launch_shape(int P, int natoms, int *threads, int *blocks, size_t *smem)
     if (G < 1) G = 1;
     *threads = ((G * 3 * P + 31) / 32) * 32;  // whole warps (the KE reduction shuffles)
     *blocks = (natoms + G - 1) / G;
-    // FP64 C and vectors, then C and two vectors per group as FP32 pairs (fast transforms)
-    *smem = sizeof(double) * ((size_t)P * P + (size_t)G * 9 * P) + sizeof(float2) * ((size_t)P * P + (size_t)G * 6 * P);
+    *smem = sizeof(double) * ((size_t)(P + 1) * P + (size_t)G * 9 * P);  // padded C, three vectors per group
+}
+
+// above 48 KB of dynamic shared memory (P > 40 beads) the kernels need the opt-in; called
+// once per bead count, outside any stream capture
+void nm_smem_optin(int P) {
+    int threads, blocks;
+    size_t smem;
+    nm_launch_shape(P, 1, &threads, &blocks, &smem);
+    smem = std::max(smem, nm_fast_smem(P, std::max(1, 256 / (3 * P))));
+    if (smem <= 48 * 1024) return;
+    cudaFuncSetAttribute(k_md_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_md_post, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_evolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_langevin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_md_pre_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_md_post_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+// rows 7-9 of the device table (A12 / msf, A21 msf, c2 sqrt(msf)) from rows 1, 2, 4, 6
+void nm_extend_A(std::vector<double> &A, int P) {
+    A.resize(10 * (size_t)P);
+    for (int j = 0; j < P; j++) {
+        const double msf = A[4 * P + j];
+        A[7 * P + j] = A[P + j] / msf;
+        A[8 * P + j] = A[2 * P + j] * msf;
+        A[9 * P + j] = A[6 * P + j] * std::sqrt(msf);
+    }
+}
+
+// the MD-step kernels: the exact ones, or for the mixed engine the FP32-pair ones
+void nm_launch_md_pre(const NMArgs &a0, cudaStream_t st, double *RRt, double *PPt, const double *dRRt, double *RRc) {
+    int threads, blocks;
+    size_t smem;
+    nm_launch_shape(a0.P, a0.natoms, &threads, &blocks, &smem);
+    if (!a0.fast) {
+        k_md_pre<<<blocks, threads, smem, st>>>(a0, RRt, PPt, dRRt, RRc);
+        return;
+    }
+    NMArgs a = a0;
+    nm_fast_args(a);
+    k_md_pre_fast<<<blocks, threads, nm_fast_smem(a.P, std::max(1, 256 / (3 * a.P))), st>>>(a, RRt, PPt, dRRt, RRc);
+}
+void nm_launch_md_post(const NMArgs &a0, cudaStream_t st, double *PPt, const double *dRRt, double *uk) {
+    int threads, blocks;
+    size_t smem;
+    nm_launch_shape(a0.P, a0.natoms, &threads, &blocks, &smem);
+    if (!a0.fast) {
+        k_md_post<<<blocks, threads, smem, st>>>(a0, PPt, dRRt, uk);
+        return;
+    }
+    NMArgs a = a0;
+    nm_fast_args(a);
+    k_md_post_fast<<<blocks, threads, nm_fast_smem(a.P, std::max(1, 256 / (3 * a.P))), st>>>(a, PPt, dRRt, uk);
 }
 
 void nm_pair_copy(const std::vector<double> &C, std::vector<double> &out) {
@@ -437,9 +669,10 @@ int pimd_nm_init(pimd_ctx *ctx, int P, double omegan, double delta, double setNM
         if (E.d_nmC) cudaFree(E.d_nmC);
         if (E.d_nmA) cudaFree(E.d_nmA);
         if (cudaMalloc((void **)&E.d_nmC, sizeof(double) * 2 * P * P) != cudaSuccess ||
-            cudaMalloc((void **)&E.d_nmA, sizeof(double) * 7 * P) != cudaSuccess)
+            cudaMalloc((void **)&E.d_nmA, sizeof(double) * 10 * P) != cudaSuccess)
             return PIMD_ERR_NOMEM;
         E.nm_P = P;
+        nm_smem_optin(P);
     }
     std::vector<double> A(7 * P, 0.0);
     for (int j = 0; j < P; j++) {
@@ -456,7 +689,8 @@ int pimd_nm_init(pimd_ctx *ctx, int P, double omegan, double delta, double setNM
     std::vector<double> CP;
     nm_pair_copy(CC, CP);
     cudaMemcpy(E.d_nmC, CP.data(), sizeof(double) * CP.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(E.d_nmA, A.data(), sizeof(double) * 7 * P, cudaMemcpyHostToDevice);
+    nm_extend_A(A, P);
+    cudaMemcpy(E.d_nmA, A.data(), sizeof(double) * 10 * P, cudaMemcpyHostToDevice);
     auto out = [&](double *dst, const std::vector<double> &v) {
         if (dst) std::memcpy(dst, v.data(), sizeof(double) * v.size());
     };
@@ -485,8 +719,10 @@ int pimd_langevin_init(pimd_ctx *ctx, double delt2, int centroid_thermostat, dou
         A[5 * P + i] = c1;
         A[6 * P + i] = c2;
     }
+    std::vector<double> Ad(A.begin(), A.begin() + 7 * P);
+    nm_extend_A(Ad, P);
     cudaSetDevice(E.device);
-    return nm_err(E, cudaMemcpy(E.d_nmA, A.data(), sizeof(double) * 7 * P, cudaMemcpyHostToDevice), "langevin_init");
+    return nm_err(E, cudaMemcpy(E.d_nmA, Ad.data(), sizeof(double) * 10 * P, cudaMemcpyHostToDevice), "langevin_init");
 }
 
 int pimd_evolve_ring(pimd_ctx *ctx, double *RR, double *PP, int P, double mass) {
@@ -557,7 +793,7 @@ static int md_step_enqueue(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt,
     nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
     if (!E.capturing) launch_set_step(E, t);  // the Langevin counter of k_md_pre reads t
     timer_begin(E, "md_pre");
-    k_md_pre<<<blocks, threads, smem, E.stream>>>(a, RRt, PPt, dRRt, RRc); ++E.nlaunch;
+    nm_launch_md_pre(a, E.stream, RRt, PPt, dRRt, RRc); ++E.nlaunch;
     timer_end(E);
     KP saved = E.kp;
     E.kp.RRt = RRt;
@@ -574,7 +810,7 @@ static int md_step_enqueue(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt,
     a.xi = xi2;
     a.phase = 1;
     timer_begin(E, "md_post");
-    k_md_post<<<blocks, threads, smem, E.stream>>>(a, PPt, dRRt, uk); ++E.nlaunch;
+    nm_launch_md_post(a, E.stream, PPt, dRRt, uk); ++E.nlaunch;
     if (out4) {
         k_md_sum<<<1, 32, 0, E.stream>>>(E.kp.P, d, d + E.kp.P, d + 2 * E.kp.P, uk, out4);
         ++E.nlaunch;

@@ -62,6 +62,29 @@ def test_md_steps_match_oracle(pkg, orc, engine_lib):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
+def test_md_steps_64_beads(pkg, orc, engine_lib, precision):
+    """Two steps at 64 beads (the integrator kernels' shared memory above 48 KB) against the
+    oracle: FP64 to the tolerances above; mixed to its force error (momenta 1e-5, positions
+    1e-9 relative)."""
+    c, p = md_setup(pkg, nw=8, P=64)
+    P, na = p["nbeads"], p["natoms"]
+    eng, mp = make_engine(pkg, c, p, precision=precision)
+    o = orc.Oracle(p)
+    md = dict(delt=0.25e-3, massO=c["massO"], massH=c["massH"], temp=300.0, langevin=1)
+    R1, P1, g1 = c["RRt"].copy(), c["PPt"].copy(), np.zeros_like(c["RRt"])
+    R2, P2, g2 = c["RRt"].copy(), c["PPt"].copy(), np.zeros_like(c["RRt"])
+    rng = np.random.default_rng(64)
+    for t in range(1, 3):
+        x1, x2 = rng.standard_normal((na, P, 3)), rng.standard_normal((na, P, 3))
+        out, RRc = eng.md_step(mp, R1, P1, g1, t, xi1=x1, xi2=x2)
+        orc.pimd_vv_step(o, md, R2, P2, g2, x1, x2, t=t)
+    tolR, tolP = (1e-12, 1e-9) if precision == 0 else (1e-9, 1e-5)
+    assert rel(R1, R2) < tolR
+    assert rel(P1, P2) < tolP
+    eng.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
 def test_graph_step_matches_eager(pkg, engine_lib, precision):
     """Eight steps as a replayed CUDA graph (device Langevin draws, predictor, dipole loop as a
     conditional node) equal eight eager steps from the same state; the graph is captured once."""
