@@ -155,17 +155,31 @@ PIMD_D void nasa_pot(const double r1[3][3], const double box[3], const double bo
     const double reoh = PIMD_NASA_REOH, b1 = PIMD_NASA_B1, roh = PIMD_NASA_ROH, alphaoh = PIMD_NASA_ALPHAOH,
                  phh2 = PIMD_NASA_PHH2;
     const double deoh = f5z * PIMD_NASA_DEOHA;
-    const double phh1 = (f5z * PIMD_NASA_PHH1A) * exp(phh2);
     const double costhe = -.24780227221366464506;
-    const double exp1 = exp(-alphaoh * (dROH1 - roh));
-    const double exp2 = exp(-alphaoh * (dROH2 - roh));
-    const double Va = deoh * (exp1 * (exp1 - 2.0) + exp2 * (exp2 - 2.0));
-    const double Vb = phh1 * exp(-phh2 * dRHH);
-    const double dVa1 = 2.0 * alphaoh * deoh * exp1 * (1.0 - exp1) / dROH1;
-    const double dVa2 = 2.0 * alphaoh * deoh * exp2 * (1.0 - exp2) / dROH2;
+    // fsum: the exponentials in FP32 as well (the FP64 ones dominate this part's FP64 work); the
+    // Morse terms from em = e^x - 1 (expm1f), which keeps 1 - e^x at FP32 relative precision
+    // where it cancels near the equilibrium bond length
+    const bool fx = fsum && !c5zg;
+    const double phh1 = (f5z * PIMD_NASA_PHH1A) * (fx ? (double)expf((float)phh2) : exp(phh2));
+    double Va, dVa1, dVa2;
+    if (fx) {
+        const double em1 = (double)expm1f((float)(-alphaoh * (dROH1 - roh)));
+        const double em2 = (double)expm1f((float)(-alphaoh * (dROH2 - roh)));
+        Va = deoh * ((em1 * em1 - 1.0) + (em2 * em2 - 1.0));
+        dVa1 = -2.0 * alphaoh * deoh * (1.0 + em1) * em1 / dROH1;
+        dVa2 = -2.0 * alphaoh * deoh * (1.0 + em2) * em2 / dROH2;
+    } else {
+        const double exp1 = exp(-alphaoh * (dROH1 - roh));
+        const double exp2 = exp(-alphaoh * (dROH2 - roh));
+        Va = deoh * (exp1 * (exp1 - 2.0) + exp2 * (exp2 - 2.0));
+        dVa1 = 2.0 * alphaoh * deoh * exp1 * (1.0 - exp1) / dROH1;
+        dVa2 = 2.0 * alphaoh * deoh * exp2 * (1.0 - exp2) / dROH2;
+    }
+    const double Vb = phh1 * (fx ? (double)expf((float)(-phh2 * dRHH)) : exp(-phh2 * dRHH));
     const double dVb = -phh2 * Vb / dRHH;
     const double x1 = (dROH1 - reoh) / reoh, x2 = (dROH2 - reoh) / reoh, x3 = costh - costhe;
-    const double efac = exp(-b1 * ((dROH1 - reoh) * (dROH1 - reoh) + (dROH2 - reoh) * (dROH2 - reoh)));
+    const double earg = -b1 * ((dROH1 - reoh) * (dROH1 - reoh) + (dROH2 - reoh) * (dROH2 - reoh));
+    const double efac = fx ? (double)expf((float)earg) : exp(earg);
     double sum0, sum1, sum2, sum3;
     if (fsum && !c5zg)
         nasa_pot_sums<float>(x1, x2, x3, nullptr, sum0, sum1, sum2, sum3);
@@ -193,7 +207,7 @@ PIMD_D void nasa_pot(const double r1[3][3], const double box[3], const double bo
 PIMD_D void nasa_dms_finish(const double ROH1[3], const double ROH2[3], double dROH1, double dROH2, double costh,
                             double efac, double P1, double P2, double dp1dr1, double dp1dr2, double dp1dcabc,
                             double dp2dr1, double dp2dr2, double dp2dcabc, double PL1, double PL2, double dms1,
-                            double dms2, double dms3, double q3[3], double gradq[3][3][3]) {
+                            double dms2, double dms3, double q3[3], double gradq[3][3][3], bool fx = false) {
     const double reoh = PIMD_NASA_REOH, b1D = PIMD_NASA_B1D, a = PIMD_NASA_A, b = PIMD_NASA_B,
                  c0 = PIMD_NASA_C0, c1 = PIMD_NASA_C1, c2 = PIMD_NASA_C2;
     const double ath0 = 1.82400520401572996557, B2A = 0.529177249;
@@ -201,11 +215,16 @@ PIMD_D void nasa_dms_finish(const double ROH1[3], const double ROH2[3], double d
     dp1dr2 = dp1dr2 / reoh * B2A;
     dp2dr1 = dp2dr1 / reoh * B2A;
     dp2dr2 = dp2dr2 / reoh * B2A;
-    const double pw1 = pow(dROH1, b), pw2 = pow(dROH2, b);
+    // fx (the mixed engine): the powers and the angle in FP32 (FP64 pow is this part's largest
+    // FP64 cost); 1e-7 relative in the charges
+    const double pw1 = fx ? (double)powf((float)dROH1, (float)b) : pow(dROH1, b);
+    const double pw2 = fx ? (double)powf((float)dROH2, (float)b) : pow(dROH2, b);
+    const double pm1 = fx ? (double)powf((float)dROH1, (float)(b - 1)) : pow(dROH1, b - 1);
+    const double pm2 = fx ? (double)powf((float)dROH2, (float)(b - 1)) : pow(dROH2, b - 1);
     const double leg = c0 + PL1 * c1 + PL2 * c2;
     const double PC0 = a * (pw1 + pw2) * leg;
-    const double dpc0dr1 = a * (b * pow(dROH1, b - 1)) * leg * B2A * B2A;
-    const double dpc0dr2 = a * (b * pow(dROH2, b - 1)) * leg * B2A * B2A;
+    const double dpc0dr1 = a * (b * pm1) * leg * B2A * B2A;
+    const double dpc0dr2 = a * (b * pm2) * leg * B2A * B2A;
     const double dpc0dcabc = a * (pw1 + pw2) * (c1 + 0.5 * (6.0 * PL1) * c2) * B2A;
     const double defacdr1 = -2.0 * b1D * (dROH1 - reoh) * efac * B2A;
     const double defacdr2 = -2.0 * b1D * (dROH2 - reoh) * efac * B2A;
@@ -231,7 +250,7 @@ PIMD_D void nasa_dms_finish(const double ROH1[3], const double ROH2[3], double d
     double AxB2 = ROH1[0] * ROH2[1] - ROH1[1] * ROH2[0];
     const double dAxB = sqrt(AxB0 * AxB0 + AxB1 * AxB1 + AxB2 * AxB2);
     const double sinth = dAxB / (dROH1 * dROH2);
-    const double ang = atan2(sinth, costh);
+    const double ang = fx ? (double)atan2f((float)sinth, (float)costh) : atan2(sinth, costh);
     const double Q1 = dms1 * (dROH1 - dms2) + dms3 * (ang - ath0);
     const double Q2 = dms1 * (dROH2 - dms2) + dms3 * (ang - ath0);
     q3[0] = q3[0] - (Q1 + Q2);
@@ -319,7 +338,8 @@ PIMD_D void nasa_dms(const double r1[3][3], const double box[3], const double bo
     const double dROH1 = sqrt(ROH1[0] * ROH1[0] + ROH1[1] * ROH1[1] + ROH1[2] * ROH1[2]);
     const double dROH2 = sqrt(ROH2[0] * ROH2[0] + ROH2[1] * ROH2[1] + ROH2[2] * ROH2[2]);
     const double costh = (ROH1[0] * ROH2[0] + ROH1[1] * ROH2[1] + ROH1[2] * ROH2[2]) / (dROH1 * dROH2);
-    const double efac = exp(-b1D * ((dROH1 - reoh) * (dROH1 - reoh) + (dROH2 - reoh) * (dROH2 - reoh)));
+    const double earg = -b1D * ((dROH1 - reoh) * (dROH1 - reoh) + (dROH2 - reoh) * (dROH2 - reoh));
+    const double efac = fsum ? (double)expf((float)earg) : exp(earg);
     const double x1 = (dROH1 - reoh) / reoh, x2 = (dROH2 - reoh) / reoh, x3 = costh - costhe;
     const double PL1 = costh, PL2 = 0.5 * (3.0 * PL1 * PL1 - 1.0);
     double sums[8];
@@ -330,7 +350,7 @@ PIMD_D void nasa_dms(const double r1[3][3], const double box[3], const double bo
     const double P1 = sums[0], P2 = sums[1], dp1dr1 = sums[2], dp1dr2 = sums[3], dp1dcabc = sums[4], dp2dr1 = sums[5],
                  dp2dr2 = sums[6], dp2dcabc = sums[7];
     nasa_dms_finish(ROH1, ROH2, dROH1, dROH2, costh, efac, P1, P2, dp1dr1, dp1dr2, dp1dcabc, dp2dr1, dp2dr2, dp2dcabc,
-                    PL1, PL2, dms1, dms2, dms3, q3, gradq);
+                    PL1, PL2, dms1, dms2, dms3, q3, gradq, fsum);
 }
 
 }  // namespace pimd

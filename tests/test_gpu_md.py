@@ -65,7 +65,7 @@ def test_md_steps_match_oracle(pkg, orc, engine_lib):
 def test_md_steps_64_beads(pkg, orc, engine_lib, precision):
     """Two steps at 64 beads (the integrator kernels' shared memory above 48 KB) against the
     oracle: FP64 to the tolerances above; mixed to its force error (momenta 1e-5, positions
-    1e-9 relative)."""
+    1e-8 relative: ~1e-5 relative force error moves an H atom by ~1e-8 A per step)."""
     c, p = md_setup(pkg, nw=8, P=64)
     P, na = p["nbeads"], p["natoms"]
     eng, mp = make_engine(pkg, c, p, precision=precision)
@@ -78,7 +78,7 @@ def test_md_steps_64_beads(pkg, orc, engine_lib, precision):
         x1, x2 = rng.standard_normal((na, P, 3)), rng.standard_normal((na, P, 3))
         out, RRc = eng.md_step(mp, R1, P1, g1, t, xi1=x1, xi2=x2)
         orc.pimd_vv_step(o, md, R2, P2, g2, x1, x2, t=t)
-    tolR, tolP = (1e-12, 1e-9) if precision == 0 else (1e-9, 1e-5)
+    tolR, tolP = (1e-12, 1e-9) if precision == 0 else (1e-8, 1e-5)
     assert rel(R1, R2) < tolR
     assert rel(P1, P2) < tolP
     eng.close()
