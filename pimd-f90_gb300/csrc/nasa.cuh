@@ -97,6 +97,10 @@ static inline void nasa_upload_constants() {
 // k-sum is a polynomial in x3, evaluated by Horner together with its derivative (two FMAs per
 // term). S = float (the mixed engine, published coefficients only) keeps the rest of the
 // monomer in FP64: the sums carry about 1e-7 relative error into the gradient.
+// a / d, or with fx (the mixed engine) a times the reciprocal id computed once: FP64 division
+// costs this part a dozen FP64 instructions
+PIMD_D double qdiv(double a, double d, double id, bool fx) { return fx ? a * id : a / d; }
+
 template <typename S>
 PIMD_D void nasa_pot_sums(double x1d, double x2d, double x3d, const double *c5zg, double &s0d, double &s1d, double &s2d,
                           double &s3d) {
@@ -151,23 +155,25 @@ PIMD_D void nasa_pot(const double r1[3][3], const double box[3], const double bo
     const double dROH1 = sqrt(ROH1[0] * ROH1[0] + ROH1[1] * ROH1[1] + ROH1[2] * ROH1[2]);
     const double dROH2 = sqrt(ROH2[0] * ROH2[0] + ROH2[1] * ROH2[1] + ROH2[2] * ROH2[2]);
     const double dRHH = sqrt(RHH[0] * RHH[0] + RHH[1] * RHH[1] + RHH[2] * RHH[2]);
-    const double costh = (ROH1[0] * ROH2[0] + ROH1[1] * ROH2[1] + ROH1[2] * ROH2[2]) / (dROH1 * dROH2);
+    // fsum: the exponentials in FP32 as well (the FP64 ones dominate this part's FP64 work); the
+    // Morse terms from em = e^x - 1 (expm1f), which keeps 1 - e^x at FP32 relative precision
+    // where it cancels near the equilibrium bond length; divisions by reciprocals
+    const bool fx = fsum && !c5zg;
+    const double i1 = fx ? 1.0 / dROH1 : 0.0, i2 = fx ? 1.0 / dROH2 : 0.0, ihh = fx ? 1.0 / dRHH : 0.0;
+    const double i12 = i1 * i2, ireoh = 1.0 / PIMD_NASA_REOH;
+    const double costh = qdiv(ROH1[0] * ROH2[0] + ROH1[1] * ROH2[1] + ROH1[2] * ROH2[2], dROH1 * dROH2, i12, fx);
     const double reoh = PIMD_NASA_REOH, b1 = PIMD_NASA_B1, roh = PIMD_NASA_ROH, alphaoh = PIMD_NASA_ALPHAOH,
                  phh2 = PIMD_NASA_PHH2;
     const double deoh = f5z * PIMD_NASA_DEOHA;
     const double costhe = -.24780227221366464506;
-    // fsum: the exponentials in FP32 as well (the FP64 ones dominate this part's FP64 work); the
-    // Morse terms from em = e^x - 1 (expm1f), which keeps 1 - e^x at FP32 relative precision
-    // where it cancels near the equilibrium bond length
-    const bool fx = fsum && !c5zg;
     const double phh1 = (f5z * PIMD_NASA_PHH1A) * (fx ? (double)expf((float)phh2) : exp(phh2));
     double Va, dVa1, dVa2;
     if (fx) {
         const double em1 = (double)expm1f((float)(-alphaoh * (dROH1 - roh)));
         const double em2 = (double)expm1f((float)(-alphaoh * (dROH2 - roh)));
         Va = deoh * ((em1 * em1 - 1.0) + (em2 * em2 - 1.0));
-        dVa1 = -2.0 * alphaoh * deoh * (1.0 + em1) * em1 / dROH1;
-        dVa2 = -2.0 * alphaoh * deoh * (1.0 + em2) * em2 / dROH2;
+        dVa1 = -2.0 * alphaoh * deoh * (1.0 + em1) * em1 * i1;
+        dVa2 = -2.0 * alphaoh * deoh * (1.0 + em2) * em2 * i2;
     } else {
         const double exp1 = exp(-alphaoh * (dROH1 - roh));
         const double exp2 = exp(-alphaoh * (dROH2 - roh));
@@ -176,8 +182,8 @@ PIMD_D void nasa_pot(const double r1[3][3], const double box[3], const double bo
         dVa2 = 2.0 * alphaoh * deoh * exp2 * (1.0 - exp2) / dROH2;
     }
     const double Vb = phh1 * (fx ? (double)expf((float)(-phh2 * dRHH)) : exp(-phh2 * dRHH));
-    const double dVb = -phh2 * Vb / dRHH;
-    const double x1 = (dROH1 - reoh) / reoh, x2 = (dROH2 - reoh) / reoh, x3 = costh - costhe;
+    const double dVb = qdiv(-phh2 * Vb, dRHH, ihh, fx);
+    const double x1 = qdiv(dROH1 - reoh, reoh, ireoh, fx), x2 = qdiv(dROH2 - reoh, reoh, ireoh, fx), x3 = costh - costhe;
     const double earg = -b1 * ((dROH1 - reoh) * (dROH1 - reoh) + (dROH2 - reoh) * (dROH2 - reoh));
     const double efac = fx ? (double)expf((float)earg) : exp(earg);
     double sum0, sum1, sum2, sum3;
@@ -187,15 +193,15 @@ PIMD_D void nasa_pot(const double r1[3][3], const double box[3], const double bo
         nasa_pot_sums<double>(x1, x2, x3, c5zg, sum0, sum1, sum2, sum3);
     const double Vc = 2.0 * (c5zg ? c5zg[0] : c_c5z[0]) + efac * sum0;
     *e1 = ((Va + Vb + Vc) + 0.44739574026257) * 0.00285914375100642899;
-    const double dVcdr1 = (-2.0 * b1 * efac * (dROH1 - reoh) * sum0 + efac * sum1 / reoh) / dROH1;
-    const double dVcdr2 = (-2.0 * b1 * efac * (dROH2 - reoh) * sum0 + efac * sum2 / reoh) / dROH2;
+    const double dVcdr1 = qdiv(-2.0 * b1 * efac * (dROH1 - reoh) * sum0 + qdiv(efac * sum1, reoh, ireoh, fx), dROH1, i1, fx);
+    const double dVcdr2 = qdiv(-2.0 * b1 * efac * (dROH2 - reoh) * sum0 + qdiv(efac * sum2, reoh, ireoh, fx), dROH2, i2, fx);
     const double dVcdcth = efac * sum3;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         double g1 = dVa1 * ROH1[c] + dVb * RHH[c] + dVcdr1 * ROH1[c] +
-                    dVcdcth * (ROH2[c] / (dROH1 * dROH2) - costh * ROH1[c] / (dROH1 * dROH1));
+                    dVcdcth * (qdiv(ROH2[c], dROH1 * dROH2, i12, fx) - qdiv(costh * ROH1[c], dROH1 * dROH1, i1 * i1, fx));
         double g2 = dVa2 * ROH2[c] - dVb * RHH[c] + dVcdr2 * ROH2[c] +
-                    dVcdcth * (ROH1[c] / (dROH1 * dROH2) - costh * ROH2[c] / (dROH2 * dROH2));
+                    dVcdcth * (qdiv(ROH1[c], dROH1 * dROH2, i12, fx) - qdiv(costh * ROH2[c], dROH2 * dROH2, i2 * i2, fx));
         dr1[1][c] = g1 * .00285914375100642899;
         dr1[2][c] = g2 * .00285914375100642899;
         dr1[0][c] = -(g1 + g2) * .00285914375100642899;
@@ -211,10 +217,12 @@ PIMD_D void nasa_dms_finish(const double ROH1[3], const double ROH2[3], double d
     const double reoh = PIMD_NASA_REOH, b1D = PIMD_NASA_B1D, a = PIMD_NASA_A, b = PIMD_NASA_B,
                  c0 = PIMD_NASA_C0, c1 = PIMD_NASA_C1, c2 = PIMD_NASA_C2;
     const double ath0 = 1.82400520401572996557, B2A = 0.529177249;
-    dp1dr1 = dp1dr1 / reoh * B2A;
-    dp1dr2 = dp1dr2 / reoh * B2A;
-    dp2dr1 = dp2dr1 / reoh * B2A;
-    dp2dr2 = dp2dr2 / reoh * B2A;
+    const double ireoh = 1.0 / PIMD_NASA_REOH;
+    const double i1 = fx ? 1.0 / dROH1 : 0.0, i2 = fx ? 1.0 / dROH2 : 0.0, i12 = i1 * i2;
+    dp1dr1 = qdiv(dp1dr1, reoh, ireoh, fx) * B2A;
+    dp1dr2 = qdiv(dp1dr2, reoh, ireoh, fx) * B2A;
+    dp2dr1 = qdiv(dp2dr1, reoh, ireoh, fx) * B2A;
+    dp2dr2 = qdiv(dp2dr2, reoh, ireoh, fx) * B2A;
     // fx (the mixed engine): the powers and the angle in FP32 (FP64 pow is this part's largest
     // FP64 cost); 1e-7 relative in the charges
     const double pw1 = fx ? (double)powf((float)dROH1, (float)b) : pow(dROH1, b);
@@ -249,7 +257,7 @@ PIMD_D void nasa_dms_finish(const double ROH1[3], const double ROH2[3], double d
     double AxB1 = -ROH1[0] * ROH2[2] + ROH1[2] * ROH2[0];
     double AxB2 = ROH1[0] * ROH2[1] - ROH1[1] * ROH2[0];
     const double dAxB = sqrt(AxB0 * AxB0 + AxB1 * AxB1 + AxB2 * AxB2);
-    const double sinth = dAxB / (dROH1 * dROH2);
+    const double sinth = qdiv(dAxB, dROH1 * dROH2, i12, fx);
     const double ang = fx ? (double)atan2f((float)sinth, (float)costh) : atan2(sinth, costh);
     const double Q1 = dms1 * (dROH1 - dms2) + dms3 * (ang - ath0);
     const double Q2 = dms1 * (dROH2 - dms2) + dms3 * (ang - ath0);
@@ -258,16 +266,17 @@ PIMD_D void nasa_dms_finish(const double ROH1[3], const double ROH2[3], double d
     q3[2] = q3[2] + Q2;
     dp1dr1 += dms1;
     dp2dr2 += dms1;
-    dp1dcabc -= dms3 / sinth;
-    dp2dcabc -= dms3 / sinth;
-    const double f1q1r13 = (dp1dr1 - (dp1dcabc * costh / dROH1)) / dROH1;
-    const double f1q1r23 = dp1dcabc / (dROH1 * dROH2);
-    const double f2q1r23 = (dp1dr2 - (dp1dcabc * costh / dROH2)) / dROH2;
-    const double f2q1r13 = dp1dcabc / (dROH2 * dROH1);
-    const double f1q2r13 = (dp2dr1 - (dp2dcabc * costh / dROH1)) / dROH1;
-    const double f1q2r23 = dp2dcabc / (dROH1 * dROH2);
-    const double f2q2r23 = (dp2dr2 - (dp2dcabc * costh / dROH2)) / dROH2;
-    const double f2q2r13 = dp2dcabc / (dROH2 * dROH1);
+    const double ds = fx ? dms3 / sinth : 0.0;
+    dp1dcabc -= fx ? ds : dms3 / sinth;
+    dp2dcabc -= fx ? ds : dms3 / sinth;
+    const double f1q1r13 = qdiv(dp1dr1 - qdiv(dp1dcabc * costh, dROH1, i1, fx), dROH1, i1, fx);
+    const double f1q1r23 = qdiv(dp1dcabc, dROH1 * dROH2, i12, fx);
+    const double f2q1r23 = qdiv(dp1dr2 - qdiv(dp1dcabc * costh, dROH2, i2, fx), dROH2, i2, fx);
+    const double f2q1r13 = qdiv(dp1dcabc, dROH2 * dROH1, i12, fx);
+    const double f1q2r13 = qdiv(dp2dr1 - qdiv(dp2dcabc * costh, dROH1, i1, fx), dROH1, i1, fx);
+    const double f1q2r23 = qdiv(dp2dcabc, dROH1 * dROH2, i12, fx);
+    const double f2q2r23 = qdiv(dp2dr2 - qdiv(dp2dcabc * costh, dROH2, i2, fx), dROH2, i2, fx);
+    const double f2q2r13 = qdiv(dp2dcabc, dROH2 * dROH1, i12, fx);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         gradq[0][0][c] = f1q1r13 * ROH1[c] + f1q1r23 * ROH2[c];
@@ -340,7 +349,8 @@ PIMD_D void nasa_dms(const double r1[3][3], const double box[3], const double bo
     const double costh = (ROH1[0] * ROH2[0] + ROH1[1] * ROH2[1] + ROH1[2] * ROH2[2]) / (dROH1 * dROH2);
     const double earg = -b1D * ((dROH1 - reoh) * (dROH1 - reoh) + (dROH2 - reoh) * (dROH2 - reoh));
     const double efac = fsum ? (double)expf((float)earg) : exp(earg);
-    const double x1 = (dROH1 - reoh) / reoh, x2 = (dROH2 - reoh) / reoh, x3 = costh - costhe;
+    const double ireoh = 1.0 / PIMD_NASA_REOH;
+    const double x1 = qdiv(dROH1 - reoh, reoh, ireoh, fsum), x2 = qdiv(dROH2 - reoh, reoh, ireoh, fsum), x3 = costh - costhe;
     const double PL1 = costh, PL2 = 0.5 * (3.0 * PL1 * PL1 - 1.0);
     double sums[8];
     if (fsum)
