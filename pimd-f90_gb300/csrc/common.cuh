@@ -204,6 +204,19 @@ PIMD_D void self1(double drsq, const EwC &e, double *ts0, double *ts1) {
     *ts1 = kr1 + ch1;
 }
 
+// self1 in FP32 (the mixed engine; the A&S erfc and the exponential as in smear2<float>): ts0
+// to ~1e-7 and ts1 to ~1e-6 relative (ts1 cancels by about (a r)^2 at intramolecular r)
+PIMD_D void self1f(float drsq, const EwCf &e, float *ts0, float *ts1) {
+    float dd, dri;
+    rinv<float>(drsq, dd, dri);
+    const float drsqi = dri * dri;
+    const float expon = exp_p(-(e.a2 * drsq));
+    const float kr0 = erfc_as<float>(e.aewald * dd) * dri;
+    const float kr1 = (kr0 + e.cts1 * expon) * drsqi;
+    *ts0 = kr0 - dri;
+    *ts1 = kr1 - dri * drsqi;
+}
+
 // smear.f90:133-156 self2
 PIMD_D void self2(double drsq, const EwC &e, double *ts1, double *ts2) {
     double dd = sqrt(drsq);

@@ -160,7 +160,16 @@ __global__ void __launch_bounds__(SITES_NT) k_sites(KP kp) {
                         Rcs[c] = min_image_rn(__dsub_rn(Rc[i][c], Rc[j][c]), kp.box[c], kp.boxi[c]);
                     }
                     double ts0, ts1;
-                    self1(dot3_rn(Rs[0], Rs[1], Rs[2]), kp.ew, &ts0, &ts1);
+                    // the mixed engine, TTM3-F: the exclusion's erfc and exponential in FP32 (TTM2.1-F's
+                    // polarisable H sites take the exclusion field into the dipoles: FP64 there)
+                    if (FSUM && MODEL == 3) {
+                        float f0, f1;
+                        self1f((float)dot3_rn(Rs[0], Rs[1], Rs[2]), kp.ewf, &f0, &f1);
+                        ts0 = f0;
+                        ts1 = f1;
+                    } else {
+                        self1(dot3_rn(Rs[0], Rs[1], Rs[2]), kp.ew, &ts0, &ts1);
+                    }
                     ph[i] += ts0 * q[j];
                     ph[j] += ts0 * q[i];
                     double d[3];
