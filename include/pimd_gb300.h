@@ -58,7 +58,7 @@ typedef struct {
 
 typedef struct pimd_ctx pimd_ctx;
 
-/* init_pot (pot_ttm/potential.f90:129-285) + ewald_set(.true.) (pot_ttm/ewald.f90:293). */
+/* init_pot (pot_ttm/potential.f90:43-199) + ewald_set(.true.) (pot_ttm/ewald.f90:293). */
 int pimd_create(pimd_ctx **ctx, const pimd_params *p);
 int pimd_destroy(pimd_ctx *ctx);
 /* Run all work of the context on this cudaStream_t (NULL = the context's own stream). */
@@ -99,7 +99,7 @@ int pimd_get_virial(pimd_ctx *ctx, int bead, double virt[9]);
 int pimd_get_dipole_info(pimd_ctx *ctx, int bead, int *niter, double *deltadip);
 
 /* The half neighbour list of bead `bead` from the last force call: O-O pairs (i, j), 0-based,
- * i < j, in find_neigh's order (find_neigh.f90:232-274). Writes min(npairs, cap) pairs to
+ * i < j, in find_neigh's order (find_neigh.f90:75-117). Writes min(npairs, cap) pairs to
  * ij[2*cap] and the total to *npairs. */
 int pimd_get_neighbors(pimd_ctx *ctx, int bead, int *ij, int cap, int *npairs);
 
@@ -272,6 +272,39 @@ int pimd_batch_autotune(pimd_batch *bt);
 int pimd_batch_step(pimd_batch *bt, int nsteps);
 int pimd_batch_sync(pimd_batch *bt);
 
+/* ---------------------------------------------------------------------------------------
+ * Configuration and checkpoint files (InputOutput.f90), host only: no context, no device work.
+ * Arrays as elsewhere: RRc(3,Natoms), RRt/PPt(3,Natoms,Nbeads) column-major, atoms O H H ...
+ */
+/* Header of a configuration file (read_and_initialize_all_nodes, InputOutput.f90:67-116).
+ * ".img": '(2i10)' Natoms, Nbeads and '(f12.6,2x,f12.6,3(1x,f12.6))' time, box. ".xyz": box and
+ * atom count as a box record then the count, the count then a box record, or the count and the
+ * box on one record (*nbeads = 0, *time = 0). nbeads and time may be NULL. PIMD_ERR_ARG for a
+ * missing file, another suffix, or a malformed header. */
+int pimd_read_config_header(const char *path, int *natoms, int *nbeads, double *time, double *box);
+/* The coordinate records of an ".xyz" file (read_coords_and_init, InputOutput.f90:422-446):
+ * read_method 0 (all O, then the H pairs) or 1 (O H H ...); with read_method 1 the coordinates
+ * are shifted by their mean, as the reference does. natoms must equal the header's. */
+int pimd_read_xyz(const char *path, int read_method, int natoms, double *RRc);
+/* save_XYZ (InputOutput.f90:948-981): one frame, '(i10)' Natoms, a blank record, then
+ * '(a2,3(1x,f12.6))' per atom; append != 0 adds it to the end of the file. */
+int pimd_write_xyz(const char *path, int append, int natoms, const double *RR);
+/* save_checkpoint (InputOutput.f90:987-1024): the ".img" image of the ring polymers (velocities
+ * PPt/mass written), then, if n_vxi_beads != 0, the bead Nose-Hoover chain velocities
+ * vxi_beads(2,Natoms,Nbeads,3) (n_vxi_beads = 6 Natoms Nbeads), and, if n_vxi_global != 0, the
+ * global chain velocities; time = t*delt + init_time. */
+int pimd_save_image(const char *path, int natoms, int nbeads, double time, const double *box,
+                    const double *RRt, const double *PPt, double massO, double massH,
+                    const double *vxi_beads, int n_vxi_beads, const double *vxi_global,
+                    int n_vxi_global);
+/* load_checkpoint with its header (InputOutput.f90:86-96, 1030-1074): RRt, PPt (velocities times
+ * the masses), the chain velocities when asked for, then the centroid RRc (may be NULL) and the
+ * centroid-following PBC shift of main_stuff.f90:107-125. Natoms and Nbeads must match the
+ * header's (else PIMD_ERR_ARG, as the reference's abort at InputOutput.f90:90-94). */
+int pimd_load_image(const char *path, int natoms, int nbeads, double massO, double massH,
+                    double *time, double *box, double *RRt, double *PPt, double *RRc,
+                    double *vxi_beads, int n_vxi_beads, double *vxi_global, int n_vxi_global);
+
 /* O-O half neighbour list of one bead without any device allocation. No counterpart in the
  * reference; it serves callers that must not let a library allocate device memory (drivers
  * that own all GPU memory through their own pool, applications with a fixed per-GPU budget,
@@ -281,7 +314,11 @@ int pimd_batch_sync(pimd_batch *bt);
  * to pimd_get_neighbors; *npairs (device int) = total pairs found, which may exceed cap (then
  * only the first cap pairs are written). Stream-ordered on cuda_stream (NULL = default stream);
  * allocates nothing and does not synchronise.
- * Limit: Natoms/3 <= 16384 molecules; larger inputs return PIMD_ERR_ARG with a message.
+ * Limit: Natoms/3 <= 16384 molecules; larger inputs, and a box edge that is not a finite
+ * positive length, return PIMD_ERR_ARG with a message. cuda_stream must belong to the current
+ * device (else PIMD_ERR_ARG). Cost: an all-pairs FP64 test run twice (count, then fill), one
+ * thread per molecule: about 1.3e8 distance tests per pass at the 16384-molecule limit, far
+ * slower than the context's neighbour step, which it is not meant to replace.
  * Its per-molecule counts and offsets live in one fixed 128 KB device array per GPU that is
  * shared by every call and fully rewritten by each call; calls that overlap on the GPU (two
  * streams, or two host threads) race on it. The first call on a device looks up the array's

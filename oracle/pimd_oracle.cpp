@@ -161,7 +161,7 @@ struct Orc {
                  double *chg);
 };
 
-// potential.f90:129-285 init_pot
+// potential.f90:43-199 init_pot
 Orc::Orc(const orc_params *pp) : p(*pp) {
     Natoms = p.natoms;
     N = Natoms / 3;
@@ -187,7 +187,7 @@ Orc::Orc(const orc_params *pp) : p(*pp) {
             shiftA = 0;
             shiftB = 0;
         } else {
-            // potential.f90:197-198 (integer powers as repeated products)
+            // potential.f90:106-113 (integer powers as repeated products)
             double rc8 = rc * rc * rc * rc * rc * rc * rc * rc;
             shiftA = -(10 * rc - 7 * rc1) / (rc8 * ((rc - rc1) * (rc - rc1)));
             shiftB = (9 * rc - 7 * rc1) / (rc8 * ((rc - rc1) * (rc - rc1) * (rc - rc1)));
@@ -240,7 +240,7 @@ Orc::Orc(const orc_params *pp) : p(*pp) {
     grdq.assign(27 * N, 0.0);
     int nslots = p.shared_history ? 1 : std::max(1, p.nbeads);
     tx_dip.assign((size_t)nslots * 4 * 3 * NM, 0.0);
-    if (!polar) {  // potential.f90:272-278
+    if (!polar) {  // potential.f90:186-192
         for (int iw = 0; iw < N; iw++) {
             charge[iw] = qO * CHARGECON;
             charge[iw + N] = qH * CHARGECON;
@@ -546,7 +546,7 @@ void Orc::ewald_pw_std_qq() {
     }
 }
 
-// find_neigh.f90:171-277: all j > iO within Rc (strict), anint min-image, ascending j
+// find_neigh.f90:14-120: all j > iO within Rc (strict), anint min-image, ascending j
 void Orc::find_neigh(int iO, std::vector<int> &nj, std::vector<double> &nR, std::vector<double> &nR2) {
     nj.clear();
     nR.clear();
@@ -1698,7 +1698,7 @@ void orc_pot_spc(void *h, const double *RR, double *En, double *dRR, double *vir
     static_cast<Orc *>(h)->pot_spc(RR, En, dRR, virt, dip_momI, chg);
 }
 
-// find_neigh.f90:171-277 for every molecule: (i, j) pairs in the reference's order
+// find_neigh.f90:14-120 for every molecule: (i, j) pairs in the reference's order
 int orc_neighbors(void *h, const double *RR, int *ij, int cap) {
     Orc *o = static_cast<Orc *>(h);
     for (int iw = 0; iw < o->N; iw++)

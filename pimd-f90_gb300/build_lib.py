@@ -1,6 +1,6 @@
 """Build libpimd_gb300.so (the C-ABI force engine) in-tree with nvcc for sm_103a.
 
-Each .cu translation unit is compiled in parallel, then linked into one shared library at
+Each translation unit (.cu, and the host-only .cpp) is compiled in parallel, then linked into one shared library at
 pimd-f90_gb300/_build/libpimd_gb300.so. Host code is compiled without floating-point
 contraction (-ffp-contract=off) so host-side set-up (k-vectors, normal-mode matrices) rounds
 the same way on x86-64 and aarch64.
@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpimd_gb300.so")
-SOURCES = ["capi.cu", "neighbors.cu", "pot.cu", "ewald.cu", "mixed.cu", "nm.cu", "peak.cu", "noalloc.cu", "spc.cu", "md_batch.cu", "adjoint.cu", "ewald_tc.cu"]
+SOURCES = ["capi.cu", "neighbors.cu", "pot.cu", "ewald.cu", "mixed.cu", "nm.cu", "peak.cu", "noalloc.cu", "spc.cu",
+           "md_batch.cu", "adjoint.cu", "ewald_tc.cu", "state_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -45,7 +46,7 @@ def build(force=False, verbose=False):
     jobs = []
     for s in SOURCES:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(OUT, s.replace(".cu", ".o"))
+        obj = os.path.join(OUT, os.path.splitext(s)[0] + ".o")
         if force or _stale(obj, src):
             jobs.append([nv] + _flags() + ["-c", src, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
@@ -55,7 +56,7 @@ def build(force=False, verbose=False):
             raise RuntimeError("nvcc failed: %s\n%s%s" % (" ".join(c), r.stdout, r.stderr))
         if verbose and (r.stdout or r.stderr):
             print(r.stdout, r.stderr)
-    objs = [os.path.join(OUT, s.replace(".cu", ".o")) for s in SOURCES]
+    objs = [os.path.join(OUT, os.path.splitext(s)[0] + ".o") for s in SOURCES]
     if force or jobs or not os.path.exists(LIB):
         link = [nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
         r = subprocess.run(link, capture_output=True, text=True)

@@ -243,7 +243,7 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
     kp.polar[4] = m.polarM;
     kp.same_acd = std::fabs(m.aCCaCD - m.aDD) < 1.e-12 ? 1 : 0;
     if (p->pot_model == 3 && p->rc != p->rc1) {
-        // potential.f90:197-198 GROMACS-style vdW force switch
+        // potential.f90:106-113 GROMACS-style vdW force switch
         const double Rc = p->rc, r1 = p->rc1;
         const double rc8 = Rc * Rc * Rc * Rc * Rc * Rc * Rc * Rc;
         kp.shiftA = -(10 * Rc - 7 * r1) / (rc8 * ((Rc - r1) * (Rc - r1)));
@@ -268,11 +268,11 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
         kp.ld = 4 * kp.N;
         kp.ndd = 1;
     }
-    {  // potential.f90:238-239 long-range vdW correction
+    {  // potential.f90:152-154 long-range vdW correction
         const double Rc = p->rc, r3 = Rc * Rc * Rc, r7 = r3 * r3 * Rc, r9 = r7 * Rc * Rc;
         kp.Uvdw_lrc = TWOPI * (double)(kp.N * kp.N) / kp.volume * (m.vdwA / (9.0 * r9) + m.vdwB / (7.0 * r7) + m.vdwC / (3.0 * r3));
     }
-    // potential.f90:244-245 polfac = polfac^(-1/2) by way of the sixth root
+    // potential.f90:157-160 polfac = polfac^(-1/2) by way of the sixth root
     double pf[5];
     const double base[5] = {0, m.polfacO, m.polfacH, m.polfacH, m.polfacM};
     for (int i = 1; i <= 4; i++) {

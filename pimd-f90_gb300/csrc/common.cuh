@@ -23,7 +23,7 @@ constexpr double HBAR = 6.35077993041;
 // ---------------------------------------------------------------------------------------
 // Minimum image exactly as the reference: r - box*anint(r*boxi), each product and
 // difference rounded separately (no FMA), anint = round half away from zero.
-// find_neigh.f90:234, pot_ttm.f90:64 etc.
+// find_neigh.f90:77, pot_ttm.f90:64 etc.
 PIMD_D double min_image_rn(double r, double box, double boxi) {
     return __dsub_rn(r, __dmul_rn(box, round(__dmul_rn(r, boxi))));
 }
@@ -87,7 +87,7 @@ PIMD_D R gammq2_3(R x, unsigned *err) {
     return R(0);
 }
 
-// Ewald constants shared by the smear kernels (potential.f90:282-284)
+// Ewald constants shared by the smear kernels (potential.f90:196-198)
 struct EwC {
     double aewald, a2, cts1, cts2, cts3;
 };

@@ -267,7 +267,7 @@ struct Engine {
     double *d_adj = nullptr;     // backward scratch
     size_t adj_bytes = 0;
     bool tape_valid = false;
-    double polfac[5] = {0, 0, 0, 0, 0};  // polfac^(-1/2) per site kind (potential.f90:244-245)
+    double polfac[5] = {0, 0, 0, 0, 0};  // polfac^(-1/2) per site kind (potential.f90:157-160)
     double vdwA_model = 0, vdwB_model = 0, rc = 0;
     // normal modes (filled by pimd_nm_init)
     int nm_P = 0;

@@ -1,4 +1,4 @@
-// neighbors.cu -- O-O neighbour lists of all beads (find_neigh.f90:171-277).
+// neighbors.cu -- O-O neighbour lists of all beads (find_neigh.f90:14-120).
 //
 // For molecule i the reference keeps every j > i with |R_Oi - R_Oj|^2 < Rc^2 under the anint
 // minimum image, in ascending j. Here one warp owns one (molecule, bead): its lanes test 32

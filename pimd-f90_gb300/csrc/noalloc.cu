@@ -4,9 +4,10 @@
 // device memory through its own pool, a host application that forbids allocations after
 // start-up (a fixed memory budget per GPU), and code that records CUDA graphs, where
 // cudaMalloc is not a stream operation. For them this entry point builds the same list as the
-// engine's neighbour step (find_neigh.f90:171-277, bit-identical) from caller-owned input and
+// engine's neighbour step (find_neigh.f90:14-120, bit-identical) from caller-owned input and
 // output buffers, and keeps its per-molecule counts and offsets in a fixed file-scope device
 // array. That array exists once per GPU that loads the library and lives until exit.
+#include <cmath>
 #include <cstdio>
 #include <mutex>
 
@@ -110,10 +111,31 @@ using namespace pimd;
 extern "C" int pimd_neighbors_noalloc(const double *RR, int natoms, const double *box, double rc, int *ij, int cap,
                                       int *npairs, void *cuda_stream) {
     if (!RR || !box || !ij || !npairs || natoms <= 0 || natoms % 3 || cap < 0 || !(rc > 0)) return PIMD_ERR_ARG;
+    for (int c = 0; c < 3; c++)
+        if (!std::isfinite(box[c]) || !(box[c] > 0)) {
+            fprintf(stderr, "pimd_neighbors_noalloc: box[%d] = %g is not a finite positive length\n", c, box[c]);
+            return PIMD_ERR_ARG;
+        }
     const int N = natoms / 3;
     if (N > NOALLOC_MAXN) {
         fprintf(stderr, "pimd_neighbors_noalloc: %d molecules exceed the static scratch limit of %d molecules\n", N,
                 NOALLOC_MAXN);
+        return PIMD_ERR_ARG;
+    }
+    // an error left pending by earlier, unrelated work is reported as such (and left for its
+    // owner to read), so it is not mistaken for a failure of these launches
+    const cudaError_t prior = cudaPeekAtLastError();
+    if (prior != cudaSuccess) {
+        fprintf(stderr, "pimd_neighbors_noalloc: a CUDA error from earlier work is pending: %s\n",
+                cudaGetErrorString(prior));
+        return PIMD_ERR_CUDA;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    int cur = -1, sdev = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cudaStreamGetDevice(s, &sdev) != cudaSuccess) return PIMD_ERR_CUDA;
+    if (sdev != cur) {
+        fprintf(stderr, "pimd_neighbors_noalloc: the stream belongs to device %d, the current device is %d\n", sdev,
+                cur);
         return PIMD_ERR_ARG;
     }
     int rc_ = PIMD_OK;
@@ -131,7 +153,6 @@ extern "C" int pimd_neighbors_noalloc(const double *RR, int natoms, const double
     x.scratch = scratch;
     x.ij = reinterpret_cast<int2 *>(ij);
     x.npairs = npairs;
-    cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
     const int blocks = (N + 127) / 128;
     k_na_count<<<blocks, 128, 0, s>>>(x);
     k_na_scan<<<1, 1024, 0, s>>>(x);

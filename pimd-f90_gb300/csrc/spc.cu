@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(128) k_pair_spc(KP kp) {
             si[k] = pos[k * N + i];
             sj[k] = pos[k * N + j];
         }
-        // find_neigh.f90:234-236: the O-O separation and its square as stored in the list
+        // find_neigh.f90:76-109: the O-O separation and its square as stored in the list
         double Rij[3];
         Rij[0] = min_image_rn(__dsub_rn(si[0].x, sj[0].x), kp.box[0], kp.boxi[0]);
         Rij[1] = min_image_rn(__dsub_rn(si[0].y, sj[0].y), kp.box[1], kp.boxi[1]);

@@ -74,6 +74,13 @@ SIGNATURES = {
                                 ctypes.c_ulonglong],
     "pimd_md_step_device": [_V, ctypes.POINTER(MDParams), _V, _V, _V, _V, _V, _V, ctypes.c_int, _V],
     "pimd_md_step": [_V, ctypes.POINTER(MDParams), _D, _D, _D, _D, _D, _D, ctypes.c_int, _D],
+    "pimd_read_config_header": [ctypes.c_char_p, _I, _I, _D, _D],
+    "pimd_read_xyz": [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _D],
+    "pimd_write_xyz": [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _D],
+    "pimd_save_image": [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, _D, _D, _D, ctypes.c_double,
+                        ctypes.c_double, _D, ctypes.c_int, _D, ctypes.c_int],
+    "pimd_load_image": [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, _D, _D, _D,
+                        _D, _D, _D, ctypes.c_int, _D, ctypes.c_int],
     "pimd_peak_flops": [ctypes.c_int, ctypes.c_int, _D],
     "pimd_set_graph": [_V, ctypes.c_int],
     "pimd_autotune": [_V, _V, _V],

@@ -70,30 +70,54 @@ def test_batch_matches_single_contexts(pkg, engine_lib):
     bt.close()
 
 
-def test_batch_uneven_mixed_precision_runs(pkg, engine_lib):
-    """Mixed-precision batch with four box sizes and three bead counts, autotuned, 5 steps:
-    finite energies and the expected grouping."""
+def rms_rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return np.sqrt(((a - b) ** 2).mean()) / np.sqrt((b ** 2).mean())
+
+
+def test_batch_uneven_mixed_matches_single_contexts(pkg, engine_lib):
+    """Mixed-precision batch with four box sizes and three bead counts, autotuned, 6 steps: each
+    replica against the same replica stepped alone in its own mixed-precision context (same
+    seed, temperature and cutoff). The two differ only by FP32 summation order (the batch's
+    tuned launch shapes, beads of several replicas per launch): gradient RMS error <= 1e-5
+    relative, positions and momenta 1e-6, energy 1e-6."""
+    W = pkg.waterbox
     specs = [(32, 8, 260.0), (64, 16, 300.0), (128, 32, 340.0), (256, 8, 280.0), (64, 8, 320.0)]
-    reps = []
-    bt_states = []
+    reps, states = [], []
     for i, (nw, P, T) in enumerate(specs):
         c = replica_state(pkg, nw, P, T, 200 + i)
         L = c["params"]["box"][0]
         reps.append(dict(natoms=3 * nw, nbeads=P, box=(L, L, L), temp=T))
-        bt_states.append(c)
-    bt = pkg.engine.ReplicaBatch(common_params(), reps, DELT, 15.9994, 1.008, seed=SEED,
-                                 precision=pkg.engine.PIMD_MIXED)
+        states.append(c)
+    common = common_params()
+    bt = pkg.engine.ReplicaBatch(common, reps, DELT, 15.9994, 1.008, seed=SEED, precision=pkg.engine.PIMD_MIXED)
     ng, gof = bt.groups()
     assert ng == 4 and gof[1] == gof[4]
-    for i, c in enumerate(bt_states):
+    for i, c in enumerate(states):
         bt.set_state(i, c["RRt"], c["PPt"])
     bt.autotune()
     bt.forces()
-    bt.step(5)
+    bt.step(6)
     bt.sync()
-    for i in range(len(reps)):
-        R, P, G, o = bt.get_state(i)
-        assert np.isfinite(R).all() and np.isfinite(G).all() and np.isfinite(o).all()
+    for i, (c, r) in enumerate(zip(states, reps)):
+        P, T, L = r["nbeads"], r["temp"], r["box"][0]
+        rc = min(9.0, L / 2)
+        p = dict(common, natoms=r["natoms"], nbeads=P, box=r["box"], rc=rc, rc1=rc * 0.8)
+        eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_MIXED)
+        eng.nm_init(P, W.KB_AMU * T * P / W.HBAR, DELT)
+        eng.langevin_init(DELT / 2, 0, 0.1, P * T)
+        mp = eng.md_params(DELT, 15.9994, 1.008, langevin=1, seed=SEED + i)
+        R, Pm = c["RRt"].copy(), c["PPt"].copy()
+        g = eng.full_bead_forces(R, R.mean(axis=0), t=0)["dRRt"]
+        for t in range(1, 7):
+            out, _ = eng.md_step(mp, R, Pm, g, t)
+        Rb, Pb, Gb, ob = bt.get_state(i)
+        assert np.isfinite(Rb).all() and np.isfinite(Gb).all() and np.isfinite(ob).all()
+        assert rms_rel(Gb, g) < 1e-5, i
+        assert rel(Rb, R) < 1e-6, i
+        assert rel(Pb, Pm) < 1e-6, i
+        assert abs(ob[0] - out[0]) < 1e-6 * abs(out[0]), i
+        eng.close()
     bt.close()
 
 

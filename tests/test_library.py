@@ -44,15 +44,18 @@ def test_engine_refuses_without_device_or_bad_args(pkg):
 
 def test_nasa_tables_match_reference_source():
     """nasa_tables.h is the mechanical extraction of pot_ttm/nasa_mod.f90 (checked only where
-    the reference source tree is present)."""
+    the reference source tree is present, named by the PIMD_REFERENCE_DIR environment variable)."""
     import subprocess
     import sys
 
-    src = "/root/reference/pot_ttm/nasa_mod.f90"
-    if not os.path.exists(src):
-        import pytest
+    import pytest
 
-        pytest.skip("reference source tree not present")
+    ref = os.environ.get("PIMD_REFERENCE_DIR")
+    if not ref:
+        pytest.skip("PIMD_REFERENCE_DIR (the reference source tree) is not set")
+    src = os.path.join(ref, "pot_ttm", "nasa_mod.f90")
+    if not os.path.exists(src):
+        pytest.skip("reference source tree not present at PIMD_REFERENCE_DIR")
     gen = os.path.join(ROOT, "pimd-f90_gb300", "csrc", "gen_nasa_tables.py")
     out = subprocess.run([sys.executable, gen, src], capture_output=True, text=True, check=True).stdout
     with open(os.path.join(ROOT, "pimd-f90_gb300", "csrc", "nasa_tables.h")) as f:

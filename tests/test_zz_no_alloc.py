@@ -38,6 +38,22 @@ def test_noalloc_neighbors_match_engine(pkg, engine_lib):
         ref = eng.neighbors(bead)
         assert int(n.item()) == len(ref)
         assert np.array_equal(ij[: len(ref)].cpu().numpy(), ref)
+    # a capacity below the pair count: the first cap pairs are written, nothing past them, and
+    # *npairs still reports the full total
+    small = len(ref) // 3
+    ij.fill_(-7)
+    torch.cuda.synchronize(dev)
+    free0 = torch.cuda.mem_get_info(dev)[0]
+    rc = L.pimd_neighbors_noalloc(RR.data_ptr(), p["natoms"], box, p["rc"], ij.data_ptr(), small, n.data_ptr(),
+                                  stream.cuda_stream)
+    assert rc == 0
+    torch.cuda.synchronize(dev)
+    assert int(n.item()) == len(ref)
+    got = ij.cpu().numpy()
+    assert np.array_equal(got[:small], ref[:small])
+    assert (got[small:] == -7).all()
+    # a warmed-up call takes no device memory (the free amount is unchanged)
+    assert torch.cuda.mem_get_info(dev)[0] == free0
     eng.close()
 
 
@@ -47,3 +63,11 @@ def test_noalloc_rejects_oversize(pkg, engine_lib):
     # 16385 molecules exceed the static scratch; rejected before any device access
     rc = L.pimd_neighbors_noalloc(1, 3 * 16385, box, 9.0, 1, 10, 1, None)
     assert rc == 1
+
+
+def test_noalloc_rejects_bad_box(pkg, engine_lib):
+    L = pkg.engine.load()
+    for bad in ((0.0, 10.0, 10.0), (10.0, float("nan"), 10.0), (10.0, 10.0, float("inf")), (-5.0, 10.0, 10.0)):
+        box = (ctypes.c_double * 3)(*bad)
+        # rejected on the host before any device access
+        assert L.pimd_neighbors_noalloc(1, 9, box, 3.0, 1, 10, 1, None) == 1
