@@ -350,7 +350,7 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
         if ((rc = dalloc(E, &kp.tabf, P * kp.ntab * S)) || (rc = dalloc(E, &kp.posf, P * S)) ||
             (rc = dalloc(E, &kp.rhof, P * S)) || (rc = dalloc(E, &kp.fcnt, P * N)) || (rc = dalloc(E, &kp.foff, P * N)) ||
             (rc = dalloc(E, &kp.fnbr, P * (size_t)kp.fcap * 2)) || (rc = dalloc(E, &kp.fntot, P)) ||
-            (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd * 6)) || (rc = dalloc(E, &kp.Wf, P * 2 * (size_t)kp.nk)) || (rc = dalloc(E, &kp.dipf, P * S)) ||
+            (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd)) || (rc = dalloc(E, &kp.fj, P * (size_t)kp.fcap)) || (rc = dalloc(E, &kp.Wf, P * 2 * (size_t)kp.nk)) || (rc = dalloc(E, &kp.dipf, P * S)) ||
             (rc = dalloc(E, &kp.ofix, P * N)) || (rc = dalloc(E, &kp.orawf, P * N)) || (rc = dalloc(E, &kp.Fx, P * S)))
             return rc;
     }

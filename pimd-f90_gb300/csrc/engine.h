@@ -120,7 +120,8 @@ struct KP {
     int *fcnt, *foff;      // [P][N] full neighbour list counts / offsets
     int *fnbr;             // [P][fcap] full neighbour list (j ascending per i)
     int *fntot;            // [P] full-list length
-    float *Tf;             // [P][fcap][ndd][6] FP32 dipole tensors of the full list
+    float2 *Tf;            // [P][fcap][ndd] FP32 (t1, 3 t2) dipole-tensor scalars of the full list
+    int *fj;               // [P][fcap] partner j of each full-list entry
     int fcap;
     double4_32a *Fpart;    // [slices][P][S] per-k-slice partial fields of the Ewald field passes
     // cell lists of large boxes (N > 1024, >= 4 cells of width >= Rc per edge)

@@ -326,8 +326,12 @@ __global__ void __launch_bounds__(128) k_pair_qq_m(KP kp) {
     block_reduce_add_f<14, 128>(av, kp.acc + (size_t)b * NACC);
 }
 
-// FP32 Thole-smeared dipole tensors for every entry (i, j) of the full neighbour list,
-// T[t] for the dipole site-kind pairs t = (isp, jsp) (pot_ttm.f90:320-338)
+// FP32 Thole-smeared dipole-tensor scalars for every entry (i, j) of the full neighbour list:
+// (t1, 3 t2) of smear2 for the dipole site-kind pairs t = (isp, jsp) (pot_ttm.f90:320-338), and
+// the partner j alone in its own array. The iterations rebuild the separation R from the O
+// fixed-point sites and the site offsets (the same FP32 operations as here) and form
+// T mu = 3 t2 (R . mu) R - t1 mu, so a list entry streams 4 + 8 ndd bytes per iteration instead
+// of the 8 + 24 ndd of a stored tensor and (i, j) pair.
 template <int MODEL>
 __global__ void __launch_bounds__(128) k_dd_tensors_m(KP kp) {
     using T = TM<MODEL>;
@@ -336,13 +340,15 @@ __global__ void __launch_bounds__(128) k_dd_tensors_m(KP kp) {
     const uint4 *of = kp.ofix + (size_t)b * N;
     const float4 *pf = kp.posf + (size_t)b * kp.S;
     const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
+    int *fj = kp.fj + (size_t)b * kp.fcap;
     const float L[3] = {kp.ptf.box[0], kp.ptf.box[1], kp.ptf.box[2]};
     const float Li[3] = {kp.ptf.boxi[0], kp.ptf.boxi[1], kp.ptf.boxi[2]};
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
         const int2 ij = fl[e];
+        fj[e] = ij.y;
         float Rf[3];
         oo_min_image(kp, of[ij.x], of[ij.y], Rf);
-        float *Te = kp.Tf + ((size_t)b * kp.fcap + e) * kp.ndd * 6;
+        float2 *Te = kp.Tf + ((size_t)b * kp.fcap + e) * kp.ndd;
         int t = 0;
 #pragma unroll
         for (int isp = T::FDI; isp <= T::LDI; isp++) {
@@ -354,13 +360,7 @@ __global__ void __launch_bounds__(128) k_dd_tensors_m(KP kp) {
                                      wrapf(Rf[2] + a.z - c.z, L[2], Li[2])};
                 float t1, t2;
                 smear2<float>(Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2], kp.ptf.apol_dd[isp][jsp], kp.ewf, &t1, &t2);
-                const float t3 = 3.f * t2;
-                Te[6 * t + 0] = t3 * Rs[0] * Rs[0] - t1;
-                Te[6 * t + 1] = t3 * Rs[1] * Rs[1] - t1;
-                Te[6 * t + 2] = t3 * Rs[2] * Rs[2] - t1;
-                Te[6 * t + 3] = t3 * Rs[0] * Rs[1];
-                Te[6 * t + 4] = t3 * Rs[0] * Rs[2];
-                Te[6 * t + 5] = t3 * Rs[1] * Rs[2];
+                Te[t] = make_float2(t1, 3.f * t2);
             }
         }
     }
@@ -368,11 +368,10 @@ __global__ void __launch_bounds__(128) k_dd_tensors_m(KP kp) {
 
 // real-space dipole field of one iteration: gather over the full list, one warp per
 // molecule, lanes striding over its entries, butterfly reduction in a fixed order
-// (deterministic); writes Efdr (pot_ttm.f90:311-365)
-// OTF: the tensors formed on the fly from the O fixed-point sites and site offsets (FP32 smear2,
-// T mu = 3 t2 (R . mu) R - t1 mu) instead of loaded from the per-entry cache: more arithmetic, no
-// 39 MB stream per iteration competing with the structure factor for DRAM (512 H2O x 32 beads,
-// TTM3-F: 27 us against 18 us cached, so the cache is the default; the autotuner tries both)
+// (deterministic); writes Efdr (pot_ttm.f90:311-365). The separation of each site pair is
+// rebuilt from the O fixed-point sites and the site offsets; its smear scalars (t1, 3 t2) come
+// from the per-entry cache of k_dd_tensors_m, or, with OTF, from smear2 in the loop (no cache
+// stream, more arithmetic; the autotuner tries both).
 template <int MODEL, bool OTF>
 __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
     using T = TM<MODEL>;
@@ -383,57 +382,49 @@ __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
     const double *dip = kp.dip + (size_t)b * kp.S * 3;
     const float4 *dipf = kp.dipf + (size_t)b * kp.S;
     const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
+    const int *fj = kp.fj + (size_t)b * kp.fcap;
+    const float2 *Tb = kp.Tf + (size_t)b * kp.fcap * kp.ndd;
     const int ne = kp.fntot[b];  // offsets run past the stored length when the list overflowed
     const int e0 = min(kp.foff[(size_t)b * N + i], ne);
     const int e1 = (i + 1 < N) ? min(kp.foff[(size_t)b * N + i + 1], ne) : ne;
     float ei[5][3];
 #pragma unroll
     for (int k = 0; k < 5; k++) ei[k][0] = ei[k][1] = ei[k][2] = 0.f;
-    if (OTF) {
-        const float4 *pf = kp.posf + (size_t)b * kp.S;
-        const uint4 *of = kp.ofix + (size_t)b * N;
-        const float L[3] = {kp.ptf.box[0], kp.ptf.box[1], kp.ptf.box[2]};
-        const float Li[3] = {kp.ptf.boxi[0], kp.ptf.boxi[1], kp.ptf.boxi[2]};
-        const uint4 oi = of[i];
-        float4 si[5];
+    const float4 *pf = kp.posf + (size_t)b * kp.S;
+    const uint4 *of = kp.ofix + (size_t)b * N;
+    const float L[3] = {kp.ptf.box[0], kp.ptf.box[1], kp.ptf.box[2]};
+    const float Li[3] = {kp.ptf.boxi[0], kp.ptf.boxi[1], kp.ptf.boxi[2]};
+    const uint4 oi = of[i];
+    float4 si[5];
 #pragma unroll
-        for (int k = T::FDI; k <= T::LDI; k++) si[k] = pf[(k - 1) * N + i];
-        for (int e = e0 + lane; e < e1; e += 32) {
-            const int j = fl[e].y;
-            float Rf[3];
-            oo_min_image(kp, oi, of[j], Rf);
-#pragma unroll
-            for (int jsp = T::FDI; jsp <= T::LDI; jsp++) {
-                const float4 c = pf[(jsp - 1) * N + j];
-                const float4 m = dipf[(jsp - 1) * N + j];
-#pragma unroll
-                for (int isp = T::FDI; isp <= T::LDI; isp++) {
-                    const float Rs[3] = {wrapf(Rf[0] + si[isp].x - c.x, L[0], Li[0]), wrapf(Rf[1] + si[isp].y - c.y, L[1], Li[1]),
-                                         wrapf(Rf[2] + si[isp].z - c.z, L[2], Li[2])};
-                    float t1, t2;
-                    smear2<float>(Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2], kp.ptf.apol_dd[isp][jsp], kp.ewf, &t1, &t2);
-                    const float rm = 3.f * t2 * (Rs[0] * m.x + Rs[1] * m.y + Rs[2] * m.z);
-                    ei[isp][0] += rm * Rs[0] - t1 * m.x;
-                    ei[isp][1] += rm * Rs[1] - t1 * m.y;
-                    ei[isp][2] += rm * Rs[2] - t1 * m.z;
-                }
-            }
-        }
-    }
-    for (int e = e0 + lane; e < e1 && !OTF; e += 32) {
-        const int j = fl[e].y;
-        const float *Te = kp.Tf + ((size_t)b * kp.fcap + e) * kp.ndd * 6;
+    for (int k = T::FDI; k <= T::LDI; k++) si[k] = pf[(k - 1) * N + i];
+    for (int e = e0 + lane; e < e1; e += 32) {
+        const int j = OTF ? fl[e].y : fj[e];
+        float Rf[3];
+        oo_min_image(kp, oi, of[j], Rf);
         int t = 0;
 #pragma unroll
         for (int isp = T::FDI; isp <= T::LDI; isp++)
 #pragma unroll
             for (int jsp = T::FDI; jsp <= T::LDI; jsp++, t++) {
+                const float4 c = pf[(jsp - 1) * N + j];
                 const float4 m = dipf[(jsp - 1) * N + j];
-                const float mx = m.x, my = m.y, mz = m.z;
-                const float *Tt = Te + 6 * t;
-                ei[isp][0] += Tt[0] * mx + Tt[3] * my + Tt[4] * mz;
-                ei[isp][1] += Tt[3] * mx + Tt[1] * my + Tt[5] * mz;
-                ei[isp][2] += Tt[4] * mx + Tt[5] * my + Tt[2] * mz;
+                const float Rs[3] = {wrapf(Rf[0] + si[isp].x - c.x, L[0], Li[0]), wrapf(Rf[1] + si[isp].y - c.y, L[1], Li[1]),
+                                     wrapf(Rf[2] + si[isp].z - c.z, L[2], Li[2])};
+                float t1, t3;
+                if (OTF) {
+                    float t2;
+                    smear2<float>(Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2], kp.ptf.apol_dd[isp][jsp], kp.ewf, &t1, &t2);
+                    t3 = 3.f * t2;
+                } else {
+                    const float2 ts = Tb[(size_t)e * kp.ndd + t];
+                    t1 = ts.x;
+                    t3 = ts.y;
+                }
+                const float rm = t3 * (Rs[0] * m.x + Rs[1] * m.y + Rs[2] * m.z);
+                ei[isp][0] += rm * Rs[0] - t1 * m.x;
+                ei[isp][1] += rm * Rs[1] - t1 * m.y;
+                ei[isp][2] += rm * Rs[2] - t1 * m.z;
             }
     }
 #pragma unroll

@@ -138,11 +138,14 @@ def test_qspcfw_input_32(pkg, orc, engine_lib):
 
 @pytest.mark.parametrize("path", ["fp32_pipe", "default"])
 def test_ewald_large_k_shell(pkg, orc, engine_lib, path):
-    """The mixed engine's Ewald passes at |n| <= 24 (the large-system k range), TTM3-F on the
-    input_128 frame, one bead, alpha 0.9: forced onto the FP32-pipe structure-factor and field
-    kernels (sf_tc = ff_tc = 0), and on the default selection."""
+    """The mixed engine's Ewald passes at |n| <= 24 (the large-system k range: 28 888 k-vectors
+    there, 29 000 here), TTM3-F on the input_128 frame, one bead, Rc 7.8 A with alpha from the
+    eps = 1e-6 rule, as the large system uses: forced onto the FP32-pipe structure-factor and
+    field kernels (sf_tc = ff_tc = 0), and on the default selection. (With a much larger alpha,
+    0.9 / A, the FP32 reciprocal field's rounding floor, ~1.7e-8 D, lies above the 1e-8
+    threshold and the iterations run to polar_maxiter; the forces stay inside the budget.)"""
     box, RRt, RRc = frame("input_128", 1)
-    p = params(3, box, RRt.shape[1], 1, 7.8, 0.9, 24)
+    p = params(3, box, RRt.shape[1], 1, 7.8, pkg.waterbox.ewald_alpha_eps(7.8), 24)
     eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_MIXED)
     if path == "fp32_pipe":
         t = eng.set_tuning(sf_tc=0, ff_tc=0)
