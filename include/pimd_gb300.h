@@ -158,6 +158,47 @@ int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, do
 int pimd_md_step(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
                  double *RRc, const double *xi1, const double *xi2, int t, double *out4);
 
+/* Thermostats of the MD step beyond PILE (main_stuff.f90:132-188, MD.f90:41-46, 96-104), after
+ * pimd_nm_init: bead_thermostat 2 runs one chain-2 Nose-Hoover thermostat (Nose_Hoover.f90:33-112,
+ * L = 1, Nbeads*temp) per (atom, normal mode k >= 2, component) with tau = 1/omega_k, and on the
+ * centroid mode too with centroid_thermostat (tau_centroid), before the first and after the second
+ * half kick (pimd_md_params.langevin must then be 0); bead_thermostat 0 leaves the bead thermostat
+ * to pimd_md_params.langevin. global_thermostat adds the global chain (THERMOSTAT: L = 3 Natoms
+ * Nbeads, temp*Nbeads, tau) on the module variable uk at the start and the end of the step, each
+ * followed by PPt = s PPt. Chain velocities start as the reference sets them (vxi_global = 1,
+ * vxi_beads = 0, InputOutput.f90:395-404) and uk at 0: set the initial uk with
+ * pimd_set_thermostat_state (the reference's initialize_velocities leaves calc_uk_centroid there).
+ * The chains and the thermostats' kinetic energies run in the exact FP64 integrator kernels in
+ * both engines. */
+typedef struct {
+    int bead_thermostat;     /* 0 (PILE / none, per pimd_md_params.langevin) or 2 (Nose-Hoover) */
+    int global_thermostat;   /* != 0: the global chain                                         */
+    double tau;              /* global chain time constant (ps)                                 */
+    double temp;             /* K; the chains couple to Nbeads*temp                             */
+    int centroid_thermostat; /* bead chains on the centroid mode as well                        */
+    double tau_centroid;     /* ps                                                              */
+} pimd_thermostat;
+int pimd_set_thermostat(pimd_ctx *ctx, const pimd_thermostat *th);
+/* Chain state for checkpoints (the reference's save_checkpoint / load_checkpoint records):
+ * vxi_global[2], the module variable uk, and vxi_beads(2,Natoms,Nbeads,3) (NULL to skip; needs
+ * bead_thermostat 2). Blocking. */
+int pimd_get_thermostat_state(pimd_ctx *ctx, double *vxi_global, double *uk, double *vxi_beads);
+int pimd_set_thermostat_state(pimd_ctx *ctx, const double *vxi_global, double uk,
+                              const double *vxi_beads);
+/* The MD step with the quantities write_out takes from it (InputOutput.f90:566-571,
+ * estimators.f90:30-96), computed on the device: out[PIMD_MD_NOUT] = {Upot, virial, virialc, uk
+ * (the module variable after the step), calc_uk after the force call, K0 = sum m (r_k -
+ * r_(k-1))^2 (amu A^2), sys_temp (K), quantum-virial energy (kcal/mol per molecule) and pressure
+ * (bar), simple-estimator energy and pressure, the global chain's last scale factor s}. Device
+ * variant: out is a device pointer, stream-ordered (no host synchronisation); host variant: as
+ * pimd_md_step with out on the host. Works with pimd_set_graph like pimd_md_step_device. */
+enum { PIMD_MD_NOUT = 12 };
+int pimd_md_step_ex_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt,
+                           double *dRRt, double *RRc, const double *xi1, const double *xi2, int t,
+                           double *out);
+int pimd_md_step_ex(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
+                    double *RRc, const double *xi1, const double *xi2, int t, double *out);
+
 /* CUDA-graph execution of pimd_md_step_device / pimd_md_step (enable != 0). The whole step --
  * Langevin, kicks, EvolveRing, PBCs and the force call -- is captured on its first call and
  * replayed on later calls with the same buffers and parameters (a change of any pointer or

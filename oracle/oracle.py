@@ -103,6 +103,13 @@ def lib():
         L.orc_pool_forces.argtypes = [ctypes.c_void_p, D, D, D, D, D, D, ctypes.c_int]
         L.orc_pimd_vv_step_pool.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(MDParams),
                                             ctypes.c_int, D, D, D, D, D, D, ctypes.c_int, D, D, D, D]
+        L.orc_nose_hoover.argtypes = [D, D, D, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double]
+        L.orc_estimators.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 7 + [D]
+        L.orc_ring_k0.restype = ctypes.c_double
+        L.orc_ring_k0.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, D]
+        L.orc_pimd_vv_step_ex.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(MDParams), ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_double, ctypes.c_int, D, D, D, D, D, D, D, D, D,
+                                          ctypes.c_int, D]
         _lib = L
     return _lib
 
@@ -295,3 +302,71 @@ def pimd_vv_step(orc, md, RRt, PPt, dRRt, xi1=None, xi2=None, t=1, pool=None):
                                 _p(dRRt), _p(RRc), x1, x2, int(t), ctypes.byref(U), ctypes.byref(v),
                                 ctypes.byref(vc), ctypes.byref(uk))
     return dict(Upot=U.value, virial=v.value, virialc=vc.value, uk=uk.value, RRc=RRc)
+
+
+MD_NOUT = 12
+MD_OUT_NAMES = ("Upot", "virial", "virialc", "uk", "uk_mid", "K0", "sys_temp", "E_virial", "P_virial", "E_simple",
+                "P_simple", "s_global")
+
+
+def _md_params(md):
+    mp = MDParams()
+    mp.delt = md["delt"]
+    mp.massO = md["massO"]
+    mp.massH = md["massH"]
+    mp.setNMfreq = md.get("setNMfreq", 0.0)
+    mp.langevin = int(md.get("langevin", 1))
+    mp.centroid_thermostat = int(md.get("centroid_thermostat", 0))
+    mp.tau_centroid = md.get("tau_centroid", 0.1)
+    mp.temp = md["temp"]
+    return mp
+
+
+def thermostat_state(P, natoms, uk=0.0):
+    """The reference's initial chain state (InputOutput.f90:397-404): vxi_global = 1, vxi_beads = 0
+    (layout (3, P, natoms, 2) = vxi_beads(2, natoms, P, 3)), and the module variable uk."""
+    return dict(vxi_global=np.ones(2), uk=float(uk), vxi_beads=np.zeros((3, P, natoms, 2)))
+
+
+def pimd_vv_step_ex(orc, md, RRt, PPt, dRRt, state, t=1, xi1=None, xi2=None, bead_thermostat=0, global_thermostat=0,
+                    tau=0.1, pool=None):
+    """PIMD_VV (MD.f90:35-110) with bead thermostat 0 none / 1 Langevin_NM (xi1, xi2) / 2 Nose-Hoover
+    on the normal modes, and the global chain thermostat; arrays updated in place, state (chain
+    velocities, uk) updated in place. Returns the 12 outputs of the step by name."""
+    mp = _md_params(md)
+    P = RRt.shape[0]
+    RRc = np.zeros(RRt.shape[1:])
+    out = np.zeros(MD_NOUT)
+    vg = state["vxi_global"]
+    vb = state["vxi_beads"]
+    assert vg.dtype == np.float64 and vg.flags.c_contiguous and vb.flags.c_contiguous
+    uk = ctypes.c_double(state["uk"])
+    x1 = _p(_f64(xi1)) if xi1 is not None else None
+    x2 = _p(_f64(xi2)) if xi2 is not None else None
+    lib().orc_pimd_vv_step_ex(orc.h, pool.h if pool is not None else None, ctypes.byref(mp), int(bead_thermostat),
+                              int(global_thermostat), float(tau), P, _p(RRt), _p(PPt), _p(dRRt), _p(RRc), x1, x2,
+                              _p(vg), ctypes.byref(uk), _p(vb), int(t), _p(out))
+    state["uk"] = uk.value
+    r = dict(zip(MD_OUT_NAMES, out.tolist()))
+    r["RRc"] = RRc
+    return r
+
+
+def nose_hoover(uk, vxi, tau, delt2, L, temp):
+    """Nose_Hoover.f90:33-112 half step: returns (s, uk); vxi (2,) updated in place."""
+    s, u = ctypes.c_double(), ctypes.c_double(uk)
+    lib().orc_nose_hoover(ctypes.byref(s), ctypes.byref(u), _p(vxi), float(tau), float(delt2), int(L), float(temp))
+    return s.value, u.value
+
+
+def estimators(natoms, P, volume, omegan, Upot, virial, virialc, uk, K0):
+    e = np.zeros(5)
+    lib().orc_estimators(int(natoms), int(P), float(volume), float(omegan), float(Upot), float(virial),
+                         float(virialc), float(uk), float(K0), _p(e))
+    return dict(zip(("sys_temp", "E_virial", "P_virial", "E_simple", "P_simple"), e.tolist()))
+
+
+def ring_k0(massO, massH, RRt):
+    """estimators.f90:57-73: K0 = sum over beads, atoms, components of m (r_k - r_(k-1))^2."""
+    RRt = _f64(RRt)
+    return lib().orc_ring_k0(RRt.shape[0], RRt.shape[1], float(massO), float(massH), _p(RRt))

@@ -1959,10 +1959,120 @@ void orc_pimd_vv_step(void *h, const orc_md_params *mp, int P, double *RRt, doub
     orc_pimd_vv_step_pool(h, nullptr, mp, P, RRt, PPt, dRRt, RRc, xi1, xi2, t, Upot, virial, virialc, uk);
 }
 
+// Nose_Hoover.f90:33-112: one half step (delt2) of a chain-2 Nose-Hoover thermostat on uk, L
+// degrees of freedom at temperature temp; returns s, updates vxi[2] and uk (= uk s^2)
+void orc_nose_hoover(double *s, double *uk, double *vxi, double tau, double delt2, int L, double temp) {
+    const double delt4 = delt2 / 2.0, delt8 = delt2 / 4.0;
+    const double kT = KB_AMU * temp;
+    const double M1 = (L * kT) * (tau * tau);
+    const double M2 = M1;
+    vxi[1] = vxi[1] + ((M1 * (vxi[0] * vxi[0]) - kT) * delt4) / M2;
+    vxi[0] = vxi[0] * std::exp(-vxi[1] * delt8);
+    vxi[0] = vxi[0] + ((2 * *uk - L * kT) * delt4) / M1;
+    vxi[0] = vxi[0] * std::exp(-vxi[1] * delt8);
+    *s = std::exp(-vxi[0] * delt2);
+    *uk = (*uk * *s) * *s;
+    vxi[0] = vxi[0] * std::exp(-vxi[1] * delt8);
+    vxi[0] = vxi[0] + ((2 * *uk - L * kT) * delt4) / M1;
+    vxi[0] = vxi[0] * std::exp(-vxi[1] * delt8);
+    vxi[1] = vxi[1] + ((M1 * (vxi[0] * vxi[0]) - kT) * delt4) / M2;
+}
+
+// main_stuff.f90:145-171: bead_thermostat with bead_thermostat_type 'Nose-Hoover', one chain per
+// (atom, normal mode, component) in normal-mode space; vxi_beads(2, natoms, P, 3)
+void orc_bead_nose_hoover(int P, int natoms, const double *C, const double *omegalist, const double *msf,
+                          double massO, double massH, double *PPt, double *vxi_beads, int centroid_thermostat,
+                          double tau_centroid, double delt2, double temp) {
+    std::vector<double> in(3 * P), tr(3 * P), out(3 * P);
+    const double imassO = 1.0 / massO, imassH = 1.0 / massH;
+    for (int i = 0; i < natoms; i++) {
+        const double imass = (i % 3 == 0) ? imassO : imassH;
+        for (int j = 0; j < P; j++)
+            for (int c = 0; c < 3; c++) in[3 * j + c] = PPt[3 * i + c + (size_t)3 * natoms * j];
+        real2NM(P, C, in.data(), tr.data());
+        auto vxi = [&](int j, int k) { return vxi_beads + 2 * ((size_t)i + (size_t)natoms * ((size_t)j + (size_t)P * k)); };
+        if (centroid_thermostat) {
+            for (int k = 0; k < 3; k++) {
+                double sbead, ukb = (0.5 * imass) * (tr[k] * tr[k]);
+                orc_nose_hoover(&sbead, &ukb, vxi(0, k), tau_centroid, delt2, 1, P * temp);
+                tr[k] = tr[k] * sbead;
+            }
+        }
+        for (int j = 1; j < P; j++) {
+            const double tau = 1.0 / omegalist[j];
+            for (int k = 0; k < 3; k++) {
+                double sbead, ukb = ((0.5 * imass) * (tr[3 * j + k] * tr[3 * j + k])) / msf[j];
+                orc_nose_hoover(&sbead, &ukb, vxi(j, k), tau, delt2, 1, P * temp);
+                tr[3 * j + k] = tr[3 * j + k] * sbead;
+            }
+        }
+        NM2real(P, C, tr.data(), out.data());
+        for (int j = 0; j < P; j++)
+            for (int c = 0; c < 3; c++) PPt[3 * i + c + (size_t)3 * natoms * j] = out[3 * j + c];
+    }
+}
+
+// estimators.f90:57-73: K0 = sum over beads k, atoms, components of m (r_k - r_(k-1))^2, ring closed
+double orc_ring_k0(int P, int natoms, double massO, double massH, const double *RRt) {
+    double K0 = 0;
+    for (int k = 0; k < P; k++) {
+        const int km = (k == 0) ? P - 1 : k - 1;
+        for (int j = 0; j < natoms; j++) {
+            const double mass = (j % 3 == 0) ? massO : massH;
+            for (int i = 0; i < 3; i++) {
+                const double d = RRt[i + 3 * (size_t)j + (size_t)3 * natoms * k] - RRt[i + 3 * (size_t)j + (size_t)3 * natoms * km];
+                K0 = K0 + mass * (d * d);
+            }
+        }
+    }
+    return K0;
+}
+
+// write_out's per-step estimators (InputOutput.f90:566-571) from estimators.f90:30-96, with the
+// reference's literal types: 1.5*Natoms(*Nbeads) is a default-real product
+void orc_estimators(int natoms, int P, double volume, double omegan, double Upot, double virial, double virialc,
+                    double uk, double K0raw, double *est5) {
+    const double TEMPFACTOR = 0.80181484527, kb = 0.0019872041, PRESSCON2 = 69477.0, MASSCONi = 1.0 / 418.4;
+    const int Nwaters = natoms / 3;
+    const double sys_temp = TEMPFACTOR * uk / (double)(natoms * P * P);
+    double KE = (double)(1.5f * (float)natoms) * kb * sys_temp;
+    const double qE = (KE + 0.5 * (virial - virialc) / P + Upot / P) / Nwaters;
+    const double qP = PRESSCON2 * (1 / (3 * volume)) * (2 * KE - virialc / P) / Nwaters;
+    KE = (double)((1.5f * (float)natoms) * (float)P) * kb * sys_temp * P;
+    const double K0 = 0.5 * K0raw * (omegan * omegan) * MASSCONi;
+    const double sE = (KE - K0 + Upot) / (double)(Nwaters * P);
+    const double sP = PRESSCON2 * (1 / (3 * volume)) * (2 * (KE - K0) - virial) / Nwaters;
+    est5[0] = sys_temp;
+    est5[1] = qE;
+    est5[2] = qP;
+    est5[3] = sE;
+    est5[4] = sP;
+}
+
 // As orc_pimd_vv_step with the force call spread over a thread pool (orc_pool_create).
 void orc_pimd_vv_step_pool(void *h, void *pool, const orc_md_params *mp, int P, double *RRt, double *PPt,
                            double *dRRt, double *RRc, const double *xi1, const double *xi2, int t, double *Upot,
                            double *virial, double *virialc, double *uk) {
+    double out[ORC_MD_NOUT], vxg[2] = {1.0, 1.0}, ukst = 0.0;
+    orc_pimd_vv_step_ex(h, pool, mp, (mp->langevin && xi1) ? 1 : 0, 0, 0.0, P, RRt, PPt, dRRt, RRc, xi1, xi2, vxg,
+                        &ukst, nullptr, t, out);
+    *Upot = out[0];
+    *virial = out[1];
+    *virialc = out[2];
+    *uk = out[3];
+}
+
+// MD.f90:35-110 PIMD_VV with the reference's thermostats: bead_thermostat (main_stuff.f90:132-188,
+// Langevin_NM or Nose-Hoover chains on the normal modes) and the global chain THERMOSTAT
+// (Nose_Hoover on uk, L = 3 Natoms Nbeads, at temp Nbeads), each at the start and the end of the
+// step; write_out's calc_uk after the force call feeds the estimators. out[ORC_MD_NOUT]: Upot,
+// virial, virialc, uk (the reference's uk after the step), uk after the force call, K0, then
+// sys_temp, virial-estimator energy and pressure, simple-estimator energy and pressure, and the
+// step's last global scale factor s. uk_state is the reference's module variable uk across steps.
+void orc_pimd_vv_step_ex(void *h, void *pool, const orc_md_params *mp, int bead_thermostat, int global_thermostat,
+                         double tau, int P, double *RRt, double *PPt, double *dRRt, double *RRc, const double *xi1,
+                         const double *xi2, double *vxi_global, double *uk_state, double *vxi_beads, int t,
+                         double *out) {
     Orc *o = static_cast<Orc *>(h);
     int na = o->Natoms, nw = na / 3;
     double delt2 = mp->delt / 2.0;
@@ -1973,8 +2083,19 @@ void orc_pimd_vv_step_pool(void *h, void *pool, const orc_md_params *mp, int P, 
     orc_langevin_init(P, om.data(), delt2, mp->centroid_thermostat, mp->tau_centroid, P * mp->temp, c1.data(),
                       c2.data());
     size_t nall = (size_t)3 * na * P;
-    if (mp->langevin && xi1)
-        orc_langevin_nm(P, na, C.data(), msf.data(), c1.data(), c2.data(), mp->massO, mp->massH, PPt, xi1);
+    auto bead_thermostat_step = [&](const double *xi) {
+        if (bead_thermostat == 1 && xi)
+            orc_langevin_nm(P, na, C.data(), msf.data(), c1.data(), c2.data(), mp->massO, mp->massH, PPt, xi);
+        else if (bead_thermostat == 2)
+            orc_bead_nose_hoover(P, na, C.data(), om.data(), msf.data(), mp->massO, mp->massH, PPt, vxi_beads,
+                                 mp->centroid_thermostat, mp->tau_centroid, delt2, mp->temp);
+    };
+    double s = 1.0;
+    bead_thermostat_step(xi1);
+    if (global_thermostat) {
+        orc_nose_hoover(&s, uk_state, vxi_global, tau, delt2, 3 * na * P, mp->temp * P);
+        for (size_t i = 0; i < nall; i++) PPt[i] = PPt[i] * s;
+    }
     for (size_t i = 0; i < nall; i++) PPt[i] = PPt[i] - MASSCON * dRRt[i] * delt2;
     if (P > 1) {
         std::vector<double> rr(3 * P), pp(3 * P);
@@ -2001,9 +2122,9 @@ void orc_pimd_vv_step_pool(void *h, void *pool, const orc_md_params *mp, int P, 
     }
     // centroid and PBCs (main_stuff.f90:107-125, cubic box assumed by the reference)
     for (int i = 0; i < 3 * na; i++) {
-        double s = 0;
-        for (int j = 0; j < P; j++) s += RRt[i + (size_t)3 * na * j];
-        RRc[i] = s / P;
+        double sum = 0;
+        for (int j = 0; j < P; j++) sum += RRt[i + (size_t)3 * na * j];
+        RRc[i] = sum / P;
     }
     for (int i = 0; i < 3 * na; i++) {
         double shift = o->box[0] * anint(RRc[i] * o->boxi[0]);
@@ -2035,13 +2156,27 @@ void orc_pimd_vv_step_pool(void *h, void *pool, const orc_md_params *mp, int P, 
             virc += vc;
         }
     }
-    *Upot = U;
-    *virial = vir;
-    *virialc = virc / P;
+    out[0] = U;
+    out[1] = vir;
+    out[2] = virc / P;
+    // calc_uk and write_out (MD.f90:86-90)
+    out[4] = orc_calc_uk(P, na, mp->massO, mp->massH, PPt, mp->setNMfreq, C.data(), msf.data());
+    out[5] = orc_ring_k0(P, na, mp->massO, mp->massH, RRt);
+    orc_estimators(na, P, o->box[0] * o->box[1] * o->box[2], omegan, out[0], out[1], out[2], out[4], out[5], out + 6);
     for (size_t i = 0; i < nall; i++) PPt[i] = PPt[i] - MASSCON * dRRt[i] * delt2;
-    if (mp->langevin && xi2)
-        orc_langevin_nm(P, na, C.data(), msf.data(), c1.data(), c2.data(), mp->massO, mp->massH, PPt, xi2);
-    *uk = orc_calc_uk(P, na, mp->massO, mp->massH, PPt, mp->setNMfreq, C.data(), msf.data());
+    bead_thermostat_step(xi2);
+    double ukv = orc_calc_uk(P, na, mp->massO, mp->massH, PPt, mp->setNMfreq, C.data(), msf.data());
+    s = 1.0;
+    if (global_thermostat) {
+        *uk_state = ukv;
+        orc_nose_hoover(&s, uk_state, vxi_global, tau, delt2, 3 * na * P, mp->temp * P);
+        for (size_t i = 0; i < nall; i++) PPt[i] = PPt[i] * s;
+        ukv = *uk_state;
+    } else {
+        *uk_state = ukv;
+    }
+    out[3] = ukv;
+    out[11] = s;
 }
 
 }  // extern "C"

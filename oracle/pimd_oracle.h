@@ -111,6 +111,27 @@ void orc_pimd_vv_step_pool(void *h, void *pool, const orc_md_params *mp, int P, 
                            const double *xi2, int t, double *Upot, double *virial,
                            double *virialc, double *uk);
 
+/* Nose_Hoover.f90:33-112 (one half step of a chain-2 thermostat), main_stuff.f90:145-171 (the
+ * bead Nose-Hoover thermostat on the normal modes, vxi_beads(2,natoms,P,3)), estimators.f90:57-73
+ * (ring K0) and estimators.f90:30-96 with InputOutput.f90:566 (sys_temp, virial-estimator energy
+ * and pressure, simple-estimator energy and pressure into est5). */
+void orc_nose_hoover(double *s, double *uk, double *vxi, double tau, double delt2, int L, double temp);
+void orc_bead_nose_hoover(int P, int natoms, const double *C, const double *omegalist, const double *msf,
+                          double massO, double massH, double *PPt, double *vxi_beads, int centroid_thermostat,
+                          double tau_centroid, double delt2, double temp);
+double orc_ring_k0(int P, int natoms, double massO, double massH, const double *RRt);
+void orc_estimators(int natoms, int P, double volume, double omegan, double Upot, double virial,
+                    double virialc, double uk, double K0raw, double *est5);
+/* PIMD_VV with bead_thermostat 0 none / 1 Langevin_NM (xi1, xi2) / 2 Nose-Hoover on the normal
+ * modes, and the global chain thermostat (tau) when global_thermostat != 0; uk_state is the
+ * reference's uk across steps, vxi_global[2] and vxi_beads the chain velocities; out[12]. */
+#define ORC_MD_NOUT 12
+void orc_pimd_vv_step_ex(void *h, void *pool, const orc_md_params *mp, int bead_thermostat,
+                         int global_thermostat, double tau, int P, double *RRt, double *PPt,
+                         double *dRRt, double *RRc, const double *xi1, const double *xi2,
+                         double *vxi_global, double *uk_state, double *vxi_beads, int t,
+                         double *out);
+
 #ifdef __cplusplus
 }
 #endif

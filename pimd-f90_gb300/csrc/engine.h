@@ -274,6 +274,14 @@ struct Engine {
     int nm_P = 0;
     double *d_nmC = nullptr, *d_nmA = nullptr;  // C(P,P), [A11,A12,A21,A22,msf,c1,c2] x P
     std::vector<double> h_nm;                     // host copy: A11..A22, omegalist, msf, C
+    double nm_omegan = 0, nm_setfreq = 0;         // InitNormalModes' omegan and setNMfreq
+    // Nose-Hoover thermostats of the MD step (pimd_set_thermostat): the global chain
+    // (MD.f90:43-46, 101-104) and the bead chains on the normal modes (main_stuff.f90:145-171)
+    bool nh_global = false, nh_bead = false, nh_centroid = false;
+    double nh_tau = 0, nh_temp = 0, nh_tau_centroid = 0;
+    long long nh_gen = 0;          // configuration generation (part of the MD-step graph key)
+    double *d_nh = nullptr;        // [vxi1, vxi2, uk, s_pre, s_post, uk_mid, K0, spare]
+    double *d_vxib = nullptr;      // vxi_beads(2, Natoms, P, 3)
 };
 
 // Arguments of the normal-mode / thermostat / integrator kernels for one ring polymer
@@ -282,7 +290,7 @@ struct NMArgs {
     int P, natoms;
     const double *C;    // C(P,P) column-major: C[j + P*k] = C(j+1, k+1); then the same as FP32
                         // pairs (hi, lo) with hi + lo = C to 2^-48 (float2[P*P], fast transforms)
-    const double *A;    // [A11, A12, A21, A22, msf, c1, c2, A12 / msf, A21 msf, c2 sqrt(msf)] x P
+    const double *A;    // [A11, A12, A21, A22, msf, c1, c2, A12 / msf, A21 msf, c2 sqrt(msf), omegalist] x P
     double massO, massH;
     double delt, delt2, box0, boxi0;
     int langevin, evolve;
@@ -296,6 +304,12 @@ struct NMArgs {
     float2 kick;                        // MASSCON dt/2 as an FP32 pair
     float2 hminv[2], pinv, boxf;        // 1/(2m) of O, H; 1/P; box edge (pairs)
     float boxif;                        // 1/box edge
+    // Nose-Hoover chains on the normal modes instead of Langevin_NM (main_stuff.f90:145-171)
+    int bead_nh, centroid_nh;
+    double tau_centroid, nh_temp;       // chains couple to nh_temp = Nbeads T
+    double *vxib;                       // vxi_beads(2, Natoms, P, 3)
+    const double *s_pre;                // global chain's scale factor applied after the bead thermostat
+    int nm_ke;                          // calc_uk in normal-mode space (setNMfreq != 0, P > 1)
 };
 __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt, double *RRc);
 __global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk);
@@ -303,7 +317,7 @@ __global__ void k_md_sum(int P, const double *Upott, const double *virialt, cons
                          double *out4);
 void nm_launch_shape(int P, int natoms, int *threads, int *blocks, size_t *smem);
 void nm_smem_optin(int P);
-void nm_extend_A(std::vector<double> &A, int P);
+void nm_extend_A(std::vector<double> &A, int P, const std::vector<double> &omegalist);
 void nm_fast_args(NMArgs &a);
 void nm_launch_md_pre(const NMArgs &a, cudaStream_t st, double *RRt, double *PPt, const double *dRRt, double *RRc);
 void nm_launch_md_post(const NMArgs &a, cudaStream_t st, double *PPt, const double *dRRt, double *uk);

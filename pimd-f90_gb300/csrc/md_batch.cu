@@ -257,7 +257,7 @@ int pimd_batch_create(pimd_batch **out, const pimd_params *common, const pimd_re
             A[5 * r.P + j] = c1;
             A[6 * r.P + j] = std::sqrt(KB_AMU * r.P * r.temp) * std::sqrt(1 - c1 * c1);
         }
-        nm_extend_A(A, r.P);
+        nm_extend_A(A, r.P, om);
         std::vector<double> CP;
         nm_pair_copy(C, CP);  // C, then its FP32 pairs for the mixed engine's transforms
         if ((rc = balloc(bt, &r.d_C, CP.size())) || (rc = balloc(bt, &r.d_A, A.size()))) break;

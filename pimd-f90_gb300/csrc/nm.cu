@@ -6,6 +6,7 @@
 // One group of 3P threads owns one atom (thread = (bead j, component c)); the P x P mode
 // matrix C sits in shared memory. The transforms are summed in the reference's order with
 // every product and sum rounded separately, so they are bit-identical to the FP64 oracle.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -79,6 +80,64 @@ PIMD_D void langevin_atom(const NMArgs &a, const double *Cs, double *p, double *
     __syncthreads();
     if (active) p[3 * j + c] = nm_row(Cs, tr, a.P, j, c, false);
     __syncthreads();
+}
+
+// Nose_Hoover.f90:33-112: one half step (delt2) of a chain-2 thermostat (vxi[0], vxi[1]) on the
+// kinetic energy uk of L degrees of freedom at temperature temp; returns s and leaves uk s^2 in
+// uk. Every product and sum rounded separately, as the FP64 oracle computes it.
+PIMD_D double nh_half(double *vxi, double &uk, double tau, double delt2, int L, double temp) {
+    const double delt4 = __ddiv_rn(delt2, 2.0), delt8 = __ddiv_rn(delt2, 4.0);
+    const double kT = __dmul_rn(KB_AMU, temp), LkT = __dmul_rn((double)L, kT);
+    const double M1 = __dmul_rn(LkT, __dmul_rn(tau, tau)), M2 = M1;
+    double v1 = vxi[0], v2 = vxi[1];
+    v2 = __dadd_rn(v2, __ddiv_rn(__dmul_rn(__dsub_rn(__dmul_rn(M1, __dmul_rn(v1, v1)), kT), delt4), M2));
+    v1 = __dmul_rn(v1, exp(__dmul_rn(-v2, delt8)));
+    v1 = __dadd_rn(v1, __ddiv_rn(__dmul_rn(__dsub_rn(__dmul_rn(2.0, uk), LkT), delt4), M1));
+    v1 = __dmul_rn(v1, exp(__dmul_rn(-v2, delt8)));
+    const double s = exp(__dmul_rn(-v1, delt2));
+    uk = __dmul_rn(__dmul_rn(uk, s), s);
+    v1 = __dmul_rn(v1, exp(__dmul_rn(-v2, delt8)));
+    v1 = __dadd_rn(v1, __ddiv_rn(__dmul_rn(__dsub_rn(__dmul_rn(2.0, uk), LkT), delt4), M1));
+    v1 = __dmul_rn(v1, exp(__dmul_rn(-v2, delt8)));
+    v2 = __dadd_rn(v2, __ddiv_rn(__dmul_rn(__dsub_rn(__dmul_rn(M1, __dmul_rn(v1, v1)), kT), delt4), M2));
+    vxi[0] = v1;
+    vxi[1] = v2;
+    return s;
+}
+
+// bead_thermostat 'Nose-Hoover' (main_stuff.f90:145-171) on one atom's momenta p[3P] in shared
+// memory: to normal modes, one chain per (mode j, component c) with L = 1 at Nbeads T (tau =
+// 1/omega_j; the centroid mode only with centroid_nh, tau_centroid), back to real space
+PIMD_D void bead_nh_atom(const NMArgs &a, const double *Cs, double *p, double *tr, int atom, int j, int c,
+                         bool active) {
+    if (active) tr[3 * j + c] = nm_row(Cs, p, a.P, j, c, true);
+    __syncthreads();
+    if (active && (j > 0 || a.centroid_nh)) {
+        const double imass = 1.0 / ((atom % 3 == 0) ? a.massO : a.massH);
+        double *vx = a.vxib + 2 * ((size_t)atom + (size_t)a.natoms * ((size_t)j + (size_t)a.P * c));
+        const double x = tr[3 * j + c];
+        double ukb = __dmul_rn(__dmul_rn(0.5, imass), __dmul_rn(x, x));
+        double tau = a.tau_centroid;
+        if (j > 0) {
+            ukb = __ddiv_rn(ukb, a.A[4 * a.P + j]);
+            tau = __ddiv_rn(1.0, a.A[10 * a.P + j]);
+        }
+        double v[2] = {vx[0], vx[1]};
+        const double sb = nh_half(v, ukb, tau, a.delt2, 1, a.nh_temp);
+        vx[0] = v[0];
+        vx[1] = v[1];
+        tr[3 * j + c] = __dmul_rn(x, sb);
+    }
+    __syncthreads();
+    if (active) p[3 * j + c] = nm_row(Cs, tr, a.P, j, c, false);
+    __syncthreads();
+}
+
+// the bead thermostat of the step (Langevin_NM or the bead chains), then the global chain's s
+PIMD_D void bead_thermostat(const NMArgs &a, const double *Cs, double *p, double *tr, int atom, int j, int c,
+                            bool active) {
+    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active);
+    else if (a.bead_nh) bead_nh_atom(a, Cs, p, tr, atom, j, c, active);
 }
 
 // ---- the mixed engine's integrator: FP32-pair (double-float) arithmetic ----------------------
@@ -362,7 +421,8 @@ __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt,
         p[3 * j + c] = PPt[gi];
     }
     __syncthreads();
-    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active);
+    bead_thermostat(a, Cs, p, tr, atom, j, c, active);
+    if (active && a.s_pre) p[3 * j + c] = __dmul_rn(p[3 * j + c], *a.s_pre);  // MD.f90:43-46
     if (active) p[3 * j + c] = __dsub_rn(p[3 * j + c], __dmul_rn(__dmul_rn(MASSCON, dRRt[gi]), a.delt2));
     __syncthreads();
     const double m = (atom % 3 == 0) ? a.massO : a.massH;
@@ -424,12 +484,17 @@ __global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk)
     const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
     if (active) p[3 * j + c] = __dsub_rn(PPt[gi], __dmul_rn(__dmul_rn(MASSCON, dRRt[gi]), a.delt2));
     __syncthreads();
-    if (a.langevin) langevin_atom(a, Cs, p, tr, atom, j, c, active);
+    bead_thermostat(a, Cs, p, tr, atom, j, c, active);
     double ke = 0.0;
     if (active) {
         PPt[gi] = p[3 * j + c];
         const double m = (atom % 3 == 0) ? a.massO : a.massH;
-        ke = (1.0 / m) * p[3 * j + c] * p[3 * j + c];
+        if (a.nm_ke) {  // calc_uk's normal-mode form (main_stuff.f90:367-384)
+            const double pt = nm_row(Cs, p, P, j, c, true);
+            ke = (1.0 / m) * pt * pt / a.A[4 * P + j];
+        } else {
+            ke = (1.0 / m) * p[3 * j + c] * p[3 * j + c];
+        }
     }
     for (int o = 16; o > 0; o >>= 1) ke += __shfl_xor_sync(0xffffffffu, ke, o);
     // the block's warps in order, then one atomic per block (not per warp: one address)
@@ -494,6 +559,114 @@ __global__ void k_langevin(NMArgs a, double *PPt) {
     if (active) PPt[gi] = p[3 * j + c];
 }
 
+// the global chain thermostat (MD.f90:43-46 at the start, 101-104 at the end of the step) on
+// the reference's module variable uk: nh = [vxi1, vxi2, uk, s_pre, s_post, ...]; at the end the
+// step's calc_uk (uk_end) replaces uk first
+__global__ void k_nh_global(double *nh, const double *uk_end, int slot, double tau, double delt2, int L, double temp) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double uk = uk_end ? *uk_end : nh[2];
+    double v[2] = {nh[0], nh[1]};
+    nh[slot] = nh_half(v, uk, tau, delt2, L, temp);
+    nh[0] = v[0];
+    nh[1] = v[1];
+    nh[2] = uk;
+}
+
+// PPt = PPt * s (MD.f90:103)
+__global__ void k_nh_scale(double *PPt, size_t n, const double *s) {
+    const double f = *s;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        PPt[i] = __dmul_rn(PPt[i], f);
+}
+
+// write_out's inputs after the force call: calc_uk (main_stuff.f90:349-388, real-space or
+// normal-mode form) into sums[0] and the ring-spring sum K0 = sum m (r_k - r_(k-1))^2 of
+// simple_quantum_estimators (estimators.f90:57-73) into sums[1]; one group of 3P threads per atom
+__global__ void k_ring_sums(NMArgs a, const double *RRt, const double *PPt, double *sums) {
+    extern __shared__ double sh[];
+    const int P = a.P, G = blockDim.x / (3 * P);
+    const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
+    const int atom = blockIdx.x * G + g;
+    double *Cs = sh;
+    double *x = Cs + nm_ld(P) * P + g * 9 * P, *p = x + 3 * P;
+    if (a.nm_ke) nm_load_C(Cs, a.C, P);
+    const bool active = g < G && atom < a.natoms;
+    const size_t gi = (size_t)3 * a.natoms * j + 3 * atom + c;
+    if (active) {
+        x[3 * j + c] = RRt[gi];
+        p[3 * j + c] = PPt[gi];
+    }
+    __syncthreads();
+    double ke = 0.0, k0 = 0.0;
+    if (active) {
+        const double m = (atom % 3 == 0) ? a.massO : a.massH;
+        if (a.nm_ke) {
+            const double pt = nm_row(Cs, p, P, j, c, true);
+            ke = (1.0 / m) * pt * pt / a.A[4 * P + j];
+        } else {
+            ke = (1.0 / m) * p[3 * j + c] * p[3 * j + c];
+        }
+        const double d = x[3 * j + c] - x[3 * ((j + P - 1) % P) + c];
+        k0 = m * (d * d);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ke += __shfl_xor_sync(0xffffffffu, ke, o);
+        k0 += __shfl_xor_sync(0xffffffffu, k0, o);
+    }
+    __shared__ double wsum[2][32];
+    if ((threadIdx.x & 31) == 0) {
+        wsum[0][threadIdx.x >> 5] = ke;
+        wsum[1][threadIdx.x >> 5] = k0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t0 = 0.0, t1 = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            t0 += wsum[0][w];
+            t1 += wsum[1][w];
+        }
+        atomicAdd(sums, 0.5 * t0);
+        atomicAdd(sums + 1, t1);
+    }
+}
+
+// the step's outputs (PIMD_MD_NOUT): sums of the force call, uk, write_out's calc_uk and K0, and
+// the estimators of InputOutput.f90:566-571 / estimators.f90:30-96 with the reference's literal
+// types (1.5*Natoms and 1.5*Natoms*Nbeads are default-real products)
+__global__ void k_md_estimators(int P, int natoms, double volume, double omegan, const double *Upott,
+                                const double *virialt, const double *virialct, const double *uk,
+                                const double *sums, const double *s_post, double *out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double TEMPFACTOR = 0.80181484527, kb = 0.0019872041, PRESSCON2 = 69477.0, MASSCONi = 1.0 / 418.4;
+    double U = 0, v = 0, vc = 0;
+    for (int k = 0; k < P; k++) {
+        U += Upott[k];
+        v += virialt[k];
+        vc += virialct[k];
+    }
+    vc = vc / P;
+    const int Nw = natoms / 3;
+    const double ukm = sums[0], K0raw = sums[1];
+    const double sys_temp = TEMPFACTOR * ukm / (double)(natoms * P * P);
+    double KE = (double)(1.5f * (float)natoms) * kb * sys_temp;
+    const double qE = (KE + 0.5 * (v - vc) / P + U / P) / Nw;
+    const double qP = PRESSCON2 * (1 / (3 * volume)) * (2 * KE - vc / P) / Nw;
+    KE = (double)((1.5f * (float)natoms) * (float)P) * kb * sys_temp * P;
+    const double K0 = 0.5 * K0raw * (omegan * omegan) * MASSCONi;
+    out[0] = U;
+    out[1] = v;
+    out[2] = vc;
+    out[3] = *uk;
+    out[4] = ukm;
+    out[5] = K0raw;
+    out[6] = sys_temp;
+    out[7] = qE;
+    out[8] = qP;
+    out[9] = (KE - K0 + U) / (double)(Nw * P);
+    out[10] = PRESSCON2 * (1 / (3 * volume)) * (2 * (KE - K0) - v) / Nw;
+    out[11] = s_post ? *s_post : 1.0;
+}
+
 __global__ void k_md_sum(int P, const double *Upott, const double *virialt, const double *virialct, const double *uk,
                          double *out4) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -534,14 +707,16 @@ void nm_smem_optin(int P) {
     cudaFuncSetAttribute(k_md_post_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-// rows 7-9 of the device table (A12 / msf, A21 msf, c2 sqrt(msf)) from rows 1, 2, 4, 6
-void nm_extend_A(std::vector<double> &A, int P) {
-    A.resize(10 * (size_t)P);
+// rows 7-9 of the device table (A12 / msf, A21 msf, c2 sqrt(msf)) from rows 1, 2, 4, 6, and
+// row 10 the mode frequencies omegalist (the bead Nose-Hoover chains' 1/tau)
+void nm_extend_A(std::vector<double> &A, int P, const std::vector<double> &omegalist) {
+    A.resize(11 * (size_t)P);
     for (int j = 0; j < P; j++) {
         const double msf = A[4 * P + j];
         A[7 * P + j] = A[P + j] / msf;
         A[8 * P + j] = A[2 * P + j] * msf;
         A[9 * P + j] = A[6 * P + j] * std::sqrt(msf);
+        A[10 * P + j] = omegalist[j];
     }
 }
 
@@ -669,10 +844,16 @@ int pimd_nm_init(pimd_ctx *ctx, int P, double omegan, double delta, double setNM
         if (E.d_nmC) cudaFree(E.d_nmC);
         if (E.d_nmA) cudaFree(E.d_nmA);
         if (cudaMalloc((void **)&E.d_nmC, sizeof(double) * 2 * P * P) != cudaSuccess ||
-            cudaMalloc((void **)&E.d_nmA, sizeof(double) * 10 * P) != cudaSuccess)
+            cudaMalloc((void **)&E.d_nmA, sizeof(double) * 11 * P) != cudaSuccess)
             return PIMD_ERR_NOMEM;
         E.nm_P = P;
         nm_smem_optin(P);
+    }
+    if (!E.d_nh) {  // chain state and step sums: vxi_global = 1 (InputOutput.f90:397), uk = 0
+        if (cudaMalloc((void **)&E.d_nh, sizeof(double) * 8) != cudaSuccess) return PIMD_ERR_NOMEM;
+        E.allocs.push_back(E.d_nh);
+        const double init[8] = {1.0, 1.0, 0.0, 1.0, 1.0, 0.0, 0.0, 0.0};
+        cudaMemcpy(E.d_nh, init, sizeof init, cudaMemcpyHostToDevice);
     }
     std::vector<double> A(7 * P, 0.0);
     for (int j = 0; j < P; j++) {
@@ -689,8 +870,10 @@ int pimd_nm_init(pimd_ctx *ctx, int P, double omegan, double delta, double setNM
     std::vector<double> CP;
     nm_pair_copy(CC, CP);
     cudaMemcpy(E.d_nmC, CP.data(), sizeof(double) * CP.size(), cudaMemcpyHostToDevice);
-    nm_extend_A(A, P);
-    cudaMemcpy(E.d_nmA, A.data(), sizeof(double) * 10 * P, cudaMemcpyHostToDevice);
+    nm_extend_A(A, P, om);
+    cudaMemcpy(E.d_nmA, A.data(), sizeof(double) * 11 * P, cudaMemcpyHostToDevice);
+    E.nm_omegan = omegan;
+    E.nm_setfreq = setNMfreq;
     auto out = [&](double *dst, const std::vector<double> &v) {
         if (dst) std::memcpy(dst, v.data(), sizeof(double) * v.size());
     };
@@ -720,9 +903,9 @@ int pimd_langevin_init(pimd_ctx *ctx, double delt2, int centroid_thermostat, dou
         A[6 * P + i] = c2;
     }
     std::vector<double> Ad(A.begin(), A.begin() + 7 * P);
-    nm_extend_A(Ad, P);
+    nm_extend_A(Ad, P, std::vector<double>(om, om + P));
     cudaSetDevice(E.device);
-    return nm_err(E, cudaMemcpy(E.d_nmA, Ad.data(), sizeof(double) * 10 * P, cudaMemcpyHostToDevice), "langevin_init");
+    return nm_err(E, cudaMemcpy(E.d_nmA, Ad.data(), sizeof(double) * 11 * P, cudaMemcpyHostToDevice), "langevin_init");
 }
 
 int pimd_evolve_ring(pimd_ctx *ctx, double *RR, double *PP, int P, double mass) {
@@ -774,9 +957,10 @@ int pimd_langevin_nm_device(pimd_ctx *ctx, double *PPt, const double *xi, double
 }
 
 // Enqueue one PIMD_VV step on the context's stream (everything but the step word, which the
-// force call or the graph launcher sets).
+// force call or the graph launcher sets). out4: [Upot, virial, virialc, uk]; outx: the
+// PIMD_MD_NOUT outputs with write_out's calc_uk, K0 and the estimators (either may be null).
 static int md_step_enqueue(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
-                           double *RRc, const double *xi1, const double *xi2, int t, double *out4) {
+                           double *RRc, const double *xi1, const double *xi2, int t, double *out4, double *outx) {
     Engine &E = ctx->E;
     NMArgs a = nm_args(E, mp->massO, mp->massH);
     a.delt = mp->delt;
@@ -787,13 +971,33 @@ static int md_step_enqueue(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt,
     a.tstep = E.kp.dstep;
     a.phase = 0;
     a.xi = xi1;
-    a.fast = E.precision == PIMD_MIXED;
+    a.nm_ke = (E.nm_setfreq != 0 && E.kp.P > 1) ? 1 : 0;
+    a.bead_nh = E.nh_bead ? 1 : 0;
+    a.centroid_nh = E.nh_centroid ? 1 : 0;
+    a.tau_centroid = E.nh_tau_centroid;
+    a.nh_temp = E.nh_temp;
+    a.vxib = E.d_vxib;
+    // the FP32-pair kernels of the mixed engine carry PILE only: the chains and the normal-mode
+    // kinetic energy run in the exact kernels
+    a.fast = E.precision == PIMD_MIXED && !E.nh_bead && !E.nh_global && !a.nm_ke;
+    const int L = 3 * E.kp.natoms * E.kp.P;
     int threads, blocks;
     size_t smem;
     nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
     if (!E.capturing) launch_set_step(E, t);  // the Langevin counter of k_md_pre reads t
     timer_begin(E, "md_pre");
+    if (E.nh_global) {
+        k_nh_global<<<1, 32, 0, E.stream>>>(E.d_nh, nullptr, 3, E.nh_tau, a.delt2, L, E.nh_temp);
+        ++E.nlaunch;
+        a.s_pre = E.d_nh + 3;
+    }
     nm_launch_md_pre(a, E.stream, RRt, PPt, dRRt, RRc); ++E.nlaunch;
+    a.s_pre = nullptr;
+    if (outx) {
+        cudaMemsetAsync(E.d_nh + 5, 0, 2 * sizeof(double), E.stream);
+        k_ring_sums<<<blocks, threads, smem, E.stream>>>(a, RRt, PPt, E.d_nh + 5);
+        ++E.nlaunch;
+    }
     timer_end(E);
     KP saved = E.kp;
     E.kp.RRt = RRt;
@@ -811,8 +1015,25 @@ static int md_step_enqueue(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt,
     a.phase = 1;
     timer_begin(E, "md_post");
     nm_launch_md_post(a, E.stream, PPt, dRRt, uk); ++E.nlaunch;
+    const double *ukout = uk;
+    if (E.nh_global) {
+        k_nh_global<<<1, 32, 0, E.stream>>>(E.d_nh, uk, 4, E.nh_tau, a.delt2, L, E.nh_temp);
+        const size_t n = (size_t)3 * E.kp.natoms * E.kp.P;
+        k_nh_scale<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, E.stream>>>(PPt, n, E.d_nh + 4);
+        E.nlaunch += 2;
+        ukout = E.d_nh + 2;
+    } else if (E.d_nh) {
+        // the module variable uk follows calc_uk when no global chain runs (MD.f90:99)
+        cudaMemcpyAsync(E.d_nh + 2, uk, sizeof(double), cudaMemcpyDeviceToDevice, E.stream);
+    }
     if (out4) {
-        k_md_sum<<<1, 32, 0, E.stream>>>(E.kp.P, d, d + E.kp.P, d + 2 * E.kp.P, uk, out4);
+        k_md_sum<<<1, 32, 0, E.stream>>>(E.kp.P, d, d + E.kp.P, d + 2 * E.kp.P, ukout, out4);
+        ++E.nlaunch;
+    }
+    if (outx) {
+        k_md_estimators<<<1, 32, 0, E.stream>>>(E.kp.P, E.kp.natoms, E.kp.volume, E.nm_omegan, d, d + E.kp.P,
+                                                d + 2 * E.kp.P, ukout, E.d_nh + 5, E.nh_global ? E.d_nh + 4 : nullptr,
+                                                outx);
         ++E.nlaunch;
     }
     timer_end(E);
@@ -822,11 +1043,11 @@ static int md_step_enqueue(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt,
 // Graph mode: the step is captured once per set of buffers and parameters (the dipole loop as a
 // conditional while node) and replayed; only the step word is written before each launch.
 static int md_step_graph(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
-                         double *RRc, const double *xi1, const double *xi2, int t, double *out4) {
+                         double *RRc, const double *xi1, const double *xi2, int t, double *out4, double *outx) {
     Engine &E = ctx->E;
     double mpv[3] = {mp->delt, mp->massO, mp->massH};
-    std::vector<const void *> key = {RRt, PPt, dRRt, RRc, xi1, xi2, out4, (const void *)(size_t)mp->langevin,
-                                     (const void *)(size_t)mp->seed};
+    std::vector<const void *> key = {RRt, PPt, dRRt, RRc, xi1, xi2, out4, outx, (const void *)(size_t)mp->langevin,
+                                     (const void *)(size_t)mp->seed, (const void *)(size_t)E.nh_gen};
     for (double v : mpv) {
         unsigned long long u;
         std::memcpy(&u, &v, sizeof u);
@@ -844,7 +1065,7 @@ static int md_step_graph(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, d
         const bool timers_on = E.timers.on;
         E.timers.on = false;  // event records cannot sit inside a conditional body
         E.capturing = true;
-        int rc = md_step_enqueue(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, out4);
+        int rc = md_step_enqueue(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, out4, outx);
         E.capturing = false;
         E.timers.on = timers_on;
         cudaGraph_t g = nullptr;
@@ -868,14 +1089,89 @@ static int md_step_graph(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, d
     return nm_err(E, e, "graph launch");
 }
 
-int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,
-                        const double *xi1, const double *xi2, int t, double *out4) {
+static int md_step_any(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,
+                       const double *xi1, const double *xi2, int t, double *out4, double *outx) {
     if (!ctx || !mp || !RRt || !PPt || !dRRt || !RRc) return PIMD_ERR_ARG;
     Engine &E = ctx->E;
     if (E.nm_P != E.kp.P) return PIMD_ERR_STATE;
+    if (E.nh_bead && mp->langevin) {
+        E.last_error = "md_step: Langevin_NM and the bead Nose-Hoover chains exclude each other";
+        return PIMD_ERR_ARG;
+    }
     cudaSetDevice(E.device);
-    if (E.graph_mode) return md_step_graph(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, out4);
-    return md_step_enqueue(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, out4);
+    if (E.graph_mode) return md_step_graph(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, out4, outx);
+    return md_step_enqueue(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, out4, outx);
+}
+
+int pimd_md_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,
+                        const double *xi1, const double *xi2, int t, double *out4) {
+    return md_step_any(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, out4, nullptr);
+}
+
+int pimd_md_step_ex_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
+                           double *RRc, const double *xi1, const double *xi2, int t, double *out) {
+    if (!out) return PIMD_ERR_ARG;
+    return md_step_any(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, nullptr, out);
+}
+
+int pimd_set_thermostat(pimd_ctx *ctx, const pimd_thermostat *th) {
+    if (!ctx || !th) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    if (!E.nm_P || !E.d_nh) return PIMD_ERR_STATE;
+    if ((th->bead_thermostat != 0 && th->bead_thermostat != 2) || (th->global_thermostat && !(th->tau > 0)) ||
+        !(th->temp > 0) || (th->bead_thermostat == 2 && th->centroid_thermostat && !(th->tau_centroid > 0)))
+        return PIMD_ERR_ARG;
+    cudaSetDevice(E.device);
+    const int P = E.nm_P, na = E.kp.natoms;
+    if (th->bead_thermostat == 2 && P < 2) return PIMD_ERR_ARG;  // InputOutput.f90:258-264
+    if (th->bead_thermostat == 2 && !E.d_vxib) {
+        if (cudaMalloc((void **)&E.d_vxib, sizeof(double) * 6 * (size_t)na * P) != cudaSuccess) return PIMD_ERR_NOMEM;
+        E.allocs.push_back(E.d_vxib);
+        cudaMemset(E.d_vxib, 0, sizeof(double) * 6 * (size_t)na * P);  // vxi_beads = 0 (InputOutput.f90:400-403)
+    }
+    E.nh_global = th->global_thermostat != 0;
+    E.nh_bead = th->bead_thermostat == 2;
+    E.nh_centroid = E.nh_bead && th->centroid_thermostat != 0;
+    E.nh_tau = th->tau;
+    E.nh_temp = th->temp * P;  // MD.f90:44 and main_stuff.f90:157, 165 pass temp*Nbeads
+    E.nh_tau_centroid = th->tau_centroid;
+    E.nh_gen++;
+    return nm_err(E, cudaDeviceSynchronize(), "set_thermostat");
+}
+
+int pimd_get_thermostat_state(pimd_ctx *ctx, double *vxi_global, double *uk, double *vxi_beads) {
+    if (!ctx) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    if (!E.d_nh) return PIMD_ERR_STATE;
+    cudaSetDevice(E.device);
+    double h[8];
+    cudaError_t e = cudaStreamSynchronize(E.stream);
+    if (e == cudaSuccess) e = cudaMemcpy(h, E.d_nh, sizeof h, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return nm_err(E, e, "get_thermostat_state");
+    if (vxi_global) {
+        vxi_global[0] = h[0];
+        vxi_global[1] = h[1];
+    }
+    if (uk) *uk = h[2];
+    if (vxi_beads) {
+        if (!E.d_vxib) return PIMD_ERR_STATE;
+        e = cudaMemcpy(vxi_beads, E.d_vxib, sizeof(double) * 6 * (size_t)E.kp.natoms * E.nm_P, cudaMemcpyDeviceToHost);
+    }
+    return nm_err(E, e, "get_thermostat_state");
+}
+
+int pimd_set_thermostat_state(pimd_ctx *ctx, const double *vxi_global, double uk, const double *vxi_beads) {
+    if (!ctx) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    if (!E.d_nh) return PIMD_ERR_STATE;
+    if (vxi_beads && !E.d_vxib) return PIMD_ERR_STATE;
+    cudaSetDevice(E.device);
+    cudaError_t e = cudaStreamSynchronize(E.stream);
+    if (e == cudaSuccess && vxi_global) e = cudaMemcpy(E.d_nh, vxi_global, 2 * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(E.d_nh + 2, &uk, sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && vxi_beads)
+        e = cudaMemcpy(E.d_vxib, vxi_beads, sizeof(double) * 6 * (size_t)E.kp.natoms * E.nm_P, cudaMemcpyHostToDevice);
+    return nm_err(E, e, "set_thermostat_state");
 }
 
 int pimd_set_graph(pimd_ctx *ctx, int enable) {
@@ -899,15 +1195,15 @@ int pimd_graph_info(pimd_ctx *ctx, long long *captures, long long *launches) {
     return PIMD_OK;
 }
 
-int pimd_md_step(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,
-                 const double *xi1, const double *xi2, int t, double *out4) {
+static int md_step_host(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,
+                        const double *xi1, const double *xi2, int t, double *out, int nout) {
     if (!ctx || !mp || !RRt || !PPt || !dRRt) return PIMD_ERR_ARG;
     Engine &E = ctx->E;
     cudaSetDevice(E.device);
     const size_t n = (size_t)E.kp.P * E.kp.natoms * 3, nc = (size_t)E.kp.natoms * 3;
     if (!E.d_md) {
-        // device copies of the MD state: RRt, PPt, dRRt, RRc, xi1, xi2, out4
-        if (cudaMalloc((void **)&E.d_md, sizeof(double) * (5 * n + nc + 8)) != cudaSuccess) return PIMD_ERR_NOMEM;
+        // device copies of the MD state: RRt, PPt, dRRt, RRc, xi1, xi2, and the step's outputs
+        if (cudaMalloc((void **)&E.d_md, sizeof(double) * (5 * n + nc + 16)) != cudaSuccess) return PIMD_ERR_NOMEM;
         E.allocs.push_back(E.d_md);
     }
     double *dR = E.d_md, *dP = dR + n, *dG = dP + n, *dx1 = dG + n, *dx2 = dx1 + n, *dC = dx2 + n, *dO = dC + nc;
@@ -916,14 +1212,26 @@ int pimd_md_step(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *P
     cudaMemcpyAsync(dG, dRRt, sizeof(double) * n, cudaMemcpyHostToDevice, E.stream);
     if (xi1) cudaMemcpyAsync(dx1, xi1, sizeof(double) * n, cudaMemcpyHostToDevice, E.stream);
     if (xi2) cudaMemcpyAsync(dx2, xi2, sizeof(double) * n, cudaMemcpyHostToDevice, E.stream);
-    int rc = pimd_md_step_device(ctx, mp, dR, dP, dG, dC, xi1 ? dx1 : nullptr, xi2 ? dx2 : nullptr, t, dO);
+    int rc = md_step_any(ctx, mp, dR, dP, dG, dC, xi1 ? dx1 : nullptr, xi2 ? dx2 : nullptr, t,
+                         nout == 4 ? dO : nullptr, nout == 4 ? nullptr : dO);
     if (rc) return rc;
     cudaMemcpyAsync(RRt, dR, sizeof(double) * n, cudaMemcpyDeviceToHost, E.stream);
     cudaMemcpyAsync(PPt, dP, sizeof(double) * n, cudaMemcpyDeviceToHost, E.stream);
     cudaMemcpyAsync(dRRt, dG, sizeof(double) * n, cudaMemcpyDeviceToHost, E.stream);
     if (RRc) cudaMemcpyAsync(RRc, dC, sizeof(double) * nc, cudaMemcpyDeviceToHost, E.stream);
-    if (out4) cudaMemcpyAsync(out4, dO, sizeof(double) * 4, cudaMemcpyDeviceToHost, E.stream);
+    if (out) cudaMemcpyAsync(out, dO, sizeof(double) * nout, cudaMemcpyDeviceToHost, E.stream);
     return nm_err(E, cudaStreamSynchronize(E.stream), "md_step");
+}
+
+int pimd_md_step(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,
+                 const double *xi1, const double *xi2, int t, double *out4) {
+    return md_step_host(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, out4, 4);
+}
+
+int pimd_md_step_ex(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,
+                    const double *xi1, const double *xi2, int t, double *out) {
+    if (!out) return PIMD_ERR_ARG;
+    return md_step_host(ctx, mp, RRt, PPt, dRRt, RRc, xi1, xi2, t, out, PIMD_MD_NOUT);
 }
 
 }  // extern "C"

@@ -81,6 +81,11 @@ SIGNATURES = {
                         ctypes.c_double, _D, ctypes.c_int, _D, ctypes.c_int],
     "pimd_load_image": [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, _D, _D, _D,
                         _D, _D, _D, ctypes.c_int, _D, ctypes.c_int],
+    "pimd_set_thermostat": [_V, _V],
+    "pimd_get_thermostat_state": [_V, _D, _D, _D],
+    "pimd_set_thermostat_state": [_V, _D, ctypes.c_double, _D],
+    "pimd_md_step_ex_device": [_V, ctypes.POINTER(MDParams), _V, _V, _V, _V, _V, _V, ctypes.c_int, _V],
+    "pimd_md_step_ex": [_V, ctypes.POINTER(MDParams), _D, _D, _D, _D, _D, _D, ctypes.c_int, _D],
     "pimd_peak_flops": [ctypes.c_int, ctypes.c_int, _D],
     "pimd_set_graph": [_V, ctypes.c_int],
     "pimd_autotune": [_V, _V, _V],
@@ -155,6 +160,16 @@ def make_params(d, precision=PIMD_FP64, device=0):
     p.precision = int(d.get("precision", precision))
     p.device = int(d.get("device", device))
     return p
+
+
+class Thermostat(ctypes.Structure):
+    _fields_ = [("bead_thermostat", ctypes.c_int), ("global_thermostat", ctypes.c_int), ("tau", ctypes.c_double),
+                ("temp", ctypes.c_double), ("centroid_thermostat", ctypes.c_int), ("tau_centroid", ctypes.c_double)]
+
+
+MD_NOUT = 12
+MD_OUT_NAMES = ("Upot", "virial", "virialc", "uk", "uk_mid", "K0", "sys_temp", "E_virial", "P_virial", "E_simple",
+                "P_simple", "s_global")
 
 
 class Replica(ctypes.Structure):
@@ -313,6 +328,46 @@ class ForceEngine:
                                  int(t), _p(out))
         self._check(rc, "md_step")
         return out, RRc
+
+    def set_thermostat(self, bead_thermostat=0, global_thermostat=0, tau=0.1, temp=300.0, centroid_thermostat=0,
+                       tau_centroid=0.1):
+        """Nose-Hoover chains of the MD step (bead_thermostat 2: on the normal modes; global)."""
+        th = Thermostat(int(bead_thermostat), int(global_thermostat), float(tau), float(temp),
+                        int(centroid_thermostat), float(tau_centroid))
+        self._check(load().pimd_set_thermostat(self.h, ctypes.byref(th)), "set_thermostat")
+
+    def thermostat_state(self, beads=False):
+        vg = np.zeros(2)
+        uk = ctypes.c_double()
+        vb = np.zeros((3, self.P, self.natoms, 2)) if beads else None
+        self._check(load().pimd_get_thermostat_state(self.h, _p(vg), ctypes.byref(uk), _p(vb)), "thermostat_state")
+        return dict(vxi_global=vg, uk=uk.value, vxi_beads=vb)
+
+    def set_thermostat_state(self, vxi_global=None, uk=0.0, vxi_beads=None):
+        vg = None if vxi_global is None else _f64(vxi_global)
+        vb = None if vxi_beads is None else _f64(vxi_beads)
+        self._check(load().pimd_set_thermostat_state(self.h, _p(vg), float(uk), _p(vb)), "set_thermostat_state")
+
+    def md_step_ex(self, mp, RRt, PPt, dRRt, t, xi1=None, xi2=None):
+        """PIMD_VV on host arrays (in place) with the step's outputs and estimators by name."""
+        for a in (RRt, PPt, dRRt):
+            assert a.dtype == np.float64 and a.flags.c_contiguous
+        RRc = np.zeros((self.natoms, 3))
+        out = np.zeros(MD_NOUT)
+        x1 = _f64(xi1) if xi1 is not None else None
+        x2 = _f64(xi2) if xi2 is not None else None
+        rc = load().pimd_md_step_ex(self.h, ctypes.byref(mp), _p(RRt), _p(PPt), _p(dRRt), _p(RRc), _p(x1), _p(x2),
+                                    int(t), _p(out))
+        self._check(rc, "md_step_ex")
+        r = dict(zip(MD_OUT_NAMES, out.tolist()))
+        r["RRc"] = RRc
+        return r
+
+    def md_step_ex_device(self, mp, RRt, PPt, dRRt, RRc, t, out, xi1=0, xi2=0):
+        """pimd_md_step_ex_device on device buffers given as raw pointers (ints), stream-ordered."""
+        rc = load().pimd_md_step_ex_device(self.h, ctypes.byref(mp), RRt, PPt, dRRt, RRc, xi1 or None, xi2 or None,
+                                           int(t), out)
+        self._check(rc, "md_step_ex_device")
 
     def md_step_device(self, mp, RRt, PPt, dRRt, RRc, t, out4, xi1=0, xi2=0):
         """PIMD_VV on device buffers given as raw pointers (ints), stream-ordered."""

@@ -201,3 +201,44 @@ def test_full_bead_forces_threads_match_serial(pkg, orc):
         s = o.pot_ttm(c["RRt"][k], c["RRc"], bead=k)
         assert s["En"] == r["Upott"][k]
         assert np.array_equal(s["dRR"], r["dRRt"][k])
+
+
+def test_nose_hoover_half_step_is_time_reversible(orc):
+    """Nose_Hoover.f90:33-112 is a symmetric Trotter splitting: the half step with -delt2 undoes
+    the half step with +delt2 (chain velocities and uk back to their start), and s = e^(-vxi1 dt/2)."""
+    vxi = np.array([0.37, -0.21])
+    s, uk = orc.nose_hoover(250.0, vxi, 0.04, 1.25e-4, 960, 9600.0)
+    assert 0 < s < 2 and abs(uk - 250.0 * s * s) < 1e-12 * uk
+    s2, uk2 = orc.nose_hoover(uk, vxi, 0.04, -1.25e-4, 960, 9600.0)
+    assert np.allclose(vxi, [0.37, -0.21], rtol=0, atol=1e-14)
+    assert abs(uk2 - 250.0) < 1e-11 and abs(s * s2 - 1.0) < 1e-14
+
+
+def test_ring_k0_and_simple_estimator_on_free_rings(orc):
+    """K0 (estimators.f90:57-73) equals its normal-mode form sum m (omega_k / omega_n)^2 x_k^2, and on
+    free ring polymers drawn from the free-ring distribution at T (NormalModes.f90:224-250) the
+    simple (primitive) energy estimator averages 4.5 kb T per molecule, the classical kinetic
+    energy of three atoms."""
+    P, nat, T = 8, 30, 300.0
+    mO, mH = 15.9994, 1.008
+    omegan = 0.831447148 * T * P / 6.35077993041
+    nm = orc.nm_init(P, omegan, 2.5e-4)
+    C, om = nm["C"], nm["omegalist"]
+    m = np.where(np.arange(nat) % 3 == 0, mO, mH)
+    rng = np.random.default_rng(17)
+    kbT = 0.0019872041 * T
+    uk = T * nat * P * P / 0.80181484527  # sys_temp = T exactly
+    Es = []
+    for it in range(2000):
+        x = np.zeros((P, nat, 3))
+        for k in range(1, P):
+            x[k] = rng.standard_normal((nat, 3)) * np.sqrt(omegan * 6.35077993041 / (m[:, None] * om[k] ** 2))
+        R = np.einsum("kj,kac->jac", C, x)  # NM2real: r_j = sum_k C(k, j) x_k
+        K0 = orc.ring_k0(mO, mH, R)
+        if it == 0:
+            k0nm = sum((m[:, None] * (om[k] / omegan) ** 2 * x[k] ** 2).sum() for k in range(P))
+            assert abs(K0 - k0nm) < 1e-10 * K0
+        e = orc.estimators(nat, P, 1000.0, omegan, 0.0, 0.0, 0.0, uk, K0)
+        assert abs(e["sys_temp"] - T) < 1e-9
+        Es.append(e["E_simple"])
+    assert abs(np.mean(Es) / (4.5 * kbT) - 1.0) < 0.03
