@@ -108,6 +108,7 @@ def test_graph_step_with_chains_equals_eager(pkg, orc, engine_lib):
         outs = []
         for t in range(1, 6):
             eng.md_step_ex_device(mp, R.data_ptr(), Pm.data_ptr(), G.data_ptr(), Rc.data_ptr(), t, out.data_ptr())
+            torch.cuda.synchronize()  # the engine's own stream, not torch's current one
             outs.append(out.cpu().numpy().copy())
         torch.cuda.synchronize()
         runs.append((R.cpu().numpy(), Pm.cpu().numpy(), np.array(outs), eng.thermostat_state(beads=True)))
