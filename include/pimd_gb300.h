@@ -125,6 +125,20 @@ int pimd_set_dipole_check(pimd_ctx *ctx, int every);
 int pimd_nm_init(pimd_ctx *ctx, int nbeads, double omegan, double delta, double setNMfreq,
                  double *A11, double *A12, double *A21, double *A22, double *omegalist,
                  double *msf, double *C);
+/* real2NM and NM2real (NormalModes.f90:308-341) for one atom with the context's C: A(3,P) in,
+ * out(3,P) (host arrays, may not alias). */
+int pimd_real2nm(pimd_ctx *ctx, const double *A, double *out, int nbeads);
+int pimd_nm2real(pimd_ctx *ctx, const double *A, double *out, int nbeads);
+/* gen_rand_ring and gen_rand_ring_momenta (NormalModes.f90:224-275) for one atom, host RR(3,P) /
+ * PP(3,P) out, with the normal-mode frequencies and mass scale factors of pimd_nm_init. xi(3,P)
+ * holds the standard normal draws (the reference's rand_norm with unit deviation); NULL draws them
+ * from the context's own host generator (splitmix64, Box-Muller; the reference's Fortran
+ * random_number stream is not reproduced). gen_rand_ring takes the physical temperature;
+ * gen_rand_ring_momenta the temperature its caller passes (temp*Nbeads, main_stuff.f90:306). */
+int pimd_gen_rand_ring(pimd_ctx *ctx, double *RR, double mass, double temp, int nbeads,
+                       const double *xi);
+int pimd_gen_rand_ring_momenta(pimd_ctx *ctx, double *PP, double mass, double temp, int nbeads,
+                               const double *xi);
 /* EvolveRing (NormalModes.f90:34-63) for one atom, host arrays RR(3,P), PP(3,P) inout. */
 int pimd_evolve_ring(pimd_ctx *ctx, double *RR, double *PP, int nbeads, double mass);
 /* EvolveRing for every atom of RRt(3,Natoms,P)/PPt (MD.f90:53-58); device pointers. */

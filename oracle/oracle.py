@@ -103,6 +103,10 @@ def lib():
         L.orc_pool_forces.argtypes = [ctypes.c_void_p, D, D, D, D, D, D, ctypes.c_int]
         L.orc_pimd_vv_step_pool.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(MDParams),
                                             ctypes.c_int, D, D, D, D, D, D, ctypes.c_int, D, D, D, D]
+        L.orc_real2nm.argtypes = [ctypes.c_int, D, D, D]
+        L.orc_nm2real.argtypes = [ctypes.c_int, D, D, D]
+        L.orc_gen_rand_ring.argtypes = [ctypes.c_int, D, D, D, ctypes.c_double, ctypes.c_double, D, D]
+        L.orc_gen_rand_ring_momenta.argtypes = [ctypes.c_int, D, D, ctypes.c_double, ctypes.c_double, D, D]
         L.orc_nose_hoover.argtypes = [D, D, D, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double]
         L.orc_estimators.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 7 + [D]
         L.orc_ring_k0.restype = ctypes.c_double
@@ -370,3 +374,41 @@ def ring_k0(massO, massH, RRt):
     """estimators.f90:57-73: K0 = sum over beads, atoms, components of m (r_k - r_(k-1))^2."""
     RRt = _f64(RRt)
     return lib().orc_ring_k0(RRt.shape[0], RRt.shape[1], float(massO), float(massH), _p(RRt))
+
+
+def _colmajor(C):
+    return np.asfortranarray(C).ravel(order="F")
+
+
+def real2nm(nm, A):
+    """NormalModes.f90:308-324 for one atom: A (P, 3) -> (P, 3)."""
+    A = _f64(A)
+    out = np.zeros_like(A)
+    lib().orc_real2nm(A.shape[0], _p(_f64(_colmajor(nm["C"]))), _p(A), _p(out))
+    return out
+
+
+def nm2real(nm, A):
+    """NormalModes.f90:327-341 for one atom."""
+    A = _f64(A)
+    out = np.zeros_like(A)
+    lib().orc_nm2real(A.shape[0], _p(_f64(_colmajor(nm["C"]))), _p(A), _p(out))
+    return out
+
+
+def gen_rand_ring(nm, mass, temp, xi):
+    """NormalModes.f90:224-250 with unit normals xi (P, 3)."""
+    P = len(nm["msf"])
+    RR = np.zeros((P, 3))
+    lib().orc_gen_rand_ring(P, _p(_f64(_colmajor(nm["C"]))), _p(_f64(nm["omegalist"])), _p(_f64(nm["msf"])),
+                            float(mass), float(temp), _p(_f64(xi)), _p(RR))
+    return RR
+
+
+def gen_rand_ring_momenta(nm, mass, temp, xi):
+    """NormalModes.f90:257-275 with unit normals xi (P, 3)."""
+    P = len(nm["msf"])
+    PP = np.zeros((P, 3))
+    lib().orc_gen_rand_ring_momenta(P, _p(_f64(_colmajor(nm["C"]))), _p(_f64(nm["msf"])), float(mass), float(temp),
+                                    _p(_f64(xi)), _p(PP))
+    return PP

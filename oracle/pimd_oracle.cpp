@@ -1872,6 +1872,36 @@ static void NM2real(int P, const double *C, const double *A, double *out) {
             for (int c = 0; c < 3; c++) out[3 * j + c] = out[3 * j + c] + C[k + P * j] * A[3 * k + c];
 }
 
+// NormalModes.f90:308-341 real2NM / NM2real for one atom
+void orc_real2nm(int P, const double *C, const double *A, double *out) { real2NM(P, C, A, out); }
+void orc_nm2real(int P, const double *C, const double *A, double *out) { NM2real(P, C, A, out); }
+
+// NormalModes.f90:224-250 gen_rand_ring, rand_norm(std_dev) = std_dev * xi with xi(3,P) supplied
+void orc_gen_rand_ring(int P, const double *C, const double *omegalist, const double *msf, double mass, double temp,
+                       const double *xi, double *RR) {
+    const double hbar = 6.35077993041;
+    const double omegan = KB_AMU * temp * P / hbar;
+    std::vector<double> tr(3 * P, 0.0);
+    for (int j = 0; j < P; j++) {
+        const double omega = omegalist[j];
+        if (omega == 0.0) continue;
+        const double sd = std::sqrt((omegan * hbar) / (mass * msf[j] * (omega * omega)));
+        for (int c = 0; c < 3; c++) tr[3 * j + c] = sd * xi[3 * j + c];
+    }
+    NM2real(P, C, tr.data(), RR);
+}
+
+// NormalModes.f90:257-275 gen_rand_ring_momenta
+void orc_gen_rand_ring_momenta(int P, const double *C, const double *msf, double mass, double temp, const double *xi,
+                               double *PP) {
+    std::vector<double> tr(3 * P);
+    for (int j = 0; j < P; j++) {
+        const double sd = std::sqrt(KB_AMU * mass * msf[j] * temp);
+        for (int c = 0; c < 3; c++) tr[3 * j + c] = sd * xi[3 * j + c];
+    }
+    NM2real(P, C, tr.data(), PP);
+}
+
 // NormalModes.f90:34-63
 void orc_evolve_ring(int P, const double *A11, const double *A12, const double *A21, const double *A22,
                      const double *msf, const double *C, double *RR, double *PP, double mass) {

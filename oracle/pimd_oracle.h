@@ -111,6 +111,14 @@ void orc_pimd_vv_step_pool(void *h, void *pool, const orc_md_params *mp, int P, 
                            const double *xi2, int t, double *Upot, double *virial,
                            double *virialc, double *uk);
 
+/* NormalModes.f90:308-341 (real2NM, NM2real) and 224-275 (gen_rand_ring, gen_rand_ring_momenta
+ * with the unit normal draws xi(3,P) supplied) for one atom. */
+void orc_real2nm(int P, const double *C, const double *A, double *out);
+void orc_nm2real(int P, const double *C, const double *A, double *out);
+void orc_gen_rand_ring(int P, const double *C, const double *omegalist, const double *msf, double mass,
+                       double temp, const double *xi, double *RR);
+void orc_gen_rand_ring_momenta(int P, const double *C, const double *msf, double mass, double temp,
+                               const double *xi, double *PP);
 /* Nose_Hoover.f90:33-112 (one half step of a chain-2 thermostat), main_stuff.f90:145-171 (the
  * bead Nose-Hoover thermostat on the normal modes, vxi_beads(2,natoms,P,3)), estimators.f90:57-73
  * (ring K0) and estimators.f90:30-96 with InputOutput.f90:566 (sys_temp, virial-estimator energy

@@ -275,6 +275,8 @@ struct Engine {
     double *d_nmC = nullptr, *d_nmA = nullptr;  // C(P,P), [A11,A12,A21,A22,msf,c1,c2] x P
     std::vector<double> h_nm;                     // host copy: A11..A22, omegalist, msf, C
     double nm_omegan = 0, nm_setfreq = 0;         // InitNormalModes' omegan and setNMfreq
+    std::vector<double> h_nmC;                    // host copy of C(P,P), column-major
+    unsigned long long host_rng = 20261203ull;    // splitmix64 state of the host normal draws
     // Nose-Hoover thermostats of the MD step (pimd_set_thermostat): the global chain
     // (MD.f90:43-46, 101-104) and the bead chains on the normal modes (main_stuff.f90:145-171)
     bool nh_global = false, nh_bead = false, nh_centroid = false;

@@ -867,6 +867,7 @@ int pimd_nm_init(pimd_ctx *ctx, int P, double omegan, double delta, double setNM
     }
     E.h_nm = A;
     E.h_nm.insert(E.h_nm.end(), om.begin(), om.end());
+    E.h_nmC = CC;
     std::vector<double> CP;
     nm_pair_copy(CC, CP);
     cudaMemcpy(E.d_nmC, CP.data(), sizeof(double) * CP.size(), cudaMemcpyHostToDevice);
@@ -885,6 +886,83 @@ int pimd_nm_init(pimd_ctx *ctx, int P, double omegan, double delta, double setNM
     out(msf, ms);
     out(C, CC);
     return nm_err(E, cudaGetLastError(), "nm_init");
+}
+
+// real2NM / NM2real (NormalModes.f90:308-341) on the host: out(:,j) = sum_k C(j,k) A(:,k) (fwd)
+// or sum_k C(k,j) A(:,k), accumulated in k order as the reference's loops
+static void nm_host_transform(const std::vector<double> &C, int P, const double *A, double *out, bool fwd) {
+    std::vector<double> r(3 * (size_t)P, 0.0);
+    for (int j = 0; j < P; j++)
+        for (int k = 0; k < P; k++) {
+            const double c = fwd ? C[j + (size_t)P * k] : C[k + (size_t)P * j];
+            for (int x = 0; x < 3; x++) r[3 * j + x] = r[3 * j + x] + c * A[3 * k + x];
+        }
+    std::memcpy(out, r.data(), sizeof(double) * 3 * P);
+}
+
+// standard normal draws of the context's host generator (splitmix64 words, Box-Muller)
+static void host_normals(Engine &E, double *xi, int n) {
+    auto next = [&E]() {
+        unsigned long long z = (E.host_rng += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    for (int i = 0; i < n; i += 2) {
+        const double u1 = ((double)(next() >> 11) + 1.0) * 0x1.0p-53, u2 = (double)(next() >> 11) * 0x1.0p-53;
+        const double r = std::sqrt(-2.0 * std::log(u1));
+        xi[i] = r * std::cos(2.0 * PI * u2);
+        if (i + 1 < n) xi[i + 1] = r * std::sin(2.0 * PI * u2);
+    }
+}
+
+int pimd_real2nm(pimd_ctx *ctx, const double *A, double *out, int P) {
+    if (!ctx || !A || !out || P != ctx->E.nm_P || ctx->E.h_nmC.empty()) return PIMD_ERR_ARG;
+    nm_host_transform(ctx->E.h_nmC, P, A, out, true);
+    return PIMD_OK;
+}
+
+int pimd_nm2real(pimd_ctx *ctx, const double *A, double *out, int P) {
+    if (!ctx || !A || !out || P != ctx->E.nm_P || ctx->E.h_nmC.empty()) return PIMD_ERR_ARG;
+    nm_host_transform(ctx->E.h_nmC, P, A, out, false);
+    return PIMD_OK;
+}
+
+// gen_rand_ring (NormalModes.f90:224-250): the free ring polymer at temp -- normal mode j drawn with
+// standard deviation sqrt(omegan hbar / (mass msf_j omega_j^2)), omegan = kB temp Nbeads / hbar,
+// the centroid (omega = 0) at zero -- then NM2real
+int pimd_gen_rand_ring(pimd_ctx *ctx, double *RR, double mass, double temp, int P, const double *xi) {
+    if (!ctx || !RR || P != ctx->E.nm_P || ctx->E.h_nmC.empty() || !(mass > 0) || !(temp > 0)) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    std::vector<double> x(3 * (size_t)P), tr(3 * (size_t)P, 0.0);
+    if (xi) std::memcpy(x.data(), xi, sizeof(double) * 3 * P);
+    else host_normals(E, x.data(), 3 * P);
+    const double *om = E.h_nm.data() + 7 * (size_t)P, *msf = E.h_nm.data() + 4 * (size_t)P;
+    const double omegan = KB_AMU * temp * P / HBAR;
+    for (int j = 0; j < P; j++) {
+        if (om[j] == 0.0) continue;
+        const double sd = std::sqrt((omegan * HBAR) / (mass * msf[j] * (om[j] * om[j])));
+        for (int c = 0; c < 3; c++) tr[3 * j + c] = sd * x[3 * j + c];
+    }
+    nm_host_transform(E.h_nmC, P, tr.data(), RR, false);
+    return PIMD_OK;
+}
+
+// gen_rand_ring_momenta (NormalModes.f90:257-275): mode momenta with standard deviation
+// sqrt(kB mass msf_j temp) (the caller passes temp*Nbeads, main_stuff.f90:306), then NM2real
+int pimd_gen_rand_ring_momenta(pimd_ctx *ctx, double *PP, double mass, double temp, int P, const double *xi) {
+    if (!ctx || !PP || P != ctx->E.nm_P || ctx->E.h_nmC.empty() || !(mass > 0) || !(temp > 0)) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    std::vector<double> x(3 * (size_t)P), tr(3 * (size_t)P);
+    if (xi) std::memcpy(x.data(), xi, sizeof(double) * 3 * P);
+    else host_normals(E, x.data(), 3 * P);
+    const double *msf = E.h_nm.data() + 4 * (size_t)P;
+    for (int j = 0; j < P; j++) {
+        const double sd = std::sqrt(KB_AMU * mass * msf[j] * temp);
+        for (int c = 0; c < 3; c++) tr[3 * j + c] = sd * x[3 * j + c];
+    }
+    nm_host_transform(E.h_nmC, P, tr.data(), PP, false);
+    return PIMD_OK;
 }
 
 int pimd_langevin_init(pimd_ctx *ctx, double delt2, int centroid_thermostat, double tau_centroid, double temp_P) {

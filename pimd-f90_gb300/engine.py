@@ -68,6 +68,11 @@ SIGNATURES = {
     "pimd_nm_init": [_V, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, _D, _D, _D, _D, _D, _D,
                      _D],
     "pimd_evolve_ring": [_V, _D, _D, ctypes.c_int, ctypes.c_double],
+    "pimd_real2nm": [_V, _D, _D, ctypes.c_int],
+    "pimd_nm2real": [_V, _D, _D, ctypes.c_int],
+    "pimd_gen_rand_ring": [_V, _D, ctypes.c_double, ctypes.c_double, ctypes.c_int, _D],
+    "pimd_gen_rand_ring_momenta": [_V, _D, ctypes.c_double, ctypes.c_double, ctypes.c_int, _D],
+
     "pimd_evolve_all_device": [_V, _V, _V, ctypes.c_double, ctypes.c_double],
     "pimd_langevin_init": [_V, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_double],
     "pimd_langevin_nm_device": [_V, _V, _V, ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong,
@@ -300,6 +305,31 @@ class ForceEngine:
         RR, PP = _f64(RR).copy(), _f64(PP).copy()
         self._check(load().pimd_evolve_ring(self.h, _p(RR), _p(PP), RR.shape[0], float(mass)), "evolve_ring")
         return RR, PP
+
+    def real2nm(self, A):
+        A = _f64(A)
+        out = np.zeros_like(A)
+        self._check(load().pimd_real2nm(self.h, _p(A), _p(out), A.shape[0]), "real2nm")
+        return out
+
+    def nm2real(self, A):
+        A = _f64(A)
+        out = np.zeros_like(A)
+        self._check(load().pimd_nm2real(self.h, _p(A), _p(out), A.shape[0]), "nm2real")
+        return out
+
+    def gen_rand_ring(self, mass, temp, P, xi=None):
+        RR = np.zeros((P, 3))
+        x = None if xi is None else _f64(xi)
+        self._check(load().pimd_gen_rand_ring(self.h, _p(RR), float(mass), float(temp), int(P), _p(x)), "gen_rand_ring")
+        return RR
+
+    def gen_rand_ring_momenta(self, mass, temp, P, xi=None):
+        PP = np.zeros((P, 3))
+        x = None if xi is None else _f64(xi)
+        self._check(load().pimd_gen_rand_ring_momenta(self.h, _p(PP), float(mass), float(temp), int(P), _p(x)),
+                    "gen_rand_ring_momenta")
+        return PP
 
     def langevin_init(self, delt2, centroid_thermostat, tau, temp_P):
         rc = load().pimd_langevin_init(self.h, float(delt2), int(centroid_thermostat), float(tau), float(temp_P))

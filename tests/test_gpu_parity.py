@@ -215,3 +215,36 @@ def test_cell_list_neighbours_large_box(pkg, orc, engine_lib, precision):
     r = o.pot_ttm(c["RRt"][0], c["RRc"])
     tol = RTOL if precision == 0 else 1e-4
     assert rel(got["dRRt"][0], r["dRR"]) < tol
+
+
+@pytest.mark.parametrize("setNMfreq", [0.0, 1500.0])
+def test_normal_mode_helpers_bit_exact(pkg, orc, engine_lib, setNMfreq):
+    """real2NM / NM2real and gen_rand_ring / gen_rand_ring_momenta (NormalModes.f90:224-341)
+    through the C ABI, with the normal draws supplied: bit-identical to the oracle; with the
+    context's own draws: the mode deviations of the free-ring distribution."""
+    c, p = small_case(pkg, 3, nw=8, P=8)
+    eng = pkg.ForceEngine(p)
+    W = pkg.waterbox
+    for P in (8, 5):
+        omegan = W.KB_AMU * 300.0 * P / W.HBAR
+        eng.nm_init(P, omegan, 2.5e-4, setNMfreq)
+        nm = orc.nm_init(P, omegan, 2.5e-4, setNMfreq)
+        rng = np.random.default_rng(P)
+        A = rng.normal(size=(P, 3))
+        assert np.array_equal(eng.real2nm(A), orc.real2nm(nm, A))
+        assert np.array_equal(eng.nm2real(A), orc.nm2real(nm, A))
+        xi = rng.standard_normal((P, 3))
+        for m in (15.9994, 1.008):
+            assert np.array_equal(eng.gen_rand_ring(m, 300.0, P, xi), orc.gen_rand_ring(nm, m, 300.0, xi))
+            assert np.array_equal(eng.gen_rand_ring_momenta(m, 300.0 * P, P, xi),
+                                  orc.gen_rand_ring_momenta(nm, m, 300.0 * P, xi))
+        # the context's generator: normal-mode deviations sqrt(kB T P / (m msf omega_k^2)) and
+        # sqrt(kB m msf T P) within 10 % over 4000 rings
+        m = 1.008
+        R = np.array([eng.real2nm(eng.gen_rand_ring(m, 300.0, P)) for _ in range(4000)])
+        Pm = np.array([eng.real2nm(eng.gen_rand_ring_momenta(m, 300.0 * P, P)) for _ in range(4000)])
+        sdr = np.sqrt(W.KB_AMU * 300.0 * P / (m * nm["msf"][1:] * nm["omegalist"][1:] ** 2))
+        assert np.allclose(R[:, 1:].std(axis=(0, 2)), sdr, rtol=0.1)
+        assert np.abs(R[:, 0]).max() < 1e-12
+        assert np.allclose(Pm.std(axis=(0, 2)), np.sqrt(W.KB_AMU * m * nm["msf"] * 300.0 * P), rtol=0.1)
+    eng.close()
