@@ -213,6 +213,18 @@ int pimd_md_step_ex_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt,
 int pimd_md_step_ex(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
                     double *RRc, const double *xi1, const double *xi2, int t, double *out);
 
+/* Exact restart (no counterpart in the reference, whose .img image keeps 6 decimals and no
+ * predictor history): writes the MD state RRt, PPt, dRRt (3,Natoms,P) host arrays, the step
+ * index t of the last completed step, the Langevin seed, and the context state the next steps read
+ * -- each bead's dipole-predictor history and the Nose-Hoover chain state -- to a little-endian
+ * binary file; reading it into a context made with the same pimd_params (and thermostats) and
+ * continuing from step t + 1 reproduces the uninterrupted run. PIMD_ERR_ARG when the file's
+ * system (atoms, beads, model) or thermostats differ from the context's. Blocking. */
+int pimd_checkpoint_write(pimd_ctx *ctx, const char *path, const double *RRt, const double *PPt,
+                          const double *dRRt, int t, unsigned long long seed);
+int pimd_checkpoint_read(pimd_ctx *ctx, const char *path, double *RRt, double *PPt, double *dRRt,
+                         int *t, unsigned long long *seed);
+
 /* CUDA-graph execution of pimd_md_step_device / pimd_md_step (enable != 0). The whole step --
  * Langevin, kicks, EvolveRing, PBCs and the force call -- is captured on its first call and
  * replayed on later calls with the same buffers and parameters (a change of any pointer or

@@ -8,6 +8,8 @@
 // every product and sum rounded separately, so they are bit-identical to the FP64 oracle.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -1271,6 +1273,94 @@ int pimd_graph_info(pimd_ctx *ctx, long long *captures, long long *launches) {
     if (captures) *captures = ctx->E.graph_captures;
     if (launches) *launches = ctx->E.graph_launches;
     return PIMD_OK;
+}
+
+// ---- exact restart file ---------------------------------------------------------------------
+// Little-endian binary (the byte order of both host architectures this builds for):
+//   "PIMDCKPT", int32 version 1, int32 natoms, nbeads, pot_model, precision, sites S, t,
+//   flags (1: bead chains, 2: global chain), uint64 seed,
+//   RRt, PPt, dRRt (3 Natoms P doubles each), the predictor history (P x 4 x S x 3 doubles),
+//   the chain state [vxi1, vxi2, uk] and, with the bead chains, vxi_beads (6 Natoms P doubles).
+struct CkptHead {
+    char magic[8];
+    int32_t version, natoms, nbeads, pot_model, precision, sites, t, flags;
+    uint64_t seed;
+};
+
+int pimd_checkpoint_write(pimd_ctx *ctx, const char *path, const double *RRt, const double *PPt, const double *dRRt,
+                          int t, unsigned long long seed) {
+    if (!ctx || !path || !RRt || !PPt || !dRRt) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    cudaSetDevice(E.device);
+    const size_t n = (size_t)3 * E.kp.natoms * E.kp.P, nh = (size_t)E.kp.P * 4 * E.kp.S * 3;
+    const size_t nb = E.nh_bead && E.d_vxib ? (size_t)6 * E.kp.natoms * E.kp.P : 0;
+    std::vector<double> hist(nh), chain(3, 0.0), vb(nb);
+    cudaError_t e = cudaStreamSynchronize(E.stream);
+    if (e == cudaSuccess) e = cudaMemcpy(hist.data(), E.kp.txdip, sizeof(double) * nh, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && E.d_nh) e = cudaMemcpy(chain.data(), E.d_nh, sizeof(double) * 3, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && nb) e = cudaMemcpy(vb.data(), E.d_vxib, sizeof(double) * nb, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return nm_err(E, e, "checkpoint_write");
+    CkptHead h{};
+    std::memcpy(h.magic, "PIMDCKPT", 8);
+    h.version = 1;
+    h.natoms = E.kp.natoms;
+    h.nbeads = E.kp.P;
+    h.pot_model = E.kp.model;
+    h.precision = E.precision;
+    h.sites = E.kp.S;
+    h.t = t;
+    h.flags = (nb ? 1 : 0) | (E.nh_global ? 2 : 0);
+    h.seed = seed;
+    FILE *f = std::fopen(path, "wb");
+    if (!f) {
+        E.last_error = std::string("checkpoint_write: cannot open ") + path;
+        return PIMD_ERR_ARG;
+    }
+    bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 && std::fwrite(RRt, sizeof(double), n, f) == n &&
+              std::fwrite(PPt, sizeof(double), n, f) == n && std::fwrite(dRRt, sizeof(double), n, f) == n &&
+              std::fwrite(hist.data(), sizeof(double), nh, f) == nh && std::fwrite(chain.data(), sizeof(double), 3, f) == 3 &&
+              (nb == 0 || std::fwrite(vb.data(), sizeof(double), nb, f) == nb);
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) E.last_error = "checkpoint_write: write failed";
+    return ok ? PIMD_OK : PIMD_ERR_ARG;
+}
+
+int pimd_checkpoint_read(pimd_ctx *ctx, const char *path, double *RRt, double *PPt, double *dRRt, int *t,
+                         unsigned long long *seed) {
+    if (!ctx || !path || !RRt || !PPt || !dRRt) return PIMD_ERR_ARG;
+    Engine &E = ctx->E;
+    cudaSetDevice(E.device);
+    FILE *f = std::fopen(path, "rb");
+    if (!f) {
+        E.last_error = std::string("checkpoint_read: cannot open ") + path;
+        return PIMD_ERR_ARG;
+    }
+    CkptHead h{};
+    bool ok = std::fread(&h, sizeof h, 1, f) == 1 && std::memcmp(h.magic, "PIMDCKPT", 8) == 0 && h.version == 1;
+    if (ok && (h.natoms != E.kp.natoms || h.nbeads != E.kp.P || h.pot_model != E.kp.model || h.sites != E.kp.S ||
+               ((h.flags & 1) && !(E.nh_bead && E.d_vxib)))) {
+        E.last_error = "checkpoint_read: the file's system or thermostats differ from this context's";
+        std::fclose(f);
+        return PIMD_ERR_ARG;
+    }
+    const size_t n = (size_t)3 * E.kp.natoms * E.kp.P, nh = (size_t)E.kp.P * 4 * E.kp.S * 3;
+    const size_t nb = (h.flags & 1) ? (size_t)6 * E.kp.natoms * E.kp.P : 0;
+    std::vector<double> hist(nh), chain(3), vb(nb);
+    ok = ok && std::fread(RRt, sizeof(double), n, f) == n && std::fread(PPt, sizeof(double), n, f) == n &&
+         std::fread(dRRt, sizeof(double), n, f) == n && std::fread(hist.data(), sizeof(double), nh, f) == nh &&
+         std::fread(chain.data(), sizeof(double), 3, f) == 3 && (nb == 0 || std::fread(vb.data(), sizeof(double), nb, f) == nb);
+    std::fclose(f);
+    if (!ok) {
+        E.last_error = "checkpoint_read: not a complete checkpoint file of this format";
+        return PIMD_ERR_ARG;
+    }
+    cudaError_t e = cudaStreamSynchronize(E.stream);
+    if (e == cudaSuccess) e = cudaMemcpy(E.kp.txdip, hist.data(), sizeof(double) * nh, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && E.d_nh) e = cudaMemcpy(E.d_nh, chain.data(), sizeof(double) * 3, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nb) e = cudaMemcpy(E.d_vxib, vb.data(), sizeof(double) * nb, cudaMemcpyHostToDevice);
+    if (t) *t = h.t;
+    if (seed) *seed = h.seed;
+    return nm_err(E, e, "checkpoint_read");
 }
 
 static int md_step_host(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt, double *RRc,

@@ -86,6 +86,8 @@ SIGNATURES = {
                         ctypes.c_double, _D, ctypes.c_int, _D, ctypes.c_int],
     "pimd_load_image": [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, _D, _D, _D,
                         _D, _D, _D, ctypes.c_int, _D, ctypes.c_int],
+    "pimd_checkpoint_write": [_V, ctypes.c_char_p, _D, _D, _D, ctypes.c_int, ctypes.c_ulonglong],
+    "pimd_checkpoint_read": [_V, ctypes.c_char_p, _D, _D, _D, _I, ctypes.POINTER(ctypes.c_ulonglong)],
     "pimd_set_thermostat": [_V, _V],
     "pimd_get_thermostat_state": [_V, _D, _D, _D],
     "pimd_set_thermostat_state": [_V, _D, ctypes.c_double, _D],
@@ -377,6 +379,20 @@ class ForceEngine:
         vg = None if vxi_global is None else _f64(vxi_global)
         vb = None if vxi_beads is None else _f64(vxi_beads)
         self._check(load().pimd_set_thermostat_state(self.h, _p(vg), float(uk), _p(vb)), "set_thermostat_state")
+
+    def checkpoint_write(self, path, RRt, PPt, dRRt, t, seed):
+        RRt, PPt, dRRt = _f64(RRt), _f64(PPt), _f64(dRRt)
+        self._check(load().pimd_checkpoint_write(self.h, str(path).encode(), _p(RRt), _p(PPt), _p(dRRt), int(t),
+                                                 int(seed)), "checkpoint_write")
+
+    def checkpoint_read(self, path):
+        """(RRt, PPt, dRRt, t, seed) of an exact restart file; the context takes its state."""
+        shape = (self.P, self.natoms, 3)
+        RRt, PPt, dRRt = np.zeros(shape), np.zeros(shape), np.zeros(shape)
+        t, seed = ctypes.c_int(), ctypes.c_ulonglong()
+        self._check(load().pimd_checkpoint_read(self.h, str(path).encode(), _p(RRt), _p(PPt), _p(dRRt),
+                                                ctypes.byref(t), ctypes.byref(seed)), "checkpoint_read")
+        return RRt, PPt, dRRt, t.value, seed.value
 
     def md_step_ex(self, mp, RRt, PPt, dRRt, t, xi1=None, xi2=None):
         """PIMD_VV on host arrays (in place) with the step's outputs and estimators by name."""
