@@ -213,6 +213,31 @@ int pimd_md_step_ex_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt,
 int pimd_md_step_ex(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
                     double *RRc, const double *xi1, const double *xi2, int t, double *out);
 
+/* Ring-polymer contraction with multiple time steps (contracted_MD, MD.f90:276-449; mode 0) and
+ * monomer PIMD (monomer_PIMD, MD.f90:117-265; mode 1), TTM models: the NASA monomer PES acts on
+ * every bead, the intermolecular potential on the centroid alone (a one-bead context made by
+ * pimd_contracted_init with the context's parameters; contraction set in mode 0, so its pot_ttm
+ * skips the monomer PES, and unset in mode 1, which keeps it at the centroid as the reference
+ * does). Mode 0 runs intra_timesteps inner steps of fast kicks and EvolveRing per step: make the
+ * normal modes with pimd_nm_init(delta = delt / intra_timesteps) first (InputOutput.f90:382-386),
+ * and for mode 1 with delta = delt. Thermostats as pimd_md_step (PILE, the bead and global
+ * chains). */
+int pimd_contracted_init(pimd_ctx *ctx, int mode, int intra_timesteps);
+/* One step: RRt, PPt, dRRt (3,Natoms,P) inout, dRRfast (3,Natoms,P) inout in mode 0 (the
+ * reference's saved fast gradient; zero before the first step; unused in mode 1), RRc out,
+ * out[PIMD_MD_NOUT] as pimd_md_step_ex with Upot = sum of the beads' monomer energies + P times
+ * the centroid's potential, virial = monomer virial + the centroid's, virialc = monomer centroid
+ * virial / P + the centroid's; dip_momIt / dip_momEt (3,Nw,P) (may be NULL) as
+ * calc_monomer_dip_moments (force_calc.f90:205-264) plus the centroid's induced dipoles. Device
+ * variant: device pointers, stream-ordered; host variant: host arrays, blocking. */
+int pimd_contracted_step_device(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt,
+                                double *dRRt, double *dRRfast, double *RRc, const double *xi1,
+                                const double *xi2, int t, double *out, double *dip_momIt,
+                                double *dip_momEt);
+int pimd_contracted_step(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt,
+                         double *dRRt, double *dRRfast, double *RRc, const double *xi1,
+                         const double *xi2, int t, double *out, double *dip_momIt, double *dip_momEt);
+
 /* Exact restart (no counterpart in the reference, whose .img image keeps 6 decimals and no
  * predictor history): writes the MD state RRt, PPt, dRRt (3,Natoms,P) host arrays, the step
  * index t of the last completed step, the Langevin seed, and the context state the next steps read

@@ -107,6 +107,9 @@ def lib():
         L.orc_nm2real.argtypes = [ctypes.c_int, D, D, D]
         L.orc_gen_rand_ring.argtypes = [ctypes.c_int, D, D, D, ctypes.c_double, ctypes.c_double, D, D]
         L.orc_gen_rand_ring_momenta.argtypes = [ctypes.c_int, D, D, ctypes.c_double, ctypes.c_double, D, D]
+        L.orc_contracted_step.argtypes = [ctypes.c_void_p, ctypes.POINTER(MDParams), ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, D, D, D, D, D, D,
+                                          D, D, D, D, ctypes.c_int, D, D, D]
         L.orc_nose_hoover.argtypes = [D, D, D, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double]
         L.orc_estimators.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 7 + [D]
         L.orc_ring_k0.restype = ctypes.c_double
@@ -412,3 +415,26 @@ def gen_rand_ring_momenta(nm, mass, temp, xi):
     lib().orc_gen_rand_ring_momenta(P, _p(_f64(_colmajor(nm["C"]))), _p(_f64(nm["msf"])), float(mass), float(temp),
                                     _p(_f64(xi)), _p(PP))
     return PP
+
+
+def contracted_step(orc_c, md, mode, intra, RRt, PPt, dRRt, dRRfast, state, t=1, xi1=None, xi2=None,
+                    bead_thermostat=0, global_thermostat=0, tau=0.1, dipoles=False):
+    """contracted_MD (mode 0, MD.f90:276-449) / monomer_PIMD (mode 1, MD.f90:117-265); orc_c is a
+    one-bead Oracle of the centroid (contraction=1 in mode 0). Arrays updated in place."""
+    mp = _md_params(md)
+    P, na = RRt.shape[0], RRt.shape[1]
+    RRc = np.zeros(RRt.shape[1:])
+    out = np.zeros(MD_NOUT)
+    uk = ctypes.c_double(state["uk"])
+    x1 = _p(_f64(xi1)) if xi1 is not None else None
+    x2 = _p(_f64(xi2)) if xi2 is not None else None
+    dI = np.zeros((P, na // 3, 3)) if dipoles else None
+    dE = np.zeros((P, na // 3, 3)) if dipoles else None
+    lib().orc_contracted_step(orc_c.h, ctypes.byref(mp), int(mode), int(intra), int(bead_thermostat),
+                              int(global_thermostat), float(tau), P, _p(RRt), _p(PPt), _p(dRRt), _p(dRRfast), _p(RRc),
+                              x1, x2, _p(state["vxi_global"]), ctypes.byref(uk), _p(state["vxi_beads"]), int(t),
+                              _p(out), _p(dI), _p(dE))
+    state["uk"] = uk.value
+    r = dict(zip(MD_OUT_NAMES, out.tolist()))
+    r.update(RRc=RRc, dip_momIt=dI, dip_momEt=dE)
+    return r

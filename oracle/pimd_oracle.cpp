@@ -2209,4 +2209,197 @@ void orc_pimd_vv_step_ex(void *h, void *pool, const orc_md_params *mp, int bead_
     out[11] = s;
 }
 
+// Ring-polymer contraction with multiple time steps (MD.f90:276-449, contracted_MD; mode 0) and
+// monomer PIMD (MD.f90:117-265, monomer_PIMD; mode 1): the NASA monomer PES on every bead (fast,
+// intra_timesteps inner steps with the normal modes made for deltfast = delt/intra_timesteps in
+// mode 0), the intermolecular potential once on the centroid (h: an oracle of one bead with
+// contraction set in mode 0 and unset in mode 1, so that monomer_PIMD's centroid call keeps the
+// monomer PES as the reference's does). dRRfast (mode 0) persists across steps like the
+// reference's saved array. Thermostats and out[12] as orc_pimd_vv_step_ex; dip_momIt/dip_momEt
+// (3, Nw, P) from calc_monomer_dip_moments (force_calc.f90:205-264) plus the centroid's induced
+// dipoles (may be null).
+void orc_contracted_step(void *h, const orc_md_params *mp, int mode, int intra_timesteps, int bead_thermostat,
+                         int global_thermostat, double tau, int P, double *RRt, double *PPt, double *dRRt,
+                         double *dRRfast, double *RRc, const double *xi1, const double *xi2, double *vxi_global,
+                         double *uk_state, double *vxi_beads, int t, double *out, double *dip_momIt,
+                         double *dip_momEt) {
+    Orc *o = static_cast<Orc *>(h);
+    const int na = o->Natoms, nw = na / 3;
+    const double delt2 = mp->delt / 2.0;
+    const double deltfast = (mode == 0) ? mp->delt / intra_timesteps : mp->delt, delt2fast = deltfast / 2.0;
+    const double omegan = KB_AMU * mp->temp * P / 6.35077993041;
+    std::vector<double> A11(P), A12(P), A21(P), A22(P), om(P), msf(P), C(P * P), c1(P), c2(P);
+    // InputOutput.f90:382-386: the normal-mode propagator of the contracted run is made for deltfast
+    orc_nm_init(P, omegan, deltfast, mp->setNMfreq, A11.data(), A12.data(), A21.data(), A22.data(), om.data(),
+                msf.data(), C.data());
+    orc_langevin_init(P, om.data(), delt2, mp->centroid_thermostat, mp->tau_centroid, P * mp->temp, c1.data(),
+                      c2.data());
+    const size_t nall = (size_t)3 * na * P;
+    auto bead_thermostat_step = [&](const double *xi) {
+        if (bead_thermostat == 1 && xi)
+            orc_langevin_nm(P, na, C.data(), msf.data(), c1.data(), c2.data(), mp->massO, mp->massH, PPt, xi);
+        else if (bead_thermostat == 2)
+            orc_bead_nose_hoover(P, na, C.data(), om.data(), msf.data(), mp->massO, mp->massH, PPt, vxi_beads,
+                                 mp->centroid_thermostat, mp->tau_centroid, delt2, mp->temp);
+    };
+    auto centroid_pbc = [&]() {
+        for (int i = 0; i < 3 * na; i++) {
+            double sum = 0;
+            for (int j = 0; j < P; j++) sum += RRt[i + (size_t)3 * na * j];
+            RRc[i] = sum / P;
+        }
+        for (int i = 0; i < 3 * na; i++) {
+            const double shift = o->box[0] * anint(RRc[i] * o->boxi[0]);
+            RRc[i] = RRc[i] - shift;
+            for (int j = 0; j < P; j++) RRt[i + (size_t)3 * na * j] = RRt[i + (size_t)3 * na * j] - shift;
+        }
+    };
+    auto drift = [&](double dt) {
+        if (P > 1) {
+            std::vector<double> rr(3 * P), pp(3 * P);
+            for (int a = 0; a < na; a++) {
+                for (int j = 0; j < P; j++)
+                    for (int c = 0; c < 3; c++) {
+                        rr[3 * j + c] = RRt[3 * a + c + (size_t)3 * na * j];
+                        pp[3 * j + c] = PPt[3 * a + c + (size_t)3 * na * j];
+                    }
+                const double mass = (a % 3 == 0) ? mp->massO : mp->massH;
+                orc_evolve_ring(P, A11.data(), A12.data(), A21.data(), A22.data(), msf.data(), C.data(), rr.data(),
+                                pp.data(), mass);
+                for (int j = 0; j < P; j++)
+                    for (int c = 0; c < 3; c++) {
+                        RRt[3 * a + c + (size_t)3 * na * j] = rr[3 * j + c];
+                        PPt[3 * a + c + (size_t)3 * na * j] = pp[3 * j + c];
+                    }
+            }
+        } else {
+            const double imassO = 1.0 / mp->massO, imassH = 1.0 / mp->massH;
+            for (int a = 0; a < na; a++)
+                for (int c = 0; c < 3; c++)
+                    RRt[3 * a + c] = RRt[3 * a + c] + (a % 3 == 0 ? imassO : imassH) * PPt[3 * a + c] * dt;
+        }
+    };
+    // the monomer PES on every bead; with acc, its energies into Upott and the monomer virials
+    // (bead and centroid separations, min-imaged) into vir[0], vir[1]
+    std::vector<double> Upott(P, 0.0);
+    auto monomer = [&](double *g, bool acc, double *vir) {
+        for (int j = 0; j < P; j++)
+            for (int iw = 0; iw < nw; iw++) {
+                const double *rb = RRt + (size_t)3 * na * j + 9 * (size_t)iw;
+                double r1[3][3], dr1[3][3], e1;
+                for (int a = 0; a < 3; a++)
+                    for (int c = 0; c < 3; c++) r1[a][c] = rb[3 * a + c];
+                o->pot_nasa(r1, dr1, &e1);
+                double *gb = g + (size_t)3 * na * j + 9 * (size_t)iw;
+                for (int a = 0; a < 3; a++)
+                    for (int c = 0; c < 3; c++) gb[3 * a + c] = dr1[a][c];
+                if (!acc) continue;
+                Upott[j] = Upott[j] + e1;
+                for (int w = 0; w < 2; w++) {  // w 1: the centroid's separations, w 0: the bead's
+                    const double *rr = w ? RRc + 9 * (size_t)iw : rb;
+                    double roh1[3], roh2[3];
+                    for (int c = 0; c < 3; c++) {
+                        roh1[c] = rr[3 + c] - rr[c];
+                        roh1[c] = roh1[c] - o->box[c] * anint(roh1[c] * o->boxi[c]);
+                        roh2[c] = rr[6 + c] - rr[c];
+                        roh2[c] = roh2[c] - o->box[c] * anint(roh2[c] * o->boxi[c]);
+                    }
+                    vir[w] = vir[w] + (roh1[0] * dr1[1][0] + roh1[1] * dr1[1][1] + roh1[2] * dr1[1][2]);
+                    vir[w] = vir[w] + (roh2[0] * dr1[2][0] + roh2[1] * dr1[2][1] + roh2[2] * dr1[2][2]);
+                }
+            }
+    };
+    double s = 1.0;
+    bead_thermostat_step(xi1);
+    if (global_thermostat) {
+        orc_nose_hoover(&s, uk_state, vxi_global, tau, delt2, 3 * na * P, mp->temp * P);
+        for (size_t i = 0; i < nall; i++) PPt[i] = PPt[i] * s;
+    }
+    for (size_t i = 0; i < nall; i++) PPt[i] = PPt[i] - MASSCON * dRRt[i] * delt2;
+    double vir[2] = {0.0, 0.0};  // virialmon, virialcmon
+    std::vector<double> dRRmon(nall);
+    if (mode == 0) {
+        centroid_pbc();
+        for (int ti = 1; ti <= intra_timesteps; ti++) {
+            for (size_t i = 0; i < nall; i++) PPt[i] = PPt[i] - MASSCON * dRRfast[i] * delt2fast;
+            drift(deltfast);
+            vir[0] = vir[1] = 0.0;
+            monomer(dRRfast, ti == intra_timesteps, vir);
+            for (size_t i = 0; i < nall; i++) PPt[i] = PPt[i] - MASSCON * dRRfast[i] * delt2fast;
+        }
+        centroid_pbc();
+    } else {
+        drift(mp->delt);
+        centroid_pbc();
+    }
+    // the intermolecular (mode 0) or the full (mode 1) potential on the centroid
+    double Uc, vt[9], vcc;
+    std::vector<double> dRRc(3 * (size_t)na), dI(3 * (size_t)nw), dE(3 * (size_t)nw), chg(na);
+    o->pot_ttm(0, RRc, RRc, &Uc, dRRc.data(), vt, &vcc, dI.data(), dE.data(), chg.data(), t);
+    if (mode == 1) {  // Upott(:) = Upot, then the beads' monomer energies (MD.f90:179-198)
+        for (int j = 0; j < P; j++) Upott[j] = Uc;
+        monomer(dRRmon.data(), true, vir);
+    }
+    for (int j = 0; j < P; j++) {
+        if (mode == 0) Upott[j] = Upott[j] + Uc;  // MD.f90:400
+        for (int i = 0; i < 3 * na; i++)
+            dRRt[i + (size_t)3 * na * j] = mode == 0 ? dRRc[i] : dRRc[i] + dRRmon[i + (size_t)3 * na * j];
+    }
+    if (dip_momIt || dip_momEt) {  // calc_monomer_dip_moments + the centroid's induced dipoles
+        const double gammaM = o->m.gammaM, tmp = 0.5 * gammaM / (1.0 - gammaM);
+        for (int j = 0; j < P; j++)
+            for (int iw = 0; iw < nw; iw++) {
+                const double *rb = RRt + (size_t)3 * na * j + 9 * (size_t)iw;
+                double r1[3][3], q3[3], dq3[3][3][3];
+                for (int a = 0; a < 3; a++)
+                    for (int c = 0; c < 3; c++) r1[a][c] = rb[3 * a + c];
+                o->dms_nasa(r1, q3, dq3);
+                for (int a = 0; a < 3; a++) q3[a] = q3[a] * CHARGECON;
+                const double cH1 = q3[1] + tmp * (q3[1] + q3[2]), cH2 = q3[2] + tmp * (q3[1] + q3[2]);
+                double roh1[3], roh2[3], Rm[3], d[3];
+                for (int c = 0; c < 3; c++) {
+                    roh1[c] = rb[3 + c] - rb[c];
+                    roh1[c] = roh1[c] - o->box[c] * anint(roh1[c] * o->boxi[c]);
+                    roh2[c] = rb[6 + c] - rb[c];
+                    roh2[c] = roh2[c] - o->box[c] * anint(roh2[c] * o->boxi[c]);
+                }
+                if (o->p.pot_model == 3 || o->p.pot_model == 4) {
+                    for (int c = 0; c < 3; c++) Rm[c] = 0.5 * gammaM * (roh1[c] + roh2[c]) + rb[c];
+                    for (int c = 0; c < 3; c++) {
+                        double h1 = rb[3 + c] - Rm[c], h2 = rb[6 + c] - Rm[c];
+                        h1 = h1 - o->box[c] * anint(h1 * o->boxi[c]);
+                        h2 = h2 - o->box[c] * anint(h2 * o->boxi[c]);
+                        d[c] = cH1 * h1 + cH2 * h2;
+                    }
+                } else {
+                    for (int c = 0; c < 3; c++) d[c] = cH1 * roh1[c] + cH2 * roh2[c];
+                }
+                for (int c = 0; c < 3; c++) {
+                    if (dip_momIt) dip_momIt[c + 3 * (size_t)iw + (size_t)3 * nw * j] = d[c] + dE[3 * iw + c];
+                    if (dip_momEt) dip_momEt[c + 3 * (size_t)iw + (size_t)3 * nw * j] = dE[3 * iw + c];
+                }
+            }
+    }
+    double U = 0;
+    for (int j = 0; j < P; j++) U += Upott[j];
+    out[0] = U;
+    out[1] = vir[0] + vt[0] + vt[4] + vt[8];
+    out[2] = vir[1] / P + vcc;
+    out[4] = orc_calc_uk(P, na, mp->massO, mp->massH, PPt, mp->setNMfreq, C.data(), msf.data());
+    out[5] = orc_ring_k0(P, na, mp->massO, mp->massH, RRt);
+    orc_estimators(na, P, o->box[0] * o->box[1] * o->box[2], omegan, out[0], out[1], out[2], out[4], out[5], out + 6);
+    for (size_t i = 0; i < nall; i++) PPt[i] = PPt[i] - MASSCON * dRRt[i] * delt2;
+    bead_thermostat_step(xi2);
+    double ukv = orc_calc_uk(P, na, mp->massO, mp->massH, PPt, mp->setNMfreq, C.data(), msf.data());
+    s = 1.0;
+    *uk_state = ukv;
+    if (global_thermostat) {
+        orc_nose_hoover(&s, uk_state, vxi_global, tau, delt2, 3 * na * P, mp->temp * P);
+        for (size_t i = 0; i < nall; i++) PPt[i] = PPt[i] * s;
+        ukv = *uk_state;
+    }
+    out[3] = ukv;
+    out[11] = s;
+}
+
 }  // extern "C"

@@ -140,6 +140,14 @@ void orc_pimd_vv_step_ex(void *h, void *pool, const orc_md_params *mp, int bead_
                          double *vxi_global, double *uk_state, double *vxi_beads, int t,
                          double *out);
 
+/* contracted_MD (MD.f90:276-449, mode 0, intra_timesteps inner steps) and monomer_PIMD
+ * (MD.f90:117-265, mode 1): h is a one-bead oracle of the centroid (contraction set in mode 0). */
+void orc_contracted_step(void *h, const orc_md_params *mp, int mode, int intra_timesteps,
+                         int bead_thermostat, int global_thermostat, double tau, int P, double *RRt,
+                         double *PPt, double *dRRt, double *dRRfast, double *RRc, const double *xi1,
+                         const double *xi2, double *vxi_global, double *uk_state, double *vxi_beads,
+                         int t, double *out, double *dip_momIt, double *dip_momEt);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpimd_gb300.so")
 SOURCES = ["capi.cu", "neighbors.cu", "pot.cu", "ewald.cu", "mixed.cu", "nm.cu", "peak.cu", "noalloc.cu", "spc.cu",
-           "md_batch.cu", "adjoint.cu", "ewald_tc.cu", "state_io.cpp"]
+           "md_batch.cu", "adjoint.cu", "ewald_tc.cu", "contracted.cu", "state_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

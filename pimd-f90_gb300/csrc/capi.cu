@@ -653,6 +653,7 @@ int pimd_create(pimd_ctx **ctx, const pimd_params *p) {
     if (!ctx) return PIMD_ERR_ARG;
     *ctx = nullptr;
     pimd_ctx *c = new pimd_ctx();
+    if (p) c->params = *p;
     int rc = create(c->E, p, 1, nullptr);
     if (rc) {
         fprintf(stderr, "pimd_create: %s\n", c->E.last_error.c_str());
@@ -665,6 +666,7 @@ int pimd_create(pimd_ctx **ctx, const pimd_params *p) {
 
 int pimd_destroy(pimd_ctx *ctx) {
     if (!ctx) return PIMD_OK;
+    if (ctx->cen) pimd_destroy(ctx->cen);
     Engine &E = ctx->E;
     cudaSetDevice(E.device);
     if (E.stream) cudaStreamSynchronize(E.stream);

@@ -312,7 +312,14 @@ struct NMArgs {
     double *vxib;                       // vxi_beads(2, Natoms, P, 3)
     const double *s_pre;                // global chain's scale factor applied after the bead thermostat
     int nm_ke;                          // calc_uk in normal-mode space (setNMfreq != 0, P > 1)
+    int nodrift;                        // k_md_pre without the drift (contracted MD: the inner steps drift)
 };
+NMArgs nm_step_args(Engine &E, const pimd_md_params *mp, const double *xi1);
+void nm_launch_evolve(const NMArgs &a, cudaStream_t st, double *RRt, double *PPt);
+void nm_launch_ring_sums(const NMArgs &a, cudaStream_t st, const double *RRt, const double *PPt, double *sums);
+void nm_launch_nh_global(Engine &E, const double *uk_end, int slot, double delt2);
+void nm_launch_nh_scale(Engine &E, double *PPt);
+void nm_launch_estimators(Engine &E, const double *uk, const double *uvv, double *out);
 __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt, double *RRc);
 __global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk);
 __global__ void k_md_sum(int P, const double *Upott, const double *virialt, const double *virialct, const double *uk,
@@ -392,4 +399,10 @@ void launch_finish_spc(Engine &E);
 struct pimd_ctx {
     pimd::Engine E;
     int check_every = 1;  // host convergence check period of the dipole iterations
+    pimd_params params{};  // as created
+    // ring-polymer contraction / monomer PIMD (contracted.cu): a one-bead context of the
+    // centroid, the mode (0 contracted MTS, 1 monomer PIMD) and the inner steps, device scratch
+    pimd_ctx *cen = nullptr;
+    int con_mode = -1, con_intra = 0;
+    double *d_con = nullptr;
 };

@@ -428,7 +428,7 @@ __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt,
     if (active) p[3 * j + c] = __dsub_rn(p[3 * j + c], __dmul_rn(__dmul_rn(MASSCON, dRRt[gi]), a.delt2));
     __syncthreads();
     const double m = (atom % 3 == 0) ? a.massO : a.massH;
-    if (a.evolve) {
+    if (a.evolve && !a.nodrift) {
         double xt = 0, pt = 0;
         if (active) {
             xt = nm_row(Cs, x, P, j, c, true);
@@ -454,7 +454,7 @@ __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt,
             p[3 * j + c] = pr;
         }
         __syncthreads();
-    } else if (active) {
+    } else if (active && !a.nodrift) {
         x[3 * j + c] = __dadd_rn(x[3 * j + c], __dmul_rn(__dmul_rn(1.0 / m, p[3 * j + c]), a.delt));
     }
     __syncthreads();
@@ -637,16 +637,22 @@ __global__ void k_ring_sums(NMArgs a, const double *RRt, const double *PPt, doub
 // types (1.5*Natoms and 1.5*Natoms*Nbeads are default-real products)
 __global__ void k_md_estimators(int P, int natoms, double volume, double omegan, const double *Upott,
                                 const double *virialt, const double *virialct, const double *uk,
-                                const double *sums, const double *s_post, double *out) {
+                                const double *sums, const double *s_post, double *out, const double *uvv) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const double TEMPFACTOR = 0.80181484527, kb = 0.0019872041, PRESSCON2 = 69477.0, MASSCONi = 1.0 / 418.4;
     double U = 0, v = 0, vc = 0;
-    for (int k = 0; k < P; k++) {
-        U += Upott[k];
-        v += virialt[k];
-        vc += virialct[k];
+    if (uvv) {  // Upot, virial, virialc formed by the caller's step (contracted / monomer PIMD)
+        U = uvv[0];
+        v = uvv[1];
+        vc = uvv[2];
+    } else {
+        for (int k = 0; k < P; k++) {
+            U += Upott[k];
+            v += virialt[k];
+            vc += virialct[k];
+        }
+        vc = vc / P;
     }
-    vc = vc / P;
     const int Nw = natoms / 3;
     const double ukm = sums[0], K0raw = sums[1];
     const double sys_temp = TEMPFACTOR * ukm / (double)(natoms * P * P);
@@ -1036,12 +1042,12 @@ int pimd_langevin_nm_device(pimd_ctx *ctx, double *PPt, const double *xi, double
     return nm_err(E, cudaGetLastError(), "langevin_nm");
 }
 
-// Enqueue one PIMD_VV step on the context's stream (everything but the step word, which the
-// force call or the graph launcher sets). out4: [Upot, virial, virialc, uk]; outx: the
-// PIMD_MD_NOUT outputs with write_out's calc_uk, K0 and the estimators (either may be null).
-static int md_step_enqueue(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
-                           double *RRc, const double *xi1, const double *xi2, int t, double *out4, double *outx) {
-    Engine &E = ctx->E;
+}  // extern "C"
+
+namespace pimd {
+// The integrator kernels' arguments for one MD step of the context (first half: phase 0, the
+// pre-kick thermostat draws xi1)
+NMArgs nm_step_args(Engine &E, const pimd_md_params *mp, const double *xi1) {
     NMArgs a = nm_args(E, mp->massO, mp->massH);
     a.delt = mp->delt;
     a.delt2 = mp->delt / 2.0;
@@ -1060,6 +1066,45 @@ static int md_step_enqueue(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt,
     // the FP32-pair kernels of the mixed engine carry PILE only: the chains and the normal-mode
     // kinetic energy run in the exact kernels
     a.fast = E.precision == PIMD_MIXED && !E.nh_bead && !E.nh_global && !a.nm_ke;
+    return a;
+}
+
+// launchers for the contracted / monomer-PIMD step (contracted.cu)
+void nm_launch_evolve(const NMArgs &a, cudaStream_t st, double *RRt, double *PPt) {
+    int threads, blocks;
+    size_t smem;
+    nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
+    k_evolve<<<blocks, threads, smem, st>>>(a, RRt, PPt);
+}
+void nm_launch_ring_sums(const NMArgs &a, cudaStream_t st, const double *RRt, const double *PPt, double *sums) {
+    int threads, blocks;
+    size_t smem;
+    nm_launch_shape(a.P, a.natoms, &threads, &blocks, &smem);
+    cudaMemsetAsync(sums, 0, 2 * sizeof(double), st);
+    k_ring_sums<<<blocks, threads, smem, st>>>(a, RRt, PPt, sums);
+}
+void nm_launch_nh_global(Engine &E, const double *uk_end, int slot, double delt2) {
+    k_nh_global<<<1, 32, 0, E.stream>>>(E.d_nh, uk_end, slot, E.nh_tau, delt2, 3 * E.kp.natoms * E.kp.P, E.nh_temp);
+}
+void nm_launch_nh_scale(Engine &E, double *PPt) {
+    const size_t n = (size_t)3 * E.kp.natoms * E.kp.P;
+    k_nh_scale<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, E.stream>>>(PPt, n, E.d_nh + 4);
+}
+void nm_launch_estimators(Engine &E, const double *uk, const double *uvv, double *out) {
+    k_md_estimators<<<1, 32, 0, E.stream>>>(E.kp.P, E.kp.natoms, E.kp.volume, E.nm_omegan, nullptr, nullptr, nullptr,
+                                            uk, E.d_nh + 5, E.nh_global ? E.d_nh + 4 : nullptr, out, uvv);
+}
+}  // namespace pimd
+
+extern "C" {
+
+// Enqueue one PIMD_VV step on the context's stream (everything but the step word, which the
+// force call or the graph launcher sets). out4: [Upot, virial, virialc, uk]; outx: the
+// PIMD_MD_NOUT outputs with write_out's calc_uk, K0 and the estimators (either may be null).
+static int md_step_enqueue(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt, double *PPt, double *dRRt,
+                           double *RRc, const double *xi1, const double *xi2, int t, double *out4, double *outx) {
+    Engine &E = ctx->E;
+    NMArgs a = nm_step_args(E, mp, xi1);
     const int L = 3 * E.kp.natoms * E.kp.P;
     int threads, blocks;
     size_t smem;
@@ -1113,7 +1158,7 @@ static int md_step_enqueue(pimd_ctx *ctx, const pimd_md_params *mp, double *RRt,
     if (outx) {
         k_md_estimators<<<1, 32, 0, E.stream>>>(E.kp.P, E.kp.natoms, E.kp.volume, E.nm_omegan, d, d + E.kp.P,
                                                 d + 2 * E.kp.P, ukout, E.d_nh + 5, E.nh_global ? E.d_nh + 4 : nullptr,
-                                                outx);
+                                                outx, nullptr);
         ++E.nlaunch;
     }
     timer_end(E);

@@ -88,6 +88,10 @@ SIGNATURES = {
                         _D, _D, _D, ctypes.c_int, _D, ctypes.c_int],
     "pimd_checkpoint_write": [_V, ctypes.c_char_p, _D, _D, _D, ctypes.c_int, ctypes.c_ulonglong],
     "pimd_checkpoint_read": [_V, ctypes.c_char_p, _D, _D, _D, _I, ctypes.POINTER(ctypes.c_ulonglong)],
+    "pimd_contracted_init": [_V, ctypes.c_int, ctypes.c_int],
+    "pimd_contracted_step_device": [_V, ctypes.POINTER(MDParams), _V, _V, _V, _V, _V, _V, _V, ctypes.c_int, _V, _V,
+                                    _V],
+    "pimd_contracted_step": [_V, ctypes.POINTER(MDParams), _D, _D, _D, _D, _D, _D, _D, ctypes.c_int, _D, _D, _D],
     "pimd_set_thermostat": [_V, _V],
     "pimd_get_thermostat_state": [_V, _D, _D, _D],
     "pimd_set_thermostat_state": [_V, _D, ctypes.c_double, _D],
@@ -407,6 +411,27 @@ class ForceEngine:
         self._check(rc, "md_step_ex")
         r = dict(zip(MD_OUT_NAMES, out.tolist()))
         r["RRc"] = RRc
+        return r
+
+    def contracted_init(self, mode, intra_timesteps=1):
+        """Ring-polymer contraction with MTS (mode 0) or monomer PIMD (mode 1)."""
+        self._check(load().pimd_contracted_init(self.h, int(mode), int(intra_timesteps)), "contracted_init")
+
+    def contracted_step(self, mp, RRt, PPt, dRRt, dRRfast, t, xi1=None, xi2=None, dipoles=False):
+        """One contracted / monomer-PIMD step on host arrays (in place); outputs by name."""
+        for a in (RRt, PPt, dRRt) + (() if dRRfast is None else (dRRfast,)):
+            assert a.dtype == np.float64 and a.flags.c_contiguous
+        RRc = np.zeros((self.natoms, 3))
+        out = np.zeros(MD_NOUT)
+        dI = np.zeros((self.P, self.nw, 3)) if dipoles else None
+        dE = np.zeros((self.P, self.nw, 3)) if dipoles else None
+        x1 = _f64(xi1) if xi1 is not None else None
+        x2 = _f64(xi2) if xi2 is not None else None
+        rc = load().pimd_contracted_step(self.h, ctypes.byref(mp), _p(RRt), _p(PPt), _p(dRRt), _p(dRRfast), _p(RRc),
+                                         _p(x1), _p(x2), int(t), _p(out), _p(dI), _p(dE))
+        self._check(rc, "contracted_step")
+        r = dict(zip(MD_OUT_NAMES, out.tolist()))
+        r.update(RRc=RRc, dip_momIt=dI, dip_momEt=dE)
         return r
 
     def md_step_ex_device(self, mp, RRt, PPt, dRRt, RRc, t, out, xi1=0, xi2=0):
