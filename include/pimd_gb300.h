@@ -397,6 +397,45 @@ int pimd_load_image(const char *path, int natoms, int nbeads, double massO, doub
                     double *time, double *box, double *RRt, double *PPt, double *RRc,
                     double *vxi_beads, int n_vxi_beads, double *vxi_global, int n_vxi_global);
 
+/* ---------------------------------------------------------------------------------------
+ * Run analyses on the device (the reference's geometry_calculator.f90, diffusion_calculator.f90,
+ * spectral_properties.f90 with math.f90:42-140). Accumulating calls take device arrays of the
+ * context's system and are stream-ordered on its stream; reports are blocking.
+ */
+/* calc_geometry (geometry_calculator.f90:21-125) of one frame: centroid RRc(3,Natoms) and beads
+ * RRt(3,Natoms,P). reset clears the accumulator (allocates it on the first call). */
+int pimd_geometry_reset(pimd_ctx *ctx);
+int pimd_geometry_accumulate_device(pimd_ctx *ctx, const double *RRc, const double *RRt);
+/* write_out_geometry (:129-190): out[14] = average and RMS of the H-H distance, the O-H distance
+ * and the H-O-H angle (A, degrees) over the centroids, the same over the beads, then the largest
+ * centroid and bead O-H distances (the centroid one updated as the reference's lines 57-58 do).
+ * hist_c / hist_b [80][2] (may be NULL): write_out_histogram's (bin end, count / (2 num_total
+ * [Nbeads])); counts[176] (may be NULL): the raw accumulator, the reference's module variables
+ * in the order sum_HH, sum_OH, sum_HOH, their squares, the bead sums, max_OH, bmax_OH,
+ * num_total, warnings (O-H > 1.5 A), dOHhist(80), bdOHhist(80). */
+int pimd_geometry_report(pimd_ctx *ctx, double *out, double *hist_c, double *hist_b, double *counts);
+/* calc_diff_RMSD (diffusion_calculator.f90:14-58) of a run of num_timesteps frames: the mean
+ * square displacement every 20 frames of atom 3i (1-based) of each molecule, as the reference
+ * tracks it, from the centroids RRc(3,Natoms). */
+int pimd_msd_init(pimd_ctx *ctx, int num_timesteps);
+int pimd_msd_accumulate_device(pimd_ctx *ctx, const double *RRc);
+/* write_out_diffusion (:60-118): aMS[ntimes] (may be NULL), *ntimes (may be NULL) and out4 =
+ * {D, errD (10^-5 cm^2/s), slope, intercept} of the fit to the last half; timestep in ps. */
+int pimd_msd_report(pimd_ctx *ctx, double timestep, double *aMS, int *ntimes, double *out4);
+/* The spectra's time series (InputOutput.f90:680-688): per frame the total dipole in Debye from
+ * dip_momIt(3,Nw,P) (write_out's dip_mom) and the centroid velocities of the atoms the reference
+ * stores as "H" velocities (the first H and the O of each molecule, momenta over massH); either
+ * pointer may be NULL. init sets the capacity (frames) and clears the series. */
+int pimd_spectra_init(pimd_ctx *ctx, int max_steps, double massH);
+int pimd_spectra_record_device(pimd_ctx *ctx, const double *dip_momIt, const double *PPt);
+/* calc_infrared_spectrum (spectral_properties.f90:10-123) and calc_DOS (:128-187) of the series
+ * recorded so far, with the transforms by cuFFT in single precision; timestep in ps, temp in K.
+ * *npoints in: the reference's NumPointsOut (350 at the start of a run), out: the points written
+ * to freq (cm^-1) and ir / dos. The IR series is zero-padded where the reference's work array is
+ * left uninitialised. */
+int pimd_ir_spectrum(pimd_ctx *ctx, double timestep, double temp, int *npoints, double *freq, double *ir);
+int pimd_dos(pimd_ctx *ctx, double timestep, int *npoints, double *freq, double *dos);
+
 /* O-O half neighbour list of one bead without any device allocation. No counterpart in the
  * reference; it serves callers that must not let a library allocate device memory (drivers
  * that own all GPU memory through their own pool, applications with a fixed per-GPU budget,

@@ -110,6 +110,14 @@ def lib():
         L.orc_contracted_step.argtypes = [ctypes.c_void_p, ctypes.POINTER(MDParams), ctypes.c_int, ctypes.c_int,
                                           ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, D, D, D, D, D, D,
                                           D, D, D, D, ctypes.c_int, D, D, D]
+        F = ctypes.POINTER(ctypes.c_float)
+        L.orc_geometry_accumulate.argtypes = [D, ctypes.c_int, ctypes.c_int, D, D, D]
+        L.orc_geometry_report.argtypes = [D, ctypes.c_int, D]
+        L.orc_msd_step.argtypes = [D, ctypes.c_int, ctypes.c_int, D, D]
+        L.orc_msd_report.argtypes = [D, ctypes.c_int, ctypes.c_double, D]
+        L.orc_four1.argtypes = [F, ctypes.c_int, ctypes.c_int]
+        L.orc_ir_spectrum.argtypes = [F, ctypes.c_int, D, ctypes.c_double, ctypes.c_double, I, D, D]
+        L.orc_dos.argtypes = [F, ctypes.c_int, ctypes.c_int, ctypes.c_double, I, D, D]
         L.orc_nose_hoover.argtypes = [D, D, D, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_double]
         L.orc_estimators.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 7 + [D]
         L.orc_ring_k0.restype = ctypes.c_double
@@ -438,3 +446,68 @@ def contracted_step(orc_c, md, mode, intra, RRt, PPt, dRRt, dRRfast, state, t=1,
     r = dict(zip(MD_OUT_NAMES, out.tolist()))
     r.update(RRc=RRc, dip_momIt=dI, dip_momEt=dE)
     return r
+
+
+def _pf(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class Geometry:
+    """geometry_calculator.f90: calc_geometry per frame, write_out_geometry / write_out_histogram."""
+
+    def __init__(self, natoms, P, box):
+        self.acc = np.zeros(176)
+        self.natoms, self.P, self.box = natoms, P, _f64(box)
+
+    def accumulate(self, RRc, RRt):
+        lib().orc_geometry_accumulate(_p(self.acc), self.natoms, self.P, _p(self.box), _p(_f64(RRc)), _p(_f64(RRt)))
+
+    def report(self):
+        out = np.zeros(14)
+        lib().orc_geometry_report(_p(self.acc), self.P, _p(out))
+        return out
+
+
+class MSD:
+    """diffusion_calculator.f90: calc_diff_RMSD per frame and write_out_diffusion."""
+
+    def __init__(self, natoms, num_timesteps, box):
+        self.ntimes = int(np.floor(np.float32(num_timesteps) / np.float32(20)))
+        self.natoms = natoms
+        self.st = np.zeros(2 + self.ntimes + 1 + 2 * natoms)
+        self.box = _f64(box)
+
+    def step(self, RRc):
+        lib().orc_msd_step(_p(self.st), self.natoms, self.ntimes, _p(self.box), _p(_f64(RRc)))
+
+    def report(self, timestep):
+        out = np.zeros(4)
+        aMS = self.st[2:2 + self.ntimes].copy()
+        lib().orc_msd_report(_p(aMS), self.ntimes, float(timestep), _p(out))
+        return dict(aMS=aMS, D=out[0], errD=out[1], slope=out[2], intercept=out[3])
+
+
+def four1(z, isign):
+    """four1.f on a complex64 array (in place on a copy)."""
+    d = np.ascontiguousarray(np.asarray(z, np.complex64)).view(np.float32).copy()
+    lib().orc_four1(_pf(d), len(d) // 2, int(isign))
+    return d.view(np.complex64)
+
+
+def ir_spectrum(dip, box, timestep, temp, npoints=350):
+    """spectral_properties.f90 calc_infrared_spectrum; dip (tread, 3) float32 total dipoles (Debye)."""
+    d = np.ascontiguousarray(dip, np.float32)
+    n = ctypes.c_int(npoints)
+    f, v = np.zeros(npoints), np.zeros(npoints)
+    lib().orc_ir_spectrum(_pf(d), d.shape[0], _p(_f64(box)), float(timestep), float(temp), ctypes.byref(n), _p(f),
+                          _p(v))
+    return f[:n.value], v[:n.value]
+
+
+def dos(hvel, timestep, npoints=350):
+    """spectral_properties.f90 calc_DOS; hvel (nhyd, tread, 3) float32."""
+    h = np.ascontiguousarray(hvel, np.float32)
+    n = ctypes.c_int(npoints)
+    f, v = np.zeros(npoints), np.zeros(npoints)
+    lib().orc_dos(_pf(h), h.shape[1], h.shape[0], float(timestep), ctypes.byref(n), _p(f), _p(v))
+    return f[:n.value], v[:n.value]

@@ -2402,4 +2402,314 @@ void orc_contracted_step(void *h, const orc_md_params *mp, int mode, int intra_t
     out[11] = s;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Analysis (geometry_calculator.f90, diffusion_calculator.f90, spectral_properties.f90, four1.f,
+// math.f90:42-140). Geometry accumulator layout (ORC_GEOM_N doubles): [0..5] sum_HH, sum_OH,
+// sum_HOH, sum_HH2, sum_OH2, sum_HOH2; [6..11] the bead sums in the same order; [12] max_OH,
+// [13] bmax_OH, [14] num_total, [15] num_warn, [16..95] dOHhist, [96..175] bdOHhist.
+static const double GEO_MIN = (double)0.6f, GEO_MAX = (double)1.6f;  // default-real literals .6 and 1.6
+static const int GEO_NB = 80;
+
+// geometry_calculator.f90:235-259 binit (normal binning)
+static void geo_binit(double *hist, double x) {
+    const double delta = (GEO_MAX - GEO_MIN) / GEO_NB;
+    if (x > GEO_MIN && x < GEO_MAX) {
+        int bin = (int)anint((x - GEO_MIN) / delta);
+        if (bin == 0) bin = 1;
+        if (bin > GEO_NB) bin = GEO_NB;
+        hist[bin - 1] = hist[bin - 1] + 1;
+    }
+}
+
+// geometry_calculator.f90:21-125 calc_geometry: centroid and bead O-H / H-H distances, H-O-H
+// angles, running sums, maxima (the centroid maximum takes d_OH1 when d_OH2 exceeds it, as the
+// reference's line does), dOH histograms; warnings counted, not printed
+void orc_geometry_accumulate(double *acc, int natoms, int P, const double *box, const double *RR, const double *RRt) {
+    const int nw = natoms / 3;
+    const double dOHmax = 1.5;
+    double boxi[3] = {1.0 / box[0], 1.0 / box[1], 1.0 / box[2]};
+    auto dist = [&](const double *a, const double *b, double *v) {
+        for (int c = 0; c < 3; c++) {
+            v[c] = a[c] - b[c];
+            v[c] = v[c] - box[c] * anint(v[c] * boxi[c]);
+        }
+    };
+    for (int pass = 0; pass <= P; pass++) {  // pass 0: the centroid; 1..P: the beads
+        const double *X = pass == 0 ? RR : RRt + (size_t)3 * natoms * (pass - 1);
+        double *sm = acc + (pass == 0 ? 0 : 6);
+        for (int i = 0; i < nw; i++) {
+            const double *rO = X + 9 * (size_t)i, *rH2 = rO + 3, *rH1 = rO + 6;  // ih1 = 3i, ih2 = 3i-1
+            double ROH1[3], ROH2[3], RHH[3];
+            dist(rO, rH1, ROH1);
+            dist(rO, rH2, ROH2);
+            dist(rH2, rH1, RHH);
+            const double dHH = std::sqrt(RHH[0] * RHH[0] + RHH[1] * RHH[1] + RHH[2] * RHH[2]);
+            const double d1 = std::sqrt(ROH1[0] * ROH1[0] + ROH1[1] * ROH1[1] + ROH1[2] * ROH1[2]);
+            const double d2 = std::sqrt(ROH2[0] * ROH2[0] + ROH2[1] * ROH2[1] + ROH2[2] * ROH2[2]);
+            const double dHOH = std::acos((d1 * d1 + d2 * d2 - dHH * dHH) / (2.0 * d1 * d2));
+            if (d1 > dOHmax) acc[15] += 1;
+            if (d2 > dOHmax) acc[15] += 1;
+            if (pass == 0) {
+                if (d1 > acc[12]) acc[12] = d1;
+                if (d2 > acc[12]) acc[12] = d1;
+                geo_binit(acc + 16, d1);
+                geo_binit(acc + 16, d2);
+            } else {
+                if (d1 > acc[13]) acc[13] = d1;
+                if (d2 > acc[13]) acc[13] = d2;
+                geo_binit(acc + 96, d1);
+                geo_binit(acc + 96, d2);
+            }
+            sm[0] = sm[0] + dHH;
+            sm[1] = sm[1] + d1 + d2;
+            if (pass == 0 || std::fabs(dHOH) > 0) sm[2] = sm[2] + dHOH;
+            sm[3] = sm[3] + dHH * dHH;
+            sm[4] = sm[4] + d1 * d1 + d2 * d2;
+            sm[5] = sm[5] + dHOH * dHOH;
+        }
+    }
+    acc[14] += nw;
+}
+
+// geometry_calculator.f90:129-190 write_out_geometry: averages and RMS (degrees for angles)
+// out[14]: avg_HH, RMS_HH, avg_OH, RMS_OH, avg_HOH, RMS_HOH, then the bead ones, max_OH, bmax_OH
+void orc_geometry_report(const double *acc, int P, double *out) {
+    const double nt = acc[14], bn = nt * P, deg = 180.0 / 3.141592;
+    for (int b = 0; b < 2; b++) {
+        const double *sm = acc + 6 * b;
+        const double n = b ? bn : nt;
+        const double aHH = sm[0] / n, aOH = sm[1] / (2.0 * n), aHOH = (sm[2] / n) * deg;
+        const double aHH2 = sm[3] / n, aOH2 = sm[4] / (2.0 * n), aHOH2 = (sm[5] / n) * (deg * deg);
+        out[6 * b + 0] = aHH;
+        out[6 * b + 1] = std::sqrt(aHH2 - aHH * aHH);
+        out[6 * b + 2] = aOH;
+        out[6 * b + 3] = std::sqrt(aOH2 - aOH * aOH);
+        out[6 * b + 4] = aHOH;
+        out[6 * b + 5] = std::sqrt(aHOH2 - aHOH * aHOH);
+    }
+    out[12] = acc[12];
+    out[13] = acc[13];
+}
+
+// diffusion_calculator.f90:14-58 calc_diff_RMSD: state = [t, initialised, aMS(ntimes + 1),
+// netdisp(3 Nw), Oxy(3 Nw)]; the tracked atom of molecule ia is atom 3 ia (1-based), as the
+// reference's Oxy2(:,ia) = RRc(:,3*ia) takes it
+void orc_msd_step(double *st, int natoms, int ntimes, const double *box, const double *RRc) {
+    const int nw = natoms / 3, t_out = 20;
+    double *aMS = st + 2, *net = aMS + ntimes + 1, *Oxy = net + 3 * nw;
+    const double boxi0 = 1.0 / box[0];
+    st[0] += 1;
+    if (st[1] == 0) {
+        st[0] = 0;
+        st[1] = 1;
+        for (int i = 0; i < nw; i++)
+            for (int c = 0; c < 3; c++) Oxy[3 * i + c] = RRc[3 * (3 * i + 2) + c];
+    }
+    const int t = (int)st[0];
+    for (int i = 0; i < nw; i++)
+        for (int c = 0; c < 3; c++) {
+            const double o2 = RRc[3 * (3 * i + 2) + c];
+            double d = o2 - Oxy[3 * i + c];
+            d = d - box[0] * anint(d * boxi0);
+            net[3 * i + c] = net[3 * i + c] + d;
+            Oxy[3 * i + c] = o2;
+        }
+    if (t % t_out == 0) {
+        const int ti = t / t_out + 1;
+        if (ti <= ntimes + 1) {
+            for (int i = 0; i < nw; i++)
+                aMS[ti - 1] = aMS[ti - 1] + (net[3 * i] * net[3 * i] + net[3 * i + 1] * net[3 * i + 1] +
+                                             net[3 * i + 2] * net[3 * i + 2]);
+            aMS[ti - 1] = aMS[ti - 1] / nw;
+        }
+    }
+}
+
+// diffusion_calculator.f90:60-118 write_out_diffusion: least squares over the last half of
+// aMS(t) with the reference's single-precision times and its (ntimesfit - 1) divisors; out[4] =
+// D, errD (10^-5 cm^2/s), slope b, intercept a
+void orc_msd_report(const double *aMS, int ntimes, double timestep, double *out) {
+    const int t_out = 20;
+    const float frac = 0.5f;
+    std::vector<float> times(ntimes);
+    for (int i = 1; i <= ntimes; i++) times[i - 1] = (float)(i * t_out * timestep);
+    const int ft = (int)std::floor(frac * ntimes) + 1;
+    const int nfit = ntimes - ft;
+    double xbar = 0, ybar = 0, sx = 0, sy = 0, cr = 0;
+    for (int i = ft; i <= ntimes; i++) xbar += (double)(times[i - 1] / (float)(nfit - 1));
+    for (int i = ft; i <= ntimes; i++) ybar += aMS[i - 1] / (nfit - 1);
+    for (int i = ft; i <= ntimes; i++) {
+        sx += ((double)times[i - 1] - xbar) * ((double)times[i - 1] - xbar);
+        sy += (aMS[i - 1] - ybar) * (aMS[i - 1] - ybar);
+        cr += (aMS[i - 1] - ybar) * ((double)times[i - 1] - xbar);
+    }
+    const double b = cr / sx, a = ybar - b * xbar;
+    double errb = (sy / sx - b * b) / (nfit - 2);
+    errb = std::sqrt(errb);
+    out[0] = 10 * b / 6;
+    out[1] = errb / 6;
+    out[2] = b;
+    out[3] = a;
+}
+
+// four1.f (Numerical Recipes): in-place FFT of nn complex REAL values, twiddles by the DOUBLE
+// recurrence; isign = 1: exp(+2 pi i jk / nn), -1: exp(-...)
+void orc_four1(float *data, int nn, int isign) {
+    const int n = 2 * nn;
+    int j = 1;
+    for (int i = 1; i <= n; i += 2) {
+        if (j > i) {
+            std::swap(data[j - 1], data[i - 1]);
+            std::swap(data[j], data[i]);
+        }
+        int m = n / 2;
+        while (m >= 2 && j > m) {
+            j -= m;
+            m /= 2;
+        }
+        j += m;
+    }
+    int mmax = 2;
+    while (n > mmax) {
+        const int istep = 2 * mmax;
+        const double theta = 6.28318530717959 / (isign * mmax);
+        const double st = std::sin(0.5 * theta);
+        const double wpr = -2.0 * st * st, wpi = std::sin(theta);
+        double wr = 1.0, wi = 0.0;
+        for (int m = 1; m <= mmax; m += 2) {
+            for (int i = m; i <= n; i += istep) {
+                const int jj = i + mmax;
+                const float tr = (float)wr * data[jj - 1] - (float)wi * data[jj];
+                const float ti = (float)wr * data[jj] + (float)wi * data[jj - 1];
+                data[jj - 1] = data[i - 1] - tr;
+                data[jj] = data[i] - ti;
+                data[i - 1] = data[i - 1] + tr;
+                data[i] = data[i] + ti;
+            }
+            const double wt = wr;
+            wr = wr * wpr - wi * wpi + wr;
+            wi = wi * wpr + wt * wpi + wi;
+        }
+        mmax = istep;
+    }
+}
+
+static int pow2_floor_log(int n, int add) { return 1 << ((int)std::floor(std::log((double)n) / std::log(2.0)) + add); }
+
+// math.f90:45-81 calc_corr_function (zero-padded to 2 trun, trun = 2^(floor(log2 tread) + 1);
+// lag i - 1 of output(i) divided by tread - i for i < tread)
+void orc_corr_function(const float *in, int tread, double *out) {
+    const int trun = pow2_floor_log(tread, 1);
+    std::vector<float> tr(4 * (size_t)trun, 0.0f);
+    for (int i = 0; i < tread; i++) tr[2 * i] = in[i];
+    orc_four1(tr.data(), 2 * trun, 1);
+    for (int i = 0; i < 2 * trun; i++) {
+        const float re = tr[2 * i], im = tr[2 * i + 1];
+        tr[2 * i] = re * re + im * im;  // z conj(z)
+        tr[2 * i + 1] = 0.0f;
+    }
+    orc_four1(tr.data(), 2 * trun, -1);
+    for (int i = 0; i < tread; i++) out[i] = (double)tr[2 * i];
+    for (int i = 1; i <= tread - 1; i++) out[i - 1] = out[i - 1] / (tread - i);
+}
+
+// math.f90:88-116 calc_DFT
+void orc_calc_dft(const double *in, int tread, double timestep, double *out, double *freqs) {
+    const int trun = pow2_floor_log(tread, 1);
+    std::vector<float> tr(4 * (size_t)trun, 0.0f);
+    for (int i = 0; i < tread; i++) tr[2 * i] = (float)in[i];
+    orc_four1(tr.data(), 2 * trun, 1);
+    for (int i = 0; i < tread; i++) out[i] = (double)tr[2 * i] / (2.0 * trun);
+    for (int i = 0; i < tread; i++) freqs[i] = (double)i / (timestep * 2.0 * trun);
+}
+
+// math.f90:123-140 block_average
+static void block_average(const double *in, int n, int N, double *out) {
+    const int bs = (int)std::floor((float)n / (float)N);
+    if (bs == 0) {
+        for (int i = 0; i < N && i < n; i++) out[i] = in[i];
+        return;
+    }
+    for (int i = 0; i < N; i++) {
+        double s = 0;
+        for (int k = i * bs; k < (i + 1) * bs; k++) s += in[k];
+        out[i] = s / bs;
+    }
+}
+
+// spectral_properties.f90:10-123 calc_infrared_spectrum from the total dipole dip(3, tread)
+// (REAL, Debye): the autocorrelation by FFT over 2 trun points (trun = 2^floor(log2 tread); the
+// first trun samples, zero-padded -- the reference leaves the padding uninitialised), its FFT, and
+// the omega^2-weighted, block-averaged line shape up to 7000 cm^-1. npoints inout (the module
+// variable NumPointsOut, 350 at start); freq (cm^-1) and ir out, npoints of each.
+void orc_ir_spectrum(const float *dip, int tread, const double *box, double timestep, double temp, int *npoints,
+                     double *freq, double *ir) {
+    const double ps2s = 1e-12, Cspeed = 3.00e10, Debye2SI = 3.33564e-30, eps0 = 8.854187e-12, kb = 0.0019872041;
+    const double vol = (box[0] * box[1] * box[2]) * 1e-30;
+    const int trun = pow2_floor_log(tread, 0), n = 2 * trun;
+    std::vector<float> ACF(2 * (size_t)n, 0.0f), aux(2 * (size_t)n);
+    for (int ix = 0; ix < 3; ix++) {
+        std::fill(aux.begin(), aux.end(), 0.0f);
+        for (int i = 0; i < trun; i++) aux[2 * i] = dip[ix + 3 * (size_t)i];
+        orc_four1(aux.data(), n, -1);
+        for (int i = 0; i < n; i++) {
+            const float re = aux[2 * i], im = aux[2 * i + 1];
+            aux[2 * i] = re * re + im * im;
+            aux[2 * i + 1] = 0.0f;
+        }
+        orc_four1(aux.data(), n, 1);
+        for (int i = 0; i < 2 * n; i++) ACF[i] = ACF[i] + aux[i];
+    }
+    aux = ACF;  // aux1 = cmplx(ACF): the complex ACF as it is
+    orc_four1(aux.data(), n, -1);
+    const double MinFreqOut = 1.0 / (timestep * ps2s * Cspeed * n);
+    const double PointsAvailable = std::floor(7000.0 / MinFreqOut);
+    int NumAvgOver;
+    if (PointsAvailable < *npoints) {
+        *npoints = (int)PointsAvailable;
+        NumAvgOver = 1;
+    } else {
+        NumAvgOver = (int)std::floor(PointsAvailable / *npoints);
+    }
+    for (int t = 0; t < *npoints; t++) {
+        double avg = 0;
+        for (int i = 1; i <= NumAvgOver; i++) {
+            const double omega = (t * NumAvgOver + i) / (timestep * n * ps2s);
+            avg = avg + (omega * omega) * (double)aux[2 * (t * NumAvgOver + i)];
+        }
+        avg = avg / (double)(float)NumAvgOver;
+        double IR = (2.0 * 3.14159 * (Debye2SI * Debye2SI) * avg) / (3.0 * vol * 2.99e8 * kb * temp * eps0);
+        IR = IR * ps2s;
+        IR = IR * .01;
+        IR = IR * 2;
+        double omega = std::floor((t + .5f) * NumAvgOver) / (timestep * n * ps2s);
+        freq[t] = omega / Cspeed;
+        ir[t] = IR;
+    }
+}
+
+// spectral_properties.f90:128-187 calc_DOS from Hvel(3, tread, nhyd) (REAL): the velocity
+// autocorrelations (calc_corr_function) summed, normalised by nhyd and lag 0, calc_DFT, and
+// block averages of frequency (cm^-1) and spectrum up to 7000 cm^-1; npoints inout as above
+void orc_dos(const float *Hvel, int tread, int nhyd, double timestep, int *npoints, double *freq, double *dos) {
+    const double ps2s = 1e-12, Cspeed = 3.00e10;
+    std::vector<double> ACF(tread, 0.0), out(tread), DFT(tread), fr(tread);
+    std::vector<float> in(tread);
+    for (int iH = 0; iH < nhyd; iH++)
+        for (int ix = 0; ix < 3; ix++) {
+            for (int i = 0; i < tread; i++) in[i] = Hvel[ix + 3 * ((size_t)i + (size_t)tread * iH)];
+            orc_corr_function(in.data(), tread, out.data());
+            for (int i = 0; i < tread; i++) ACF[i] = ACF[i] + out[i];
+        }
+    const double a0 = ACF[0];  // ACF = ACF/Nhyd/ACF(1): the right-hand side before the assignment
+    for (int i = 0; i < tread; i++) ACF[i] = ACF[i] / nhyd / a0;
+    orc_calc_dft(ACF.data(), tread, timestep, DFT.data(), fr.data());
+    for (int i = 0; i < tread; i++) fr[i] = fr[i] / (ps2s * Cspeed);
+    const double MinFreqOut = fr[1];
+    const int PointsAvailable = std::min(tread, (int)std::floor(7000.0 / MinFreqOut));
+    if (PointsAvailable < *npoints) *npoints = PointsAvailable;
+    block_average(fr.data(), PointsAvailable, *npoints, freq);
+    block_average(DFT.data(), PointsAvailable, *npoints, dos);
+}
+
 }  // extern "C"

@@ -148,6 +148,22 @@ void orc_contracted_step(void *h, const orc_md_params *mp, int mode, int intra_t
                          const double *xi2, double *vxi_global, double *uk_state, double *vxi_beads,
                          int t, double *out, double *dip_momIt, double *dip_momEt);
 
+/* Analyses: geometry_calculator.f90 (accumulator of 176 doubles), diffusion_calculator.f90 (MSD
+ * state [t, initialised, aMS(ntimes+1), netdisp(3 Nw), Oxy(3 Nw)]), four1.f, math.f90:42-140 and
+ * spectral_properties.f90 (IR spectrum of dip(3, tread), DOS of Hvel(3, tread, nhyd)). */
+void orc_geometry_accumulate(double *acc, int natoms, int P, const double *box, const double *RR,
+                             const double *RRt);
+void orc_geometry_report(const double *acc, int P, double *out);
+void orc_msd_step(double *st, int natoms, int ntimes, const double *box, const double *RRc);
+void orc_msd_report(const double *aMS, int ntimes, double timestep, double *out);
+void orc_four1(float *data, int nn, int isign);
+void orc_corr_function(const float *in, int tread, double *out);
+void orc_calc_dft(const double *in, int tread, double timestep, double *out, double *freqs);
+void orc_ir_spectrum(const float *dip, int tread, const double *box, double timestep, double temp,
+                     int *npoints, double *freq, double *ir);
+void orc_dos(const float *Hvel, int tread, int nhyd, double timestep, int *npoints, double *freq,
+             double *dos);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpimd_gb300.so")
 SOURCES = ["capi.cu", "neighbors.cu", "pot.cu", "ewald.cu", "mixed.cu", "nm.cu", "peak.cu", "noalloc.cu", "spc.cu",
-           "md_batch.cu", "adjoint.cu", "ewald_tc.cu", "contracted.cu", "state_io.cpp"]
+           "md_batch.cu", "adjoint.cu", "ewald_tc.cu", "contracted.cu", "analysis.cu", "state_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -58,7 +58,7 @@ def build(force=False, verbose=False):
             print(r.stdout, r.stderr)
     objs = [os.path.join(OUT, os.path.splitext(s)[0] + ".o") for s in SOURCES]
     if force or jobs or not os.path.exists(LIB):
-        link = [nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        link = [nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-ldl"]
         r = subprocess.run(link, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s" % (r.stdout, r.stderr))

@@ -405,4 +405,11 @@ struct pimd_ctx {
     pimd_ctx *cen = nullptr;
     int con_mode = -1, con_intra = 0;
     double *d_con = nullptr;
+    // run analyses (analysis.cu): geometry accumulator and the centroid O-H pairs of a frame, MSD
+    // state, spectra time series (device memory, freed with the context's allocations)
+    double *an_geo = nullptr, *an_dcen = nullptr, *an_msd = nullptr;
+    int an_msd_ntimes = 0;
+    float *an_dip = nullptr, *an_hvel = nullptr;
+    int an_nmax = 0, an_n = 0;
+    double an_massH = 1.008;
 };

@@ -92,6 +92,16 @@ SIGNATURES = {
     "pimd_contracted_step_device": [_V, ctypes.POINTER(MDParams), _V, _V, _V, _V, _V, _V, _V, ctypes.c_int, _V, _V,
                                     _V],
     "pimd_contracted_step": [_V, ctypes.POINTER(MDParams), _D, _D, _D, _D, _D, _D, _D, ctypes.c_int, _D, _D, _D],
+    "pimd_geometry_reset": [_V],
+    "pimd_geometry_accumulate_device": [_V, _V, _V],
+    "pimd_geometry_report": [_V, _D, _D, _D, _D],
+    "pimd_msd_init": [_V, ctypes.c_int],
+    "pimd_msd_accumulate_device": [_V, _V],
+    "pimd_msd_report": [_V, ctypes.c_double, _D, _I, _D],
+    "pimd_spectra_init": [_V, ctypes.c_int, ctypes.c_double],
+    "pimd_spectra_record_device": [_V, _V, _V],
+    "pimd_ir_spectrum": [_V, ctypes.c_double, ctypes.c_double, _I, _D, _D],
+    "pimd_dos": [_V, ctypes.c_double, _I, _D, _D],
     "pimd_set_thermostat": [_V, _V],
     "pimd_get_thermostat_state": [_V, _D, _D, _D],
     "pimd_set_thermostat_state": [_V, _D, ctypes.c_double, _D],
@@ -433,6 +443,50 @@ class ForceEngine:
         r = dict(zip(MD_OUT_NAMES, out.tolist()))
         r.update(RRc=RRc, dip_momIt=dI, dip_momEt=dE)
         return r
+
+    # ---- run analyses (geometry_calculator, diffusion_calculator, spectral_properties) ---------
+    def geometry_reset(self):
+        self._check(load().pimd_geometry_reset(self.h), "geometry_reset")
+
+    def geometry_accumulate_device(self, RRc_ptr, RRt_ptr):
+        self._check(load().pimd_geometry_accumulate_device(self.h, RRc_ptr, RRt_ptr), "geometry_accumulate")
+
+    def geometry_report(self):
+        out, hc, hb, acc = np.zeros(14), np.zeros((80, 2)), np.zeros((80, 2)), np.zeros(176)
+        self._check(load().pimd_geometry_report(self.h, _p(out), _p(hc), _p(hb), _p(acc)), "geometry_report")
+        return dict(report=out, hist_centroid=hc, hist_beads=hb, accumulator=acc)
+
+    def msd_init(self, num_timesteps):
+        self._check(load().pimd_msd_init(self.h, int(num_timesteps)), "msd_init")
+
+    def msd_accumulate_device(self, RRc_ptr):
+        self._check(load().pimd_msd_accumulate_device(self.h, RRc_ptr), "msd_accumulate")
+
+    def msd_report(self, timestep):
+        n = ctypes.c_int()
+        out = np.zeros(4)
+        aMS = np.zeros(100000)
+        self._check(load().pimd_msd_report(self.h, float(timestep), _p(aMS), ctypes.byref(n), _p(out)), "msd_report")
+        return dict(aMS=aMS[:n.value].copy(), D=out[0], errD=out[1], slope=out[2], intercept=out[3])
+
+    def spectra_init(self, max_steps, massH):
+        self._check(load().pimd_spectra_init(self.h, int(max_steps), float(massH)), "spectra_init")
+
+    def spectra_record_device(self, dip_ptr, PPt_ptr):
+        self._check(load().pimd_spectra_record_device(self.h, dip_ptr or None, PPt_ptr or None), "spectra_record")
+
+    def ir_spectrum(self, timestep, temp, npoints=350):
+        n = ctypes.c_int(int(npoints))
+        f, v = np.zeros(npoints), np.zeros(npoints)
+        self._check(load().pimd_ir_spectrum(self.h, float(timestep), float(temp), ctypes.byref(n), _p(f), _p(v)),
+                    "ir_spectrum")
+        return f[:n.value].copy(), v[:n.value].copy()
+
+    def dos(self, timestep, npoints=350):
+        n = ctypes.c_int(int(npoints))
+        f, v = np.zeros(npoints), np.zeros(npoints)
+        self._check(load().pimd_dos(self.h, float(timestep), ctypes.byref(n), _p(f), _p(v)), "dos")
+        return f[:n.value].copy(), v[:n.value].copy()
 
     def md_step_ex_device(self, mp, RRt, PPt, dRRt, RRc, t, out, xi1=0, xi2=0):
         """pimd_md_step_ex_device on device buffers given as raw pointers (ints), stream-ordered."""

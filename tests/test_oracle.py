@@ -242,3 +242,27 @@ def test_ring_k0_and_simple_estimator_on_free_rings(orc):
         assert abs(e["sys_temp"] - T) < 1e-9
         Es.append(e["E_simple"])
     assert abs(np.mean(Es) / (4.5 * kbT) - 1.0) < 0.03
+
+
+def test_four1_is_the_discrete_fourier_transform(orc):
+    """four1.f: isign = -1 is the DFT exp(-2 pi i jk/n), isign = +1 the unnormalised inverse
+    (checked against numpy.fft in single precision)."""
+    rng = np.random.default_rng(9)
+    for n in (8, 64, 1024):
+        z = (rng.normal(size=n) + 1j * rng.normal(size=n)).astype(np.complex64)
+        assert np.abs(orc.four1(z, -1) - np.fft.fft(z)).max() < 2e-5 * np.sqrt(n) * np.abs(z).max()
+        assert np.abs(orc.four1(z, 1) - np.fft.ifft(z) * n).max() < 2e-5 * np.sqrt(n) * np.abs(z).max()
+
+
+def test_msd_of_a_uniform_drift(orc):
+    """calc_diff_RMSD / write_out_diffusion on a uniform drift v per frame: aMS(k) = |v|^2 (20 (k-1))^2
+    (the first sample is taken at the first frame), so the fitted slope is that of the samples."""
+    nat, box = 12, np.array([30.0, 30.0, 30.0])
+    m = orc.MSD(nat, 200, box)
+    R = np.random.default_rng(3).uniform(-5, 5, size=(nat, 3))
+    v = np.array([0.01, -0.02, 0.005])
+    for k in range(200):
+        m.step(R + k * v)
+    r = m.report(0.25e-3)
+    k = np.arange(len(r["aMS"]))
+    assert np.allclose(r["aMS"], (v ** 2).sum() * (20.0 * k) ** 2, rtol=1e-9, atol=1e-15)
