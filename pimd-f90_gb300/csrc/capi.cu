@@ -1052,6 +1052,7 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     if (n >= 13) k[12] = E.ewald_overlap && E.aux_stream != nullptr && E.kp.Fx != nullptr;
     if (n >= 14) k[13] = E.dd_otf && E.precision == PIMD_MIXED;
     if (n >= 15) k[14] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
+    if (n >= 16) k[15] = E.l2_keep && E.precision == PIMD_MIXED;
     return PIMD_OK;
 }
 
@@ -1076,6 +1077,7 @@ int pimd_set_tuning(pimd_ctx *ctx, const int *k, int n) {
     }
     if (n >= 13) E.ewald_overlap = k[12] != 0;
     if (n >= 14) E.dd_otf = k[13] != 0;
+    if (n >= 16) E.l2_keep = k[15] != 0;
     E.gkey.clear();  // a captured MD-step graph holds the old launches: capture again
     return PIMD_OK;
 }

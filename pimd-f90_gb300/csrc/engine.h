@@ -122,6 +122,7 @@ struct KP {
     int *fntot;            // [P] full-list length
     float2 *Tf;            // [P][fcap][ndd] FP32 (t1, 3 t2) dipole-tensor scalars of the full list
     int *fj;               // [P][fcap] partner j of each full-list entry
+    int l2keep;            // k_dd_real_m loads fj / Tf with the L2 evict-last policy
     int fcap;
     double4_32a *Fpart;    // [slices][P][S] per-k-slice partial fields of the Ewald field passes
     // cell lists of large boxes (N > 1024, >= 4 cells of width >= Rc per edge)
@@ -220,6 +221,7 @@ struct Engine {
     int loop_unroll = 2;              // dipole iterations per body of the graph's conditional loop
     bool ewald_overlap = true;        // reciprocal charge / force passes beside the pair gathers
     bool dd_otf = false;              // real-space dipole tensors formed in each iteration (no cache)
+    bool l2_keep = false;             // the iterations' cached operands (X blocks, dipole-pair scalars) loaded evict-last in L2
     bool ff_tc = true;                // tensor-core dipole field pass (k_field_tc) when tf_ready
     bool tf_ready = false;
     int tf_nr = 0, tf_nph = 0, tf_jm = 0, tf_ncol = 0, tf_kq = 0;

@@ -98,6 +98,7 @@ struct TcArgs {
     int skipconv;
     uint4 *xcache;        // X operand blocks of the dipole sites (null: no cache), see k_sfac_tc
     int xsub, xblock;     // 16-site blocks per bead and run group, bytes per block
+    int xkeep;            // load the cached X blocks with the L2 evict-last policy
 };
 
 // Shared-memory carve-up (bytes from a 1024-aligned base), used by the kernel and the launcher.
@@ -144,11 +145,15 @@ PIMD_D void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
                  "l"((unsigned long long)src), "r"(bytes), "r"(umma::smem_u32(bar))
                  : "memory");
 }
-// the same with an L2 evict-first policy (data read once per kernel that should not displace
-// the working set of the other kernels)
-PIMD_D void bulk_load_stream(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+// the same with an L2 eviction policy: evict-first (data read once per kernel that should not
+// displace the working set of the other kernels) or, with keep, evict-last (data read again by
+// every dipole iteration of the force call, kept in L2 across them)
+PIMD_D void bulk_load_stream(void *dst, const void *src, uint32_t bytes, uint64_t *bar, bool keep = false) {
     uint64_t pol;
-    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    if (keep)
+        asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    else
+        asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
                      umma::smem_u32(dst)),
                  "l"((unsigned long long)src), "r"(bytes), "r"(umma::smem_u32(bar)), "l"(pol)
@@ -341,8 +346,8 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
                 uint4 *xb = xm ? xc + (size_t)sub * (a.xblock / 16) : nullptr;  // this block in the cache
                 if (xm == 2 && bt == 0) {
                     mbar_expect_tx(&xfull[ab], 2u * (uint32_t)xbytes);
-                    bulk_load_stream(Bf + L.xoff, xb, (uint32_t)xbytes, &xfull[ab]);
-                    bulk_load_stream(Bf + L.xoff + xlo, xb + xbytes / 16, (uint32_t)xbytes, &xfull[ab]);
+                    bulk_load_stream(Bf + L.xoff, xb, (uint32_t)xbytes, &xfull[ab], a.xkeep);
+                    bulk_load_stream(Bf + L.xoff + xlo, xb + xbytes / 16, (uint32_t)xbytes, &xfull[ab], a.xkeep);
                 }
 #pragma unroll
                 for (int u = 0; u < 2; u++) {
@@ -1322,6 +1327,7 @@ int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv) {
     a.xcache = xok ? reinterpret_cast<uint4 *>(E.d_tcx) : nullptr;
     a.xsub = E.tc_xsub;
     a.xblock = E.tc_xblock;
+    a.xkeep = E.l2_keep ? 1 : 0;
     // one CTA per SM (shared memory); site groups (= cluster size) so that one wave fills the GPU
     static int nsm_cache[64] = {0};
     int &nsm = nsm_cache[E.device & 63];

@@ -398,8 +398,16 @@ __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
     float4 si[5];
 #pragma unroll
     for (int k = T::FDI; k <= T::LDI; k++) si[k] = pf[(k - 1) * N + i];
+    uint64_t pol = 0;
+    if (kp.l2keep) asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
     for (int e = e0 + lane; e < e1; e += 32) {
-        const int j = OTF ? fl[e].y : fj[e];
+        int j;
+        if (OTF)
+            j = fl[e].y;
+        else if (kp.l2keep)
+            asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(j) : "l"(fj + e), "l"(pol));
+        else
+            j = fj[e];
         float Rf[3];
         oo_min_image(kp, oi, of[j], Rf);
         int t = 0;
@@ -417,7 +425,14 @@ __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
                     smear2<float>(Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2], kp.ptf.apol_dd[isp][jsp], kp.ewf, &t1, &t2);
                     t3 = 3.f * t2;
                 } else {
-                    const float2 ts = Tb[(size_t)e * kp.ndd + t];
+                    float2 ts;
+                    const float2 *pt = Tb + (size_t)e * kp.ndd + t;
+                    if (kp.l2keep)
+                        asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+                                     : "=f"(ts.x), "=f"(ts.y)
+                                     : "l"(pt), "l"(pol));
+                    else
+                        ts = *pt;
                     t1 = ts.x;
                     t3 = ts.y;
                 }
@@ -689,6 +704,7 @@ void launch_pair_qq_m(Engine &E) {
 
 void launch_dd_real_m(Engine &E) {
     dim3 g((E.kp.N * 32 + 127) / 128, E.kp.P);
+    E.kp.l2keep = E.l2_keep ? 1 : 0;
     if (E.kp.model == 2)
         E.dd_otf ? k_dd_real_m<2, true><<<g, 128, 0, E.stream>>>(E.kp) : k_dd_real_m<2, false><<<g, 128, 0, E.stream>>>(E.kp);
     else

@@ -558,15 +558,17 @@ class ForceEngine:
         self._check(load().pimd_autotune(self.h, RRt_ptr, RRc_ptr), "autotune")
         return self.tuning()
 
-    TUNING_KEYS = ("sf_tiled", "sf_groups", "ff_regs", "max_slices", "nbr_block", "wave_shapes", "sf_tc", "ff_tc",
-                   "dd_overlap", "x_cache", "pdl", "loop_unroll", "ewald_overlap", "dd_otf")
-    TUNING_REPORTS = ("qd_tc",)  # read-only: tensor-core force pass in use
+    # pimd_get_tuning / pimd_set_tuning order; qd_tc is a report only (tensor-core force pass in use)
+    TUNING_ORDER = ("sf_tiled", "sf_groups", "ff_regs", "max_slices", "nbr_block", "wave_shapes", "sf_tc", "ff_tc",
+                    "dd_overlap", "x_cache", "pdl", "loop_unroll", "ewald_overlap", "dd_otf", "qd_tc", "l2_keep")
+    TUNING_REPORTS = ("qd_tc",)
+    TUNING_KEYS = TUNING_ORDER[:14] + TUNING_ORDER[15:]
 
     def tuning(self):
-        n = len(self.TUNING_KEYS) + len(self.TUNING_REPORTS)
+        n = len(self.TUNING_ORDER)
         k = (ctypes.c_int * n)()
         self._check(load().pimd_get_tuning(self.h, k, n), "get_tuning")
-        return {name: k[i] for i, name in enumerate(self.TUNING_KEYS + self.TUNING_REPORTS)}
+        return {name: k[i] for i, name in enumerate(self.TUNING_ORDER)}
 
     def set_tuning(self, **knobs):
         """Set launch-shape knobs by name (the keys of tuning()); the others keep their values."""
@@ -575,8 +577,8 @@ class ForceEngine:
         if unknown:
             raise ValueError("unknown tuning knobs: %s" % sorted(unknown))
         cur.update({k: int(v) for k, v in knobs.items()})
-        n = len(self.TUNING_KEYS)
-        k = (ctypes.c_int * n)(*[cur[name] for name in self.TUNING_KEYS])
+        n = len(self.TUNING_ORDER)
+        k = (ctypes.c_int * n)(*[cur[name] for name in self.TUNING_ORDER])
         self._check(load().pimd_set_tuning(self.h, k, n), "set_tuning")
         return self.tuning()
 

@@ -58,7 +58,7 @@ def test_msd_matches_oracle(pkg, orc, engine_lib):
 
     RRc0, box, eng = setup(pkg, 2)
     dev = torch.device("cuda", 0)
-    steps = 120
+    steps = 400  # 20 samples: the fit takes the last 9
     m = orc.MSD(len(RRc0), steps, box)
     eng.msd_init(steps)
     rng = np.random.default_rng(2)
