@@ -515,7 +515,7 @@ static int capture_dipole_loop(Engine &E, bool mixed) {
     cudaStream_t keep = E.stream;
     E.stream = E.body_stream;
     E.kp.cond = h;
-    // iterations per body: 2 halves the conditional's relaunches; an iteration after every bead
+    // iterations per body: 3 divides the conditional's relaunches by three; an iteration after every bead
     // has converged is empty (each kernel returns at the bead's flag, the test leaves the
     // per-bead counts alone)
     for (int u = 0; u < std::max(1, E.loop_unroll); u++) dipole_iteration(E, mixed);

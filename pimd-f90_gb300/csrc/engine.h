@@ -217,8 +217,8 @@ struct Engine {
     void *d_tcx = nullptr;            // X-operand cache of the dipole sites (uint4 blocks)
     int tc_xsub = 0, tc_xblock = 0;   // 16-site blocks per bead and run group, bytes per block
     bool tc_xcache = true;            // use the X cache in the dipole iterations
-    bool tc_pdl = true;               // field pass as a programmatic dependent launch
-    int loop_unroll = 2;              // dipole iterations per body of the graph's conditional loop
+    bool tc_pdl = true;               // field pass and next structure factor as programmatic dependent launches
+    int loop_unroll = 3;              // dipole iterations per body of the graph's conditional loop
     bool ewald_overlap = true;        // reciprocal charge / force passes beside the pair gathers
     bool dd_otf = false;              // real-space dipole tensors formed in each iteration (no cache)
     bool l2_keep = false;             // the iterations' cached operands (X blocks, dipole-pair scalars) loaded evict-last in L2

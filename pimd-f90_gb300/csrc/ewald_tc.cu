@@ -99,6 +99,7 @@ struct TcArgs {
     uint4 *xcache;        // X operand blocks of the dipole sites (null: no cache), see k_sfac_tc
     int xsub, xblock;     // 16-site blocks per bead and run group, bytes per block
     int xkeep;            // load the cached X blocks with the L2 evict-last policy
+    int pdl;              // launched as a programmatic dependent of the previous iteration's field pass
 };
 
 // Shared-memory carve-up (bytes from a 1024-aligned base), used by the kernel and the launcher.
@@ -209,6 +210,9 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     constexpr int NCZ = (OP == TC_OP_Q) ? 1 : 3;
     constexpr int NPT = (OP == TC_OP_DIP) ? 3 : 1;
     const int grp = blockIdx.x, tg = blockIdx.y, b = blockIdx.z;
+    // a programmatic launch starts under the previous field pass: the convergence flags, the
+    // dipoles and the weights are that grid's output
+    if (a.pdl) pdl_wait();
     // the whole cluster (same bead) leaves together
     if (a.skipconv && bead_converged(kp, b)) return;
     const TcGroup G = a.grp[tg];
@@ -662,6 +666,8 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     constexpr bool DG = MODE == TF_DG;
     constexpr int NC = DG ? 6 : 4;
     const int t = blockIdx.x, b = blockIdx.y;
+    // the next iteration's structure factor may be scheduled now; it waits for this grid
+    if (MODE == TF_D) pdl_launch_dependents();
     if (MODE == TF_D && bead_converged(kp, b)) {
         // converged bead: no update, but the block still counts towards the convergence test
         const double zero[2] = {0.0, 0.0};
@@ -1328,6 +1334,9 @@ int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv) {
     a.xsub = E.tc_xsub;
     a.xblock = E.tc_xblock;
     a.xkeep = E.l2_keep ? 1 : 0;
+    // the iterations' structure factor follows the previous iteration's field pass on the stream
+    // (or the charge passes, which need no overlap): its CTAs are scheduled as that grid drains
+    a.pdl = (op == TC_OP_MU && skipconv && E.tc_pdl && E.tf_ready && E.ff_tc) ? 1 : 0;
     // one CTA per SM (shared memory); site groups (= cluster size) so that one wave fills the GPU
     static int nsm_cache[64] = {0};
     int &nsm = nsm_cache[E.device & 63];
@@ -1356,15 +1365,17 @@ int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv) {
         if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess) prio_cache[E.device & 63] = greatest;
         prio_set[E.device & 63] = 1;
     }
-    cudaLaunchAttribute at[2];
+    cudaLaunchAttribute at[3];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = ng;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
     at[1].id = cudaLaunchAttributePriority;
     at[1].val.priority = prio_cache[E.device & 63];
+    at[2].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[2].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
-    cfg.numAttrs = 2;
+    cfg.numAttrs = a.pdl ? 3 : 2;
     const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(E.tc_map);
     cudaError_t e = cudaErrorInvalidValue;
     if (op == TC_OP_MU)
@@ -1373,6 +1384,12 @@ int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv) {
         e = cudaLaunchKernelEx(&cfg, k_sfac_tc<TC_OP_Q>, *map, kp, a);
     else
         e = cudaLaunchKernelEx(&cfg, k_sfac_tc<TC_OP_DIP>, *map, kp, a);
+    if (e != cudaSuccess && a.pdl) {  // the attribute refused: a plain cluster launch
+        cudaGetLastError();
+        a.pdl = 0;
+        cfg.numAttrs = 2;
+        e = cudaLaunchKernelEx(&cfg, k_sfac_tc<TC_OP_MU>, *map, kp, a);
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
         E.sf_tc = false;  // e.g. no room for the cluster: the FP32-pipe kernel from now on

@@ -35,7 +35,7 @@ struct TM {
     }
 };
 
-PIMD_D float wrapf(float v, float L, float Li) { return v - L * rintf(v * Li); }
+PIMD_D float wrapf(float v, float L, float Li) { return v - L * rint_small(__fmul_rn(v, Li)); }
 
 // ---------------------------------------------------------------------------------------
 // Q(2/3, x) of the Thole-smeared charge pairs (smear.f90:2-34 calls math.f90:188-285 with

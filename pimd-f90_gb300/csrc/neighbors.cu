@@ -13,7 +13,7 @@
 
 namespace pimd {
 
-PIMD_D float wrapf_n(float v, float L, float Li) { return v - L * rintf(v * Li); }
+PIMD_D float wrapf_n(float v, float L, float Li) { return v - L * rint_small(__fmul_rn(v, Li)); }
 
 template <bool PRE>
 PIMD_D bool oo_test(const double4_32a &a, const double4_32a &b, const KP &kp) {

@@ -72,14 +72,17 @@ __global__ void __launch_bounds__(SITES_NT) k_sites(KP kp) {
                 Rc[k][c] = RC[3 * k + c];
             }
         const double hg = 0.5 * kp.gammaM;
+        // the O-H minimum images of the bead and the centroid (the M sites, and in the mixed
+        // engine the FP32 site offsets of the exclusion pairs)
+        double oh[2][3], ohc[2][3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            double r1 = min_image_rn(__dsub_rn(R[1][c], R[0][c]), kp.box[c], kp.boxi[c]);
-            double r2 = min_image_rn(__dsub_rn(R[2][c], R[0][c]), kp.box[c], kp.boxi[c]);
-            R[3][c] = __dadd_rn(__dmul_rn(hg, __dadd_rn(r1, r2)), R[0][c]);
-            r1 = min_image_rn(__dsub_rn(Rc[1][c], Rc[0][c]), kp.box[c], kp.boxi[c]);
-            r2 = min_image_rn(__dsub_rn(Rc[2][c], Rc[0][c]), kp.box[c], kp.boxi[c]);
-            Rc[3][c] = __dadd_rn(__dmul_rn(hg, __dadd_rn(r1, r2)), Rc[0][c]);
+            oh[0][c] = min_image_rn(__dsub_rn(R[1][c], R[0][c]), kp.box[c], kp.boxi[c]);
+            oh[1][c] = min_image_rn(__dsub_rn(R[2][c], R[0][c]), kp.box[c], kp.boxi[c]);
+            R[3][c] = __dadd_rn(__dmul_rn(hg, __dadd_rn(oh[0][c], oh[1][c])), R[0][c]);
+            ohc[0][c] = min_image_rn(__dsub_rn(Rc[1][c], Rc[0][c]), kp.box[c], kp.boxi[c]);
+            ohc[1][c] = min_image_rn(__dsub_rn(Rc[2][c], Rc[0][c]), kp.box[c], kp.boxi[c]);
+            Rc[3][c] = __dadd_rn(__dmul_rn(hg, __dadd_rn(ohc[0][c], ohc[1][c])), Rc[0][c]);
         }
         if (pes) {
             double dr1[3][3], e1 = 0.0;
@@ -149,6 +152,60 @@ __global__ void __launch_bounds__(SITES_NT) k_sites(KP kp) {
                 ph[k] = (k == 0) ? 0.0 : -kp.ew.aewald * TSP * q[k];
                 Ef[k][0] = Ef[k][1] = Ef[k][2] = 0.0;
             }
+            if (FSUM && MODEL == 3) {
+                // the mixed engine, TTM3-F: the six exclusion pairs in FP32 from the sites' offsets
+                // to their O site (a molecule spans far less than half a box, so a pair's minimum
+                // image is the difference of the two offsets); sums converted once
+                float rel[4][3], relc[4][3];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    rel[0][c] = relc[0][c] = 0.f;
+                    rel[1][c] = (float)oh[0][c];
+                    rel[2][c] = (float)oh[1][c];
+                    rel[3][c] = (float)__dsub_rn(R[3][c], R[0][c]);
+                    relc[1][c] = (float)ohc[0][c];
+                    relc[2][c] = (float)ohc[1][c];
+                    relc[3][c] = (float)__dsub_rn(Rc[3][c], Rc[0][c]);
+                }
+                const float qf[4] = {(float)q[0], (float)q[1], (float)q[2], (float)q[3]};
+                float phf[4] = {0.f, 0.f, 0.f, 0.f}, Eff[4][3], vcf = 0.f, vtf[9];
+#pragma unroll
+                for (int k = 0; k < 4; k++) Eff[k][0] = Eff[k][1] = Eff[k][2] = 0.f;
+#pragma unroll
+                for (int k = 0; k < 9; k++) vtf[k] = 0.f;
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = i + 1; j < 4; j++) {
+                        const float Rs[3] = {rel[i][0] - rel[j][0], rel[i][1] - rel[j][1], rel[i][2] - rel[j][2]};
+                        const float Rcs[3] = {relc[i][0] - relc[j][0], relc[i][1] - relc[j][1], relc[i][2] - relc[j][2]};
+                        float ts0, ts1;
+                        self1f(Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2], kp.ewf, &ts0, &ts1);
+                        phf[i] += ts0 * qf[j];
+                        phf[j] += ts0 * qf[i];
+                        float d[3];
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            Eff[i][c] += ts1 * qf[j] * Rs[c];
+                            Eff[j][c] -= ts1 * qf[i] * Rs[c];
+                            d[c] = -ts1 * qf[i] * qf[j] * Rs[c];
+                        }
+                        vcf += Rcs[0] * d[0] + Rcs[1] * d[1] + Rcs[2] * d[2];
+#pragma unroll
+                        for (int col = 0; col < 3; col++)
+#pragma unroll
+                            for (int c = 0; c < 3; c++) vtf[c + 3 * col] += d[col] * Rs[c];
+                    }
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    ph[k] += (double)phf[k];
+#pragma unroll
+                    for (int c = 0; c < 3; c++) Ef[k][c] = (double)Eff[k][c];
+                }
+                av[ACC_VIRIALC] += (double)vcf;
+#pragma unroll
+                for (int k = 0; k < 9; k++) av[ACC_VIRT + k] += (double)vtf[k];
+            } else
 #pragma unroll
             for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -159,17 +216,10 @@ __global__ void __launch_bounds__(SITES_NT) k_sites(KP kp) {
                         Rs[c] = min_image_rn(__dsub_rn(R[i][c], R[j][c]), kp.box[c], kp.boxi[c]);
                         Rcs[c] = min_image_rn(__dsub_rn(Rc[i][c], Rc[j][c]), kp.box[c], kp.boxi[c]);
                     }
+                    // FP64 (TTM2.1-F's polarisable H sites take the exclusion field into the
+                    // dipoles, so its mixed engine keeps these in FP64 as well)
                     double ts0, ts1;
-                    // the mixed engine, TTM3-F: the exclusion's erfc and exponential in FP32 (TTM2.1-F's
-                    // polarisable H sites take the exclusion field into the dipoles: FP64 there)
-                    if (FSUM && MODEL == 3) {
-                        float f0, f1;
-                        self1f((float)dot3_rn(Rs[0], Rs[1], Rs[2]), kp.ewf, &f0, &f1);
-                        ts0 = f0;
-                        ts1 = f1;
-                    } else {
-                        self1(dot3_rn(Rs[0], Rs[1], Rs[2]), kp.ew, &ts0, &ts1);
-                    }
+                    self1(dot3_rn(Rs[0], Rs[1], Rs[2]), kp.ew, &ts0, &ts1);
                     ph[i] += ts0 * q[j];
                     ph[j] += ts0 * q[i];
                     double d[3];
