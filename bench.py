@@ -338,8 +338,13 @@ def run_gpu_arm(args, pkg, rank, world, local, precision, steps, graph=False):
     eng.timers_reset(False)
     dev_ms = reduce_max(sum(step_ms), dev, world)
     out = out4.cpu().numpy()
-    # e2e: the host-array C-ABI step, copies in and out every step
-    hR, hP, hG = RRt.cpu().numpy().copy(), PPt.cpu().numpy().copy(), dRRt.cpu().numpy().copy()
+    # e2e: the host-array C-ABI step, copies in and out every step, from pinned host memory
+    def pinned(x):
+        h = torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
+        h.copy_(x)
+        return h.numpy()
+
+    hR, hP, hG = pinned(RRt), pinned(PPt), pinned(dRRt)
     e2e_steps = max(3, steps // 2)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()

@@ -320,14 +320,16 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc);
  * force passes on a second stream beside the pair kernels (mixed engine)], when n >= 14
  * [real-space dipole tensors formed inside each iteration rather than cached per list entry
  * (mixed engine)], when n >= 15 [tensor-core force pass in use (follows the field-pass knob;
- * reported only)]; n >= 5. */
+ * reported only)], when n >= 16 [the iterations' cached operands loaded evict-last in L2], when
+ * n >= 17 [the real-space dipole field beside the field pass too, each unit of 128 dipole
+ * sites updated by whichever of the two finishes it last (mixed engine, TTM3-F)]; n >= 5. */
 int pimd_get_tuning(pimd_ctx *ctx, int *knobs, int n);
-/* Sets the shapes in the order pimd_get_tuning reports them (n >= 5; the first n up to 14 are
- * set, later entries are reports only),
- * e.g. to reuse an earlier autotune result without timing again. Tensor-core paths are used
- * only where available whatever their knob says. Site groups must lie in [0, 1024] and max
- * k-slices in [1, 16], iterations per graph-loop body in [1, 4] (else PIMD_ERR_ARG). A captured MD-step graph is captured again at the
- * next step. No counterpart in the reference. */
+/* Sets the shapes in the order pimd_get_tuning reports them (n >= 5; entry 15, the tensor-core
+ * force pass, is a report only), e.g. to reuse an earlier autotune result without timing
+ * again. Tensor-core paths are used only where available whatever their knob says. Site groups
+ * must lie in [0, 1024] and max k-slices in [1, 16], iterations per graph-loop body in [1, 4]
+ * (else PIMD_ERR_ARG). A captured MD-step graph is captured again at the next step. No
+ * counterpart in the reference. */
 int pimd_set_tuning(pimd_ctx *ctx, const int *knobs, int n);
 
 /* ---------------------------------------------------------------------------------------

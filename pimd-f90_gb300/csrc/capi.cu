@@ -351,8 +351,13 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
             (rc = dalloc(E, &kp.rhof, P * S)) || (rc = dalloc(E, &kp.fcnt, P * N)) || (rc = dalloc(E, &kp.foff, P * N)) ||
             (rc = dalloc(E, &kp.fnbr, P * (size_t)kp.fcap * 2)) || (rc = dalloc(E, &kp.fntot, P)) ||
             (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd)) || (rc = dalloc(E, &kp.fj, P * (size_t)kp.fcap)) || (rc = dalloc(E, &kp.Wf, P * 2 * (size_t)kp.nk)) || (rc = dalloc(E, &kp.dipf, P * S)) ||
-            (rc = dalloc(E, &kp.ofix, P * N)) || (rc = dalloc(E, &kp.orawf, P * N)) || (rc = dalloc(E, &kp.Fx, P * S)))
+            (rc = dalloc(E, &kp.ofix, P * N)) || (rc = dalloc(E, &kp.orawf, P * N)) || (rc = dalloc(E, &kp.Fx, P * S)) ||
+            (rc = dalloc(E, &kp.dipf_alt, P * S)) || (rc = dalloc(E, &kp.Erec, P * S)) ||
+            (rc = dalloc(E, &kp.unit_cnt, P * ((size_t)S / 128 + 2))))
             return rc;
+        cudaMemset(kp.unit_cnt, 0, sizeof(unsigned) * P * ((size_t)S / 128 + 2));
+        kp.unit_sbase = kp.fd & ~31;  // the field pass's first CTA (TMA-aligned site base)
+        kp.nunits = (kp.ld - kp.unit_sbase + 127) / 128;
     }
     // cell lists for boxes beyond the one-block neighbour kernel (cells of width >= Rc + 1e-3 A)
     kp.cl_ncell = 0;
@@ -473,8 +478,11 @@ static void dipole_iteration(Engine &E, bool mixed) {
         PHASE("dd_real", launch_dd_real_m(E));
         E.stream = keep;
         cudaEventRecord(E.loop_join, E.loop_aux);
-        cudaStreamWaitEvent(E.stream, E.loop_join, 0);
+        // asynchronous: the field pass runs beside the real-space field as well (whichever ends
+        // a unit of sites last updates its dipoles); the iteration ends when both are done
+        if (!E.kp.dd_async) cudaStreamWaitEvent(E.stream, E.loop_join, 0);
         PHASE("dd_update", launch_dd_update(E));  // includes the convergence test (last block)
+        if (E.kp.dd_async) cudaStreamWaitEvent(E.stream, E.loop_join, 0);
         return;
     }
     if (mixed)
@@ -588,9 +596,13 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
     PHASE("after_qq", launch_after_qq(E));
     kp.fx_mode = 0;
     if (E.tape_on) tape_record(E, 0);
+    kp.dd_async = (mixed && dd_async_ok(E)) ? 1 : 0;
     if (E.capturing) {
         int rc = capture_dipole_loop(E, mixed);
-        if (rc) return rc;
+        if (rc) {
+            kp.dd_async = 0;
+            return rc;
+        }
         E.last_niter_max = -1;  // known on the device only
     } else {
         int iter = 1;
@@ -605,6 +617,10 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
             }
         }
         E.last_niter_max = std::min(iter, kp.polar_maxiter);
+    }
+    if (kp.dd_async) {
+        PHASE("dipf_sync", launch_dipf_sync(E));
+        kp.dd_async = 0;
     }
     if (ovf) {
         cudaEventRecord(E.ev_fork, E.stream);
@@ -971,7 +987,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
     };
     int sf_tiled = E.sf_tiled, ff_regs = E.ff_regs, nbr_block = E.nbr_block, wave = E.wave_shapes;
     int nbr_cells = E.nbr_cells, sf_tc = E.sf_tc, ff_tc = E.ff_tc, dd_overlap = E.dd_overlap, xcache = E.tc_xcache, pdl = E.tc_pdl,
-        ewo = E.ewald_overlap, otf = E.dd_otf;
+        ewo = E.ewald_overlap, otf = E.dd_otf, dda = E.dd_async;
     std::vector<Knob> knobs;
     const bool mixed = E.precision == PIMD_MIXED && E.kp.model < 4;
     if (mixed) {
@@ -981,6 +997,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         knobs.push_back({&E.sf_groups, {0, 4, 8, 16, 32}});
         knobs.push_back({&ff_regs, {1, 0}});
         if (E.loop_aux) knobs.push_back({&dd_overlap, {1, 0}});
+        if (dd_async_ok(E)) knobs.push_back({&dda, {1, 0}});
         if (E.d_tcx) knobs.push_back({&xcache, {1, 0}});
         if (E.tf_ready) knobs.push_back({&pdl, {1, 0}});
         if (E.kp.Fx) knobs.push_back({&ewo, {1, 0}});
@@ -1003,6 +1020,7 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc) {
         E.tc_pdl = pdl != 0;
         E.ewald_overlap = ewo != 0;
         E.dd_otf = otf != 0;
+        E.dd_async = dda != 0;
     };
     int rc = PIMD_OK;
     float best;
@@ -1053,6 +1071,7 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     if (n >= 14) k[13] = E.dd_otf && E.precision == PIMD_MIXED;
     if (n >= 15) k[14] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
     if (n >= 16) k[15] = E.l2_keep && E.precision == PIMD_MIXED;
+    if (n >= 17) k[16] = dd_async_ok(E);
     return PIMD_OK;
 }
 
@@ -1078,6 +1097,7 @@ int pimd_set_tuning(pimd_ctx *ctx, const int *k, int n) {
     if (n >= 13) E.ewald_overlap = k[12] != 0;
     if (n >= 14) E.dd_otf = k[13] != 0;
     if (n >= 16) E.l2_keep = k[15] != 0;
+    if (n >= 17) E.dd_async = k[16] != 0;
     E.gkey.clear();  // a captured MD-step graph holds the old launches: capture again
     return PIMD_OK;
 }

@@ -117,6 +117,15 @@ struct KP {
     int fx_s0;             // first site the tensor-core passes write (sites below are not in Fx)
     float4 *gq23;          // [GQ_N] cubic pieces of h(u) = Gamma(2/3) Q(2/3, u^3) exp(u^3) (mixed.cu)
     float4 *dipf;          // [P][S] FP32 copy of the induced dipoles (written with every update)
+    // asynchronous real-space dipole field (mixed engine, TTM3-F, tensor-core field pass): the
+    // field pass does not wait for k_dd_real_m; of the two, the last to finish a unit of 128
+    // dipole sites runs the unit's SOR update, which writes the other FP32 dipole buffer (the
+    // real-space gathers of the iteration may still be reading this one)
+    int dd_async;          // the dipole iterations run so (0: the field pass runs the SOR)
+    int unit_sbase, nunits;  // first site of unit 0 (a multiple of 32), units per bead
+    float4 *dipf_alt;      // [P][S] the second FP32 dipole buffer
+    float4 *Erec;          // [P][S] reciprocal field of the iteration at the dipole sites
+    unsigned *unit_cnt;    // [P][nunits] arrivals at each unit (reset by the last)
     int *fcnt, *foff;      // [P][N] full neighbour list counts / offsets
     int *fnbr;             // [P][fcap] full neighbour list (j ascending per i)
     int *fntot;            // [P] full-list length
@@ -169,6 +178,11 @@ PIMD_D bool bead_converged(const KP &kp, int b) {
     return (u & 0x7fffffffffffffffULL) != 0ULL;
 }
 
+// The FP32 dipoles an iteration reads and the buffer its SOR update writes: the same buffer
+// unless the real-space field runs asynchronously (then iteration d + 1 reads buffer d & 1).
+PIMD_D const float4 *dipf_cur(const KP &kp) { return (kp.dd_async && (kp.dstep[1] & 1)) ? kp.dipf_alt : kp.dipf; }
+PIMD_D float4 *dipf_next(const KP &kp) { return (kp.dd_async && !(kp.dstep[1] & 1)) ? kp.dipf_alt : kp.dipf; }
+
 // replica of bead b and its centroid sites (posc[replica][S])
 PIMD_HD int rep_of(const KP &kp, int b) { return kp.brep ? kp.brep[b] : 0; }
 PIMD_HD const double4_32a *posc_of(const KP &kp, int b) { return kp.posc + (size_t)rep_of(kp, b) * kp.S; }
@@ -204,6 +218,7 @@ struct Engine {
     bool nbr_cells = true; // cell lists for N > 1024 when the box holds >= 4 cells per edge
     bool wave_shapes = true;  // k-slices / site groups chosen by wave quantisation (occupancy API)
     bool dd_overlap = true;   // mixed engine: real-space dipole field beside the structure factor
+    bool dd_async = false;    // ... and beside the field pass too, the SOR by the last to finish (TTM3-F)
     // tensor-core (tcgen05, 3xTF32) dipole structure factor of the mixed engine (ewald_tc.cu)
     bool sf_tc = true;        // use it when tc_ready
     bool tc_ready = false;    // run groups built and the table tensor map encoded
@@ -372,6 +387,8 @@ cudaError_t mixed_init(Engine &E);  // FP32 lookup tables of the mixed engine
 void launch_site_offsets(Engine &E);
 void launch_pair_qq_m(Engine &E);
 void launch_dd_real_m(Engine &E);
+bool dd_async_ok(const Engine &E);
+void launch_dipf_sync(Engine &E);
 void launch_pair_force_m(Engine &E);
 // launchers (ewald.cu)
 void ewald_init(Engine &E);

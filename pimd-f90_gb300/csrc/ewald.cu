@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(SF_MAXT) k_sfac_f(KP kp, int s0, int nsites, i
                 if (OP == OP_Q)
                     w.x = (float)kp.pos[gs].w;
                 else
-                    w = kp.dipf[gs];  // FP32 copy written with every dipole update
+                    w = dipf_cur(kp)[gs];  // FP32 copy written with every dipole update
             }
             wt[tid] = w;
         }

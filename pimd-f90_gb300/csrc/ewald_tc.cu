@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
         mbar_expect_tx(&tfull[tb], 2 * box_tx + mub);
         tma_load_2d(dst, &tmap, 2 * sfirst, b * kp.ntab, &tfull[tb]);
         tma_load_2d(dst + L.boxb, &tmap, 2 * sfirst + 32, b * kp.ntab, &tfull[tb]);
-        const float4 *wsrc = (OP == TC_OP_Q) ? kp.posf : kp.dipf;  // (offset, q) or (mu, 0)
+        const float4 *wsrc = (OP == TC_OP_Q) ? kp.posf : dipf_cur(kp);  // (offset, q) or (mu, 0)
         bulk_load(dst + L.mu, wsrc + (size_t)b * kp.S + sfirst, mub, &tfull[tb]);
     };
     if (tid == 0) {
@@ -671,6 +671,11 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     if (MODE == TF_D && bead_converged(kp, b)) {
         // converged bead: no update, but the block still counts towards the convergence test
         const double zero[2] = {0.0, 0.0};
+        if (kp.dd_async) {  // (a unit's arrivals still complete it)
+            const float z[3] = {0.f, 0.f, 0.f};
+            if (dd_unit_arrive(kp, b, t)) dd_unit_sor<TF_NT>(kp, b, t, false, z);
+            return;
+        }
         dd_block_end<TF_NT>(kp, b, zero, false);
         return;
     }
@@ -768,7 +773,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     const int s_own = sb + tid;
     const bool own = tid < TF_SITES && s_own >= a.s_lo && s_own < a.s_hi;
     DdSite din;
-    if (MODE == TF_D && own) dd_sor_load(kp, b, s_own, din);
+    if (MODE == TF_D && own && !kp.dd_async) dd_sor_load(kp, b, s_own, din);
     err |= (uint32_t)umma::mbar_wait(&wbar, 0, TC_WAIT);
     const float2 *W = reinterpret_cast<const float2 *>(sm + L.W);
     // V of runs [p0, p0 + nrow): run p0 + pl, component c at row vrow0 + c nrow + pl; 8 halves
@@ -1003,6 +1008,14 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
             kp.dR[3 * gs + 2] -= q * (double)e[2];
             if (MODE == TF_QG && s_own >= kp.fq) kp.F[gs].w += (double)e[3];
         }
+        return;
+    }
+    if (kp.dd_async) {
+        // the real-space field runs beside this pass: store the reciprocal field, arrive, and
+        // run the unit's SOR update if the real-space blocks of its molecules are done
+        if (own && !bad) kp.Erec[(size_t)b * kp.S + s_own] = make_float4(e[0], e[1], e[2], 0.f);
+        const float er[3] = {e[0], e[1], e[2]};
+        if (dd_unit_arrive(kp, b, t)) dd_unit_sor<TF_NT>(kp, b, t, own && !bad, er);
         return;
     }
     // the iteration's FP64 SOR update at the CTA's dipole sites, then the block's end

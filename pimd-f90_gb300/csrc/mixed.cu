@@ -18,6 +18,7 @@
 #include <cmath>
 
 #include "engine.h"
+#include "dipole_check.cuh"
 
 namespace pimd {
 
@@ -373,14 +374,11 @@ __global__ void __launch_bounds__(128) k_dd_tensors_m(KP kp) {
 // from the per-entry cache of k_dd_tensors_m, or, with OTF, from smear2 in the loop (no cache
 // stream, more arithmetic; the autotuner tries both).
 template <int MODEL, bool OTF>
-__global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
+PIMD_D void dd_real_mol(const KP &kp, int i, int b, int lane) {
     using T = TM<MODEL>;
-    const int lane = threadIdx.x & 31;
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, b = blockIdx.y, N = kp.N;
-    if (i >= N) return;
-    if (bead_converged(kp, b)) return;
+    const int N = kp.N;
     const double *dip = kp.dip + (size_t)b * kp.S * 3;
-    const float4 *dipf = kp.dipf + (size_t)b * kp.S;
+    const float4 *dipf = dipf_cur(kp) + (size_t)b * kp.S;
     const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
     const int *fj = kp.fj + (size_t)b * kp.fcap;
     const float2 *Tb = kp.Tf + (size_t)b * kp.fcap * kp.ndd;
@@ -482,6 +480,32 @@ __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
     for (int k = T::FDI; k <= T::LDI; k++)
 #pragma unroll
         for (int c = 0; c < 3; c++) Ef[3 * ((k - 1) * N + i) + c] = (double)ei[k][c];
+}
+
+// ASYNC (TTM3-F): the block then arrives at the units of its molecules' M sites and runs the
+// SOR update of those it completes (dipole_check.cuh); converged beads and molecules past N
+// still arrive.
+template <int MODEL, bool OTF, bool ASYNC>
+__global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
+    const int lane = threadIdx.x & 31;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, b = blockIdx.y;
+    if (i < kp.N && !bead_converged(kp, b)) dd_real_mol<MODEL, OTF>(kp, i, b, lane);
+    if constexpr (ASYNC) {
+        const int m0 = blockIdx.x * 4, m1 = min(m0 + 4, kp.N) - 1;
+        const int t0 = (kp.fd + m0 - kp.unit_sbase) >> 7, t1 = (kp.fd + m1 - kp.unit_sbase) >> 7;
+        const float z[3] = {0.f, 0.f, 0.f};
+        for (int t = t0; t <= t1; t++)
+            if (dd_unit_arrive(kp, b, t)) dd_unit_sor<128>(kp, b, t, false, z);
+    }
+}
+
+// After asynchronous iterations the last FP32 dipoles of a bead sit in either buffer: refresh
+// the main one from the FP64 dipoles (the same rounding as the SOR update's)
+__global__ void __launch_bounds__(128) k_dipf_sync(KP kp) {
+    const int s = kp.fd + blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (s >= kp.ld) return;
+    const size_t gs = (size_t)b * kp.S + s;
+    kp.dipf[gs] = make_float4((float)kp.dip[3 * gs], (float)kp.dip[3 * gs + 1], (float)kp.dip[3 * gs + 2], 0.f);
 }
 
 PIMD_D void dd_force_f(const float R[3], const float di[3], const float dj[3], float t2, float t3, float dij[3]) {
@@ -706,9 +730,29 @@ void launch_dd_real_m(Engine &E) {
     dim3 g((E.kp.N * 32 + 127) / 128, E.kp.P);
     E.kp.l2keep = E.l2_keep ? 1 : 0;
     if (E.kp.model == 2)
-        E.dd_otf ? k_dd_real_m<2, true><<<g, 128, 0, E.stream>>>(E.kp) : k_dd_real_m<2, false><<<g, 128, 0, E.stream>>>(E.kp);
+        E.dd_otf ? k_dd_real_m<2, true, false><<<g, 128, 0, E.stream>>>(E.kp)
+                 : k_dd_real_m<2, false, false><<<g, 128, 0, E.stream>>>(E.kp);
+    else if (E.kp.dd_async)
+        E.dd_otf ? k_dd_real_m<3, true, true><<<g, 128, 0, E.stream>>>(E.kp)
+                 : k_dd_real_m<3, false, true><<<g, 128, 0, E.stream>>>(E.kp);
     else
-        E.dd_otf ? k_dd_real_m<3, true><<<g, 128, 0, E.stream>>>(E.kp) : k_dd_real_m<3, false><<<g, 128, 0, E.stream>>>(E.kp);
+        E.dd_otf ? k_dd_real_m<3, true, false><<<g, 128, 0, E.stream>>>(E.kp)
+                 : k_dd_real_m<3, false, false><<<g, 128, 0, E.stream>>>(E.kp);
+    ++E.nlaunch;
+}
+
+// Whether the dipole iterations can run with the asynchronous real-space field: mixed engine,
+// TTM3-F (M-site dipoles, in molecule order), the tensor-core structure factor and field pass,
+// the second stream, and the buffers of the protocol.
+bool dd_async_ok(const Engine &E) {
+    const KP &kp = E.kp;
+    return E.dd_async && E.dd_overlap && E.loop_aux && E.precision == PIMD_MIXED && kp.model == 3 && E.tc_ready &&
+           E.sf_tc && E.tf_ready && E.ff_tc && kp.Erec && kp.unit_cnt && kp.dipf_alt && kp.ld - kp.fd == kp.N;
+}
+
+void launch_dipf_sync(Engine &E) {
+    dim3 g((E.kp.ld - E.kp.fd + 127) / 128, E.kp.P);
+    k_dipf_sync<<<g, 128, 0, E.stream>>>(E.kp);
     ++E.nlaunch;
 }
 
