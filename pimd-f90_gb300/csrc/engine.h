@@ -242,6 +242,8 @@ struct Engine {
     int tf_nr = 0, tf_nph = 0, tf_jm = 0, tf_ncol = 0, tf_kq = 0;
     bool tf_qd_ready = false;         // the force-pass modes (charge / dipole halves of ewald_std_qd)
     int tf_nphd = 0, tf_ncold = 0;    // runs per pass and V rows of the dipole-force mode
+    int tf_vpp = 0, tf_wglob = 0;     // field passes: V built per pass (> 2 passes), weights read from global
+    int tf_wglob_d = 0;               // the same for the dipole-force mode's weights
     const int2 *d_tfkpm = nullptr;    // per (run slot, j): k-vectors of kz = +j, -j
     alignas(64) unsigned char tc_map[128];  // CUtensorMap of the FP32 tables tabf
     size_t cap = 0;

@@ -74,8 +74,11 @@ enum { TC_OP_Q = 0, TC_OP_MU = 1, TC_OP_DIP = 2 };
 // the dipole structure factor, TF_DG the dipole force from the total (charge + dipole) one
 enum { TF_Q = 0, TF_D = 1, TF_QG = 2, TF_DG = 3 };
 
+// A run group: slots [p0, p0 + nr), MMA columns, the |kz| rows j0 .. j0 + jm - 1 of its Z
+// operand (6 jm <= 128: |kz| above 20 goes to band groups, j0 = 21, of the same runs), k-vectors
+// (local indices; those of a run outside the group's |kz| rows are entries with k = -1)
 struct TcGroup {
-    int p0, nr, ncol, jm, nkl, kgoff, pad0, pad1;  // slots, runs, MMA columns, kz rows, k-vectors
+    int p0, nr, ncol, jm, nkl, kgoff, j0, pad1;
 };
 
 // k-vector of a local index and its 4 pi Ak / V
@@ -333,7 +336,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
             const int zr = zi >> 1, c = zr / (2 * jm);
             zoff[u] = rowchunk(zr, zi & 1);
             zmo[u] = c * TC_SS + 8 * (zi & 1);         // component row of muz, first site
-            zer[u] = yrow + kp.kmax + 1 + ((zr >> 1) % jm);  // ez row of j
+            zer[u] = yrow + kp.kmax + 1 + G.j0 + ((zr >> 1) % jm);  // ez row of |kz| = j0 + j
             zcs[u] = zr & 1;
             zq[u] = 8 * (zi & 1);
         }
@@ -520,7 +523,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
         }
         __syncthreads();
         for (int i = tid; i < TC_CH * jm; i += TC_NT) {
-            const int q = i % TC_CH, j = i / TC_CH, p = ch * TC_CH + q;
+            const int q = i % TC_CH, jj = i / TC_CH, p = ch * TC_CH + q, j = G.j0 + jj;  // row jj: |kz| = j
             if (p >= nr) continue;
             const int4 sl = sslot[p];  // run, local offset, kzlo, nkz
             const bool plus = j >= sl.z && j < sl.z + sl.w;
@@ -529,7 +532,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
             float2 gp[NCZ], gm[NCZ];
 #pragma unroll
             for (int c = 0; c < NCZ; c++) {
-                const int rc = (c * jm + j) * 2;
+                const int rc = (c * jm + jj) * 2;
                 // (x, y) = (Re exy, Im exy) against mu_c c_j (row rc) and mu_c s_j (row rc + 1)
                 const float2 dc = *reinterpret_cast<const float2 *>(stg + rc * TC_LD + 2 * q);
                 const float2 ds = *reinterpret_cast<const float2 *>(stg + (rc + 1) * TC_LD + 2 * q);
@@ -573,6 +576,7 @@ __global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CU
     if (!bad) {
         const uint32_t pbase = umma::smem_u32(pt);
         auto reduce_one = [&](int i, const TcKW &kw) {
+            if (kw.k < 0) return;  // a k-vector of the run that another (band) group sums
 #pragma unroll
             for (int e = 0; e < NPT; e++) {
                 float2 v[TC_CLMAX];
@@ -642,6 +646,8 @@ struct TfArgs {
     int nr, nph, ncol, kq, jm;  // runs, runs per pass (rounded up to 8), V rows (8 nph), K terms (x16), kz rows
     int sbase, s_lo, s_hi;
     int pdl;  // launched as a programmatic dependent of the structure factor (pdl_wait before W)
+    int vpp;    // more than two passes: V of each pass built before it (4 nph rows), as TF_DG does
+    int wglob;  // the bead's weights read from global memory (too many k-vectors for shared memory)
 };
 
 struct TfSmem {
@@ -662,9 +668,11 @@ PIMD_D int rowchunk_k(int n, int jc, int kcm) { return (((n >> 3) * kcm + jc) <<
 template <int MODE>
 __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ CUtensorMap tmap, KP kp, TfArgs a) {
     // TF_DG: 6 components per run (T0, T1 and T2 = sum kz^2 W ez, complex), V rebuilt for each
-    // pass of nph runs; the other modes: 4 components, V of both passes built once
+    // pass of nph runs; the other modes: 4 components, V of both passes built once (or, with
+    // a.vpp, V of each pass before it, for more than two passes)
     constexpr bool DG = MODE == TF_DG;
     constexpr int NC = DG ? 6 : 4;
+    const bool vpp = DG || a.vpp;
     const int t = blockIdx.x, b = blockIdx.y;
     // the next iteration's structure factor may be scheduled now; it waits for this grid
     if (MODE == TF_D) pdl_launch_dependents();
@@ -680,13 +688,13 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         return;
     }
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const TfSmem L(kp.ntab, a.ncol, a.kq, kp.nk, DG ? 2 : 1);
+    const TfSmem L(kp.ntab, a.ncol, a.kq, kp.nk, a.wglob ? 0 : (DG ? 2 : 1));
     extern __shared__ __align__(1024) unsigned char sm_raw[];
     unsigned char *sm = sm_raw + ((1024u - (umma::smem_u32(sm_raw) & 1023u)) & 1023u);
     __shared__ uint64_t tbar, wbar, mbar;
     __shared__ uint32_t tslot;
-    // per run: byte offsets of the ex and ey table rows in a stage and their swizzle keys (16 x
-    // (row & 7)); bit 0 of the ey key: ky < 0 (conjugate ey)
+    // per run of the current pass: byte offsets of the ex and ey table rows in a stage and their
+    // swizzle keys (16 x (row & 7)); bit 0 of the ey key: ky < 0 (conjugate ey)
     __shared__ int4 sroff[TC_MAXRUN];
     __shared__ float2 sskv[TC_MAXRUN];
     const int sb = a.sbase + t * TF_SITES;
@@ -696,7 +704,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
         umma::mbar_init(&wbar, 1);
         umma::mbar_init(&mbar, 1);
         // weight slots: charge (0), dipole (1); TF_DG takes both (adjacent in Wf)
-        if (!a.pdl) {
+        if (!a.pdl && !a.wglob) {
             const int slot = (MODE == TF_D || MODE == TF_QG) ? 1 : 0;
             const uint32_t wbytes = (uint32_t)kp.nk * 8u * (DG ? 2u : 1u);
             mbar_expect_tx(&wbar, wbytes);
@@ -708,15 +716,20 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     }
     const int iter = kp.dstep[1] + 1;  // dipole iteration of this update
     const int kcm = a.kq / 8, nr = a.nr, nph = a.nph, jm = a.jm;
-    const int npass = DG ? (nr + nph - 1) / nph : 2;
+    const int npass = vpp ? (nr + nph - 1) / nph : 2;
     const int yrow = kp.hmax + 1, zrow = yrow + kp.kmax + 1;
-    if (tid < nr) {
-        const int kxy = a.slot[tid].x, kx = kxy & 255, ky = (kxy >> 8) - 128;
-        const int ry = yrow + (ky < 0 ? -ky : ky);
-        sroff[tid] = make_int4(kx * 128, (kx & 7) << 4, ry * 128, ((ry & 7) << 4) | (ky < 0 ? 1 : 0));
-        const float ws = DG ? 1.f : 1.f / TF_WS;  // TF_DG scales its sums once at the end
-        sskv[tid] = make_float2(a.skv[tid].x * ws, a.skv[tid].y * ws);
-    }
+    // the runs of a pass (pass-local index; the caller syncs before the epilogue reads them)
+    auto load_runs = [&](int pass) {
+        const int p = pass * nph + tid;
+        if (tid < nph && p < nr) {
+            const int kxy = a.slot[p].x, kx = kxy & 255, ky = (kxy >> 8) - 128;
+            const int ry = yrow + (ky < 0 ? -ky : ky);
+            sroff[tid] = make_int4(kx * 128, (kx & 7) << 4, ry * 128, ((ry & 7) << 4) | (ky < 0 ? 1 : 0));
+            const float ws = DG ? 1.f : 1.f / TF_WS;  // TF_DG scales its sums once at the end
+            sskv[tid] = make_float2(a.skv[p].x * ws, a.skv[p].y * ws);
+        }
+    };
+    load_runs(0);
     if (warp == 0) umma::tmem_alloc(&tslot, 512);
     // the (k(+j), k(-j)) pairs and k_z of a V item (run p0 + it % nrow, j = 4 (it / nrow) + e):
     // this thread's first item of each early V build is fetched now, before the weights land
@@ -733,7 +746,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     int2 km0[4], km1[4];
     float kz0[4], kz1[4];
     fetch_km(0, nph, tid, km0, kz0);
-    fetch_km(DG ? 0 : nph, nph, tid, km1, kz1);
+    fetch_km(vpp ? 0 : nph, nph, tid, km1, kz1);
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
@@ -762,7 +775,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     // and the iteration's dipoles and fields (a programmatic launch waits for them here)
     if (a.pdl) {
         pdl_wait();
-        if (tid == 0) {
+        if (tid == 0 && !a.wglob) {
             const int slot = (MODE == TF_D || MODE == TF_QG) ? 1 : 0;
             const uint32_t wbytes = (uint32_t)kp.nk * 8u * (DG ? 2u : 1u);
             mbar_expect_tx(&wbar, wbytes);
@@ -774,8 +787,9 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     const bool own = tid < TF_SITES && s_own >= a.s_lo && s_own < a.s_hi;
     DdSite din;
     if (MODE == TF_D && own && !kp.dd_async) dd_sor_load(kp, b, s_own, din);
-    err |= (uint32_t)umma::mbar_wait(&wbar, 0, TC_WAIT);
-    const float2 *W = reinterpret_cast<const float2 *>(sm + L.W);
+    if (!a.wglob) err |= (uint32_t)umma::mbar_wait(&wbar, 0, TC_WAIT);
+    const float2 *W = a.wglob ? kp.Wf + ((size_t)b * 2 + ((MODE == TF_D || MODE == TF_QG) ? 1 : 0)) * kp.nk
+                              : reinterpret_cast<const float2 *>(sm + L.W);
     // V of runs [p0, p0 + nrow): run p0 + pl, component c at row vrow0 + c nrow + pl; 8 halves
     // (4 j) per item, zero for runs >= nr and j >= jm
     auto build_v = [&](int p0, int nrow, int vrow0, const int2 (&kmf)[4], const float (&kzf)[4]) {
@@ -831,7 +845,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
             }
         }
     };
-    if (!DG) {  // both passes: pass q's rows from q 4 nph
+    if (!vpp) {  // both passes: pass q's rows from q 4 nph
         build_v(0, nph, 0, km0, kz0);
         build_v(nph, nph, 4 * nph, km1, kz1);
     }
@@ -852,7 +866,8 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     }
     bool bad = err != 0;
     for (int pass = 0; pass < npass; pass++) {
-        if (DG) {
+        if (pass > 0) load_runs(pass);  // (the previous pass's epilogue is past its last sync)
+        if (vpp) {
             if (pass == 0) {
                 build_v(0, nph, 0, km0, kz0);
             } else {
@@ -873,7 +888,7 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
                 const int N = min(256, NC * nph - c0);
                 const uint32_t id = idesc_base | ((uint32_t)(N >> 3) << 17);
                 const uint32_t d = tm + (uint32_t)c0;
-                const int vr = (DG ? 0 : pass * 4 * nph) + c0;  // first V row of the MMA
+                const int vr = (vpp ? 0 : pass * 4 * nph) + c0;  // first V row of the MMA
                 const uint32_t vo = (uint32_t)((vr >> 3) * kcm * 128);
                 for (int ks = 0; ks < a.kq / 16; ks++) {
                     const uint64_t dq_h = umma::sdesc(qh + ks * 256, 128, kcm * 128), dq_l = umma::sdesc(ql + ks * 256, 128, kcm * 128);
@@ -904,13 +919,13 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
                 const int pl = pl0 + e, p = pass * nph + pl;
                 if (pl >= (part + 1) * q4 || p >= nr) break;
                 // tab_elem(sm, boxb, row, sl) with the run's row offsets and keys precomputed
-                const int4 ro = sroff[p];
+                const int4 ro = sroff[pl];
                 const float2 ex = *reinterpret_cast<const float2 *>(tsite + ro.x + (cs4 ^ ro.y));
                 float2 ey = *reinterpret_cast<const float2 *>(tsite + ro.z + (cs4 ^ (ro.w & ~1)));
                 if (ro.w & 1) ey.y = -ey.y;
                 // ewald.f90:30-31: coskxky = cx cy - sx sy, sinkxky = sx cy + cx sy
                 const float er = ex.x * ey.x - ex.y * ey.y, ei = ex.y * ey.x + ex.x * ey.y;
-                const float2 kv = sskv[p];
+                const float2 kv = sskv[pl];
                 if constexpr (DG) {
                     // sum_k k (k . mu) Re(e W) with the run's kz sums (ewald.f90:146-187)
                     const float R0 = fmaf(er, v[e], -ei * v[16 + e]);       // Re(exy T0)
@@ -1077,35 +1092,59 @@ void tc_init(Engine &E) {
         order[r] = r;
     }
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return jr[x] > jr[y]; });
-    std::vector<int4> slots(kp.nrun);
-    std::vector<float2> skv(kp.nrun);
+    // slots: every run once with its |kz| rows below TC_JB, then the runs reaching beyond once
+    // per further band of TC_JB rows (j0 = TC_JB, 2 TC_JB, ...), each band in groups of <= 256
+    // slots; a slot's k-vectors outside its group's rows are local entries with k = -1
+    constexpr int TC_JB = 21;  // 6 TC_JB <= 128 Z rows
+    std::vector<int2> src;     // (run, j0)
+    for (int q = 0; q < kp.nrun; q++) src.push_back(make_int2(order[q], 0));
+    for (int j0 = TC_JB;; j0 += TC_JB) {
+        const size_t n0 = src.size();
+        for (int q = 0; q < kp.nrun; q++)
+            if (jr[order[q]] > j0) src.push_back(make_int2(order[q], j0));
+        if (src.size() == n0) break;
+    }
+    const int nslot = (int)src.size();
+    std::vector<int4> slots(nslot);
+    std::vector<float2> skv(nslot);
     std::vector<TcGroup> groups;
     std::vector<TcKW> kloc;
     std::vector<float2> runkf(kp.nrun);
     for (int r = 0; r < kp.nrun; r++)
         runkf[r] = make_float2((float)E.h_kvec[3 * E.h_runs[r].kbeg], (float)E.h_kvec[3 * E.h_runs[r].kbeg + 1]);
-    int ncolmax = 16, nklmax = 0;
-    for (int p0 = 0; p0 < kp.nrun; p0 += TC_MAXRUN) {
-        TcGroup g{p0, std::min(TC_MAXRUN, kp.nrun - p0), 0, jr[order[p0]], 0, (int)kloc.size(), 0, 0};
-        if (6 * g.jm > 128) return;
-        {   // the builders' Z items fit TC_ZMAX per thread (the kernel's split of warps)
-            const int zw = std::max(1, TC_NB - (2 * g.nr + 31) / 32);
-            if ((12 * g.jm + 32 * zw - 1) / (32 * zw) > TC_ZMAX) return;
-        }
+    int ncolmax = 16, nklmax = 0, nvalid = 0;
+    // while a group's X is built, its 2 nr X items take whole builder warps first and the Z items
+    // (12 jm at most) the warps left over, TC_ZMAX per thread: the most runs a group of jm rows holds
+    auto zfit = [](int nr, int jm) {
+        const int zw = std::max(1, TC_NB - (2 * nr + 31) / 32);
+        return (12 * jm + 32 * zw - 1) / (32 * zw) <= TC_ZMAX;
+    };
+    for (int p0 = 0; p0 < nslot;) {
+        const int j0 = src[p0].y, jmg = std::min(TC_JB, jr[src[p0].x] - j0);
+        int nr = 0;
+        while (p0 + nr < nslot && nr < TC_MAXRUN && src[p0 + nr].y == j0 && zfit(nr + 1, jmg)) nr++;
+        if (nr == 0) return;
+        TcGroup g{p0, nr, 0, jmg, 0, (int)kloc.size(), j0, 0};
         g.ncol = ((2 * g.nr + 15) / 16) * 16;
         for (int p = p0; p < p0 + g.nr; p++) {
-            const int r = order[p];
+            const int r = src[p].x;
             const KRun &run = E.h_runs[r];
             slots[p] = make_int4(run.kx + 256 * (run.ky + 128), g.nkl, run.kzlo, run.nkz);
             skv[p] = runkf[r];
-            for (int j = 0; j < run.nkz; j++) kloc.push_back(TcKW{run.kbeg + j, (float)(FOURPI * E.h_Ak[run.kbeg + j] / kp.volume)});
+            for (int j = 0; j < run.nkz; j++) {
+                const int akz = std::abs(run.kzlo + j);
+                const bool mine = akz >= j0 && akz < j0 + g.jm;
+                nvalid += mine;
+                kloc.push_back(TcKW{mine ? run.kbeg + j : -1, (float)(FOURPI * E.h_Ak[run.kbeg + j] / kp.volume)});
+            }
             g.nkl += run.nkz;
         }
         groups.push_back(g);
         ncolmax = std::max(ncolmax, g.ncol);
         nklmax = std::max(nklmax, g.nkl);
+        p0 += nr;
     }
-    if ((int)kloc.size() != kp.nk) return;
+    if (nvalid != kp.nk) return;  // every k-vector in exactly one group
     // dynamic shared memory available: the opt-in limit minus the kernel's static part
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, E.device);
@@ -1193,14 +1232,10 @@ void tc_init(Engine &E) {
     E.tc_ncolmax = ncolmax;
     E.tc_nabuf = nabuf;
     E.tc_ready = true;
-    // field kernel: one run group; per (slot, j) the k-vectors of kz = +j and -j
+    // field kernel: every run once (the first kp.nrun slots, in the same order), K over its
+    // whole |kz| range; per (run, j) the k-vectors of kz = +j and -j
     E.tf_ready = false;
-    if (groups.size() != 1) return;
-    const int nr = groups[0].nr, jm = groups[0].jm;
-    // two passes of nph runs (a multiple of 8) x 4 components in TMEM, plus the columns the last
-    // 16-run load of a run quarter reaches past the pass
-    const int nph = ((nr + 1) / 2 + 7) / 8 * 8, ncolf = 8 * nph, kq = ((2 * jm + 15) / 16) * 16;
-    if (4 * nph + 16 > 512) return;
+    const int nr = kp.nrun, jm = jr[order[0]], kq = ((2 * jm + 15) / 16) * 16;
     cudaFuncAttributes fb[4];
     if (cudaFuncGetAttributes(&fb[0], k_field_tc<TF_Q>) != cudaSuccess || cudaFuncGetAttributes(&fb[1], k_field_tc<TF_D>) != cudaSuccess ||
         cudaFuncGetAttributes(&fb[2], k_field_tc<TF_QG>) != cudaSuccess || cudaFuncGetAttributes(&fb[3], k_field_tc<TF_DG>) != cudaSuccess) {
@@ -1210,8 +1245,6 @@ void tc_init(Engine &E) {
     size_t fstat = 0;
     for (int i = 0; i < 4; i++) fstat = std::max(fstat, fb[i].sharedSizeBytes);
     const int dmaxf = optin - (int)fstat;
-    // the weights arrive by one bulk copy: 8 nk bytes, a multiple of 16
-    if (TfSmem(kp.ntab, ncolf, kq, kp.nk).total > dmaxf || kp.ntab > 128 || (kp.nk & 1)) return;
     if (cudaFuncSetAttribute(k_field_tc<TF_D>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess ||
         cudaFuncSetAttribute(k_field_tc<TF_Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess ||
         cudaFuncSetAttribute(k_field_tc<TF_QG>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess ||
@@ -1219,6 +1252,27 @@ void tc_init(Engine &E) {
         cudaGetLastError();
         return;
     }
+    // passes: two passes of nph runs (a multiple of 8) x 4 components in TMEM with V of both built
+    // once, when that fits (plus the 16 columns the last 16-run load of a run quarter reaches past
+    // a pass); else passes of nph runs with V of each built before it. The bead's weights sit in
+    // shared memory (one bulk copy: 8 nk bytes, a multiple of 16) when they fit, else the V
+    // builders read them from global memory.
+    auto fits = [&](int nph_, int vpp_, int wglob_, int ncomp, int nslot_) {
+        return ncomp * nph_ + 16 <= 512 && TfSmem(kp.ntab, (vpp_ ? ncomp : 2 * ncomp) * nph_, kq, kp.nk, wglob_ ? 0 : nslot_).total <= dmaxf;
+    };
+    const bool w_ok = (kp.nk & 1) == 0;
+    int nph = ((nr + 1) / 2 + 7) / 8 * 8, vpp = 0, wglob = w_ok ? 0 : 1;
+    if (!fits(nph, 0, wglob, 4, 1)) {
+        vpp = 1;
+        for (wglob = w_ok ? 0 : 1; wglob < 2; wglob++) {
+            for (nph = std::min(120, (nr + 7) / 8 * 8); nph > 8 && !fits(nph, 1, wglob, 4, 1); nph -= 8) {
+            }
+            if (fits(nph, 1, wglob, 4, 1)) break;
+        }
+        if (wglob == 2) return;
+    }
+    const int ncolf = (vpp ? 4 : 8) * nph;
+    if (kp.ntab > 128) return;
     std::vector<int2> kpm((size_t)nr * jm, make_int2(-1, -1));
     for (int p = 0; p < nr; p++) {
         const KRun &run = E.h_runs[order[p]];
@@ -1242,14 +1296,23 @@ void tc_init(Engine &E) {
     E.tf_jm = jm;
     E.tf_ncol = ncolf;
     E.tf_kq = kq;
+    E.tf_vpp = vpp;
+    E.tf_wglob = wglob;
     E.tf_ready = true;
     // dipole-force mode: 6 components per run, passes of nphd runs (a multiple of 8) with
-    // 6 nphd + 16 <= 512 TMEM columns, V of one pass at a time, both weight slots resident
+    // 6 nphd + 16 <= 512 TMEM columns, V of one pass at a time, both weight slots in shared
+    // memory when they fit
     const int npd = (nr + 79) / 80;
-    const int nphd = ((nr + npd - 1) / npd + 7) / 8 * 8, ncold = 6 * nphd;
-    E.tf_qd_ready = 6 * nphd + 16 <= 512 && TfSmem(kp.ntab, ncold, kq, kp.nk, 2).total <= dmaxf;
+    int nphd = ((nr + npd - 1) / npd + 7) / 8 * 8, wgd = w_ok ? 0 : 1;
+    for (; wgd < 2; wgd++) {
+        for (nphd = ((nr + npd - 1) / npd + 7) / 8 * 8; nphd > 8 && !fits(nphd, 1, wgd, 6, 2); nphd -= 8) {
+        }
+        if (fits(nphd, 1, wgd, 6, 2)) break;
+    }
+    E.tf_qd_ready = wgd < 2;
     E.tf_nphd = nphd;
-    E.tf_ncold = ncold;
+    E.tf_ncold = 6 * nphd;
+    E.tf_wglob_d = wgd;
 }
 
 // mode TF_D: dipole field, SOR update and convergence test of one iteration at the dipole sites
@@ -1272,11 +1335,15 @@ int launch_field_tc(Engine &E, int mode, int s0, int s1) {
     a.sbase = s0 & ~(TC_SS - 1);  // TMA x coordinates 2 (sbase + 16 i): 128-byte aligned
     a.s_lo = s0;
     a.s_hi = s1;
+    a.vpp = E.tf_vpp;
+    a.wglob = E.tf_wglob;
     if (mode == TF_DG) {
         a.nph = E.tf_nphd;
         a.ncol = E.tf_ncold;
+        a.vpp = 1;
+        a.wglob = E.tf_wglob_d;
     }
-    const TfSmem L(kp.ntab, a.ncol, a.kq, kp.nk, mode == TF_DG ? 2 : 1);
+    const TfSmem L(kp.ntab, a.ncol, a.kq, kp.nk, a.wglob ? 0 : (mode == TF_DG ? 2 : 1));
     dim3 g((s1 - a.sbase + TF_SITES - 1) / TF_SITES, kp.P);
     const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(E.tc_map);
     a.pdl = 0;

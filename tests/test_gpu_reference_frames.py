@@ -136,20 +136,26 @@ def test_qspcfw_input_32(pkg, orc, engine_lib):
     eng.close()
 
 
-@pytest.mark.parametrize("path", ["fp32_pipe", "default"])
-def test_ewald_large_k_shell(pkg, orc, engine_lib, path):
+@pytest.mark.parametrize("path,nmax", [("fp32_pipe", 24), ("tensor_core", 24), ("tensor_core", 16)])
+def test_ewald_large_k_shell(pkg, orc, engine_lib, path, nmax):
     """The mixed engine's Ewald passes at |n| <= 24 (the large-system k range: 28 888 k-vectors
     there, 29 000 here), TTM3-F on the input_128 frame, one bead, Rc 7.8 A with alpha from the
     eps = 1e-6 rule, as the large system uses: forced onto the FP32-pipe structure-factor and
-    field kernels (sf_tc = ff_tc = 0), and on the default selection. (With a much larger alpha,
-    0.9 / A, the FP32 reciprocal field's rounding floor, ~1.7e-8 D, lies above the 1e-8
-    threshold and the iterations run to polar_maxiter; the forces stay inside the budget.)"""
+    field kernels (sf_tc = ff_tc = 0), and on the tensor-core kernels, which take |kz| > 20 in
+    a second band of run groups and run the field passes in several passes with the weights
+    read from global memory. (With a much larger alpha, 0.9 / A, the FP32 reciprocal field's
+    rounding floor, ~1.7e-8 D, lies above the 1e-8 threshold and the iterations run to
+    polar_maxiter; the forces stay inside the budget.) |n| <= 16 has more runs than two field
+    passes hold but no second band."""
     box, RRt, RRc = frame("input_128", 1)
-    p = params(3, box, RRt.shape[1], 1, 7.8, pkg.waterbox.ewald_alpha_eps(7.8), 24)
+    p = params(3, box, RRt.shape[1], 1, 7.8, pkg.waterbox.ewald_alpha_eps(7.8), nmax)
     eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_MIXED)
+    t = eng.tuning()
     if path == "fp32_pipe":
         t = eng.set_tuning(sf_tc=0, ff_tc=0)
         assert t["sf_tc"] == 0 and t["ff_tc"] == 0 and t["qd_tc"] == 0
+    else:
+        assert t["sf_tc"] == 1 and t["ff_tc"] == 1 and t["qd_tc"] == 1
     got = eng.full_bead_forces(RRt, RRc, t=1)
     o = orc.Oracle(p)
     assert eng.ewald_info()[1] == o.ewald_info()[1]
