@@ -207,8 +207,12 @@ PIMD_D void split8_h(const float (&x)[8], uint4 &hi, uint4 &lo) {
 // FP16 sites (two core matrices along K)
 PIMD_D int rowchunk(int n, int c) { return (((n >> 3) * 2 + c) << 7) + ((n & 7) << 4); }
 
+// 64 registers a thread (a few bytes spill): one CTA of 576 threads then leaves 28 K registers
+// of the SM to the real-space dipole field running beside it on the second stream (4 blocks
+// instead of 1 at 95 registers); the graph step at 512 x 32 measured 677 -> 702 steps/s
+// (72 registers: 695, 56: 697, 48: 680)
 template <int OP>
-__global__ void __launch_bounds__(TC_NT, 1) k_sfac_tc(const __grid_constant__ CUtensorMap tmap, KP kp, TcArgs a) {
+__global__ void __maxnreg__(64) k_sfac_tc(const __grid_constant__ CUtensorMap tmap, KP kp, TcArgs a) {
     // Z components: q (charges) or mu_x, mu_y, mu_z; partial sums per k: S, or the three G_c
     constexpr int NCZ = (OP == TC_OP_Q) ? 1 : 3;
     constexpr int NPT = (OP == TC_OP_DIP) ? 3 : 1;
