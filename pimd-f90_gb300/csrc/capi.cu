@@ -466,13 +466,20 @@ void timer_end(Engine &E) {
 
 // One induced-dipole iteration (pot_ttm.f90:298-390): real-space dipole field, ewald_std_dd
 // structure factor, field + SOR update, convergence test.
-static void dipole_iteration(Engine &E, bool mixed) {
+static void dipole_iteration(Engine &E, bool mixed, bool body_start = false) {
     if (mixed && E.loop_aux && E.dd_overlap) {
         // the real-space field runs on the second stream beside the structure factor (both only
         // read the iteration's dipoles); the field + SOR pass waits for both
         cudaEventRecord(E.loop_fork, E.stream);
         cudaStreamWaitEvent(E.loop_aux, E.loop_fork, 0);
+        // first iteration of a graph loop body: nothing gives the structure factor a head start
+        // (later ones are programmatic dependents of the field pass), so the real-space blocks
+        // would fill the SMs first; they wait until the structure factor's CTAs are resident
+        E.sfac_pev_req = body_start && E.dd_pev && E.loop_pev;
+        E.sfac_pev_armed = false;
         PHASE("dd_smu", launch_ewald_smu(E));
+        if (E.sfac_pev_armed) cudaStreamWaitEvent(E.loop_aux, E.loop_pev, 0);
+        E.sfac_pev_req = false;
         cudaStream_t keep = E.stream;
         E.stream = E.loop_aux;
         PHASE("dd_real", launch_dd_real_m(E));
@@ -526,7 +533,7 @@ static int capture_dipole_loop(Engine &E, bool mixed) {
     // iterations per body: 3 divides the conditional's relaunches by three; an iteration after every bead
     // has converged is empty (each kernel returns at the bead's flag, the test leaves the
     // per-bead counts alone)
-    for (int u = 0; u < std::max(1, E.loop_unroll); u++) dipole_iteration(E, mixed);
+    for (int u = 0; u < std::max(1, E.loop_unroll); u++) dipole_iteration(E, mixed, u == 0);
     E.kp.cond = 0;
     E.stream = keep;
     cudaGraph_t out = nullptr;
@@ -706,6 +713,7 @@ int pimd_destroy(pimd_ctx *ctx) {
     if (E.ev_join) cudaEventDestroy(E.ev_join);
     if (E.loop_aux) cudaStreamDestroy(E.loop_aux);
     if (E.loop_fork) cudaEventDestroy(E.loop_fork);
+    if (E.loop_pev) cudaEventDestroy(E.loop_pev);
     if (E.loop_join) cudaEventDestroy(E.loop_join);
     if (E.own_stream && E.stream) cudaStreamDestroy(E.stream);
     delete ctx;
@@ -1072,6 +1080,7 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     if (n >= 15) k[14] = E.ff_tc && E.tf_ready && E.tf_qd_ready;
     if (n >= 16) k[15] = E.l2_keep && E.precision == PIMD_MIXED;
     if (n >= 17) k[16] = dd_async_ok(E);
+    if (n >= 18) k[17] = E.dd_pev && E.loop_pev != nullptr;
     return PIMD_OK;
 }
 
@@ -1098,6 +1107,7 @@ int pimd_set_tuning(pimd_ctx *ctx, const int *k, int n) {
     if (n >= 14) E.dd_otf = k[13] != 0;
     if (n >= 16) E.l2_keep = k[15] != 0;
     if (n >= 17) E.dd_async = k[16] != 0;
+    if (n >= 18) E.dd_pev = k[17] != 0;
     E.gkey.clear();  // a captured MD-step graph holds the old launches: capture again
     return PIMD_OK;
 }

@@ -274,6 +274,11 @@ struct Engine {
     // loop's body, a graph of its own, which must not share a stream with the outer capture)
     cudaStream_t loop_aux = nullptr;
     cudaEvent_t loop_fork = nullptr, loop_join = nullptr;
+    // at the start of a loop body the real-space field waits on this programmatic event of the
+    // structure factor (all its CTAs resident), so that it does not take the SMs first
+    cudaEvent_t loop_pev = nullptr;
+    bool sfac_pev_req = false, sfac_pev_armed = false;
+    bool dd_pev = true;  // use it (knob)
     cudaGraphExec_t gexec = nullptr;
     std::vector<const void *> gkey;
     long long graph_launches = 0, graph_captures = 0;

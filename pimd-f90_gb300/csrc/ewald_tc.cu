@@ -722,10 +722,12 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     const int kcm = a.kq / 8, nr = a.nr, nph = a.nph, jm = a.jm;
     const int npass = vpp ? (nr + nph - 1) / nph : 2;
     const int yrow = kp.hmax + 1, zrow = yrow + kp.kmax + 1;
-    // the runs of a pass (pass-local index; the caller syncs before the epilogue reads them)
+    // the runs' table offsets: all of them once when they fit the arrays, else those of each
+    // pass before it (index p - rbase; the caller syncs before the epilogue reads them)
+    const bool rall = nr <= TC_MAXRUN;
     auto load_runs = [&](int pass) {
-        const int p = pass * nph + tid;
-        if (tid < nph && p < nr) {
+        const int p = (rall ? 0 : pass * nph) + tid;
+        if (tid < (rall ? nr : nph) && p < nr) {
             const int kxy = a.slot[p].x, kx = kxy & 255, ky = (kxy >> 8) - 128;
             const int ry = yrow + (ky < 0 ? -ky : ky);
             sroff[tid] = make_int4(kx * 128, (kx & 7) << 4, ry * 128, ((ry & 7) << 4) | (ky < 0 ? 1 : 0));
@@ -870,7 +872,8 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
     }
     bool bad = err != 0;
     for (int pass = 0; pass < npass; pass++) {
-        if (pass > 0) load_runs(pass);  // (the previous pass's epilogue is past its last sync)
+        if (pass > 0 && !rall) load_runs(pass);  // (the previous pass's epilogue is past its last sync)
+        const int rbase = rall ? 0 : pass * nph;
         if (vpp) {
             if (pass == 0) {
                 build_v(0, nph, 0, km0, kz0);
@@ -923,13 +926,13 @@ __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ C
                 const int pl = pl0 + e, p = pass * nph + pl;
                 if (pl >= (part + 1) * q4 || p >= nr) break;
                 // tab_elem(sm, boxb, row, sl) with the run's row offsets and keys precomputed
-                const int4 ro = sroff[pl];
+                const int4 ro = sroff[p - rbase];
                 const float2 ex = *reinterpret_cast<const float2 *>(tsite + ro.x + (cs4 ^ ro.y));
                 float2 ey = *reinterpret_cast<const float2 *>(tsite + ro.z + (cs4 ^ (ro.w & ~1)));
                 if (ro.w & 1) ey.y = -ey.y;
                 // ewald.f90:30-31: coskxky = cx cy - sx sy, sinkxky = sx cy + cx sy
                 const float er = ex.x * ey.x - ex.y * ey.y, ei = ex.y * ey.x + ex.x * ey.y;
-                const float2 kv = sskv[pl];
+                const float2 kv = sskv[p - rbase];
                 if constexpr (DG) {
                     // sum_k k (k . mu) Re(e W) with the run's kz sums (ewald.f90:146-187)
                     const float R0 = fmaf(er, v[e], -ei * v[16 + e]);       // Re(exy T0)
@@ -1449,17 +1452,31 @@ int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv) {
         if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess) prio_cache[E.device & 63] = greatest;
         prio_set[E.device & 63] = 1;
     }
-    cudaLaunchAttribute at[3];
+    cudaLaunchAttribute at[4];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = ng;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
     at[1].id = cudaLaunchAttributePriority;
     at[1].val.priority = prio_cache[E.device & 63];
-    at[2].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[2].val.programmaticStreamSerializationAllowed = 1;
+    int na = 2;
+    if (a.pdl) {
+        at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[na].val.programmaticStreamSerializationAllowed = 1;
+        na++;
+    }
+    // the caller's programmatic event: recorded once every CTA has passed its set-up
+    // (griddepcontrol.launch_dependents) or left
+    const bool pev = E.sfac_pev_req && op == TC_OP_MU && E.loop_pev;
+    if (pev) {
+        at[na].id = cudaLaunchAttributeProgrammaticEvent;
+        at[na].val.programmaticEvent.event = E.loop_pev;
+        at[na].val.programmaticEvent.flags = 0;
+        at[na].val.programmaticEvent.triggerAtBlockStart = 0;
+        na++;
+    }
     cfg.attrs = at;
-    cfg.numAttrs = a.pdl ? 3 : 2;
+    cfg.numAttrs = na;
     const CUtensorMap *map = reinterpret_cast<const CUtensorMap *>(E.tc_map);
     cudaError_t e = cudaErrorInvalidValue;
     if (op == TC_OP_MU)
@@ -1468,7 +1485,8 @@ int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv) {
         e = cudaLaunchKernelEx(&cfg, k_sfac_tc<TC_OP_Q>, *map, kp, a);
     else
         e = cudaLaunchKernelEx(&cfg, k_sfac_tc<TC_OP_DIP>, *map, kp, a);
-    if (e != cudaSuccess && a.pdl) {  // the attribute refused: a plain cluster launch
+    if (e == cudaSuccess && pev) E.sfac_pev_armed = true;
+    if (e != cudaSuccess && na > 2) {  // an attribute refused: a plain cluster launch
         cudaGetLastError();
         a.pdl = 0;
         cfg.numAttrs = 2;

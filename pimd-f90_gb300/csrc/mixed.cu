@@ -100,6 +100,7 @@ cudaError_t mixed_init(Engine &E) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E.loop_aux, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.loop_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.loop_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.loop_pev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void **)&E.kp.gq23, sizeof(tab));
     if (e == cudaSuccess) E.allocs.push_back(E.kp.gq23);
     if (e == cudaSuccess) e = cudaMemcpy(E.kp.gq23, tab, sizeof(tab), cudaMemcpyHostToDevice);
@@ -521,8 +522,10 @@ PIMD_D void dd_force_f(const float R[3], const float di[3], const float dj[3], f
 // molecule i over its full-list entries accumulate i's side (gradients at i's sites, the
 // potentials at i's sites from j's dipoles) with virials at weight 1/2, then lane 0 of the group
 // adds the intramolecular terms (pot_ttm.f90:482-542) before the group sums go into dR and F.w.
+// (at most 102 registers, 5 blocks a SM: 99.1 -> 91.6 us at 512 x 32; the charge gather k_pair_qq_m
+// measured slower so bounded, 106.7 -> 108.3 us, and keeps its 121 registers)
 template <int MODEL>
-__global__ void __launch_bounds__(128) k_pair_force_m(KP kp) {
+__global__ void __launch_bounds__(128, 5) k_pair_force_m(KP kp) {
     using T = TM<MODEL>;
     const int b = blockIdx.y, N = kp.N;
     const int sub = threadIdx.x & (QL - 1);
