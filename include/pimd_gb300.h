@@ -324,7 +324,9 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc);
  * n >= 17 [the real-space dipole field beside the field pass too, each unit of 128 dipole
  * sites updated by whichever of the two finishes it last (mixed engine, TTM3-F)], when n >= 18
  * [at the start of each graph-loop body the real-space dipole field waits until every CTA of
- * the structure factor is resident (a programmatic event), mixed engine]; n >= 5. */
+ * the structure factor is resident (a programmatic event), mixed engine], when n >= 19 [the
+ * iterations' field pass may start as the real-space dipole field drains (a programmatic
+ * event; it waits for that grid before reading its output), mixed engine]; n >= 5. */
 int pimd_get_tuning(pimd_ctx *ctx, int *knobs, int n);
 /* Sets the shapes in the order pimd_get_tuning reports them (n >= 5; entry 15, the tensor-core
  * force pass, is a report only), e.g. to reuse an earlier autotune result without timing

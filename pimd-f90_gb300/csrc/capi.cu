@@ -482,14 +482,24 @@ static void dipole_iteration(Engine &E, bool mixed, bool body_start = false) {
         E.sfac_pev_req = false;
         cudaStream_t keep = E.stream;
         E.stream = E.loop_aux;
+        // the field pass, a programmatic dependent of the structure factor, may also start as
+        // the real-space field drains when its griddepcontrol.wait covers that grid too
+        E.dd_jpev_req = E.dd_jpev && !E.kp.dd_async && field_pdl_ok(E);
+        E.dd_jpev_armed = false;
         PHASE("dd_real", launch_dd_real_m(E));
+        E.dd_jpev_req = false;
         E.stream = keep;
         cudaEventRecord(E.loop_join, E.loop_aux);
         // asynchronous: the field pass runs beside the real-space field as well (whichever ends
         // a unit of sites last updates its dipoles); the iteration ends when both are done
-        if (!E.kp.dd_async) cudaStreamWaitEvent(E.stream, E.loop_join, 0);
+        if (E.dd_jpev_armed)
+            cudaStreamWaitEvent(E.stream, E.loop_jpev, 0);
+        else if (!E.kp.dd_async)
+            cudaStreamWaitEvent(E.stream, E.loop_join, 0);
+        E.field_needs_join = E.dd_jpev_armed;
         PHASE("dd_update", launch_dd_update(E));  // includes the convergence test (last block)
-        if (E.kp.dd_async) cudaStreamWaitEvent(E.stream, E.loop_join, 0);
+        E.field_needs_join = false;
+        if (E.kp.dd_async || E.dd_jpev_armed) cudaStreamWaitEvent(E.stream, E.loop_join, 0);
         return;
     }
     if (mixed)
@@ -714,6 +724,7 @@ int pimd_destroy(pimd_ctx *ctx) {
     if (E.loop_aux) cudaStreamDestroy(E.loop_aux);
     if (E.loop_fork) cudaEventDestroy(E.loop_fork);
     if (E.loop_pev) cudaEventDestroy(E.loop_pev);
+    if (E.loop_jpev) cudaEventDestroy(E.loop_jpev);
     if (E.loop_join) cudaEventDestroy(E.loop_join);
     if (E.own_stream && E.stream) cudaStreamDestroy(E.stream);
     delete ctx;
@@ -1081,6 +1092,7 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     if (n >= 16) k[15] = E.l2_keep && E.precision == PIMD_MIXED;
     if (n >= 17) k[16] = dd_async_ok(E);
     if (n >= 18) k[17] = E.dd_pev && E.loop_pev != nullptr;
+    if (n >= 19) k[18] = E.dd_jpev && E.loop_jpev != nullptr && field_pdl_ok(E);
     return PIMD_OK;
 }
 
@@ -1108,6 +1120,7 @@ int pimd_set_tuning(pimd_ctx *ctx, const int *k, int n) {
     if (n >= 16) E.l2_keep = k[15] != 0;
     if (n >= 17) E.dd_async = k[16] != 0;
     if (n >= 18) E.dd_pev = k[17] != 0;
+    if (n >= 19) E.dd_jpev = k[18] != 0;
     E.gkey.clear();  // a captured MD-step graph holds the old launches: capture again
     return PIMD_OK;
 }

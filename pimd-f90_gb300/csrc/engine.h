@@ -279,6 +279,13 @@ struct Engine {
     cudaEvent_t loop_pev = nullptr;
     bool sfac_pev_req = false, sfac_pev_armed = false;
     bool dd_pev = true;  // use it (knob)
+    // the field pass waits on this programmatic event of the real-space field (all its blocks
+    // started) instead of its completion; griddepcontrol.wait in the field pass then waits for
+    // the real-space grid before anything reads its output
+    cudaEvent_t loop_jpev = nullptr;
+    bool dd_jpev_req = false, dd_jpev_armed = false;
+    bool dd_jpev = true;  // use it (knob)
+    bool field_needs_join = false;  // a field pass launched without griddepcontrol.wait must first wait on loop_join
     cudaGraphExec_t gexec = nullptr;
     std::vector<const void *> gkey;
     long long graph_launches = 0, graph_captures = 0;
@@ -413,6 +420,7 @@ int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv);
 // tensor-core field passes (ewald_tc.cu): mode F_D (dipole field, SOR update, convergence test)
 // or F_Q (charge field and potential into F); 1 when launched
 int launch_field_tc(Engine &E, int mode, int s0, int s1);
+bool field_pdl_ok(const Engine &E);
 int launch_field_qd_tc(Engine &E, int s0, int s1);  // ewald_std_qd force pass on the tensor cores
 // launchers (spc.cu): q-SPC/Fw and SPC/F
 void launch_sites_spc(Engine &E);

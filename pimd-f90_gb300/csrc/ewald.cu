@@ -1050,6 +1050,7 @@ static void run_field(Engine &E, int s0, int s1) {
     // tensor-core field passes (ewald_tc.cu): dipole field with the SOR update and convergence
     // test, and the charge field and potential
     if (MODE != F_QD && E.precision == PIMD_PREC_MIXED && launch_field_tc(E, MODE, s0, s1)) return;
+    if (MODE == F_D && E.field_needs_join) cudaStreamWaitEvent(E.stream, E.loop_join, 0);
     if (MODE == F_QD && E.precision == PIMD_PREC_MIXED && launch_field_qd_tc(E, s0, s1)) return;
     if (E.precision == PIMD_PREC_MIXED && E.ff_regs && LZ <= 49) {
         if (LZ <= 17)

@@ -58,7 +58,7 @@ constexpr int TC_NT = (TC_NB + 2) * 32;   // 576 threads
 constexpr int TC_SS = 32;                 // sites per table stage
 constexpr int TC_KS = 16;                 // sites per MMA step (kind::f16: 32 bytes of K)
 constexpr float TC_ZS = 64.f;             // power-of-two scale of Z (keeps small mu_c ez normal in FP16)
-constexpr int TC_NABUF_MAX = 3;           // operand buffers
+constexpr int TC_NABUF_MAX = 4;           // operand buffers (4: 708 -> 712 graph steps/s over 3)
 constexpr int TC_NST = 4;                 // table stage buffers (a CTA's 128 sites at 512 x 32)
 constexpr int TC_ZMAX = 4;                // Z items per builder thread (6 (|kz|max + 1) x 2 <= 256)
 constexpr int TC_CLMAX = 8;               // site groups per cluster (portable cluster size)
@@ -669,14 +669,16 @@ struct TfSmem {
 // with kcm core matrices along K
 PIMD_D int rowchunk_k(int n, int jc, int kcm) { return (((n >> 3) * kcm + jc) << 7) + ((n & 7) << 4); }
 
-template <int MODE>
+// VPP: V built before each pass (more than two passes); a template argument so that the
+// two-pass form keeps its registers (118 against 127 with a run-time choice)
+template <int MODE, bool VPP>
 __global__ void __launch_bounds__(TF_NT, 1) k_field_tc(const __grid_constant__ CUtensorMap tmap, KP kp, TfArgs a) {
     // TF_DG: 6 components per run (T0, T1 and T2 = sum kz^2 W ez, complex), V rebuilt for each
     // pass of nph runs; the other modes: 4 components, V of both passes built once (or, with
     // a.vpp, V of each pass before it, for more than two passes)
     constexpr bool DG = MODE == TF_DG;
     constexpr int NC = DG ? 6 : 4;
-    const bool vpp = DG || a.vpp;
+    constexpr bool vpp = DG || VPP;
     const int t = blockIdx.x, b = blockIdx.y;
     // the next iteration's structure factor may be scheduled now; it waits for this grid
     if (MODE == TF_D) pdl_launch_dependents();
@@ -1243,22 +1245,25 @@ void tc_init(Engine &E) {
     // whole |kz| range; per (run, j) the k-vectors of kz = +j and -j
     E.tf_ready = false;
     const int nr = kp.nrun, jm = jr[order[0]], kq = ((2 * jm + 15) / 16) * 16;
-    cudaFuncAttributes fb[4];
-    if (cudaFuncGetAttributes(&fb[0], k_field_tc<TF_Q>) != cudaSuccess || cudaFuncGetAttributes(&fb[1], k_field_tc<TF_D>) != cudaSuccess ||
-        cudaFuncGetAttributes(&fb[2], k_field_tc<TF_QG>) != cudaSuccess || cudaFuncGetAttributes(&fb[3], k_field_tc<TF_DG>) != cudaSuccess) {
-        cudaGetLastError();
-        return;
-    }
+    const void *fk[7] = {(const void *)k_field_tc<TF_Q, false>, (const void *)k_field_tc<TF_D, false>,
+                         (const void *)k_field_tc<TF_QG, false>, (const void *)k_field_tc<TF_Q, true>,
+                         (const void *)k_field_tc<TF_D, true>, (const void *)k_field_tc<TF_QG, true>,
+                         (const void *)k_field_tc<TF_DG, true>};
     size_t fstat = 0;
-    for (int i = 0; i < 4; i++) fstat = std::max(fstat, fb[i].sharedSizeBytes);
-    const int dmaxf = optin - (int)fstat;
-    if (cudaFuncSetAttribute(k_field_tc<TF_D>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess ||
-        cudaFuncSetAttribute(k_field_tc<TF_Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess ||
-        cudaFuncSetAttribute(k_field_tc<TF_QG>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess ||
-        cudaFuncSetAttribute(k_field_tc<TF_DG>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess) {
-        cudaGetLastError();
-        return;
+    for (const void *f : fk) {
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, f) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        fstat = std::max(fstat, fa.sharedSizeBytes);
     }
+    const int dmaxf = optin - (int)fstat;
+    for (const void *f : fk)
+        if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, dmaxf) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
     // passes: two passes of nph runs (a multiple of 8) x 4 components in TMEM with V of both built
     // once, when that fits (plus the 16 columns the last 16-run load of a run quarter reaches past
     // a pass); else passes of nph runs with V of each built before it. The bead's weights sit in
@@ -1322,6 +1327,10 @@ void tc_init(Engine &E) {
     E.tf_wglob_d = wgd;
 }
 
+// whether the iterations' field pass is launched as a programmatic dependent (griddepcontrol.wait
+// before it reads the iteration's fields)
+bool field_pdl_ok(const Engine &E) { return E.tc_ready && E.tf_ready && E.ff_tc && E.tc_pdl && E.sf_tc; }
+
 // mode TF_D: dipole field, SOR update and convergence test of one iteration at the dipole sites
 // [s0, s1) (k_field_f<F_D> + k_field_finish<F_D>); TF_Q: charge field and potential added to F at
 // [s0, s1) (k_field_f<F_Q> + k_field_finish<F_Q>); TF_QG, TF_DG: the halves of the force pass
@@ -1368,22 +1377,28 @@ int launch_field_tc(Engine &E, int mode, int s0, int s1) {
         at[0].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        if (cudaLaunchKernelEx(&cfg, k_field_tc<TF_D>, *map, kp, a) == cudaSuccess) {
+        const cudaError_t le = a.vpp ? cudaLaunchKernelEx(&cfg, k_field_tc<TF_D, true>, *map, kp, a)
+                                     : cudaLaunchKernelEx(&cfg, k_field_tc<TF_D, false>, *map, kp, a);
+        if (le == cudaSuccess) {
             ++E.nlaunch;
             return 1;
         }
         cudaGetLastError();
         a.pdl = 0;
         E.tc_pdl = false;  // not available: plain launches from now on
+        if (E.field_needs_join) cudaStreamWaitEvent(E.stream, E.loop_join, 0);
     }
     if (mode == TF_D)
-        k_field_tc<TF_D><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
+        a.vpp ? k_field_tc<TF_D, true><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a)
+              : k_field_tc<TF_D, false><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
     else if (mode == TF_Q)
-        k_field_tc<TF_Q><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
+        a.vpp ? k_field_tc<TF_Q, true><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a)
+              : k_field_tc<TF_Q, false><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
     else if (mode == TF_QG)
-        k_field_tc<TF_QG><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
+        a.vpp ? k_field_tc<TF_QG, true><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a)
+              : k_field_tc<TF_QG, false><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
     else
-        k_field_tc<TF_DG><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
+        k_field_tc<TF_DG, true><<<g, TF_NT, L.total, E.stream>>>(*map, kp, a);
     ++E.nlaunch;
     return 1;
 }

@@ -101,6 +101,7 @@ cudaError_t mixed_init(Engine &E) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.loop_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.loop_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.loop_pev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.loop_jpev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc((void **)&E.kp.gq23, sizeof(tab));
     if (e == cudaSuccess) E.allocs.push_back(E.kp.gq23);
     if (e == cudaSuccess) e = cudaMemcpy(E.kp.gq23, tab, sizeof(tab), cudaMemcpyHostToDevice);
@@ -738,7 +739,29 @@ void launch_dd_real_m(Engine &E) {
     else if (E.kp.dd_async)
         E.dd_otf ? k_dd_real_m<3, true, true><<<g, 128, 0, E.stream>>>(E.kp)
                  : k_dd_real_m<3, false, true><<<g, 128, 0, E.stream>>>(E.kp);
-    else
+    else if (E.dd_jpev_req && E.loop_jpev) {
+        // a programmatic event once every block has started (see Engine::loop_jpev)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = g;
+        cfg.blockDim = dim3(128);
+        cfg.stream = E.stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticEvent;
+        at[0].val.programmaticEvent.event = E.loop_jpev;
+        at[0].val.programmaticEvent.flags = 0;
+        at[0].val.programmaticEvent.triggerAtBlockStart = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaError_t e = E.dd_otf ? cudaLaunchKernelEx(&cfg, k_dd_real_m<3, true, false>, E.kp)
+                                 : cudaLaunchKernelEx(&cfg, k_dd_real_m<3, false, false>, E.kp);
+        if (e == cudaSuccess) {
+            E.dd_jpev_armed = true;
+        } else {
+            cudaGetLastError();
+            E.dd_otf ? k_dd_real_m<3, true, false><<<g, 128, 0, E.stream>>>(E.kp)
+                     : k_dd_real_m<3, false, false><<<g, 128, 0, E.stream>>>(E.kp);
+        }
+    } else
         E.dd_otf ? k_dd_real_m<3, true, false><<<g, 128, 0, E.stream>>>(E.kp)
                  : k_dd_real_m<3, false, false><<<g, 128, 0, E.stream>>>(E.kp);
     ++E.nlaunch;

@@ -6,7 +6,9 @@ equal the synchronous order's (1e-9 relative: FP64 atomics of the force sums and
 convergence sums add in another order). Cases: unit boundaries that split a block of four
 molecules (202 H2O), a unit base below the first M site (100 H2O), odd and even iteration
 counts (polar_eps 0, so every bead runs to polar_maxiter), beads converging at different
-iterations, the eager host loop and the CUDA-graph step, and agreement with the oracle."""
+iterations, the eager host loop and the CUDA-graph step, and agreement with the oracle. Also:
+the field pass started on a programmatic event of the real-space field (tuning knob dd_jpev)
+equals the full join."""
 import numpy as np
 import pytest
 
@@ -105,5 +107,41 @@ def test_async_graph_steps_equal_synchronous(pkg, engine_lib):
         eng.close()
     (Ra, Ga, oa, na), (Rs, Gs, os_, ns) = runs
     assert na == ns
+    assert rel(Ra, Rs) < 1e-12 and rel(Ga, Gs) < 1e-8
+    assert np.abs(oa - os_).max() <= 1e-8 * np.abs(os_).max()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_programmatic_join_equals_full_join(pkg, engine_lib, graph):
+    """The field pass launched on a programmatic event of the real-space field (dd_jpev: it may
+    start as that grid drains and waits for it in griddepcontrol.wait before reading its field)
+    gives the same steps as the full join."""
+    import torch
+
+    runs = []
+    for v in (1, 0):
+        c, p = case(pkg, 128, 4)
+        P, na = p["nbeads"], p["natoms"]
+        W = pkg.waterbox
+        eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_MIXED)
+        assert eng.set_tuning(dd_jpev=v)["dd_jpev"] == v
+        eng.nm_init(P, W.KB_AMU * T * P / W.HBAR, DELT)
+        eng.langevin_init(DELT / 2, 0, 0.1, P * T)
+        eng.set_graph(graph)
+        mp = eng.md_params(DELT, c["massO"], c["massH"], langevin=1, seed=3)
+        dev = torch.device("cuda", 0)
+        R = torch.from_numpy(c["RRt"].copy()).to(dev)
+        Pm = torch.from_numpy(c["PPt"].copy()).to(dev)
+        G = torch.zeros_like(R)
+        Rc = torch.zeros((na, 3), dtype=torch.float64, device=dev)
+        out = torch.zeros(4, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        for t in range(1, 6):
+            eng.md_step_device(mp, R.data_ptr(), Pm.data_ptr(), G.data_ptr(), Rc.data_ptr(), t, out.data_ptr())
+        torch.cuda.synchronize()
+        runs.append((R.cpu().numpy(), G.cpu().numpy(), out.cpu().numpy(), eng.energies(0)["niter"]))
+        eng.close()
+    (Ra, Ga, oa, na_), (Rs, Gs, os_, ns) = runs
+    assert na_ == ns
     assert rel(Ra, Rs) < 1e-12 and rel(Ga, Gs) < 1e-8
     assert np.abs(oa - os_).max() <= 1e-8 * np.abs(os_).max()
