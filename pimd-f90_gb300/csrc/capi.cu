@@ -353,6 +353,7 @@ static int create(Engine &E, const pimd_params *p, int nrep, const int *brep) {
             (rc = dalloc(E, &kp.Tf, P * (size_t)kp.fcap * kp.ndd)) || (rc = dalloc(E, &kp.fj, P * (size_t)kp.fcap)) || (rc = dalloc(E, &kp.Wf, P * 2 * (size_t)kp.nk)) || (rc = dalloc(E, &kp.dipf, P * S)) ||
             (rc = dalloc(E, &kp.ofix, P * N)) || (rc = dalloc(E, &kp.orawf, P * N)) || (rc = dalloc(E, &kp.Fx, P * S)) ||
             (rc = dalloc(E, &kp.dipf_alt, P * S)) || (rc = dalloc(E, &kp.Erec, P * S)) ||
+            (kp.model == 3 && (rc = dalloc(E, &kp.mrec, P * 2 * (size_t)N))) ||
             (rc = dalloc(E, &kp.unit_cnt, P * ((size_t)S / 128 + 2))))
             return rc;
         cudaMemset(kp.unit_cnt, 0, sizeof(unsigned) * P * ((size_t)S / 128 + 2));

@@ -72,7 +72,9 @@ PIMD_D void dd_sor_apply(const KP &kp, int b, int s, const DdSite &d, const doub
         kp.dip[3 * gs + c] = mn[c];
         kp.Efdr[3 * gs + c] = 0.0;
     }
-    if (kp.dipf) dipf_next(kp)[gs] = make_float4((float)mn[0], (float)mn[1], (float)mn[2], 0.f);
+    const float4 mf = make_float4((float)mn[0], (float)mn[1], (float)mn[2], 0.f);
+    if (kp.dipf) dipf_next(kp)[gs] = mf;
+    if (!kp.dd_async) mrec_dipole(kp, b, s, mf);  // (the asynchronous gather reads the buffers)
 }
 PIMD_D void dd_sor_site(const KP &kp, int b, int s, const double (&E)[3], int iter, double (&av)[2]) {
     DdSite d;

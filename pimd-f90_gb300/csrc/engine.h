@@ -110,6 +110,10 @@ struct KP {
     uint4 *ofix;           // [P][N] O sites as 32-bit fractions of the box edges: the wrapping
                            // unsigned difference of two of them is the minimum image
     float4 *orawf;         // [P][N] O sites (unwrapped) in FP32: force-phase centroid-virial lever
+    // TTM3-F mixed engine: per molecule [P][N][2] the M site as 32-bit fractions of the box
+    // edges (as float bits) and its FP32 dipole, the one record a real-space dipole-field entry
+    // reads of its partner (null: other models)
+    float4 *mrec;
     double4_32a *Fx;       // [P][S] reciprocal charge field / force-pass sums when those passes run
                            // beside the pair kernels (mixed engine): (x, y, z, potential)
     int fx_mode;           // bit 0: the charge field is in Fx (k_after_qq adds it to F); bit 1: the
@@ -182,6 +186,10 @@ PIMD_D bool bead_converged(const KP &kp, int b) {
 // unless the real-space field runs asynchronously (then iteration d + 1 reads buffer d & 1).
 PIMD_D const float4 *dipf_cur(const KP &kp) { return (kp.dd_async && (kp.dstep[1] & 1)) ? kp.dipf_alt : kp.dipf; }
 PIMD_D float4 *dipf_next(const KP &kp) { return (kp.dd_async && !(kp.dstep[1] & 1)) ? kp.dipf_alt : kp.dipf; }
+// the FP32 dipole of dipole site s of bead b into the molecule record (TTM3-F: s = fd + i)
+PIMD_D void mrec_dipole(const KP &kp, int b, int s, float4 m) {
+    if (kp.mrec && s >= kp.fd && s < kp.ld) kp.mrec[2 * ((size_t)b * kp.N + (s - kp.fd)) + 1] = m;
+}
 
 // replica of bead b and its centroid sites (posc[replica][S])
 PIMD_HD int rep_of(const KP &kp, int b) { return kp.brep ? kp.brep[b] : 0; }

@@ -165,6 +165,17 @@ __global__ void __launch_bounds__(128) k_site_offsets(KP kp) {
         d = make_float4((float)min_image_rn(__dsub_rn(R.x, O.x), kp.box[0], kp.boxi[0]),
                         (float)min_image_rn(__dsub_rn(R.y, O.y), kp.box[1], kp.boxi[1]),
                         (float)min_image_rn(__dsub_rn(R.z, O.z), kp.box[2], kp.boxi[2]), (float)R.w);
+        if (kp.mrec && s >= kp.fd && s < kp.ld) {  // the M site in the same fixed point as ofix
+            const double r[3] = {R.x, R.y, R.z};
+            unsigned u[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const double t = r[c] * kp.boxi[c];
+                u[c] = (unsigned)(unsigned long long)__double2ll_rn((t - floor(t)) * 0x1p32);
+            }
+            kp.mrec[2 * ((size_t)b * kp.N + (s - kp.fd))] =
+                make_float4(__uint_as_float(u[0]), __uint_as_float(u[1]), __uint_as_float(u[2]), 0.f);
+        }
     }
     kp.posf[gs] = d;
     kp.rhof[gs] = make_float4((float)(C.x - O.x), (float)(C.y - O.y), (float)(C.z - O.z), 0.f);
@@ -484,6 +495,64 @@ PIMD_D void dd_real_mol(const KP &kp, int i, int b, int lane) {
         for (int c = 0; c < 3; c++) Ef[3 * ((k - 1) * N + i) + c] = (double)ei[k][c];
 }
 
+// TTM3-F with the molecule records: the M-M separation is the wrapping difference of the M sites'
+// fixed-point coordinates (the nearest image, one rounding to FP32), and an entry reads its
+// partner's position and dipole in one 32-byte record besides its index and smear scalars (DBUF:
+// the dipole from the double-buffered FP32 dipoles instead, for the asynchronous iterations)
+template <bool OTF, bool DBUF>
+PIMD_D void dd_real_rec(const KP &kp, int i, int b, int lane) {
+    const int N = kp.N;
+    const float4 *rec = kp.mrec + (size_t)b * N * 2;
+    const float4 *dcur = dipf_cur(kp) + (size_t)b * kp.S + kp.fd;
+    const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
+    const int *fj = kp.fj + (size_t)b * kp.fcap;
+    const float2 *Tb = kp.Tf + (size_t)b * kp.fcap * kp.ndd;
+    const int ne = kp.fntot[b];  // offsets run past the stored length when the list overflowed
+    const int e0 = min(kp.foff[(size_t)b * N + i], ne);
+    const int e1 = (i + 1 < N) ? min(kp.foff[(size_t)b * N + i + 1], ne) : ne;
+    const float4 ri = rec[2 * i];
+    const unsigned mi[3] = {__float_as_uint(ri.x), __float_as_uint(ri.y), __float_as_uint(ri.z)};
+    float ei[3] = {0.f, 0.f, 0.f};
+    uint64_t pol = 0;
+    if (kp.l2keep) asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    for (int e = e0 + lane; e < e1; e += 32) {
+        int j;
+        if (OTF)
+            j = fl[e].y;
+        else if (kp.l2keep)
+            asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(j) : "l"(fj + e), "l"(pol));
+        else
+            j = fj[e];
+        const float4 rj = rec[2 * j], m = DBUF ? dcur[j] : rec[2 * j + 1];
+        const float R[3] = {(float)(int)(mi[0] - __float_as_uint(rj.x)) * kp.boxq[0],
+                            (float)(int)(mi[1] - __float_as_uint(rj.y)) * kp.boxq[1],
+                            (float)(int)(mi[2] - __float_as_uint(rj.z)) * kp.boxq[2]};
+        float t1, t3;
+        if (OTF) {
+            float t2;
+            smear2<float>(R[0] * R[0] + R[1] * R[1] + R[2] * R[2], kp.ptf.apol_dd[4][4], kp.ewf, &t1, &t2);
+            t3 = 3.f * t2;
+        } else {
+            float2 ts;
+            if (kp.l2keep)
+                asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(ts.x), "=f"(ts.y) : "l"(Tb + e), "l"(pol));
+            else
+                ts = Tb[e];
+            t1 = ts.x;
+            t3 = ts.y;
+        }
+        const float rm = t3 * (R[0] * m.x + R[1] * m.y + R[2] * m.z);
+        ei[0] += rm * R[0] - t1 * m.x;
+        ei[1] += rm * R[1] - t1 * m.y;
+        ei[2] += rm * R[2] - t1 * m.z;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ei[c] += __shfl_xor_sync(0xffffffffu, ei[c], o);
+    if (lane < 3) kp.Efdr[3 * ((size_t)b * kp.S + kp.fd + i) + lane] = (double)(lane == 0 ? ei[0] : lane == 1 ? ei[1] : ei[2]);
+}
+
 // ASYNC (TTM3-F): the block then arrives at the units of its molecules' M sites and runs the
 // SOR update of those it completes (dipole_check.cuh); converged beads and molecules past N
 // still arrive.
@@ -491,7 +560,12 @@ template <int MODEL, bool OTF, bool ASYNC>
 __global__ void __launch_bounds__(128) k_dd_real_m(KP kp) {
     const int lane = threadIdx.x & 31;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, b = blockIdx.y;
-    if (i < kp.N && !bead_converged(kp, b)) dd_real_mol<MODEL, OTF>(kp, i, b, lane);
+    if (i < kp.N && !bead_converged(kp, b)) {
+        if (MODEL == 3 && kp.mrec)
+            dd_real_rec<OTF, ASYNC>(kp, i, b, lane);
+        else
+            dd_real_mol<MODEL, OTF>(kp, i, b, lane);
+    }
     if constexpr (ASYNC) {
         const int m0 = blockIdx.x * 4, m1 = min(m0 + 4, kp.N) - 1;
         const int t0 = (kp.fd + m0 - kp.unit_sbase) >> 7, t1 = (kp.fd + m1 - kp.unit_sbase) >> 7;
@@ -507,7 +581,9 @@ __global__ void __launch_bounds__(128) k_dipf_sync(KP kp) {
     const int s = kp.fd + blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     if (s >= kp.ld) return;
     const size_t gs = (size_t)b * kp.S + s;
-    kp.dipf[gs] = make_float4((float)kp.dip[3 * gs], (float)kp.dip[3 * gs + 1], (float)kp.dip[3 * gs + 2], 0.f);
+    const float4 mf = make_float4((float)kp.dip[3 * gs], (float)kp.dip[3 * gs + 1], (float)kp.dip[3 * gs + 2], 0.f);
+    kp.dipf[gs] = mf;
+    mrec_dipole(kp, b, s, mf);
 }
 
 PIMD_D void dd_force_f(const float R[3], const float di[3], const float dj[3], float t2, float t3, float dij[3]) {

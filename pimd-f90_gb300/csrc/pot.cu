@@ -469,7 +469,9 @@ __global__ void __launch_bounds__(128) k_after_qq(KP kp) {
             kp.dip[3 * gs + 0] = mu[0];
             kp.dip[3 * gs + 1] = mu[1];
             kp.dip[3 * gs + 2] = mu[2];
-            if (kp.dipf) kp.dipf[gs] = make_float4((float)mu[0], (float)mu[1], (float)mu[2], 0.f);
+            const float4 mf = make_float4((float)mu[0], (float)mu[1], (float)mu[2], 0.f);
+            if (kp.dipf) kp.dipf[gs] = mf;
+            mrec_dipole(kp, b, s, mf);
         }
     }
     block_reduce_add<3, 128>(av, kp.acc + (size_t)b * NACC);  // slot 2 = ACC_UELEC2
