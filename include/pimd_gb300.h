@@ -326,7 +326,9 @@ int pimd_autotune(pimd_ctx *ctx, const double *RRt, const double *RRc);
  * [at the start of each graph-loop body the real-space dipole field waits until every CTA of
  * the structure factor is resident (a programmatic event), mixed engine], when n >= 19 [the
  * iterations' field pass may start as the real-space dipole field drains (a programmatic
- * event; it waits for that grid before reading its output), mixed engine]; n >= 5. */
+ * event; it waits for that grid before reading its output), mixed engine], when n >= 20 [the
+ * neighbour lists built from the input positions on the second stream beside the monomer
+ * kernel, mixed engine]; n >= 5. */
 int pimd_get_tuning(pimd_ctx *ctx, int *knobs, int n);
 /* Sets the shapes in the order pimd_get_tuning reports them (n >= 5; entry 15, the tensor-core
  * force pass, is a report only), e.g. to reuse an earlier autotune result without timing

@@ -574,13 +574,24 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
         PHASE("totals", launch_totals(E, Upott, virialt, virialct, virt9));
         return cuda_check(E, cudaGetLastError(), "force kernels");
     }
-    PHASE("sites", launch_sites(E));
     // mixed engine with the tensor-core field passes: the reciprocal charge passes run on the
     // second stream beside the neighbour list and the charge pair gather, and the force pass
     // beside the force pair gather; their field / gradient sums go to the scratch Fx, which
-    // k_after_qq and k_finish add (the pair kernels update F and dR in place)
+    // k_after_qq and k_finish add (the pair kernels update F and dR in place). The neighbour
+    // lists, which need only the input O sites, are built on the second stream beside k_sites.
     const bool ovl = mixed && E.ewald_overlap && E.aux_stream && kp.Fx && E.tc_ready && E.tf_ready && E.ff_tc;
     const bool ovq = ovl, ovf = ovl && E.tf_qd_ready;
+    const bool nbe = ovq && E.nbr_overlap && E.ev_nbr && nbr_from_inputs(E);
+    if (nbe) {
+        cudaEventRecord(E.ev_fork, E.stream);
+        cudaStreamWaitEvent(E.aux_stream, E.ev_fork, 0);
+        cudaStream_t keep = E.stream;
+        E.stream = E.aux_stream;
+        PHASE("neighbors", launch_neighbors(E));
+        E.stream = keep;
+        cudaEventRecord(E.ev_nbr, E.aux_stream);
+    }
+    PHASE("sites", launch_sites(E));
     kp.fx_mode = 0;
     if (mixed) {
         PHASE("site_offsets", launch_site_offsets(E));
@@ -594,11 +605,18 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
             PHASE("ewald_sq", launch_ewald_sq(E));
             PHASE("ewald_fq", launch_ewald_fq(E));
             kp.fx_mode = 0;
+            // the iterations' dipole-pair scalars fill this stream's slack beside the charge
+            // gather (after the full lists this stream built)
+            if (nbe) PHASE("dd_tensors", launch_dd_tensors_m(E));
             E.stream = keep;
             cudaEventRecord(E.ev_join, E.aux_stream);
         }
-        PHASE("neighbors", launch_neighbors(E));
+        if (nbe)
+            cudaStreamWaitEvent(E.stream, E.ev_nbr, 0);
+        else
+            PHASE("neighbors", launch_neighbors(E));
         PHASE("pair_qq", launch_pair_qq_m(E));
+        if (!nbe) PHASE("dd_tensors", launch_dd_tensors_m(E));
     } else {
         PHASE("neighbors", launch_neighbors(E));
         PHASE("pair_qq", launch_pair_qq(E));
@@ -722,6 +740,7 @@ int pimd_destroy(pimd_ctx *ctx) {
     if (E.aux_stream) cudaStreamDestroy(E.aux_stream);
     if (E.ev_fork) cudaEventDestroy(E.ev_fork);
     if (E.ev_join) cudaEventDestroy(E.ev_join);
+    if (E.ev_nbr) cudaEventDestroy(E.ev_nbr);
     if (E.loop_aux) cudaStreamDestroy(E.loop_aux);
     if (E.loop_fork) cudaEventDestroy(E.loop_fork);
     if (E.loop_pev) cudaEventDestroy(E.loop_pev);
@@ -1094,6 +1113,7 @@ int pimd_get_tuning(pimd_ctx *ctx, int *k, int n) {
     if (n >= 17) k[16] = dd_async_ok(E);
     if (n >= 18) k[17] = E.dd_pev && E.loop_pev != nullptr;
     if (n >= 19) k[18] = E.dd_jpev && E.loop_jpev != nullptr && field_pdl_ok(E);
+    if (n >= 20) k[19] = E.nbr_overlap && E.ev_nbr != nullptr && E.precision == PIMD_MIXED && nbr_from_inputs(E);
     return PIMD_OK;
 }
 
@@ -1122,6 +1142,7 @@ int pimd_set_tuning(pimd_ctx *ctx, const int *k, int n) {
     if (n >= 17) E.dd_async = k[16] != 0;
     if (n >= 18) E.dd_pev = k[17] != 0;
     if (n >= 19) E.dd_jpev = k[18] != 0;
+    if (n >= 20) E.nbr_overlap = k[19] != 0;
     E.gkey.clear();  // a captured MD-step graph holds the old launches: capture again
     return PIMD_OK;
 }

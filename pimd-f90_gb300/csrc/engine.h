@@ -278,6 +278,8 @@ struct Engine {
     // beside the structure factor (fork / join events; branches of the graph when captured)
     cudaStream_t aux_stream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_nbr = nullptr;  // the neighbour lists built on the second stream beside k_sites
+    bool nbr_overlap = true;       // (knob)
     // the dipole iterations' own pair (inside a graph they are captured into the conditional
     // loop's body, a graph of its own, which must not share a stream with the outer capture)
     cudaStream_t loop_aux = nullptr;
@@ -393,6 +395,7 @@ void adj_rec(Engine &E, int mode, const double *a, const double *bvec, const dou
 // launchers (neighbors.cu)
 void neighbors_init(Engine &E);
 void launch_neighbors(Engine &E);
+bool nbr_from_inputs(const Engine &E);
 // launchers (pot.cu)
 void pot_init_constants(Engine &E);
 void launch_sites(Engine &E);
@@ -408,6 +411,7 @@ void launch_totals(Engine &E, double *Upott, double *virialt, double *virialct, 
 cudaError_t mixed_init(Engine &E);  // FP32 lookup tables of the mixed engine
 void launch_site_offsets(Engine &E);
 void launch_pair_qq_m(Engine &E);
+void launch_dd_tensors_m(Engine &E);
 void launch_dd_real_m(Engine &E);
 bool dd_async_ok(const Engine &E);
 void launch_dipf_sync(Engine &E);

@@ -97,6 +97,7 @@ cudaError_t mixed_init(Engine &E) {
     cudaError_t e = cudaStreamCreateWithFlags(&E.aux_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.ev_nbr, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E.loop_aux, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.loop_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E.loop_join, cudaEventDisableTiming);
@@ -800,10 +801,14 @@ void launch_site_offsets(Engine &E) {
 void launch_pair_qq_m(Engine &E) {
     dim3 g((E.kp.N * QL + 127) / 128, E.kp.P);
     DISPATCH_M(E, k_pair_qq_m, g, 128);
-    if (!E.dd_otf) {
-        dim3 g2(pair_blocks_m(E, 128), E.kp.P);
-        DISPATCH_M(E, k_dd_tensors_m, g2, 128);
-    }
+}
+
+// the per-entry dipole-pair smear scalars of the iterations (none when they are formed in each
+// iteration); after the full lists and the site offsets
+void launch_dd_tensors_m(Engine &E) {
+    if (E.dd_otf) return;
+    dim3 g2(pair_blocks_m(E, 128), E.kp.P);
+    DISPATCH_M(E, k_dd_tensors_m, g2, 128);
 }
 
 void launch_dd_real_m(Engine &E) {

@@ -150,9 +150,11 @@ __global__ void __launch_bounds__(NB_MAXN) k_nbr_block(KP kp) {
     unsigned *mk = reinterpret_cast<unsigned *>(of + N);
     __shared__ int wsum[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const double4_32a *O = kp.pos + (size_t)b * kp.S;
+    // the O sites straight from the input positions (atom 3 i; the same values k_sites copies into
+    // pos), so that the lists can be built beside k_sites
+    const double *Rb = kp.RRt + (size_t)b * kp.natoms * 3;
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        const double4_32a o = O[i];
+        const double4_32a o = make_double4_32a(Rb[9 * i], Rb[9 * i + 1], Rb[9 * i + 2], 0.0);
         sO[i] = o;
         // the FP32 copy is wrapped into the primary box first (in FP64), so its rounding error
         // stays ~1e-7 of the box whatever the magnitude of the input coordinates
@@ -408,6 +410,12 @@ static void build_list(Engine &E, int *cnt, int *tot, int cap) {
 }
 
 // half list for every engine; the mixed engine adds the full list (row offsets in foff)
+// whether launch_neighbors builds the lists from the input positions alone (the one-launch
+// block path; the cell-list path reads the site array k_sites writes)
+bool nbr_from_inputs(const Engine &E) {
+    return !(E.kp.N > NB_MAXN && E.kp.cl_ncell > 0 && E.nbr_cells) && E.kp.N <= NB_MAXN && E.nbr_block;
+}
+
 void launch_neighbors(Engine &E) {
     KP &kp = E.kp;
     if (kp.N > NB_MAXN && kp.cl_ncell > 0 && E.nbr_cells) {

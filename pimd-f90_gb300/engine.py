@@ -561,7 +561,7 @@ class ForceEngine:
     # pimd_get_tuning / pimd_set_tuning order; qd_tc is a report only (tensor-core force pass in use)
     TUNING_ORDER = ("sf_tiled", "sf_groups", "ff_regs", "max_slices", "nbr_block", "wave_shapes", "sf_tc", "ff_tc",
                     "dd_overlap", "x_cache", "pdl", "loop_unroll", "ewald_overlap", "dd_otf", "qd_tc", "l2_keep",
-                    "dd_async", "dd_pev", "dd_jpev")
+                    "dd_async", "dd_pev", "dd_jpev", "nbr_overlap")
     TUNING_REPORTS = ("qd_tc",)
     TUNING_KEYS = TUNING_ORDER[:14] + TUNING_ORDER[15:]
 

@@ -130,7 +130,7 @@ def test_autotune_keeps_results(pkg, engine_lib):
     tuned = eng.autotune()
     assert set(tuned) == {"sf_tiled", "sf_groups", "ff_regs", "max_slices", "nbr_block", "wave_shapes", "sf_tc", "ff_tc",
                           "dd_overlap", "x_cache", "pdl", "loop_unroll", "ewald_overlap", "dd_otf", "qd_tc", "l2_keep",
-                          "dd_async", "dd_pev", "dd_jpev"}
+                          "dd_async", "dd_pev", "dd_jpev", "nbr_overlap"}
     assert 1 <= tuned["max_slices"] <= 16
     b = eng.full_bead_forces(c["RRt"], c["RRc"], t=0)
     assert rel(b["dRRt"], a["dRRt"]) < 1e-6
