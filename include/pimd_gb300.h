@@ -287,15 +287,18 @@ enum {
 int pimd_get_theta(pimd_ctx *ctx, double *theta);
 int pimd_set_theta(pimd_ctx *ctx, const double *theta);
 /* Forward: the force call of pimd_full_bead_forces (host arrays) that also records every
- * induced-dipole iteration for the backward. Needs the dipole predictor off at this step
- * (guess_initdip = 0 or t <= 4). No counterpart in the reference. */
+ * induced-dipole iteration for the backward. TTM3-F contexts of either precision. Needs the
+ * dipole predictor off at this step (guess_initdip = 0 or t <= 4). No counterpart in the
+ * reference. */
 int pimd_pot_forward(pimd_ctx *ctx, const double *RRt, const double *RRc, double *Upott, int t);
 /* Backward: for E = sum_k Ebar[k] Upot_k of the last forward, the exact derivative of the
  * computed energies -- the induced dipoles as the forward computed them, after its own number of
  * Jacobi-SOR iterations per bead, differentiated through those iterations by the transposed
  * (adjoint) iteration, which reuses the symmetric dipole-field operator -- with respect to the
  * positions, dRRt(3,Natoms,P), and to theta, dtheta[PIMD_NTHETA]. Pair geometry is recomputed,
- * not stored. No counterpart in the reference. */
+ * not stored. A mixed context runs the backward with the forward's FP32 operators (FP32 pair,
+ * table and reciprocal products, FP64 sums): the gradients agree with an FP64 context's within
+ * the mixed force budget (~1e-6 relative on water boxes). No counterpart in the reference. */
 int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *dtheta);
 
 /* ---------------------------------------------------------------------------------------

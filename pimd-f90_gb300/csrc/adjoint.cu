@@ -1,4 +1,4 @@
-// adjoint.cu -- differentiation form of the TTM3-F force call (FP64 engine).
+// adjoint.cu -- differentiation form of the TTM3-F force call (FP64 and mixed engines).
 //
 // The energy of bead b as the forward computes it (pot_ttm.f90:3-630) is
 //   E = Umon(theta) + Uvdw(theta) + Uelec + Uind + Uvdw_lrc,   Uind = -1/2 mu_K . E_q
@@ -16,8 +16,14 @@
 // through the DMS charges (grdq) and the M-site construction. Pair geometry is recomputed from
 // the site positions, never stored. The forward records mu_0..mu_K (the tape) and the
 // charge-only potential; nothing else is kept beyond the forward's own buffers.
+// On the mixed engine the reverse sweep's operators are the forward's FP32 ones: D_real from
+// its per-entry smear scalars with alpha g_k in the molecule records, the reciprocal passes from
+// its FP32 tables, and the bilinear real-space term as a full-list FP32 gather (no atomics); the
+// sums stay FP64 as in the forward. The terms outside the sweep (charge-field pairs, monomer
+// chain) run once, in FP64, on the forward's FP64 sites.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <vector>
 
@@ -110,10 +116,12 @@ __global__ void __launch_bounds__(128) k_adj_init(KP kp, const double *ebar, dou
 }
 
 // iteration k of the reverse sweep, first half: u = alpha g_k, v = mu_{k-1}, nu += w u, and
-// d/dalpha of mu_k = (1-w) mu_{k-1} + w alpha F_k, with w alpha F_k = mu_k - (1-w) mu_{k-1}
+// d/dalpha of mu_k = (1-w) mu_{k-1} + w alpha F_k, with w alpha F_k = mu_k - (1-w) mu_{k-1}.
+// Mixed engine (uf, vf given, float4 [P][S]; TTM3-F, dipole site fd + i of molecule i): FP32
+// copies of u and v, and u in the molecule records, where the real-space field reads its dipoles.
 __global__ void __launch_bounds__(128) k_adj_u(KP kp, int k, const int *iters, const double *tape, const double *g,
                                                double *u, double *v, double *nu, double *bacc, double *bw,
-                                               double *thacc, double omega) {
+                                               double *thacc, double omega, float4 *uf, float4 *vf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y, nd = kp.ld - kp.fd;
     const bool active = k <= iters[b];
     const double alpha = kp.polar[4];
@@ -124,19 +132,25 @@ __global__ void __launch_bounds__(128) k_adj_u(KP kp, int k, const int *iters, c
     double th[1] = {0.0};
     if (i < nd) {
         const size_t gs = (size_t)b * kp.S + kp.fd + i;
+        double uu[3] = {0.0, 0.0, 0.0}, vv[3] = {0.0, 0.0, 0.0};
         for (int c = 0; c < 3; c++) {
             const double gi = g[((size_t)b * nd + i) * 3 + c];
             if (active) {
                 const double mk = tape[(((size_t)k * kp.P + b) * nd + i) * 3 + c];
                 const double mp = tape[(((size_t)(k - 1) * kp.P + b) * nd + i) * 3 + c];
-                u[3 * gs + c] = alpha * gi;
-                v[3 * gs + c] = mp;
+                uu[c] = alpha * gi;
+                vv[c] = mp;
                 nu[3 * gs + c] += omega * alpha * gi;
                 th[0] += gi * (mk - (1.0 - omega) * mp) / alpha;
-            } else {
-                u[3 * gs + c] = 0.0;
-                v[3 * gs + c] = 0.0;
             }
+            u[3 * gs + c] = uu[c];
+            v[3 * gs + c] = vv[c];
+        }
+        if (uf) {
+            const float4 u4 = make_float4((float)uu[0], (float)uu[1], (float)uu[2], 0.f);
+            uf[gs] = u4;
+            vf[gs] = make_float4((float)vv[0], (float)vv[1], (float)vv[2], 0.f);
+            mrec_dipole(kp, b, kp.fd + i, u4);
         }
     }
     block_reduce_add<1, 128>(th, thacc + PIMD_TH_POLAR_M);
@@ -235,6 +249,70 @@ __global__ void __launch_bounds__(128) k_adj_ddbil(KP kp, Polfac pf, const doubl
         }
     }
     block_reduce_add<1, 128>(th, thacc + PIMD_TH_A_DD);
+}
+
+// The same bilinear term on the mixed engine (TTM3-F), as a gather over the full list like its
+// real-space field: one warp per molecule i, lanes over its entries (i, j); the M-M separation
+// from the molecule records (fixed-point M sites, the forward's own R), smear3 and the rank-3
+// contraction in FP32, and only i's side accumulated (j's side when j gathers i), so each site
+// has one writer; the d/da_dd sum, which sees every pair twice, at weight 1/2.
+__global__ void __launch_bounds__(128) k_adj_ddbil_m(KP kp, double pfm2, const float4 *uf, const float4 *vf,
+                                                     const double *bw, double *grad, double *thacc) {
+    const int lane = threadIdx.x & 31;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, b = blockIdx.y, N = kp.N;
+    const double w = bw[b];
+    float gi[3] = {0.f, 0.f, 0.f}, th = 0.f;
+    if (i < N && w != 0.0) {
+        const float4 *rec = kp.mrec + (size_t)b * N * 2;
+        const float4 *ub = uf + (size_t)b * kp.S + kp.fd, *vb = vf + (size_t)b * kp.S + kp.fd;
+        const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
+        const int ne = kp.fntot[b];
+        const int e0 = min(kp.foff[(size_t)b * N + i], ne);
+        const int e1 = (i + 1 < N) ? min(kp.foff[(size_t)b * N + i + 1], ne) : ne;
+        const float4 ri = rec[2 * i], u4 = ub[i], v4 = vb[i];
+        const unsigned mi[3] = {__float_as_uint(ri.x), __float_as_uint(ri.y), __float_as_uint(ri.z)};
+        const float ui[3] = {u4.x, u4.y, u4.z}, vi[3] = {v4.x, v4.y, v4.z};
+        const float a12 = kp.ptf.apol_dd[4][4];
+        for (int e = e0 + lane; e < e1; e += 32) {
+            const int j = fl[e].y;
+            const float4 rj = rec[2 * j], uj4 = ub[j], vj4 = vb[j];
+            const float R[3] = {(float)(int)(mi[0] - __float_as_uint(rj.x)) * kp.boxq[0],
+                                (float)(int)(mi[1] - __float_as_uint(rj.y)) * kp.boxq[1],
+                                (float)(int)(mi[2] - __float_as_uint(rj.z)) * kp.boxq[2]};
+            const float uj[3] = {uj4.x, uj4.y, uj4.z}, vj[3] = {vj4.x, vj4.y, vj4.z};
+            const float d2 = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
+            float t1, t2, t3;
+            smear3<float>(d2, a12, kp.ewf, &t1, &t2, &t3);
+            float dij[3] = {0.f, 0.f, 0.f};
+            dd_force_f(R, ui, vj, t2, t3, dij);
+            dd_force_f(R, vi, uj, t2, t3, dij);
+            gi[0] -= dij[0];
+            gi[1] -= dij[1];
+            gi[2] -= dij[2];
+            if (d2 < 25.f) {
+                const float r = sqrtf(d2), e1x = __expf(-a12 * d2 * r);
+                const float rui = R[0] * ui[0] + R[1] * ui[1] + R[2] * ui[2];
+                const float ruj = R[0] * uj[0] + R[1] * uj[1] + R[2] * uj[2];
+                const float rvi = R[0] * vi[0] + R[1] * vi[1] + R[2] * vi[2];
+                const float rvj = R[0] * vj[0] + R[1] * vj[1] + R[2] * vj[2];
+                const float uv = ui[0] * vj[0] + ui[1] * vj[1] + ui[2] * vj[2];
+                const float vu = vi[0] * uj[0] + vi[1] * uj[1] + vi[2] * uj[2];
+                th += 3.f * a12 * r * e1x * (rui * rvj + rvi * ruj) - e1x * (uv + vu);
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        gi[0] += __shfl_xor_sync(0xffffffffu, gi[0], o);
+        gi[1] += __shfl_xor_sync(0xffffffffu, gi[1], o);
+        gi[2] += __shfl_xor_sync(0xffffffffu, gi[2], o);
+    }
+    if (i < N && lane < 3) {
+        const size_t si = 3 * ((size_t)b * kp.S + kp.fd + i) + lane;
+        grad[si] += w * (double)(lane == 0 ? gi[0] : lane == 1 ? gi[1] : gi[2]);
+    }
+    double tv[1] = {0.5 * w * (double)th * pfm2};
+    block_reduce_add<1, 128>(tv, thacc + PIMD_TH_A_DD);
 }
 
 // Q(2/3, x) by the Numerical-Recipes series / continued fraction used by the forward
@@ -522,8 +600,7 @@ int pimd_set_theta(pimd_ctx *ctx, const double *theta) {
 int pimd_pot_forward(pimd_ctx *ctx, const double *RRt, const double *RRc, double *Upott, int t) {
     if (!ctx || !RRt || !RRc) return PIMD_ERR_ARG;
     Engine &E = ctx->E;
-    if (E.kp.model != 3 || E.precision != PIMD_FP64)
-        return adj_fail(E, PIMD_ERR_ARG, "the differentiation form needs a TTM3-F FP64 context");
+    if (E.kp.model != 3) return adj_fail(E, PIMD_ERR_ARG, "the differentiation form needs a TTM3-F context");
     if (E.kp.guess && t > 4) return adj_fail(E, PIMD_ERR_ARG, "the dipole predictor must be off (guess_initdip = 0 or t <= 4)");
     cudaSetDevice(E.device);
     const KP &kp = E.kp;
@@ -539,9 +616,12 @@ int pimd_pot_forward(pimd_ctx *ctx, const double *RRt, const double *RRc, double
     }
     E.tape_on = true;
     const int save_check = ctx->check_every;
+    const bool save_async = E.dd_async;
     ctx->check_every = 1;
+    E.dd_async = false;  // one recorded SOR step per iteration
     int rc = pimd_full_bead_forces(ctx, RRt, RRc, Upott, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, t);
     ctx->check_every = save_check;
+    E.dd_async = save_async;
     E.tape_on = false;
     E.tape_valid = rc == PIMD_OK;
     return rc;
@@ -554,10 +634,11 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
     cudaSetDevice(E.device);
     KP &kp = E.kp;
     const size_t P = kp.P, S = kp.S, nd = kp.ld - kp.fd, sv = 3 * P * S;
+    const bool mixed = E.precision == PIMD_MIXED;
     // scratch: g, u, v, Dr, grad, nu (site vectors), phin, Smu, Smv, Snu, bacc, bw, ebar, ones,
-    // thacc, iters, dRRt
+    // thacc, dRRt, FP32 u and v per molecule (mixed engine), iters
     const size_t nbytes = sizeof(double) * (3 * P * nd + 5 * sv + P * S + 6 * P * kp.nk + P * NACC + 3 * P + PIMD_NTHETA +
-                                            P * kp.natoms * 3) + sizeof(int) * P + 256;
+                                            P * kp.natoms * 3) + sizeof(float4) * 2 * P * S + sizeof(int) * P + 256;
     if (E.adj_bytes < nbytes) {
         if (E.d_adj) cudaFree(E.d_adj);
         if (cudaMalloc((void **)&E.d_adj, nbytes) != cudaSuccess) {
@@ -569,10 +650,13 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
     }
     double *g = E.d_adj, *u = g + 3 * P * nd, *v = u + sv, *Dr = v + sv, *grad = Dr + sv, *nu = grad + sv;
     double *phin = nu + sv;
-    double2 *Smu = reinterpret_cast<double2 *>(phin + P * S), *Smv = Smu + P * kp.nk, *Snu = Smv + P * kp.nk;
+    const uintptr_t sa = (reinterpret_cast<uintptr_t>(phin + P * S) + 15) & ~uintptr_t(15);  // 16-byte rows
+    double2 *Smu = reinterpret_cast<double2 *>(sa), *Smv = Smu + P * kp.nk, *Snu = Smv + P * kp.nk;
     double *bacc = reinterpret_cast<double *>(Snu + P * kp.nk), *bw = bacc + P * NACC, *ebar = bw + P, *ones = ebar + P;
     double *thacc = ones + P, *dR = thacc + PIMD_NTHETA;
-    int *iters = reinterpret_cast<int *>(dR + P * kp.natoms * 3);
+    const uintptr_t ua = (reinterpret_cast<uintptr_t>(dR + P * kp.natoms * 3) + 15) & ~uintptr_t(15);  // 16-byte rows
+    float4 *uf = reinterpret_cast<float4 *>(ua), *vf = uf + P * S;
+    int *iters = reinterpret_cast<int *>(vf + P * S);
     cudaStream_t st = E.stream;
     // per-bead iteration counts of the forward
     std::vector<double> acc(P * NACC);
@@ -601,33 +685,48 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
     Polfac pf;
     for (int i = 0; i < 5; i++) pf.v[i] = E.polfac[i];
     const double omega = kp.polar_sor;
+    const dim3 gw((unsigned)((kp.N * 32 + 127) / 128), (unsigned)P);  // a warp per molecule
     k_adj_init<<<gd, 128, 0, st>>>(kp, ebar, g, nu);
     for (int k = kmax; k >= 1; k--) {
-        k_adj_u<<<gd, 128, 0, st>>>(kp, k, iters, E.d_tape, g, u, v, nu, bacc, bw, thacc, omega);
+        k_adj_u<<<gd, 128, 0, st>>>(kp, k, iters, E.d_tape, g, u, v, nu, bacc, bw, thacc, omega, mixed ? uf : nullptr,
+                                    mixed ? vf : nullptr);
         cudaMemsetAsync(Dr, 0, sizeof(double) * sv, st);
-        {  // D_real u from the forward's cached Thole tensors
+        {  // D_real u: the forward's cached Thole tensors (FP64), or its per-entry smear scalars
+           // with u in the molecule records (mixed)
             KP kq = kp;
             kq.dip = u;
             kq.Efdr = Dr;
             kq.acc = bacc;
+            kq.dd_async = 0;
             const KP keep = E.kp;
             E.kp = kq;
-            launch_dd_real(E);
+            if (mixed)
+                launch_dd_real_m(E);
+            else
+                launch_dd_real(E);
             E.kp = keep;
         }
-        adj_structure_factor(E, u, Smu, bacc);
-        adj_structure_factor(E, v, Smv, bacc);
+        // v first: the mixed field pass reads the weights of the last structure factor
+        adj_structure_factor(E, v, mixed ? vf : nullptr, Smv, bacc);
+        adj_structure_factor(E, u, mixed ? uf : nullptr, Smu, bacc);
         adj_dipole_field(E, Smu, bacc, Dr);
         k_adj_g<<<gd, 128, 0, st>>>(kp, k, iters, g, u, Dr, omega);
-        k_adj_ddbil<<<gp, 128, 0, st>>>(kp, pf, u, v, bw, grad, thacc);
+        if (mixed)
+            k_adj_ddbil_m<<<gw, 128, 0, st>>>(kp, pf.v[4] * pf.v[4], uf, vf, bw, grad, thacc);
+        else
+            k_adj_ddbil<<<gp, 128, 0, st>>>(kp, pf, u, v, bw, grad, thacc);
         adj_rec(E, 0, u, v, Smu, Smv, bw, grad, nullptr);
     }
     k_adj_final<<<gd, 128, 0, st>>>(kp, g, nu, thacc);
     // charge-field adjoint nu: real-space pairs, reciprocal, intramolecular; vdW; Uelec d/da_cc
     cudaMemsetAsync(bacc, 0, sizeof(double) * P * NACC, st);
-    adj_structure_factor(E, nu, Snu, bacc);
+    adj_charge_sfac(E, bacc);
+    adj_structure_factor(E, nu, nullptr, Snu, bacc);
     adj_rec(E, 1, nu, nullptr, Snu, nullptr, ones, grad, phin);
-    k_adj_pairs<<<gp, 128, 0, st>>>(kp, pf, ebar, nu, grad, phin, thacc);
+    if (mixed)
+        launch_adj_pairs_m(E, pf.v, ebar, nu, grad, phin, thacc);
+    else
+        k_adj_pairs<<<gp, 128, 0, st>>>(kp, pf, ebar, nu, grad, phin, thacc);
     k_adj_mol<0><<<gm, 128, 0, st>>>(kp, ebar, E.d_phiq, nu, grad, phin, dR, thacc);
     k_adj_mol<1><<<gm, 128, 0, st>>>(kp, ebar, E.d_phiq, nu, grad, phin, dR, thacc);
     E.nlaunch += 5 + 8 * (long long)kmax;

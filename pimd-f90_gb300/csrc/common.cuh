@@ -250,6 +250,15 @@ PIMD_D void dd_force(const double R[3], const double di[3], const double dj[3], 
 #pragma unroll
     for (int c = 0; c < 3; c++) dij[c] += a * R[c] - 3.0 * t2 * (rdi * dj[c] + rdj * di[c]);
 }
+// the same in FP32 (the mixed engine)
+PIMD_D void dd_force_f(const float R[3], const float di[3], const float dj[3], float t2, float t3, float dij[3]) {
+    const float rdi = R[0] * di[0] + R[1] * di[1] + R[2] * di[2];
+    const float rdj = R[0] * dj[0] + R[1] * dj[1] + R[2] * dj[2];
+    const float didj = di[0] * dj[0] + di[1] * dj[1] + di[2] * dj[2];
+    const float a = 15.f * t3 * rdi * rdj - 3.f * t2 * didj;
+#pragma unroll
+    for (int c = 0; c < 3; c++) dij[c] += a * R[c] - 3.f * t2 * (rdi * dj[c] + rdj * di[c]);
+}
 
 // ---------------------------------------------------------------------------------------
 // block-wide sum of NV doubles into per-bead accumulators (one atomic per value per block)

@@ -387,7 +387,10 @@ int run_forces(Engine &E, int t, int check_every, double *Upott, double *virialt
 void tape_record(Engine &E, int iter);
 int apply_theta(Engine &E);
 void adjoint_init(Engine &E);
-void adj_structure_factor(Engine &E, const double *dipbuf, double2 *Sout, double *bacc);
+void adj_structure_factor(Engine &E, const double *dipbuf, const float4 *dipf32, double2 *Sout, double *bacc);
+void adj_charge_sfac(Engine &E, double *bacc);
+void launch_adj_pairs_m(Engine &E, const double pf[5], const double *ebar, const double *nu, double *grad, double *phin,
+                        double *thacc);
 void adj_dipole_field(Engine &E, double2 *Sm_u, double *bacc, double *Dr);
 void adj_rec(Engine &E, int mode, const double *a, const double *bvec, const double2 *SA, const double2 *SB,
              const double *ebw, double *grad, double *phi);

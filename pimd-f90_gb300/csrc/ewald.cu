@@ -1154,17 +1154,40 @@ void launch_ewald_tables(Engine &E) {
 }
 
 // ---------------------------------------------------------------------------------------
-// Backward (adjoint) helpers of the differentiation form, FP64 engine only.
+// Backward (adjoint) helpers of the differentiation form. They follow the context's precision:
+// FP64 tables and arithmetic on the FP64 engine; on the mixed engine the FP32 tables of the
+// forward with FP32 products and FP64 sums (per tile, chunk or run), like its FP32-pipe passes.
 
 // Structure factor of the dipole set dipbuf ([P][S][3], dipole sites filled) into Sout in the
 // forward's rotated form (-Im, Re) of sum_s (k.mu_s) e^{ik.r_s}; beads with bacc[ACC_CONV] != 0
-// are skipped.
-void adj_structure_factor(Engine &E, const double *dipbuf, double2 *Sout, double *bacc) {
+// are skipped. Mixed engine: also the FP32 field weights of Sout (Wf), which the field pass
+// of adj_dipole_field reads, so the last structure factor before it must be its own.
+// dipf32: the same dipoles as FP32 float4 [P][S] (mixed engine), read by the register-tiled pass.
+void adj_structure_factor(Engine &E, const double *dipbuf, const float4 *dipf32, double2 *Sout, double *bacc) {
     const KP keep = E.kp;
     E.kp.dip = const_cast<double *>(dipbuf);
     E.kp.Sm = Sout;
     E.kp.acc = bacc;
-    run_spass_t<OP_MU, double>(E, E.kp.fd, E.kp.ld - E.kp.fd, 1);
+    E.kp.dd_async = 0;
+    if (E.precision == PIMD_PREC_MIXED && dipf32 && E.sf_tiled && E.sf_nkg_max * SF_RT <= SF_MAXT) {
+        E.kp.dipf = const_cast<float4 *>(dipf32);
+        run_sfac_f<OP_MU>(E, E.kp.fd, E.kp.ld - E.kp.fd, 1);
+    } else if (E.precision == PIMD_PREC_MIXED) {
+        run_spass_t<OP_MU, float>(E, E.kp.fd, E.kp.ld - E.kp.fd, 1);
+    } else {
+        run_spass_t<OP_MU, double>(E, E.kp.fd, E.kp.ld - E.kp.fd, 1);
+    }
+    E.kp = keep;
+}
+
+// The charge structure factor (raw, sum_s q_s e^{ik.r_s}) into kp.Sq again, in the layout the
+// backward's cross term reads (the mixed forward's tensor-core passes keep their own); the
+// pass's sums go to bacc.
+void adj_charge_sfac(Engine &E, double *bacc) {
+    if (E.precision != PIMD_PREC_MIXED) return;  // the FP64 forward's Sq is already this one
+    const KP keep = E.kp;
+    E.kp.acc = bacc;
+    run_spass_t<OP_Q, float>(E, E.kp.fq, E.kp.S - E.kp.fq, 0);
     E.kp = keep;
 }
 
@@ -1186,26 +1209,68 @@ __global__ void __launch_bounds__(128) k_adj_fsum(KP kp, int s0, int s1, int nsl
     o[2] += E[2];
 }
 
+template <int NT, typename R>
+static void adj_field_t(Engine &E, double *Dr) {
+    const int s0 = E.kp.fd, s1 = E.kp.ld;
+    const int LZ = 2 * E.kp.lmax + 1;
+    const size_t smem = ((size_t)LZ * NT * 2 + (size_t)KCH * 5) * sizeof(R);
+    const int sblocks = (s1 - s0 + NT - 1) / NT;
+    const long want = (sizeof(R) == 4 ? 8L : 4L) * 152;
+    int ns = (int)((want + (long)sblocks * E.kp.P - 1) / ((long)sblocks * E.kp.P));
+    ns = std::max(1, std::min(ns, std::min(E.nchunk, E.max_slices)));
+    dim3 g(sblocks, E.kp.P, ns);
+    k_field<F_D, NT, R><<<g, NT, smem, E.stream>>>(E.kp, s0, s1);
+    dim3 g2((s1 - s0 + 127) / 128, E.kp.P);
+    k_adj_fsum<<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns, Dr);
+    E.nlaunch += 2;
+}
+
+template <int LZM>
+static void adj_field_f(Engine &E, double *Dr) {
+    const int s0 = E.kp.fd, s1 = E.kp.ld;
+    const size_t smem = sizeof(float2) * FF_RUNS * LZM;
+    const int sblocks = (s1 - s0 + FF_NT - 1) / FF_NT;
+    const int cmax = std::min(E.nchunk, E.max_slices);
+    const int ns = std::max(1, std::min((int)((8L * 152 + (long)sblocks * E.kp.P - 1) / ((long)sblocks * E.kp.P)), cmax));
+    dim3 g(sblocks, E.kp.P, ns);
+    k_field_f<F_D, LZM><<<g, FF_NT, smem, E.stream>>>(E.kp, s0, s1);
+    dim3 g2((s1 - s0 + 127) / 128, E.kp.P);
+    k_adj_fsum<<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns, Dr);
+    E.nlaunch += 2;
+}
+
+// Dr += the reciprocal dipole field of the structure factor Sm_u at the dipole sites (the
+// forward's field pass without the SOR update; mixed engine: from the FP32 weights that the
+// last adj_structure_factor wrote, which must be Sm_u's)
 void adj_dipole_field(Engine &E, double2 *Sm_u, double *bacc, double *Dr) {
     const KP keep = E.kp;
     E.kp.Sm = Sm_u;
     E.kp.acc = bacc;
-    const int s0 = E.kp.fd, s1 = E.kp.ld, NT = 128;
     const int LZ = 2 * E.kp.lmax + 1;
-    const size_t smem = ((size_t)LZ * NT * 2 + (size_t)KCH * 5) * sizeof(double);
-    const int sblocks = (s1 - s0 + NT - 1) / NT;
-    int ns = (int)((4L * 152 + (long)sblocks * E.kp.P - 1) / ((long)sblocks * E.kp.P));
-    ns = std::max(1, std::min(ns, std::min(E.nchunk, E.max_slices)));
-    dim3 g(sblocks, E.kp.P, ns);
-    if ((size_t)LZ * 128 * 16 <= 64 * 1024)
-        k_field<F_D, 128, double><<<g, NT, smem, E.stream>>>(E.kp, s0, s1);
-    dim3 g2((s1 - s0 + 127) / 128, E.kp.P);
-    k_adj_fsum<<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns, Dr);
-    E.nlaunch += 2;
+    if (E.precision == PIMD_PREC_MIXED && E.ff_regs && LZ <= 49) {
+        if (LZ <= 17)
+            adj_field_f<17>(E, Dr);
+        else if (LZ <= 25)
+            adj_field_f<25>(E, Dr);
+        else if (LZ <= 33)
+            adj_field_f<33>(E, Dr);
+        else
+            adj_field_f<49>(E, Dr);
+    } else if (E.precision == PIMD_PREC_MIXED) {
+        if ((size_t)LZ * 128 * 8 <= 64 * 1024)
+            adj_field_t<128, float>(E, Dr);
+        else
+            adj_field_t<64, float>(E, Dr);
+    } else {
+        if ((size_t)LZ * 128 * 16 <= 64 * 1024)
+            adj_field_t<128, double>(E, Dr);
+        else
+            adj_field_t<64, double>(E, Dr);
+    }
     E.kp = keep;
 }
 
-// Reciprocal-space gradients of the backward, thread per site, FP64, direct sum over the
+// Reciprocal-space gradients of the backward, thread per site, direct sum over the
 // k-list (c_k = 4 pi A_k / V, S raw = sum (k.mu) e^{ik.r} or sum q e^{ik.r}):
 //   BIL  : d/dr_s [u^T D_rec v] = sum_k c_k k [(k.u_s) Im(e_s conj S_v) + (k.v_s) Im(e_s conj S_u)]
 //   CROSS: d/dr_s [nu^T E_q,rec] = sum_k c_k k (k.nu_s) Re(e_s conj S_q) (dipole sites)
@@ -1213,64 +1278,112 @@ void adj_dipole_field(Engine &E, double2 *Sm_u, double *bacc, double *Dr) {
 //          and the potential of the nu dipoles phi_s = -sum_k c_k Im(e_s conj S_nu).
 // Derived from the forward's field formula E_s = sum_k c_k k Im(e_s conj S) (ewald.f90:45-49,
 // 114-117): the k-space operator is the Hessian of a quadratic form, so these are exact.
+// The mixed engine's instance reads the FP32 tables and forms each product in FP32; each run's
+// sums go to the FP64 totals. A block stages each chunk's k-vectors, weights and structure
+// factors in shared memory (converted once per block, not per site). The k-list is split over
+// gridDim.z slices of whole chunks; each slice's per-site sums (G, phi) go to Fpart, and
+// k_adj_rfin adds the slices in a fixed order.
 enum { ADJ_BIL = 0, ADJ_CROSS = 1 };
-template <int MODE>
+template <int MODE, typename R>
 __global__ void __launch_bounds__(128) k_adj_rec(KP kp, int s0, int s1, const double *a, const double *bvec,
                                                  const double2 *SA, const double2 *SB, const double *ebw,
                                                  double *grad, double *phi) {
+    using V = typename C2<R>::T;
+    __shared__ R sk[KCH][4];            // kx, ky, kz, c_k
+    __shared__ R s1x[KCH][2], s2x[KCH][2];  // BIL: conj(raw S_u), conj(raw S_v); CROSS: raw S_q, conj(raw S_nu)
     const int b = blockIdx.y, s = s0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= s1 || ebw[b] == 0.0) return;
-    const size_t gs = (size_t)b * kp.S + s;
-    const double q = kp.pos[gs].w;
-    const bool isdip = s >= kp.fd && s < kp.ld;
-    double av[3] = {0, 0, 0}, bv[3] = {0, 0, 0};
+    if (ebw[b] == 0.0) return;  // the whole block: bead inactive
+    const bool valid = s < s1;
+    const size_t gs = (size_t)b * kp.S + (valid ? s : s0);
+    const R q = valid ? R(kp.pos[gs].w) : R(0);
+    const bool isdip = valid && s >= kp.fd && s < kp.ld;
+    const bool act = (MODE == ADJ_BIL) ? isdip : valid;
+    R av[3] = {R(0), R(0), R(0)}, bv[3] = {R(0), R(0), R(0)};
     if (isdip) {
         for (int c = 0; c < 3; c++) {
-            av[c] = a[3 * gs + c];
-            if (MODE == ADJ_BIL) bv[c] = bvec[3 * gs + c];
+            av[c] = R(a[3 * gs + c]);
+            if (MODE == ADJ_BIL) bv[c] = R(bvec[3 * gs + c]);
         }
     }
     double G[3] = {0, 0, 0}, ph = 0.0;
-    for (int r = 0; r < kp.nrun; r++) {
-        const KRun run = kp.runs[r];
-        const double2 ex = tab_x<double>(kp, b, run.kx, s);
-        const double2 ey = tab_y<double>(kp, b, run.ky, s);
-        const double2 exy = make_double2(ex.x * ey.x - ex.y * ey.y, ex.y * ey.x + ex.x * ey.y);
-        for (int j = 0; j < run.nkz; j++) {
-            const int k = run.kbeg + j, kz = run.kzlo + j;
-            double2 z = tab_z<double>(kp, b, kz < 0 ? -kz : kz, s);
-            if (kz < 0) z = cconj(z);
-            const double2 e = cmul(exy, z);
+    const int slice = blockIdx.z, nslice = gridDim.z;
+    const int c0 = (int)((long)slice * kp.nchunk / nslice), c1 = (int)((long)(slice + 1) * kp.nchunk / nslice);
+    for (int chn = c0; chn < c1; chn++) {
+        const KChunk ch = kp.chunks[chn];
+        __syncthreads();
+        for (int i = threadIdx.x; i < ch.k1 - ch.k0; i += blockDim.x) {
+            const int k = ch.k0 + i;
             const double4_32a ki = kp.kinfo[k];
-            const double kv[3] = {ki.x, ki.y, ki.z}, ck = ki.w;
-            if (MODE == ADJ_BIL) {
-                if (!isdip) continue;
-                // raw S from the rotated (-Im, Re) form: raw = (y, -x)
-                const double2 su = SA[(size_t)b * kp.nk + k], sv = SB[(size_t)b * kp.nk + k];
-                const double2 cu = make_double2(su.y, su.x), cv = make_double2(sv.y, sv.x);  // conj(raw)
-                const double imv = e.x * cv.y + e.y * cv.x, imu = e.x * cu.y + e.y * cu.x;
-                const double ku = kv[0] * av[0] + kv[1] * av[1] + kv[2] * av[2];
-                const double kw = kv[0] * bv[0] + kv[1] * bv[1] + kv[2] * bv[2];
-                const double f = ck * (ku * imv + kw * imu);
-                for (int c = 0; c < 3; c++) G[c] += f * kv[c];
-            } else {
-                if (isdip) {
-                    const double2 sq = kp.Sq[(size_t)b * kp.nk + k];  // raw charge structure factor
-                    const double re = e.x * sq.x + e.y * sq.y;          // Re(e conj Sq)
-                    const double kn = kv[0] * av[0] + kv[1] * av[1] + kv[2] * av[2];
-                    for (int c = 0; c < 3; c++) G[c] += ck * kn * re * kv[c];
-                }
-                if (q != 0.0) {
-                    const double2 sn = SA[(size_t)b * kp.nk + k];
-                    const double2 cn = make_double2(sn.y, sn.x);  // conj(raw S_nu)
-                    const double re = e.x * cn.x - e.y * cn.y, im = e.x * cn.y + e.y * cn.x;
-                    for (int c = 0; c < 3; c++) G[c] -= q * ck * re * kv[c];
-                    ph -= ck * im;
+            sk[i][0] = R(ki.x);
+            sk[i][1] = R(ki.y);
+            sk[i][2] = R(ki.z);
+            sk[i][3] = R(ki.w);
+            const double2 x1 = (MODE == ADJ_BIL) ? SA[(size_t)b * kp.nk + k] : kp.Sq[(size_t)b * kp.nk + k];
+            const double2 x2 = (MODE == ADJ_BIL) ? SB[(size_t)b * kp.nk + k] : SA[(size_t)b * kp.nk + k];
+            // rotated (-Im, Re) forms: conj(raw) = (y, x); the raw charge structure factor as is
+            s1x[i][0] = (MODE == ADJ_BIL) ? R(x1.y) : R(x1.x);
+            s1x[i][1] = (MODE == ADJ_BIL) ? R(x1.x) : R(x1.y);
+            s2x[i][0] = R(x2.y);
+            s2x[i][1] = R(x2.x);
+        }
+        __syncthreads();
+        if (!act) continue;
+        for (int r = ch.r0; r < ch.r1; r++) {
+            const KRun run = kp.runs[r];
+            const V ex = tab_x<R>(kp, b, run.kx, s);
+            const V ey = tab_y<R>(kp, b, run.ky, s);
+            const V exy = C2<R>::make(ex.x * ey.x - ex.y * ey.y, ex.y * ey.x + ex.x * ey.y);
+            R Gr[3] = {R(0), R(0), R(0)}, phr = R(0);
+            const int i0 = run.kbeg - ch.k0;
+            for (int j = 0; j < run.nkz; j++) {
+                const int kz = run.kzlo + j, i = i0 + j;
+                V z = tab_z<R>(kp, b, kz < 0 ? -kz : kz, s);
+                if (kz < 0) z = cconj(z);
+                const V e = C2<R>::make(exy.x * z.x - exy.y * z.y, exy.y * z.x + exy.x * z.y);
+                const R kv[3] = {sk[i][0], sk[i][1], sk[i][2]}, ck = sk[i][3];
+                if (MODE == ADJ_BIL) {
+                    const R imu = e.x * s1x[i][1] + e.y * s1x[i][0], imv = e.x * s2x[i][1] + e.y * s2x[i][0];
+                    const R ku = kv[0] * av[0] + kv[1] * av[1] + kv[2] * av[2];
+                    const R kw = kv[0] * bv[0] + kv[1] * bv[1] + kv[2] * bv[2];
+                    const R f = ck * (ku * imv + kw * imu);
+                    for (int c = 0; c < 3; c++) Gr[c] += f * kv[c];
+                } else {
+                    if (isdip) {
+                        const R re = e.x * s1x[i][0] + e.y * s1x[i][1];  // Re(e conj Sq)
+                        const R kn = kv[0] * av[0] + kv[1] * av[1] + kv[2] * av[2];
+                        for (int c = 0; c < 3; c++) Gr[c] += ck * kn * re * kv[c];
+                    }
+                    if (q != R(0)) {
+                        const R re = e.x * s2x[i][0] - e.y * s2x[i][1], im = e.x * s2x[i][1] + e.y * s2x[i][0];
+                        for (int c = 0; c < 3; c++) Gr[c] -= q * ck * re * kv[c];
+                        phr -= ck * im;
+                    }
                 }
             }
+            for (int c = 0; c < 3; c++) G[c] += (double)Gr[c];
+            ph += (double)phr;
         }
     }
-    const double w = ebw[b];  // per-bead scale (0: bead inactive)
+    if (valid)
+        kp.Fpart[((size_t)slice * kp.P + b) * (s1 - s0) + (s - s0)] = make_double4_32a(G[0], G[1], G[2], ph);
+}
+
+// grad += w (sum of the slices' G), phi += w (sum of their potentials) (CROSS), slices in order
+template <int MODE>
+__global__ void __launch_bounds__(128) k_adj_rfin(KP kp, int s0, int s1, int nslice, const double *ebw, double *grad,
+                                                  double *phi) {
+    const int b = blockIdx.y, s = s0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= s1 || ebw[b] == 0.0) return;
+    double G[3] = {0, 0, 0}, ph = 0.0;
+    for (int z = 0; z < nslice; z++) {
+        const double4_32a p = kp.Fpart[((size_t)z * kp.P + b) * (s1 - s0) + (s - s0)];
+        G[0] += p.x;
+        G[1] += p.y;
+        G[2] += p.z;
+        ph += p.w;
+    }
+    const size_t gs = (size_t)b * kp.S + s;
+    const double w = ebw[b];  // per-bead scale
     for (int c = 0; c < 3; c++) grad[3 * gs + c] += w * G[c];
     if (MODE == ADJ_CROSS && phi) phi[gs] += w * ph;
 }
@@ -1278,12 +1391,25 @@ __global__ void __launch_bounds__(128) k_adj_rec(KP kp, int s0, int s1, const do
 void adj_rec(Engine &E, int mode, const double *a, const double *bvec, const double2 *SA, const double2 *SB,
              const double *ebw, double *grad, double *phi) {
     const int s0 = (mode == ADJ_BIL) ? E.kp.fd : 0, s1 = (mode == ADJ_BIL) ? E.kp.ld : E.kp.S;
-    dim3 g((s1 - s0 + 127) / 128, E.kp.P);
-    if (mode == ADJ_BIL)
-        k_adj_rec<ADJ_BIL><<<g, 128, 0, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
-    else
-        k_adj_rec<ADJ_CROSS><<<g, 128, 0, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
-    ++E.nlaunch;
+    const int sblocks = (s1 - s0 + 127) / 128;
+    const int ns = std::max(1, std::min((int)((8L * 152 + (long)sblocks * E.kp.P - 1) / ((long)sblocks * E.kp.P)),
+                                        std::min(E.kp.nchunk, E.max_slices)));
+    dim3 g(sblocks, E.kp.P, ns), g2(sblocks, E.kp.P);
+    const bool f = E.precision == PIMD_PREC_MIXED;
+    if (mode == ADJ_BIL) {
+        if (f)
+            k_adj_rec<ADJ_BIL, float><<<g, 128, 0, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
+        else
+            k_adj_rec<ADJ_BIL, double><<<g, 128, 0, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
+        k_adj_rfin<ADJ_BIL><<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns, ebw, grad, phi);
+    } else {
+        if (f)
+            k_adj_rec<ADJ_CROSS, float><<<g, 128, 0, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
+        else
+            k_adj_rec<ADJ_CROSS, double><<<g, 128, 0, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
+        k_adj_rfin<ADJ_CROSS><<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns, ebw, grad, phi);
+    }
+    E.nlaunch += 2;
 }
 
 // first site whose charge field is read: TTM3-F never reads the O-site field (no charge, no

@@ -587,15 +587,6 @@ __global__ void __launch_bounds__(128) k_dipf_sync(KP kp) {
     mrec_dipole(kp, b, s, mf);
 }
 
-PIMD_D void dd_force_f(const float R[3], const float di[3], const float dj[3], float t2, float t3, float dij[3]) {
-    const float rdi = R[0] * di[0] + R[1] * di[1] + R[2] * di[2];
-    const float rdj = R[0] * dj[0] + R[1] * dj[1] + R[2] * dj[2];
-    const float didj = di[0] * dj[0] + di[1] * dj[1] + di[2] * dj[2];
-    const float a = 15.f * t3 * rdi * rdj - 3.f * t2 * didj;
-#pragma unroll
-    for (int c = 0; c < 3; c++) dij[c] += a * R[c] - 3.f * t2 * (rdi * dj[c] + rdj * di[c]);
-}
-
 // pot_ttm.f90:399-542 in FP32 pair arithmetic, as a gather like k_pair_qq_m: QL lanes per
 // molecule i over its full-list entries accumulate i's side (gradients at i's sites, the
 // potentials at i's sites from j's dipoles) with virials at weight 1/2, then lane 0 of the group
@@ -773,6 +764,129 @@ __global__ void __launch_bounds__(128, 5) k_pair_force_m(KP kp) {
         }
     }
     block_reduce_add_f<14, 128>(av, kp.acc + (size_t)b * NACC);
+}
+
+// ---------------------------------------------------------------------------------------
+// Differentiation form, mixed engine (TTM3-F): the real-space terms of the backward outside the
+// dipole sweep (the FP64 engine's k_adj_pairs) as a gather over the full list like the force
+// pass -- QL lanes per molecule i over its entries (i, j), FP32 pair arithmetic from the O
+// fixed-point sites and the site offsets, only i's side accumulated (the gradient at i's sites
+// and the potential of the adjoint dipoles nu at i's charges; j's side when j gathers i), so
+// there are no atomics per entry. Per entry:
+//   * van der Waals on O-O: eb grad(C/r^6 + D e^{-E r} + A/r^12 + B/r^10) at O(i);
+//   * for the charged sites a of i and c of j (H1, H2, M), with the charge-dipole smear2
+//     (ts1, ts2) at R = r_a(i) - r_c(j): if a = M, nu_M(i) in the field of q_c(j) gives
+//     q_c (ts1 nu - 3 ts2 (R.nu) R) at M(i); if c = M, nu_M(j) in the field of q_a(i) gives
+//     minus the same form (R -> -R, nu_M(j), q_a) at a(i) and ts1 (R.nu) to its potential;
+//   * the theta sums (a_cc: e^{-a r^3} (R.nu) and the Uelec term q_a q_c dts0/da with
+//     dts0/da = exp(-a r^3) h(a^(1/3) r) / (3 a^(2/3)) from the tabulated Q(2/3, x); vdW C, D, E),
+//     which see every pair twice, at weight 1/2.
+__global__ void __launch_bounds__(128) k_adj_pairs_m(KP kp, float4 pfa, const double *ebar, const double *nu,
+                                                     double *grad, double *phin, double *thacc) {
+    const int b = blockIdx.y, N = kp.N;
+    const int sub = threadIdx.x & (QL - 1);
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) / QL;
+    const float pf[5] = {0.f, pfa.x, pfa.y, pfa.z, pfa.w};  // polfac of site kinds 1..4
+    const float eb = (float)ebar[b];
+    const float vA = kp.ptf.vdw[0], vB = kp.ptf.vdw[1], vC = kp.ptf.vdw[2], vD = kp.ptf.vdw[3], vE = kp.ptf.vdw[4];
+    float gI[5][3], phI[5], th[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 5; k++) gI[k][0] = gI[k][1] = gI[k][2] = phI[k] = 0.f;
+    if (i < N) {
+        const float4 *pf4 = kp.posf + (size_t)b * kp.S;
+        const uint4 *of = kp.ofix + (size_t)b * N;
+        const int2 *fl = reinterpret_cast<const int2 *>(kp.fnbr) + (size_t)b * kp.fcap;
+        const double *nub = nu + 3 * ((size_t)b * kp.S + 3 * N);
+        const float L[3] = {kp.ptf.box[0], kp.ptf.box[1], kp.ptf.box[2]};
+        const float Li[3] = {kp.ptf.boxi[0], kp.ptf.boxi[1], kp.ptf.boxi[2]};
+        const int ne = kp.fntot[b];
+        const int e0 = min(kp.foff[(size_t)b * N + i], ne);
+        const int e1 = (i + 1 < N) ? min(kp.foff[(size_t)b * N + i + 1], ne) : ne;
+        const uint4 oi = of[i];
+        float4 di[5];
+#pragma unroll
+        for (int k = 2; k <= 4; k++) di[k] = pf4[(k - 1) * N + i];
+        const float ni[3] = {(float)nub[3 * i], (float)nub[3 * i + 1], (float)nub[3 * i + 2]};
+        for (int e = e0 + sub; e < e1; e += QL) {
+            const int j = fl[e].y;
+            float Rf[3];
+            oo_min_image(kp, oi, of[j], Rf);
+            {  // van der Waals, O-O
+                const float r2 = Rf[0] * Rf[0] + Rf[1] * Rf[1] + Rf[2] * Rf[2], r = sqrtf(r2);
+                const float r2i = 1.f / r2, r6i = r2i * r2i * r2i, ex = __expf(-vE * r);
+                const float dur = (-12.f * vA * r6i * r6i - 10.f * vB * r6i * r2i * r2i - 6.f * vC * r6i) * r2i - vD * vE * ex / r;
+#pragma unroll
+                for (int c = 0; c < 3; c++) gI[1][c] += eb * dur * Rf[c];
+                th[1] += eb * r6i;
+                th[2] += eb * ex;
+                th[3] -= eb * vD * r * ex;
+            }
+            float4 dj[5];
+#pragma unroll
+            for (int k = 2; k <= 4; k++) dj[k] = pf4[(k - 1) * N + j];
+            const float nj[3] = {(float)nub[3 * j], (float)nub[3 * j + 1], (float)nub[3 * j + 2]};
+#pragma unroll
+            for (int a = 2; a <= 4; a++) {
+#pragma unroll
+                for (int c = 2; c <= 4; c++) {
+                    const float Rs[3] = {wrapf(Rf[0] + di[a].x - dj[c].x, L[0], Li[0]),
+                                         wrapf(Rf[1] + di[a].y - dj[c].y, L[1], Li[1]),
+                                         wrapf(Rf[2] + di[a].z - dj[c].z, L[2], Li[2])};
+                    const float d2 = Rs[0] * Rs[0] + Rs[1] * Rs[1] + Rs[2] * Rs[2];
+                    const float a12 = kp.ptf.apol_cd[a][c];
+                    float ts1, ts2;
+                    smear2<float>(d2, a12, kp.ewf, &ts1, &ts2);
+                    const float pfac = pf[a] * pf[c], qa = di[a].w, qc = dj[c].w;
+                    float e1 = 0.f;
+                    if (d2 < 25.f) {
+                        const float dd = sqrtf(d2), ra = cbrtf(a12);
+                        e1 = __expf(-a12 * d2 * dd);
+                        th[0] += eb * qa * qc * (e1 * gq_h(kp.gq23, ra * dd) / (3.f * ra * ra)) * pfac;
+                    }
+                    if (a == 4) {  // nu at M(i) in the field of q_c(j)
+                        const float rn = Rs[0] * ni[0] + Rs[1] * ni[1] + Rs[2] * ni[2];
+#pragma unroll
+                        for (int q = 0; q < 3; q++) gI[4][q] += qc * (ts1 * ni[q] - 3.f * ts2 * rn * Rs[q]);
+                        th[0] += qc * e1 * rn * pfac;
+                    }
+                    if (c == 4) {  // nu at M(j) in the field of q_a(i): R = r_M(j) - r_a(i) = -Rs
+                        const float rn = -(Rs[0] * nj[0] + Rs[1] * nj[1] + Rs[2] * nj[2]);
+#pragma unroll
+                        for (int q = 0; q < 3; q++) gI[a][q] -= qa * (ts1 * nj[q] + 3.f * ts2 * rn * Rs[q]);
+                        phI[a] += ts1 * rn;
+                        th[0] += qa * e1 * rn * pfac;
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 1; k <= 4; k++) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) gI[k][c] = group_sum<QL>(gI[k][c]);
+        phI[k] = group_sum<QL>(phI[k]);
+    }
+    if (i < N && sub == 0) {
+        const size_t base = (size_t)b * kp.S;
+#pragma unroll
+        for (int k = 1; k <= 4; k++) {
+            double *g = grad + 3 * (base + (k - 1) * N + i);
+#pragma unroll
+            for (int c = 0; c < 3; c++) g[c] += (double)gI[k][c];
+            if (k >= 2) phin[base + (k - 1) * N + i] += (double)phI[k];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) th[q] *= 0.5f;
+    block_reduce_add_f<4, 128>(th, thacc + PIMD_TH_A_CC);  // slots A_CC, VDW_C, VDW_D, VDW_E (contiguous)
+}
+
+void launch_adj_pairs_m(Engine &E, const double pf[5], const double *ebar, const double *nu, double *grad, double *phin,
+                        double *thacc) {
+    dim3 g((E.kp.N * QL + 127) / 128, E.kp.P);
+    const float4 pfa = make_float4((float)pf[1], (float)pf[2], (float)pf[3], (float)pf[4]);
+    k_adj_pairs_m<<<g, 128, 0, E.stream>>>(E.kp, pfa, ebar, nu, grad, phin, thacc);
+    ++E.nlaunch;
 }
 
 // ---------------------------------------------------------------------------------------

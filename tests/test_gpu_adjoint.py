@@ -94,3 +94,44 @@ def test_backward_requires_forward(pkg, engine_lib):
     eng = pkg.ForceEngine(p)
     with pytest.raises(pkg.engine.PimdError):
         eng.pot_backward(np.ones(1))
+
+
+def rms_rel(a, b):
+    return float(np.sqrt(((a - b) ** 2).mean() / (b ** 2).mean()))
+
+
+@pytest.mark.parametrize("eps", [0.0, 1e-4])
+def test_mixed_backward_matches_fp64(pkg, engine_lib, eps):
+    """The mixed engine's forward + backward (FP32 pair, table and reciprocal products, FP64 sums)
+    against the FP64 engine's on the same coordinates and parameters: the position gradient
+    within the mixed force budget (1e-4 RMS relative) and every dE/dtheta within 1e-4 of the
+    largest. eps = 0 runs a fixed 6 iterations; eps = 1e-4 stops at a loose tolerance, where
+    the backward differentiates the truncated iteration (both engines stop at the same count)."""
+    c, p = case(pkg, nw=64, P=2, K=6 if eps == 0.0 else 40, eps=eps)
+    ebar = np.array([1.0, 0.5])
+    res = []
+    for prec in (pkg.engine.PIMD_FP64, pkg.engine.PIMD_MIXED):
+        eng = pkg.ForceEngine(p, precision=prec)
+        U = eng.pot_forward(c["RRt"], c["RRc"])
+        n = [eng.energies(k)["niter"] for k in range(2)]
+        g, dth = eng.pot_backward(ebar)
+        res.append((U, n, g, dth))
+        eng.close()
+    (U64, n64, g64, th64), (Um, nm, gm, thm) = res
+    assert n64 == nm
+    assert np.abs(Um - U64).max() < 1e-5 * np.abs(U64).max()
+    assert rms_rel(gm, g64) < 1e-4
+    assert np.abs(thm - th64).max() < 1e-4 * np.abs(th64).max()
+
+
+def test_mixed_backward_equals_mixed_forces_when_converged(pkg, engine_lib):
+    """At converged dipoles (1e-10) and rc1 = rc the mixed backward's position gradient equals the
+    mixed engine's own analytic forces within the mixed budget."""
+    c, p = case(pkg, nw=64, P=2, K=100, eps=1e-10)
+    p["rc1"] = p["rc"]
+    eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_MIXED)
+    eng.pot_forward(c["RRt"], c["RRc"])
+    g, _ = eng.pot_backward(np.ones(2))
+    ref = eng.full_bead_forces(c["RRt"], c["RRc"])["dRRt"]
+    assert rms_rel(g, ref) < 1e-4
+    eng.close()
