@@ -83,20 +83,25 @@ int apply_theta(Engine &E) {
 }
 
 // ---------------------------------------------------------------------------------------
-// tape: mu_iter of the dipole sites, and (iteration 0) the charge-only potential
-__global__ void k_tape(KP kp, double *tape, double *phiq, int iter) {
+// tape: mu_iter of the dipole sites, (iteration 0) the charge-only potential, and (iteration
+// iter >= 1) the structure factor that iteration formed from mu_{iter-1} (kp.Sm, unchanged in
+// beads already converged, which the backward does not read at that iteration)
+__global__ void k_tape(KP kp, double *tape, double *phiq, double2 *tapeS, int iter) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     const int nd = kp.ld - kp.fd;
     if (t < nd)
         for (int c = 0; c < 3; c++)
             tape[(((size_t)iter * kp.P + b) * nd + t) * 3 + c] = kp.dip[3 * ((size_t)b * kp.S + kp.fd + t) + c];
     if (iter == 0 && t < kp.S) phiq[(size_t)b * kp.S + t] = kp.F[(size_t)b * kp.S + t].w;
+    if (iter >= 1)
+        for (int k = t; k < kp.nk; k += gridDim.x * blockDim.x)
+            tapeS[((size_t)(iter - 1) * kp.P + b) * kp.nk + k] = kp.Sm[(size_t)b * kp.nk + k];
 }
 
 void tape_record(Engine &E, int iter) {
     if (!E.d_tape || iter > E.tape_kmax) return;
     dim3 g((E.kp.S + 127) / 128, E.kp.P);
-    k_tape<<<g, 128, 0, E.stream>>>(E.kp, E.d_tape, E.d_phiq, iter);
+    k_tape<<<g, 128, 0, E.stream>>>(E.kp, E.d_tape, E.d_phiq, E.d_tapeS, iter);
     ++E.nlaunch;
 }
 
@@ -608,9 +613,13 @@ int pimd_pot_forward(pimd_ctx *ctx, const double *RRt, const double *RRc, double
     if (!E.d_tape || E.tape_kmax != kp.polar_maxiter) {
         if (E.d_tape) cudaFree(E.d_tape);
         if (E.d_phiq) cudaFree(E.d_phiq);
+        if (E.d_tapeS) cudaFree(E.d_tapeS);
         E.d_tape = E.d_phiq = nullptr;
+        E.d_tapeS = nullptr;
+        E.tape_kmax = 0;
         if (cudaMalloc((void **)&E.d_tape, sizeof(double) * (kp.polar_maxiter + 1) * kp.P * nd * 3) != cudaSuccess ||
-            cudaMalloc((void **)&E.d_phiq, sizeof(double) * kp.P * kp.S) != cudaSuccess)
+            cudaMalloc((void **)&E.d_phiq, sizeof(double) * kp.P * kp.S) != cudaSuccess ||
+            cudaMalloc((void **)&E.d_tapeS, sizeof(double2) * std::max(1, kp.polar_maxiter) * kp.P * kp.nk) != cudaSuccess)
             return adj_fail(E, PIMD_ERR_NOMEM, "tape allocation");
         E.tape_kmax = kp.polar_maxiter;
     }
@@ -651,7 +660,7 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
     double *g = E.d_adj, *u = g + 3 * P * nd, *v = u + sv, *Dr = v + sv, *grad = Dr + sv, *nu = grad + sv;
     double *phin = nu + sv;
     const uintptr_t sa = (reinterpret_cast<uintptr_t>(phin + P * S) + 15) & ~uintptr_t(15);  // 16-byte rows
-    double2 *Smu = reinterpret_cast<double2 *>(sa), *Smv = Smu + P * kp.nk, *Snu = Smv + P * kp.nk;
+    double2 *Smu = reinterpret_cast<double2 *>(sa), *Snu = Smu + 2 * P * kp.nk;
     double *bacc = reinterpret_cast<double *>(Snu + P * kp.nk), *bw = bacc + P * NACC, *ebar = bw + P, *ones = ebar + P;
     double *thacc = ones + P, *dR = thacc + PIMD_NTHETA;
     const uintptr_t ua = (reinterpret_cast<uintptr_t>(dR + P * kp.natoms * 3) + 15) & ~uintptr_t(15);  // 16-byte rows
@@ -706,8 +715,8 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
                 launch_dd_real(E);
             E.kp = keep;
         }
-        // v first: the mixed field pass reads the weights of the last structure factor
-        adj_structure_factor(E, v, mixed ? vf : nullptr, Smv, bacc);
+        // S(v) = S(mu_{k-1}) is on the tape (the forward's iteration k formed it)
+        const double2 *Smv = E.d_tapeS + (size_t)(k - 1) * P * kp.nk;
         adj_structure_factor(E, u, mixed ? uf : nullptr, Smu, bacc);
         adj_dipole_field(E, Smu, bacc, Dr);
         k_adj_g<<<gd, 128, 0, st>>>(kp, k, iters, g, u, Dr, omega);
@@ -720,7 +729,6 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
     k_adj_final<<<gd, 128, 0, st>>>(kp, g, nu, thacc);
     // charge-field adjoint nu: real-space pairs, reciprocal, intramolecular; vdW; Uelec d/da_cc
     cudaMemsetAsync(bacc, 0, sizeof(double) * P * NACC, st);
-    adj_charge_sfac(E, bacc);
     adj_structure_factor(E, nu, nullptr, Snu, bacc);
     adj_rec(E, 1, nu, nullptr, Snu, nullptr, ones, grad, phin);
     if (mixed)

@@ -734,6 +734,7 @@ int pimd_destroy(pimd_ctx *ctx) {
     if (E.h_pin) cudaFreeHost(E.h_pin);
     if (E.d_tape) cudaFree(E.d_tape);
     if (E.d_phiq) cudaFree(E.d_phiq);
+    if (E.d_tapeS) cudaFree(E.d_tapeS);
     if (E.d_adj) cudaFree(E.d_adj);
     if (E.gexec) cudaGraphExecDestroy(E.gexec);
     if (E.body_stream) cudaStreamDestroy(E.body_stream);

@@ -306,6 +306,7 @@ struct Engine {
     int tape_kmax = 0;           // iterations the tape holds
     double *d_tape = nullptr;    // [kmax + 1][P][N][3] dipoles of the dipole sites per iteration
     double *d_phiq = nullptr;    // [P][S] charge-only potential after the charge phase
+    double2 *d_tapeS = nullptr;  // [kmax][P][nk] structure factor S(mu_k) of each iteration's dipoles (Sm form)
     double *d_adj = nullptr;     // backward scratch
     size_t adj_bytes = 0;
     bool tape_valid = false;
@@ -388,7 +389,6 @@ void tape_record(Engine &E, int iter);
 int apply_theta(Engine &E);
 void adjoint_init(Engine &E);
 void adj_structure_factor(Engine &E, const double *dipbuf, const float4 *dipf32, double2 *Sout, double *bacc);
-void adj_charge_sfac(Engine &E, double *bacc);
 void launch_adj_pairs_m(Engine &E, const double pf[5], const double *ebar, const double *nu, double *grad, double *phin,
                         double *thacc);
 void adj_dipole_field(Engine &E, double2 *Sm_u, double *bacc, double *Dr);

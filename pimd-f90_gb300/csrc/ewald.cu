@@ -1180,17 +1180,6 @@ void adj_structure_factor(Engine &E, const double *dipbuf, const float4 *dipf32,
     E.kp = keep;
 }
 
-// The charge structure factor (raw, sum_s q_s e^{ik.r_s}) into kp.Sq again, in the layout the
-// backward's cross term reads (the mixed forward's tensor-core passes keep their own); the
-// pass's sums go to bacc.
-void adj_charge_sfac(Engine &E, double *bacc) {
-    if (E.precision != PIMD_PREC_MIXED) return;  // the FP64 forward's Sq is already this one
-    const KP keep = E.kp;
-    E.kp.acc = bacc;
-    run_spass_t<OP_Q, float>(E, E.kp.fq, E.kp.S - E.kp.fq, 0);
-    E.kp = keep;
-}
-
 // Dr[b][s] += reciprocal dipole field at the dipole sites from the structure factor Sm_u (the
 // forward's k_field<F_D> without the SOR update)
 __global__ void __launch_bounds__(128) k_adj_fsum(KP kp, int s0, int s1, int nslice, double *Dr) {
@@ -1305,6 +1294,12 @@ __global__ void __launch_bounds__(128) k_adj_rec(KP kp, int s0, int s1, const do
             if (MODE == ADJ_BIL) bv[c] = R(bvec[3 * gs + c]);
         }
     }
+    // FP32: this site's kz table column in shared memory (dynamic, (lmax + 1) x 128), read in
+    // the k loop instead of from the global table
+    extern __shared__ float2 adj_ez[];
+    if constexpr (sizeof(R) == 4)
+        for (int n = 0; n <= kp.lmax; n++)
+            adj_ez[n * 128 + threadIdx.x] = valid ? tab_z<float>(kp, b, n, s) : make_float2(0.f, 0.f);
     double G[3] = {0, 0, 0}, ph = 0.0;
     const int slice = blockIdx.z, nslice = gridDim.z;
     const int c0 = (int)((long)slice * kp.nchunk / nslice), c1 = (int)((long)(slice + 1) * kp.nchunk / nslice);
@@ -1337,7 +1332,11 @@ __global__ void __launch_bounds__(128) k_adj_rec(KP kp, int s0, int s1, const do
             const int i0 = run.kbeg - ch.k0;
             for (int j = 0; j < run.nkz; j++) {
                 const int kz = run.kzlo + j, i = i0 + j;
-                V z = tab_z<R>(kp, b, kz < 0 ? -kz : kz, s);
+                V z;
+                if constexpr (sizeof(R) == 4)
+                    z = adj_ez[(kz < 0 ? -kz : kz) * 128 + threadIdx.x];
+                else
+                    z = tab_z<R>(kp, b, kz < 0 ? -kz : kz, s);
                 if (kz < 0) z = cconj(z);
                 const V e = C2<R>::make(exy.x * z.x - exy.y * z.y, exy.y * z.x + exy.x * z.y);
                 const R kv[3] = {sk[i][0], sk[i][1], sk[i][2]}, ck = sk[i][3];
@@ -1396,15 +1395,20 @@ void adj_rec(Engine &E, int mode, const double *a, const double *bvec, const dou
                                         std::min(E.kp.nchunk, E.max_slices)));
     dim3 g(sblocks, E.kp.P, ns), g2(sblocks, E.kp.P);
     const bool f = E.precision == PIMD_PREC_MIXED;
+    const size_t ezb = sizeof(float2) * 128 * (E.kp.lmax + 1);  // FP32 kz column, <= 128 KB (lmax <= 127)
+    if (f && ezb > 48 * 1024) {
+        cudaFuncSetAttribute(k_adj_rec<ADJ_BIL, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ezb);
+        cudaFuncSetAttribute(k_adj_rec<ADJ_CROSS, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ezb);
+    }
     if (mode == ADJ_BIL) {
         if (f)
-            k_adj_rec<ADJ_BIL, float><<<g, 128, 0, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
+            k_adj_rec<ADJ_BIL, float><<<g, 128, ezb, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
         else
             k_adj_rec<ADJ_BIL, double><<<g, 128, 0, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
         k_adj_rfin<ADJ_BIL><<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns, ebw, grad, phi);
     } else {
         if (f)
-            k_adj_rec<ADJ_CROSS, float><<<g, 128, 0, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
+            k_adj_rec<ADJ_CROSS, float><<<g, 128, ezb, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
         else
             k_adj_rec<ADJ_CROSS, double><<<g, 128, 0, E.stream>>>(E.kp, s0, s1, a, bvec, SA, SB, ebw, grad, phi);
         k_adj_rfin<ADJ_CROSS><<<g2, 128, 0, E.stream>>>(E.kp, s0, s1, ns, ebw, grad, phi);
