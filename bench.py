@@ -56,6 +56,8 @@ def parse():
                     help="run two force calls of the workload and exit (the case profiled with ncu)")
     ap.add_argument("--profile-md", choices=["fp64", "mixed"],
                     help="run three eager MD steps of the workload and exit (integrator kernels under ncu)")
+    ap.add_argument("--profile-backward", choices=["fp64", "mixed"],
+                    help="run two forward + backward pairs of the differentiation form on the workload and exit")
     return ap.parse_args()
 
 
@@ -82,6 +84,22 @@ def profile_md(pkg, which):
     for t in (1, 2, 3):
         out, _ = eng.md_step(mp, RRt, PPt, dRRt, t)
     print(json.dumps(dict(profile_md=which, Upot=float(out[0]), uk=float(out[3]))))
+    eng.close()
+
+
+def profile_backward(pkg, which):
+    c, p = workload(pkg, CONFIG)
+    prec = pkg.engine.PIMD_MIXED if which == "mixed" else pkg.engine.PIMD_FP64
+    eng = pkg.ForceEngine(p, precision=prec)
+    ebar = np.ones(p["nbeads"])
+    for _ in range(2):
+        t0 = time.perf_counter()
+        U = eng.pot_forward(c["RRt"], c["RRc"])
+        t1 = time.perf_counter()
+        g, dth = eng.pot_backward(ebar)
+        t2 = time.perf_counter()
+    print(json.dumps(dict(profile_backward=which, Upot=float(U.sum()), forward_ms=round(1e3 * (t1 - t0), 2),
+                          backward_ms=round(1e3 * (t2 - t1), 2), grad_max=float(np.abs(g).max()))))
     eng.close()
 
 
@@ -396,6 +414,10 @@ def main():
     if args.profile_md:
         pkg.build_lib.build()
         profile_md(pkg, args.profile_md)
+        return 0
+    if args.profile_backward:
+        pkg.build_lib.build()
+        profile_backward(pkg, args.profile_backward)
         return 0
     if args.impl == "reference":
         if rank != 0:

@@ -1267,7 +1267,7 @@ void adj_dipole_field(Engine &E, double2 *Sm_u, double *bacc, double *Dr) {
 //          and the potential of the nu dipoles phi_s = -sum_k c_k Im(e_s conj S_nu).
 // Derived from the forward's field formula E_s = sum_k c_k k Im(e_s conj S) (ewald.f90:45-49,
 // 114-117): the k-space operator is the Hessian of a quadratic form, so these are exact.
-// The mixed engine's instance reads the FP32 tables and forms each product in FP32; each run's
+// The mixed engine's instance reads the FP32 tables and forms each product in FP32; each chunk's
 // sums go to the FP64 totals. A block stages each chunk's k-vectors, weights and structure
 // factors in shared memory (converted once per block, not per site). The k-list is split over
 // gridDim.z slices of whole chunks; each slice's per-site sums (G, phi) go to Fpart, and
@@ -1323,12 +1323,14 @@ __global__ void __launch_bounds__(128) k_adj_rec(KP kp, int s0, int s1, const do
         }
         __syncthreads();
         if (!act) continue;
+        // per-chunk partial sums in R, added to the FP64 totals once per chunk (FP64 is a narrow
+        // pipe on this part)
+        R Gr[3] = {R(0), R(0), R(0)}, phr = R(0);
         for (int r = ch.r0; r < ch.r1; r++) {
             const KRun run = kp.runs[r];
             const V ex = tab_x<R>(kp, b, run.kx, s);
             const V ey = tab_y<R>(kp, b, run.ky, s);
             const V exy = C2<R>::make(ex.x * ey.x - ex.y * ey.y, ex.y * ey.x + ex.x * ey.y);
-            R Gr[3] = {R(0), R(0), R(0)}, phr = R(0);
             const int i0 = run.kbeg - ch.k0;
             for (int j = 0; j < run.nkz; j++) {
                 const int kz = run.kzlo + j, i = i0 + j;
@@ -1359,9 +1361,9 @@ __global__ void __launch_bounds__(128) k_adj_rec(KP kp, int s0, int s1, const do
                     }
                 }
             }
-            for (int c = 0; c < 3; c++) G[c] += (double)Gr[c];
-            ph += (double)phr;
         }
+        for (int c = 0; c < 3; c++) G[c] += (double)Gr[c];
+        ph += (double)phr;
     }
     if (valid)
         kp.Fpart[((size_t)slice * kp.P + b) * (s1 - s0) + (s - s0)] = make_double4_32a(G[0], G[1], G[2], ph);

@@ -319,21 +319,21 @@ __global__ void __launch_bounds__(128) k_pair_qq_m(KP kp) {
         for (int c = 0; c < 4; c++) Fi[k][c] = group_sum<QL>(Fi[k][c]);
 #pragma unroll
     for (int c = 0; c < 3; c++) gR[c] = group_sum<QL>(gR[c]);
-    if (i < N && sub == 0) {
-        double4_32a *Fb = kp.F + (size_t)b * kp.S;
+    // the FP64 adds spread over the group's lanes, one value each (FP64 is a narrow pipe on this
+    // part): lane sub adds component sub % 4 of site sub / 4 + 1, lanes 0-2 the O gradient
+    if (i < N) {
+        const int k = sub / 4 + 1, c = sub % 4;
+        float v = 0.f;
 #pragma unroll
-        for (int k = 1; k <= 4; k++) {
-            if (MODEL != 2 && k == 1) continue;
-            double4_32a f = Fb[(k - 1) * N + i];
-            f.x += (double)Fi[k][0];
-            f.y += (double)Fi[k][1];
-            f.z += (double)Fi[k][2];
-            if (k != 1) f.w += (double)Fi[k][3];
-            Fb[(k - 1) * N + i] = f;
+        for (int kk = 1; kk <= 4; kk++)
+#pragma unroll
+            for (int cc = 0; cc < 4; cc++)
+                if ((kk - 1) * 4 + cc == sub) v = Fi[kk][cc];
+        if (!(MODEL != 2 && k == 1) && !(k == 1 && c == 3)) {
+            double *Fd = reinterpret_cast<double *>(kp.F + (size_t)b * kp.S + (size_t)(k - 1) * N + i);
+            Fd[c] += (double)v;
         }
-        double *dRi = kp.dR + 3 * ((size_t)b * kp.S + i);
-#pragma unroll
-        for (int c = 0; c < 3; c++) dRi[c] += (double)gR[c];
+        if (sub < 3) kp.dR[3 * ((size_t)b * kp.S + i) + sub] += (double)(sub == 0 ? gR[0] : sub == 1 ? gR[1] : gR[2]);
     }
     // each unordered pair was visited from both ends
 #pragma unroll
@@ -753,14 +753,23 @@ __global__ void __launch_bounds__(128, 5) k_pair_force_m(KP kp) {
         for (int c = 0; c < 3; c++) gi[k][c] = group_sum<QL>(gi[k][c]);
         if (k != 1) pi[k] = group_sum<QL>(pi[k]);
     }
-    if (i < N && sub == 0) {
-        double *dR = kp.dR + (size_t)b * kp.S * 3;
-        double4_32a *Fb = kp.F + (size_t)b * kp.S;
+    // the FP64 adds spread over the group's lanes: lanes 0-11 the gradient components (site
+    // sub / 3 + 1, component sub % 3), lanes 12-14 the potentials of sites 2-4
+    if (i < N) {
+        float v = 0.f;
 #pragma unroll
-        for (int k = 1; k <= 4; k++) {
+        for (int kk = 1; kk <= 4; kk++)
 #pragma unroll
-            for (int c = 0; c < 3; c++) dR[3 * ((k - 1) * N + i) + c] += (double)gi[k][c];
-            if (k != 1) Fb[(k - 1) * N + i].w += (double)pi[k];
+            for (int cc = 0; cc < 3; cc++)
+                if ((kk - 1) * 3 + cc == sub) v = gi[kk][cc];
+#pragma unroll
+        for (int kk = 2; kk <= 4; kk++)
+            if (10 + kk == sub) v = pi[kk];
+        if (sub < 12) {
+            const int k = sub / 3 + 1, c = sub % 3;
+            kp.dR[3 * ((size_t)b * kp.S + (size_t)(k - 1) * N + i) + c] += (double)v;
+        } else if (sub < 15) {
+            kp.F[(size_t)b * kp.S + (size_t)(sub - 11) * N + i].w += (double)v;
         }
     }
     block_reduce_add_f<14, 128>(av, kp.acc + (size_t)b * NACC);

@@ -14,11 +14,11 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def case(pkg, nw=32, P=2, K=6, eps=0.0, seed=31):
+def case(pkg, nw=32, P=2, K=6, eps=0.0, seed=31, nmax=7):
     c = pkg.waterbox.make_config("ttm3f_512x32", nw=nw, P=P, seed=seed)
     L = c["params"]["box"][0]
     rc = min(9.0, L / 2 - 0.01)
-    p = dict(c["params"], rc=rc, rc1=0.8 * rc, alpha=3.2 / rc, nmax=7, polar_maxiter=K, polar_eps=eps,
+    p = dict(c["params"], rc=rc, rc1=0.8 * rc, alpha=3.2 / rc, nmax=nmax, polar_maxiter=K, polar_eps=eps,
              guess_initdip=0)
     return c, p
 
@@ -100,14 +100,15 @@ def rms_rel(a, b):
     return float(np.sqrt(((a - b) ** 2).mean() / (b ** 2).mean()))
 
 
-@pytest.mark.parametrize("eps", [0.0, 1e-4])
-def test_mixed_backward_matches_fp64(pkg, engine_lib, eps):
+@pytest.mark.parametrize("eps,nmax", [(0.0, 7), (1e-4, 7), (0.0, 16)])
+def test_mixed_backward_matches_fp64(pkg, engine_lib, eps, nmax):
     """The mixed engine's forward + backward (FP32 pair, table and reciprocal products, FP64 sums)
     against the FP64 engine's on the same coordinates and parameters: the position gradient
     within the mixed force budget (1e-4 RMS relative) and every dE/dtheta within 1e-4 of the
     largest. eps = 0 runs a fixed 6 iterations; eps = 1e-4 stops at a loose tolerance, where
-    the backward differentiates the truncated iteration (both engines stop at the same count)."""
-    c, p = case(pkg, nw=64, P=2, K=6 if eps == 0.0 else 40, eps=eps)
+    the backward differentiates the truncated iteration (both engines stop at the same count);
+    |n| <= 16 takes the wider register-row field pass and kz columns of the reverse sweep."""
+    c, p = case(pkg, nw=64, P=2, K=6 if eps == 0.0 else 40, eps=eps, nmax=nmax)
     ebar = np.array([1.0, 0.5])
     res = []
     for prec in (pkg.engine.PIMD_FP64, pkg.engine.PIMD_MIXED):
