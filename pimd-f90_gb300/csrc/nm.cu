@@ -675,19 +675,29 @@ __global__ void k_md_estimators(int P, int natoms, double volume, double omegan,
     out[11] = s_post ? *s_post : 1.0;
 }
 
+// one warp: lane-strided bead sums, then a fixed butterfly (FP64 is a narrow pipe on this part:
+// a serial loop of dependent adds would take microseconds at the end of every step)
 __global__ void k_md_sum(int P, const double *Upott, const double *virialt, const double *virialct, const double *uk,
                          double *out4) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
     double u = 0, v = 0, vc = 0;
-    for (int k = 0; k < P; k++) {
+    for (int k = threadIdx.x; k < P; k += 32) {
         u += Upott[k];
         v += virialt[k];
         vc += virialct[k];
     }
-    out4[0] = u;
-    out4[1] = v;
-    out4[2] = vc / P;
-    out4[3] = *uk;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        u += __shfl_xor_sync(0xffffffffu, u, o);
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+        vc += __shfl_xor_sync(0xffffffffu, vc, o);
+    }
+    if (threadIdx.x == 0) {
+        out4[0] = u;
+        out4[1] = v;
+        out4[2] = vc / P;
+        out4[3] = *uk;
+    }
 }
 
 // ---------------------------------------------------------------------------------------
