@@ -1162,16 +1162,23 @@ void launch_ewald_tables(Engine &E) {
 // forward's rotated form (-Im, Re) of sum_s (k.mu_s) e^{ik.r_s}; beads with bacc[ACC_CONV] != 0
 // are skipped. Mixed engine: also the FP32 field weights of Sout (Wf), which the field pass
 // of adj_dipole_field reads, so the last structure factor before it must be its own.
-// dipf32: the same dipoles as FP32 float4 [P][S] (mixed engine), read by the register-tiled pass.
+// dipf32: the same dipoles as FP32 float4 [P][S] (mixed engine), read by the forward's passes.
 void adj_structure_factor(Engine &E, const double *dipbuf, const float4 *dipf32, double2 *Sout, double *bacc) {
     const KP keep = E.kp;
     E.kp.dip = const_cast<double *>(dipbuf);
     E.kp.Sm = Sout;
     E.kp.acc = bacc;
     E.kp.dd_async = 0;
-    if (E.precision == PIMD_PREC_MIXED && dipf32 && E.sf_tiled && E.sf_nkg_max * SF_RT <= SF_MAXT) {
+    if (E.precision == PIMD_PREC_MIXED && dipf32) {
+        // the forward's own passes on the FP32 copy: tensor cores (the X operand cached by this
+        // force call's first iteration), else the register-tiled FP32 pass
         E.kp.dipf = const_cast<float4 *>(dipf32);
-        run_sfac_f<OP_MU>(E, E.kp.fd, E.kp.ld - E.kp.fd, 1);
+        if (!launch_sfac_tc(E, OP_MU, E.kp.fd, E.kp.ld - E.kp.fd, 1)) {
+            if (E.sf_tiled && E.sf_nkg_max * SF_RT <= SF_MAXT)
+                run_sfac_f<OP_MU>(E, E.kp.fd, E.kp.ld - E.kp.fd, 1);
+            else
+                run_spass_t<OP_MU, float>(E, E.kp.fd, E.kp.ld - E.kp.fd, 1);
+        }
     } else if (E.precision == PIMD_PREC_MIXED) {
         run_spass_t<OP_MU, float>(E, E.kp.fd, E.kp.ld - E.kp.fd, 1);
     } else {
