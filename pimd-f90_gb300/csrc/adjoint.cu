@@ -161,15 +161,44 @@ __global__ void __launch_bounds__(128) k_adj_u(KP kp, int k, const int *iters, c
     block_reduce_add<1, 128>(th, thacc + PIMD_TH_POLAR_M);
 }
 
-// second half: g_{k-1} = (1-w) g_k + w (D u + f u), D u accumulated in Dr by the field kernels
+// second half: g_{k-1} = (1-w) g_k + w (D u + f u), D u accumulated in Dr by the field kernels.
+// Mixed engine with the tensor-core sweep (Erec given): the reciprocal part of D u is in Erec
+// (kp.Fx, x y z), and dDg (kp.dR) holds the two dipole-force passes of the reciprocal bilinear
+// term, grad -= w_b dDg at the dipole sites.
 __global__ void __launch_bounds__(128) k_adj_g(KP kp, int k, const int *iters, double *g, const double *u,
-                                               const double *Dr, double omega) {
+                                               const double *Dr, double omega, const double4_32a *Erec,
+                                               const double *dDg, const double *bw, double *grad) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y, nd = kp.ld - kp.fd;
     if (i >= nd || k > iters[b]) return;
     const size_t gs = (size_t)b * kp.S + kp.fd + i;
+    double er[3] = {0.0, 0.0, 0.0};
+    if (Erec) {
+        const double4_32a x = Erec[gs];
+        er[0] = x.x, er[1] = x.y, er[2] = x.z;
+    }
     for (int c = 0; c < 3; c++) {
         double &gi = g[((size_t)b * nd + i) * 3 + c];
-        gi = (1.0 - omega) * gi + omega * (Dr[3 * gs + c] + kp.factor * u[3 * gs + c]);
+        gi = (1.0 - omega) * gi + omega * ((Dr[3 * gs + c] + er[c]) + kp.factor * u[3 * gs + c]);
+    }
+    if (dDg)
+        for (int c = 0; c < 3; c++) grad[3 * gs + c] -= bw[b] * dDg[3 * gs + c];
+}
+
+// Weight slots of the tensor-core sweep (FP32 4 pi A_k / V conj(S) in the field passes' form):
+// MODE 0: slot 0 <- slot 1 (the structure factor just formed), slot 1 <- 0; MODE 1: slot 0 <-
+// the weights of Sm (the forward's structure factor of mu_{k-1}, from the tape), slot 1 stays 0.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_adj_wslots(KP kp, const double2 *Sm) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (k >= kp.nk) return;
+    float2 *w0 = kp.Wf + (size_t)b * 2 * kp.nk, *w1 = w0 + kp.nk;
+    if (MODE == 0) {
+        w0[k] = w1[k];
+        w1[k] = make_float2(0.f, 0.f);
+    } else {
+        const double w = kp.kinfo[k].w;
+        const double2 a = Sm[(size_t)b * kp.nk + k];
+        w0[k] = make_float2((float)(w * a.x), (float)(-w * a.y));
     }
 }
 
@@ -695,6 +724,10 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
     for (int i = 0; i < 5; i++) pf.v[i] = E.polfac[i];
     const double omega = kp.polar_sor;
     const dim3 gw((unsigned)((kp.N * 32 + 127) / 128), (unsigned)P);  // a warp per molecule
+    // the mixed sweep's reciprocal passes on the tensor cores when the forward has them (the
+    // structure factor, the field pass and the force pass's dipole half)
+    const bool tcs = mixed && kp.model == 3 && E.tc_ready && E.sf_tc && E.tf_ready && E.ff_tc && E.tf_qd_ready &&
+                     kp.Fx && kp.ld - kp.fd == kp.N;
     k_adj_init<<<gd, 128, 0, st>>>(kp, ebar, g, nu);
     for (int k = kmax; k >= 1; k--) {
         k_adj_u<<<gd, 128, 0, st>>>(kp, k, iters, E.d_tape, g, u, v, nu, bacc, bw, thacc, omega, mixed ? uf : nullptr,
@@ -718,13 +751,39 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
         // S(v) = S(mu_{k-1}) is on the tape (the forward's iteration k formed it)
         const double2 *Smv = E.d_tapeS + (size_t)(k - 1) * P * kp.nk;
         adj_structure_factor(E, u, mixed ? uf : nullptr, Smu, bacc);
-        adj_dipole_field(E, Smu, bacc, Dr);
-        k_adj_g<<<gd, 128, 0, st>>>(kp, k, iters, g, u, Dr, omega);
+        if (tcs) {
+            // tensor-core sweep: the field of u (TF_Q on the weights of S_u moved to slot 0) into
+            // Fx, then the reciprocal bilinear term as the dipole force of v in the field of u
+            // plus that of u in the field of v (TF_DG, slot 1 zero) into dR:
+            // d/dx [u^T D_rec v] = -(dipole force of u in E_v + dipole force of v in E_u)
+            const dim3 gk((unsigned)((kp.nk + 255) / 256), (unsigned)P);
+            k_adj_wslots<0><<<gk, 256, 0, st>>>(kp, nullptr);
+            KP kq = kp;
+            kq.acc = bacc;
+            kq.dd_async = 0;
+            kq.fx_mode = 1;
+            const KP keep = E.kp;
+            E.kp = kq;
+            launch_adj_field_tc(E);
+            cudaMemsetAsync(kp.dR, 0, sizeof(double) * sv, st);
+            E.kp.fx_mode = 0;
+            E.kp.dipf = vf;
+            launch_adj_dforce_tc(E);
+            k_adj_wslots<1><<<gk, 256, 0, st>>>(kp, Smv);
+            E.kp.dipf = uf;
+            launch_adj_dforce_tc(E);
+            E.kp = keep;
+            E.nlaunch += 2;
+            k_adj_g<<<gd, 128, 0, st>>>(kp, k, iters, g, u, Dr, omega, kp.Fx, kp.dR, bw, grad);
+        } else {
+            adj_dipole_field(E, Smu, bacc, Dr);
+            k_adj_g<<<gd, 128, 0, st>>>(kp, k, iters, g, u, Dr, omega, nullptr, nullptr, bw, grad);
+        }
         if (mixed)
             k_adj_ddbil_m<<<gw, 128, 0, st>>>(kp, pf.v[4] * pf.v[4], uf, vf, bw, grad, thacc);
         else
             k_adj_ddbil<<<gp, 128, 0, st>>>(kp, pf, u, v, bw, grad, thacc);
-        adj_rec(E, 0, u, v, Smu, Smv, bw, grad, nullptr);
+        if (!tcs) adj_rec(E, 0, u, v, Smu, Smv, bw, grad, nullptr);
     }
     k_adj_final<<<gd, 128, 0, st>>>(kp, g, nu, thacc);
     // charge-field adjoint nu: real-space pairs, reciprocal, intramolecular; vdW; Uelec d/da_cc

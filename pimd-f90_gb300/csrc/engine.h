@@ -435,6 +435,8 @@ int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv);
 // tensor-core field passes (ewald_tc.cu): mode F_D (dipole field, SOR update, convergence test)
 // or F_Q (charge field and potential into F); 1 when launched
 int launch_field_tc(Engine &E, int mode, int s0, int s1);
+int launch_adj_field_tc(Engine &E);
+int launch_adj_dforce_tc(Engine &E);
 bool field_pdl_ok(const Engine &E);
 int launch_field_qd_tc(Engine &E, int s0, int s1);  // ewald_std_qd force pass on the tensor cores
 // launchers (spc.cu): q-SPC/Fw and SPC/F

@@ -1403,6 +1403,19 @@ int launch_field_tc(Engine &E, int mode, int s0, int s1) {
     return 1;
 }
 
+// The differentiation form's reverse sweep on the mixed engine: the reciprocal field at the
+// dipole sites from the charge weight slot (TF_Q: into kp.Fx with fx_mode 1), and the dipole
+// force of kp.dipf from the two weight slots (TF_DG: into kp.dR, or kp.Fx with fx_mode 2), at
+// [fd, ld). 1 when launched, else 0.
+int launch_adj_field_tc(Engine &E) {
+    if (!E.tf_qd_ready || E.kp.ld <= E.kp.fd) return 0;
+    return launch_field_tc(E, TF_Q, E.kp.fd, E.kp.ld);
+}
+int launch_adj_dforce_tc(Engine &E) {
+    if (!E.tf_qd_ready || E.kp.ld <= E.kp.fd) return 0;
+    return launch_field_tc(E, TF_DG, E.kp.fd, E.kp.ld);
+}
+
 // ewald_std_qd's force pass (k_field_f<F_QD> + k_field_finish<F_QD>) as two tensor-core passes:
 // the charge force -q E and potential from the dipole structure factor at [s0, s1), then the
 // dipole force at the dipole sites from the total structure factor. 1 when launched, else 0.

@@ -107,12 +107,16 @@ def test_mixed_backward_matches_fp64(pkg, engine_lib, eps, nmax):
     within the mixed force budget (1e-4 RMS relative) and every dE/dtheta within 1e-4 of the
     largest. eps = 0 runs a fixed 6 iterations; eps = 1e-4 stops at a loose tolerance, where
     the backward differentiates the truncated iteration (both engines stop at the same count);
-    |n| <= 16 takes the wider register-row field pass and kz columns of the reverse sweep."""
+    |n| <= 16 takes more field-pass columns. The mixed sweep runs the forward's tensor-core
+    structure factor, field pass and dipole-force pass (asserted)."""
     c, p = case(pkg, nw=64, P=2, K=6 if eps == 0.0 else 40, eps=eps, nmax=nmax)
     ebar = np.array([1.0, 0.5])
     res = []
     for prec in (pkg.engine.PIMD_FP64, pkg.engine.PIMD_MIXED):
         eng = pkg.ForceEngine(p, precision=prec)
+        if prec == pkg.engine.PIMD_MIXED:  # the sweep's reciprocal passes run on the tensor cores
+            t = eng.tuning()
+            assert t["sf_tc"] == 1 and t["ff_tc"] == 1 and t["qd_tc"] == 1
         U = eng.pot_forward(c["RRt"], c["RRc"])
         n = [eng.energies(k)["niter"] for k in range(2)]
         g, dth = eng.pot_backward(ebar)
