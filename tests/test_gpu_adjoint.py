@@ -129,6 +129,26 @@ def test_mixed_backward_matches_fp64(pkg, engine_lib, eps, nmax):
     assert np.abs(thm - th64).max() < 1e-4 * np.abs(th64).max()
 
 
+def test_mixed_backward_fp32_pipe_sweep(pkg, engine_lib):
+    """The mixed sweep without the tensor-core passes (sf_tc = ff_tc = 0: the register-tiled
+    structure factor and field pass, and the site-parallel reciprocal bilinear kernel) against the
+    FP64 backward, same tolerances."""
+    c, p = case(pkg, nw=64, P=2, K=6, eps=0.0)
+    ebar = np.array([1.0, 0.5])
+    eng = pkg.ForceEngine(p)
+    eng.pot_forward(c["RRt"], c["RRc"])
+    g64, th64 = eng.pot_backward(ebar)
+    eng.close()
+    eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_MIXED)
+    t = eng.set_tuning(sf_tc=0, ff_tc=0)
+    assert t["sf_tc"] == 0 and t["ff_tc"] == 0
+    eng.pot_forward(c["RRt"], c["RRc"])
+    gm, thm = eng.pot_backward(ebar)
+    eng.close()
+    assert rms_rel(gm, g64) < 1e-4
+    assert np.abs(thm - th64).max() < 1e-4 * np.abs(th64).max()
+
+
 def test_mixed_backward_equals_mixed_forces_when_converged(pkg, engine_lib):
     """At converged dipoles (1e-10) and rc1 = rc the mixed backward's position gradient equals the
     mixed engine's own analytic forces within the mixed budget."""
