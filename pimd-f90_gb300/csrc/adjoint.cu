@@ -673,9 +673,9 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
     KP &kp = E.kp;
     const size_t P = kp.P, S = kp.S, nd = kp.ld - kp.fd, sv = 3 * P * S;
     const bool mixed = E.precision == PIMD_MIXED;
-    // scratch: g, u, v, Dr, grad, nu (site vectors), phin, Smu, Smv, Snu, bacc, bw, ebar, ones,
-    // thacc, dRRt, FP32 u and v per molecule (mixed engine), iters
-    const size_t nbytes = sizeof(double) * (3 * P * nd + 5 * sv + P * S + 6 * P * kp.nk + P * NACC + 3 * P + PIMD_NTHETA +
+    // scratch: g, u, v, Dr, grad, nu (site vectors), phin, Smu, Snu, bacc, bw, ebar, ones, thacc,
+    // dRRt, FP32 u and v per site (mixed engine), iters
+    const size_t nbytes = sizeof(double) * (3 * P * nd + 5 * sv + P * S + 4 * P * kp.nk + P * NACC + 3 * P + PIMD_NTHETA +
                                             P * kp.natoms * 3) + sizeof(float4) * 2 * P * S + sizeof(int) * P + 256;
     if (E.adj_bytes < nbytes) {
         if (E.d_adj) cudaFree(E.d_adj);
@@ -689,7 +689,7 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
     double *g = E.d_adj, *u = g + 3 * P * nd, *v = u + sv, *Dr = v + sv, *grad = Dr + sv, *nu = grad + sv;
     double *phin = nu + sv;
     const uintptr_t sa = (reinterpret_cast<uintptr_t>(phin + P * S) + 15) & ~uintptr_t(15);  // 16-byte rows
-    double2 *Smu = reinterpret_cast<double2 *>(sa), *Snu = Smu + 2 * P * kp.nk;
+    double2 *Smu = reinterpret_cast<double2 *>(sa), *Snu = Smu + P * kp.nk;
     double *bacc = reinterpret_cast<double *>(Snu + P * kp.nk), *bw = bacc + P * NACC, *ebar = bw + P, *ones = ebar + P;
     double *thacc = ones + P, *dR = thacc + PIMD_NTHETA;
     const uintptr_t ua = (reinterpret_cast<uintptr_t>(dR + P * kp.natoms * 3) + 15) & ~uintptr_t(15);  // 16-byte rows
