@@ -366,8 +366,8 @@ class ForceEngine:
         """One PIMD_VV step on host arrays (updated in place); returns (Upot, virial, virialc, uk), RRc."""
         for a in (RRt, PPt, dRRt):
             assert a.dtype == np.float64 and a.flags.c_contiguous
-        RRc = np.zeros((self.natoms, 3))
-        out = np.zeros(4)
+        RRc = np.empty((self.natoms, 3))  # both written by the call
+        out = np.empty(4)
         x1 = _f64(xi1) if xi1 is not None else None
         x2 = _f64(xi2) if xi2 is not None else None
         rc = load().pimd_md_step(self.h, ctypes.byref(mp), _p(RRt), _p(PPt), _p(dRRt), _p(RRc), _p(x1), _p(x2),
