@@ -14,13 +14,15 @@
 // nu then enters like a dipole set in the charge-field derivative (real, intramolecular and
 // reciprocal), and its potential at the charge sites joins the charge potential in the chain
 // through the DMS charges (grdq) and the M-site construction. Pair geometry is recomputed from
-// the site positions, never stored. The forward records mu_0..mu_K (the tape) and the
-// charge-only potential; nothing else is kept beyond the forward's own buffers.
-// On the mixed engine the reverse sweep's operators are the forward's FP32 ones: D_real from
-// its per-entry smear scalars with alpha g_k in the molecule records, the reciprocal passes from
-// its FP32 tables, and the bilinear real-space term as a full-list FP32 gather (no atomics); the
-// sums stay FP64 as in the forward. The terms outside the sweep (charge-field pairs, monomer
-// chain) run once, in FP64, on the forward's FP64 sites.
+// the site positions, never stored. The forward records mu_0..mu_K and the structure factor of
+// each iteration's dipoles (the tape) and the charge-only potential; nothing else is kept beyond
+// the forward's own buffers.
+// On the mixed engine the reverse sweep's operators are the forward's: D_real from its per-entry
+// smear scalars with alpha g_k in the molecule records; the reciprocal passes on the tensor cores
+// (structure factor, charge-field pass on moved weights, and the force pass's dipole half for the
+// bilinear term), or on the FP32 pipe without them; the bilinear real-space term and the
+// charge-field pair terms as full-list FP32 gathers (no atomics); sums in FP64 as in the forward.
+// The monomer chain runs once, in FP64, on the forward's FP64 sites.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
