@@ -356,6 +356,21 @@ struct NMArgs {
     int nm_ke;                          // calc_uk in normal-mode space (setNMfreq != 0, P > 1)
     int nodrift;                        // k_md_pre without the drift (contracted MD: the inner steps drift)
 };
+// one replica of a batch for the batched MD-step kernels: its arguments and state pointers
+struct NMBatchRep {
+    NMArgs a;
+    double *RRt, *PPt, *dRRt, *RRc, *uk;
+};
+struct NMSumRep {  // its step outputs (k_md_sum's inputs)
+    int P;
+    const double *Upott, *virialt, *virialct, *uk;
+    double *out4;
+};
+// the batched phases of every replica's MD step (phase 0 before the force call, 1 after); with
+// nblk = 0 only the shared-memory opt-in (call once outside any stream capture)
+void nm_launch_md_batch(int phase, bool fast, int nblk, size_t smem, cudaStream_t st, const NMBatchRep *reps,
+                        const int2 *blkmap);
+__global__ void k_md_sum_batch(const NMSumRep *reps);
 NMArgs nm_step_args(Engine &E, const pimd_md_params *mp, const double *xi1);
 void nm_launch_evolve(const NMArgs &a, cudaStream_t st, double *RRt, double *PPt);
 void nm_launch_ring_sums(const NMArgs &a, cudaStream_t st, const double *RRt, const double *PPt, double *sums);
@@ -370,6 +385,7 @@ void nm_launch_shape(int P, int natoms, int *threads, int *blocks, size_t *smem)
 void nm_smem_optin(int P);
 void nm_extend_A(std::vector<double> &A, int P, const std::vector<double> &omegalist);
 void nm_fast_args(NMArgs &a);
+size_t nm_fast_smem(int P, int G);
 void nm_launch_md_pre(const NMArgs &a, cudaStream_t st, double *RRt, double *PPt, const double *dRRt, double *RRc);
 void nm_launch_md_post(const NMArgs &a, cudaStream_t st, double *PPt, const double *dRRt, double *uk);
 void nm_pair_copy(const std::vector<double> &C, std::vector<double> &out);  // C then its FP32 pairs

@@ -4,10 +4,11 @@
 // batch holds any number of replicas, each with its own molecule count, bead count and
 // temperature. Replicas that share a box (same molecule count, box and cutoff) are stacked on
 // the bead axis of one force-engine context, so every force kernel covers all beads of all
-// those replicas in one launch; the normal-mode, thermostat and kick kernels run per replica
-// (own P, own NM matrices and Langevin coefficients at its own temperature). A step of the whole
-// batch is one CUDA graph: one branch per box group on its own stream, each with its dipole loop
-// as a conditional while node, joined at the end.
+// those replicas in one launch; the normal-mode, thermostat and kick work of all replicas (own P,
+// own NM matrices and Langevin coefficients at its own temperature) runs in one launch per phase
+// of the step, each block on one replica's atoms. A step of the whole batch is one CUDA graph:
+// the integrator up to the force call, one branch per box group on its own stream (each with its
+// dipole loop as a conditional while node), then the integrator after it and the step outputs.
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -37,7 +38,7 @@ struct BatchGroup {
     pimd_ctx *ctx = nullptr;
     std::vector<int> reps;
     int Ptot = 0, natoms = 0;
-    double *RRt = nullptr, *PPt = nullptr, *dRRt = nullptr, *RRc = nullptr, *uk = nullptr;
+    double *RRt = nullptr, *PPt = nullptr, *dRRt = nullptr, *RRc = nullptr;
 };
 
 }  // namespace
@@ -51,7 +52,15 @@ struct pimd_batch {
     cudaEvent_t ev_fork = nullptr;
     std::vector<cudaEvent_t> ev_join;
     cudaGraphExec_t gexec = nullptr;
-    double *d_out4 = nullptr;
+    double *d_out4 = nullptr, *d_uk = nullptr;
+    // the integrator of every replica in one launch per phase: per-replica arguments, the block map
+    // (replica, block of its own grid) and the step-output table
+    NMBatchRep *d_reps = nullptr;
+    int2 *d_blkmap = nullptr;
+    NMSumRep *d_sums = nullptr;
+    int nblk = 0;
+    size_t smem = 0;
+    bool fast = false;
     std::vector<void *> allocs;
     int t = 0;
     std::string err;
@@ -97,37 +106,15 @@ static NMArgs replica_args(const pimd_batch *bt, const BatchReplica &r, const En
     return a;
 }
 
-// One PIMD_VV step of every replica of a box group, on the group context's stream.
-static int enqueue_group_step(pimd_batch *bt, BatchGroup &g) {
-    Engine &E = g.ctx->E;
-    const size_t na3 = (size_t)g.natoms * 3;
-    for (int ri : g.reps) {
-        const BatchReplica &r = bt->reps[ri];
-        NMArgs a = replica_args(bt, r, E);
-        a.phase = 0;
-        nm_launch_md_pre(a, E.stream, g.RRt + r.bead0 * na3, g.PPt + r.bead0 * na3, g.dRRt + r.bead0 * na3,
-                         g.RRc + r.local * na3);
-        ++E.nlaunch;
-    }
-    double *d = E.d_out;  // Upott, virialt, virialct of all beads of the group
-    int rc = run_forces(E, 0, 0, d, d + g.Ptot, d + 2 * g.Ptot, nullptr);
-    if (rc) return bfail(bt, rc, E.last_error);
-    cudaMemsetAsync(g.uk, 0, sizeof(double) * g.reps.size(), E.stream);
-    for (int ri : g.reps) {
-        const BatchReplica &r = bt->reps[ri];
-        NMArgs a = replica_args(bt, r, E);
-        a.phase = 1;
-        nm_launch_md_post(a, E.stream, g.PPt + r.bead0 * na3, g.dRRt + r.bead0 * na3, g.uk + r.local);
-        k_md_sum<<<1, 32, 0, E.stream>>>(r.P, d + r.bead0, d + g.Ptot + r.bead0, d + 2 * g.Ptot + r.bead0, g.uk + r.local,
-                                         bt->d_out4 + 4 * (size_t)ri);
-        E.nlaunch += 2;
-    }
-    return bcuda(bt, cudaGetLastError(), "batch step");
-}
-
+// One PIMD_VV step of every replica (MD.f90:35-110): the integrator of all replicas up to the
+// force call in one launch, the force call of each box group on the group context's stream (one
+// graph branch per group, each with its dipole loop as a conditional node), then the integrator
+// after it and the step outputs of all replicas, one launch each.
 static int capture_batch(pimd_batch *bt) {
     cudaError_t e = cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return bcuda(bt, e, "batch capture");
+    cudaMemsetAsync(bt->d_uk, 0, sizeof(double) * bt->reps.size(), bt->stream);
+    nm_launch_md_batch(0, bt->fast, bt->nblk, bt->smem, bt->stream, bt->d_reps, bt->d_blkmap);
     cudaEventRecord(bt->ev_fork, bt->stream);
     int rc = PIMD_OK;
     for (size_t gi = 0; gi < bt->groups.size() && !rc; gi++) {
@@ -138,12 +125,16 @@ static int capture_batch(pimd_batch *bt) {
         const bool timers_on = E.timers.on;
         E.timers.on = false;
         E.capturing = true;
-        rc = enqueue_group_step(bt, g);
+        double *d = E.d_out;  // Upott, virialt, virialct of all beads of the group
+        rc = run_forces(E, 0, 0, d, d + g.Ptot, d + 2 * g.Ptot, nullptr);
+        if (rc) bt->err = E.last_error;
         E.capturing = false;
         E.timers.on = timers_on;
         cudaEventRecord(bt->ev_join[gi], E.stream);
         cudaStreamWaitEvent(bt->stream, bt->ev_join[gi], 0);
     }
+    nm_launch_md_batch(1, bt->fast, bt->nblk, bt->smem, bt->stream, bt->d_reps, bt->d_blkmap);
+    k_md_sum_batch<<<(unsigned)bt->reps.size(), 32, 0, bt->stream>>>(bt->d_sums);
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(bt->stream, &graph);
     if (rc) {
@@ -205,6 +196,7 @@ int pimd_batch_create(pimd_batch **out, const pimd_params *common, const pimd_re
     if (!rc) rc = bcuda(bt, cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking), "stream");
     if (!rc) rc = bcuda(bt, cudaEventCreateWithFlags(&bt->ev_fork, cudaEventDisableTiming), "event");
     if (!rc) rc = balloc(bt, &bt->d_out4, 4 * (size_t)nrep);
+    if (!rc) rc = balloc(bt, &bt->d_uk, (size_t)nrep);
     for (size_t gi = 0; gi < bt->groups.size() && !rc; gi++) {
         BatchGroup &g = bt->groups[gi];
         const pimd_replica &r0 = reps[g.reps[0]];
@@ -229,7 +221,7 @@ int pimd_batch_create(pimd_batch **out, const pimd_params *common, const pimd_re
         g.ctx->check_every = 0;
         const size_t n = (size_t)g.Ptot * g.natoms * 3;
         if ((rc = balloc(bt, &g.RRt, n)) || (rc = balloc(bt, &g.PPt, n)) || (rc = balloc(bt, &g.dRRt, n)) ||
-            (rc = balloc(bt, &g.RRc, g.reps.size() * (size_t)g.natoms * 3)) || (rc = balloc(bt, &g.uk, g.reps.size())))
+            (rc = balloc(bt, &g.RRc, g.reps.size() * (size_t)g.natoms * 3)))
             break;
         Engine &E = g.ctx->E;
         E.kp.RRt = g.RRt;
@@ -264,6 +256,40 @@ int pimd_batch_create(pimd_batch **out, const pimd_params *common, const pimd_re
         cudaMemcpy(r.d_C, CP.data(), sizeof(double) * CP.size(), cudaMemcpyHostToDevice);
         nm_smem_optin(r.P);
         cudaMemcpy(r.d_A, A.data(), sizeof(double) * A.size(), cudaMemcpyHostToDevice);
+    }
+    // the tables of the batched integrator launches (k_md_batch, k_md_sum_batch)
+    if (!rc) {
+        std::vector<NMBatchRep> hr(bt->reps.size());
+        std::vector<NMSumRep> hs(bt->reps.size());
+        std::vector<int2> map;
+        for (size_t i = 0; i < bt->reps.size(); i++) {
+            const BatchReplica &r = bt->reps[i];
+            BatchGroup &g = bt->groups[r.group];
+            Engine &E = g.ctx->E;
+            const size_t na3 = (size_t)r.natoms * 3;
+            NMArgs a = replica_args(bt, r, E);
+            if (a.fast) nm_fast_args(a);
+            bt->fast = a.fast != 0;
+            hr[i] = NMBatchRep{a, g.RRt + r.bead0 * na3, g.PPt + r.bead0 * na3, g.dRRt + r.bead0 * na3, g.RRc + r.local * na3,
+                               bt->d_uk + i};
+            double *d = E.d_out;
+            hs[i] = NMSumRep{r.P, d + r.bead0, d + g.Ptot + r.bead0, d + 2 * g.Ptot + r.bead0, bt->d_uk + i, bt->d_out4 + 4 * i};
+            const int G = std::max(1, 256 / (3 * r.P));  // atoms per block of 256 threads
+            const int nb = (r.natoms + G - 1) / G;
+            for (int k = 0; k < nb; k++) map.push_back(make_int2((int)i, k));
+            const size_t sm = a.fast ? nm_fast_smem(r.P, G) : sizeof(double) * ((size_t)(r.P + 1) * r.P + (size_t)G * 9 * r.P);
+            bt->smem = std::max(bt->smem, sm);
+        }
+        bt->nblk = (int)map.size();
+        if ((rc = balloc(bt, &bt->d_reps, hr.size())) || (rc = balloc(bt, &bt->d_blkmap, map.size())) ||
+            (rc = balloc(bt, &bt->d_sums, hs.size())))
+            ;
+        else {
+            cudaMemcpy(bt->d_reps, hr.data(), sizeof(NMBatchRep) * hr.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(bt->d_blkmap, map.data(), sizeof(int2) * map.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(bt->d_sums, hs.data(), sizeof(NMSumRep) * hs.size(), cudaMemcpyHostToDevice);
+            nm_launch_md_batch(0, bt->fast, 0, bt->smem, bt->stream, nullptr, nullptr);  // the opt-in
+        }
     }
     if (!rc) rc = bcuda(bt, cudaDeviceSynchronize(), "batch set-up");
     if (rc) {

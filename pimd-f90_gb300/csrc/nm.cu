@@ -307,10 +307,12 @@ void nm_fast_args(NMArgs &a) {
     a.boxif = (float)a.boxi0;
 }
 
-__global__ void k_md_pre_fast(NMArgs a, double *RRt, double *PPt, const double *dRRt, double *RRc) {
+// The MD-step kernels' bodies take the block index blk (of the replica's own grid), so that a
+// replica batch runs every replica's blocks in one launch (k_md_batch).
+PIMD_D void md_pre_fast_body(const NMArgs &a, int blk, double *RRt, double *PPt, const double *dRRt, double *RRc) {
     const int P = a.P, G = blockDim.x / (3 * P);
     const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
-    const int atom = blockIdx.x * G + g;
+    const int atom = blk * G + g;
     float2 *Cf, *kf, *vx, *vp;
     float *nsh;
     nm_fast_layout(P, min(g, G - 1), Cf, kf, vx, vp, nsh);
@@ -374,10 +376,10 @@ __global__ void k_md_pre_fast(NMArgs a, double *RRt, double *PPt, const double *
     }
 }
 
-__global__ void k_md_post_fast(NMArgs a, double *PPt, const double *dRRt, double *uk) {
+PIMD_D void md_post_fast_body(const NMArgs &a, int blk, double *PPt, const double *dRRt, double *uk) {
     const int P = a.P, G = blockDim.x / (3 * P);
     const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
-    const int atom = blockIdx.x * G + g;
+    const int atom = blk * G + g;
     float2 *Cf, *kf, *vx, *vp;
     float *nsh;
     nm_fast_layout(P, min(g, G - 1), Cf, kf, vx, vp, nsh);
@@ -408,11 +410,11 @@ __global__ void k_md_post_fast(NMArgs a, double *PPt, const double *dRRt, double
 
 // MD.f90:40-73 up to the force call: Langevin, half kick, EvolveRing (or free flight for
 // P = 1), centroid and the centroid-following PBC shift (main_stuff.f90:107-125).
-__global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt, double *RRc) {
+PIMD_D void md_pre_body(const NMArgs &a, int blk, double *RRt, double *PPt, const double *dRRt, double *RRc) {
     extern __shared__ double sh[];
     const int P = a.P, G = blockDim.x / (3 * P);
     const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
-    const int atom = blockIdx.x * G + g;
+    const int atom = blk * G + g;
     double *Cs = sh;
     double *x = Cs + nm_ld(P) * P + g * 9 * P, *p = x + 3 * P, *tr = p + 3 * P;
     nm_load_C(Cs, a.C, P);
@@ -474,11 +476,11 @@ __global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt,
 }
 
 // MD.f90:94-101: half kick with the new gradient, Langevin, kinetic energy (calc_uk)
-__global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk) {
+PIMD_D void md_post_body(const NMArgs &a, int blk, double *PPt, const double *dRRt, double *uk) {
     extern __shared__ double sh[];
     const int P = a.P, G = blockDim.x / (3 * P);
     const int g = threadIdx.x / (3 * P), r = threadIdx.x % (3 * P), j = r / 3, c = r % 3;
-    const int atom = blockIdx.x * G + g;
+    const int atom = blk * G + g;
     double *Cs = sh;
     double *p = Cs + nm_ld(P) * P + g * 9 * P, *tr = p + 3 * P;
     nm_load_C(Cs, a.C, P);
@@ -508,6 +510,65 @@ __global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk)
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += wke[w];
         atomicAdd(uk, 0.5 * t);
     }
+}
+
+__global__ void k_md_pre_fast(NMArgs a, double *RRt, double *PPt, const double *dRRt, double *RRc) {
+    md_pre_fast_body(a, blockIdx.x, RRt, PPt, dRRt, RRc);
+}
+__global__ void k_md_post_fast(NMArgs a, double *PPt, const double *dRRt, double *uk) {
+    md_post_fast_body(a, blockIdx.x, PPt, dRRt, uk);
+}
+__global__ void k_md_pre(NMArgs a, double *RRt, double *PPt, const double *dRRt, double *RRc) {
+    md_pre_body(a, blockIdx.x, RRt, PPt, dRRt, RRc);
+}
+__global__ void k_md_post(NMArgs a, double *PPt, const double *dRRt, double *uk) {
+    md_post_body(a, blockIdx.x, PPt, dRRt, uk);
+}
+
+// A replica batch's MD-step phase (PHASE 0: up to the force call, 1: after it) for every replica
+// in one launch: block blockIdx.x runs block blkmap.y of replica blkmap.x with that replica's
+// arguments (own P, matrices, Langevin coefficients, seed and state pointers); blocks of 256
+// threads hold 256 / (3P) atoms each, as the replica's own launch shape.
+template <int PHASE, bool FAST>
+__global__ void __launch_bounds__(256) k_md_batch(const NMBatchRep *reps, const int2 *blkmap) {
+    __shared__ NMBatchRep sr;
+    const int2 m = blkmap[blockIdx.x];
+    if (threadIdx.x == 0) {
+        sr = reps[m.x];
+        sr.a.phase = PHASE;
+    }
+    __syncthreads();
+    if (PHASE == 0) {
+        if (FAST)
+            md_pre_fast_body(sr.a, m.y, sr.RRt, sr.PPt, sr.dRRt, sr.RRc);
+        else
+            md_pre_body(sr.a, m.y, sr.RRt, sr.PPt, sr.dRRt, sr.RRc);
+    } else {
+        if (FAST)
+            md_post_fast_body(sr.a, m.y, sr.PPt, sr.dRRt, sr.uk);
+        else
+            md_post_body(sr.a, m.y, sr.PPt, sr.dRRt, sr.uk);
+    }
+}
+void nm_launch_md_batch(int phase, bool fast, int nblk, size_t smem, cudaStream_t st, const NMBatchRep *reps,
+                        const int2 *blkmap) {
+    if (smem > 48 * 1024) {  // the opt-in above 48 KB (large bead counts), outside any capture
+        static size_t set = 0;
+        if (smem > set) {
+            cudaFuncSetAttribute(k_md_batch<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(k_md_batch<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(k_md_batch<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(k_md_batch<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            set = smem;
+        }
+    }
+    if (nblk <= 0) return;
+    if (phase == 0)
+        fast ? k_md_batch<0, true><<<nblk, 256, smem, st>>>(reps, blkmap)
+             : k_md_batch<0, false><<<nblk, 256, smem, st>>>(reps, blkmap);
+    else
+        fast ? k_md_batch<1, true><<<nblk, 256, smem, st>>>(reps, blkmap)
+             : k_md_batch<1, false><<<nblk, 256, smem, st>>>(reps, blkmap);
 }
 
 // EvolveRing alone for every atom (no kick, no thermostat)
@@ -677,9 +738,9 @@ __global__ void k_md_estimators(int P, int natoms, double volume, double omegan,
 
 // one warp: lane-strided bead sums, then a fixed butterfly (FP64 is a narrow pipe on this part:
 // a serial loop of dependent adds would take microseconds at the end of every step)
-__global__ void k_md_sum(int P, const double *Upott, const double *virialt, const double *virialct, const double *uk,
-                         double *out4) {
-    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+PIMD_D void md_sum_warp(int P, const double *Upott, const double *virialt, const double *virialct, const double *uk,
+                           double *out4) {
+    if (threadIdx.x >= 32) return;
     double u = 0, v = 0, vc = 0;
     for (int k = threadIdx.x; k < P; k += 32) {
         u += Upott[k];
@@ -698,6 +759,16 @@ __global__ void k_md_sum(int P, const double *Upott, const double *virialt, cons
         out4[2] = vc / P;
         out4[3] = *uk;
     }
+}
+__global__ void k_md_sum(int P, const double *Upott, const double *virialt, const double *virialct, const double *uk,
+                         double *out4) {
+    if (blockIdx.x == 0) md_sum_warp(P, Upott, virialt, virialct, uk, out4);
+}
+
+// the step outputs of every replica of a batch: one warp per replica (as k_md_sum)
+__global__ void k_md_sum_batch(const NMSumRep *reps) {
+    const NMSumRep s = reps[blockIdx.x];
+    md_sum_warp(s.P, s.Upott, s.virialt, s.virialct, s.uk, s.out4);
 }
 
 // ---------------------------------------------------------------------------------------
