@@ -189,6 +189,7 @@ __global__ void __launch_bounds__(128) k_adj_g(KP kp, int k, const int *iters, d
 // Weight slots of the tensor-core sweep (FP32 4 pi A_k / V conj(S) in the field passes' form):
 // MODE 0: slot 0 <- slot 1 (the structure factor just formed), slot 1 <- 0; MODE 1: slot 0 <-
 // the weights of Sm (the forward's structure factor of mu_{k-1}, from the tape), slot 1 stays 0.
+// MODE 2: slot 0 <- the weights of S (the raw charge structure factor), slot 1 <- 0.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_adj_wslots(KP kp, const double2 *Sm) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
@@ -201,24 +202,47 @@ __global__ void __launch_bounds__(256) k_adj_wslots(KP kp, const double2 *Sm) {
         const double w = kp.kinfo[k].w;
         const double2 a = Sm[(size_t)b * kp.nk + k];
         w0[k] = make_float2((float)(w * a.x), (float)(-w * a.y));
+        if (MODE == 2) w1[k] = make_float2(0.f, 0.f);
     }
 }
 
 // mu_0 = alpha E_q: nu += alpha g_0, d/dalpha += g_0 . E_q
-__global__ void __launch_bounds__(128) k_adj_final(KP kp, const double *g, double *nu, double *thacc) {
+// (nuf given: an FP32 copy of nu at the dipole sites, for the tensor-core cross term)
+__global__ void __launch_bounds__(128) k_adj_final(KP kp, const double *g, double *nu, double *thacc, float4 *nuf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y, nd = kp.ld - kp.fd;
     double th[1] = {0.0};
     if (i < nd) {
         const size_t gs = (size_t)b * kp.S + kp.fd + i;
         const double4_32a F = kp.F[gs];
         const double eq[3] = {F.x, F.y, F.z};
+        double n[3];
         for (int c = 0; c < 3; c++) {
             const double gi = g[((size_t)b * nd + i) * 3 + c];
-            nu[3 * gs + c] += kp.polar[4] * gi;
+            n[c] = nu[3 * gs + c] + kp.polar[4] * gi;
+            nu[3 * gs + c] = n[c];
             th[0] += gi * eq[c];
         }
+        if (nuf) nuf[gs] = make_float4((float)n[0], (float)n[1], (float)n[2], 0.f);
     }
     block_reduce_add<1, 128>(th, thacc + PIMD_TH_POLAR_M);
+}
+
+// The reciprocal cross term of the charge-field adjoint from the tensor-core passes:
+// d/dx [nu^T E_q,rec] is q_s E_nu(s) at the charged sites (E_nu, phi_nu: the force pass's charge
+// half on the weights of S_nu, Fx = (-q E_nu, phi_nu)) with -phi_nu(s) its derivative in q_s,
+// plus the derivative at the dipole sites of nu . E_q at fixed S_q, minus the force pass's
+// dipole half of nu on the charge weights (in dR).
+__global__ void __launch_bounds__(128) k_adj_cross_fold(KP kp, int s0, double *grad, double *phin) {
+    const int s = s0 + blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (s >= kp.S) return;
+    const size_t gs = (size_t)b * kp.S + s;
+    const double4_32a x = kp.Fx[gs];
+    grad[3 * gs + 0] -= x.x;
+    grad[3 * gs + 1] -= x.y;
+    grad[3 * gs + 2] -= x.z;
+    phin[gs] -= x.w;
+    if (s >= kp.fd && s < kp.ld)
+        for (int c = 0; c < 3; c++) grad[3 * gs + c] -= kp.dR[3 * gs + c];
 }
 
 // the forward's site-pair vector between site kinds isp of i and jsp of j (pot_ttm.f90:318-319)
@@ -787,11 +811,34 @@ int pimd_pot_backward(pimd_ctx *ctx, const double *Ebar, double *dRRt, double *d
             k_adj_ddbil<<<gp, 128, 0, st>>>(kp, pf, u, v, bw, grad, thacc);
         if (!tcs) adj_rec(E, 0, u, v, Smu, Smv, bw, grad, nullptr);
     }
-    k_adj_final<<<gd, 128, 0, st>>>(kp, g, nu, thacc);
+    k_adj_final<<<gd, 128, 0, st>>>(kp, g, nu, thacc, tcs ? uf : nullptr);
     // charge-field adjoint nu: real-space pairs, reciprocal, intramolecular; vdW; Uelec d/da_cc
     cudaMemsetAsync(bacc, 0, sizeof(double) * P * NACC, st);
-    adj_structure_factor(E, nu, nullptr, Snu, bacc);
-    adj_rec(E, 1, nu, nullptr, Snu, nullptr, ones, grad, phin);
+    if (tcs) {
+        // the cross term on the tensor cores: S_nu, the force pass's charge half on its weights
+        // (Fx at the charged sites), then its dipole half of nu on the charge weights (dR)
+        adj_structure_factor(E, nu, uf, Snu, bacc);
+        KP kq = kp;
+        kq.acc = bacc;
+        kq.dd_async = 0;
+        kq.fx_mode = 2;
+        const KP keep = E.kp;
+        E.kp = kq;
+        launch_adj_qforce_tc(E);
+        const dim3 gk((unsigned)((kp.nk + 255) / 256), (unsigned)P);
+        k_adj_wslots<2><<<gk, 256, 0, st>>>(kp, kp.Sq);
+        cudaMemsetAsync(kp.dR, 0, sizeof(double) * sv, st);
+        E.kp.fx_mode = 0;
+        E.kp.dipf = uf;
+        launch_adj_dforce_tc(E);
+        E.kp = keep;
+        const dim3 gq((unsigned)((kp.S - kp.N + 127) / 128), (unsigned)P);
+        k_adj_cross_fold<<<gq, 128, 0, st>>>(kp, kp.N, grad, phin);
+        E.nlaunch += 2;
+    } else {
+        adj_structure_factor(E, nu, nullptr, Snu, bacc);
+        adj_rec(E, 1, nu, nullptr, Snu, nullptr, ones, grad, phin);
+    }
     if (mixed)
         launch_adj_pairs_m(E, pf.v, ebar, nu, grad, phin, thacc);
     else

@@ -453,6 +453,7 @@ int launch_sfac_tc(Engine &E, int op, int s0, int nsites, int skipconv);
 int launch_field_tc(Engine &E, int mode, int s0, int s1);
 int launch_adj_field_tc(Engine &E);
 int launch_adj_dforce_tc(Engine &E);
+int launch_adj_qforce_tc(Engine &E);
 bool field_pdl_ok(const Engine &E);
 int launch_field_qd_tc(Engine &E, int s0, int s1);  // ewald_std_qd force pass on the tensor cores
 // launchers (spc.cu): q-SPC/Fw and SPC/F

@@ -1415,6 +1415,12 @@ int launch_adj_dforce_tc(Engine &E) {
     if (!E.tf_qd_ready || E.kp.ld <= E.kp.fd) return 0;
     return launch_field_tc(E, TF_DG, E.kp.fd, E.kp.ld);
 }
+// the charge half of the force pass (TF_QG: -q E and phi of the dipole slot's weights) at the
+// charged sites from N on (TTM3-F: H1, H2, M), into kp.Fx with fx_mode 2
+int launch_adj_qforce_tc(Engine &E) {
+    if (!E.tf_qd_ready) return 0;
+    return launch_field_tc(E, TF_QG, E.kp.N, E.kp.S);
+}
 
 // ewald_std_qd's force pass (k_field_f<F_QD> + k_field_finish<F_QD>) as two tensor-core passes:
 // the charge force -q E and potential from the dipole structure factor at [s0, s1), then the
