@@ -160,3 +160,17 @@ def test_mixed_backward_equals_mixed_forces_when_converged(pkg, engine_lib):
     ref = eng.full_bead_forces(c["RRt"], c["RRc"])["dRRt"]
     assert rms_rel(g, ref) < 1e-4
     eng.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_backward_repeats(pkg, engine_lib, precision):
+    """Two backward calls after one forward give the same gradients (the sweep leaves the tape and
+    the forward's buffers it reads intact)."""
+    c, p = case(pkg, nw=64, P=2, K=6, eps=0.0)
+    eng = pkg.ForceEngine(p, precision=precision)
+    eng.pot_forward(c["RRt"], c["RRc"])
+    g1, t1 = eng.pot_backward(np.array([1.0, 0.5]))
+    g2, t2 = eng.pot_backward(np.array([1.0, 0.5]))
+    eng.close()
+    assert np.array_equal(g1, g2) or np.abs(g1 - g2).max() < 1e-12 * np.abs(g1).max()
+    assert np.abs(t1 - t2).max() < 1e-12 * np.abs(t1).max()
