@@ -217,6 +217,27 @@ def test_cell_list_neighbours_large_box(pkg, orc, engine_lib, precision):
     assert rel(got["dRRt"][0], r["dRR"]) < tol
 
 
+@pytest.mark.parametrize("nw,precision", [(1024, 0), (1024, 1), (1100, 0), (1100, 1)])
+def test_neighbour_path_edges(pkg, orc, engine_lib, nw, precision):
+    """The edges of the neighbour-list paths: 1024 molecules, the most the one-cluster build
+    takes (hit masks of 128 KB in a CTA), and 1100 (L = 32.0 A: three cells of >= 9 A per edge,
+    too few for the cell lists), which takes the count / scan / fill build. Lists bit for bit equal
+    to the reference's, forces FP64 1e-10, mixed 1e-4 relative."""
+    c = pkg.waterbox.make_config("ttm3f_512x32", nw=nw, P=1, seed=7 + nw)
+    L = c["params"]["box"][0]
+    p = dict(c["params"], rc=9.0, rc1=7.2, alpha=0.39, nmax=6, polar_maxiter=8, polar_eps=0.0)
+    if nw > 1024:
+        assert L / 9.001 < 4  # fewer than four cells per edge: not the cell-list build
+    eng = pkg.ForceEngine(p, precision=precision)
+    got = eng.full_bead_forces(c["RRt"], c["RRc"])
+    o = orc.Oracle(p)
+    assert np.array_equal(eng.neighbors(0), o.neighbors(c["RRt"][0]))
+    r = o.pot_ttm(c["RRt"][0], c["RRc"])
+    tol = RTOL if precision == 0 else 1e-4
+    assert rel(got["dRRt"][0], r["dRR"]) < tol
+    eng.close()
+
+
 @pytest.mark.parametrize("setNMfreq", [0.0, 1500.0])
 def test_normal_mode_helpers_bit_exact(pkg, orc, engine_lib, setNMfreq):
     """real2NM / NM2real and gen_rand_ring / gen_rand_ring_momenta (NormalModes.f90:224-341)
