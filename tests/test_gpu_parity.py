@@ -217,6 +217,24 @@ def test_cell_list_neighbours_large_box(pkg, orc, engine_lib, precision):
     assert rel(got["dRRt"][0], r["dRR"]) < tol
 
 
+@pytest.mark.parametrize("nmol", [1, 2])
+def test_one_and_two_molecules(pkg, orc, engine_lib, nmol):
+    """The smallest systems (FP64): one molecule (no intermolecular pair: the monomer PES, its
+    intramolecular terms and its own periodic images through the Ewald sums) and two, cut from a
+    32-molecule box (L = 9.86 A, Rc 4.92 A), 2 beads, against the oracle."""
+    c, p = small_case(pkg, 3, nw=32, P=2)
+    RRt = np.ascontiguousarray(c["RRt"][:, :3 * nmol, :])
+    RRc = np.ascontiguousarray(c["RRc"][:3 * nmol])
+    p = dict(p, natoms=3 * nmol)
+    eng = pkg.ForceEngine(p)
+    got = eng.full_bead_forces(RRt, RRc, t=1)
+    ref = orc.full_bead_forces(p, RRt, RRc, t=1)
+    compare_beads(got, ref)
+    if nmol == 2:
+        assert np.array_equal(eng.neighbors(0), orc.Oracle(p).neighbors(RRt[0]))
+    eng.close()
+
+
 @pytest.mark.parametrize("nw,precision", [(1024, 0), (1024, 1), (1100, 0), (1100, 1)])
 def test_neighbour_path_edges(pkg, orc, engine_lib, nw, precision):
     """The edges of the neighbour-list paths: 1024 molecules, the most the one-cluster build
