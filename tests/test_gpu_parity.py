@@ -235,6 +235,29 @@ def test_one_and_two_molecules(pkg, orc, engine_lib, nmol):
     eng.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_neighbour_overflow_reported(pkg, engine_lib, precision):
+    """100 molecules packed at liquid density into one corner of a 40 A box: far more pairs than
+    the list capacity sized from the box's mean density (1024 here). The call reports the
+    overflow (the lists keep their first entries; every kernel stays within the stored length),
+    and the next call on spread-out molecules runs normally."""
+    c = pkg.waterbox.make_config("ttm3f_512x32", nw=100, P=1, seed=3)
+    L0, L = c["params"]["box"][0], 40.0
+    p = dict(c["params"], box=(L, L, L), rc=9.0, rc1=7.2, alpha=0.39, nmax=6, polar_maxiter=6,
+             polar_eps=0.0)
+    eng = pkg.ForceEngine(p, precision=precision)
+    with pytest.raises(pkg.engine.PimdError, match="neighbour list capacity"):
+        eng.full_bead_forces(c["RRt"], c["RRc"])
+    # the same molecules with their O sites spread over the whole box
+    R = c["RRt"].copy()
+    O = R[:, 0::3, :].copy()
+    for a in range(3):
+        R[:, a::3, :] += (L / L0 - 1.0) * O
+    got = eng.full_bead_forces(R, R.mean(axis=0))
+    assert np.isfinite(got["dRRt"]).all() and np.isfinite(got["Upott"]).all()
+    eng.close()
+
+
 @pytest.mark.parametrize("nw,precision", [(1024, 0), (1024, 1), (1100, 0), (1100, 1)])
 def test_neighbour_path_edges(pkg, orc, engine_lib, nw, precision):
     """The edges of the neighbour-list paths: 1024 molecules, the most the one-cluster build
