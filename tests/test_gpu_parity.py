@@ -310,3 +310,23 @@ def test_normal_mode_helpers_bit_exact(pkg, orc, engine_lib, setNMfreq):
         assert np.abs(R[:, 0]).max() < 1e-12
         assert np.allclose(Pm.std(axis=(0, 2)), np.sqrt(W.KB_AMU * m * nm["msf"] * 300.0 * P), rtol=0.1)
     eng.close()
+
+
+def test_invalid_input_rejected(pkg, engine_lib):
+    """Invalid input is refused with PIMD_ERR_ARG before any device work: a cutoff beyond half the
+    box (the reference's check, InputOutput.f90:277-281), an atom count that is not a multiple of
+    three, no beads, an unknown model or precision; and a knob out of range."""
+    c, p = small_case(pkg, 3, nw=32, P=2)
+    L = p["box"][0]
+    bad = [dict(rc=0.5 * L + 0.1), dict(natoms=p["natoms"] - 1), dict(nbeads=0), dict(pot_model=7)]
+    for d in bad:
+        with pytest.raises(pkg.engine.PimdError):
+            pkg.ForceEngine(dict(p, **d))
+    with pytest.raises(pkg.engine.PimdError):
+        pkg.ForceEngine(p, precision=5)
+    eng = pkg.ForceEngine(p, precision=pkg.engine.PIMD_MIXED)
+    with pytest.raises(pkg.engine.PimdError):
+        eng.set_tuning(loop_unroll=0)
+    got = eng.full_bead_forces(c["RRt"], c["RRc"])  # still usable
+    assert np.isfinite(got["dRRt"]).all()
+    eng.close()
